@@ -1,0 +1,256 @@
+"""ctypes access to the test oracle.  TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module, and only as the checker (or the timed CPU baseline).  The
+shipped package never imports it.
+
+* ``Oracle`` wraps ``oracle/liboracle.so``, the C restatement of the
+  reference's hot path (msk_oracle.c): FP32 mirror and FP64 oracle.
+* ``Reference`` wraps ``oracle/_ref/libautoslic_ref.so``, the reference's own
+  TemsimLibrary sources compiled here (only where the reference tree exists).
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_ORACLE = os.path.join(HERE, "liboracle.so")
+LIB_REF = os.path.join(HERE, "_ref", "libautoslic_ref.so")
+REF_TREE = "/root/reference"
+
+# param[] offsets (slicelib.hpp:142-240)
+pXCTILT, pYCTILT, pDEFOCUS, pENERGY, pOAPERT = 9, 10, 11, 16, 17
+pDELTAZ, pAX, pBY, pNX, pNY = 30, 101, 102, 104, 105
+NPARAM = 200
+
+_fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+
+def build(with_ref=None):
+    """Compile liboracle.so (and oracle/_ref when the reference tree exists)."""
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    if with_ref is None:
+        with_ref = os.path.isdir(os.path.join(REF_TREE, "TemsimLibrary"))
+    if with_ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + REF_TREE], check=True)
+
+
+class SeriesParams(C.Structure):
+    _fields_ = [("ax", C.c_float), ("ctblengthz", C.c_float), ("nx", C.c_int), ("ny", C.c_int),
+                ("v0", C.c_float), ("deltaz", C.c_float), ("aobj", C.c_float),
+                ("cs3", C.c_double), ("cs5", C.c_double), ("dxc", C.c_double),
+                ("dyc", C.c_double), ("dzc", C.c_double), ("nmode", C.c_int),
+                ("max_slices", C.c_int)]
+
+
+def make_param(ax, by, nx, ny, v0, deltaz, ctiltx=0.0, ctilty=0.0, aobj=0.0):
+    p = np.zeros(NPARAM, np.float32)
+    p[pAX], p[pBY], p[pNX], p[pNY] = ax, by, nx, ny
+    p[pENERGY], p[pDELTAZ], p[pXCTILT], p[pYCTILT], p[pOAPERT] = v0, deltaz, ctiltx, ctilty, aobj
+    return p
+
+
+def _atoms(Znum, x, y, z, occ):
+    return (np.ascontiguousarray(Znum, np.int32), np.ascontiguousarray(x, np.float32),
+            np.ascontiguousarray(y, np.float32), np.ascontiguousarray(z, np.float32),
+            np.ascontiguousarray(occ, np.float32))
+
+
+class Oracle:
+    def __init__(self, path=LIB_ORACLE):
+        if not os.path.exists(path):
+            build(with_ref=False)
+        L = C.CDLL(path)
+        self.L = L
+        L.mo_wavelength.restype = C.c_double
+        L.mo_wavelength.argtypes = [C.c_double]
+        L.mo_sigma.restype = C.c_double
+        L.mo_sigma.argtypes = [C.c_double]
+        L.mo_vzatom.restype = C.c_double
+        L.mo_vzatom.argtypes = [C.c_int, C.c_double]
+        L.mo_vzatomLUT.restype = C.c_double
+        L.mo_vzatomLUT.argtypes = [C.c_int, C.c_double]
+        L.mo_bessk0.restype = C.c_double
+        L.mo_bessk0.argtypes = [C.c_double]
+        L.mo_bessi0.restype = C.c_double
+        L.mo_bessi0.argtypes = [C.c_double]
+        L.mo_freqn.argtypes = [_fp, _fp, _fp, C.c_int, C.c_double]
+        L.mo_lut_table.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _dp]
+        L.mo_sortByZ.argtypes = [_fp, _fp, _fp, _fp, _ip, C.c_int]
+        L.mo_rotate.argtypes = [C.c_float, C.c_double, C.c_double, C.c_double, C.c_double,
+                                C.c_double, C.c_int, _fp, _fp, _fp]
+        L.mo_drop_outside.argtypes = [C.c_float, C.c_float, C.c_int, _fp, _fp, _fp, _fp, _ip]
+        L.mo_slice_count.argtypes = [C.c_float, C.c_float]
+        L.mo_slice_assign.argtypes = [C.c_float, C.c_float, C.c_int, _fp, _ip]
+        for nm, T in (("mo_calculate_f32", _fp), ("mo_calculate_f64", _dp)):
+            getattr(L, nm).argtypes = [T, T, _fp, C.c_int, _ip, _fp, _fp, _fp, _fp, C.c_float,
+                                       C.c_float, C.c_int, C.c_int]
+        for nm, T in (("mo_defocus_f32", _fp), ("mo_defocus_f64", _dp)):
+            getattr(L, nm).argtypes = [T, C.c_int, C.c_int, C.c_float, C.c_float, C.c_double,
+                                       C.c_double, C.c_float, C.c_double, C.c_double, C.c_double,
+                                       C.c_double, T]
+        for nm, T in (("mo_orientation_f32", _fp), ("mo_orientation_f64", _dp)):
+            getattr(L, nm).argtypes = [C.POINTER(SeriesParams), C.c_int, _ip, _fp, _fp, _fp, _fp,
+                                       C.c_double, C.c_double, C.c_int, _dp, T, C.c_void_p]
+        L.mo_orientations_f32.argtypes = [C.POINTER(SeriesParams), C.c_int, C.c_int, C.c_int,
+                                          C.c_long, _ip, _fp, _fp, _fp, _fp, _dp, _dp, C.c_int,
+                                          _dp, _fp]
+
+    # -- physics
+    def wavelength(self, kev):
+        return self.L.mo_wavelength(kev)
+
+    def sigma(self, kev):
+        return self.L.mo_sigma(kev)
+
+    def freqn(self, n, a):
+        k, k2, xp = (np.zeros(n, np.float32) for _ in range(3))
+        self.L.mo_freqn(k, k2, xp, n, a)
+        return k, k2, xp
+
+    def lut_table(self, Z):
+        arrs = [np.zeros(100) for _ in range(5)]
+        st = self.L.mo_lut_table(Z, *arrs)
+        if st:
+            raise ValueError("bad atomic number %d" % Z)
+        return arrs
+
+    # -- host prep
+    def sort_by_z(self, Znum, x, y, z, occ):
+        Znum, x, y, z, occ = (a.copy() for a in _atoms(Znum, x, y, z, occ))
+        self.L.mo_sortByZ(x, y, z, occ, Znum, len(x))
+        return Znum, x, y, z, occ
+
+    def rotate(self, ctblength, angleZ, angleY, x, y, z, dxc=0.0, dyc=0.0, dzc=0.0):
+        x, y, z = (np.array(a, np.float32) for a in (x, y, z))
+        self.L.mo_rotate(ctblength, dxc, dyc, dzc, angleZ, angleY, len(x), x, y, z)
+        return x, y, z
+
+    def drop_outside(self, ctblength, ctblengthz, Znum, x, y, z, occ):
+        Znum, x, y, z, occ = (a.copy() for a in _atoms(Znum, x, y, z, occ))
+        n = self.L.mo_drop_outside(ctblength, ctblengthz, len(x), x, y, z, occ, Znum)
+        return Znum[:n], x[:n], y[:n], z[:n], occ[:n]
+
+    def slice_count(self, deltaz, zmax):
+        return self.L.mo_slice_count(deltaz, zmax)
+
+    def slice_assign(self, deltaz, zmax, zsorted):
+        zs = np.ascontiguousarray(zsorted, np.float32)
+        out = np.zeros(len(zs), np.int32)
+        n = self.L.mo_slice_assign(deltaz, zmax, len(zs), zs, out)
+        return out, n
+
+    # -- multislice
+    def calculate(self, param, Znum, x, y, z, occ, ctblength, ctblengthz, nmode=0,
+                  wave0=None, fp64=False, max_slices=-1):
+        nx, ny = int(param[pNX] + 0.1), int(param[pNY] + 0.1)
+        T = np.float64 if fp64 else np.float32
+        if wave0 is None:
+            wave0 = np.zeros((nx, ny, 2), T)
+            wave0[..., 0] = 1
+        wave0 = np.ascontiguousarray(wave0, T).reshape(-1)
+        pix = np.zeros(2 * nx * ny, T)
+        fn = self.L.mo_calculate_f64 if fp64 else self.L.mo_calculate_f32
+        st = fn(pix, wave0, np.ascontiguousarray(param, np.float32), len(x),
+                *_atoms(Znum, x, y, z, occ), ctblength, ctblengthz, nmode, max_slices)
+        if st:
+            raise RuntimeError("oracle calculate failed: %d" % st)
+        return pix.reshape(nx, ny, 2)
+
+    def defocus(self, pix, ax, by, wavlen, rprime, k2maxo=0.0, cs3=0.0, cs5=0.0, astig=0.0,
+                astig_angle=0.0, fp64=False):
+        nx, ny = pix.shape[0], pix.shape[1]
+        T = np.float64 if fp64 else np.float32
+        out = np.zeros(nx * ny, T)
+        fn = self.L.mo_defocus_f64 if fp64 else self.L.mo_defocus_f32
+        fn(np.ascontiguousarray(pix, T).reshape(-1), nx, ny, ax, by, wavlen, rprime, k2maxo,
+           cs3, cs5, astig, astig_angle, out)
+        return out.reshape(nx, ny)
+
+    def orientation(self, sp, Znum, x, y, z, occ, angleZ, angleY, defoci, fp64=False,
+                    want_exit=False):
+        T = np.float64 if fp64 else np.float32
+        n = sp.nx * sp.ny
+        imgs = np.zeros(len(defoci) * n, T)
+        ew = np.zeros(2 * n, T) if want_exit else None
+        fn = self.L.mo_orientation_f64 if fp64 else self.L.mo_orientation_f32
+        kept = fn(C.byref(sp), len(x), *_atoms(Znum, x, y, z, occ), angleZ, angleY,
+                  len(defoci), np.ascontiguousarray(defoci, np.float64), imgs,
+                  ew.ctypes.data if want_exit else None)
+        if kept < 0:
+            raise RuntimeError("oracle orientation failed: %d" % kept)
+        imgs = imgs.reshape(len(defoci), sp.nx, sp.ny)
+        return (imgs, ew.reshape(sp.nx, sp.ny, 2), kept) if want_exit else (imgs, kept)
+
+    def orientations_f32(self, sp, Znum, x, y, z, occ, angZ, angY, defoci, nthreads,
+                         coord_stride=0):
+        nunits = len(angZ)
+        imgs = np.zeros(nunits * len(defoci) * sp.nx * sp.ny, np.float32)
+        natom = len(Znum) if coord_stride == 0 else coord_stride
+        st = self.L.mo_orientations_f32(C.byref(sp), nunits, nthreads, natom, coord_stride,
+                                         *_atoms(Znum, x, y, z, occ),
+                                         np.ascontiguousarray(angZ, np.float64),
+                                         np.ascontiguousarray(angY, np.float64), len(defoci),
+                                         np.ascontiguousarray(defoci, np.float64), imgs)
+        if st:
+            raise RuntimeError("oracle orientations failed: %d" % st)
+        return imgs.reshape(nunits, len(defoci), sp.nx, sp.ny)
+
+
+class Reference:
+    """The reference's own code compiled here (oracle/_ref)."""
+
+    def __init__(self, path=LIB_REF):
+        L = C.CDLL(path)
+        self.L = L
+        L.ref_calculate.argtypes = [_fp, _fp, _fp, C.c_int, _ip, _fp, _fp, _fp, _fp, _fp,
+                                    C.c_float, C.c_float, C.c_int, C.c_int, C.c_void_p, C.c_int]
+        L.ref_calculate_many.argtypes = [C.c_int, C.c_int, _fp, _fp, _fp,
+                                         np.ctypeslib.ndpointer(dtype=np.int32),
+                                         np.ctypeslib.ndpointer(dtype=np.int64),
+                                         _ip, _fp, _fp, _fp, _fp, _fp, C.c_float, C.c_float,
+                                         C.c_int]
+        L.ref_sortByZ.argtypes = [_fp, _fp, _fp, _fp, _ip, C.c_int]
+        for nm in ("ref_vzatomLUT", "ref_vzatom"):
+            getattr(L, nm).restype = C.c_double
+            getattr(L, nm).argtypes = [C.c_int, C.c_double]
+        for nm in ("ref_wavelength", "ref_sigma", "ref_bessk0", "ref_bessi0"):
+            getattr(L, nm).restype = C.c_double
+            getattr(L, nm).argtypes = [C.c_double]
+        L.ref_freqn.argtypes = [_fp, _fp, _fp, C.c_int, C.c_double]
+        self._planned = None
+
+    def calculate(self, param, Znum, x, y, z, occ, ctblength, ctblengthz, nmode=0, wave0=None):
+        param = np.array(param, np.float32)
+        nx, ny = int(param[pNX] + 0.1), int(param[pNY] + 0.1)
+        if wave0 is None:
+            wave0 = np.zeros((nx, ny, 2), np.float32)
+            wave0[..., 0] = 1
+        wave0 = np.ascontiguousarray(wave0, np.float32).reshape(-1)
+        pix = np.zeros(2 * nx * ny, np.float32)
+        Znum, x, y, z, occ = (a.copy() for a in _atoms(Znum, x, y, z, occ))
+        wob = np.zeros(len(x), np.float32)
+        self.L.ref_calculate(pix, wave0, param, len(x), Znum, x, y, z, occ, wob, ctblength,
+                             ctblengthz, nmode, 0, None, 1)
+        return pix.reshape(nx, ny, 2)
+
+    def sort_by_z(self, Znum, x, y, z, occ):
+        Znum, x, y, z, occ = (a.copy() for a in _atoms(Znum, x, y, z, occ))
+        self.L.ref_sortByZ(x, y, z, occ, Znum, len(x))
+        return Znum, x, y, z, occ
+
+    def vzatomLUT(self, Z, rsq):
+        return self.L.ref_vzatomLUT(Z, rsq)
+
+    def freqn(self, n, a):
+        k, k2, xp = (np.zeros(n, np.float32) for _ in range(3))
+        self.L.ref_freqn(k, k2, xp, n, a)
+        return k, k2, xp
+
+
+def reference_available():
+    return os.path.exists(LIB_REF)
