@@ -1,0 +1,147 @@
+/*
+ * msk.h -- C ABI of the GB300 multislice library (libmsk.so).
+ *
+ * Drop-in for the hot path of timg021/UTR_public's MsctKirkland: Kirkland's
+ * autoslic multislice (TemsimLibrary/autoslic.cpp) and the per-orientation
+ * loop around it (TemsimLibrary/autosliccmd.cpp), with FFTW replaced by
+ * hand-written sm_103a kernels.  Plain pointers and sizes only.
+ *
+ * Conventions shared by every entry point:
+ *   - complex grids are interleaved float pairs (re, im), x-major: element
+ *     (ix, iy) at index iy + ix*ny, as the reference's cfpix stores them
+ *     (TemsimLibrary/cfpix.hpp:117,133);
+ *   - intensity images are float [nx][ny] in the same order;
+ *   - the return value is MSK_OK or a negative status; the reference calls
+ *     exit(0) in the corresponding cases (autoslic.cpp:258-262, 288-299,
+ *     734-739; slicelib.cpp:2847-2851) -- this library returns instead;
+ *   - a context owns one CUDA device, one stream and every device buffer;
+ *     calls on one context must come from one host thread at a time.
+ *   - grid sizes nx, ny: powers of two from 16 to 4096.
+ */
+#ifndef MSK_H
+#define MSK_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct msk_context msk_context;
+
+enum {
+    MSK_OK = 0,
+    MSK_EBADSIZE = -1,     /* nx, ny < 1 or ax, by < 0                   (autoslic.cpp:258-262) */
+    MSK_EBOX = -2,         /* an atom outside [0,ctblength]^2 x [0,ctblengthz] (autoslic.cpp:288-299) */
+    MSK_EZSORT = -3,       /* sorted z outside [0, ctblengthz]           (autoslic.cpp:734-739) */
+    MSK_EZNUM = -4,        /* atomic number outside 1..103               (slicelib.cpp:2847-2851) */
+    MSK_ENOMEM = -5,       /* device or host allocation failed */
+    MSK_EUNSUPPORTED = -6, /* grid size or mode this library does not provide */
+    MSK_ECUDA = -7,        /* a CUDA call failed; msk_last_error() has the text */
+    MSK_EINVAL = -8        /* bad argument (null pointer, negative count, ...) */
+};
+
+/* param[] offsets read by autoslic::calculate (slicelib.hpp:142-240). */
+enum {
+    MSK_pXCTILT = 9, MSK_pYCTILT = 10, MSK_pENERGY = 16, MSK_pOAPERT = 17, MSK_pDELTAZ = 30,
+    MSK_pAX = 101, MSK_pBY = 102, MSK_pNX = 104, MSK_pNY = 105, MSK_pNWOBBLE = 111,
+    MSK_pTEMPER = 120
+};
+
+/* Create a context on CUDA device `device`.  Replaces the one-time FFTW plan
+ * set-up of cfpix::init (cfpix.cpp:205-264); no FFT plan is shared between
+ * contexts or threads. */
+int msk_create(int device, msk_context **ctx);
+void msk_destroy(msk_context *ctx);
+/* Text of the last failure on this context ("" if none). */
+const char *msk_last_error(const msk_context *ctx);
+const char *msk_status_string(int status);
+
+/* autoslic::calculate, coherent branch (autoslic.hpp:166-169,
+ * autoslic.cpp:209-869 with lpartl = lbeams = lcross = 0).
+ *   pix     out: complex nx*ny exit wave (resized and overwritten in the reference)
+ *   wave0   in:  complex nx*ny incident wave (autoslic.cpp:365)
+ *   param   in:  float[>=121]; reads pAX, pBY, pNX, pNY, pENERGY, pDELTAZ,
+ *                pXCTILT, pYCTILT (autoslic.cpp:238-252)
+ *   Znum, x, y, z, occ, wobble: natom atoms (read only; sorted copies are
+ *                made internally, autoslic.cpp:689-724)
+ *   ctblength, ctblengthz: the box (autoslic.cpp:288-303)
+ *   nmode:  0 multislice; 1, 2 transmission only (autoslic.cpp:783)
+ *   lwobble: must be 0 (the thermal branches are not provided: MSK_EUNSUPPORTED)
+ * Host pointers.  Blocks until the result is in pix. */
+int msk_calculate(msk_context *ctx, float *pix, const float *wave0, const float *param,
+                  int natom, const int *Znum, const float *x, const float *y, const float *z,
+                  const float *occ, const float *wobble, float ctblength, float ctblengthz,
+                  int nmode, int lwobble);
+
+/* One tilt series as MsctKirkland produces it (MultisliceT.cpp:398-448 driving
+ * autosliccmd.cpp:711-1224 per orientation): for every orientation, rotate
+ * the specimen about z then y' (autosliccmd.cpp:727-748), remove atoms that
+ * leave the box (the reference's own rule, autosliccmd.cpp:791-820), for
+ * every thermal configuration run calculate() from a plane wave, propagate
+ * the exit wave to every detector defocus and record |psi|^2, averaged over
+ * configurations in configuration order (autosliccmd.cpp:1205-1224).
+ * The free-space step is this library's definition of XArray2DFFT::FresnelA
+ * (autosliccmd.cpp:1060,1087), whose source is not part of the reference:
+ *   Psi = fft(psi) (cfpix convention), multiply by exp(-i chi) inside the
+ *   objective aperture k^2 < (aobj/lambda)^2 (everywhere if aobj == 0), with
+ *   chi = pi lambda R k^2 + (pi/2) cs3 lambda^3 k^4 + (pi/3) cs5 lambda^5 k^6
+ *       + (pi/2) lambda astig ((kx^2 - ky^2) cos 2a + 2 kx ky sin 2a),
+ *   R = defocus - ctblengthz/2 (autosliccmd.cpp:1060), chi in double and
+ *   reduced modulo 2 pi, then ifft / (nx*ny) and I = |psi|^2. */
+typedef struct {
+    int nx, ny;            /* grid */
+    float ctblength;       /* field of view = box edge in x and y, Angstrom */
+    float ctblengthz;      /* box depth, Angstrom */
+    float v0;              /* beam energy, keV */
+    float deltaz;          /* slice thickness, Angstrom */
+    float aobj;            /* objective aperture semi-angle, rad (0: none) */
+    double cs3, cs5;       /* spherical aberrations, Angstrom */
+    double astig, astig_angle;  /* two-fold astigmatism, Angstrom and rad */
+    double dxc, dyc, dzc;  /* rotation centre shift from the box centre, Angstrom */
+    int nmode;             /* as in msk_calculate */
+    int max_batch;         /* waves in flight at once (0: as many as memory allows) */
+} msk_series;
+
+/*   natom atoms: Znum, x, y, z, occ (host)
+ *   nangles orientations: angleZ[i], angleY[i] in radians (host)
+ *   ndefocus defoci in Angstrom from the box centre (host)
+ *   nconfig >= 1 thermal configurations; displacements (host, may be NULL
+ *     when nconfig == 1): float[nconfig][3][natom] added to x, y, z after the
+ *     rotation (the reference's calculate() adds its random displacement to
+ *     the rotated coordinates, autoslic.cpp:701-713)
+ *   images   out: float[nangles][ndefocus][nx][ny]; host or device pointer
+ *   exitwaves out (may be NULL): complex [nangles][nconfig][nx][ny]; host or
+ *     device pointer
+ *   kept     out (may be NULL): int[nangles*nconfig], atoms inside the box */
+int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int *Znum,
+                    const float *x, const float *y, const float *z, const float *occ,
+                    int nangles, const double *angleZ, const double *angleY, int ndefocus,
+                    const double *defocus, int nconfig, const float *displacements,
+                    float *images, float *exitwaves, int *kept);
+
+/* Number of slice-steps calculate() runs for a box of depth ctblengthz
+ * (autoslic.cpp:747-830: zslice = dz, dz + dz, ... while < ctblengthz + dz). */
+int msk_slice_count(float deltaz, float ctblengthz);
+
+/* Slice index (0-based) of every atom of a z-sorted list, with the
+ * reference's double-precision slice boundaries (autoslic.cpp:756-762). */
+int msk_slice_assign(float deltaz, float ctblengthz, int natom, const float *zsorted,
+                     int *slice_of_atom);
+
+/* The reference's Shell sort by z (slicelib.cpp:2467-2504), in place: the
+ * same permutation as the reference for the same input. */
+void msk_sort_by_z(float *x, float *y, float *z, float *occ, int *Znum, int natom);
+
+/* Rotation about z then y' in float (autosliccmd.cpp:727-748), in place. */
+void msk_rotate(float ctblength, double dxc, double dyc, double dzc, double angleZ,
+                double angleY, int natom, float *x, float *y, float *z);
+
+/* The projected-potential spline table of atomic number Z as the kernels use
+ * it (slicelib.cpp:2812-2875): knots[100] (r^2) and coef[100][4] = {y,b,c,d}
+ * computed in double.  Returns MSK_EZNUM for Z outside 1..103. */
+int msk_potential_table(int Z, double *knots, double *coef);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MSK_H */

@@ -852,8 +852,8 @@ static void fill_param(const mo_series_params *sp, float *param)
 /* Rotate and drop atoms for one orientation; returns malloc'ed copies. */
 static int prep_orientation(const mo_series_params *sp, int natom, const int *Znum,
                             const float *x, const float *y, const float *z, const float *occ,
-                            double angleZ, double angleY, float **xo, float **yo, float **zo,
-                            float **oo, int **Zo)
+                            double angleZ, double angleY, const float *disp, float **xo,
+                            float **yo, float **zo, float **oo, int **Zo)
 {
     size_t n = natom > 0 ? (size_t)natom : 1;
     *xo = (float *)malloc(sizeof(float) * n);
@@ -869,17 +869,24 @@ static int prep_orientation(const mo_series_params *sp, int natom, const int *Zn
         memcpy(*Zo, Znum, sizeof(int) * natom);
     }
     mo_rotate(sp->ax, sp->dxc, sp->dyc, sp->dzc, angleZ, angleY, natom, *xo, *yo, *zo);
+    if (disp) /* thermal displacement of the rotated atoms (autoslic.cpp:701-713) */
+        for (int k = 0; k < natom; k++) {
+            (*xo)[k] += disp[k];
+            (*yo)[k] += disp[natom + k];
+            (*zo)[k] += disp[2 * natom + k];
+        }
     return mo_drop_outside(sp->ax, sp->ctblengthz, natom, *xo, *yo, *zo, *oo, *Zo);
 }
 
 int mo_orientation_f32(const mo_series_params *sp, int natom, const int *Znum,
                        const float *x, const float *y, const float *z, const float *occ,
-                       double angleZ, double angleY, int ndef, const double *defocus,
+                       double angleZ, double angleY, const float *disp, int ndef,
+                       const double *defocus,
                        float *images, float *exitwave)
 {
     float *xo, *yo, *zo, *oo;
     int *Zo;
-    int kept = prep_orientation(sp, natom, Znum, x, y, z, occ, angleZ, angleY, &xo, &yo, &zo, &oo, &Zo);
+    int kept = prep_orientation(sp, natom, Znum, x, y, z, occ, angleZ, angleY, disp, &xo, &yo, &zo, &oo, &Zo);
     float param[MO_NPARAM];
     fill_param(sp, param);
     size_t n = (size_t)sp->nx * sp->ny;
@@ -911,12 +918,13 @@ int mo_orientation_f32(const mo_series_params *sp, int natom, const int *Znum,
 
 int mo_orientation_f64(const mo_series_params *sp, int natom, const int *Znum,
                        const float *x, const float *y, const float *z, const float *occ,
-                       double angleZ, double angleY, int ndef, const double *defocus,
+                       double angleZ, double angleY, const float *disp, int ndef,
+                       const double *defocus,
                        double *images, double *exitwave)
 {
     float *xo, *yo, *zo, *oo;
     int *Zo;
-    int kept = prep_orientation(sp, natom, Znum, x, y, z, occ, angleZ, angleY, &xo, &yo, &zo, &oo, &Zo);
+    int kept = prep_orientation(sp, natom, Znum, x, y, z, occ, angleZ, angleY, disp, &xo, &yo, &zo, &oo, &Zo);
     float param[MO_NPARAM];
     fill_param(sp, param);
     size_t n = (size_t)sp->nx * sp->ny;
@@ -966,7 +974,7 @@ static void *many_worker(void *arg)
         if (u >= j->nunits) break;
         long o = (long)u * j->stride;
         int st = mo_orientation_f32(j->sp, j->natom, j->Znum + o, j->x + o, j->y + o, j->z + o,
-                                    j->occ + o, j->angZ[u], j->angY[u], j->ndef, j->defocus,
+                                    j->occ + o, j->angZ[u], j->angY[u], NULL, j->ndef, j->defocus,
                                     j->images + img * u, NULL);
         if (st < 0) __atomic_store_n(&j->status, st, __ATOMIC_RELAXED);
     }

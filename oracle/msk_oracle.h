@@ -102,7 +102,9 @@ int mo_defocus_f64(const double *pix, int nx, int ny, float ax, float by, double
 /* One orientation of MsctKirkland's per-angle worker (autosliccmd.cpp:711-748,
  * 936, 1051-1087, 1205-1224), FP32 mirror: rotate the specimen, drop atoms
  * outside the box, calculate() from a plane wave, then one intensity image
- * per defocus.  images: ndef * nx*ny floats.  exitwave (optional): 2*nx*ny.
+ * per defocus.  disp (optional): float[3][natom] added to the rotated
+ * coordinates before the box rule (a frozen-phonon configuration).
+ * images: ndef * nx*ny floats.  exitwave (optional): 2*nx*ny.
  * Returns the number of atoms kept, or a negative status. */
 typedef struct {
     float ax;           /* field of view = ctblength, Angstrom */
@@ -119,11 +121,13 @@ typedef struct {
 
 int mo_orientation_f32(const mo_series_params *sp, int natom, const int *Znum,
                        const float *x, const float *y, const float *z, const float *occ,
-                       double angleZ, double angleY, int ndef, const double *defocus,
+                       double angleZ, double angleY, const float *disp, int ndef,
+                       const double *defocus,
                        float *images, float *exitwave);
 int mo_orientation_f64(const mo_series_params *sp, int natom, const int *Znum,
                        const float *x, const float *y, const float *z, const float *occ,
-                       double angleZ, double angleY, int ndef, const double *defocus,
+                       double angleZ, double angleY, const float *disp, int ndef,
+                       const double *defocus,
                        double *images, double *exitwave);
 
 /* Many orientations on nthreads host threads (one orientation per thread at

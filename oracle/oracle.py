@@ -95,7 +95,8 @@ class Oracle:
                                        C.c_double, T]
         for nm, T in (("mo_orientation_f32", _fp), ("mo_orientation_f64", _dp)):
             getattr(L, nm).argtypes = [C.POINTER(SeriesParams), C.c_int, _ip, _fp, _fp, _fp, _fp,
-                                       C.c_double, C.c_double, C.c_int, _dp, T, C.c_void_p]
+                                       C.c_double, C.c_double, C.c_void_p, C.c_int, _dp, T,
+                                       C.c_void_p]
         L.mo_orientations_f32.argtypes = [C.POINTER(SeriesParams), C.c_int, C.c_int, C.c_int,
                                           C.c_long, _ip, _fp, _fp, _fp, _fp, _dp, _dp, C.c_int,
                                           _dp, _fp]
@@ -172,14 +173,16 @@ class Oracle:
         return out.reshape(nx, ny)
 
     def orientation(self, sp, Znum, x, y, z, occ, angleZ, angleY, defoci, fp64=False,
-                    want_exit=False):
+                    want_exit=False, disp=None):
         T = np.float64 if fp64 else np.float32
         n = sp.nx * sp.ny
         imgs = np.zeros(len(defoci) * n, T)
         ew = np.zeros(2 * n, T) if want_exit else None
         fn = self.L.mo_orientation_f64 if fp64 else self.L.mo_orientation_f32
+        d = None if disp is None else np.ascontiguousarray(disp, np.float32)
         kept = fn(C.byref(sp), len(x), *_atoms(Znum, x, y, z, occ), angleZ, angleY,
-                  len(defoci), np.ascontiguousarray(defoci, np.float64), imgs,
+                  None if d is None else d.ctypes.data, len(defoci),
+                  np.ascontiguousarray(defoci, np.float64), imgs,
                   ew.ctypes.data if want_exit else None)
         if kept < 0:
             raise RuntimeError("oracle orientation failed: %d" % kept)

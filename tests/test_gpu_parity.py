@@ -1,0 +1,194 @@
+"""Parity of the CUDA path (through the C ABI) with the reference and the
+oracle.  Tolerances (relative L2 over the whole grid):
+  * exit wave vs the reference's FP32 CPU result (golden):  2e-5
+  * exit wave and images vs the FP64 oracle:                1e-5 at these sizes
+    (the benchmark spec's bound is 1e-4)
+Bit-exact where the arithmetic is exact (plane wave through an empty box).
+"""
+import numpy as np
+import pytest
+
+from conftest import golden, rel_l2
+from utr_public_gb300 import specimen as sp
+
+pytestmark = pytest.mark.gpu
+
+EXIT_CASES = ["c1_128", "c1_256", "rect_64x128", "proj_64"]
+
+
+def golden_case(name):
+    g = golden("ref_exit_%s.npz" % name)
+    s = sp.plain_specimen(int(g["seed"]))
+    n = int(g["natom"])
+    atoms = (s.Znum[:n], s.x[:n], s.y[:n], s.z[:n], s.occ[:n])
+    return g, atoms
+
+
+@pytest.mark.parametrize("name", EXIT_CASES)
+def test_calculate_matches_reference_golden(ctx, msk, oracle, name):
+    g, atoms = golden_case(name)
+    fov, nx, ny = float(g["fov"]), int(g["nx"]), int(g["ny"])
+    param = msk.make_param(fov, fov, nx, ny, float(g["v0"]), float(g["deltaz"]))
+    pix = ctx.calculate(param, *atoms, fov, fov, nmode=int(g["nmode"]))
+    assert rel_l2(pix, g["pix"]) < 2e-5
+    ref64 = oracle.calculate(param, *atoms, fov, fov, nmode=int(g["nmode"]), fp64=True)
+    assert rel_l2(pix, ref64) < 1e-5
+
+
+@pytest.mark.parametrize("nx,ny,fov,dz", [(16, 16, 8.0, 2.0), (32, 32, 16.0, 2.0),
+                                          (32, 64, 20.0, 1.0), (64, 32, 20.0, 1.0),
+                                          (512, 512, 64.0, 2.0), (128, 2048, 64.0, 4.0),
+                                          (2048, 64, 64.0, 4.0), (4096, 32, 64.0, 8.0)])
+def test_calculate_grid_sizes(ctx, msk, oracle, nx, ny, fov, dz):
+    s = sp.random_specimen(120, fov, 0.1 * fov, 0.9 * fov, 4242 + nx + ny)
+    atoms = (s.Znum, s.x, s.y, s.z, s.occ)
+    param = msk.make_param(fov, fov, nx, ny, 300.0, dz)
+    pix = ctx.calculate(param, *atoms, fov, fov)
+    ref64 = oracle.calculate(param, *atoms, fov, fov, fp64=True)
+    assert rel_l2(pix, ref64) < 1e-5
+
+
+def test_calculate_with_tilt_and_incident_wave(ctx, msk, oracle):
+    s = sp.random_specimen(200, 32.0, 4.0, 28.0, 99)
+    atoms = (s.Znum, s.x, s.y, s.z, s.occ)
+    param = msk.make_param(32.0, 32.0, 128, 128, 200.0, 1.0, ctiltx=0.004, ctilty=-0.003)
+    rng = np.random.default_rng(5)
+    ph = rng.uniform(0, 2 * np.pi, (128, 128))
+    w0 = np.stack([np.cos(ph), np.sin(ph)], -1).astype(np.float32)
+    pix = ctx.calculate(param, *atoms, 32.0, 32.0, wave0=w0)
+    ref64 = oracle.calculate(param, *atoms, 32.0, 32.0, wave0=w0.astype(np.float64), fp64=True)
+    assert rel_l2(pix, ref64) < 1e-5
+
+
+def test_empty_box_keeps_plane_wave_exactly(ctx, msk):
+    param = msk.make_param(32.0, 32.0, 64, 64, 200.0, 2.0)
+    e = np.zeros(0, np.float32)
+    pix = ctx.calculate(param, e.astype(np.int32), e, e, e, e, 32.0, 32.0)
+    assert np.all(pix[..., 0] == 1.0) and np.all(pix[..., 1] == 0.0)
+
+
+def test_deterministic(ctx, msk):
+    g, atoms = golden_case("c1_256")
+    param = msk.make_param(64.0, 64.0, 256, 256, 200.0, 2.0)
+    a = ctx.calculate(param, *atoms, 64.0, 64.0)
+    b = ctx.calculate(param, *atoms, 64.0, 64.0)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_error_statuses(ctx, msk):
+    s = sp.random_specimen(50, 32.0, 4.0, 28.0, 3)
+    atoms = [s.Znum, s.x, s.y, s.z, s.occ]
+    param = msk.make_param(32.0, 32.0, 64, 64, 200.0, 2.0)
+    bad = [a.copy() for a in atoms]
+    bad[1][7] = 40.0
+    with pytest.raises(msk.MskError) as e:
+        ctx.calculate(param, *bad, 32.0, 32.0)
+    assert e.value.status == msk.MSK_EBOX
+    bad = [a.copy() for a in atoms]
+    bad[0][3] = 104
+    with pytest.raises(msk.MskError) as e:
+        ctx.calculate(param, *bad, 32.0, 32.0)
+    assert e.value.status == msk.MSK_EZNUM
+    with pytest.raises(msk.MskError) as e:
+        ctx.calculate(msk.make_param(32.0, 32.0, 100, 64, 200.0, 2.0), *atoms, 32.0, 32.0)
+    assert e.value.status == msk.MSK_EUNSUPPORTED
+    with pytest.raises(msk.MskError) as e:
+        ctx.calculate(param, *atoms, 32.0, 32.0, lwobble=1)
+    assert e.value.status == msk.MSK_EUNSUPPORTED
+    # the context stays usable after every failure
+    pix = ctx.calculate(param, *atoms, 32.0, 32.0)
+    assert np.isfinite(pix).all()
+
+
+def series(msk, nx, fov, v0, dz, aobj=0.0, cs3=0.0, max_batch=0):
+    s = msk.Series()
+    s.nx = s.ny = nx
+    s.ctblength = s.ctblengthz = fov
+    s.v0, s.deltaz, s.aobj, s.cs3 = v0, dz, aobj, cs3
+    s.max_batch = max_batch
+    return s
+
+
+def oracle_series(oracle, nx, fov, v0, dz, aobj=0.0, cs3=0.0):
+    from oracle.oracle import SeriesParams
+    p = SeriesParams()
+    p.ax, p.ctblengthz, p.nx, p.ny, p.v0, p.deltaz = fov, fov, nx, nx, v0, dz
+    p.aobj, p.cs3, p.max_slices = aobj, cs3, -1
+    return p
+
+
+@pytest.mark.parametrize("aobj,cs3", [(0.0, 0.0), (0.02, 1.2e7)])
+def test_tilt_series_matches_oracle(ctx, msk, oracle, aobj, cs3):
+    spec = sp.random_specimen(800, 64.0, 10.0, 54.0, 1010)
+    atoms = (spec.Znum, spec.x, spec.y, spec.z, spec.occ)
+    angY = np.deg2rad([0.0, 30.0, 45.0, 90.0, 137.0])
+    angZ = np.array([0.0, 0.0, 0.3, 0.0, 1.1])
+    defoci = np.array([0.0, 500.0, -120.0])
+    imgs, ew, kept = ctx.tilt_series(series(msk, 128, 64.0, 300.0, 1.0, aobj, cs3), *atoms, angZ,
+                                     angY, defoci, want_exit=True)
+    sp64 = oracle_series(oracle, 128, 64.0, 300.0, 1.0, aobj, cs3)
+    for a in range(len(angY)):
+        ref, ref_ew, k = oracle.orientation(sp64, *atoms, angZ[a], angY[a], defoci, fp64=True,
+                                            want_exit=True)
+        assert kept[a] == k
+        assert rel_l2(ew[a, 0], ref_ew) < 1e-5
+        for d in range(len(defoci)):
+            assert rel_l2(imgs[a, d], ref[d]) < 1e-5, (a, d)
+
+
+def test_tilt_series_angle_zero_equals_calculate(ctx, msk):
+    spec = sp.random_specimen(600, 64.0, 10.0, 54.0, 1011)
+    atoms = (spec.Znum, spec.x, spec.y, spec.z, spec.occ)
+    _, ew, _ = ctx.tilt_series(series(msk, 128, 64.0, 200.0, 2.0), *atoms, [0.0], [0.0], [0.0],
+                               want_exit=True)
+    x, y, z = msk.rotate(64.0, 0.0, 0.0, spec.x, spec.y, spec.z)
+    param = msk.make_param(64.0, 64.0, 128, 128, 200.0, 2.0)
+    pix = ctx.calculate(param, spec.Znum, x, y, z, spec.occ, 64.0, 64.0)
+    assert np.array_equal(ew[0, 0].view(np.uint32), pix.view(np.uint32))
+
+
+@pytest.mark.parametrize("max_batch", [0, 3, 4])
+def test_frozen_phonon_average(ctx, msk, oracle, max_batch):
+    spec = sp.random_specimen(400, 64.0, 10.0, 54.0, 1003)
+    atoms = (spec.Znum, spec.x, spec.y, spec.z, spec.occ)
+    nconf = 4
+    disp = sp.phonon_displacements(spec, nconf, 0.08, 1003)
+    angY = np.deg2rad([0.0, 40.0, 95.0])
+    angZ = np.zeros(3)
+    defoci = np.array([0.0, 300.0])
+    imgs, kept = ctx.tilt_series(series(msk, 64, 64.0, 200.0, 1.0, max_batch=max_batch), *atoms,
+                                 angZ, angY, defoci, nconfig=nconf, displacements=disp)
+    sp64 = oracle_series(oracle, 64, 64.0, 200.0, 1.0)
+    for a in range(3):
+        acc = np.zeros((len(defoci), 64, 64))
+        for c in range(nconf):
+            ref, _ = oracle.orientation(sp64, *atoms, angZ[a], angY[a], defoci, fp64=True,
+                                        disp=disp[c])
+            acc += ref
+        acc /= nconf
+        for d in range(len(defoci)):
+            assert rel_l2(imgs[a, d], acc[d]) < 1e-5
+
+
+def test_tilt_series_device_output(ctx, msk):
+    torch = pytest.importorskip("torch")
+    spec = sp.random_specimen(300, 64.0, 10.0, 54.0, 1012)
+    atoms = (spec.Znum, spec.x, spec.y, spec.z, spec.occ)
+    s = series(msk, 64, 64.0, 200.0, 2.0)
+    host, _ = ctx.tilt_series(s, *atoms, [0.0, 0.5], [0.2, 1.0], [0.0, 100.0])
+    dev = torch.zeros((2, 2, 64, 64), dtype=torch.float32, device="cuda")
+    ctx.tilt_series(s, *atoms, [0.0, 0.5], [0.2, 1.0], [0.0, 100.0], images=dev)
+    torch.cuda.synchronize()
+    assert np.array_equal(dev.cpu().numpy(), host)
+
+
+def test_full_grid_thin_slab(ctx, msk, oracle):
+    """The tilt-series grid (1024^2 over 160 A, 300 keV, 1 A slices) on a
+    thin slab that the FP64 oracle finishes in seconds."""
+    spec = sp.random_specimen(400, 160.0, 20.0, 140.0, 1013)
+    spec.z[:] = np.float32(2.0) + (spec.z - 20.0) * np.float32(4.0 / 120.0)
+    atoms = (spec.Znum, spec.x, spec.y, spec.z, spec.occ)
+    param = msk.make_param(160.0, 160.0, 1024, 1024, 300.0, 1.0)
+    pix = ctx.calculate(param, *atoms, 160.0, 8.0)
+    ref64 = oracle.calculate(param, *atoms, 160.0, 8.0, fp64=True)
+    assert rel_l2(pix, ref64) < 1e-5

@@ -1,0 +1,127 @@
+"""The oracle pinned against the reference's own outputs (tests/golden, made
+by tests/golden/make_golden.py from the reference compiled unmodified).
+
+The FP32 restatement mirrors the reference operation by operation and uses
+the same CPU FFT as the reference build, so on the machine that made the
+fixtures (x86-64) it reproduces them bit for bit; elsewhere libm may round a
+last bit differently, so the bound there is 1e-6 relative L2.
+"""
+import platform
+
+import numpy as np
+import pytest
+
+from conftest import golden, rel_l2
+from utr_public_gb300 import specimen as sp
+
+EXIT_CASES = ["c1_128", "c1_256", "rect_64x128", "proj_64"]
+SAME_MACHINE = platform.machine() == "x86_64"
+
+
+def case(g):
+    s = sp.plain_specimen(int(g["seed"]))
+    n = int(g["natom"])
+    return s.Znum[:n], s.x[:n], s.y[:n], s.z[:n], s.occ[:n]
+
+
+def test_physics_matches_reference(oracle):
+    g = golden("ref_physics.npz")
+    for k, w, s in zip(g["kev"], g["wavelength"], g["sigma"]):
+        assert oracle.wavelength(k) == w
+        assert oracle.sigma(k) == s
+    for xv, k0, i0 in zip(g["bessk0_x"], g["bessk0"], g["bessi0"]):
+        assert oracle.L.mo_bessk0(xv) == pytest.approx(k0, rel=1e-15, abs=0)
+        assert oracle.L.mo_bessi0(xv) == pytest.approx(i0, rel=1e-15, abs=0)
+    for zi, Z in enumerate(g["lut_Z"]):
+        for ri, r2 in enumerate(g["lut_rsq"]):
+            assert oracle.L.mo_vzatomLUT(int(Z), float(r2)) == pytest.approx(
+                g["lut"][zi, ri], rel=1e-14, abs=1e-300)
+            assert oracle.L.mo_vzatom(int(Z), float(np.sqrt(r2))) == pytest.approx(
+                g["vzatom"][zi, ri], rel=1e-14, abs=1e-300)
+
+
+@pytest.mark.parametrize("n,a", [(64, 64.0), (128, 64.0), (256, 64.0), (1024, 160.0), (100, 37.5)])
+def test_freqn_bit_exact(oracle, n, a):
+    g = golden("ref_physics.npz")
+    k, k2, xp = oracle.freqn(n, a)
+    assert np.array_equal(k, g["freqn_%d_k" % n])
+    assert np.array_equal(k2, g["freqn_%d_k2" % n])
+    assert np.array_equal(xp, g["freqn_%d_x" % n])
+
+
+def test_sort_permutation_bit_exact(oracle):
+    g = golden("ref_sort.npz")
+    s = sp.plain_specimen(1001)
+    idx = np.arange(s.natom, dtype=np.float32)
+    _, _, _, zs, perm = oracle.sort_by_z(s.Znum, s.x, s.y, s.z, idx)
+    assert np.array_equal(perm.astype(np.int32), g["perm"])
+    assert np.array_equal(zs, g["zsorted"])
+    assert np.all(np.diff(zs) >= 0)
+
+
+@pytest.mark.parametrize("name", EXIT_CASES)
+def test_fp32_restatement_matches_reference(oracle, name):
+    g = golden("ref_exit_%s.npz" % name)
+    from oracle.oracle import make_param
+    fov, nx, ny = float(g["fov"]), int(g["nx"]), int(g["ny"])
+    param = make_param(fov, fov, nx, ny, float(g["v0"]), float(g["deltaz"]))
+    pix = oracle.calculate(param, *case(g), fov, fov, nmode=int(g["nmode"]))
+    if SAME_MACHINE:
+        assert np.array_equal(pix.view(np.uint32), g["pix"].view(np.uint32))
+    else:
+        assert rel_l2(pix, g["pix"]) < 1e-6
+
+
+@pytest.mark.parametrize("name", EXIT_CASES)
+def test_fp64_oracle_close_to_reference(oracle, name):
+    g = golden("ref_exit_%s.npz" % name)
+    from oracle.oracle import make_param
+    fov, nx, ny = float(g["fov"]), int(g["nx"]), int(g["ny"])
+    param = make_param(fov, fov, nx, ny, float(g["v0"]), float(g["deltaz"]))
+    pix = oracle.calculate(param, *case(g), fov, fov, nmode=int(g["nmode"]), fp64=True)
+    # the reference's own FP32 rounding error, well inside the 1e-4 budget
+    assert rel_l2(g["pix"], pix) < 1e-5
+
+
+def test_slice_counts(oracle):
+    # C1: 64 A box in 2 A slices; C2: 160 A box in 1 A slices (autoslic.cpp:756)
+    assert oracle.slice_count(2.0, 64.0) == 32
+    assert oracle.slice_count(1.0, 160.0) == 160
+    assert oracle.slice_count(1.25, 100.0) == 80
+
+
+def test_slice_assign_consistent(oracle):
+    s = sp.plain_specimen(1001)
+    _, _, _, zs, _ = oracle.sort_by_z(s.Znum, s.x, s.y, s.z, s.occ)
+    sl, n = oracle.slice_assign(2.0, 64.0, zs)
+    assert n == 32
+    assert np.all(np.diff(sl) >= 0)
+    # slice k holds (k*dz, (k+1)*dz] in double arithmetic
+    for k in range(n):
+        zk = zs[sl == k].astype(np.float64)
+        if zk.size:
+            assert zk.max() < (k + 1) * 2.0 and (k == 0 or zk.min() >= k * 2.0)
+
+
+def test_empty_specimen_plane_wave_is_exact(oracle):
+    from oracle.oracle import make_param
+    param = make_param(32.0, 32.0, 64, 64, 200.0, 2.0)
+    e = np.zeros(0)
+    pix = oracle.calculate(param, e.astype(np.int32), e, e, e, e, 32.0, 32.0)
+    assert np.all(pix[..., 0] == 1.0) and np.all(pix[..., 1] == 0.0)
+
+
+def test_defocus_properties(oracle):
+    from oracle.oracle import make_param
+    s = sp.plain_specimen(1001)
+    param = make_param(64.0, 64.0, 128, 128, 200.0, 2.0)
+    pix = oracle.calculate(param, s.Znum[:300], s.x[:300], s.y[:300], s.z[:300], s.occ[:300],
+                           64.0, 64.0, fp64=True)
+    lam = oracle.wavelength(200.0)
+    # R = 0, no aperture: the intensity of the exit wave itself
+    i0 = oracle.defocus(pix, 64.0, 64.0, lam, 0.0, fp64=True)
+    assert rel_l2(i0, pix[..., 0] ** 2 + pix[..., 1] ** 2) < 1e-12
+    # free-space propagation is unitary: total intensity is kept
+    i1 = oracle.defocus(pix, 64.0, 64.0, lam, 250.0, fp64=True)
+    assert abs(i1.sum() / i0.sum() - 1.0) < 1e-12
+    assert rel_l2(i1, i0) > 1e-3  # and it does change the image

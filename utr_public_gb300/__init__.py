@@ -1,0 +1,215 @@
+"""GB300 multislice: ctypes binding of libmsk.so (include/msk.h).
+
+The library itself is C++/CUDA; this module is the Python plumbing used by
+the tests and the benchmark.  It loads the in-tree libmsk.so and fails
+loudly when it is missing -- there is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import specimen  # noqa: F401
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libmsk.so")
+
+# status codes (include/msk.h)
+MSK_OK, MSK_EBADSIZE, MSK_EBOX, MSK_EZSORT, MSK_EZNUM = 0, -1, -2, -3, -4
+MSK_ENOMEM, MSK_EUNSUPPORTED, MSK_ECUDA, MSK_EINVAL = -5, -6, -7, -8
+
+# param[] offsets (slicelib.hpp:142-240)
+pXCTILT, pYCTILT, pENERGY, pOAPERT, pDELTAZ = 9, 10, 16, 17, 30
+pAX, pBY, pNX, pNY, pNWOBBLE, pTEMPER = 101, 102, 104, 105, 111, 120
+NPARAM = 200
+
+EXPORTS = ("msk_create", "msk_destroy", "msk_last_error", "msk_status_string", "msk_calculate",
+           "msk_tilt_series", "msk_slice_count", "msk_slice_assign", "msk_sort_by_z",
+           "msk_rotate", "msk_potential_table")
+
+
+class MskError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s (status %d)" % (msg, status))
+        self.status = status
+
+
+class Series(C.Structure):
+    """msk_series (include/msk.h)."""
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("ctblength", C.c_float),
+                ("ctblengthz", C.c_float), ("v0", C.c_float), ("deltaz", C.c_float),
+                ("aobj", C.c_float), ("cs3", C.c_double), ("cs5", C.c_double),
+                ("astig", C.c_double), ("astig_angle", C.c_double), ("dxc", C.c_double),
+                ("dyc", C.c_double), ("dzc", C.c_double), ("nmode", C.c_int),
+                ("max_batch", C.c_int)]
+
+
+_lib = None
+_fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+
+
+def lib_path():
+    return LIB_PATH
+
+
+def load():
+    """Load libmsk.so (built by utr_public_gb300._build); raise if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libmsk.so is not built: run `python -m utr_public_gb300._build` "
+                           "(or __graft_entry__.build()); there is no CPU fallback")
+    L = C.CDLL(LIB_PATH)
+    vp = C.c_void_p
+    L.msk_create.argtypes = [C.c_int, C.POINTER(vp)]
+    L.msk_destroy.argtypes = [vp]
+    L.msk_destroy.restype = None
+    L.msk_last_error.argtypes = [vp]
+    L.msk_last_error.restype = C.c_char_p
+    L.msk_status_string.argtypes = [C.c_int]
+    L.msk_status_string.restype = C.c_char_p
+    L.msk_calculate.argtypes = [vp, vp, vp, _fp, C.c_int, vp, vp, vp, vp, vp, vp, C.c_float,
+                                C.c_float, C.c_int, C.c_int]
+    L.msk_tilt_series.argtypes = [vp, C.POINTER(Series), C.c_int, vp, vp, vp, vp, vp, C.c_int,
+                                  _dp, _dp, C.c_int, vp, C.c_int, vp, vp, vp, vp]
+    L.msk_slice_count.argtypes = [C.c_float, C.c_float]
+    L.msk_slice_assign.argtypes = [C.c_float, C.c_float, C.c_int, _fp, _ip]
+    L.msk_sort_by_z.argtypes = [_fp, _fp, _fp, _fp, _ip, C.c_int]
+    L.msk_sort_by_z.restype = None
+    L.msk_rotate.argtypes = [C.c_float, C.c_double, C.c_double, C.c_double, C.c_double,
+                             C.c_double, C.c_int, _fp, _fp, _fp]
+    L.msk_rotate.restype = None
+    L.msk_potential_table.argtypes = [C.c_int, _dp, _dp]
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if hasattr(a, "data_ptr"):  # torch tensor (device or host)
+        return a.data_ptr()
+    return a.ctypes.data
+
+
+def make_param(ax, by, nx, ny, v0, deltaz, ctiltx=0.0, ctilty=0.0):
+    p = np.zeros(NPARAM, np.float32)
+    p[pAX], p[pBY], p[pNX], p[pNY] = ax, by, nx, ny
+    p[pENERGY], p[pDELTAZ], p[pXCTILT], p[pYCTILT] = v0, deltaz, ctiltx, ctilty
+    return p
+
+
+# ------------------------------------------------------------- host helpers
+
+def slice_count(deltaz, ctblengthz):
+    return load().msk_slice_count(deltaz, ctblengthz)
+
+
+def slice_assign(deltaz, ctblengthz, zsorted):
+    zs = np.ascontiguousarray(zsorted, np.float32)
+    out = np.zeros(len(zs), np.int32)
+    n = load().msk_slice_assign(deltaz, ctblengthz, len(zs), zs, out)
+    return out, n
+
+
+def sort_by_z(Znum, x, y, z, occ):
+    Znum, x, y, z, occ = (np.array(a, dt) for a, dt in
+                          ((Znum, np.int32), (x, np.float32), (y, np.float32), (z, np.float32),
+                           (occ, np.float32)))
+    load().msk_sort_by_z(x, y, z, occ, Znum, len(x))
+    return Znum, x, y, z, occ
+
+
+def rotate(ctblength, angleZ, angleY, x, y, z, dxc=0.0, dyc=0.0, dzc=0.0):
+    x, y, z = (np.array(a, np.float32) for a in (x, y, z))
+    load().msk_rotate(ctblength, dxc, dyc, dzc, angleZ, angleY, len(x), x, y, z)
+    return x, y, z
+
+
+def potential_table(Z):
+    knots, coef = np.zeros(100), np.zeros(400)
+    st = load().msk_potential_table(Z, knots, coef)
+    if st:
+        raise MskError(st, "bad atomic number")
+    return knots, coef.reshape(100, 4)
+
+
+# ------------------------------------------------------------------ context
+
+class Context:
+    """One libmsk context (device, stream and buffers)."""
+
+    def __init__(self, device=0):
+        L = load()
+        h = C.c_void_p()
+        st = L.msk_create(device, C.byref(h))
+        if st:
+            raise MskError(st, "msk_create failed: %s" % L.msk_status_string(st).decode())
+        self.h = h
+        self.L = L
+
+    def close(self):
+        if self.h:
+            self.L.msk_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st:
+            msg = self.L.msk_last_error(self.h).decode() or self.L.msk_status_string(st).decode()
+            raise MskError(st, msg)
+
+    def calculate(self, param, Znum, x, y, z, occ, ctblength, ctblengthz, nmode=0, wave0=None,
+                  wobble=None, lwobble=0):
+        """autoslic::calculate coherent branch; returns the exit wave [nx, ny, 2] float32."""
+        param = np.ascontiguousarray(param, np.float32)
+        nx, ny = int(param[pNX] + 0.1), int(param[pNY] + 0.1)
+        if wave0 is None:
+            wave0 = np.zeros((nx, ny, 2), np.float32)
+            wave0[..., 0] = 1.0
+        wave0 = np.ascontiguousarray(wave0, np.float32)
+        pix = np.zeros((nx, ny, 2), np.float32)
+        arrs = [np.ascontiguousarray(a, dt) for a, dt in
+                ((Znum, np.int32), (x, np.float32), (y, np.float32), (z, np.float32),
+                 (occ, np.float32))]
+        wob = np.zeros(len(arrs[1]), np.float32) if wobble is None else \
+            np.ascontiguousarray(wobble, np.float32)
+        st = self.L.msk_calculate(self.h, _ptr(pix), _ptr(wave0), param, len(arrs[1]),
+                                  *[_ptr(a) for a in arrs], _ptr(wob), ctblength, ctblengthz,
+                                  nmode, lwobble)
+        self._check(st)
+        return pix
+
+    def tilt_series(self, series, Znum, x, y, z, occ, angleZ, angleY, defocus, nconfig=1,
+                    displacements=None, images=None, exitwaves=None, want_exit=False):
+        """All orientations x configurations x defoci; returns images
+        [nangles, ndef, nx, ny] (and exit waves [nangles, nconfig, nx, ny, 2]).
+        images / exitwaves may be preallocated numpy arrays or torch CUDA tensors."""
+        angleZ = np.ascontiguousarray(angleZ, np.float64)
+        angleY = np.ascontiguousarray(angleY, np.float64)
+        defocus = np.ascontiguousarray(defocus, np.float64)
+        na, nd = len(angleZ), len(defocus)
+        if images is None:
+            images = np.zeros((na, nd, series.nx, series.ny), np.float32)
+        if exitwaves is None and want_exit:
+            exitwaves = np.zeros((na, nconfig, series.nx, series.ny, 2), np.float32)
+        kept = np.zeros(na * nconfig, np.int32)
+        arrs = [np.ascontiguousarray(a, dt) for a, dt in
+                ((Znum, np.int32), (x, np.float32), (y, np.float32), (z, np.float32),
+                 (occ, np.float32))]
+        disp = None if displacements is None else np.ascontiguousarray(displacements, np.float32)
+        st = self.L.msk_tilt_series(self.h, C.byref(series), len(arrs[1]), *[_ptr(a) for a in arrs],
+                                    na, angleZ, angleY, nd, _ptr(defocus), nconfig, _ptr(disp),
+                                    _ptr(images), _ptr(exitwaves), _ptr(kept))
+        self._check(st)
+        return (images, exitwaves, kept) if want_exit or exitwaves is not None else (images, kept)

@@ -1,0 +1,221 @@
+// fft_line.cuh -- shared-memory staged complex FFT of one line held across a
+// group of threads (the building block of every row and column pass).
+//
+// Convention (the reference's cfpix, TemsimLibrary/cfpix.cpp:137-193):
+//   forward  X[k] = sum_j x[j] exp(+2 pi i jk/N)     (cfpix::fft, FFTW_BACKWARD)
+//   inverse  x[j] = sum_k X[k] exp(-2 pi i jk/N)     (cfpix::ifft before its 1/N)
+// Both are unnormalised; callers fold 1/N into their pointwise multipliers.
+//
+// Work distribution: a line of N points is owned by T = N/E threads, E = 32
+// (E = N below 32).  Thread t holds elements t + m*T, m = 0..E-1, in registers
+// ("strided order") both before and after a transform, so a row pass loads and
+// stores fully coalesced and a forward transform, a pointwise multiply and an
+// inverse transform chain without any extra exchange.
+//
+// Algorithm: Stockham autosort.  Stage 1 is a radix-32 DFT in registers; the
+// remaining stages (radix 2..32) read the line from shared memory, apply
+// twiddles from a precomputed per-stage table and write back (or, for the
+// last stage, keep the result in registers).  1024 = 32*32 needs a single
+// shared-memory round trip per transform.
+//
+// Shared-memory layout of a line group: element idx of column c (of C lines
+// interleaved column-fastest) lives at (idx + idx/32)*C + c.  The one-in-32
+// padding makes the radix-32 scatter of stage 1 bank-conflict free; with C
+// columns innermost, a half-warp of a column pass touches 128 contiguous bytes.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace msk {
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+{
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cmul_conj(float2 a, float2 b)  // a * conj(b)
+{
+    return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+
+// cos / sin of 2*pi*k/32, k < 16 (only these occur in a radix-2 DIT of size <= 32)
+__device__ constexpr float kTwC[16] = {1.0f, 0.98078528f, 0.923879533f, 0.831469612f,
+                                       0.707106781f, 0.555570233f, 0.382683432f, 0.195090322f,
+                                       0.0f, -0.195090322f, -0.382683432f, -0.555570233f,
+                                       -0.707106781f, -0.831469612f, -0.923879533f, -0.98078528f};
+__device__ constexpr float kTwS[16] = {0.0f, 0.195090322f, 0.382683432f, 0.555570233f,
+                                       0.707106781f, 0.831469612f, 0.923879533f, 0.98078528f,
+                                       1.0f, 0.98078528f, 0.923879533f, 0.831469612f,
+                                       0.707106781f, 0.555570233f, 0.382683432f, 0.195090322f};
+
+__host__ __device__ constexpr int ilog2(int n)
+{
+    int b = 0;
+    while ((1 << b) < n) b++;
+    return b;
+}
+__host__ __device__ __forceinline__ constexpr int brev(int x, int bits)
+{
+    int r = 0;
+    for (int i = 0; i < bits; i++) r |= ((x >> i) & 1) << (bits - 1 - i);
+    return r;
+}
+
+// b * exp(+-2 pi i k/32), k < 16 known at compile time
+template <int K, bool INV>
+__device__ __forceinline__ float2 twc(float2 b)
+{
+    if constexpr (K == 0) {
+        return b;
+    } else if constexpr (K == 8) {
+        return INV ? make_float2(b.y, -b.x) : make_float2(-b.y, b.x);
+    } else {
+        constexpr float c = kTwC[K];
+        constexpr float s = INV ? -kTwS[K] : kTwS[K];
+        return make_float2(b.x * c - b.y * s, b.x * s + b.y * c);
+    }
+}
+
+// In-register DFT of R points v[0], v[S], ..., v[(R-1)*S], natural order in
+// and out.  Radix-2 decimation in time, all indices compile-time.
+template <int R, bool INV, int S, int LEN = 2>
+__device__ __forceinline__ void dft_levels(float2 *a)
+{
+    if constexpr (LEN <= R) {
+#pragma unroll
+        for (int i = 0; i < R; i += LEN) {
+#pragma unroll
+            for (int j = 0; j < LEN / 2; j++) {
+                // twiddle exp(+-2 pi i j/LEN) = kTw[j * 32/LEN]
+                float2 u = a[i + j];
+                float2 w;
+                switch (j * (32 / LEN)) {
+#define MSK_TWCASE(K) case K: w = twc<K, INV>(a[i + j + LEN / 2]); break;
+                    MSK_TWCASE(0) MSK_TWCASE(1) MSK_TWCASE(2) MSK_TWCASE(3)
+                    MSK_TWCASE(4) MSK_TWCASE(5) MSK_TWCASE(6) MSK_TWCASE(7)
+                    MSK_TWCASE(8) MSK_TWCASE(9) MSK_TWCASE(10) MSK_TWCASE(11)
+                    MSK_TWCASE(12) MSK_TWCASE(13) MSK_TWCASE(14) MSK_TWCASE(15)
+#undef MSK_TWCASE
+                    default: w = a[i + j + LEN / 2]; break;
+                }
+                a[i + j] = cadd(u, w);
+                a[i + j + LEN / 2] = csub(u, w);
+            }
+        }
+        dft_levels<R, INV, S, LEN * 2>(a);
+    }
+}
+
+template <int R, bool INV, int S>
+__device__ __forceinline__ void dft(float2 *v)
+{
+    static_assert(R >= 1 && R <= 32 && (R & (R - 1)) == 0, "radix");
+    if constexpr (R == 1) return;
+    float2 a[R];
+    constexpr int B = ilog2(R);
+#pragma unroll
+    for (int i = 0; i < R; i++) a[brev(i, B)] = v[i * S];
+    dft_levels<R, INV, S>(a);
+#pragma unroll
+    for (int i = 0; i < R; i++) v[i * S] = a[i];
+}
+
+// Radix plan per line length.
+template <int N>
+struct FftPlan {
+    static_assert(N >= 16 && N <= 4096 && (N & (N - 1)) == 0, "line length");
+    static constexpr int E = N >= 32 ? 32 : N;   // elements per thread
+    static constexpr int T = N / E;              // threads per line
+    static constexpr int REST = N / E;
+    // stages after the first: REST <= 32 -> one stage; else two
+    static constexpr int S = (REST == 1) ? 1 : (REST <= 32 ? 2 : 3);
+    static constexpr int R2 = (S >= 2) ? (REST <= 32 ? REST : (REST == 64 ? 8 : 16)) : 1;
+    static constexpr int R3 = (S == 3) ? REST / R2 : 1;
+    static constexpr int NS2 = E;          // sub-transform size entering stage 2
+    static constexpr int NS3 = E * R2;     // entering stage 3
+    // per-stage twiddle tables tw[r*Ns + j], r < R, j < Ns
+    static constexpr int TW2 = (S >= 2) ? NS2 * R2 : 0;
+    static constexpr int TW3 = (S == 3) ? NS3 * R3 : 0;
+    static constexpr int TWN = TW2 + TW3;
+    static constexpr int PADN = N + N / 32;  // padded line length in shared memory
+};
+
+template <int N>
+__device__ __forceinline__ int pidx(int idx) { return idx + (idx >> 5); }
+
+// Barrier among the threads that share a line group.
+template <bool BLOCK>
+__device__ __forceinline__ void group_sync()
+{
+    if constexpr (BLOCK) __syncthreads();
+    else __syncwarp();
+}
+
+// One middle/last Stockham stage.  Reads the line from shared memory into
+// registers (all reads before any write), twiddles, radix-R DFT; a middle
+// stage writes back, the last stage leaves the result in strided order.
+template <int N, int R, int NS, bool LAST, bool INV, int C, bool BLOCK>
+__device__ __forceinline__ void fft_stage(float2 (&v)[FftPlan<N>::E], float2 *buf, int c, int t,
+                                          const float2 *tw)
+{
+    constexpr int E = FftPlan<N>::E, T = FftPlan<N>::T, KB = E / R;
+#pragma unroll
+    for (int k = 0; k < KB; k++) {
+        const int b = t + k * T;
+#pragma unroll
+        for (int r = 0; r < R; r++) v[k + r * KB] = buf[pidx<N>(b + r * (N / R)) * C + c];
+    }
+    if constexpr (!LAST) group_sync<BLOCK>();
+#pragma unroll
+    for (int k = 0; k < KB; k++) {
+        const int b = t + k * T;
+        const int j = b % NS;
+#pragma unroll
+        for (int r = 1; r < R; r++) {
+            const float2 w = tw[r * NS + j];
+            v[k + r * KB] = INV ? cmul_conj(v[k + r * KB], w) : cmul(v[k + r * KB], w);
+        }
+        dft<R, INV, KB>(&v[k]);
+    }
+    if constexpr (!LAST) {
+#pragma unroll
+        for (int k = 0; k < KB; k++) {
+            const int b = t + k * T;
+            const int j = b % NS;
+            const int o = (b / NS) * NS * R + j;
+#pragma unroll
+            for (int r = 0; r < R; r++) buf[pidx<N>(o + r * NS) * C + c] = v[k + r * KB];
+        }
+        group_sync<BLOCK>();
+    }
+}
+
+// Full transform of one line: strided order in, strided order out.
+//   buf: the line group's shared buffer (C interleaved lines, padded)
+//   c:   this thread's line within the group; t: index within the line
+//   tw:  FftPlan<N>::TWN twiddles (stage 2 table, then stage 3 table)
+// Every thread of the group must call it (it contains group barriers).
+template <int N, bool INV, int C, bool BLOCK>
+__device__ __forceinline__ void fft_line(float2 (&v)[FftPlan<N>::E], float2 *buf, int c, int t,
+                                         const float2 *tw)
+{
+    using P = FftPlan<N>;
+    constexpr int E = P::E;
+    dft<E, INV, 1>(v);
+    if constexpr (P::S >= 2) {
+        group_sync<BLOCK>();  // earlier readers of buf are done
+#pragma unroll
+        for (int r = 0; r < E; r++) buf[pidx<N>(t * E + r) * C + c] = v[r];
+        group_sync<BLOCK>();
+        if constexpr (P::S == 2) {
+            fft_stage<N, P::R2, P::NS2, true, INV, C, BLOCK>(v, buf, c, t, tw);
+        } else {
+            fft_stage<N, P::R2, P::NS2, false, INV, C, BLOCK>(v, buf, c, t, tw);
+            fft_stage<N, P::R3, P::NS3, true, INV, C, BLOCK>(v, buf, c, t, tw + P::TW2);
+        }
+    }
+}
+
+}  // namespace msk

@@ -1,0 +1,1088 @@
+// msk_host.cu -- host side of libmsk: the C ABI (include/msk.h), the
+// reference-exact host preparation (rotation, Shell sort, slice assignment),
+// the potential tables, and the schedule of passes over a batch of waves.
+//
+// Host arithmetic that must round like the reference (rotation, slice
+// boundaries, frequency grids, propagator tables) is compiled with
+// -ffp-contract=off so that x86-64 and aarch64 give the same bits.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "msk.h"
+#include "msk_launch.cuh"
+
+namespace msk {
+
+const SizeOps *size_ops_16();
+const SizeOps *size_ops_32();
+const SizeOps *size_ops_64();
+const SizeOps *size_ops_128();
+const SizeOps *size_ops_256();
+const SizeOps *size_ops_512();
+const SizeOps *size_ops_1024();
+const SizeOps *size_ops_2048();
+const SizeOps *size_ops_4096();
+
+const SizeOps *size_ops(int n)
+{
+    switch (n) {
+    case 16: return size_ops_16();
+    case 32: return size_ops_32();
+    case 64: return size_ops_64();
+    case 128: return size_ops_128();
+    case 256: return size_ops_256();
+    case 512: return size_ops_512();
+    case 1024: return size_ops_1024();
+    case 2048: return size_ops_2048();
+    case 4096: return size_ops_4096();
+    default: return nullptr;
+    }
+}
+
+__global__ void k_plane_init(float2 *psi, const int *__restrict__ units, int nunits, int nx, int ny)
+{
+    const size_t plane = (size_t)nx * ny;
+    const size_t total = plane * nunits;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const size_t ui = i / plane, r = i % plane;
+        const int u = units ? units[ui] : (int)ui;
+        psi[(size_t)u * plane + r] = make_float2((r % ny) == 0 ? (float)ny : 0.0f, 0.0f);
+    }
+}
+
+// ------------------------------------------------------------------ physics
+// Restatements of the reference's slicelib routines used to build tables.
+namespace phys {
+
+static const double kFe[104][12] = {
+#include "kirkland_fparams.inc"
+};
+
+// slicelib.cpp:2891-2902
+double wavelength(double kev)
+{
+    const double emass = 510.99906, hc = 12.3984244;
+    return hc / sqrt(kev * (2 * emass + kev));
+}
+
+// slicelib.cpp:2441-2455
+double sigma(double kev)
+{
+    const double emass = 510.99906;
+    double x = (emass + kev) / (2.0 * emass + kev);
+    double wavl = wavelength(kev);
+    double pi = 4.0 * atan(1.0);
+    return 2.0 * pi * x / (wavl * kev);
+}
+
+// slicelib.cpp:457-474
+void freqn(float *ko, float *ko2, float *xo, int nk, double ak)
+{
+    int imid = (int)(nk / 2.0 + 0.5);
+    for (int i = 0; i < nk; i++) {
+        xo[i] = ((float)(i * ak)) / ((float)(nk - 1));
+        ko[i] = (i > imid) ? ((float)(i - nk)) / ((float)ak) : ((float)i) / ((float)ak);
+        ko2[i] = ko[i] * ko[i];
+    }
+}
+
+// Abramowitz & Stegun 9.8.1-9.8.6 polynomial fits (slicelib.cpp:189-258)
+double bessi0(double x)
+{
+    static const double a[] = {1.0, 3.5156229, 3.0899424, 1.2067492, 0.2659732, 0.0360768, 0.0045813};
+    static const double b[] = {0.39894228, 0.01328592, 0.00225319, -0.00157565, 0.00916281,
+                               -0.02057706, 0.02635537, -0.01647633, 0.00392377};
+    double ax = fabs(x), sum, t;
+    if (ax <= 3.75) {
+        t = x / 3.75;
+        t = t * t;
+        sum = a[6];
+        for (int i = 5; i >= 0; i--) sum = sum * t + a[i];
+    } else {
+        t = 3.75 / ax;
+        sum = b[8];
+        for (int i = 7; i >= 0; i--) sum = sum * t + b[i];
+        sum = exp(ax) * sum / sqrt(ax);
+    }
+    return sum;
+}
+
+double bessk0(double x)
+{
+    static const double a[] = {-0.57721566, 0.42278420, 0.23069756, 0.03488590, 0.00262698, 0.00010750, 0.00000740};
+    static const double b[] = {1.25331414, -0.07832358, 0.02189568, -0.01062446, 0.00587872, -0.00251540, 0.00053208};
+    double ax = fabs(x), x2, sum;
+    if ((ax > 0.0) && (ax <= 2.0)) {
+        x2 = ax / 2.0;
+        x2 = x2 * x2;
+        sum = a[6];
+        for (int i = 5; i >= 0; i--) sum = sum * x2 + a[i];
+        sum = -log(ax / 2.0) * bessi0(x) + sum;
+    } else if (ax > 2.0) {
+        x2 = 2.0 / ax;
+        sum = b[6];
+        for (int i = 5; i >= 0; i--) sum = sum * x2 + b[i];
+        sum = exp(-ax) * sum / sqrt(ax);
+    } else {
+        sum = 1.0e20;
+    }
+    return sum;
+}
+
+// Projected potential, 3 Lorentzians + 3 Gaussians (slicelib.cpp:2759-2792)
+double vzatom(int Z, double radius)
+{
+    const double al = 300.8242834, ag = 150.4121417, pi = 3.141592654;
+    if (Z < 1 || Z > 103) return 0.0;
+    double r = fabs(radius);
+    if (r < 1.0e-10) r = 1.0e-10;
+    double suml = 0.0, sumg = 0.0;
+    double x = 2.0 * pi * r;
+    for (int i = 0; i < 6; i += 2) suml += kFe[Z][i] * bessk0(x * sqrt(kFe[Z][i + 1]));
+    x = pi * r;
+    x = x * x;
+    for (int i = 6; i < 12; i += 2) sumg += kFe[Z][i] * exp(-x / kFe[Z][i + 1]) / kFe[Z][i + 1];
+    return al * suml + ag * sumg;
+}
+
+// Akima quasi-Hermite spline (slicelib.cpp:2537-2603)
+void splinh(const double *x, const double *y, double *b, double *c, double *d, int n)
+{
+    const double SMALL = 1.0e-25;
+    if (n < 4) return;
+    double m5 = (y[3] - y[2]) / (x[3] - x[2]);
+    double m4 = (y[2] - y[1]) / (x[2] - x[1]);
+    double m3 = (y[1] - y[0]) / (x[1] - x[0]);
+    double m2 = m3 + m3 - m4;
+    double m1 = m2 + m2 - m3;
+    double m54 = fabs(m5 - m4), m43 = fabs(m4 - m3), m32 = fabs(m3 - m2), m21 = fabs(m2 - m1);
+    double t1 = ((m43 + m21) > SMALL) ? (m43 * m2 + m21 * m3) / (m43 + m21) : 0.5 * (m2 + m3);
+    for (int i = 0; i < n - 1; i++) {
+        double t2 = ((m54 + m32) > SMALL) ? (m54 * m3 + m32 * m4) / (m54 + m32) : 0.5 * (m3 + m4);
+        double x43 = x[i + 1] - x[i];
+        b[i] = t1;
+        c[i] = (3.0 * m3 - t1 - t1 - t2) / x43;
+        d[i] = (t1 + t2 - m3 - m3) / (x43 * x43);
+        m1 = m2;
+        m2 = m3;
+        m3 = m4;
+        m4 = m5;
+        m5 = (i < n - 4) ? (y[i + 4] - y[i + 3]) / (x[i + 4] - x[i + 3]) : m4 + m4 - m3;
+        m21 = m32;
+        m32 = m43;
+        m43 = m54;
+        m54 = fabs(m5 - m4);
+        t1 = t2;
+    }
+    (void)m1;
+    (void)m21;
+}
+
+constexpr int kN = 100;
+
+// vzatomLUT tables (slicelib.cpp:2812-2875): knots r^2 with r log-spaced in
+// [0.01, 5] Angstrom; coefficients per Z built once and kept.
+struct Lut {
+    double knots[kN];
+    double y[104][kN], b[104][kN], c[104][kN], d[104][kN];
+    bool ready[104];
+    std::mutex mu;
+    Lut()
+    {
+        const double RMIN = 0.01, RMAX = 5.0;
+        double dlnr = log(RMAX / RMIN) / (kN - 1);
+        for (int i = 0; i < kN; i++) knots[i] = RMIN * exp(i * dlnr);
+        for (int i = 0; i < kN; i++) knots[i] = knots[i] * knots[i];
+        for (int z = 0; z < 104; z++) ready[z] = false;
+    }
+    void build(int Z)
+    {
+        std::lock_guard<std::mutex> g(mu);
+        if (ready[Z]) return;
+        for (int i = 0; i < kN; i++) y[Z][i] = vzatom(Z, sqrt(knots[i]));
+        splinh(knots, y[Z], b[Z], c[Z], d[Z], kN);
+        ready[Z] = true;
+    }
+};
+
+Lut &lut()
+{
+    static Lut L;
+    return L;
+}
+
+}  // namespace phys
+
+// ------------------------------------------------------------------ host prep
+
+// Shell sort by z (slicelib.cpp:2467-2504); same comparisons and moves, so
+// the same permutation.
+static void sort_by_z(float *x, float *y, float *z, float *occ, int *Znum, int natom)
+{
+    int h;
+    for (h = 1; h <= (natom - 1) / 9; h = 3 * h + 1)
+        ;
+    for (; h > 0; h /= 3)
+        for (int i = h; i < natom; i++) {
+            int j = i;
+            const float x2 = x[i], y2 = y[i], z2 = z[i], occ2 = occ[i];
+            const int Z2 = Znum[i];
+            while ((j >= h) && (z2 < z[j - h])) {
+                x[j] = x[j - h];
+                y[j] = y[j - h];
+                z[j] = z[j - h];
+                occ[j] = occ[j - h];
+                Znum[j] = Znum[j - h];
+                j -= h;
+            }
+            x[j] = x2;
+            y[j] = y2;
+            z[j] = z2;
+            occ[j] = occ2;
+            Znum[j] = Z2;
+        }
+}
+
+// Rotation about z then y' (autosliccmd.cpp:727-748), float arithmetic.
+static void rotate(float ctblength, double dxc, double dyc, double dzc, double angleZ,
+                   double angleY, int natom, float *x, float *y, float *z)
+{
+    const float xc = (float)(ctblength / 2.0 + dxc), yc = (float)(ctblength / 2.0 + dyc),
+                zc = (float)(ctblength / 2.0 + dzc);
+    const float sinZ = (float)sin(angleZ), cosZ = (float)cos(angleZ);
+    const float sinY = (float)sin(angleY), cosY = (float)cos(angleY);
+    for (int k = 0; k < natom; k++) {
+        const float xxx = xc + (x[k] - xc) * cosZ + (-y[k] + yc) * sinZ;
+        const float yyy = yc + (x[k] - xc) * sinZ + (y[k] - yc) * cosZ;
+        x[k] = xxx;
+        y[k] = yyy;
+    }
+    for (int k = 0; k < natom; k++) {
+        const float xxx = xc + (x[k] - xc) * cosY + (z[k] - zc) * sinY;
+        const float zzz = zc + (-x[k] + xc) * sinY + (z[k] - zc) * cosY;
+        x[k] = xxx;
+        z[k] = zzz;
+    }
+}
+
+// Slice boundaries of the coherent branch (autoslic.cpp:747-756, 828):
+// zslice = dz, 2dz, ... accumulated in double while < zmax + dz.
+static int slice_count(float deltaz_f, float zmax)
+{
+    const double deltaz = deltaz_f;
+    double zslice = deltaz;
+    int n = 0;
+    while (zslice < (zmax + deltaz)) {
+        n++;
+        zslice += deltaz;
+    }
+    return n;
+}
+
+// Atoms per slice of a z-sorted list (autoslic.cpp:756-762, 828-830).
+static void slice_counts(float deltaz_f, float zmax, int natom, const float *z2, int nslices,
+                         int *counts)
+{
+    const double deltaz = deltaz_f;
+    double zslice = deltaz;
+    int istart = 0;
+    for (int s = 0; s < nslices; s++) {
+        int na = 0;
+        for (int i = istart; i < natom; i++)
+            if (z2[i] < zslice) na++;
+            else break;
+        counts[s] = na;
+        zslice += deltaz;
+        istart += na;
+    }
+}
+
+// Plan-wide geometry computed on the host exactly as the reference does.
+struct GridPre {
+    int nx, ny;
+    float ax, by, v0, wavlen, k2max;
+    double scalex, scaley;  // float-divided pixel pitch, promoted
+    double sigma;
+    Geom g;                 // device pointers filled at upload
+    std::vector<float> kx, kx2, ky, ky2;
+    std::vector<float2> propx, propy;
+};
+
+static void grid_pre(GridPre &gp, int nx, int ny, float ax, float by, float v0, float deltaz,
+                     float ctiltx, float ctilty)
+{
+    gp.nx = nx;
+    gp.ny = ny;
+    gp.ax = ax;
+    gp.by = by;
+    gp.v0 = v0;
+    gp.wavlen = (float)phys::wavelength(v0);
+    gp.kx.resize(nx);
+    gp.kx2.resize(nx);
+    gp.ky.resize(ny);
+    gp.ky2.resize(ny);
+    std::vector<float> xp(std::max(nx, ny));
+    phys::freqn(gp.kx.data(), gp.kx2.data(), xp.data(), nx, ax);
+    phys::freqn(gp.ky.data(), gp.ky2.data(), xp.data(), ny, by);
+    // autoslic.cpp:383-393
+    const float BW = 2.0F / 3.0F;
+    float k2max = nx / (2.0F * ax);
+    float tctx = ny / (2.0F * by);
+    if (tctx < k2max) k2max = tctx;
+    k2max = BW * k2max;
+    gp.k2max = k2max * k2max;
+    // autoslic.cpp:395-414
+    tctx = (float)(2.0 * tan(ctiltx));
+    const float tcty = (float)(2.0 * tan(ctilty));
+    const float pi = (float)(4.0 * atan(1.0));
+    const float scale = pi * deltaz;
+    gp.propx.resize(nx);
+    gp.propy.resize(ny);
+    for (int ix = 0; ix < nx; ix++) {
+        const double t = scale * (gp.kx2[ix] * gp.wavlen - gp.kx[ix] * tctx);
+        gp.propx[ix] = make_float2((float)cos(t), (float)-sin(t));
+    }
+    for (int iy = 0; iy < ny; iy++) {
+        const double t = scale * (gp.ky2[iy] * gp.wavlen - gp.ky[iy] * tcty);
+        gp.propy[iy] = make_float2((float)cos(t), (float)-sin(t));
+    }
+    // trlayer constants (autoslic.cpp:927-941)
+    gp.sigma = phys::sigma(v0) / 1000.0;
+    gp.scalex = ax / nx;  // float division, as the reference
+    gp.scaley = by / ny;
+    double rmin = ax / ((double)nx);
+    const double r = by / ((double)ny);
+    rmin = 0.25 * sqrt(0.5 * (rmin * rmin + r * r));
+    Geom &g = gp.g;
+    g = Geom{};
+    g.nx = nx;
+    g.ny = ny;
+    g.k2max = gp.k2max;
+    g.inv_n = 1.0f / ((float)nx * (float)ny);
+    g.sigma_f = (float)gp.sigma;
+    g.scalex_f = (float)gp.scalex;
+    g.scaley_f = (float)gp.scaley;
+    g.rminsq = (float)(rmin * rmin);
+    g.idx = (int)(nx * 3.0 / ax) + 1;
+    g.idy = (int)(ny * 3.0 / by) + 1;
+}
+
+// Stockham stage twiddles for line length n, matching FftPlan<n>.
+template <int N>
+static void twiddles_n(std::vector<float2> &out)
+{
+    using P = FftPlan<N>;
+    out.assign(std::max(P::TWN, 1), make_float2(1.0f, 0.0f));
+    const double twopi = 8.0 * atan(1.0);
+    auto fill = [&](int off, int ns, int r_) {
+        for (int r = 0; r < r_; r++)
+            for (int j = 0; j < ns; j++) {
+                const double a = twopi * (double)r * (double)j / (double)(ns * r_);
+                out[off + r * ns + j] = make_float2((float)cos(a), (float)sin(a));
+            }
+    };
+    if (P::S >= 2) fill(0, P::NS2, P::R2);
+    if (P::S == 3) fill(P::TW2, P::NS3, P::R3);
+}
+
+static bool twiddles(int n, std::vector<float2> &out)
+{
+    switch (n) {
+    case 16: twiddles_n<16>(out); return true;
+    case 32: twiddles_n<32>(out); return true;
+    case 64: twiddles_n<64>(out); return true;
+    case 128: twiddles_n<128>(out); return true;
+    case 256: twiddles_n<256>(out); return true;
+    case 512: twiddles_n<512>(out); return true;
+    case 1024: twiddles_n<1024>(out); return true;
+    case 2048: twiddles_n<2048>(out); return true;
+    case 4096: twiddles_n<4096>(out); return true;
+    default: return false;
+    }
+}
+
+// One orientation/configuration ready for the splat: atoms inside the box,
+// sorted by z, grouped by slice, positions relative to their pixel.
+struct UnitAtoms {
+    std::vector<SplatAtom> atoms;
+    std::vector<int> counts;  // per slice
+    int kept = 0;
+    int status = MSK_OK;
+};
+
+struct PrepSpec {
+    int natom;
+    const int *Znum;
+    const float *x, *y, *z, *occ;
+    float ctblength, ctblengthz, deltaz;
+    int nslices;
+    bool rotate;
+    double angZ, angY, dxc, dyc, dzc;
+    const float *disp;  // [3][natom] or null
+    bool drop_outside;
+    const int *zmap;    // Z -> compact index
+};
+
+static void prep_unit(const GridPre &gp, const PrepSpec &ps, UnitAtoms &out)
+{
+    const int n0 = ps.natom;
+    std::vector<float> x(ps.x, ps.x + n0), y(ps.y, ps.y + n0), z(ps.z, ps.z + n0),
+        occ(ps.occ, ps.occ + n0);
+    std::vector<int> Z(ps.Znum, ps.Znum + n0);
+    if (ps.rotate)
+        rotate(ps.ctblength, ps.dxc, ps.dyc, ps.dzc, ps.angZ, ps.angY, n0, x.data(), y.data(),
+               z.data());
+    if (ps.disp) {
+        for (int k = 0; k < n0; k++) {
+            x[k] += ps.disp[k];
+            y[k] += ps.disp[n0 + k];
+            z[k] += ps.disp[2 * n0 + k];
+        }
+    }
+    int n = n0;
+    if (ps.drop_outside) {
+        n = 0;
+        for (int k = 0; k < n0; k++) {
+            if (x[k] < 0 || x[k] > ps.ctblength || y[k] < 0 || y[k] > ps.ctblength || z[k] < 0 ||
+                z[k] > ps.ctblengthz)
+                continue;
+            x[n] = x[k];
+            y[n] = y[k];
+            z[n] = z[k];
+            occ[n] = occ[k];
+            Z[n] = Z[k];
+            n++;
+        }
+    } else if (n > 0) {
+        // the reference's range checks (autoslic.cpp:270-299)
+        float xmin = x[0], xmax = x[0], ymin = y[0], ymax = y[0], zmin = z[0], zmax = z[0];
+        for (int i = 0; i < n; i++) {
+            xmin = std::min(xmin, x[i]);
+            xmax = std::max(xmax, x[i]);
+            ymin = std::min(ymin, y[i]);
+            ymax = std::max(ymax, y[i]);
+            zmin = std::min(zmin, z[i]);
+            zmax = std::max(zmax, z[i]);
+        }
+        if (xmin < 0 || ymin < 0 || zmin < 0 || xmax > ps.ctblength || ymax > ps.ctblength ||
+            zmax > ps.ctblengthz) {
+            out.status = MSK_EBOX;
+            return;
+        }
+    }
+    for (int i = 0; i < n; i++)
+        if (Z[i] < 1 || Z[i] > 103) {
+            out.status = MSK_EZNUM;
+            return;
+        }
+    sort_by_z(x.data(), y.data(), z.data(), occ.data(), Z.data(), n);
+    if (n > 0 && (z[0] < 0 || z[n - 1] > ps.ctblengthz)) {  // autoslic.cpp:734-739
+        out.status = MSK_EZSORT;
+        return;
+    }
+    out.counts.assign(ps.nslices, 0);
+    slice_counts(ps.deltaz, ps.ctblengthz, n, z.data(), ps.nslices, out.counts.data());
+    int used = 0;
+    for (int s = 0; s < ps.nslices; s++) used += out.counts[s];
+    out.atoms.resize(used);
+    for (int i = 0; i < used; i++) {
+        // trlayer's pixel of the atom (autoslic.cpp:952-953) and the offset
+        // of the atom from it, in double
+        const int ixo = (int)(x[i] / gp.scalex), iyo = (int)(y[i] / gp.scaley);
+        SplatAtom a;
+        a.fx = (float)((double)x[i] - (double)ixo * gp.scalex);
+        a.fy = (float)((double)y[i] - (double)iyo * gp.scaley);
+        a.occ = occ[i];
+        a.meta = (uint32_t)ixo | ((uint32_t)iyo << kMetaBits) |
+                 ((uint32_t)ps.zmap[Z[i]] << (2 * kMetaBits));
+        out.atoms[i] = a;
+    }
+    out.kept = n;
+    out.status = MSK_OK;
+}
+
+static void parallel_for(int n, int nthreads, const std::function<void(int)> &fn)
+{
+    nthreads = std::max(1, std::min(nthreads, n));
+    if (nthreads == 1) {
+        for (int i = 0; i < n; i++) fn(i);
+        return;
+    }
+    std::atomic<int> next(0);
+    std::vector<std::thread> th;
+    for (int t = 0; t < nthreads; t++)
+        th.emplace_back([&] {
+            for (;;) {
+                const int i = next.fetch_add(1);
+                if (i >= n) break;
+                fn(i);
+            }
+        });
+    for (auto &t : th) t.join();
+}
+
+static int host_threads()
+{
+    const unsigned hc = std::thread::hardware_concurrency();
+    return hc ? (int)hc : 4;
+}
+
+}  // namespace msk
+
+// ------------------------------------------------------------------ context
+
+using namespace msk;
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t reserve(size_t bytes)
+    {
+        if (bytes <= cap) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e == cudaSuccess) cap = bytes;
+        return e;
+    }
+    template <typename T> T *as() const { return reinterpret_cast<T *>(p); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+}  // namespace
+
+struct msk_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    DevBuf psi, tbuf, atoms, slice_off, act, tables, imgmeta, wave0, images, exitw;
+    std::vector<int> zmap = std::vector<int>(104, -1);
+};
+
+namespace {
+
+int fail(msk_context *ctx, int code, const std::string &msg)
+{
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+#define MSK_CUDA(ctx, call)                                                                     \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess)                                                                  \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? MSK_ENOMEM : MSK_ECUDA,          \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                    \
+    } while (0)
+
+bool pow2_supported(int n) { return size_ops(n) != nullptr; }
+
+// Compact atomic-number map and device tables (frequency grids, propagator,
+// twiddles, potential spline) for one grid.
+int upload_tables(msk_context *ctx, GridPre &gp, const std::vector<int> &zlist)
+{
+    std::vector<float2> twr, twc;
+    twiddles(gp.ny, twr);
+    twiddles(gp.nx, twc);
+    const int nz = (int)zlist.size();
+    auto &L = phys::lut();
+    for (int Z : zlist) L.build(Z);
+    std::vector<float> knots(phys::kN);
+    for (int i = 0; i < phys::kN; i++) knots[i] = (float)L.knots[i];
+    std::vector<float4> coef((size_t)std::max(nz, 1) * phys::kN);
+    for (int zi = 0; zi < nz; zi++) {
+        const int Z = zlist[zi];
+        for (int i = 0; i < phys::kN; i++)
+            coef[(size_t)zi * phys::kN + i] = make_float4((float)L.y[Z][i], (float)L.b[Z][i],
+                                                          (float)L.c[Z][i], (float)L.d[Z][i]);
+    }
+    // one allocation, 256-byte aligned pieces
+    size_t off = 0;
+    auto piece = [&](size_t bytes) {
+        size_t o = off;
+        off += (bytes + 255) & ~size_t(255);
+        return o;
+    };
+    const size_t o_kx2 = piece(4 * gp.nx), o_ky2 = piece(4 * gp.ny), o_kx = piece(4 * gp.nx),
+                 o_ky = piece(4 * gp.ny), o_px = piece(8 * gp.nx), o_py = piece(8 * gp.ny),
+                 o_twr = piece(8 * twr.size()), o_twc = piece(8 * twc.size()),
+                 o_kn = piece(4 * knots.size()), o_cf = piece(16 * coef.size());
+    std::vector<unsigned char> host(off);
+    std::memcpy(&host[o_kx2], gp.kx2.data(), 4 * gp.nx);
+    std::memcpy(&host[o_ky2], gp.ky2.data(), 4 * gp.ny);
+    std::memcpy(&host[o_kx], gp.kx.data(), 4 * gp.nx);
+    std::memcpy(&host[o_ky], gp.ky.data(), 4 * gp.ny);
+    std::memcpy(&host[o_px], gp.propx.data(), 8 * gp.nx);
+    std::memcpy(&host[o_py], gp.propy.data(), 8 * gp.ny);
+    std::memcpy(&host[o_twr], twr.data(), 8 * twr.size());
+    std::memcpy(&host[o_twc], twc.data(), 8 * twc.size());
+    std::memcpy(&host[o_kn], knots.data(), 4 * knots.size());
+    std::memcpy(&host[o_cf], coef.data(), 16 * coef.size());
+    MSK_CUDA(ctx, ctx->tables.reserve(off));
+    MSK_CUDA(ctx, cudaMemcpyAsync(ctx->tables.p, host.data(), off, cudaMemcpyHostToDevice,
+                                  ctx->stream));
+    // the host staging vector must outlive the copy
+    MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    unsigned char *b = ctx->tables.as<unsigned char>();
+    Geom &g = gp.g;
+    g.kx2 = reinterpret_cast<const float *>(b + o_kx2);
+    g.ky2 = reinterpret_cast<const float *>(b + o_ky2);
+    g.propx = reinterpret_cast<const float2 *>(b + o_px);
+    g.propy = reinterpret_cast<const float2 *>(b + o_py);
+    g.tw_row = reinterpret_cast<const float2 *>(b + o_twr);
+    g.tw_col = reinterpret_cast<const float2 *>(b + o_twc);
+    g.knots = reinterpret_cast<const float *>(b + o_kn);
+    g.coef = reinterpret_cast<const float4 *>(b + o_cf);
+    (void)o_kx;
+    (void)o_ky;
+    return MSK_OK;
+}
+
+const float *tables_kx(msk_context *ctx, const GridPre &gp)
+{
+    // kx follows kx2 and ky2 in the table block (see upload_tables)
+    size_t o = ((4 * (size_t)gp.nx + 255) & ~size_t(255)) + ((4 * (size_t)gp.ny + 255) & ~size_t(255));
+    return reinterpret_cast<const float *>(ctx->tables.as<unsigned char>() + o);
+}
+const float *tables_ky(msk_context *ctx, const GridPre &gp)
+{
+    size_t o = ((4 * (size_t)gp.nx + 255) & ~size_t(255)) * 2 + ((4 * (size_t)gp.ny + 255) & ~size_t(255));
+    return reinterpret_cast<const float *>(ctx->tables.as<unsigned char>() + o);
+}
+
+bool is_device_ptr(const void *p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// A batch of units (waves) with their atoms uploaded: the slice loop.
+struct Batch {
+    int nunits = 0, nslices = 0;
+    std::vector<int> slice_off;   // [nunits][nslices+1] absolute atom offsets
+    std::vector<int> act_off;     // [nslices+1]
+    std::vector<int> act;         // active units per slice
+};
+
+int upload_batch(msk_context *ctx, const std::vector<UnitAtoms> &ua, int u0, int nunits,
+                 int nslices, Batch &b)
+{
+    b.nunits = nunits;
+    b.nslices = nslices;
+    const int nsl1 = nslices + 1;
+    b.slice_off.assign((size_t)nunits * nsl1, 0);
+    size_t total = 0;
+    for (int i = 0; i < nunits; i++) {
+        const UnitAtoms &u = ua[u0 + i];
+        int o = (int)total;
+        for (int s = 0; s < nslices; s++) {
+            b.slice_off[(size_t)i * nsl1 + s] = o;
+            o += u.counts[s];
+        }
+        b.slice_off[(size_t)i * nsl1 + nslices] = o;
+        total = (size_t)o;
+    }
+    b.act_off.assign(nsl1, 0);
+    b.act.clear();
+    for (int s = 0; s < nslices; s++) {
+        b.act_off[s] = (int)b.act.size();
+        for (int i = 0; i < nunits; i++)
+            if (ua[u0 + i].counts[s] > 0) b.act.push_back(i);
+    }
+    b.act_off[nslices] = (int)b.act.size();
+    std::vector<SplatAtom> atoms(std::max<size_t>(total, 1));
+    size_t o = 0;
+    for (int i = 0; i < nunits; i++) {
+        const auto &a = ua[u0 + i].atoms;
+        std::copy(a.begin(), a.end(), atoms.begin() + o);
+        o += a.size();
+    }
+    MSK_CUDA(ctx, ctx->atoms.reserve(atoms.size() * sizeof(SplatAtom)));
+    MSK_CUDA(ctx, ctx->slice_off.reserve(b.slice_off.size() * sizeof(int)));
+    MSK_CUDA(ctx, ctx->act.reserve(std::max<size_t>(b.act.size(), 1) * sizeof(int)));
+    MSK_CUDA(ctx, cudaMemcpyAsync(ctx->atoms.p, atoms.data(), atoms.size() * sizeof(SplatAtom),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    MSK_CUDA(ctx, cudaMemcpyAsync(ctx->slice_off.p, b.slice_off.data(),
+                                  b.slice_off.size() * sizeof(int), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+    if (!b.act.empty())
+        MSK_CUDA(ctx, cudaMemcpyAsync(ctx->act.p, b.act.data(), b.act.size() * sizeof(int),
+                                      cudaMemcpyHostToDevice, ctx->stream));
+    MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return MSK_OK;
+}
+
+// The slice loop over a batch: the psi buffer holds W0 = S(wave0) on entry
+// and W = S(exit wave) on return.
+int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode)
+{
+    const SizeOps *rop = size_ops(gp.ny), *cop = size_ops(gp.nx);
+    const Geom &g = gp.g;
+    cudaStream_t s = ctx->stream;
+    float2 *psi = ctx->psi.as<float2>(), *tb = ctx->tbuf.as<float2>();
+    const int *act = ctx->act.as<int>();
+    const int nsl1 = b.nslices + 1;
+    for (int sl = 0; sl < b.nslices; sl++) {
+        const int na = b.act_off[sl + 1] - b.act_off[sl];
+        const int *units = act + b.act_off[sl];
+        if (na > 0) {
+            rop->splat(g, units, na, sl, nsl1, ctx->slice_off.as<int>(),
+                       ctx->atoms.as<SplatAtom>(), tb, s);
+            cop->col_mask(g, units, na, tb, tb, s);
+            rop->row_transmit(g, units, na, tb, psi, 1.0f / ((float)gp.ny * (float)gp.ny), s);
+        }
+        if (nmode == 0) cop->col_prop(g, nullptr, b.nunits, psi, psi, s);
+    }
+    MSK_CUDA(ctx, cudaGetLastError());
+    return MSK_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ C ABI
+
+extern "C" {
+
+int msk_create(int device, msk_context **out)
+{
+    if (!out) return MSK_EINVAL;
+    *out = nullptr;
+    msk_context *ctx = new (std::nothrow) msk_context();
+    if (!ctx) return MSK_ENOMEM;
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete ctx;
+        return MSK_ECUDA;
+    }
+    *out = ctx;
+    return MSK_OK;
+}
+
+void msk_destroy(msk_context *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (DevBuf *b : {&ctx->psi, &ctx->tbuf, &ctx->atoms, &ctx->slice_off, &ctx->act, &ctx->tables,
+                      &ctx->imgmeta, &ctx->wave0, &ctx->images, &ctx->exitw})
+        b->release();
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char *msk_last_error(const msk_context *ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+const char *msk_status_string(int st)
+{
+    switch (st) {
+    case MSK_OK: return "ok";
+    case MSK_EBADSIZE: return "bad size parameters";
+    case MSK_EBOX: return "atom outside the box";
+    case MSK_EZSORT: return "sorted z outside [0, ctblengthz]";
+    case MSK_EZNUM: return "atomic number outside 1..103";
+    case MSK_ENOMEM: return "out of memory";
+    case MSK_EUNSUPPORTED: return "unsupported grid size or mode";
+    case MSK_ECUDA: return "CUDA error";
+    case MSK_EINVAL: return "invalid argument";
+    default: return "unknown status";
+    }
+}
+
+int msk_slice_count(float deltaz, float ctblengthz) { return slice_count(deltaz, ctblengthz); }
+
+int msk_slice_assign(float deltaz_f, float zmax, int natom, const float *z2, int *slice_of)
+{
+    const int n = slice_count(deltaz_f, zmax);
+    std::vector<int> counts(n);
+    slice_counts(deltaz_f, zmax, natom, z2, n, counts.data());
+    int i = 0;
+    for (int s = 0; s < n; s++)
+        for (int k = 0; k < counts[s]; k++) slice_of[i++] = s;
+    for (; i < natom; i++) slice_of[i] = -1;
+    return n;
+}
+
+void msk_sort_by_z(float *x, float *y, float *z, float *occ, int *Znum, int natom)
+{
+    sort_by_z(x, y, z, occ, Znum, natom);
+}
+
+void msk_rotate(float ctblength, double dxc, double dyc, double dzc, double angleZ,
+                double angleY, int natom, float *x, float *y, float *z)
+{
+    rotate(ctblength, dxc, dyc, dzc, angleZ, angleY, natom, x, y, z);
+}
+
+int msk_potential_table(int Z, double *knots, double *coef)
+{
+    if (Z < 1 || Z > 103) return MSK_EZNUM;
+    auto &L = phys::lut();
+    L.build(Z);
+    for (int i = 0; i < phys::kN; i++) {
+        knots[i] = L.knots[i];
+        coef[4 * i] = L.y[Z][i];
+        coef[4 * i + 1] = L.b[Z][i];
+        coef[4 * i + 2] = L.c[Z][i];
+        coef[4 * i + 3] = L.d[Z][i];
+    }
+    return MSK_OK;
+}
+
+
+static int build_zmap(msk_context *ctx, int natom, const int *Znum, std::vector<int> &zlist)
+{
+    std::vector<int> &zmap = ctx->zmap;
+    std::fill(zmap.begin(), zmap.end(), -1);
+    zlist.clear();
+    for (int i = 0; i < natom; i++) {
+        const int Z = Znum[i];
+        if (Z < 1 || Z > 103) return fail(ctx, MSK_EZNUM, "atomic number " + std::to_string(Z));
+        if (zmap[Z] < 0) {
+            if ((int)zlist.size() >= kMaxZidx)
+                return fail(ctx, MSK_EUNSUPPORTED, "more than 64 distinct atomic numbers");
+            zmap[Z] = (int)zlist.size();
+            zlist.push_back(Z);
+        }
+    }
+    return MSK_OK;
+}
+
+int msk_calculate(msk_context *ctx, float *pix, const float *wave0, const float *param,
+                  int natom, const int *Znum, const float *x, const float *y, const float *z,
+                  const float *occ, const float *wobble, float ctblength, float ctblengthz,
+                  int nmode, int lwobble)
+{
+    (void)wobble;
+    if (!ctx) return MSK_EINVAL;
+    ctx->err.clear();
+    if (!pix || !wave0 || !param || natom < 0 ||
+        (natom > 0 && (!Znum || !x || !y || !z || !occ)))
+        return fail(ctx, MSK_EINVAL, "null pointer or negative atom count");
+    if (lwobble) return fail(ctx, MSK_EUNSUPPORTED, "thermal (lwobble) branches are not provided");
+    const float ax = param[MSK_pAX], by = param[MSK_pBY];
+    const int nx = (int)(param[MSK_pNX] + 0.1F), ny = (int)(param[MSK_pNY] + 0.1F);
+    if (nx < 1 || ny < 1 || ax < 0.0 || by < 0.0)
+        return fail(ctx, MSK_EBADSIZE, "bad size parameters");
+    if (!pow2_supported(nx) || !pow2_supported(ny))
+        return fail(ctx, MSK_EUNSUPPORTED, "grid must be a power of two from 16 to 4096");
+    MSK_CUDA(ctx, cudaSetDevice(ctx->device));
+    GridPre gp;
+    grid_pre(gp, nx, ny, ax, by, param[MSK_pENERGY], param[MSK_pDELTAZ], param[MSK_pXCTILT],
+             param[MSK_pYCTILT]);
+    const int nslices = slice_count(param[MSK_pDELTAZ], ctblengthz);
+    std::vector<int> zlist;
+    // the reference's range check comes before any atomic-number check
+    // (autoslic.cpp:270-299 before vzatomLUT)
+    if (natom > 0) {
+        float xmin = x[0], xmax = x[0], ymin = y[0], ymax = y[0], zmin = z[0], zmax = z[0];
+        for (int i = 0; i < natom; i++) {
+            xmin = std::min(xmin, x[i]);
+            xmax = std::max(xmax, x[i]);
+            ymin = std::min(ymin, y[i]);
+            ymax = std::max(ymax, y[i]);
+            zmin = std::min(zmin, z[i]);
+            zmax = std::max(zmax, z[i]);
+        }
+        if (xmin < 0 || ymin < 0 || zmin < 0 || xmax > ctblength || ymax > ctblength ||
+            zmax > ctblengthz)
+            return fail(ctx, MSK_EBOX, "atom outside the box");
+    }
+    {
+        int st = build_zmap(ctx, natom, Znum, zlist);
+        if (st) return st;
+    }
+    std::vector<UnitAtoms> ua(1);
+    PrepSpec ps{natom, Znum, x, y, z, occ, ctblength, ctblengthz, param[MSK_pDELTAZ], nslices,
+                false, 0, 0, 0, 0, 0, nullptr, false, ctx->zmap.data()};
+    prep_unit(gp, ps, ua[0]);
+    if (ua[0].status) return fail(ctx, ua[0].status, msk_status_string(ua[0].status));
+    int st = upload_tables(ctx, gp, zlist);
+    if (st) return st;
+    Batch b;
+    st = upload_batch(ctx, ua, 0, 1, nslices, b);
+    if (st) return st;
+    const size_t plane = (size_t)nx * ny;
+    MSK_CUDA(ctx, ctx->psi.reserve(plane * sizeof(float2)));
+    MSK_CUDA(ctx, ctx->tbuf.reserve(plane * sizeof(float2)));
+    MSK_CUDA(ctx, ctx->wave0.reserve(plane * sizeof(float2)));
+    MSK_CUDA(ctx, cudaMemcpyAsync(ctx->wave0.p, wave0, plane * sizeof(float2),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    const SizeOps *rop = size_ops(ny);
+    rop->row_init(gp.g, nullptr, 1, ctx->wave0.as<float2>(), ctx->psi.as<float2>(), 1.0f,
+                  ctx->stream);
+    st = run_slices(ctx, gp, b, nmode);
+    if (st) return st;
+    rop->row_exit(gp.g, nullptr, 1, ctx->psi.as<float2>(), ctx->tbuf.as<float2>(), ctx->stream);
+    MSK_CUDA(ctx, cudaGetLastError());
+    MSK_CUDA(ctx, cudaMemcpyAsync(pix, ctx->tbuf.p, plane * sizeof(float2),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return MSK_OK;
+}
+
+int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int *Znum,
+                    const float *x, const float *y, const float *z, const float *occ,
+                    int nangles, const double *angleZ, const double *angleY, int ndefocus,
+                    const double *defocus, int nconfig, const float *displacements,
+                    float *images, float *exitwaves, int *kept)
+{
+    if (!ctx) return MSK_EINVAL;
+    ctx->err.clear();
+    if (!s || natom < 0 || nangles < 1 || ndefocus < 0 || nconfig < 1 || !angleZ || !angleY ||
+        (ndefocus > 0 && (!defocus || !images)) ||
+        (natom > 0 && (!Znum || !x || !y || !z || !occ)) || (nconfig > 1 && !displacements))
+        return fail(ctx, MSK_EINVAL, "bad tilt-series arguments");
+    const int nx = s->nx, ny = s->ny;
+    if (nx < 1 || ny < 1 || s->ctblength < 0.0f) return fail(ctx, MSK_EBADSIZE, "bad size parameters");
+    if (!pow2_supported(nx) || !pow2_supported(ny))
+        return fail(ctx, MSK_EUNSUPPORTED, "grid must be a power of two from 16 to 4096");
+    MSK_CUDA(ctx, cudaSetDevice(ctx->device));
+    GridPre gp;
+    // MsctKirkland passes a zero crystal tilt (autosliccmd.cpp:435-437)
+    grid_pre(gp, nx, ny, s->ctblength, s->ctblength, s->v0, s->deltaz, 0.0f, 0.0f);
+    const int nslices = slice_count(s->deltaz, s->ctblengthz);
+    std::vector<int> zlist;
+    int st = build_zmap(ctx, natom, Znum, zlist);
+    if (st) return st;
+    st = upload_tables(ctx, gp, zlist);
+    if (st) return st;
+
+    const size_t plane = (size_t)nx * ny;
+    const int nunits = nangles * nconfig;
+    size_t free_b = 0, total_b = 0;
+    MSK_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
+    // psi + t per unit; the image and exit-wave outputs are held separately
+    const bool img_dev = ndefocus > 0 && is_device_ptr(images);
+    const bool ew_dev = exitwaves && is_device_ptr(exitwaves);
+    const size_t img_bytes = (size_t)nangles * ndefocus * plane * sizeof(float);
+    size_t budget = free_b - std::min(free_b, (size_t)(img_dev ? 0 : img_bytes));
+    budget = std::min<size_t>(budget / 2, (size_t)64 << 30);
+    int B = (int)std::max<size_t>(1, std::min<size_t>(nunits, budget / (2 * plane * sizeof(float2))));
+    if (s->max_batch > 0) B = std::min(B, s->max_batch);
+    if (nconfig > 1 && B > nconfig) B = (B / nconfig) * nconfig;  // whole angles per batch
+
+    float *d_images = images;
+    if (ndefocus > 0 && !img_dev) {
+        MSK_CUDA(ctx, ctx->images.reserve(img_bytes));
+        d_images = ctx->images.as<float>();
+    }
+    MSK_CUDA(ctx, ctx->psi.reserve((size_t)B * plane * sizeof(float2)));
+    MSK_CUDA(ctx, ctx->tbuf.reserve((size_t)B * plane * sizeof(float2)));
+
+    const float wavlen = gp.wavlen;
+    float k2maxo = s->aobj / wavlen;  // autosliccmd.cpp:1042-1043
+    k2maxo = k2maxo * k2maxo;
+    const double pi = 4.0 * atan(1.0);
+    const double l = wavlen;
+
+    std::vector<UnitAtoms> ua(nunits);
+    const SizeOps *rop = size_ops(ny), *cop = size_ops(nx);
+    for (int u0 = 0; u0 < nunits; u0 += B) {
+        const int nb = std::min(B, nunits - u0);
+        parallel_for(nb, host_threads(), [&](int i) {
+            const int u = u0 + i, a = u / nconfig, c = u % nconfig;
+            PrepSpec ps{natom, Znum, x, y, z, occ, s->ctblength, s->ctblengthz, s->deltaz,
+                        nslices, true, angleZ[a], angleY[a], s->dxc, s->dyc, s->dzc,
+                        displacements ? displacements + (size_t)c * 3 * natom : nullptr, true,
+                        ctx->zmap.data()};
+            prep_unit(gp, ps, ua[u]);
+        });
+        for (int i = 0; i < nb; i++)
+            if (ua[u0 + i].status)
+                return fail(ctx, ua[u0 + i].status, msk_status_string(ua[u0 + i].status));
+        Batch b;
+        st = upload_batch(ctx, ua, u0, nb, nslices, b);
+        if (st) return st;
+        float2 *psi = ctx->psi.as<float2>(), *tb = ctx->tbuf.as<float2>();
+        k_plane_init<<<1024, 256, 0, ctx->stream>>>(psi, nullptr, nb, nx, ny);
+        st = run_slices(ctx, gp, b, s->nmode);
+        if (st) return st;
+        if (exitwaves) {
+            rop->row_exit(gp.g, nullptr, nb, psi, tb, ctx->stream);
+            MSK_CUDA(ctx, cudaMemcpyAsync(exitwaves + (size_t)u0 * plane * 2, tb,
+                                          (size_t)nb * plane * sizeof(float2),
+                                          ew_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                          ctx->stream));
+        }
+        if (ndefocus > 0) {
+            // one image per angle in this batch; its configurations in order
+            const int a_first = u0 / nconfig, a_last = (u0 + nb - 1) / nconfig;
+            const int nimg = a_last - a_first + 1;
+            std::vector<int> meta;  // img_off[nimg+1] | img_units | img_dst[nimg] | img_flags[nimg]
+            std::vector<int> off(nimg + 1), units, flags(nimg);
+            for (int a = a_first; a <= a_last; a++) {
+                const int c0 = std::max(u0, a * nconfig), c1 = std::min(u0 + nb, (a + 1) * nconfig);
+                off[a - a_first] = (int)units.size();
+                for (int u = c0; u < c1; u++) units.push_back(u - u0);
+                int f = 0;
+                if (c0 > a * nconfig) f |= 1;                        // continue a partial sum
+                if (c1 == (a + 1) * nconfig && nconfig > 1) f |= 2;   // last configuration
+                flags[a - a_first] = f;
+            }
+            off[nimg] = (int)units.size();
+            const size_t nmeta = off.size() + units.size() + 2 * (size_t)nimg;
+            MSK_CUDA(ctx, ctx->imgmeta.reserve(nmeta * sizeof(int) * (size_t)ndefocus));
+            for (int d = 0; d < ndefocus; d++) {
+                const double rprime = defocus[d] - 0.5 * s->ctblengthz;  // autosliccmd.cpp:1060
+                Fresnel fr;
+                fr.a1 = pi * l * rprime;
+                fr.a3 = (pi / 2.0) * s->cs3 * l * l * l;
+                fr.a5 = (pi / 3.0) * s->cs5 * l * l * l * l * l;
+                fr.a2c = (pi / 2.0) * l * s->astig * cos(2.0 * s->astig_angle);
+                fr.a2s = (pi / 2.0) * l * s->astig * sin(2.0 * s->astig_angle);
+                fr.k2maxo = k2maxo;
+                fr.kx = tables_kx(ctx, gp);
+                fr.ky = tables_ky(ctx, gp);
+                // psi_d = iS(iF(exp(-i chi) F(W)))/N
+                cop->col_fresnel(gp.g, nullptr, nb, psi, tb, fr, 1.0f / ((float)nx * (float)ny),
+                                 ctx->stream);
+                meta.clear();
+                meta.insert(meta.end(), off.begin(), off.end());
+                meta.insert(meta.end(), units.begin(), units.end());
+                for (int a = a_first; a <= a_last; a++) meta.push_back(a * ndefocus + d);
+                meta.insert(meta.end(), flags.begin(), flags.end());
+                int *dm = ctx->imgmeta.as<int>() + (size_t)d * nmeta;
+                MSK_CUDA(ctx, cudaMemcpyAsync(dm, meta.data(), meta.size() * sizeof(int),
+                                              cudaMemcpyHostToDevice, ctx->stream));
+                const int *d_off = dm, *d_units = dm + off.size(),
+                          *d_dst = d_units + units.size(), *d_flags = d_dst + nimg;
+                rop->row_intensity(gp.g, nimg, d_off, d_units, d_dst, d_flags, tb, d_images,
+                                   (float)nconfig, ctx->stream);
+            }
+        }
+        MSK_CUDA(ctx, cudaGetLastError());
+        MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    if (ndefocus > 0 && !img_dev)
+        MSK_CUDA(ctx, cudaMemcpyAsync(images, d_images, img_bytes, cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+    MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (kept)
+        for (int u = 0; u < nunits; u++) kept[u] = ua[u].kept;
+    return MSK_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,143 @@
+// msk_launch.cuh -- host launchers for the passes of one line length N.
+// Each msk_size_<N>.cu instantiates SizeOps for its N; the dispatcher picks
+// row passes by ny and column passes by nx.
+#pragma once
+
+#include <mutex>
+
+#include "msk_passes.cuh"
+#include "msk_types.h"
+
+namespace msk {
+
+struct SizeOps {
+    int n;
+    void (*splat)(const Geom &, const int *units, int nunits, int slice, int nsl1,
+                  const int *slice_off, const SplatAtom *atoms, float2 *tbuf, cudaStream_t);
+    void (*col_mask)(const Geom &, const int *units, int nunits, const float2 *in, float2 *out,
+                     cudaStream_t);
+    void (*col_prop)(const Geom &, const int *units, int nunits, const float2 *in, float2 *out,
+                     cudaStream_t);
+    void (*col_fresnel)(const Geom &, const int *units, int nunits, const float2 *in,
+                        float2 *out, const Fresnel &, float scale, cudaStream_t);
+    void (*row_transmit)(const Geom &, const int *units, int nunits, const float2 *tbuf,
+                         float2 *psi, float out_scale, cudaStream_t);
+    void (*row_init)(const Geom &, const int *units, int nunits, const float2 *wave0,
+                     float2 *psi, float scale, cudaStream_t);
+    void (*row_exit)(const Geom &, const int *units, int nunits, const float2 *psi,
+                     float2 *out, cudaStream_t);
+    void (*row_intensity)(const Geom &, int nimg, const int *img_off, const int *img_units,
+                          const int *img_dst, const int *img_flags, const float2 *ebuf,
+                          float *images, float nconf, cudaStream_t);
+};
+
+// Line lengths with kernels: 16 .. 4096, powers of two.
+const SizeOps *size_ops(int n);
+
+template <int N> struct Smem {
+    using P = FftPlan<N>;
+    static constexpr int NTS = RowCfg<N>::L * P::T;
+    static constexpr size_t splat = (size_t)(P::TWN + RowCfg<N>::L * P::PADN) * 8 + NTS * 16 +
+                                    128 * 4 + ((NTS + 31) / 32 + 1) * 4;
+    static constexpr size_t col = (size_t)(P::TWN + ColCfg<N>::C * P::PADN) * 8;
+    static constexpr size_t transmit = (size_t)(P::TWN + RowCfg<N>::LT * (P::PADN + N)) * 8;
+    static constexpr size_t row = (size_t)(P::TWN + RowCfg<N>::L * P::PADN) * 8;
+};
+
+template <typename K>
+inline void set_smem(K kernel, size_t bytes, std::once_flag &flag)
+{
+    std::call_once(flag, [&] {
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    });
+}
+
+template <int N>
+struct Launch {
+    using P = FftPlan<N>;
+    static int row_blocks(const Geom &g, int L) { return (g.nx + L - 1) / L; }
+
+    static void splat(const Geom &g, const int *units, int nunits, int slice, int nsl1,
+                      const int *slice_off, const SplatAtom *atoms, float2 *tbuf, cudaStream_t s)
+    {
+        static std::once_flag f;
+        set_smem(k_row_splat<N>, Smem<N>::splat, f);
+        const int L = RowCfg<N>::L;
+        k_row_splat<N><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::splat, s>>>(
+            g, units, slice, nsl1, slice_off, atoms, tbuf);
+    }
+    template <int MODE>
+    static void col(const Geom &g, const int *units, int nunits, const float2 *in, float2 *out,
+                    const Fresnel &fr, float scale, cudaStream_t s)
+    {
+        static std::once_flag f;
+        set_smem(k_col_pass<N, MODE>, Smem<N>::col, f);
+        const int C = ColCfg<N>::C;
+        k_col_pass<N, MODE><<<nunits * (g.ny / C), ColCfg<N>::NT, Smem<N>::col, s>>>(
+            g, units, in, out, fr, scale);
+    }
+    static void col_mask(const Geom &g, const int *units, int nunits, const float2 *in,
+                         float2 *out, cudaStream_t s)
+    {
+        col<kColMask>(g, units, nunits, in, out, Fresnel{}, 1.0f / (float)g.nx, s);
+    }
+    static void col_prop(const Geom &g, const int *units, int nunits, const float2 *in,
+                         float2 *out, cudaStream_t s)
+    {
+        col<kColProp>(g, units, nunits, in, out, Fresnel{}, 1.0f / (float)g.nx, s);
+    }
+    static void col_fresnel(const Geom &g, const int *units, int nunits, const float2 *in,
+                            float2 *out, const Fresnel &fr, float scale, cudaStream_t s)
+    {
+        col<kColFresnel>(g, units, nunits, in, out, fr, scale, s);
+    }
+    static void row_transmit(const Geom &g, const int *units, int nunits, const float2 *tbuf,
+                             float2 *psi, float out_scale, cudaStream_t s)
+    {
+        static std::once_flag f;
+        set_smem(k_row_transmit<N>, Smem<N>::transmit, f);
+        const int L = RowCfg<N>::LT;
+        k_row_transmit<N><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::transmit, s>>>(
+            g, units, tbuf, psi, out_scale);
+    }
+    static void row_init(const Geom &g, const int *units, int nunits, const float2 *wave0,
+                         float2 *psi, float scale, cudaStream_t s)
+    {
+        static std::once_flag f;
+        set_smem(k_row_simple<N, kRowInit>, Smem<N>::row, f);
+        const int L = RowCfg<N>::L;
+        k_row_simple<N, kRowInit><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::row, s>>>(
+            g, units, wave0, psi, scale);
+    }
+    static void row_exit(const Geom &g, const int *units, int nunits, const float2 *psi,
+                         float2 *out, cudaStream_t s)
+    {
+        static std::once_flag f;
+        set_smem(k_row_simple<N, kRowExit>, Smem<N>::row, f);
+        const int L = RowCfg<N>::L;
+        k_row_simple<N, kRowExit><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::row, s>>>(
+            g, units, psi, out, 1.0f / (float)g.ny);
+    }
+    static void row_intensity(const Geom &g, int nimg, const int *img_off, const int *img_units,
+                              const int *img_dst, const int *img_flags, const float2 *ebuf,
+                              float *images, float nconf, cudaStream_t s)
+    {
+        static std::once_flag f;
+        set_smem(k_row_intensity<N>, Smem<N>::row, f);
+        const int L = RowCfg<N>::L;
+        k_row_intensity<N><<<nimg * row_blocks(g, L), L * P::T, Smem<N>::row, s>>>(
+            g, img_off, img_units, img_dst, img_flags, ebuf, images, nconf);
+    }
+
+    static const SizeOps *ops()
+    {
+        static const SizeOps o = {N,         splat,        col_mask, col_prop,     col_fresnel,
+                                  row_transmit, row_init,  row_exit, row_intensity};
+        return &o;
+    }
+};
+
+}  // namespace msk
+
+#define MSK_INSTANTIATE_SIZE(N) \
+    namespace msk { const SizeOps *size_ops_##N() { return Launch<N>::ops(); } }

@@ -1,0 +1,411 @@
+// msk_passes.cuh -- the fused row and column passes of the batched multislice.
+//
+// HBM layout: every wave / transmission buffer is complex64 [unit][ix][iy],
+// iy contiguous (the reference's cfpix layout, data[iy + ix*ny]).  A "row"
+// is one ix (ny contiguous points), a "column" one iy (nx points, stride ny).
+//
+// State kept between passes (S = the row transform along iy, unnormalised,
+// kernel exp(+2 pi i ..); iS its inverse, unnormalised, kernel exp(-..);
+// F, iF the same along ix; iS(S(f)) = ny f):
+//   psi buffer:  W = S(psi)          (between slices; psi = iS(W)/ny)
+//   t buffer:    A = S(t)            (after P1)
+//                B = S(t_bl)         (after P2, t_bl the band-limited t)
+// One slice (TemsimLibrary/autoslic.cpp:756-830, trlayer 917-1013):
+//   P1 k_row_splat     potential v by splat, t = exp(i sigma v), A = S(t)
+//   P2 k_col_pass<0>   B = iF(M F(A))/nx        (M: 2/3 band limit)
+//   P3 k_row_transmit  W = S(iS(W) * iS(B))/ny^2          (wave *= trans)
+//   P4 k_col_pass<1>   W = iF(P F(W))/nx        (P: propagator + aperture)
+// With unnormalised transforms these scalings are exactly the reference's
+// fft / ifft-with-1/(nx*ny) pairs.  An empty slice is P4 alone: the
+// wave's row iFFT and FFT around a missing transmit cancel.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "fft_line.cuh"
+#include "msk_types.h"
+
+namespace msk {
+
+__device__ __forceinline__ int pmod(int a, int n)
+{
+    int r = a % n;
+    return r < 0 ? r + n : r;
+}
+
+// Rows (lines of length NY) per CTA for the plain row passes and for P3.
+template <int NY> struct RowCfg {
+    static constexpr int T = FftPlan<NY>::T;
+    static constexpr int L = (256 / T) > 0 ? 256 / T : 1;
+    static constexpr int LT = (128 / T) > 0 ? 128 / T : 1;  // P3 (needs a stash)
+    static constexpr bool BLK = T > 32;
+};
+// Columns per CTA for the column passes.
+template <int NX> struct ColCfg {
+    // 256 threads per CTA (at most 16 columns): keeps 255 registers per thread
+    // available for the 32 strided elements of each column
+    static constexpr int C = (8192 / NX) < 16 ? (8192 / NX) : 16;
+    static constexpr int NT = C * FftPlan<NX>::T;
+};
+
+constexpr int kKnots = 100;
+
+// Spline of the projected potential vs r^2 (TemsimLibrary/slicelib.cpp:2402-2425,
+// 2812-2875), evaluated in float: bisection for the interval as seval does.
+__device__ __forceinline__ float spline_vz(const float *knots, const float4 *coef, float rsq)
+{
+    int i;
+    if (rsq <= knots[0]) {
+        i = 0;
+    } else if (rsq >= knots[kKnots - 2]) {
+        i = kKnots - 2;
+    } else {
+        int lo = 0, hi = kKnots;
+#pragma unroll 1
+        while (hi - lo > 1) {
+            int mid = (lo + hi) >> 1;
+            if (rsq < knots[mid]) hi = mid;
+            else lo = mid;
+        }
+        i = lo;
+    }
+    const float4 c = __ldg(&coef[i]);
+    const float z = rsq - knots[i];
+    return c.x + (c.y + (c.z + c.w * z) * z) * z;
+}
+
+// ---------------------------------------------------------------- P1
+// One CTA = L rows of one unit.  Atoms of the (unit, slice) whose window
+// touches these rows are staged into shared memory in slice order (ordered
+// block compaction), then every thread adds the potential of each staged
+// atom to the pixels it owns (iy = t mod T of its row) -- a gather with a
+// fixed pixel owner, so the sum order per pixel is the atom order and the
+// result is deterministic, with no atomics (autoslic.cpp:950-984 is a racy
+// scatter in the reference).  Then t = exp(i sigma v) and the row FFT.
+template <int NY>
+__global__ void __launch_bounds__(RowCfg<NY>::L * FftPlan<NY>::T)
+k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
+            const int *__restrict__ slice_off, const SplatAtom *__restrict__ atoms,
+            float2 *__restrict__ tbuf)
+{
+    using P = FftPlan<NY>;
+    constexpr int T = P::T, E = P::E, L = RowCfg<NY>::L, NT = L * T, NW = (NT + 31) / 32;
+    constexpr bool BLK = RowCfg<NY>::BLK;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2 *s_tw = reinterpret_cast<float2 *>(smem);
+    float2 *s_lines = s_tw + P::TWN;
+    SplatAtom *s_atoms = reinterpret_cast<SplatAtom *>(s_lines + L * P::PADN);
+    float *s_knots = reinterpret_cast<float *>(s_atoms + NT);
+    int *s_cnt = reinterpret_cast<int *>(s_knots + 128);
+
+    const int tid = threadIdx.x, l = tid / T, t = tid % T;
+    const int nx = g.nx;
+    const int bpu = (nx + L - 1) / L;
+    const int u = units[blockIdx.x / bpu];
+    const int ix0 = (blockIdx.x % bpu) * L;
+    const int ix = ix0 + l;
+    const bool row_ok = ix < nx;
+
+    for (int i = tid; i < P::TWN; i += NT) s_tw[i] = g.tw_row[i];
+    for (int i = tid; i < kKnots; i += NT) s_knots[i] = g.knots[i];
+    float *vacc = reinterpret_cast<float *>(s_lines + l * P::PADN);
+#pragma unroll
+    for (int m = 0; m < E; m++) vacc[t + m * T] = 0.0f;
+    __syncthreads();
+
+    const int a0 = slice_off[u * nsl1 + slice], a1 = slice_off[u * nsl1 + slice + 1];
+    const int W = 2 * g.idx + 1;
+    const int lane = tid & 31, warp = tid >> 5;
+    for (int base = a0; base < a1; base += NT) {
+        const int a = base + tid;
+        bool hit = false;
+        SplatAtom at;
+        if (a < a1) {
+            at = atoms[a];
+            const int ixo = (int)(at.meta & kMetaMask);
+            const int rel = pmod(ixo - g.idx - ix0, nx);
+            hit = (W >= nx) || (rel < L) || (rel + W > nx);
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, hit);
+        if (lane == 0) s_cnt[warp] = __popc(bal);
+        __syncthreads();
+        if (warp == 0) {
+            int c = lane < NW ? s_cnt[lane] : 0;
+            int incl = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            if (lane < NW) s_cnt[lane] = incl - c;
+            if (lane == 31) s_cnt[NW] = incl;
+        }
+        __syncthreads();
+        if (hit) s_atoms[s_cnt[warp] + __popc(bal & ((1u << lane) - 1u))] = at;
+        const int nsel = s_cnt[NW];
+        __syncthreads();
+        if (row_ok) {
+            for (int k = 0; k < nsel; k++) {
+                const SplatAtom sa = s_atoms[k];
+                const int ixo = (int)(sa.meta & kMetaMask);
+                const int iyo = (int)((sa.meta >> kMetaBits) & kMetaMask);
+                const float4 *coef = g.coef + (sa.meta >> (2 * kMetaBits)) * kKnots;
+                const int ws = ixo - g.idx;
+                for (int ixp = ws + pmod(ix - ws, nx); ixp < ws + W; ixp += nx) {
+                    const float dx = sa.fx - (float)(ixp - ixo) * g.scalex_f;
+                    const float dx2 = dx * dx;
+                    const int ys = iyo - g.idy;
+                    for (int iyp = ys + pmod(t - ys, T); iyp <= iyo + g.idy; iyp += T) {
+                        const float dy = sa.fy - (float)(iyp - iyo) * g.scaley_f;
+                        float rsq = dx2 + dy * dy;
+                        if (rsq <= 9.0f) {
+                            rsq = fmaxf(rsq, g.rminsq);
+                            vacc[pmod(iyp, NY)] += sa.occ * spline_vz(s_knots, coef, rsq);
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+
+    float2 v[E];
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+        float s, c;
+        sincosf(vacc[t + m * T] * g.sigma_f, &s, &c);
+        v[m] = make_float2(c, s);
+    }
+    fft_line<NY, false, 1, BLK>(v, s_lines + l * P::PADN, 0, t, s_tw);
+    if (row_ok) {
+        float2 *dst = tbuf + ((size_t)u * nx + ix) * NY;
+#pragma unroll
+        for (int m = 0; m < E; m++) dst[t + m * T] = v[m];
+    }
+}
+
+// ---------------------------------------------------------------- P2 / P4 / free space
+// Column FFT, pointwise multiplier times fscale, column inverse FFT.  One
+// CTA = C adjacent columns of one unit; C columns interleave in shared
+// memory so each half-warp moves whole 32-byte sectors.
+//   MODE 0: 2/3 band limit of the transmission function
+//           (autoslic.cpp:999-1009)
+//   MODE 1: Fresnel propagator p_y then p_x with the 2/3 aperture
+//           (slicelib.cpp:811-849)
+//   MODE 2: free-space step exp(-i chi) with the objective aperture
+enum { kColMask = 0, kColProp = 1, kColFresnel = 2 };
+
+template <int NX, int MODE>
+__global__ void __launch_bounds__(ColCfg<NX>::NT)
+k_col_pass(const Geom g, const int *__restrict__ units, const float2 *in, float2 *out,
+           const Fresnel fr, float fscale)
+{
+    using P = FftPlan<NX>;
+    constexpr int T = P::T, E = P::E, C = ColCfg<NX>::C, NT = ColCfg<NX>::NT;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2 *s_tw = reinterpret_cast<float2 *>(smem);
+    float2 *s_buf = s_tw + P::TWN;
+
+    const int tid = threadIdx.x, c = tid % C, t = tid / C;
+    const int ny = g.ny;
+    const int bpu = ny / C;
+    const int u = units ? units[blockIdx.x / bpu] : (int)(blockIdx.x / bpu);
+    const int iy = (blockIdx.x % bpu) * C + c;
+    for (int i = tid; i < P::TWN; i += NT) s_tw[i] = g.tw_col[i];
+
+    const size_t plane = (size_t)NX * ny;
+    const float2 *src = in + (size_t)u * plane + iy;
+    float2 v[E];
+#pragma unroll
+    for (int m = 0; m < E; m++) v[m] = src[(size_t)(t + m * T) * ny];
+    __syncthreads();
+    fft_line<NX, false, C, true>(v, s_buf, c, t, s_tw);
+
+    if constexpr (MODE == kColMask) {
+        const float ky2 = __ldg(&g.ky2[iy]);
+#pragma unroll
+        for (int m = 0; m < E; m++) {
+            const float k2 = __fadd_rn(__ldg(&g.kx2[t + m * T]), ky2);
+            v[m] = (k2 < g.k2max) ? cscale(v[m], fscale) : make_float2(0.0f, 0.0f);
+        }
+    } else if constexpr (MODE == kColProp) {
+        const float ky2 = __ldg(&g.ky2[iy]);
+        const float2 py = __ldg(&g.propy[iy]);
+#pragma unroll
+        for (int m = 0; m < E; m++) {
+            const int ix = t + m * T;
+            const float kx2 = __ldg(&g.kx2[ix]);
+            if (kx2 < g.k2max && __fadd_rn(kx2, ky2) < g.k2max) {
+                const float2 w = cmul(cmul(v[m], py), __ldg(&g.propx[ix]));
+                v[m] = cscale(w, fscale);
+            } else {
+                v[m] = make_float2(0.0f, 0.0f);
+            }
+        }
+    } else {
+        const float ky2 = __ldg(&g.ky2[iy]);
+        const double ky = (double)__ldg(&fr.ky[iy]);
+        const double twopi = 6.283185307179586;
+#pragma unroll
+        for (int m = 0; m < E; m++) {
+            const int ix = t + m * T;
+            const float k2f = __fadd_rn(__ldg(&g.kx2[ix]), ky2);
+            if (fr.k2maxo > 0.0f && !(k2f < fr.k2maxo)) {
+                v[m] = make_float2(0.0f, 0.0f);
+            } else {
+                const double kx = (double)__ldg(&fr.kx[ix]);
+                const double k2 = kx * kx + ky * ky;
+                double chi = fr.a1 * k2 + fr.a3 * k2 * k2 + fr.a5 * k2 * k2 * k2 +
+                             fr.a2c * (kx * kx - ky * ky) + fr.a2s * (2.0 * kx * ky);
+                chi -= twopi * rint(chi / twopi);
+                float s, cc;
+                sincosf((float)chi, &s, &cc);
+                const float2 w = cmul(v[m], make_float2(cc, -s));
+                v[m] = cscale(w, fscale);
+            }
+        }
+    }
+    fft_line<NX, true, C, true>(v, s_buf, c, t, s_tw);
+    float2 *dst = out + (size_t)u * plane + iy;
+#pragma unroll
+    for (int m = 0; m < E; m++) dst[(size_t)(t + m * T) * ny] = v[m];
+}
+
+// ---------------------------------------------------------------- P3
+// W = S(iS(W) * iS(B)) * out_scale (out_scale = 1/ny^2): wave *= trans
+// (cfpix.cpp:349-372) between the transmission's and the wave's row
+// transforms.
+template <int NY>
+__global__ void __launch_bounds__(RowCfg<NY>::LT * FftPlan<NY>::T)
+k_row_transmit(const Geom g, const int *__restrict__ units, const float2 *__restrict__ tbuf,
+               float2 *__restrict__ psi, float out_scale)
+{
+    using P = FftPlan<NY>;
+    constexpr int T = P::T, E = P::E, L = RowCfg<NY>::LT, NT = L * T;
+    constexpr bool BLK = RowCfg<NY>::BLK;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2 *s_tw = reinterpret_cast<float2 *>(smem);
+    float2 *s_lines = s_tw + P::TWN;
+    float2 *s_stash = s_lines + L * P::PADN;
+
+    const int tid = threadIdx.x, l = tid / T, t = tid % T;
+    const int nx = g.nx;
+    const int bpu = (nx + L - 1) / L;
+    const int u = units[blockIdx.x / bpu];
+    const int ix = (blockIdx.x % bpu) * L + l;
+    const bool row_ok = ix < nx;
+    for (int i = tid; i < P::TWN; i += NT) s_tw[i] = g.tw_row[i];
+
+    const size_t off = ((size_t)u * nx + (row_ok ? ix : 0)) * NY;
+    float2 v[E];
+#pragma unroll
+    for (int m = 0; m < E; m++) v[m] = tbuf[off + t + m * T];
+    __syncthreads();
+    float2 *buf = s_lines + l * P::PADN;
+    float2 *stash = s_stash + l * NY;
+    fft_line<NY, true, 1, BLK>(v, buf, 0, t, s_tw);
+#pragma unroll
+    for (int m = 0; m < E; m++) stash[t + m * T] = v[m];
+#pragma unroll
+    for (int m = 0; m < E; m++) v[m] = psi[off + t + m * T];
+    fft_line<NY, true, 1, BLK>(v, buf, 0, t, s_tw);
+#pragma unroll
+    for (int m = 0; m < E; m++) v[m] = cmul(v[m], stash[t + m * T]);
+    fft_line<NY, false, 1, BLK>(v, buf, 0, t, s_tw);
+    if (row_ok) {
+#pragma unroll
+        for (int m = 0; m < E; m++) psi[off + t + m * T] = cscale(v[m], out_scale);
+    }
+}
+
+// ---------------------------------------------------------------- row utilities
+// MODE 0: W0 = S(wave0) * scale (start state from an incident wave; wave0
+//         shared by all units, units[i] selects the destination)
+// MODE 1: psi = iS(W) * scale, scale = 1/ny (exit wave)
+enum { kRowInit = 0, kRowExit = 1 };
+
+template <int NY, int MODE>
+__global__ void __launch_bounds__(RowCfg<NY>::L * FftPlan<NY>::T)
+k_row_simple(const Geom g, const int *__restrict__ units, const float2 *__restrict__ in,
+             float2 *__restrict__ out, float scale)
+{
+    using P = FftPlan<NY>;
+    constexpr int T = P::T, E = P::E, L = RowCfg<NY>::L, NT = L * T;
+    constexpr bool BLK = RowCfg<NY>::BLK;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2 *s_tw = reinterpret_cast<float2 *>(smem);
+    float2 *s_lines = s_tw + P::TWN;
+    const int tid = threadIdx.x, l = tid / T, t = tid % T;
+    const int nx = g.nx;
+    const int bpu = (nx + L - 1) / L;
+    const int ui = blockIdx.x / bpu;
+    const int u = units ? units[ui] : ui;
+    const int ix = (blockIdx.x % bpu) * L + l;
+    const bool row_ok = ix < nx;
+    for (int i = tid; i < P::TWN; i += NT) s_tw[i] = g.tw_row[i];
+    const size_t row = (size_t)(row_ok ? ix : 0) * NY;
+    const float2 *src = (MODE == kRowInit) ? in + row : in + (size_t)u * nx * NY + row;
+    float2 v[E];
+#pragma unroll
+    for (int m = 0; m < E; m++) v[m] = src[t + m * T];
+    __syncthreads();
+    fft_line<NY, MODE == kRowExit, 1, BLK>(v, s_lines + l * P::PADN, 0, t, s_tw);
+    if (row_ok) {
+        float2 *dst = out + (size_t)u * nx * NY + row;
+#pragma unroll
+        for (int m = 0; m < E; m++) dst[t + m * T] = cscale(v[m], scale);
+    }
+}
+
+// Detector intensity, averaged over thermal configurations
+// (autosliccmd.cpp:1205-1224: I = |psi|^2, summed in configuration order,
+// divided by the configuration count after the last one).
+//   img_units[img_off[i] .. img_off[i+1]) : units (configurations, in order)
+//                                           whose free-space waves make image i
+//   img_dst[i]: destination image index; img_flags[i]: 1 = add onto the
+//   partial sum already stored, 2 = divide by nconf after adding.
+template <int NY>
+__global__ void __launch_bounds__(RowCfg<NY>::L * FftPlan<NY>::T)
+k_row_intensity(const Geom g, const int *__restrict__ img_off, const int *__restrict__ img_units,
+                const int *__restrict__ img_dst, const int *__restrict__ img_flags,
+                const float2 *__restrict__ ebuf, float *__restrict__ images, float nconf)
+{
+    using P = FftPlan<NY>;
+    constexpr int T = P::T, E = P::E, L = RowCfg<NY>::L, NT = L * T;
+    constexpr bool BLK = RowCfg<NY>::BLK;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2 *s_tw = reinterpret_cast<float2 *>(smem);
+    float2 *s_lines = s_tw + P::TWN;
+    const int tid = threadIdx.x, l = tid / T, t = tid % T;
+    const int nx = g.nx;
+    const int bpu = (nx + L - 1) / L;
+    const int img = blockIdx.x / bpu;
+    const int ix = (blockIdx.x % bpu) * L + l;
+    const bool row_ok = ix < nx;
+    for (int i = tid; i < P::TWN; i += NT) s_tw[i] = g.tw_row[i];
+    __syncthreads();
+    const size_t row = (size_t)(row_ok ? ix : 0) * NY;
+    float acc[E];
+    const int flags = img_flags[img];
+    float *dst = images + (size_t)img_dst[img] * nx * NY + row;
+#pragma unroll
+    for (int m = 0; m < E; m++) acc[m] = (flags & 1) && row_ok ? dst[t + m * T] : 0.0f;
+    for (int k = img_off[img]; k < img_off[img + 1]; k++) {
+        const float2 *src = ebuf + (size_t)img_units[k] * nx * NY + row;
+        float2 v[E];
+#pragma unroll
+        for (int m = 0; m < E; m++) v[m] = src[t + m * T];
+        fft_line<NY, true, 1, BLK>(v, s_lines + l * P::PADN, 0, t, s_tw);
+#pragma unroll
+        for (int m = 0; m < E; m++) acc[m] += v[m].x * v[m].x + v[m].y * v[m].y;
+    }
+    if (row_ok) {
+#pragma unroll
+        for (int m = 0; m < E; m++) dst[t + m * T] = (flags & 2) ? __fdiv_rn(acc[m], nconf) : acc[m];
+    }
+}
+
+// Plane incident wave: W0 = S(1) = ny at iy = 0, zero elsewhere, per row.
+__global__ void k_plane_init(float2 *psi, const int *__restrict__ units, int nunits, int nx, int ny);
+
+}  // namespace msk

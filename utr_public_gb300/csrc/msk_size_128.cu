@@ -1,0 +1,3 @@
+// Kernel instantiations for line length 128 (row passes for ny = 128, column passes for nx = 128).
+#include "msk_launch.cuh"
+MSK_INSTANTIATE_SIZE(128)

@@ -1,0 +1,56 @@
+// msk_types.h -- host/device descriptors shared by the launchers and kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace msk {
+
+// Everything a pass needs to know about one grid (one plan).  Passed to the
+// kernels by value.  Float members hold exactly the float values the
+// reference computes (TemsimLibrary/autoslic.cpp:326-414, 929-941), so that
+// band-limit and aperture decisions are bit-identical with it.
+struct Geom {
+    int nx, ny;
+    float k2max;        // (2/3 * min(nx/2ax, ny/2by))^2, float
+    float inv_n;        // 1/(nx*ny)
+    float sigma_f;      // sigma(keV)/1000, rad/(V*Angstrom)
+    float scalex_f;     // ax/nx as float (pixel pitch used by the splat)
+    float scaley_f;
+    float rminsq;       // (rmin)^2, rmin = 1/4 sqrt((dx^2+dy^2)/2)
+    int idx, idy;       // splat window half widths int(n*3/a)+1
+    const float *kx2;   // [nx] kx^2 (freqn, float)
+    const float *ky2;   // [ny]
+    const float2 *propx;  // [nx] (cos t, -sin t), t = pi dz (kx^2 lambda - kx 2 tan(tilt_x))
+    const float2 *propy;  // [ny]
+    const float2 *tw_row;  // twiddles for line length ny
+    const float2 *tw_col;  // twiddles for line length nx
+    const float *knots;    // [100] spline knots in r^2
+    const float4 *coef;    // [nz][100] spline {y, b, c, d} per compact atomic number
+};
+
+// Atoms of one (unit, slice) for the splat: x and y relative to the pixel
+// that contains them, computed on the host in double.
+//   geom = {fx = x - ixo*scalex, fy = y - iyo*scaley, occ, bits(meta)}
+//   meta = ixo | iyo << 13 | zidx << 26
+struct SplatAtom {
+    float fx, fy, occ;
+    uint32_t meta;
+};
+static_assert(sizeof(SplatAtom) == 16, "SplatAtom layout");
+
+constexpr int kMetaBits = 13;
+constexpr uint32_t kMetaMask = (1u << kMetaBits) - 1u;
+constexpr int kMaxZidx = 64;
+
+// Free-space step to one detector plane (this build's FresnelA definition):
+// chi = a1 k^2 + a3 k^4 + a5 k^6 + a2c (kx^2 - ky^2) + a2s 2 kx ky,
+// multiplier exp(-i chi) where k^2 < k2maxo (k2maxo == 0: everywhere).
+struct Fresnel {
+    double a1, a3, a5, a2c, a2s;
+    float k2maxo;
+    const float *kx;  // [nx]
+    const float *ky;  // [ny]
+};
+
+}  // namespace msk
