@@ -118,6 +118,25 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
                     const double *defocus, int nconfig, const float *displacements,
                     float *images, float *exitwaves, int *kept);
 
+/* Use the caller's CUDA stream (a cudaStream_t) for this context's work
+ * instead of the context's own; NULL restores the context's stream. */
+int msk_set_stream(msk_context *ctx, void *stream);
+
+/* Per-kernel accounting: with profiling on, every launch is bracketed by CUDA
+ * events on the context's stream and its algorithmic HBM bytes are counted
+ * (the bytes a launch must move at minimum: a complex64 grid read or written
+ * is 8 bytes per pixel).  msk_profile(ctx, 1) clears the counters and starts;
+ * msk_profile(ctx, 0) stops.  msk_profile_read fills up to max entries and
+ * returns how many kernel kinds have counts. */
+typedef struct {
+    char name[32];
+    long long launches;
+    double ms;      /* summed event time */
+    double bytes;   /* summed algorithmic bytes */
+} msk_kernel_stat;
+int msk_profile(msk_context *ctx, int enable);
+int msk_profile_read(msk_context *ctx, msk_kernel_stat *out, int max);
+
 /* Number of slice-steps calculate() runs for a box of depth ctblengthz
  * (autoslic.cpp:747-830: zslice = dz, dz + dz, ... while < ctblengthz + dz). */
 int msk_slice_count(float deltaz, float ctblengthz);

@@ -605,6 +605,15 @@ int mo_calculate_f32(float *pix, const float *wave0, const float *param, int nat
                      const float *occ, float ctblength, float ctblengthz, int nmode,
                      int max_slices)
 {
+    return mo_calculate_sample_f32(pix, wave0, param, natom, Znum, x, y, z, occ, ctblength,
+                                   ctblengthz, nmode, 0, max_slices);
+}
+
+int mo_calculate_sample_f32(float *pix, const float *wave0, const float *param, int natom,
+                            const int *Znum, const float *x, const float *y, const float *z,
+                            const float *occ, float ctblength, float ctblengthz, int nmode,
+                            int min_slice, int max_slices)
+{
     calc_setup s;
     int st = calc_setup_init(&s, param, natom, Znum, x, y, z, ctblength, ctblengthz);
     if (st) { setup_free(&s); return st; }
@@ -639,6 +648,12 @@ int mo_calculate_f32(float *pix, const float *wave0, const float *param, int nat
             for (int i = istart; i < natom; i++)
                 if (z2[i] < zslice) na++;
                 else break;
+            if (islice <= min_slice) {  /* skipped (timing samples only) */
+                zslice += s.deltaz;
+                istart += na;
+                islice++;
+                continue;
+            }
             if (na > 0) {
                 trlayer_f32(&x2[istart], &y2[istart], &occ2[istart], &Z2[istart], na, s.ax, s.by,
                             s.v0, trans, nx, ny, s.kx2, s.ky2, s.k2max);
@@ -893,8 +908,8 @@ int mo_orientation_f32(const mo_series_params *sp, int natom, const int *Znum,
     float *wave0 = (float *)malloc(sizeof(float) * 2 * n);
     float *pix = (float *)malloc(sizeof(float) * 2 * n);
     for (size_t j = 0; j < n; j++) { wave0[2 * j] = 1.0f; wave0[2 * j + 1] = 0.0f; }
-    int st = mo_calculate_f32(pix, wave0, param, kept, Zo, xo, yo, zo, oo, sp->ax, sp->ctblengthz,
-                              sp->nmode, sp->max_slices);
+    int st = mo_calculate_sample_f32(pix, wave0, param, kept, Zo, xo, yo, zo, oo, sp->ax,
+                                     sp->ctblengthz, sp->nmode, sp->min_slice, sp->max_slices);
     if (st == MO_OK) {
         float wavlen = (float)mo_wavelength(sp->v0);
         float k2maxo = sp->aobj / wavlen;

@@ -76,6 +76,13 @@ int mo_calculate_f32(float *pix, const float *wave0, const float *param, int nat
                      const int *Znum, const float *x, const float *y, const float *z,
                      const float *occ, float ctblength, float ctblengthz, int nmode,
                      int max_slices);
+/* The same loop over slices [min_slice, max_slices) only -- earlier slices'
+ * atoms are skipped and no transforms run for them.  For timing samples:
+ * the wave it returns is not the physical one. */
+int mo_calculate_sample_f32(float *pix, const float *wave0, const float *param, int natom,
+                            const int *Znum, const float *x, const float *y, const float *z,
+                            const float *occ, float ctblength, float ctblengthz, int nmode,
+                            int min_slice, int max_slices);
 int mo_calculate_f64(double *pix, const double *wave0, const float *param, int natom,
                      const int *Znum, const float *x, const float *y, const float *z,
                      const float *occ, float ctblength, float ctblengthz, int nmode,
@@ -117,6 +124,7 @@ typedef struct {
     double dxc, dyc, dzc;  /* rotation centre shifts, Angstrom */
     int nmode;
     int max_slices;     /* < 0: all */
+    int min_slice;      /* slices before it are skipped (cost samples only) */
 } mo_series_params;
 
 int mo_orientation_f32(const mo_series_params *sp, int natom, const int *Znum,

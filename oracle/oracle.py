@@ -44,7 +44,7 @@ class SeriesParams(C.Structure):
                 ("v0", C.c_float), ("deltaz", C.c_float), ("aobj", C.c_float),
                 ("cs3", C.c_double), ("cs5", C.c_double), ("dxc", C.c_double),
                 ("dyc", C.c_double), ("dzc", C.c_double), ("nmode", C.c_int),
-                ("max_slices", C.c_int)]
+                ("max_slices", C.c_int), ("min_slice", C.c_int)]
 
 
 def make_param(ax, by, nx, ny, v0, deltaz, ctiltx=0.0, ctilty=0.0, aobj=0.0):

@@ -25,7 +25,8 @@ NPARAM = 200
 
 EXPORTS = ("msk_create", "msk_destroy", "msk_last_error", "msk_status_string", "msk_calculate",
            "msk_tilt_series", "msk_slice_count", "msk_slice_assign", "msk_sort_by_z",
-           "msk_rotate", "msk_potential_table")
+           "msk_rotate", "msk_potential_table", "msk_set_stream", "msk_profile",
+           "msk_profile_read")
 
 
 class MskError(RuntimeError):
@@ -42,6 +43,12 @@ class Series(C.Structure):
                 ("astig", C.c_double), ("astig_angle", C.c_double), ("dxc", C.c_double),
                 ("dyc", C.c_double), ("dzc", C.c_double), ("nmode", C.c_int),
                 ("max_batch", C.c_int)]
+
+
+class KernelStat(C.Structure):
+    """msk_kernel_stat (include/msk.h)."""
+    _fields_ = [("name", C.c_char * 32), ("launches", C.c_longlong), ("ms", C.c_double),
+                ("bytes", C.c_double)]
 
 
 _lib = None
@@ -83,6 +90,9 @@ def load():
                              C.c_double, C.c_int, _fp, _fp, _fp]
     L.msk_rotate.restype = None
     L.msk_potential_table.argtypes = [C.c_int, _dp, _dp]
+    L.msk_set_stream.argtypes = [vp, vp]
+    L.msk_profile.argtypes = [vp, C.c_int]
+    L.msk_profile_read.argtypes = [vp, C.POINTER(KernelStat), C.c_int]
     _lib = L
     return L
 
@@ -168,6 +178,22 @@ class Context:
         if st:
             msg = self.L.msk_last_error(self.h).decode() or self.L.msk_status_string(st).decode()
             raise MskError(st, msg)
+
+    def set_stream(self, stream_handle):
+        """Run on the caller's CUDA stream (an int cudaStream_t; 0/None: own stream)."""
+        self._check(self.L.msk_set_stream(self.h, stream_handle or None))
+
+    def profile(self, enable):
+        self._check(self.L.msk_profile(self.h, 1 if enable else 0))
+
+    def profile_read(self):
+        """{kernel: (launches, total ms, algorithmic bytes)} since profile(True)."""
+        buf = (KernelStat * 16)()
+        n = self.L.msk_profile_read(self.h, buf, 16)
+        if n < 0:
+            self._check(n)
+        return {buf[i].name.decode(): (int(buf[i].launches), float(buf[i].ms),
+                                       float(buf[i].bytes)) for i in range(min(n, 16))}
 
     def calculate(self, param, Znum, x, y, z, occ, ctblength, ctblengthz, nmode=0, wave0=None,
                   wobble=None, lwobble=0):

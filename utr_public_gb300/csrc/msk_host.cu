@@ -568,9 +568,27 @@ struct DevBuf {
 
 }  // namespace
 
+// Kinds of launches for the per-kernel accounting (msk_profile).
+enum Kind { kSplat, kKColMask, kTransmit, kKColProp, kFresnel, kIntensity, kExit, kInit, kPlane, kKinds };
+static const char *const kKindName[kKinds] = {"row_splat",     "col_bandlimit", "row_transmit",
+                                              "col_propagate", "col_fresnel",   "row_intensity",
+                                              "row_exit",      "row_init",      "plane_init"};
+
+struct ProfRec {
+    int kind;
+    cudaEvent_t a, b;
+    double bytes;
+};
+
 struct msk_context {
     int device = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;      // the stream work goes to
+    cudaStream_t own_stream = nullptr;  // created with the context
+    bool prof_on = false;
+    std::vector<ProfRec> prof_pending;
+    std::vector<cudaEvent_t> prof_pool;
+    long long prof_launches[kKinds] = {};
+    double prof_ms[kKinds] = {}, prof_bytes[kKinds] = {};
     std::string err;
     DevBuf psi, tbuf, atoms, slice_off, act, tables, imgmeta, wave0, images, exitw;
     std::vector<int> zmap = std::vector<int>(104, -1);
@@ -593,6 +611,56 @@ int fail(msk_context *ctx, int code, const std::string &msg)
     } while (0)
 
 bool pow2_supported(int n) { return size_ops(n) != nullptr; }
+
+// Brackets one launch with events when profiling is on.
+struct Prof {
+    msk_context *ctx;
+    int kind;
+    double bytes;
+    cudaEvent_t a = nullptr;
+    static cudaEvent_t get(msk_context *c)
+    {
+        if (!c->prof_pool.empty()) {
+            cudaEvent_t e = c->prof_pool.back();
+            c->prof_pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e = nullptr;
+        cudaEventCreate(&e);
+        return e;
+    }
+    Prof(msk_context *c, int k, double b) : ctx(c), kind(k), bytes(b)
+    {
+        if (ctx->prof_on) {
+            a = get(ctx);
+            cudaEventRecord(a, ctx->stream);
+        }
+    }
+    ~Prof()
+    {
+        if (a) {
+            cudaEvent_t b = get(ctx);
+            cudaEventRecord(b, ctx->stream);
+            ctx->prof_pending.push_back({kind, a, b, bytes});
+        }
+    }
+};
+
+// After a stream synchronisation: fold the recorded events into the totals.
+void prof_collect(msk_context *ctx)
+{
+    for (const ProfRec &r : ctx->prof_pending) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+            ctx->prof_ms[r.kind] += ms;
+            ctx->prof_launches[r.kind] += 1;
+            ctx->prof_bytes[r.kind] += r.bytes;
+        }
+        ctx->prof_pool.push_back(r.a);
+        ctx->prof_pool.push_back(r.b);
+    }
+    ctx->prof_pending.clear();
+}
 
 // Compact atomic-number map and device tables (frequency grids, propagator,
 // twiddles, potential spline) for one grid.
@@ -743,16 +811,29 @@ int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode)
     float2 *psi = ctx->psi.as<float2>(), *tb = ctx->tbuf.as<float2>();
     const int *act = ctx->act.as<int>();
     const int nsl1 = b.nslices + 1;
+    const double plane = (double)gp.nx * gp.ny;
     for (int sl = 0; sl < b.nslices; sl++) {
         const int na = b.act_off[sl + 1] - b.act_off[sl];
         const int *units = act + b.act_off[sl];
         if (na > 0) {
-            rop->splat(g, units, na, sl, nsl1, ctx->slice_off.as<int>(),
-                       ctx->atoms.as<SplatAtom>(), tb, s);
-            cop->col_mask(g, units, na, tb, tb, s);
-            rop->row_transmit(g, units, na, tb, psi, 1.0f / ((float)gp.ny * (float)gp.ny), s);
+            {
+                Prof p(ctx, kSplat, 8.0 * plane * na);
+                rop->splat(g, units, na, sl, nsl1, ctx->slice_off.as<int>(),
+                           ctx->atoms.as<SplatAtom>(), tb, s);
+            }
+            {
+                Prof p(ctx, kKColMask, 16.0 * plane * na);
+                cop->col_mask(g, units, na, tb, tb, s);
+            }
+            {
+                Prof p(ctx, kTransmit, 24.0 * plane * na);
+                rop->row_transmit(g, units, na, tb, psi, 1.0f / ((float)gp.ny * (float)gp.ny), s);
+            }
         }
-        if (nmode == 0) cop->col_prop(g, nullptr, b.nunits, psi, psi, s);
+        if (nmode == 0) {
+            Prof p(ctx, kKColProp, 16.0 * plane * b.nunits);
+            cop->col_prop(g, nullptr, b.nunits, psi, psi, s);
+        }
     }
     MSK_CUDA(ctx, cudaGetLastError());
     return MSK_OK;
@@ -772,7 +853,8 @@ int msk_create(int device, msk_context **out)
     if (!ctx) return MSK_ENOMEM;
     ctx->device = device;
     cudaError_t e = cudaSetDevice(device);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+    ctx->stream = ctx->own_stream;
     if (e != cudaSuccess) {
         delete ctx;
         return MSK_ECUDA;
@@ -786,10 +868,12 @@ void msk_destroy(msk_context *ctx)
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    prof_collect(ctx);
+    for (cudaEvent_t e : ctx->prof_pool) cudaEventDestroy(e);
     for (DevBuf *b : {&ctx->psi, &ctx->tbuf, &ctx->atoms, &ctx->slice_off, &ctx->act, &ctx->tables,
                       &ctx->imgmeta, &ctx->wave0, &ctx->images, &ctx->exitw})
         b->release();
-    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }
 
@@ -809,6 +893,48 @@ const char *msk_status_string(int st)
     case MSK_EINVAL: return "invalid argument";
     default: return "unknown status";
     }
+}
+
+int msk_set_stream(msk_context *ctx, void *stream)
+{
+    if (!ctx) return MSK_EINVAL;
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return MSK_OK;
+}
+
+int msk_profile(msk_context *ctx, int enable)
+{
+    if (!ctx) return MSK_EINVAL;
+    if (enable) {
+        cudaStreamSynchronize(ctx->stream);
+        prof_collect(ctx);
+        for (int k = 0; k < kKinds; k++) {
+            ctx->prof_launches[k] = 0;
+            ctx->prof_ms[k] = 0.0;
+            ctx->prof_bytes[k] = 0.0;
+        }
+    }
+    ctx->prof_on = enable != 0;
+    return MSK_OK;
+}
+
+int msk_profile_read(msk_context *ctx, msk_kernel_stat *out, int max)
+{
+    if (!ctx || (max > 0 && !out)) return MSK_EINVAL;
+    cudaStreamSynchronize(ctx->stream);
+    prof_collect(ctx);
+    int n = 0;
+    for (int k = 0; k < kKinds; k++) {
+        if (!ctx->prof_launches[k]) continue;
+        if (n < max) {
+            std::snprintf(out[n].name, sizeof out[n].name, "%s", kKindName[k]);
+            out[n].launches = ctx->prof_launches[k];
+            out[n].ms = ctx->prof_ms[k];
+            out[n].bytes = ctx->prof_bytes[k];
+        }
+        n++;
+    }
+    return n;
 }
 
 int msk_slice_count(float deltaz, float ctblengthz) { return slice_count(deltaz, ctblengthz); }
@@ -931,15 +1057,22 @@ int msk_calculate(msk_context *ctx, float *pix, const float *wave0, const float 
     MSK_CUDA(ctx, cudaMemcpyAsync(ctx->wave0.p, wave0, plane * sizeof(float2),
                                   cudaMemcpyHostToDevice, ctx->stream));
     const SizeOps *rop = size_ops(ny);
-    rop->row_init(gp.g, nullptr, 1, ctx->wave0.as<float2>(), ctx->psi.as<float2>(), 1.0f,
-                  ctx->stream);
+    {
+        Prof p(ctx, kInit, 16.0 * plane);
+        rop->row_init(gp.g, nullptr, 1, ctx->wave0.as<float2>(), ctx->psi.as<float2>(), 1.0f,
+                      ctx->stream);
+    }
     st = run_slices(ctx, gp, b, nmode);
     if (st) return st;
-    rop->row_exit(gp.g, nullptr, 1, ctx->psi.as<float2>(), ctx->tbuf.as<float2>(), ctx->stream);
+    {
+        Prof p(ctx, kExit, 16.0 * plane);
+        rop->row_exit(gp.g, nullptr, 1, ctx->psi.as<float2>(), ctx->tbuf.as<float2>(), ctx->stream);
+    }
     MSK_CUDA(ctx, cudaGetLastError());
     MSK_CUDA(ctx, cudaMemcpyAsync(pix, ctx->tbuf.p, plane * sizeof(float2),
                                   cudaMemcpyDeviceToHost, ctx->stream));
     MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    prof_collect(ctx);
     return MSK_OK;
 }
 
@@ -1017,11 +1150,17 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
         st = upload_batch(ctx, ua, u0, nb, nslices, b);
         if (st) return st;
         float2 *psi = ctx->psi.as<float2>(), *tb = ctx->tbuf.as<float2>();
-        k_plane_init<<<1024, 256, 0, ctx->stream>>>(psi, nullptr, nb, nx, ny);
+        {
+            Prof p(ctx, kPlane, 8.0 * plane * nb);
+            k_plane_init<<<1024, 256, 0, ctx->stream>>>(psi, nullptr, nb, nx, ny);
+        }
         st = run_slices(ctx, gp, b, s->nmode);
         if (st) return st;
         if (exitwaves) {
-            rop->row_exit(gp.g, nullptr, nb, psi, tb, ctx->stream);
+            {
+                Prof p(ctx, kExit, 16.0 * plane * nb);
+                rop->row_exit(gp.g, nullptr, nb, psi, tb, ctx->stream);
+            }
             MSK_CUDA(ctx, cudaMemcpyAsync(exitwaves + (size_t)u0 * plane * 2, tb,
                                           (size_t)nb * plane * sizeof(float2),
                                           ew_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
@@ -1057,8 +1196,11 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
                 fr.kx = tables_kx(ctx, gp);
                 fr.ky = tables_ky(ctx, gp);
                 // psi_d = iS(iF(exp(-i chi) F(W)))/N
-                cop->col_fresnel(gp.g, nullptr, nb, psi, tb, fr, 1.0f / ((float)nx * (float)ny),
-                                 ctx->stream);
+                {
+                    Prof p(ctx, kFresnel, 16.0 * plane * nb);
+                    cop->col_fresnel(gp.g, nullptr, nb, psi, tb, fr,
+                                     1.0f / ((float)nx * (float)ny), ctx->stream);
+                }
                 meta.clear();
                 meta.insert(meta.end(), off.begin(), off.end());
                 meta.insert(meta.end(), units.begin(), units.end());
@@ -1069,12 +1211,14 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
                                               cudaMemcpyHostToDevice, ctx->stream));
                 const int *d_off = dm, *d_units = dm + off.size(),
                           *d_dst = d_units + units.size(), *d_flags = d_dst + nimg;
+                Prof p(ctx, kIntensity, 8.0 * plane * units.size() + 4.0 * plane * nimg);
                 rop->row_intensity(gp.g, nimg, d_off, d_units, d_dst, d_flags, tb, d_images,
                                    (float)nconfig, ctx->stream);
             }
         }
         MSK_CUDA(ctx, cudaGetLastError());
         MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        prof_collect(ctx);
     }
     if (ndefocus > 0 && !img_dev)
         MSK_CUDA(ctx, cudaMemcpyAsync(images, d_images, img_bytes, cudaMemcpyDeviceToHost,
