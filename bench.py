@@ -1,0 +1,365 @@
+#!/usr/bin/env python3
+"""Benchmark of the batched multislice tilt series on GB300.
+
+Workload (one "step"): the MsctKirkland tilt series on a synthetic specimen
+-- 20000 atoms (C:N:O:S = 0.50:0.17:0.30:0.03, seeded) uniform in a
+120^3 A cube centred in a 160 A box, 300 keV, 1024 x 1024 complex64 grid,
+1 A slices (160 slice-steps per orientation), 180 rotations about y in 1
+degree steps, two detector defoci (0 and 500 A), fp32 intensities.  The
+metric is slice-steps/s = orientations x slices / wall time of the whole
+step (host preparation, every pass, the free-space step and the intensity).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl ours (default) prints one JSON line with
+  value        device-timed (CUDA events on the library's stream) with the
+               specimen resident in host memory and images left in HBM
+  e2e          the same call with host input and output buffers (pinned),
+               host<->device copies inside the timed region
+  roofline     the dominant kernel's algorithmic HBM bytes per launch over its
+               event-timed duration, against MEASURED_PEAKS.json
+  cpu_baseline the oracle's FP32 restatement of the reference on the host
+               cores (a bounded sample of the same workload)
+--impl reference times that CPU restatement alone (the reference's own code
+cannot be built on the GPU host: its FFT library and XArrayLibrary are not
+part of it).
+Under torchrun every rank runs its own 180 orientations (weak scaling; the
+orientations are independent, there is no collective on the data path).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "tilt-series slice-steps/s (1024², FP32) batched vs per-angle GPU; err vs FP64"
+UNIT = "slice-steps/s"
+NX = 1024
+FOV = 160.0
+V0 = 300.0
+DZ = 1.0
+NANG = 180
+DEFOCI = (0.0, 500.0)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index),
+                                       "--query-gpu=" + self.FIELDS,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def gpu_index(local_rank):
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+    ids = [v for v in vis.split(",") if v.strip()]
+    if ids and all(v.strip().isdigit() for v in ids):
+        return int(ids[local_rank % len(ids)])
+    return local_rank
+
+
+def workload(rank, nang=NANG):
+    from utr_public_gb300 import specimen
+    spec = specimen.tilt_specimen(1002)
+    angY = np.deg2rad(np.arange(nang, dtype=np.float64) * (NANG / nang))
+    angZ = np.full(nang, 0.1 * rank)  # each rank its own orientations
+    return spec, angZ, angY, np.array(DEFOCI)
+
+
+def cpu_sample(threads, slices=(60, 70), spec=None):
+    """The oracle's FP32 restatement of the reference on `threads` host
+    threads, one orientation per thread (as MsctKirkland drives the
+    reference), slices slices[0]+1..slices[1] of each orientation."""
+    from oracle import oracle as orc
+    O = orc.Oracle()
+    if spec is None:
+        spec, _, _, _ = workload(0)
+    sp = orc.SeriesParams()
+    sp.ax, sp.ctblengthz, sp.nx, sp.ny, sp.v0, sp.deltaz = FOV, FOV, NX, NX, V0, DZ
+    sp.min_slice, sp.max_slices, sp.nmode = slices[0], slices[1], 0
+    angY = np.deg2rad(np.linspace(0, 179, threads))
+    angZ = np.zeros(threads)
+    t0 = time.perf_counter()
+    O.orientations_f32(sp, spec.Znum, spec.x, spec.y, spec.z, spec.occ, angZ, angY,
+                       np.array([]), threads)
+    dt = time.perf_counter() - t0
+    steps = threads * (slices[1] - slices[0])
+    return steps / dt, dt, steps
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_sample(threads, (60, 62))
+    vals, total = [], 0.0
+    for _ in range(args.steps):
+        v, dt, _ = cpu_sample(threads, (60, 64))
+        vals.append(v)
+        total += dt
+    v = float(np.median(vals))
+    sample = ("%d orientations x slices 61-64 of the 180-orientation 1024^2 tilt series, one "
+              "orientation per thread" % threads)
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "tilt series 1024^2, 160 A box, 20000 atoms, 300 keV, 1 A slices, "
+                               "180 orientations x 2 defoci", "sample": sample},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def fp64_error_job(result):
+    """Relative L2 error of one orientation (45 degrees) of the workload vs the
+    FP64 oracle -- runs on a host thread while the GPU is timed."""
+    try:
+        from oracle import oracle as orc
+        import utr_public_gb300 as msk
+        spec, _, _, defoci = workload(0)
+        O = orc.Oracle()
+        sp = orc.SeriesParams()
+        sp.ax, sp.ctblengthz, sp.nx, sp.ny, sp.v0, sp.deltaz = FOV, FOV, NX, NX, V0, DZ
+        sp.max_slices, sp.min_slice = -1, 0
+        t0 = time.perf_counter()
+        ref_img, ref_ew, _ = O.orientation(sp, spec.Znum, spec.x, spec.y, spec.z, spec.occ,
+                                           0.0, np.deg2rad(45.0), defoci, fp64=True,
+                                           want_exit=True)
+        result["oracle_s"] = time.perf_counter() - t0
+        result["ref"] = (ref_img, ref_ew)
+    except Exception as e:  # reported, not fatal
+        result["error"] = repr(e)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-check", action="store_true")
+    ap.add_argument("--orientations", type=int, default=NANG,
+                    help="orientations per step (180 for the headline workload)")
+    ap.add_argument("--profile-run", action="store_true",
+                    help="one tilt series and its per-kernel table, for profilers")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    import utr_public_gb300 as msk
+    msk.load()  # raises if the CUDA library is not built
+
+    ctx = msk.Context(local_rank)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    nang = args.orientations
+    spec, angZ, angY, defoci = workload(rank, nang)
+    s = msk.Series()
+    s.nx = s.ny = NX
+    s.ctblength = s.ctblengthz = FOV
+    s.v0, s.deltaz = V0, DZ
+    nslices = msk.slice_count(DZ, FOV)
+    steps_per = nang * nslices
+    atoms = (spec.Znum, spec.x, spec.y, spec.z, spec.occ)
+    images = torch.empty((nang, len(defoci), NX, NX), dtype=torch.float32, device="cuda")
+
+    def step(img):
+        ctx.tilt_series(s, *atoms, angZ, angY, defoci, images=img)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def timed(img, k):
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            step(img)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ms = e0.elapsed_time(e1) / k
+        if dist is not None:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    if args.profile_run:
+        ctx.profile(True)
+        step(images)
+        torch.cuda.synchronize()
+        for k, v in sorted(ctx.profile_read().items(), key=lambda kv: -kv[1][1]):
+            print("%-14s launches %6d  ms %9.3f  GB/s %8.1f" % (k, v[0], v[1],
+                  v[2] / (v[1] / 1e3) / 1e9 if v[1] > 0 else 0.0))
+        return
+
+    for _ in range(args.warmup):
+        step(images)
+    torch.cuda.synchronize()
+
+    clocks = Clocks(gpu_index(local_rank))
+    ctx.profile(True)
+    ms = timed(images, args.steps)
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    clk = clocks.stop()
+    value = world * steps_per / (ms / 1000.0)
+
+    # end to end: host buffers (pinned), copies inside the timed region
+    host_images = torch.empty((nang, len(defoci), NX, NX), dtype=torch.float32, pin_memory=True)
+    step(host_images)
+    ctx.profile(True)
+    ms_e2e = timed(host_images, max(1, min(args.steps, 3)))
+    prof_e2e = ctx.profile_read()
+    ctx.profile(False)
+    k_e2e = max(1, min(args.steps, 3))
+    h2d = prof_e2e.get("copy_h2d", (0, 0.0, 0.0))[2] / k_e2e
+    d2h = prof_e2e.get("copy_d2h", (0, 0.0, 0.0))[2] / k_e2e
+    e2e_value = world * steps_per / (ms_e2e / 1000.0)
+    if rank == 0:
+        same = torch.equal(host_images, images.cpu())
+
+    kernels = {k: v for k, v in prof.items() if not k.startswith("copy_")}
+    launches = int(sum(v[0] for v in kernels.values()))
+    dom = max(kernels, key=lambda k: kernels[k][1])
+    n_l, t_ms, nbytes = kernels[dom]
+    peak, peak_kind = peaks()
+    achieved = (nbytes / n_l) / (t_ms / n_l / 1000.0) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    if os.path.exists(tf):
+        d = json.load(open(tf)).get(dom)
+        if d:
+            traffic = (nbytes / n_l) * d["dram_bytes"] / d["algorithmic_bytes"]
+
+    if rank != 0:
+        return
+    fp64 = {}
+    if not args.no_fp64_check:
+        fp64_error_job(fp64)
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, dt, n = cpu_sample(threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "%d orientations x slices 61-70 (%d slice-steps, %.1f s) of this "
+                         "workload, one orientation per thread" % (threads, n, dt)}
+    err = None
+    if not args.no_fp64_check:
+        if "ref" in fp64:
+            ref_img, ref_ew = fp64["ref"]
+            sub = msk.Series()
+            for f, _ in msk.Series._fields_:
+                setattr(sub, f, getattr(s, f))
+            img1, ew1, _ = ctx.tilt_series(sub, *atoms, [0.0], [np.deg2rad(45.0)], defoci,
+                                           want_exit=True)
+            rl2 = lambda a, b: float(np.linalg.norm(a.astype(np.float64) - b) / np.linalg.norm(b))
+            err = {"orientation_deg": 45.0, "exit_wave_rel_l2": rl2(ew1[0, 0], ref_ew),
+                   "image_rel_l2": [rl2(img1[0, d], ref_img[d]) for d in range(len(defoci))],
+                   "oracle_seconds": fp64.get("oracle_s")}
+        else:
+            err = {"error": fp64.get("error", "not run")}
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "tilt series 1024^2, 160 A box, 20000 atoms in a 120^3 A cube, "
+                               "300 keV, 1 A slices, 180 orientations (1 deg about y) x 2 "
+                               "defoci (0, 500 A); seeded synthetic specimen",
+                   "orientations": nang,
+                   "slice_steps_per_step": steps_per * world, "images_per_step": nang * 2 * world,
+                   "l2": "inputs larger than L2 (wave and transmission buffers 2.9 GB per GPU)",
+                   "parallelism": "weak: one tilt series per GPU"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": ms_e2e,
+                "matches_device_output": bool(same)},
+        "gpu_launches": launches * world,
+        "kernels": {k: {"launches": v[0], "ms": round(v[1], 3),
+                        "GBps": round(v[2] / (v[1] / 1000.0) / 1e9, 1) if v[1] > 0 else None}
+                    for k, v in kernels.items()},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "peak_source": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": nbytes / n_l},
+        "clocks": clk,
+        "cpu_baseline": cpu,
+        "err_vs_fp64": err,
+    }
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -127,7 +127,8 @@ int msk_set_stream(msk_context *ctx, void *stream);
  * (the bytes a launch must move at minimum: a complex64 grid read or written
  * is 8 bytes per pixel).  msk_profile(ctx, 1) clears the counters and starts;
  * msk_profile(ctx, 0) stops.  msk_profile_read fills up to max entries and
- * returns how many kernel kinds have counts. */
+ * returns how many kinds have counts; host<->device copies made by the
+ * library appear as "copy_h2d" / "copy_d2h" (launches = copies, ms = 0). */
 typedef struct {
     char name[32];
     long long launches;

@@ -589,6 +589,8 @@ struct msk_context {
     std::vector<cudaEvent_t> prof_pool;
     long long prof_launches[kKinds] = {};
     double prof_ms[kKinds] = {}, prof_bytes[kKinds] = {};
+    long long copies[2] = {};      // host-to-device, device-to-host copies while profiling
+    double copy_bytes[2] = {};
     std::string err;
     DevBuf psi, tbuf, atoms, slice_off, act, tables, imgmeta, wave0, images, exitw;
     std::vector<int> zmap = std::vector<int>(104, -1);
@@ -645,6 +647,14 @@ struct Prof {
         }
     }
 };
+
+// Host<->device copy accounting (dir 0: to the device, 1: to the host).
+void count_copy(msk_context *ctx, int dir, double bytes)
+{
+    if (!ctx->prof_on) return;
+    ctx->copies[dir] += 1;
+    ctx->copy_bytes[dir] += bytes;
+}
 
 // After a stream synchronisation: fold the recorded events into the totals.
 void prof_collect(msk_context *ctx)
@@ -706,6 +716,7 @@ int upload_tables(msk_context *ctx, GridPre &gp, const std::vector<int> &zlist)
     MSK_CUDA(ctx, ctx->tables.reserve(off));
     MSK_CUDA(ctx, cudaMemcpyAsync(ctx->tables.p, host.data(), off, cudaMemcpyHostToDevice,
                                   ctx->stream));
+    count_copy(ctx, 0, (double)off);
     // the host staging vector must outlive the copy
     MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     unsigned char *b = ctx->tables.as<unsigned char>();
@@ -791,6 +802,8 @@ int upload_batch(msk_context *ctx, const std::vector<UnitAtoms> &ua, int u0, int
     MSK_CUDA(ctx, ctx->act.reserve(std::max<size_t>(b.act.size(), 1) * sizeof(int)));
     MSK_CUDA(ctx, cudaMemcpyAsync(ctx->atoms.p, atoms.data(), atoms.size() * sizeof(SplatAtom),
                                   cudaMemcpyHostToDevice, ctx->stream));
+    count_copy(ctx, 0, (double)(atoms.size() * sizeof(SplatAtom) + b.slice_off.size() * sizeof(int) +
+                                b.act.size() * sizeof(int)));
     MSK_CUDA(ctx, cudaMemcpyAsync(ctx->slice_off.p, b.slice_off.data(),
                                   b.slice_off.size() * sizeof(int), cudaMemcpyHostToDevice,
                                   ctx->stream));
@@ -913,6 +926,8 @@ int msk_profile(msk_context *ctx, int enable)
             ctx->prof_ms[k] = 0.0;
             ctx->prof_bytes[k] = 0.0;
         }
+        ctx->copies[0] = ctx->copies[1] = 0;
+        ctx->copy_bytes[0] = ctx->copy_bytes[1] = 0.0;
     }
     ctx->prof_on = enable != 0;
     return MSK_OK;
@@ -931,6 +946,16 @@ int msk_profile_read(msk_context *ctx, msk_kernel_stat *out, int max)
             out[n].launches = ctx->prof_launches[k];
             out[n].ms = ctx->prof_ms[k];
             out[n].bytes = ctx->prof_bytes[k];
+        }
+        n++;
+    }
+    for (int d = 0; d < 2; d++) {
+        if (!ctx->copies[d]) continue;
+        if (n < max) {
+            std::snprintf(out[n].name, sizeof out[n].name, "%s", d ? "copy_d2h" : "copy_h2d");
+            out[n].launches = ctx->copies[d];
+            out[n].ms = 0.0;
+            out[n].bytes = ctx->copy_bytes[d];
         }
         n++;
     }
@@ -1056,6 +1081,7 @@ int msk_calculate(msk_context *ctx, float *pix, const float *wave0, const float 
     MSK_CUDA(ctx, ctx->wave0.reserve(plane * sizeof(float2)));
     MSK_CUDA(ctx, cudaMemcpyAsync(ctx->wave0.p, wave0, plane * sizeof(float2),
                                   cudaMemcpyHostToDevice, ctx->stream));
+    count_copy(ctx, 0, (double)(plane * sizeof(float2)));
     const SizeOps *rop = size_ops(ny);
     {
         Prof p(ctx, kInit, 16.0 * plane);
@@ -1071,6 +1097,7 @@ int msk_calculate(msk_context *ctx, float *pix, const float *wave0, const float 
     MSK_CUDA(ctx, cudaGetLastError());
     MSK_CUDA(ctx, cudaMemcpyAsync(pix, ctx->tbuf.p, plane * sizeof(float2),
                                   cudaMemcpyDeviceToHost, ctx->stream));
+    count_copy(ctx, 1, (double)(plane * sizeof(float2)));
     MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     prof_collect(ctx);
     return MSK_OK;
@@ -1165,6 +1192,7 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
                                           (size_t)nb * plane * sizeof(float2),
                                           ew_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
                                           ctx->stream));
+            if (!ew_dev) count_copy(ctx, 1, (double)nb * plane * sizeof(float2));
         }
         if (ndefocus > 0) {
             // one image per angle in this batch; its configurations in order
@@ -1209,6 +1237,7 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
                 int *dm = ctx->imgmeta.as<int>() + (size_t)d * nmeta;
                 MSK_CUDA(ctx, cudaMemcpyAsync(dm, meta.data(), meta.size() * sizeof(int),
                                               cudaMemcpyHostToDevice, ctx->stream));
+                count_copy(ctx, 0, (double)(meta.size() * sizeof(int)));
                 const int *d_off = dm, *d_units = dm + off.size(),
                           *d_dst = d_units + units.size(), *d_flags = d_dst + nimg;
                 Prof p(ctx, kIntensity, 8.0 * plane * units.size() + 4.0 * plane * nimg);
@@ -1221,8 +1250,11 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
         prof_collect(ctx);
     }
     if (ndefocus > 0 && !img_dev)
+    {
         MSK_CUDA(ctx, cudaMemcpyAsync(images, d_images, img_bytes, cudaMemcpyDeviceToHost,
                                       ctx->stream));
+        count_copy(ctx, 1, (double)img_bytes);
+    }
     MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (kept)
         for (int u = 0; u < nunits; u++) kept[u] = ua[u].kept;
