@@ -59,6 +59,29 @@ __global__ void k_plane_init(float2 *psi, const int *__restrict__ units, int nun
     }
 }
 
+__global__ void k_fresnel_table(const Geom g, const Fresnel fr, float scale, float2 *table)
+{
+    const size_t n = (size_t)g.nx * g.ny;
+    const double twopi = 6.283185307179586;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const int ix = (int)(i / g.ny), iy = (int)(i % g.ny);
+        const float k2f = __fadd_rn(g.kx2[ix], g.ky2[iy]);
+        if (fr.k2maxo > 0.0f && !(k2f < fr.k2maxo)) {
+            table[i] = make_float2(0.0f, 0.0f);
+            continue;
+        }
+        const double kx = (double)fr.kx[ix], ky = (double)fr.ky[iy];
+        const double k2 = kx * kx + ky * ky;
+        double chi = fr.a1 * k2 + fr.a3 * k2 * k2 + fr.a5 * k2 * k2 * k2 +
+                     fr.a2c * (kx * kx - ky * ky) + fr.a2s * (2.0 * kx * ky);
+        chi -= twopi * rint(chi / twopi);
+        float s, c;
+        sincosf((float)chi, &s, &c);
+        table[i] = make_float2(c * scale, -s * scale);
+    }
+}
+
 // ------------------------------------------------------------------ physics
 // Restatements of the reference's slicelib routines used to build tables.
 namespace phys {
@@ -374,6 +397,10 @@ static void grid_pre(GridPre &gp, int nx, int ny, float ax, float by, float v0, 
     g.rminsq = (float)(rmin * rmin);
     g.idx = (int)(nx * 3.0 / ax) + 1;
     g.idy = (int)(ny * 3.0 / by) + 1;
+    // knots r_i^2 = (0.01 exp(i dlnr))^2: i = (log r^2 - 2 log 0.01) / (2 dlnr)
+    const double dlnr = log(5.0 / 0.01) / (phys::kN - 1);
+    g.lut_c0 = (float)(-2.0 * log(0.01));
+    g.lut_c1 = (float)(1.0 / (2.0 * dlnr));
 }
 
 // Stockham stage twiddles for line length n, matching FftPlan<n>.
@@ -569,10 +596,13 @@ struct DevBuf {
 }  // namespace
 
 // Kinds of launches for the per-kernel accounting (msk_profile).
-enum Kind { kSplat, kKColMask, kTransmit, kKColProp, kFresnel, kIntensity, kExit, kInit, kPlane, kKinds };
-static const char *const kKindName[kKinds] = {"row_splat",     "col_bandlimit", "row_transmit",
-                                              "col_propagate", "col_fresnel",   "row_intensity",
-                                              "row_exit",      "row_init",      "plane_init"};
+enum Kind {
+    kSplat, kKColMask, kTransmit, kKColProp, kFresnel, kIntensity, kExit, kInit, kPlane, kFresTab,
+    kKinds
+};
+static const char *const kKindName[kKinds] = {
+    "row_splat", "col_bandlimit", "row_transmit", "col_propagate", "col_fresnel",
+    "row_intensity", "row_exit", "row_init", "plane_init", "fresnel_table"};
 
 struct ProfRec {
     int kind;
@@ -592,7 +622,7 @@ struct msk_context {
     long long copies[2] = {};      // host-to-device, device-to-host copies while profiling
     double copy_bytes[2] = {};
     std::string err;
-    DevBuf psi, tbuf, atoms, slice_off, act, tables, imgmeta, wave0, images, exitw;
+    DevBuf psi, tbuf, atoms, slice_off, act, tables, imgmeta, wave0, images, exitw, fresnel;
     std::vector<int> zmap = std::vector<int>(104, -1);
 };
 
@@ -884,7 +914,7 @@ void msk_destroy(msk_context *ctx)
     prof_collect(ctx);
     for (cudaEvent_t e : ctx->prof_pool) cudaEventDestroy(e);
     for (DevBuf *b : {&ctx->psi, &ctx->tbuf, &ctx->atoms, &ctx->slice_off, &ctx->act, &ctx->tables,
-                      &ctx->imgmeta, &ctx->wave0, &ctx->images, &ctx->exitw})
+                      &ctx->imgmeta, &ctx->wave0, &ctx->images, &ctx->exitw, &ctx->fresnel})
         b->release();
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;

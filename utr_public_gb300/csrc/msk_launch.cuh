@@ -49,6 +49,10 @@ inline void set_smem(K kernel, size_t bytes, std::once_flag &flag)
 {
     std::call_once(flag, [&] {
         cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        // the default carve-out leaves ~100 KB of shared memory per SM, one
+        // CTA of the larger passes; ask for the whole 228 KB
+        cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
     });
 }
 

@@ -51,24 +51,17 @@ template <int NX> struct ColCfg {
 constexpr int kKnots = 100;
 
 // Spline of the projected potential vs r^2 (TemsimLibrary/slicelib.cpp:2402-2425,
-// 2812-2875), evaluated in float: bisection for the interval as seval does.
-__device__ __forceinline__ float spline_vz(const float *knots, const float4 *coef, float rsq)
+// 2812-2875), evaluated in float.  The interval is the one seval's bisection
+// finds (knot[i] <= r^2 < knot[i+1], clamped to [0, 98]); the knots are
+// log-spaced, so a logarithm gives the index to within one and a compare
+// with each neighbour settles it.
+__device__ __forceinline__ float spline_vz(const Geom &g, const float *knots, const float4 *coef,
+                                          float rsq)
 {
-    int i;
-    if (rsq <= knots[0]) {
-        i = 0;
-    } else if (rsq >= knots[kKnots - 2]) {
-        i = kKnots - 2;
-    } else {
-        int lo = 0, hi = kKnots;
-#pragma unroll 1
-        while (hi - lo > 1) {
-            int mid = (lo + hi) >> 1;
-            if (rsq < knots[mid]) hi = mid;
-            else lo = mid;
-        }
-        i = lo;
-    }
+    int i = __float2int_rd((__logf(rsq) + g.lut_c0) * g.lut_c1);
+    i = min(max(i, 0), kKnots - 2);
+    if (i > 0 && rsq < knots[i]) i--;
+    else if (i < kKnots - 2 && rsq >= knots[i + 1]) i++;
     const float4 c = __ldg(&coef[i]);
     const float z = rsq - knots[i];
     return c.x + (c.y + (c.z + c.w * z) * z) * z;
@@ -160,7 +153,7 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
                         float rsq = dx2 + dy * dy;
                         if (rsq <= 9.0f) {
                             rsq = fmaxf(rsq, g.rminsq);
-                            vacc[pmod(iyp, NY)] += sa.occ * spline_vz(s_knots, coef, rsq);
+                            vacc[pmod(iyp, NY)] += sa.occ * spline_vz(g, s_knots, coef, rsq);
                         }
                     }
                 }
@@ -196,7 +189,7 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
 enum { kColMask = 0, kColProp = 1, kColFresnel = 2 };
 
 template <int NX, int MODE>
-__global__ void __launch_bounds__(ColCfg<NX>::NT)
+__global__ void __launch_bounds__(ColCfg<NX>::NT, 2)
 k_col_pass(const Geom g, const int *__restrict__ units, const float2 *in, float2 *out,
            const Fresnel fr, float fscale)
 {
@@ -243,27 +236,9 @@ k_col_pass(const Geom g, const int *__restrict__ units, const float2 *in, float2
             }
         }
     } else {
-        const float ky2 = __ldg(&g.ky2[iy]);
-        const double ky = (double)__ldg(&fr.ky[iy]);
-        const double twopi = 6.283185307179586;
+        const float2 *tab = fr.table + iy;
 #pragma unroll
-        for (int m = 0; m < E; m++) {
-            const int ix = t + m * T;
-            const float k2f = __fadd_rn(__ldg(&g.kx2[ix]), ky2);
-            if (fr.k2maxo > 0.0f && !(k2f < fr.k2maxo)) {
-                v[m] = make_float2(0.0f, 0.0f);
-            } else {
-                const double kx = (double)__ldg(&fr.kx[ix]);
-                const double k2 = kx * kx + ky * ky;
-                double chi = fr.a1 * k2 + fr.a3 * k2 * k2 + fr.a5 * k2 * k2 * k2 +
-                             fr.a2c * (kx * kx - ky * ky) + fr.a2s * (2.0 * kx * ky);
-                chi -= twopi * rint(chi / twopi);
-                float s, cc;
-                sincosf((float)chi, &s, &cc);
-                const float2 w = cmul(v[m], make_float2(cc, -s));
-                v[m] = cscale(w, fscale);
-            }
-        }
+        for (int m = 0; m < E; m++) v[m] = cmul(v[m], __ldg(&tab[(size_t)(t + m * T) * ny]));
     }
     fft_line<NX, true, C, true>(v, s_buf, c, t, s_tw);
     float2 *dst = out + (size_t)u * plane + iy;
@@ -405,7 +380,10 @@ k_row_intensity(const Geom g, const int *__restrict__ img_off, const int *__rest
     }
 }
 
-// Plane incident wave: W0 = S(1) = ny at iy = 0, zero elsewhere, per row.
+// The free-space multiplier of one detector plane, in double, reduced modulo
+// 2 pi before the single-precision sine and cosine: table[ix*ny + iy] =
+// scale * exp(-i chi(kx, ky)) inside the aperture, 0 outside.
+__global__ void k_fresnel_table(const Geom g, const Fresnel fr, float scale, float2 *table);
 __global__ void k_plane_init(float2 *psi, const int *__restrict__ units, int nunits, int nx, int ny);
 
 }  // namespace msk

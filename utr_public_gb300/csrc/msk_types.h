@@ -19,6 +19,7 @@ struct Geom {
     float scaley_f;
     float rminsq;       // (rmin)^2, rmin = 1/4 sqrt((dx^2+dy^2)/2)
     int idx, idy;       // splat window half widths int(n*3/a)+1
+    float lut_c0, lut_c1;  // knot index of r^2 ~ (log(r^2) + lut_c0) * lut_c1
     const float *kx2;   // [nx] kx^2 (freqn, float)
     const float *ky2;   // [ny]
     const float2 *propx;  // [nx] (cos t, -sin t), t = pi dz (kx^2 lambda - kx 2 tan(tilt_x))
@@ -46,11 +47,14 @@ constexpr int kMaxZidx = 64;
 // Free-space step to one detector plane (this build's FresnelA definition):
 // chi = a1 k^2 + a3 k^4 + a5 k^6 + a2c (kx^2 - ky^2) + a2s 2 kx ky,
 // multiplier exp(-i chi) where k^2 < k2maxo (k2maxo == 0: everywhere).
+// k_fresnel_table evaluates it once per plane in double into `table`
+// ([nx][ny] complex64, times a scale); the column pass then reads the table.
 struct Fresnel {
     double a1, a3, a5, a2c, a2s;
     float k2maxo;
     const float *kx;  // [nx]
     const float *ky;  // [ny]
+    const float2 *table;
 };
 
 }  // namespace msk
