@@ -1244,7 +1244,7 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
             MSK_CUDA(ctx, ctx->imgmeta.reserve(nmeta * sizeof(int) * (size_t)ndefocus));
             for (int d = 0; d < ndefocus; d++) {
                 const double rprime = defocus[d] - 0.5 * s->ctblengthz;  // autosliccmd.cpp:1060
-                Fresnel fr;
+                Fresnel fr{};
                 fr.a1 = pi * l * rprime;
                 fr.a3 = (pi / 2.0) * s->cs3 * l * l * l;
                 fr.a5 = (pi / 3.0) * s->cs5 * l * l * l * l * l;
@@ -1253,11 +1253,18 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
                 fr.k2maxo = k2maxo;
                 fr.kx = tables_kx(ctx, gp);
                 fr.ky = tables_ky(ctx, gp);
-                // psi_d = iS(iF(exp(-i chi) F(W)))/N
+                // psi_d = iS(iF(exp(-i chi) F(W)))/N: the multiplier (with 1/N)
+                // once per plane, then one column pass per wave
+                MSK_CUDA(ctx, ctx->fresnel.reserve(plane * sizeof(float2)));
+                fr.table = ctx->fresnel.as<float2>();
+                {
+                    Prof p(ctx, kFresTab, 8.0 * plane);
+                    k_fresnel_table<<<4 * 152, 256, 0, ctx->stream>>>(
+                        gp.g, fr, 1.0f / ((float)nx * (float)ny), ctx->fresnel.as<float2>());
+                }
                 {
                     Prof p(ctx, kFresnel, 16.0 * plane * nb);
-                    cop->col_fresnel(gp.g, nullptr, nb, psi, tb, fr,
-                                     1.0f / ((float)nx * (float)ny), ctx->stream);
+                    cop->col_fresnel(gp.g, nullptr, nb, psi, tb, fr, 1.0f, ctx->stream);
                 }
                 meta.clear();
                 meta.insert(meta.end(), off.begin(), off.end());

@@ -93,6 +93,7 @@ struct Launch {
     static void col_fresnel(const Geom &g, const int *units, int nunits, const float2 *in,
                             float2 *out, const Fresnel &fr, float scale, cudaStream_t s)
     {
+        if (!fr.table) return;  // the pass multiplies by fr.table; nothing to run without it
         col<kColFresnel>(g, units, nunits, in, out, fr, scale, s);
     }
     static void row_transmit(const Geom &g, const int *units, int nunits, const float2 *tbuf,
