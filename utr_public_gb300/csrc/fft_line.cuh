@@ -174,7 +174,7 @@ __device__ __forceinline__ void fft_stage(float2 (&v)[FftPlan<N>::E], float2 *bu
         const int j = b % NS;
 #pragma unroll
         for (int r = 1; r < R; r++) {
-            const float2 w = tw[r * NS + j];
+            const float2 w = __ldg(&tw[r * NS + j]);
             v[k + r * KB] = INV ? cmul_conj(v[k + r * KB], w) : cmul(v[k + r * KB], w);
         }
         dft<R, INV, KB>(&v[k]);
@@ -195,7 +195,8 @@ __device__ __forceinline__ void fft_stage(float2 (&v)[FftPlan<N>::E], float2 *bu
 // Full transform of one line: strided order in, strided order out.
 //   buf: the line group's shared buffer (C interleaved lines, padded)
 //   c:   this thread's line within the group; t: index within the line
-//   tw:  FftPlan<N>::TWN twiddles (stage 2 table, then stage 3 table)
+//   tw:  FftPlan<N>::TWN twiddles in global memory (stage 2 table, then
+//        stage 3 table), read through the L1 cache
 // Every thread of the group must call it (it contains group barriers).
 template <int N, bool INV, int C, bool BLOCK>
 __device__ __forceinline__ void fft_line(float2 (&v)[FftPlan<N>::E], float2 *buf, int c, int t,

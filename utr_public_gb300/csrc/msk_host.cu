@@ -16,6 +16,8 @@
 #include <thread>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
 #include "msk.h"
 #include "msk_launch.cuh"
 
@@ -622,7 +624,8 @@ struct msk_context {
     long long copies[2] = {};      // host-to-device, device-to-host copies while profiling
     double copy_bytes[2] = {};
     std::string err;
-    DevBuf psi, tbuf, atoms, slice_off, act, tables, imgmeta, wave0, images, exitw, fresnel;
+    DevBuf psi, tbuf, atoms, slice_off, act, tables, imgmeta, wave0, images, exitw, fresnel, flags;
+    size_t units_alloc = 0;  // units the psi / tbuf buffers hold
     std::vector<int> zmap = std::vector<int>(104, -1);
 };
 
@@ -643,6 +646,60 @@ int fail(msk_context *ctx, int code, const std::string &msg)
     } while (0)
 
 bool pow2_supported(int n) { return size_ops(n) != nullptr; }
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// dependency on libcuda).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaDriverEntryPointQueryResult q;
+        void *p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+// 2D view of a wave buffer for the column passes: rows = units * nx, each
+// row ny complex64 = 2*ny floats; box = the pass's column tile.
+int column_map(msk_context *ctx, CUtensorMap *map, void *base, int nx, int ny, size_t units,
+               const SizeOps *cop)
+{
+    auto enc = tensor_map_encoder();
+    if (!enc) return fail(ctx, MSK_ECUDA, "cuTensorMapEncodeTiled is not available");
+    const cuuint64_t dims[2] = {(cuuint64_t)2 * ny, (cuuint64_t)units * nx};
+    const cuuint64_t strides[1] = {(cuuint64_t)ny * 8};
+    const cuuint32_t box[2] = {(cuuint32_t)(2 * cop->col_c), (cuuint32_t)cop->col_box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(ctx, MSK_ECUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    return MSK_OK;
+}
+
+// Device error flags: cleared at the start of a call, read after its last
+// synchronisation (a bounded wait in a kernel that gave up sets a bit).
+int flags_reset(msk_context *ctx, Geom &g)
+{
+    MSK_CUDA(ctx, ctx->flags.reserve(256));
+    MSK_CUDA(ctx, cudaMemsetAsync(ctx->flags.p, 0, sizeof(int), ctx->stream));
+    g.err = ctx->flags.as<int>();
+    return MSK_OK;
+}
+
+int flags_check(msk_context *ctx)
+{
+    int h = 0;
+    MSK_CUDA(ctx, cudaMemcpyAsync(&h, ctx->flags.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h) return fail(ctx, MSK_ECUDA, "a kernel's bounded wait for its copies timed out");
+    return MSK_OK;
+}
 
 // Brackets one launch with events when profiling is on.
 struct Prof {
@@ -854,6 +911,11 @@ int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode)
     float2 *psi = ctx->psi.as<float2>(), *tb = ctx->tbuf.as<float2>();
     const int *act = ctx->act.as<int>();
     const int nsl1 = b.nslices + 1;
+    CUtensorMap tmap, pmap;
+    int st = column_map(ctx, &tmap, tb, gp.nx, gp.ny, ctx->units_alloc, cop);
+    if (st) return st;
+    st = column_map(ctx, &pmap, psi, gp.nx, gp.ny, ctx->units_alloc, cop);
+    if (st) return st;
     const double plane = (double)gp.nx * gp.ny;
     for (int sl = 0; sl < b.nslices; sl++) {
         const int na = b.act_off[sl + 1] - b.act_off[sl];
@@ -866,7 +928,7 @@ int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode)
             }
             {
                 Prof p(ctx, kKColMask, 16.0 * plane * na);
-                cop->col_mask(g, units, na, tb, tb, s);
+                cop->col_mask(g, tmap, tmap, units, na, s);
             }
             {
                 Prof p(ctx, kTransmit, 24.0 * plane * na);
@@ -875,7 +937,7 @@ int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode)
         }
         if (nmode == 0) {
             Prof p(ctx, kKColProp, 16.0 * plane * b.nunits);
-            cop->col_prop(g, nullptr, b.nunits, psi, psi, s);
+            cop->col_prop(g, pmap, pmap, nullptr, b.nunits, s);
         }
     }
     MSK_CUDA(ctx, cudaGetLastError());
@@ -914,7 +976,8 @@ void msk_destroy(msk_context *ctx)
     prof_collect(ctx);
     for (cudaEvent_t e : ctx->prof_pool) cudaEventDestroy(e);
     for (DevBuf *b : {&ctx->psi, &ctx->tbuf, &ctx->atoms, &ctx->slice_off, &ctx->act, &ctx->tables,
-                      &ctx->imgmeta, &ctx->wave0, &ctx->images, &ctx->exitw, &ctx->fresnel})
+                      &ctx->imgmeta, &ctx->wave0, &ctx->images, &ctx->exitw, &ctx->fresnel,
+                      &ctx->flags})
         b->release();
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
@@ -1108,7 +1171,10 @@ int msk_calculate(msk_context *ctx, float *pix, const float *wave0, const float 
     const size_t plane = (size_t)nx * ny;
     MSK_CUDA(ctx, ctx->psi.reserve(plane * sizeof(float2)));
     MSK_CUDA(ctx, ctx->tbuf.reserve(plane * sizeof(float2)));
+    ctx->units_alloc = 1;
     MSK_CUDA(ctx, ctx->wave0.reserve(plane * sizeof(float2)));
+    st = flags_reset(ctx, gp.g);
+    if (st) return st;
     MSK_CUDA(ctx, cudaMemcpyAsync(ctx->wave0.p, wave0, plane * sizeof(float2),
                                   cudaMemcpyHostToDevice, ctx->stream));
     count_copy(ctx, 0, (double)(plane * sizeof(float2)));
@@ -1130,7 +1196,7 @@ int msk_calculate(msk_context *ctx, float *pix, const float *wave0, const float 
     count_copy(ctx, 1, (double)(plane * sizeof(float2)));
     MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     prof_collect(ctx);
-    return MSK_OK;
+    return flags_check(ctx);
 }
 
 int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int *Znum,
@@ -1181,6 +1247,14 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
     }
     MSK_CUDA(ctx, ctx->psi.reserve((size_t)B * plane * sizeof(float2)));
     MSK_CUDA(ctx, ctx->tbuf.reserve((size_t)B * plane * sizeof(float2)));
+    ctx->units_alloc = B;
+    st = flags_reset(ctx, gp.g);
+    if (st) return st;
+    CUtensorMap pmap, tmap;
+    st = column_map(ctx, &pmap, ctx->psi.p, nx, ny, B, size_ops(nx));
+    if (st) return st;
+    st = column_map(ctx, &tmap, ctx->tbuf.p, nx, ny, B, size_ops(nx));
+    if (st) return st;
 
     const float wavlen = gp.wavlen;
     float k2maxo = s->aobj / wavlen;  // autosliccmd.cpp:1042-1043
@@ -1264,7 +1338,7 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
                 }
                 {
                     Prof p(ctx, kFresnel, 16.0 * plane * nb);
-                    cop->col_fresnel(gp.g, nullptr, nb, psi, tb, fr, 1.0f, ctx->stream);
+                    cop->col_fresnel(gp.g, pmap, tmap, nullptr, nb, fr, 1.0f, ctx->stream);
                 }
                 meta.clear();
                 meta.insert(meta.end(), off.begin(), off.end());
@@ -1295,7 +1369,7 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
     MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (kept)
         for (int u = 0; u < nunits; u++) kept[u] = ua[u].kept;
-    return MSK_OK;
+    return flags_check(ctx);
 }
 
 }  // extern "C"

@@ -12,14 +12,15 @@ namespace msk {
 
 struct SizeOps {
     int n;
+    int col_c, col_box_rows;  // column tile width and TMA box height for line length n
     void (*splat)(const Geom &, const int *units, int nunits, int slice, int nsl1,
                   const int *slice_off, const SplatAtom *atoms, float2 *tbuf, cudaStream_t);
-    void (*col_mask)(const Geom &, const int *units, int nunits, const float2 *in, float2 *out,
-                     cudaStream_t);
-    void (*col_prop)(const Geom &, const int *units, int nunits, const float2 *in, float2 *out,
-                     cudaStream_t);
-    void (*col_fresnel)(const Geom &, const int *units, int nunits, const float2 *in,
-                        float2 *out, const Fresnel &, float scale, cudaStream_t);
+    void (*col_mask)(const Geom &, const CUtensorMap &in, const CUtensorMap &out,
+                     const int *units, int nunits, cudaStream_t);
+    void (*col_prop)(const Geom &, const CUtensorMap &in, const CUtensorMap &out,
+                     const int *units, int nunits, cudaStream_t);
+    void (*col_fresnel)(const Geom &, const CUtensorMap &in, const CUtensorMap &out,
+                        const int *units, int nunits, const Fresnel &, float scale, cudaStream_t);
     void (*row_transmit)(const Geom &, const int *units, int nunits, const float2 *tbuf,
                          float2 *psi, float out_scale, cudaStream_t);
     void (*row_init)(const Geom &, const int *units, int nunits, const float2 *wave0,
@@ -37,11 +38,11 @@ const SizeOps *size_ops(int n);
 template <int N> struct Smem {
     using P = FftPlan<N>;
     static constexpr int NTS = RowCfg<N>::L * P::T;
-    static constexpr size_t splat = (size_t)(P::TWN + RowCfg<N>::L * P::PADN) * 8 + NTS * 16 +
-                                    128 * 4 + ((NTS + 31) / 32 + 1) * 4;
-    static constexpr size_t col = (size_t)(P::TWN + ColCfg<N>::C * P::PADN) * 8;
-    static constexpr size_t transmit = (size_t)(P::TWN + RowCfg<N>::LT * (P::PADN + N)) * 8;
-    static constexpr size_t row = (size_t)(P::TWN + RowCfg<N>::L * P::PADN) * 8;
+    static constexpr size_t splat = (size_t)RowCfg<N>::L * P::PADN * 8 + NTS * 16 + 128 * 4 +
+                                    ((NTS + 31) / 32 + 1) * 4;
+    static constexpr size_t col = (size_t)ColCfg<N>::C * P::PADN * 8 + 16;
+    static constexpr size_t transmit = (size_t)2 * RowCfg<N>::LT * P::PADN * 8 + 16;
+    static constexpr size_t row = (size_t)RowCfg<N>::L * P::PADN * 8;
 };
 
 template <typename K>
@@ -71,30 +72,31 @@ struct Launch {
             g, units, slice, nsl1, slice_off, atoms, tbuf);
     }
     template <int MODE>
-    static void col(const Geom &g, const int *units, int nunits, const float2 *in, float2 *out,
-                    const Fresnel &fr, float scale, cudaStream_t s)
+    static void col(const Geom &g, const CUtensorMap &in, const CUtensorMap &out,
+                    const int *units, int nunits, const Fresnel &fr, float scale, cudaStream_t s)
     {
         static std::once_flag f;
         set_smem(k_col_pass<N, MODE>, Smem<N>::col, f);
         const int C = ColCfg<N>::C;
         k_col_pass<N, MODE><<<nunits * (g.ny / C), ColCfg<N>::NT, Smem<N>::col, s>>>(
-            g, units, in, out, fr, scale);
+            g, in, out, units, fr, scale);
     }
-    static void col_mask(const Geom &g, const int *units, int nunits, const float2 *in,
-                         float2 *out, cudaStream_t s)
+    static void col_mask(const Geom &g, const CUtensorMap &in, const CUtensorMap &out,
+                         const int *units, int nunits, cudaStream_t s)
     {
-        col<kColMask>(g, units, nunits, in, out, Fresnel{}, 1.0f / (float)g.nx, s);
+        col<kColMask>(g, in, out, units, nunits, Fresnel{}, 1.0f / (float)g.nx, s);
     }
-    static void col_prop(const Geom &g, const int *units, int nunits, const float2 *in,
-                         float2 *out, cudaStream_t s)
+    static void col_prop(const Geom &g, const CUtensorMap &in, const CUtensorMap &out,
+                         const int *units, int nunits, cudaStream_t s)
     {
-        col<kColProp>(g, units, nunits, in, out, Fresnel{}, 1.0f / (float)g.nx, s);
+        col<kColProp>(g, in, out, units, nunits, Fresnel{}, 1.0f / (float)g.nx, s);
     }
-    static void col_fresnel(const Geom &g, const int *units, int nunits, const float2 *in,
-                            float2 *out, const Fresnel &fr, float scale, cudaStream_t s)
+    static void col_fresnel(const Geom &g, const CUtensorMap &in, const CUtensorMap &out,
+                            const int *units, int nunits, const Fresnel &fr, float scale,
+                            cudaStream_t s)
     {
         if (!fr.table) return;  // the pass multiplies by fr.table; nothing to run without it
-        col<kColFresnel>(g, units, nunits, in, out, fr, scale, s);
+        col<kColFresnel>(g, in, out, units, nunits, fr, scale, s);
     }
     static void row_transmit(const Geom &g, const int *units, int nunits, const float2 *tbuf,
                              float2 *psi, float out_scale, cudaStream_t s)
@@ -136,8 +138,9 @@ struct Launch {
 
     static const SizeOps *ops()
     {
-        static const SizeOps o = {N,         splat,        col_mask, col_prop,     col_fresnel,
-                                  row_transmit, row_init,  row_exit, row_intensity};
+        static const SizeOps o = {N,        ColCfg<N>::C, ColCfg<N>::BR, splat,
+                                  col_mask, col_prop,     col_fresnel,   row_transmit,
+                                  row_init, row_exit,     row_intensity};
         return &o;
     }
 };

@@ -24,6 +24,7 @@
 
 #include "fft_line.cuh"
 #include "msk_types.h"
+#include "tma.cuh"
 
 namespace msk {
 
@@ -33,20 +34,40 @@ __device__ __forceinline__ int pmod(int a, int n)
     return r < 0 ? r + n : r;
 }
 
-// Rows (lines of length NY) per CTA for the plain row passes and for P3.
+// Rows (lines of length NY) per CTA for the row passes.
 template <int NY> struct RowCfg {
     static constexpr int T = FftPlan<NY>::T;
-    static constexpr int L = (256 / T) > 0 ? 256 / T : 1;
-    static constexpr int LT = (128 / T) > 0 ? 128 / T : 1;  // P3 (needs a stash)
+    static constexpr int L = (256 / T) > 0 ? 256 / T : 1;   // P1 and the row utilities
+    static constexpr int LT = (128 / T) > 0 ? 128 / T : 1;  // P3 (two tiles in flight)
     static constexpr bool BLK = T > 32;
 };
-// Columns per CTA for the column passes.
+// Columns per CTA for the column passes, and the TMA boxes of a column tile.
 template <int NX> struct ColCfg {
-    // 256 threads per CTA (at most 16 columns): keeps 255 registers per thread
-    // available for the 32 strided elements of each column
-    static constexpr int C = (8192 / NX) < 16 ? (8192 / NX) : 16;
-    static constexpr int NT = C * FftPlan<NX>::T;
+    static constexpr int T = FftPlan<NX>::T;
+    static constexpr int C = (128 / T) < 2 ? 2 : ((128 / T) > 16 ? 16 : 128 / T);
+    static constexpr int NT = C * T;
+    static constexpr int BR = NX < 256 ? NX : 256;  // rows per box (TMA boxes are <= 256)
+    static constexpr int NBOX = NX / BR;
+    static constexpr uint32_t TILE_BYTES = (uint32_t)NX * C * 8;
 };
+
+// One thread arms the CTA's barrier; everyone waits for the phase with a
+// bound.  On a timeout the flag is raised and every thread returns false.
+__device__ __forceinline__ bool cta_wait(uint64_t *bar, uint32_t parity, int *err)
+{
+    const bool ok = mbar_wait(bar, parity);
+    const bool all = __syncthreads_and(ok) != 0;
+    if (!all && threadIdx.x == 0) atomicOr(err, kErrWaitTimeout);
+    return all;
+}
+
+// After a timeout: wait (bounded) for the copy to land so the CTA does not
+// exit under an in-flight write to its shared memory.
+__device__ __forceinline__ void cta_drain(uint64_t *bar, uint32_t parity)
+{
+    if (threadIdx.x == 0) (void)mbar_wait(bar, parity);
+    __syncthreads();
+}
 
 constexpr int kKnots = 100;
 
@@ -84,9 +105,8 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
     using P = FftPlan<NY>;
     constexpr int T = P::T, E = P::E, L = RowCfg<NY>::L, NT = L * T, NW = (NT + 31) / 32;
     constexpr bool BLK = RowCfg<NY>::BLK;
-    extern __shared__ __align__(16) unsigned char smem[];
-    float2 *s_tw = reinterpret_cast<float2 *>(smem);
-    float2 *s_lines = s_tw + P::TWN;
+    extern __shared__ __align__(128) unsigned char smem[];
+    float2 *s_lines = reinterpret_cast<float2 *>(smem);
     SplatAtom *s_atoms = reinterpret_cast<SplatAtom *>(s_lines + L * P::PADN);
     float *s_knots = reinterpret_cast<float *>(s_atoms + NT);
     int *s_cnt = reinterpret_cast<int *>(s_knots + 128);
@@ -99,7 +119,6 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
     const int ix = ix0 + l;
     const bool row_ok = ix < nx;
 
-    for (int i = tid; i < P::TWN; i += NT) s_tw[i] = g.tw_row[i];
     for (int i = tid; i < kKnots; i += NT) s_knots[i] = g.knots[i];
     float *vacc = reinterpret_cast<float *>(s_lines + l * P::PADN);
 #pragma unroll
@@ -169,11 +188,18 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
         sincosf(vacc[t + m * T] * g.sigma_f, &s, &c);
         v[m] = make_float2(c, s);
     }
-    fft_line<NY, false, 1, BLK>(v, s_lines + l * P::PADN, 0, t, s_tw);
-    if (row_ok) {
-        float2 *dst = tbuf + ((size_t)u * nx + ix) * NY;
+    fft_line<NY, false, 1, BLK>(v, s_lines + l * P::PADN, 0, t, g.tw_row);
+    // dense rows into shared memory, then one bulk store of the whole tile
+    __syncthreads();
 #pragma unroll
-        for (int m = 0; m < E; m++) dst[t + m * T] = v[m];
+    for (int m = 0; m < E; m++) s_lines[l * NY + t + m * T] = v[m];
+    fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+        const int rows = min(L, nx - ix0);
+        bulk_store(tbuf + ((size_t)u * nx + ix0) * NY, s_lines, (uint32_t)rows * NY * 8u);
+        bulk_commit();
+        bulk_wait_read();
     }
 }
 
@@ -189,30 +215,44 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
 enum { kColMask = 0, kColProp = 1, kColFresnel = 2 };
 
 template <int NX, int MODE>
-__global__ void __launch_bounds__(ColCfg<NX>::NT, 2)
-k_col_pass(const Geom g, const int *__restrict__ units, const float2 *in, float2 *out,
+__global__ void __launch_bounds__(ColCfg<NX>::NT, 512 / ColCfg<NX>::NT > 0 ? 512 / ColCfg<NX>::NT : 1)
+k_col_pass(const Geom g, const __grid_constant__ CUtensorMap in_map,
+           const __grid_constant__ CUtensorMap out_map, const int *__restrict__ units,
            const Fresnel fr, float fscale)
 {
     using P = FftPlan<NX>;
-    constexpr int T = P::T, E = P::E, C = ColCfg<NX>::C, NT = ColCfg<NX>::NT;
-    extern __shared__ __align__(16) unsigned char smem[];
-    float2 *s_tw = reinterpret_cast<float2 *>(smem);
-    float2 *s_buf = s_tw + P::TWN;
+    using CC = ColCfg<NX>;
+    constexpr int T = P::T, E = P::E, C = CC::C;
+    extern __shared__ __align__(128) unsigned char smem[];
+    float2 *buf = reinterpret_cast<float2 *>(smem);                       // PADN*C
+    uint64_t *bar = reinterpret_cast<uint64_t *>(buf + P::PADN * C);
 
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
     const int ny = g.ny;
     const int bpu = ny / C;
     const int u = units ? units[blockIdx.x / bpu] : (int)(blockIdx.x / bpu);
-    const int iy = (blockIdx.x % bpu) * C + c;
-    for (int i = tid; i < P::TWN; i += NT) s_tw[i] = g.tw_col[i];
-
-    const size_t plane = (size_t)NX * ny;
-    const float2 *src = in + (size_t)u * plane + iy;
+    const int cb = blockIdx.x % bpu;
+    const int iy = cb * C + c;
+    // tile = rows u*NX .. u*NX+NX-1, float columns 2*cb*C .. 2*cb*C+2C-1
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        mbar_arrive_expect_tx(bar, CC::TILE_BYTES);
+#pragma unroll
+        for (int j = 0; j < CC::NBOX; j++)
+            tma_load_2d(buf + j * CC::BR * C, &in_map, 2 * cb * C, u * NX + j * CC::BR, bar);
+    }
+    if (!cta_wait(bar, 0, g.err)) {
+        cta_drain(bar, 0);
+        return;
+    }
     float2 v[E];
 #pragma unroll
-    for (int m = 0; m < E; m++) v[m] = src[(size_t)(t + m * T) * ny];
-    __syncthreads();
-    fft_line<NX, false, C, true>(v, s_buf, c, t, s_tw);
+    for (int m = 0; m < E; m++) v[m] = buf[(t + m * T) * C + c];
+    fft_line<NX, false, C, true>(v, buf, c, t, g.tw_col);
 
     if constexpr (MODE == kColMask) {
         const float ky2 = __ldg(&g.ky2[iy]);
@@ -240,10 +280,19 @@ k_col_pass(const Geom g, const int *__restrict__ units, const float2 *in, float2
 #pragma unroll
         for (int m = 0; m < E; m++) v[m] = cmul(v[m], __ldg(&tab[(size_t)(t + m * T) * ny]));
     }
-    fft_line<NX, true, C, true>(v, s_buf, c, t, s_tw);
-    float2 *dst = out + (size_t)u * plane + iy;
+    fft_line<NX, true, C, true>(v, buf, c, t, g.tw_col);
+    __syncthreads();  // every thread is done with the exchange layout
 #pragma unroll
-    for (int m = 0; m < E; m++) dst[(size_t)(t + m * T) * ny] = v[m];
+    for (int m = 0; m < E; m++) buf[(t + m * T) * C + c] = v[m];
+    fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+#pragma unroll
+        for (int j = 0; j < CC::NBOX; j++)
+            tma_store_2d(&out_map, 2 * cb * C, u * NX + j * CC::BR, buf + j * CC::BR * C);
+        bulk_commit();
+        bulk_wait_read();
+    }
 }
 
 // ---------------------------------------------------------------- P3
@@ -251,45 +300,64 @@ k_col_pass(const Geom g, const int *__restrict__ units, const float2 *in, float2
 // (cfpix.cpp:349-372) between the transmission's and the wave's row
 // transforms.
 template <int NY>
-__global__ void __launch_bounds__(RowCfg<NY>::LT * FftPlan<NY>::T)
+__global__ void __launch_bounds__(RowCfg<NY>::LT * FftPlan<NY>::T, 4)
 k_row_transmit(const Geom g, const int *__restrict__ units, const float2 *__restrict__ tbuf,
                float2 *__restrict__ psi, float out_scale)
 {
     using P = FftPlan<NY>;
-    constexpr int T = P::T, E = P::E, L = RowCfg<NY>::LT, NT = L * T;
+    constexpr int T = P::T, E = P::E, L = RowCfg<NY>::LT;
     constexpr bool BLK = RowCfg<NY>::BLK;
-    extern __shared__ __align__(16) unsigned char smem[];
-    float2 *s_tw = reinterpret_cast<float2 *>(smem);
-    float2 *s_lines = s_tw + P::TWN;
-    float2 *s_stash = s_lines + L * P::PADN;
+    extern __shared__ __align__(128) unsigned char smem[];
+    float2 *bufB = reinterpret_cast<float2 *>(smem);   // transmission rows, then t_bl
+    float2 *bufW = bufB + L * P::PADN;                  // wave rows
+    uint64_t *bar = reinterpret_cast<uint64_t *>(bufW + L * P::PADN);
 
     const int tid = threadIdx.x, l = tid / T, t = tid % T;
     const int nx = g.nx;
     const int bpu = (nx + L - 1) / L;
     const int u = units[blockIdx.x / bpu];
-    const int ix = (blockIdx.x % bpu) * L + l;
-    const bool row_ok = ix < nx;
-    for (int i = tid; i < P::TWN; i += NT) s_tw[i] = g.tw_row[i];
-
-    const size_t off = ((size_t)u * nx + (row_ok ? ix : 0)) * NY;
+    const int ix0 = (blockIdx.x % bpu) * L;
+    const int rows = min(L, nx - ix0);
+    const uint32_t bytes = (uint32_t)rows * NY * 8u;
+    const size_t off = ((size_t)u * nx + ix0) * NY;
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        mbar_arrive_expect_tx(bar, 2u * bytes);
+        bulk_load(bufB, tbuf + off, bytes, bar);
+        bulk_load(bufW, psi + off, bytes, bar);
+    }
+    if (!cta_wait(bar, 0, g.err)) {
+        cta_drain(bar, 0);
+        return;
+    }
     float2 v[E];
 #pragma unroll
-    for (int m = 0; m < E; m++) v[m] = tbuf[off + t + m * T];
+    for (int m = 0; m < E; m++) v[m] = bufB[l * NY + t + m * T];
+    __syncthreads();  // dense rows read before any line's exchange overwrites them
+    fft_line<NY, true, 1, BLK>(v, bufB + l * P::PADN, 0, t, g.tw_row);
     __syncthreads();
-    float2 *buf = s_lines + l * P::PADN;
-    float2 *stash = s_stash + l * NY;
-    fft_line<NY, true, 1, BLK>(v, buf, 0, t, s_tw);
 #pragma unroll
-    for (int m = 0; m < E; m++) stash[t + m * T] = v[m];
+    for (int m = 0; m < E; m++) bufB[l * NY + t + m * T] = v[m];  // t_bl, own elements only
 #pragma unroll
-    for (int m = 0; m < E; m++) v[m] = psi[off + t + m * T];
-    fft_line<NY, true, 1, BLK>(v, buf, 0, t, s_tw);
+    for (int m = 0; m < E; m++) v[m] = bufW[l * NY + t + m * T];
+    __syncthreads();
+    fft_line<NY, true, 1, BLK>(v, bufW + l * P::PADN, 0, t, g.tw_row);
 #pragma unroll
-    for (int m = 0; m < E; m++) v[m] = cmul(v[m], stash[t + m * T]);
-    fft_line<NY, false, 1, BLK>(v, buf, 0, t, s_tw);
-    if (row_ok) {
+    for (int m = 0; m < E; m++) v[m] = cmul(v[m], bufB[l * NY + t + m * T]);
+    fft_line<NY, false, 1, BLK>(v, bufW + l * P::PADN, 0, t, g.tw_row);
+    __syncthreads();
 #pragma unroll
-        for (int m = 0; m < E; m++) psi[off + t + m * T] = cscale(v[m], out_scale);
+    for (int m = 0; m < E; m++) bufW[l * NY + t + m * T] = cscale(v[m], out_scale);
+    fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+        bulk_store(psi + off, bufW, bytes);
+        bulk_commit();
+        bulk_wait_read();
     }
 }
 
@@ -307,9 +375,8 @@ k_row_simple(const Geom g, const int *__restrict__ units, const float2 *__restri
     using P = FftPlan<NY>;
     constexpr int T = P::T, E = P::E, L = RowCfg<NY>::L, NT = L * T;
     constexpr bool BLK = RowCfg<NY>::BLK;
-    extern __shared__ __align__(16) unsigned char smem[];
-    float2 *s_tw = reinterpret_cast<float2 *>(smem);
-    float2 *s_lines = s_tw + P::TWN;
+    extern __shared__ __align__(128) unsigned char smem[];
+    float2 *s_lines = reinterpret_cast<float2 *>(smem);
     const int tid = threadIdx.x, l = tid / T, t = tid % T;
     const int nx = g.nx;
     const int bpu = (nx + L - 1) / L;
@@ -317,14 +384,12 @@ k_row_simple(const Geom g, const int *__restrict__ units, const float2 *__restri
     const int u = units ? units[ui] : ui;
     const int ix = (blockIdx.x % bpu) * L + l;
     const bool row_ok = ix < nx;
-    for (int i = tid; i < P::TWN; i += NT) s_tw[i] = g.tw_row[i];
     const size_t row = (size_t)(row_ok ? ix : 0) * NY;
     const float2 *src = (MODE == kRowInit) ? in + row : in + (size_t)u * nx * NY + row;
     float2 v[E];
 #pragma unroll
     for (int m = 0; m < E; m++) v[m] = src[t + m * T];
-    __syncthreads();
-    fft_line<NY, MODE == kRowExit, 1, BLK>(v, s_lines + l * P::PADN, 0, t, s_tw);
+    fft_line<NY, MODE == kRowExit, 1, BLK>(v, s_lines + l * P::PADN, 0, t, g.tw_row);
     if (row_ok) {
         float2 *dst = out + (size_t)u * nx * NY + row;
 #pragma unroll
@@ -348,17 +413,14 @@ k_row_intensity(const Geom g, const int *__restrict__ img_off, const int *__rest
     using P = FftPlan<NY>;
     constexpr int T = P::T, E = P::E, L = RowCfg<NY>::L, NT = L * T;
     constexpr bool BLK = RowCfg<NY>::BLK;
-    extern __shared__ __align__(16) unsigned char smem[];
-    float2 *s_tw = reinterpret_cast<float2 *>(smem);
-    float2 *s_lines = s_tw + P::TWN;
+    extern __shared__ __align__(128) unsigned char smem[];
+    float2 *s_lines = reinterpret_cast<float2 *>(smem);
     const int tid = threadIdx.x, l = tid / T, t = tid % T;
     const int nx = g.nx;
     const int bpu = (nx + L - 1) / L;
     const int img = blockIdx.x / bpu;
     const int ix = (blockIdx.x % bpu) * L + l;
     const bool row_ok = ix < nx;
-    for (int i = tid; i < P::TWN; i += NT) s_tw[i] = g.tw_row[i];
-    __syncthreads();
     const size_t row = (size_t)(row_ok ? ix : 0) * NY;
     float acc[E];
     const int flags = img_flags[img];
@@ -370,7 +432,7 @@ k_row_intensity(const Geom g, const int *__restrict__ img_off, const int *__rest
         float2 v[E];
 #pragma unroll
         for (int m = 0; m < E; m++) v[m] = src[t + m * T];
-        fft_line<NY, true, 1, BLK>(v, s_lines + l * P::PADN, 0, t, s_tw);
+        fft_line<NY, true, 1, BLK>(v, s_lines + l * P::PADN, 0, t, g.tw_row);
 #pragma unroll
         for (int m = 0; m < E; m++) acc[m] += v[m].x * v[m].x + v[m].y * v[m].y;
     }

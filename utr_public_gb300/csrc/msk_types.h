@@ -28,6 +28,7 @@ struct Geom {
     const float2 *tw_col;  // twiddles for line length nx
     const float *knots;    // [100] spline knots in r^2
     const float4 *coef;    // [nz][100] spline {y, b, c, d} per compact atomic number
+    int *err;              // device error flags (kErrWaitTimeout ...), 0 when all is well
 };
 
 // Atoms of one (unit, slice) for the splat: x and y relative to the pixel
