@@ -172,10 +172,16 @@ __device__ __forceinline__ void fft_stage(float2 (&v)[FftPlan<N>::E], float2 *bu
     for (int k = 0; k < KB; k++) {
         const int b = t + k * T;
         const int j = b % NS;
+        // twiddles in groups of 8: the empty asm keeps the compiler from
+        // hoisting all R-1 loads (2 registers each) ahead of the multiplies
 #pragma unroll
-        for (int r = 1; r < R; r++) {
-            const float2 w = __ldg(&tw[r * NS + j]);
-            v[k + r * KB] = INV ? cmul_conj(v[k + r * KB], w) : cmul(v[k + r * KB], w);
+        for (int r0 = 1; r0 < R; r0 += 8) {
+#pragma unroll
+            for (int r = r0; r < r0 + 8 && r < R; r++) {
+                const float2 w = __ldg(&tw[r * NS + j]);
+                v[k + r * KB] = INV ? cmul_conj(v[k + r * KB], w) : cmul(v[k + r * KB], w);
+            }
+            asm volatile("" ::: "memory");
         }
         dft<R, INV, KB>(&v[k]);
     }

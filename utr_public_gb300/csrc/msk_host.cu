@@ -333,6 +333,7 @@ static void slice_counts(float deltaz_f, float zmax, int natom, const float *z2,
 
 // Plan-wide geometry computed on the host exactly as the reference does.
 struct GridPre {
+    std::vector<int2> kband;  // per column iy: kx2 + ky2 < k2max <=> ix <= A or ix >= B
     int nx, ny;
     float ax, by, v0, wavlen, k2max;
     double scalex, scaley;  // float-divided pixel pitch, promoted
@@ -342,7 +343,7 @@ struct GridPre {
     std::vector<float2> propx, propy;
 };
 
-static void grid_pre(GridPre &gp, int nx, int ny, float ax, float by, float v0, float deltaz,
+static bool grid_pre(GridPre &gp, int nx, int ny, float ax, float by, float v0, float deltaz,
                      float ctiltx, float ctilty)
 {
     gp.nx = nx;
@@ -380,6 +381,27 @@ static void grid_pre(GridPre &gp, int nx, int ny, float ax, float by, float v0, 
         const double t = scale * (gp.ky2[iy] * gp.wavlen - gp.ky[iy] * tcty);
         gp.propy[iy] = make_float2((float)cos(t), (float)-sin(t));
     }
+    // Band limit as index ranges per column: freqn's kx2 rises on [0, imid]
+    // and falls on (imid, nx), and a float sum is monotone in each term, so
+    // the pixels kept by kx2[ix] + ky2[iy] < k2max (autoslic.cpp:1004,
+    // slicelib.cpp:827-829) are ix <= A or ix >= B.  Checked element by element.
+    gp.kband.resize(ny);
+    for (int iy = 0; iy < ny; iy++) {
+        int A = -1, B = nx;
+        for (int ix = 0; ix < nx; ix++)
+            if (gp.ky2[iy] + gp.kx2[ix] < gp.k2max) {
+                if (B == nx && (A == ix - 1)) A = ix;
+            }
+        for (int ix = nx - 1; ix > A; ix--)
+            if (gp.ky2[iy] + gp.kx2[ix] < gp.k2max) B = ix;
+            else break;
+        for (int ix = 0; ix < nx; ix++) {
+            const bool keep = gp.ky2[iy] + gp.kx2[ix] < gp.k2max;
+            const bool prop = gp.kx2[ix] < gp.k2max && (gp.kx2[ix] + gp.ky2[iy]) < gp.k2max;
+            if (keep != (ix <= A || ix >= B) || prop != keep) return false;
+        }
+        gp.kband[iy] = make_int2(A, B);
+    }
     // trlayer constants (autoslic.cpp:927-941)
     gp.sigma = phys::sigma(v0) / 1000.0;
     gp.scalex = ax / nx;  // float division, as the reference
@@ -403,6 +425,7 @@ static void grid_pre(GridPre &gp, int nx, int ny, float ax, float by, float v0, 
     const double dlnr = log(5.0 / 0.01) / (phys::kN - 1);
     g.lut_c0 = (float)(-2.0 * log(0.01));
     g.lut_c1 = (float)(1.0 / (2.0 * dlnr));
+    return true;
 }
 
 // Stockham stage twiddles for line length n, matching FftPlan<n>.
@@ -788,7 +811,8 @@ int upload_tables(msk_context *ctx, GridPre &gp, const std::vector<int> &zlist)
     const size_t o_kx2 = piece(4 * gp.nx), o_ky2 = piece(4 * gp.ny), o_kx = piece(4 * gp.nx),
                  o_ky = piece(4 * gp.ny), o_px = piece(8 * gp.nx), o_py = piece(8 * gp.ny),
                  o_twr = piece(8 * twr.size()), o_twc = piece(8 * twc.size()),
-                 o_kn = piece(4 * knots.size()), o_cf = piece(16 * coef.size());
+                 o_kn = piece(4 * knots.size()), o_cf = piece(16 * coef.size()),
+                 o_kb = piece(8 * gp.ny);
     std::vector<unsigned char> host(off);
     std::memcpy(&host[o_kx2], gp.kx2.data(), 4 * gp.nx);
     std::memcpy(&host[o_ky2], gp.ky2.data(), 4 * gp.ny);
@@ -800,6 +824,7 @@ int upload_tables(msk_context *ctx, GridPre &gp, const std::vector<int> &zlist)
     std::memcpy(&host[o_twc], twc.data(), 8 * twc.size());
     std::memcpy(&host[o_kn], knots.data(), 4 * knots.size());
     std::memcpy(&host[o_cf], coef.data(), 16 * coef.size());
+    std::memcpy(&host[o_kb], gp.kband.data(), 8 * gp.ny);
     MSK_CUDA(ctx, ctx->tables.reserve(off));
     MSK_CUDA(ctx, cudaMemcpyAsync(ctx->tables.p, host.data(), off, cudaMemcpyHostToDevice,
                                   ctx->stream));
@@ -816,6 +841,7 @@ int upload_tables(msk_context *ctx, GridPre &gp, const std::vector<int> &zlist)
     g.tw_col = reinterpret_cast<const float2 *>(b + o_twc);
     g.knots = reinterpret_cast<const float *>(b + o_kn);
     g.coef = reinterpret_cast<const float4 *>(b + o_cf);
+    g.kband = reinterpret_cast<const int2 *>(b + o_kb);
     (void)o_kx;
     (void)o_ky;
     return MSK_OK;
@@ -1134,8 +1160,9 @@ int msk_calculate(msk_context *ctx, float *pix, const float *wave0, const float 
         return fail(ctx, MSK_EUNSUPPORTED, "grid must be a power of two from 16 to 4096");
     MSK_CUDA(ctx, cudaSetDevice(ctx->device));
     GridPre gp;
-    grid_pre(gp, nx, ny, ax, by, param[MSK_pENERGY], param[MSK_pDELTAZ], param[MSK_pXCTILT],
-             param[MSK_pYCTILT]);
+    if (!grid_pre(gp, nx, ny, ax, by, param[MSK_pENERGY], param[MSK_pDELTAZ], param[MSK_pXCTILT],
+                  param[MSK_pYCTILT]))
+        return fail(ctx, MSK_EUNSUPPORTED, "band limit is not two index ranges per column");
     const int nslices = slice_count(param[MSK_pDELTAZ], ctblengthz);
     std::vector<int> zlist;
     // the reference's range check comes before any atomic-number check
@@ -1218,7 +1245,8 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
     MSK_CUDA(ctx, cudaSetDevice(ctx->device));
     GridPre gp;
     // MsctKirkland passes a zero crystal tilt (autosliccmd.cpp:435-437)
-    grid_pre(gp, nx, ny, s->ctblength, s->ctblength, s->v0, s->deltaz, 0.0f, 0.0f);
+    if (!grid_pre(gp, nx, ny, s->ctblength, s->ctblength, s->v0, s->deltaz, 0.0f, 0.0f))
+        return fail(ctx, MSK_EUNSUPPORTED, "band limit is not two index ranges per column");
     const int nslices = slice_count(s->deltaz, s->ctblengthz);
     std::vector<int> zlist;
     int st = build_zmap(ctx, natom, Znum, zlist);

@@ -184,8 +184,10 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
     float2 v[E];
 #pragma unroll
     for (int m = 0; m < E; m++) {
-        float s, c;
-        sincosf(vacc[t + m * T] * g.sigma_f, &s, &c);
+        // most of a slice is empty: exp(i*0) = 1 exactly, as sincosf(0) gives
+        const float ph = vacc[t + m * T] * g.sigma_f;
+        float s = 0.0f, c = 1.0f;
+        if (__any_sync(0xffffffffu, ph != 0.0f)) sincosf(ph, &s, &c);
         v[m] = make_float2(c, s);
     }
     fft_line<NY, false, 1, BLK>(v, s_lines + l * P::PADN, 0, t, g.tw_row);
@@ -215,7 +217,7 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
 enum { kColMask = 0, kColProp = 1, kColFresnel = 2 };
 
 template <int NX, int MODE>
-__global__ void __launch_bounds__(ColCfg<NX>::NT, 512 / ColCfg<NX>::NT > 0 ? 512 / ColCfg<NX>::NT : 1)
+__global__ void __launch_bounds__(ColCfg<NX>::NT, 384 / ColCfg<NX>::NT > 0 ? 384 / ColCfg<NX>::NT : 1)
 k_col_pass(const Geom g, const __grid_constant__ CUtensorMap in_map,
            const __grid_constant__ CUtensorMap out_map, const int *__restrict__ units,
            const Fresnel fr, float fscale)
@@ -255,20 +257,21 @@ k_col_pass(const Geom g, const __grid_constant__ CUtensorMap in_map,
     fft_line<NX, false, C, true>(v, buf, c, t, g.tw_col);
 
     if constexpr (MODE == kColMask) {
-        const float ky2 = __ldg(&g.ky2[iy]);
-#pragma unroll
-        for (int m = 0; m < E; m++) {
-            const float k2 = __fadd_rn(__ldg(&g.kx2[t + m * T]), ky2);
-            v[m] = (k2 < g.k2max) ? cscale(v[m], fscale) : make_float2(0.0f, 0.0f);
-        }
-    } else if constexpr (MODE == kColProp) {
-        const float ky2 = __ldg(&g.ky2[iy]);
-        const float2 py = __ldg(&g.propy[iy]);
+        // the band limit ky2 + kx2 < k2max keeps ix <= A or ix >= B (host-exact)
+        const int2 ab = __ldg(&g.kband[iy]);
 #pragma unroll
         for (int m = 0; m < E; m++) {
             const int ix = t + m * T;
-            const float kx2 = __ldg(&g.kx2[ix]);
-            if (kx2 < g.k2max && __fadd_rn(kx2, ky2) < g.k2max) {
+            v[m] = (ix <= ab.x || ix >= ab.y) ? cscale(v[m], fscale) : make_float2(0.0f, 0.0f);
+        }
+    } else if constexpr (MODE == kColProp) {
+        // kx2 < k2max and kx2 + ky2 < k2max: the same index set as the band limit
+        const int2 ab = __ldg(&g.kband[iy]);
+        const float2 py = cscale(__ldg(&g.propy[iy]), 1.0f);
+#pragma unroll
+        for (int m = 0; m < E; m++) {
+            const int ix = t + m * T;
+            if (ix <= ab.x || ix >= ab.y) {
                 const float2 w = cmul(cmul(v[m], py), __ldg(&g.propx[ix]));
                 v[m] = cscale(w, fscale);
             } else {
@@ -300,7 +303,7 @@ k_col_pass(const Geom g, const __grid_constant__ CUtensorMap in_map,
 // (cfpix.cpp:349-372) between the transmission's and the wave's row
 // transforms.
 template <int NY>
-__global__ void __launch_bounds__(RowCfg<NY>::LT * FftPlan<NY>::T, 4)
+__global__ void __launch_bounds__(RowCfg<NY>::LT * FftPlan<NY>::T, 3)
 k_row_transmit(const Geom g, const int *__restrict__ units, const float2 *__restrict__ tbuf,
                float2 *__restrict__ psi, float out_scale)
 {

@@ -24,6 +24,7 @@ struct Geom {
     const float *ky2;   // [ny]
     const float2 *propx;  // [nx] (cos t, -sin t), t = pi dz (kx^2 lambda - kx 2 tan(tilt_x))
     const float2 *propy;  // [ny]
+    const int2 *kband;    // [ny] (A, B): kx2[ix] + ky2[iy] < k2max  <=>  ix <= A or ix >= B
     const float2 *tw_row;  // twiddles for line length ny
     const float2 *tw_col;  // twiddles for line length nx
     const float *knots;    // [100] spline knots in r^2
