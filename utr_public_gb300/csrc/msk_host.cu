@@ -639,6 +639,8 @@ struct msk_context {
     int device = 0;
     cudaStream_t stream = nullptr;      // the stream work goes to
     cudaStream_t own_stream = nullptr;  // created with the context
+    cudaStream_t aux = nullptr;         // second stream: the wave chain of the slice loop
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_t[2] = {}, ev_free[2] = {};
     bool prof_on = false;
     std::vector<ProfRec> prof_pending;
     std::vector<cudaEvent_t> prof_pool;
@@ -647,7 +649,8 @@ struct msk_context {
     long long copies[2] = {};      // host-to-device, device-to-host copies while profiling
     double copy_bytes[2] = {};
     std::string err;
-    DevBuf psi, tbuf, atoms, slice_off, act, tables, imgmeta, wave0, images, exitw, fresnel, flags;
+    DevBuf psi, tbuf, tbuf2, atoms, slice_off, act, tables, imgmeta, wave0, images, exitw, fresnel,
+        flags;
     size_t units_alloc = 0;  // units the psi / tbuf buffers hold
     std::vector<int> zmap = std::vector<int>(104, -1);
 };
@@ -741,18 +744,20 @@ struct Prof {
         cudaEventCreate(&e);
         return e;
     }
-    Prof(msk_context *c, int k, double b) : ctx(c), kind(k), bytes(b)
+    cudaStream_t st;
+    Prof(msk_context *c, int k, double b, cudaStream_t stream = nullptr)
+        : ctx(c), kind(k), bytes(b), st(stream ? stream : c->stream)
     {
         if (ctx->prof_on) {
             a = get(ctx);
-            cudaEventRecord(a, ctx->stream);
+            cudaEventRecord(a, st);
         }
     }
     ~Prof()
     {
         if (a) {
             cudaEvent_t b = get(ctx);
-            cudaEventRecord(b, ctx->stream);
+            cudaEventRecord(b, st);
             ctx->prof_pending.push_back({kind, a, b, bytes});
         }
     }
@@ -929,42 +934,76 @@ int upload_batch(msk_context *ctx, const std::vector<UnitAtoms> &ua, int u0, int
 
 // The slice loop over a batch: the psi buffer holds W0 = S(wave0) on entry
 // and W = S(exit wave) on return.
+//
+// Two chains per slice: the transmission chain (P1 splat, P2 band limit) and
+// the wave chain (P3 transmit, P4 propagate).  With two transmission buffers
+// the transmission chain of the next non-empty slice runs on the context's
+// stream while the wave chain of the current one runs on the second stream,
+// so the compute-bound splat overlaps the memory-bound wave passes.  Events
+// order P3 after its P2 and the reuse of a transmission buffer after the P3
+// that read it.  With per-kernel profiling on, everything runs in order on
+// one stream so that each launch is timed alone.
 int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode)
 {
     const SizeOps *rop = size_ops(gp.ny), *cop = size_ops(gp.nx);
     const Geom &g = gp.g;
-    cudaStream_t s = ctx->stream;
-    float2 *psi = ctx->psi.as<float2>(), *tb = ctx->tbuf.as<float2>();
+    const bool overlap = !ctx->prof_on && ctx->tbuf2.cap >= ctx->tbuf.cap;
+    cudaStream_t sA = ctx->stream, sB = overlap ? ctx->aux : ctx->stream;
+    float2 *psi = ctx->psi.as<float2>();
+    float2 *tbs[2] = {ctx->tbuf.as<float2>(), overlap ? ctx->tbuf2.as<float2>() : ctx->tbuf.as<float2>()};
     const int *act = ctx->act.as<int>();
     const int nsl1 = b.nslices + 1;
-    CUtensorMap tmap, pmap;
-    int st = column_map(ctx, &tmap, tb, gp.nx, gp.ny, ctx->units_alloc, cop);
+    CUtensorMap tmaps[2], pmap;
+    int st = column_map(ctx, &tmaps[0], tbs[0], gp.nx, gp.ny, ctx->units_alloc, cop);
+    if (st) return st;
+    st = column_map(ctx, &tmaps[1], tbs[1], gp.nx, gp.ny, ctx->units_alloc, cop);
     if (st) return st;
     st = column_map(ctx, &pmap, psi, gp.nx, gp.ny, ctx->units_alloc, cop);
     if (st) return st;
     const double plane = (double)gp.nx * gp.ny;
+    if (overlap) {
+        MSK_CUDA(ctx, cudaEventRecord(ctx->ev_fork, sA));
+        MSK_CUDA(ctx, cudaStreamWaitEvent(sB, ctx->ev_fork, 0));
+    }
+    bool pending_free[2] = {false, false};
+    int uses = 0;
     for (int sl = 0; sl < b.nslices; sl++) {
         const int na = b.act_off[sl + 1] - b.act_off[sl];
         const int *units = act + b.act_off[sl];
         if (na > 0) {
+            const int k = overlap ? (uses++ & 1) : 0;
+            float2 *tb = tbs[k];
+            if (overlap && pending_free[k]) MSK_CUDA(ctx, cudaStreamWaitEvent(sA, ctx->ev_free[k], 0));
             {
-                Prof p(ctx, kSplat, 8.0 * plane * na);
+                Prof p(ctx, kSplat, 8.0 * plane * na, sA);
                 rop->splat(g, units, na, sl, nsl1, ctx->slice_off.as<int>(),
-                           ctx->atoms.as<SplatAtom>(), tb, s);
+                           ctx->atoms.as<SplatAtom>(), tb, sA);
             }
             {
-                Prof p(ctx, kKColMask, 16.0 * plane * na);
-                cop->col_mask(g, tmap, tmap, units, na, s);
+                Prof p(ctx, kKColMask, 16.0 * plane * na, sA);
+                cop->col_mask(g, tmaps[k], tmaps[k], units, na, sA);
+            }
+            if (overlap) {
+                MSK_CUDA(ctx, cudaEventRecord(ctx->ev_t[k], sA));
+                MSK_CUDA(ctx, cudaStreamWaitEvent(sB, ctx->ev_t[k], 0));
             }
             {
-                Prof p(ctx, kTransmit, 24.0 * plane * na);
-                rop->row_transmit(g, units, na, tb, psi, 1.0f / ((float)gp.ny * (float)gp.ny), s);
+                Prof p(ctx, kTransmit, 24.0 * plane * na, sB);
+                rop->row_transmit(g, units, na, tb, psi, 1.0f / ((float)gp.ny * (float)gp.ny), sB);
+            }
+            if (overlap) {
+                MSK_CUDA(ctx, cudaEventRecord(ctx->ev_free[k], sB));
+                pending_free[k] = true;
             }
         }
         if (nmode == 0) {
-            Prof p(ctx, kKColProp, 16.0 * plane * b.nunits);
-            cop->col_prop(g, pmap, pmap, nullptr, b.nunits, s);
+            Prof p(ctx, kKColProp, 16.0 * plane * b.nunits, sB);
+            cop->col_prop(g, pmap, pmap, nullptr, b.nunits, sB);
         }
+    }
+    if (overlap) {
+        MSK_CUDA(ctx, cudaEventRecord(ctx->ev_join, sB));
+        MSK_CUDA(ctx, cudaStreamWaitEvent(sA, ctx->ev_join, 0));
     }
     MSK_CUDA(ctx, cudaGetLastError());
     return MSK_OK;
@@ -985,6 +1024,10 @@ int msk_create(int device, msk_context **out)
     ctx->device = device;
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking);
+    for (cudaEvent_t *ev : {&ctx->ev_fork, &ctx->ev_join, &ctx->ev_t[0], &ctx->ev_t[1],
+                            &ctx->ev_free[0], &ctx->ev_free[1]})
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
     ctx->stream = ctx->own_stream;
     if (e != cudaSuccess) {
         delete ctx;
@@ -1001,10 +1044,14 @@ void msk_destroy(msk_context *ctx)
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     prof_collect(ctx);
     for (cudaEvent_t e : ctx->prof_pool) cudaEventDestroy(e);
-    for (DevBuf *b : {&ctx->psi, &ctx->tbuf, &ctx->atoms, &ctx->slice_off, &ctx->act, &ctx->tables,
+    for (DevBuf *b : {&ctx->psi, &ctx->tbuf, &ctx->tbuf2, &ctx->atoms, &ctx->slice_off, &ctx->act, &ctx->tables,
                       &ctx->imgmeta, &ctx->wave0, &ctx->images, &ctx->exitw, &ctx->fresnel,
                       &ctx->flags})
         b->release();
+    for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_join, ctx->ev_t[0], ctx->ev_t[1], ctx->ev_free[0],
+                          ctx->ev_free[1]})
+        if (e) cudaEventDestroy(e);
+    if (ctx->aux) cudaStreamDestroy(ctx->aux);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }
@@ -1198,6 +1245,7 @@ int msk_calculate(msk_context *ctx, float *pix, const float *wave0, const float 
     const size_t plane = (size_t)nx * ny;
     MSK_CUDA(ctx, ctx->psi.reserve(plane * sizeof(float2)));
     MSK_CUDA(ctx, ctx->tbuf.reserve(plane * sizeof(float2)));
+    MSK_CUDA(ctx, ctx->tbuf2.reserve(plane * sizeof(float2)));
     ctx->units_alloc = 1;
     MSK_CUDA(ctx, ctx->wave0.reserve(plane * sizeof(float2)));
     st = flags_reset(ctx, gp.g);
@@ -1264,7 +1312,8 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
     const size_t img_bytes = (size_t)nangles * ndefocus * plane * sizeof(float);
     size_t budget = free_b - std::min(free_b, (size_t)(img_dev ? 0 : img_bytes));
     budget = std::min<size_t>(budget / 2, (size_t)64 << 30);
-    int B = (int)std::max<size_t>(1, std::min<size_t>(nunits, budget / (2 * plane * sizeof(float2))));
+    // psi and two transmission buffers per unit in flight
+    int B = (int)std::max<size_t>(1, std::min<size_t>(nunits, budget / (3 * plane * sizeof(float2))));
     if (s->max_batch > 0) B = std::min(B, s->max_batch);
     if (nconfig > 1 && B > nconfig) B = (B / nconfig) * nconfig;  // whole angles per batch
 
@@ -1275,6 +1324,7 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
     }
     MSK_CUDA(ctx, ctx->psi.reserve((size_t)B * plane * sizeof(float2)));
     MSK_CUDA(ctx, ctx->tbuf.reserve((size_t)B * plane * sizeof(float2)));
+    MSK_CUDA(ctx, ctx->tbuf2.reserve((size_t)B * plane * sizeof(float2)));
     ctx->units_alloc = B;
     st = flags_reset(ctx, gp.g);
     if (st) return st;

@@ -69,6 +69,14 @@ __device__ __forceinline__ void cta_drain(uint64_t *bar, uint32_t parity)
     __syncthreads();
 }
 
+// Resident CTAs per SM the column pass is compiled for (its register budget):
+// the propagator pass fits 128 registers, the band-limit and free-space
+// passes need ~168 to stay free of spills at 1024 points.
+template <int NX, int MODE> struct ColMinBlocks {
+    static constexpr int per = (MODE == 1 ? 512 : 384) / ColCfg<NX>::NT;
+    static constexpr int value = per > 0 ? per : 1;
+};
+
 constexpr int kKnots = 100;
 
 // Spline of the projected potential vs r^2 (TemsimLibrary/slicelib.cpp:2402-2425,
@@ -217,7 +225,7 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
 enum { kColMask = 0, kColProp = 1, kColFresnel = 2 };
 
 template <int NX, int MODE>
-__global__ void __launch_bounds__(ColCfg<NX>::NT, 384 / ColCfg<NX>::NT > 0 ? 384 / ColCfg<NX>::NT : 1)
+__global__ void __launch_bounds__(ColCfg<NX>::NT, ColMinBlocks<NX, MODE>::value)
 k_col_pass(const Geom g, const __grid_constant__ CUtensorMap in_map,
            const __grid_constant__ CUtensorMap out_map, const int *__restrict__ units,
            const Fresnel fr, float fscale)
