@@ -33,7 +33,7 @@ __device__ __forceinline__ int pmod(int a, int n) { return a & (n - 1); }
 
 // exp(i*ph), kept out of line: 32 inlined sincosf bodies per thread (with
 // their large-argument paths) overflow the instruction cache of the splat
-__device__ __noinline__ float2 expi(float ph)
+static __device__ __noinline__ float2 expi(float ph)
 {
     float s, c;
     sincosf(ph, &s, &c);
