@@ -3,7 +3,6 @@
 // row passes by ny and column passes by nx.
 #pragma once
 
-#include <algorithm>
 #include <mutex>
 
 #include "msk_passes.cuh"
@@ -41,7 +40,7 @@ template <int N> struct Smem {
     static constexpr int NTS = RowCfg<N>::L * P::T;
     static constexpr size_t splat = (size_t)RowCfg<N>::L * P::PADN * 8 + NTS * 16 + 128 * 4 +
                                     ((NTS + 31) / 32 + 1) * 4;
-    static constexpr size_t col = (size_t)2 * ColCfg<N>::C * P::PADN * 8 + 16;
+    static constexpr size_t col = (size_t)ColCfg<N>::C * P::PADN * 8 + 16;
     static constexpr size_t transmit = (size_t)2 * RowCfg<N>::LT * P::PADN * 8 + 16;
     static constexpr size_t row = (size_t)RowCfg<N>::L * P::PADN * 8;
 };
@@ -72,29 +71,15 @@ struct Launch {
         k_row_splat<N><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::splat, s>>>(
             g, units, slice, nsl1, slice_off, atoms, tbuf);
     }
-    // Persistent: as many CTAs as fit on the GPU at once, each walking the
-    // tiles with a grid stride and prefetching its next tile.
     template <int MODE>
     static void col(const Geom &g, const CUtensorMap &in, const CUtensorMap &out,
                     const int *units, int nunits, const Fresnel &fr, float scale, cudaStream_t s)
     {
         static std::once_flag f;
-        static int resident = 0;
         set_smem(k_col_pass<N, MODE>, Smem<N>::col, f);
-        static std::once_flag fr_once;
-        std::call_once(fr_once, [] {
-            int dev = 0, sms = 0, per = 0;
-            cudaGetDevice(&dev);
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_col_pass<N, MODE>,
-                                                          ColCfg<N>::NT, Smem<N>::col);
-            resident = std::max(1, sms * std::max(per, 1));
-        });
-        const int ntiles = nunits * (g.ny / ColCfg<N>::C);
-        const int grid = std::min(ntiles, resident);
-        if (grid <= 0) return;
-        k_col_pass<N, MODE><<<grid, ColCfg<N>::NT, Smem<N>::col, s>>>(g, in, out, units, ntiles,
-                                                                     fr, scale);
+        const int C = ColCfg<N>::C;
+        k_col_pass<N, MODE><<<nunits * (g.ny / C), ColCfg<N>::NT, Smem<N>::col, s>>>(
+            g, in, out, units, fr, scale);
     }
     static void col_mask(const Geom &g, const CUtensorMap &in, const CUtensorMap &out,
                          const int *units, int nunits, cudaStream_t s)

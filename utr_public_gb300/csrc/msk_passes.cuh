@@ -76,9 +76,10 @@ __device__ __forceinline__ void cta_drain(uint64_t *bar, uint32_t parity)
 }
 
 // Resident CTAs per SM the column pass is compiled for (its register budget):
-// three double-buffered CTAs per SM (168 registers a thread at 128 threads).
+// the propagator pass fits 128 registers, the band-limit and free-space
+// passes need ~168 to stay free of spills at 1024 points.
 template <int NX, int MODE> struct ColMinBlocks {
-    static constexpr int per = 384 / ColCfg<NX>::NT;
+    static constexpr int per = (MODE == 1 ? 512 : 384) / ColCfg<NX>::NT;
     static constexpr int value = per > 0 ? per : 1;
 };
 
@@ -231,102 +232,83 @@ enum { kColMask = 0, kColProp = 1, kColFresnel = 2 };
 template <int NX, int MODE>
 __global__ void __launch_bounds__(ColCfg<NX>::NT, ColMinBlocks<NX, MODE>::value)
 k_col_pass(const Geom g, const __grid_constant__ CUtensorMap in_map,
-           const __grid_constant__ CUtensorMap out_map, const int *__restrict__ units, int ntiles,
+           const __grid_constant__ CUtensorMap out_map, const int *__restrict__ units,
            const Fresnel fr, float fscale)
 {
     using P = FftPlan<NX>;
     using CC = ColCfg<NX>;
     constexpr int T = P::T, E = P::E, C = CC::C;
     extern __shared__ __align__(128) unsigned char smem[];
-    float2 *bufs = reinterpret_cast<float2 *>(smem);                         // 2 x PADN*C
-    uint64_t *bar = reinterpret_cast<uint64_t *>(bufs + 2 * P::PADN * C);   // 2 barriers
+    float2 *buf = reinterpret_cast<float2 *>(smem);                       // PADN*C
+    uint64_t *bar = reinterpret_cast<uint64_t *>(buf + P::PADN * C);
 
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
     const int ny = g.ny;
     const int bpu = ny / C;
-    // tile tau: unit units[tau / bpu] (or tau / bpu), columns (tau % bpu)*C ..
-    auto tile_row = [&](int tau) { return (units ? units[tau / bpu] : tau / bpu) * NX; };
-    auto tile_x = [&](int tau) { return 2 * (tau % bpu) * C; };
-    auto issue_load = [&](int tau, int b) {
-        mbar_arrive_expect_tx(&bar[b], CC::TILE_BYTES);
-        const int y0 = tile_row(tau), x = tile_x(tau);
-#pragma unroll
-        for (int j = 0; j < CC::NBOX; j++)
-            tma_load_2d(bufs + b * P::PADN * C + j * CC::BR * C, &in_map, x, y0 + j * CC::BR, &bar[b]);
-    };
+    const int u = units ? units[blockIdx.x / bpu] : (int)(blockIdx.x / bpu);
+    const int cb = blockIdx.x % bpu;
+    const int iy = cb * C + c;
+    // tile = rows u*NX .. u*NX+NX-1, float columns 2*cb*C .. 2*cb*C+2C-1
     if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        mbar_init(bar, 1);
         fence_mbar_init();
     }
     __syncthreads();
-    int tau = blockIdx.x;
-    if (tid == 0 && tau < ntiles) issue_load(tau, 0);
-    for (int k = 0; tau < ntiles; k++, tau += gridDim.x) {
-        const int cur = k & 1;
-        float2 *buf = bufs + cur * P::PADN * C;
-        // prefetch the next tile into the other buffer once the store that
-        // last read it is done reading
-        if (tid == 0 && tau + (int)gridDim.x < ntiles) {
-            bulk_wait_read();
-            issue_load(tau + gridDim.x, cur ^ 1);
-        }
-        if (!cta_wait(&bar[cur], (k >> 1) & 1, g.err)) {
-            if (tid == 0) {
-                (void)mbar_wait(&bar[cur ^ 1], ((k + 1) >> 1) & 1);  // the prefetch, if any
-                bulk_wait_read();
-            }
-            __syncthreads();
-            return;
-        }
-        const int iy = (tau % bpu) * C + c;
-        float2 v[E];
+    if (tid == 0) {
+        mbar_arrive_expect_tx(bar, CC::TILE_BYTES);
 #pragma unroll
-        for (int m = 0; m < E; m++) v[m] = buf[(t + m * T) * C + c];
-        fft_line<NX, false, C, true>(v, buf, c, t, g.tw_col);
-
-        if constexpr (MODE == kColMask) {
-            // the band limit ky2 + kx2 < k2max keeps ix <= A or ix >= B (host-exact)
-            const int2 ab = __ldg(&g.kband[iy]);
-#pragma unroll
-            for (int m = 0; m < E; m++) {
-                const int ix = t + m * T;
-                v[m] = (ix <= ab.x || ix >= ab.y) ? cscale(v[m], fscale) : make_float2(0.0f, 0.0f);
-            }
-        } else if constexpr (MODE == kColProp) {
-            // kx2 < k2max and kx2 + ky2 < k2max: the same index set as the band limit
-            const int2 ab = __ldg(&g.kband[iy]);
-            const float2 py = __ldg(&g.propy[iy]);
-#pragma unroll
-            for (int m = 0; m < E; m++) {
-                const int ix = t + m * T;
-                if (ix <= ab.x || ix >= ab.y) {
-                    const float2 w = cmul(cmul(v[m], py), __ldg(&g.propx[ix]));
-                    v[m] = cscale(w, fscale);
-                } else {
-                    v[m] = make_float2(0.0f, 0.0f);
-                }
-            }
-        } else {
-            const float2 *tab = fr.table + iy;
-#pragma unroll
-            for (int m = 0; m < E; m++) v[m] = cmul(v[m], __ldg(&tab[(size_t)(t + m * T) * ny]));
-        }
-        fft_line<NX, true, C, true>(v, buf, c, t, g.tw_col);
-        __syncthreads();  // every thread is done with the exchange layout
-#pragma unroll
-        for (int m = 0; m < E; m++) buf[(t + m * T) * C + c] = v[m];
-        fence_proxy_async();
-        __syncthreads();
-        if (tid == 0) {
-            const int y0 = tile_row(tau), x = tile_x(tau);
-#pragma unroll
-            for (int j = 0; j < CC::NBOX; j++)
-                tma_store_2d(&out_map, x, y0 + j * CC::BR, buf + j * CC::BR * C);
-            bulk_commit();
-        }
+        for (int j = 0; j < CC::NBOX; j++)
+            tma_load_2d(buf + j * CC::BR * C, &in_map, 2 * cb * C, u * NX + j * CC::BR, bar);
     }
-    if (tid == 0) bulk_wait_all();
+    if (!cta_wait(bar, 0, g.err)) {
+        cta_drain(bar, 0);
+        return;
+    }
+    float2 v[E];
+#pragma unroll
+    for (int m = 0; m < E; m++) v[m] = buf[(t + m * T) * C + c];
+    fft_line<NX, false, C, true>(v, buf, c, t, g.tw_col);
+
+    if constexpr (MODE == kColMask) {
+        // the band limit ky2 + kx2 < k2max keeps ix <= A or ix >= B (host-exact)
+        const int2 ab = __ldg(&g.kband[iy]);
+#pragma unroll
+        for (int m = 0; m < E; m++) {
+            const int ix = t + m * T;
+            v[m] = (ix <= ab.x || ix >= ab.y) ? cscale(v[m], fscale) : make_float2(0.0f, 0.0f);
+        }
+    } else if constexpr (MODE == kColProp) {
+        // kx2 < k2max and kx2 + ky2 < k2max: the same index set as the band limit
+        const int2 ab = __ldg(&g.kband[iy]);
+        const float2 py = cscale(__ldg(&g.propy[iy]), 1.0f);
+#pragma unroll
+        for (int m = 0; m < E; m++) {
+            const int ix = t + m * T;
+            if (ix <= ab.x || ix >= ab.y) {
+                const float2 w = cmul(cmul(v[m], py), __ldg(&g.propx[ix]));
+                v[m] = cscale(w, fscale);
+            } else {
+                v[m] = make_float2(0.0f, 0.0f);
+            }
+        }
+    } else {
+        const float2 *tab = fr.table + iy;
+#pragma unroll
+        for (int m = 0; m < E; m++) v[m] = cmul(v[m], __ldg(&tab[(size_t)(t + m * T) * ny]));
+    }
+    fft_line<NX, true, C, true>(v, buf, c, t, g.tw_col);
+    __syncthreads();  // every thread is done with the exchange layout
+#pragma unroll
+    for (int m = 0; m < E; m++) buf[(t + m * T) * C + c] = v[m];
+    fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+#pragma unroll
+        for (int j = 0; j < CC::NBOX; j++)
+            tma_store_2d(&out_map, 2 * cb * C, u * NX + j * CC::BR, buf + j * CC::BR * C);
+        bulk_commit();
+        bulk_wait_read();
+    }
 }
 
 // ---------------------------------------------------------------- P3
