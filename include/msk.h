@@ -36,7 +36,8 @@ enum {
     MSK_ENOMEM = -5,       /* device or host allocation failed */
     MSK_EUNSUPPORTED = -6, /* grid size or mode this library does not provide */
     MSK_ECUDA = -7,        /* a CUDA call failed; msk_last_error() has the text */
-    MSK_EINVAL = -8        /* bad argument (null pointer, negative count, ...) */
+    MSK_EINVAL = -8,       /* bad argument (null pointer, negative count, ...) */
+    MSK_ETOOLARGE = -9     /* beyond the fixed scratch of msk_calculate_static */
 };
 
 /* param[] offsets read by autoslic::calculate (slicelib.hpp:142-240). */
@@ -117,6 +118,26 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
                     int nangles, const double *angleZ, const double *angleY, int ndefocus,
                     const double *defocus, int nconfig, const float *displacements,
                     float *images, float *exitwaves, int *kept);
+
+/* calculate() without any allocation -- no counterpart in the reference.
+ * For callers that cannot allocate device memory (a plug-in inside a host
+ * framework that owns all device memory through its own pool, or a loop that
+ * cannot take cudaMalloc's latency and implicit synchronisation).  Same
+ * arguments and result as msk_calculate, minus the context, plus the CUDA
+ * stream to run on (NULL: the legacy default stream); host pointers; blocks
+ * until pix is written.  Its device scratch is a fixed 8.04 MiB array in this
+ * library, held by every GPU that loads it until the process exits.
+ * Limits: nx*ny <= 512*512, natom <= 65536, <= 4096 slices; beyond them it
+ * returns MSK_ETOOLARGE.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) with that device current; make that
+ * first call before any stream capture.  Every call reuses the same array and
+ * leaves its contents behind (each call initialises what it reads), so calls
+ * that overlap on the GPU -- from two host threads or on two streams -- race
+ * and corrupt each other's results: serialise them. */
+int msk_calculate_static(void *stream, float *pix, const float *wave0, const float *param,
+                         int natom, const int *Znum, const float *x, const float *y,
+                         const float *z, const float *occ, float ctblength, float ctblengthz,
+                         int nmode);
 
 /* Use the caller's CUDA stream (a cudaStream_t) for this context's work
  * instead of the context's own; NULL restores the context's stream. */

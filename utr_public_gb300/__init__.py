@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(PKG, "libmsk.so")
 
 # status codes (include/msk.h)
 MSK_OK, MSK_EBADSIZE, MSK_EBOX, MSK_EZSORT, MSK_EZNUM = 0, -1, -2, -3, -4
-MSK_ENOMEM, MSK_EUNSUPPORTED, MSK_ECUDA, MSK_EINVAL = -5, -6, -7, -8
+MSK_ENOMEM, MSK_EUNSUPPORTED, MSK_ECUDA, MSK_EINVAL, MSK_ETOOLARGE = -5, -6, -7, -8, -9
 
 # param[] offsets (slicelib.hpp:142-240)
 pXCTILT, pYCTILT, pENERGY, pOAPERT, pDELTAZ = 9, 10, 16, 17, 30
@@ -26,7 +26,7 @@ NPARAM = 200
 EXPORTS = ("msk_create", "msk_destroy", "msk_last_error", "msk_status_string", "msk_calculate",
            "msk_tilt_series", "msk_slice_count", "msk_slice_assign", "msk_sort_by_z",
            "msk_rotate", "msk_potential_table", "msk_set_stream", "msk_profile",
-           "msk_profile_read")
+           "msk_profile_read", "msk_calculate_static")
 
 
 class MskError(RuntimeError):
@@ -93,6 +93,8 @@ def load():
     L.msk_set_stream.argtypes = [vp, vp]
     L.msk_profile.argtypes = [vp, C.c_int]
     L.msk_profile_read.argtypes = [vp, C.POINTER(KernelStat), C.c_int]
+    L.msk_calculate_static.argtypes = [vp, vp, vp, _fp, C.c_int, vp, vp, vp, vp, vp, C.c_float,
+                                       C.c_float, C.c_int]
     _lib = L
     return L
 
@@ -147,6 +149,31 @@ def potential_table(Z):
     if st:
         raise MskError(st, "bad atomic number")
     return knots, coef.reshape(100, 4)
+
+
+def calculate_static(param, Znum, x, y, z, occ, ctblength, ctblengthz, nmode=0, wave0=None,
+                     stream=None):
+    """calculate() through msk_calculate_static, the entry point that allocates
+    no device memory (for callers whose device memory is owned by someone
+    else).  Its scratch is a fixed array inside libmsk.so, shared by every
+    call: calls must not overlap.  Limits: nx*ny <= 512*512, 65536 atoms,
+    4096 slices (MskError with MSK_ETOOLARGE beyond them)."""
+    L = load()
+    param = np.ascontiguousarray(param, np.float32)
+    nx, ny = int(param[pNX] + 0.1), int(param[pNY] + 0.1)
+    if wave0 is None:
+        wave0 = np.zeros((nx, ny, 2), np.float32)
+        wave0[..., 0] = 1.0
+    wave0 = np.ascontiguousarray(wave0, np.float32)
+    pix = np.zeros((nx, ny, 2), np.float32)
+    arrs = [np.ascontiguousarray(a, dt) for a, dt in
+            ((Znum, np.int32), (x, np.float32), (y, np.float32), (z, np.float32),
+             (occ, np.float32))]
+    st = L.msk_calculate_static(stream, _ptr(pix), _ptr(wave0), param, len(arrs[1]),
+                                *[_ptr(a) for a in arrs], ctblength, ctblengthz, nmode)
+    if st:
+        raise MskError(st, L.msk_status_string(st).decode())
+    return pix
 
 
 # ------------------------------------------------------------------ context

@@ -1070,6 +1070,7 @@ const char *msk_status_string(int st)
     case MSK_EUNSUPPORTED: return "unsupported grid size or mode";
     case MSK_ECUDA: return "CUDA error";
     case MSK_EINVAL: return "invalid argument";
+    case MSK_ETOOLARGE: return "beyond the fixed scratch limits of msk_calculate_static";
     default: return "unknown status";
     }
 }
@@ -1451,3 +1452,152 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ allocation-free calculate()
+//
+// msk_calculate_static: calculate() for callers that cannot allocate device
+// memory -- a plug-in whose host framework owns all device memory through
+// its own pool, or a latency-critical loop where a cudaMalloc (and the
+// synchronisation it implies) is not acceptable.  It creates no context, no
+// stream, no event and no device buffer: its device scratch is one fixed
+// array compiled into this library, which every GPU that loads the library
+// holds until the process exits.  Limits (MSK_ETOOLARGE beyond them):
+// nx*ny <= 512*512 pixels, natom <= 65536, at most 4096 slices.
+namespace {
+
+constexpr size_t kStaticPixels = 512 * 512;
+constexpr int kStaticAtoms = 65536;
+constexpr int kStaticSlices = 4096;
+// regions of the scratch, 256-byte aligned
+constexpr size_t kSGrid = kStaticPixels * sizeof(float2);          // 2 MiB
+constexpr size_t kSTables = (size_t)1 << 20;                          // 1 MiB
+constexpr size_t kSAtoms = (size_t)kStaticAtoms * sizeof(SplatAtom);  // 1 MiB
+constexpr size_t kSSliceOff = 20 << 10;
+constexpr size_t kSAct = 20 << 10;
+constexpr size_t kSFlags = 256;
+constexpr size_t kOffPsi = 0, kOffTbuf = kOffPsi + kSGrid, kOffWave0 = kOffTbuf + kSGrid,
+                 kOffTables = kOffWave0 + kSGrid, kOffAtoms = kOffTables + kSTables,
+                 kOffSliceOff = kOffAtoms + kSAtoms, kOffAct = kOffSliceOff + kSSliceOff,
+                 kOffFlags = kOffAct + kSAct, kStaticBytes = kOffFlags + kSFlags;
+
+}  // namespace
+
+// The scratch of msk_calculate_static.  Host code cannot use this name as a
+// device address: its address comes from cudaGetSymbolAddress, per device.
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
+
+namespace {
+
+struct StaticScratch {
+    std::once_flag once;
+    void *ptr = nullptr;
+    cudaError_t err = cudaSuccess;
+};
+constexpr int kStaticDevices = 64;
+StaticScratch g_static[kStaticDevices];
+
+// Bytes upload_tables() needs for this grid (its 256-byte aligned pieces).
+size_t static_table_bytes(int nx, int ny, int nz)
+{
+    auto a = [](size_t b) { return (b + 255) & ~size_t(255); };
+    std::vector<float2> t;
+    twiddles(nx, t);
+    const size_t twc = t.size();
+    twiddles(ny, t);
+    const size_t twr = t.size();
+    return a(4 * (size_t)nx) * 2 + a(4 * (size_t)ny) * 2 + a(8 * (size_t)nx) + a(8 * (size_t)ny) +
+           a(8 * twr) + a(8 * twc) + a(4 * phys::kN) + a(16 * (size_t)std::max(nz, 1) * phys::kN) +
+           a(8 * (size_t)ny);
+}
+
+}  // namespace
+
+extern "C" int msk_calculate_static(void *stream, float *pix, const float *wave0,
+                                    const float *param, int natom, const int *Znum,
+                                    const float *x, const float *y, const float *z,
+                                    const float *occ, float ctblength, float ctblengthz, int nmode)
+{
+    if (!pix || !wave0 || !param || natom < 0 || (natom > 0 && (!Znum || !x || !y || !z || !occ)))
+        return MSK_EINVAL;
+    const float ax = param[MSK_pAX], by = param[MSK_pBY];
+    const int nx = (int)(param[MSK_pNX] + 0.1F), ny = (int)(param[MSK_pNY] + 0.1F);
+    if (nx < 1 || ny < 1 || ax < 0.0 || by < 0.0) return MSK_EBADSIZE;
+    if (!pow2_supported(nx) || !pow2_supported(ny)) return MSK_EUNSUPPORTED;
+    const int nslices = slice_count(param[MSK_pDELTAZ], ctblengthz);
+    if ((size_t)nx * ny > kStaticPixels || natom > kStaticAtoms || nslices > kStaticSlices)
+        return MSK_ETOOLARGE;
+
+    // once per device, with that device current: the array's device address
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kStaticDevices) return MSK_ECUDA;
+    StaticScratch &sc = g_static[dev];
+    std::call_once(sc.once, [&] { sc.err = cudaGetSymbolAddress(&sc.ptr, g_static_scratch); });
+    if (sc.err != cudaSuccess || !sc.ptr) return MSK_ECUDA;
+
+    // A context on the stack whose buffers are views of the scratch; with
+    // every view as large as the call needs, no reserve() below allocates.
+    msk_context ctx;
+    ctx.device = dev;
+    ctx.stream = (cudaStream_t)stream;
+    unsigned char *base = static_cast<unsigned char *>(sc.ptr);
+    auto view = [&](DevBuf &b, size_t off, size_t bytes) {
+        b.p = base + off;
+        b.cap = bytes;
+    };
+    view(ctx.psi, kOffPsi, kSGrid);
+    view(ctx.tbuf, kOffTbuf, kSGrid);
+    view(ctx.wave0, kOffWave0, kSGrid);
+    view(ctx.tables, kOffTables, kSTables);
+    view(ctx.atoms, kOffAtoms, kSAtoms);
+    view(ctx.slice_off, kOffSliceOff, kSSliceOff);
+    view(ctx.act, kOffAct, kSAct);
+    view(ctx.flags, kOffFlags, kSFlags);
+    // ctx.tbuf2 stays empty: the slice loop then runs in order on `stream`
+
+    GridPre gp;
+    if (!grid_pre(gp, nx, ny, ax, by, param[MSK_pENERGY], param[MSK_pDELTAZ], param[MSK_pXCTILT],
+                  param[MSK_pYCTILT]))
+        return MSK_EUNSUPPORTED;
+    if (natom > 0) {  // the reference's range check first (autoslic.cpp:270-299)
+        float xmin = x[0], xmax = x[0], ymin = y[0], ymax = y[0], zmin = z[0], zmax = z[0];
+        for (int i = 0; i < natom; i++) {
+            xmin = std::min(xmin, x[i]);
+            xmax = std::max(xmax, x[i]);
+            ymin = std::min(ymin, y[i]);
+            ymax = std::max(ymax, y[i]);
+            zmin = std::min(zmin, z[i]);
+            zmax = std::max(zmax, z[i]);
+        }
+        if (xmin < 0 || ymin < 0 || zmin < 0 || xmax > ctblength || ymax > ctblength ||
+            zmax > ctblengthz)
+            return MSK_EBOX;
+    }
+    std::vector<int> zlist;
+    int st = build_zmap(&ctx, natom, Znum, zlist);
+    if (st) return st;
+    if (static_table_bytes(nx, ny, (int)zlist.size()) > kSTables) return MSK_ETOOLARGE;
+    std::vector<UnitAtoms> ua(1);
+    PrepSpec ps{natom, Znum, x, y, z, occ, ctblength, ctblengthz, param[MSK_pDELTAZ], nslices,
+                false, 0, 0, 0, 0, 0, nullptr, false, ctx.zmap.data()};
+    prep_unit(gp, ps, ua[0]);
+    if (ua[0].status) return ua[0].status;
+    if ((st = upload_tables(&ctx, gp, zlist))) return st;
+    Batch b;
+    if ((st = upload_batch(&ctx, ua, 0, 1, nslices, b))) return st;
+    ctx.units_alloc = 1;
+    // the device error flag is the only scratch a call reads before writing
+    if ((st = flags_reset(&ctx, gp.g))) return st;
+    const size_t plane = (size_t)nx * ny;
+    if (cudaMemcpyAsync(ctx.wave0.p, wave0, plane * sizeof(float2), cudaMemcpyHostToDevice,
+                        ctx.stream) != cudaSuccess)
+        return MSK_ECUDA;
+    const SizeOps *rop = size_ops(ny);
+    rop->row_init(gp.g, nullptr, 1, ctx.wave0.as<float2>(), ctx.psi.as<float2>(), 1.0f, ctx.stream);
+    if ((st = run_slices(&ctx, gp, b, nmode))) return st;
+    rop->row_exit(gp.g, nullptr, 1, ctx.psi.as<float2>(), ctx.tbuf.as<float2>(), ctx.stream);
+    if (cudaGetLastError() != cudaSuccess) return MSK_ECUDA;
+    if (cudaMemcpyAsync(pix, ctx.tbuf.p, plane * sizeof(float2), cudaMemcpyDeviceToHost,
+                        ctx.stream) != cudaSuccess)
+        return MSK_ECUDA;
+    return flags_check(&ctx);
+}
