@@ -192,6 +192,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-check", action="store_true")
+    ap.add_argument("--no-per-angle", action="store_true")
     ap.add_argument("--orientations", type=int, default=NANG,
                     help="orientations per step (180 for the headline workload)")
     ap.add_argument("--profile-run", action="store_true",
@@ -296,6 +297,30 @@ def main():
     if rank == 0:
         same = torch.equal(host_images, images.cpu())
 
+    # the per-orientation comparison form (cuFFT, unfused kernels, one orientation
+    # at a time) on a subset of the same orientations
+    per_angle = None
+    if not args.no_per_angle:
+        sub = np.linspace(0, nang - 1, min(12, nang)).astype(int)
+        pa_imgs = torch.empty((len(sub), len(defoci), NX, NX), dtype=torch.float32, device="cuda")
+        try:
+            ctx.tilt_series_per_angle(s, *atoms, angZ[sub[:1]], angY[sub[:1]], defoci,
+                                      images=pa_imgs[:1])
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.tilt_series_per_angle(s, *atoms, angZ[sub], angY[sub], defoci, images=pa_imgs)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            pa_ms = e0.elapsed_time(e1)
+            pa_val = len(sub) * nslices / (pa_ms / 1000.0)
+            same = float(torch.linalg.norm(pa_imgs - images[sub]) / torch.linalg.norm(images[sub]))
+            per_angle = {"value": pa_val, "unit": UNIT, "orientations_timed": int(len(sub)),
+                         "ms": pa_ms, "batched_over_per_angle": value / pa_val,
+                         "images_rel_l2_vs_batched": same}
+        except Exception as ex:  # reported, not fatal
+            per_angle = {"error": repr(ex)}
+
     kernels = {k: v for k, v in prof.items() if not k.startswith("copy_")}
     launches = int(sum(v[0] for v in kernels.values())) * args.steps
     dom = max(kernels, key=lambda k: kernels[k][1])
@@ -355,6 +380,7 @@ def main():
         "kernels": {k: {"launches": v[0], "ms": round(v[1], 3),
                         "GBps": round(v[2] / (v[1] / 1000.0) / 1e9, 1) if v[1] > 0 else None}
                     for k, v in kernels.items()},
+        "per_angle_gpu": per_angle,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "peak_source": peak_kind, "traffic": traffic,

@@ -159,6 +159,20 @@ typedef struct {
 int msk_profile(msk_context *ctx, int enable);
 int msk_profile_read(msk_context *ctx, msk_kernel_stat *out, int max);
 
+/* The same tilt series (same arguments except exit waves, same results within
+ * rounding) computed as a direct GPU port of the reference's loop would:
+ * orientation by orientation (MultisliceT.cpp:403-448 runs one host thread
+ * per orientation), per slice an atomic scatter of the potential
+ * (autoslic.cpp:950-984), unfused element-wise kernels and library 2D FFTs
+ * (cuFFT, loaded at run time: MSK_EUNSUPPORTED if it cannot be), a
+ * synchronisation after every orientation.  The comparison form for the
+ * batched msk_tilt_series. */
+int msk_tilt_series_per_angle(msk_context *ctx, const msk_series *s, int natom, const int *Znum,
+                              const float *x, const float *y, const float *z, const float *occ,
+                              int nangles, const double *angleZ, const double *angleY,
+                              int ndefocus, const double *defocus, int nconfig,
+                              const float *displacements, float *images, int *kept);
+
 /* Number of slice-steps calculate() runs for a box of depth ctblengthz
  * (autoslic.cpp:747-830: zslice = dz, dz + dz, ... while < ctblengthz + dz). */
 int msk_slice_count(float deltaz, float ctblengthz);

@@ -192,3 +192,21 @@ def test_full_grid_thin_slab(ctx, msk, oracle):
     pix = ctx.calculate(param, *atoms, 160.0, 8.0)
     ref64 = oracle.calculate(param, *atoms, 160.0, 8.0, fp64=True)
     assert rel_l2(pix, ref64) < 1e-5
+
+
+def test_per_angle_form_matches_batched(ctx, msk, oracle):
+    """The per-orientation comparison form computes the same images."""
+    spec = sp.random_specimen(500, 64.0, 10.0, 54.0, 1014)
+    atoms = (spec.Znum, spec.x, spec.y, spec.z, spec.occ)
+    angY = np.deg2rad([0.0, 33.0, 71.0])
+    angZ = np.array([0.0, 0.2, 0.0])
+    defoci = np.array([0.0, 250.0])
+    s = series(msk, 128, 64.0, 300.0, 1.0, 0.02, 0.0)
+    imgs, _ = ctx.tilt_series(s, *atoms, angZ, angY, defoci)
+    pa, _ = ctx.tilt_series_per_angle(s, *atoms, angZ, angY, defoci)
+    sp64 = oracle_series(oracle, 128, 64.0, 300.0, 1.0, 0.02, 0.0)
+    for a in range(3):
+        ref, _ = oracle.orientation(sp64, *atoms, angZ[a], angY[a], defoci, fp64=True)
+        for d in range(2):
+            assert rel_l2(pa[a, d], ref[d]) < 1e-5
+            assert rel_l2(imgs[a, d], pa[a, d]) < 1e-5

@@ -26,7 +26,7 @@ NPARAM = 200
 EXPORTS = ("msk_create", "msk_destroy", "msk_last_error", "msk_status_string", "msk_calculate",
            "msk_tilt_series", "msk_slice_count", "msk_slice_assign", "msk_sort_by_z",
            "msk_rotate", "msk_potential_table", "msk_set_stream", "msk_profile",
-           "msk_profile_read", "msk_calculate_static")
+           "msk_profile_read", "msk_calculate_static", "msk_tilt_series_per_angle")
 
 
 class MskError(RuntimeError):
@@ -93,6 +93,8 @@ def load():
     L.msk_set_stream.argtypes = [vp, vp]
     L.msk_profile.argtypes = [vp, C.c_int]
     L.msk_profile_read.argtypes = [vp, C.POINTER(KernelStat), C.c_int]
+    L.msk_tilt_series_per_angle.argtypes = [vp, C.POINTER(Series), C.c_int, vp, vp, vp, vp, vp,
+                                            C.c_int, _dp, _dp, C.c_int, vp, C.c_int, vp, vp, vp]
     L.msk_calculate_static.argtypes = [vp, vp, vp, _fp, C.c_int, vp, vp, vp, vp, vp, C.c_float,
                                        C.c_float, C.c_int]
     _lib = L
@@ -266,3 +268,25 @@ class Context:
                                     _ptr(images), _ptr(exitwaves), _ptr(kept))
         self._check(st)
         return (images, exitwaves, kept) if want_exit or exitwaves is not None else (images, kept)
+
+    def tilt_series_per_angle(self, series, Znum, x, y, z, occ, angleZ, angleY, defocus,
+                              nconfig=1, displacements=None, images=None):
+        """The same tilt series through msk_tilt_series_per_angle (orientation by
+        orientation, cuFFT, unfused kernels): the comparison form."""
+        angleZ = np.ascontiguousarray(angleZ, np.float64)
+        angleY = np.ascontiguousarray(angleY, np.float64)
+        defocus = np.ascontiguousarray(defocus, np.float64)
+        na, nd = len(angleZ), len(defocus)
+        if images is None:
+            images = np.zeros((na, nd, series.nx, series.ny), np.float32)
+        kept = np.zeros(na * nconfig, np.int32)
+        arrs = [np.ascontiguousarray(a, dt) for a, dt in
+                ((Znum, np.int32), (x, np.float32), (y, np.float32), (z, np.float32),
+                 (occ, np.float32))]
+        disp = None if displacements is None else np.ascontiguousarray(displacements, np.float32)
+        st = self.L.msk_tilt_series_per_angle(self.h, C.byref(series), len(arrs[1]),
+                                              *[_ptr(a) for a in arrs], na, angleZ, angleY, nd,
+                                              _ptr(defocus), nconfig, _ptr(disp), _ptr(images),
+                                              _ptr(kept))
+        self._check(st)
+        return images, kept

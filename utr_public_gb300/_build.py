@@ -77,7 +77,7 @@ def build(verbose=False, jobs=None):
                 if verbose:
                     print("compiled", os.path.relpath(src, ROOT))
     if todo or _stale(LIB, objs):
-        cmd = [cc] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-cudart", "static"]
+        cmd = [cc] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-cudart", "static", "-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

@@ -17,6 +17,8 @@
 #include <vector>
 
 #include <cudaTypedefs.h>
+#include <cufft.h>
+#include <dlfcn.h>
 
 #include "msk.h"
 #include "msk_launch.cuh"
@@ -651,6 +653,7 @@ struct msk_context {
     std::string err;
     DevBuf psi, tbuf, tbuf2, atoms, slice_off, act, tables, imgmeta, wave0, images, exitw, fresnel,
         flags;
+    DevBuf pa_v, pa_t, pa_psi, pa_e;  // buffers of the per-orientation comparison form
     size_t units_alloc = 0;  // units the psi / tbuf buffers hold
     std::vector<int> zmap = std::vector<int>(104, -1);
 };
@@ -1046,7 +1049,7 @@ void msk_destroy(msk_context *ctx)
     for (cudaEvent_t e : ctx->prof_pool) cudaEventDestroy(e);
     for (DevBuf *b : {&ctx->psi, &ctx->tbuf, &ctx->tbuf2, &ctx->atoms, &ctx->slice_off, &ctx->act, &ctx->tables,
                       &ctx->imgmeta, &ctx->wave0, &ctx->images, &ctx->exitw, &ctx->fresnel,
-                      &ctx->flags})
+                      &ctx->flags, &ctx->pa_v, &ctx->pa_t, &ctx->pa_psi, &ctx->pa_e})
         b->release();
     for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_join, ctx->ev_t[0], ctx->ev_t[1], ctx->ev_free[0],
                           ctx->ev_free[1]})
@@ -1600,4 +1603,251 @@ extern "C" int msk_calculate_static(void *stream, float *pix, const float *wave0
                         ctx.stream) != cudaSuccess)
         return MSK_ECUDA;
     return flags_check(&ctx);
+}
+
+// ------------------------------------------------------------------ per-orientation form
+//
+// msk_tilt_series_per_angle: the same tilt series computed the way a direct GPU
+// port of the reference would compute it -- one orientation at a time, one
+// launch sequence per slice with unfused kernels and library 2D FFTs (cuFFT,
+// loaded at run time), an atomic scatter for the potential, and a
+// synchronisation after every orientation (MultisliceT.cpp:403-448 runs one
+// host thread per orientation).  It is the comparison form for the batched
+// path; the batched path never uses cuFFT.
+namespace {
+
+struct CufftApi {
+    bool ok = false;
+    cufftResult (*plan2d)(cufftHandle *, int, int, cufftType) = nullptr;
+    cufftResult (*set_stream)(cufftHandle, cudaStream_t) = nullptr;
+    cufftResult (*exec_c2c)(cufftHandle, cufftComplex *, cufftComplex *, int) = nullptr;
+    cufftResult (*destroy)(cufftHandle) = nullptr;
+};
+
+const CufftApi &cufft_api()
+{
+    static CufftApi api;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        const char *names[] = {getenv("MSK_CUFFT_LIBRARY"), "libcufft.so.12", "libcufft.so",
+                               "/usr/local/cuda/lib64/libcufft.so.12",
+                               "/usr/local/cuda/targets/sbsa-linux/lib/libcufft.so.12",
+                               "/usr/local/cuda/targets/x86_64-linux/lib/libcufft.so.12"};
+        void *h = nullptr;
+        for (const char *n : names)
+            if (n && (h = dlopen(n, RTLD_NOW | RTLD_LOCAL))) break;
+        if (!h) return;
+        api.plan2d = reinterpret_cast<decltype(api.plan2d)>(dlsym(h, "cufftPlan2d"));
+        api.set_stream = reinterpret_cast<decltype(api.set_stream)>(dlsym(h, "cufftSetStream"));
+        api.exec_c2c = reinterpret_cast<decltype(api.exec_c2c)>(dlsym(h, "cufftExecC2C"));
+        api.destroy = reinterpret_cast<decltype(api.destroy)>(dlsym(h, "cufftDestroy"));
+        api.ok = api.plan2d && api.set_stream && api.exec_c2c && api.destroy;
+    });
+    return api;
+}
+
+}  // namespace
+
+namespace msk {
+
+// One thread per (atom, window pixel), atomically added: the reference's
+// trlayer loop (autoslic.cpp:950-984) run in parallel as written.
+__global__ void k_plain_splat(const Geom g, const SplatAtom *__restrict__ atoms, int a0, int na,
+                              float *v)
+{
+    const int W = 2 * g.idx + 1, H = 2 * g.idy + 1;
+    const long total = (long)na * W * H;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total;
+         i += (long)gridDim.x * blockDim.x) {
+        const int a = (int)(i / (W * H)), r = (int)(i % (W * H));
+        const int dxw = r / H - g.idx, dyw = r % H - g.idy;
+        const SplatAtom at = atoms[a0 + a];
+        const int ixo = (int)(at.meta & kMetaMask), iyo = (int)((at.meta >> kMetaBits) & kMetaMask);
+        const float dx = at.fx - (float)dxw * g.scalex_f, dy = at.fy - (float)dyw * g.scaley_f;
+        float rsq = dx * dx + dy * dy;
+        if (rsq <= 9.0f) {
+            rsq = fmaxf(rsq, g.rminsq);
+            const float4 *coef = g.coef + (at.meta >> (2 * kMetaBits)) * kKnots;
+            const int ix = (ixo + dxw) & (g.nx - 1), iy = (iyo + dyw) & (g.ny - 1);
+            atomicAdd(&v[(size_t)ix * g.ny + iy], at.occ * spline_vz(g, g.knots, coef, rsq));
+        }
+    }
+}
+
+__global__ void k_plain_exp(const float *__restrict__ v, float sigma, size_t n, float2 *t)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        float s, c;
+        sincosf(v[i] * sigma, &s, &c);
+        t[i] = make_float2(c, s);
+    }
+}
+
+// MODE 0: 2/3 band limit; MODE 1: propagator with the 2/3 aperture
+template <int MODE>
+__global__ void k_plain_kmul(const Geom g, float scale, float2 *w)
+{
+    const size_t n = (size_t)g.nx * g.ny;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int ix = (int)(i / g.ny), iy = (int)(i % g.ny);
+        const int2 ab = g.kband[iy];
+        if (ix <= ab.x || ix >= ab.y) {
+            float2 x = w[i];
+            if (MODE == 1) x = cmul(cmul(x, g.propy[iy]), g.propx[ix]);
+            w[i] = cscale(x, scale);
+        } else {
+            w[i] = make_float2(0.0f, 0.0f);
+        }
+    }
+}
+
+__global__ void k_plain_mul(float2 *a, const float2 *__restrict__ b, size_t n)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        a[i] = cmul(a[i], b[i]);
+}
+
+__global__ void k_plain_fill(float2 *a, float2 val, size_t n)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        a[i] = val;
+}
+
+// image += |e|^2; after the last configuration, / nconf
+__global__ void k_plain_accum(const float2 *__restrict__ e, size_t n, int first, int last, float nconf,
+                              float *img)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float2 x = e[i];
+        float acc = x.x * x.x + x.y * x.y;
+        if (!first) acc = img[i] + acc;
+        img[i] = last ? __fdiv_rn(acc, nconf) : acc;
+    }
+}
+
+}  // namespace msk
+
+extern "C" int msk_tilt_series_per_angle(msk_context *ctx, const msk_series *s, int natom,
+                                         const int *Znum, const float *x, const float *y,
+                                         const float *z, const float *occ, int nangles,
+                                         const double *angleZ, const double *angleY,
+                                         int ndefocus, const double *defocus, int nconfig,
+                                         const float *displacements, float *images, int *kept)
+{
+    if (!ctx) return MSK_EINVAL;
+    ctx->err.clear();
+    if (!s || natom < 0 || nangles < 1 || ndefocus < 0 || nconfig < 1 || !angleZ || !angleY ||
+        (ndefocus > 0 && (!defocus || !images)) ||
+        (natom > 0 && (!Znum || !x || !y || !z || !occ)) || (nconfig > 1 && !displacements))
+        return fail(ctx, MSK_EINVAL, "bad tilt-series arguments");
+    const int nx = s->nx, ny = s->ny;
+    if (!pow2_supported(nx) || !pow2_supported(ny))
+        return fail(ctx, MSK_EUNSUPPORTED, "grid must be a power of two from 16 to 4096");
+    const CufftApi &fft = cufft_api();
+    if (!fft.ok) return fail(ctx, MSK_EUNSUPPORTED, "cuFFT could not be loaded");
+    MSK_CUDA(ctx, cudaSetDevice(ctx->device));
+    GridPre gp;
+    if (!grid_pre(gp, nx, ny, s->ctblength, s->ctblength, s->v0, s->deltaz, 0.0f, 0.0f))
+        return fail(ctx, MSK_EUNSUPPORTED, "band limit is not two index ranges per column");
+    const int nslices = slice_count(s->deltaz, s->ctblengthz);
+    std::vector<int> zlist;
+    int st = build_zmap(ctx, natom, Znum, zlist);
+    if (st) return st;
+    if ((st = upload_tables(ctx, gp, zlist))) return st;
+    const size_t plane = (size_t)nx * ny;
+    const Geom &g = gp.g;
+    cudaStream_t sm = ctx->stream;
+    MSK_CUDA(ctx, ctx->pa_v.reserve(plane * sizeof(float)));
+    MSK_CUDA(ctx, ctx->pa_t.reserve(plane * sizeof(float2)));
+    MSK_CUDA(ctx, ctx->pa_psi.reserve(plane * sizeof(float2)));
+    MSK_CUDA(ctx, ctx->pa_e.reserve(plane * sizeof(float2)));
+    MSK_CUDA(ctx, ctx->fresnel.reserve(plane * sizeof(float2) * std::max(ndefocus, 1)));
+    const bool img_dev = ndefocus > 0 && is_device_ptr(images);
+    const size_t img_bytes = (size_t)nangles * ndefocus * plane * sizeof(float);
+    float *d_images = images;
+    if (ndefocus > 0 && !img_dev) {
+        MSK_CUDA(ctx, ctx->images.reserve(img_bytes));
+        d_images = ctx->images.as<float>();
+    }
+    float *v = ctx->pa_v.as<float>();
+    float2 *t = ctx->pa_t.as<float2>(), *psi = ctx->pa_psi.as<float2>(), *e = ctx->pa_e.as<float2>();
+    // free-space multipliers (with 1/N) for every plane, once
+    const double pi = 4.0 * atan(1.0), l = gp.wavlen;
+    float k2maxo = s->aobj / gp.wavlen;
+    k2maxo = k2maxo * k2maxo;
+    for (int d = 0; d < ndefocus; d++) {
+        Fresnel fr{};
+        const double rprime = defocus[d] - 0.5 * s->ctblengthz;
+        fr.a1 = pi * l * rprime;
+        fr.a3 = (pi / 2.0) * s->cs3 * l * l * l;
+        fr.a5 = (pi / 3.0) * s->cs5 * l * l * l * l * l;
+        fr.a2c = (pi / 2.0) * l * s->astig * cos(2.0 * s->astig_angle);
+        fr.a2s = (pi / 2.0) * l * s->astig * sin(2.0 * s->astig_angle);
+        fr.k2maxo = k2maxo;
+        fr.kx = tables_kx(ctx, gp);
+        fr.ky = tables_ky(ctx, gp);
+        k_fresnel_table<<<4 * 152, 256, 0, sm>>>(g, fr, 1.0f / ((float)nx * (float)ny),
+                                                  ctx->fresnel.as<float2>() + (size_t)d * plane);
+    }
+    cufftHandle plan;
+    if (fft.plan2d(&plan, nx, ny, CUFFT_C2C) != CUFFT_SUCCESS)
+        return fail(ctx, MSK_ECUDA, "cufftPlan2d failed");
+    fft.set_stream(plan, sm);
+    auto FFT = [&](float2 *a, int dir) {  // cfpix::fft is the +1 kernel, ifft the -1 kernel
+        fft.exec_c2c(plan, reinterpret_cast<cufftComplex *>(a), reinterpret_cast<cufftComplex *>(a), dir);
+    };
+    const int G = 4 * 152, TB = 256;
+    const float invN = 1.0f / ((float)nx * (float)ny);
+    std::vector<UnitAtoms> ua(1);
+    int status = MSK_OK;
+    for (int u = 0; u < nangles * nconfig && status == MSK_OK; u++) {
+        const int a = u / nconfig, c = u % nconfig;
+        PrepSpec ps{natom, Znum, x, y, z, occ, s->ctblength, s->ctblengthz, s->deltaz, nslices, true,
+                    angleZ[a], angleY[a], s->dxc, s->dyc, s->dzc,
+                    displacements ? displacements + (size_t)c * 3 * natom : nullptr, true,
+                    ctx->zmap.data()};
+        prep_unit(gp, ps, ua[0]);
+        if (ua[0].status) {
+            status = fail(ctx, ua[0].status, msk_status_string(ua[0].status));
+            break;
+        }
+        if (kept) kept[u] = ua[0].kept;
+        Batch b;
+        if ((status = upload_batch(ctx, ua, 0, 1, nslices, b))) break;
+        k_plain_fill<<<G, TB, 0, sm>>>(psi, make_float2(1.0f, 0.0f), plane);
+        for (int sl = 0; sl < nslices; sl++) {
+            const int a0 = b.slice_off[sl], na = b.slice_off[sl + 1] - a0;
+            if (na > 0) {
+                cudaMemsetAsync(v, 0, plane * sizeof(float), sm);
+                k_plain_splat<<<G, TB, 0, sm>>>(g, ctx->atoms.as<SplatAtom>(), a0, na, v);
+                k_plain_exp<<<G, TB, 0, sm>>>(v, g.sigma_f, plane, t);
+                FFT(t, CUFFT_INVERSE);
+                k_plain_kmul<0><<<G, TB, 0, sm>>>(g, invN, t);
+                FFT(t, CUFFT_FORWARD);
+                k_plain_mul<<<G, TB, 0, sm>>>(psi, t, plane);
+            }
+            if (s->nmode == 0) {
+                FFT(psi, CUFFT_INVERSE);
+                k_plain_kmul<1><<<G, TB, 0, sm>>>(g, invN, psi);
+                FFT(psi, CUFFT_FORWARD);
+            }
+        }
+        for (int d = 0; d < ndefocus; d++) {
+            cudaMemcpyAsync(e, psi, plane * sizeof(float2), cudaMemcpyDeviceToDevice, sm);
+            FFT(e, CUFFT_INVERSE);
+            k_plain_mul<<<G, TB, 0, sm>>>(e, ctx->fresnel.as<float2>() + (size_t)d * plane, plane);
+            FFT(e, CUFFT_FORWARD);
+            k_plain_accum<<<G, TB, 0, sm>>>(e, plane, c == 0, c == nconfig - 1 && nconfig > 1,
+                                           (float)nconfig,
+                                           d_images + ((size_t)a * ndefocus + d) * plane);
+        }
+        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(sm) != cudaSuccess)
+            status = fail(ctx, MSK_ECUDA, "per-orientation form: CUDA error");
+    }
+    fft.destroy(plan);
+    if (status) return status;
+    if (ndefocus > 0 && !img_dev)
+        MSK_CUDA(ctx, cudaMemcpyAsync(images, d_images, img_bytes, cudaMemcpyDeviceToHost, sm));
+    MSK_CUDA(ctx, cudaStreamSynchronize(sm));
+    return MSK_OK;
 }
