@@ -173,6 +173,56 @@ int msk_tilt_series_per_angle(msk_context *ctx, const msk_series *s, int natom, 
                               int ndefocus, const double *defocus, int nconfig,
                               const float *displacements, float *images, int *kept);
 
+/* Multislice from given per-slice projected potentials, and its adjoint.
+ * The slice loop of calculate() (autoslic.cpp:838-861: transmission
+ * exp(i sigma v_k) band-limited to 2/3 kmax, wave *= trans, Fresnel
+ * propagator) with v_k supplied instead of splatted from atoms, from a plane
+ * wave psi_0 = 1, then the free-space step of msk_tilt_series to each
+ * detector plane and I = |psi|^2.  The adjoint returns dL/dv for the image
+ * misfit L = sum over units, planes, pixels of (I - target)^2; its backward
+ * pass keeps the wave every `checkpoint` slices and recomputes the waves
+ * inside a block from its checkpoint.  The reference has no adjoint. */
+typedef struct {
+    int nx, ny;            /* grid */
+    float ax, by;          /* cell size, Angstrom (param[pAX], param[pBY]) */
+    float v0;              /* beam energy, keV */
+    float deltaz;          /* slice thickness, Angstrom */
+    float ctiltx, ctilty;  /* crystal tilt, rad (param[pXCTILT], param[pYCTILT]) */
+    float aobj;            /* objective aperture semi-angle, rad (0: none) */
+    double cs3, cs5;       /* spherical aberrations, Angstrom */
+    int nslices;           /* slices per stack (>= 1) */
+    int checkpoint;        /* slices per checkpoint block of the adjoint (0: 8) */
+    int max_batch;         /* units in flight at once (0: as many as memory allows) */
+} msk_stack;
+
+/*   nunits independent stacks (orientations): v float[nunits][nslices][nx][ny]
+ *     in the potential units of the atom path (phase = sigma * v), host or device
+ *   ndefocus detector planes at distance defocus[d] (Angstrom) past the exit face
+ *   images out: float[nunits][ndefocus][nx][ny], host or device */
+int msk_stack_images(msk_context *ctx, const msk_stack *s, int nunits, const float *v,
+                     int ndefocus, const double *defocus, float *images);
+
+/*   target: float[nunits][ndefocus][nx][ny], host or device (ndefocus >= 1)
+ *   grad out: float[nunits][nslices][nx][ny] = dL/dv, host or device
+ *   loss out (may be NULL): L, summed in double in a fixed order */
+int msk_stack_adjoint(msk_context *ctx, const msk_stack *s, int nunits, const float *v,
+                      int ndefocus, const double *defocus, const float *target, float *grad,
+                      double *loss);
+
+/* The projected potential of every slice of every orientation of a tilt
+ * series, as the atom path splats it before the transmission exp(i sigma v)
+ * (trlayer, autoslic.cpp:917-984): orientations, box and slicing as in
+ * msk_tilt_series (s->nx, ny, ctblength, ctblengthz, deltaz, v0, dxc..dzc,
+ * max_batch are read).  Feeding v to msk_stack_images with defocus
+ * d - ctblengthz/2 gives msk_tilt_series's images.
+ *   v out: float[nangles][msk_slice_count(deltaz, ctblengthz)][nx][ny],
+ *          host or device
+ *   kept out (may be NULL): int[nangles], atoms inside the box */
+int msk_potential_stack(msk_context *ctx, const msk_series *s, int natom, const int *Znum,
+                        const float *x, const float *y, const float *z, const float *occ,
+                        int nangles, const double *angleZ, const double *angleY, float *v,
+                        int *kept);
+
 /* Number of slice-steps calculate() runs for a box of depth ctblengthz
  * (autoslic.cpp:747-830: zslice = dz, dz + dz, ... while < ctblengthz + dz). */
 int msk_slice_count(float deltaz, float ctblengthz);

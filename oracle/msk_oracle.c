@@ -407,14 +407,13 @@ static void trlayer_f32(const float *x, const float *y, const float *occ, const 
     cf_ifft_f(trans, nx, ny);
 }
 
-/* Same slice in double: potential summed in double, double transform. */
-static void trlayer_f64(const float *x, const float *y, const float *occ, const int *Znum,
-                        int natom, float ax, float by, float kev, double *trans, int nx, int ny,
-                        const float *kx2, const float *ky2, float k2max)
+/* Projected potential of one slice summed in double (the accumulation of
+ * trlayer, autoslic.cpp:950-984): v[(iy + ix*ny) * vstride], V*Angstrom. */
+static void potential_f64(const float *x, const float *y, const float *occ, const int *Znum,
+                          int natom, float ax, float by, double *v, size_t vstride, int nx,
+                          int ny)
 {
     const double rmax = 3.0, rmax2 = rmax * rmax;
-    double scale = mo_sigma(kev) / 1000.0;
-    double scalex = (double)ax / nx, scaley = (double)by / ny;
     double rmin = ax / ((double)nx);
     double r = by / ((double)ny);
     rmin = 0.25 * sqrt(0.5 * (rmin * rmin + r * r));
@@ -425,7 +424,7 @@ static void trlayer_f64(const float *x, const float *y, const float *occ, const 
     int idx = (int)(nx * rmax / ax) + 1;
     int idy = (int)(ny * rmax / by) + 1;
     size_t n = (size_t)nx * ny;
-    for (size_t j = 0; j < n; j++) trans[2 * j] = 0.0;
+    for (size_t j = 0; j < n; j++) v[j * vstride] = 0.0;
     for (int i = 0; i < natom; i++) {
         int ixo = (int)(x[i] / scalex_f), iyo = (int)(y[i] / scaley_f);
         for (int ix = ixo - idx; ix <= ixo + idx; ix++) {
@@ -442,13 +441,22 @@ static void trlayer_f64(const float *x, const float *y, const float *occ, const 
                     while (iyw < 0) iyw += ny;
                     iyw %= ny;
                     if (rsq < rminsq) rsq = rminsq;
-                    trans[2 * ((size_t)iyw + (size_t)ixw * ny)] += occ[i] * mo_vzatomLUT(Znum[i], rsq);
+                    v[((size_t)iyw + (size_t)ixw * ny) * vstride] +=
+                        occ[i] * mo_vzatomLUT(Znum[i], rsq);
                 }
             }
         }
     }
-    (void)scalex;
-    (void)scaley;
+}
+
+/* Same slice in double: potential summed in double, double transform. */
+static void trlayer_f64(const float *x, const float *y, const float *occ, const int *Znum,
+                        int natom, float ax, float by, float kev, double *trans, int nx, int ny,
+                        const float *kx2, const float *ky2, float k2max)
+{
+    double scale = mo_sigma(kev) / 1000.0;
+    size_t n = (size_t)nx * ny;
+    potential_f64(x, y, occ, Znum, natom, ax, by, trans, 2, nx, ny);
     for (size_t j = 0; j < n; j++) {
         double vz = scale * trans[2 * j];
         trans[2 * j] = cos(vz);
@@ -1011,4 +1019,268 @@ int mo_orientations_f32(const mo_series_params *sp, int nunits, int nthreads, in
     for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
     free(th);
     return j.status;
+}
+
+/* ------------------------------------------------ potential stacks and adjoint */
+
+/* Per-slice projected potentials of one orientation (FP64 sums): the
+ * atoms rotated and dropped as mo_orientation_*, sorted, and split into the
+ * slices of calculate() (autoslic.cpp:747-830); v[k][ix][iy] for
+ * k < mo_slice_count(deltaz, ctblengthz).  Returns atoms kept or a status. */
+int mo_orientation_potential_f64(const mo_series_params *sp, int natom, const int *Znum,
+                                 const float *x, const float *y, const float *z,
+                                 const float *occ, double angleZ, double angleY, double *v)
+{
+    float *xo, *yo, *zo, *oo;
+    int *Zo;
+    int kept = prep_orientation(sp, natom, Znum, x, y, z, occ, angleZ, angleY, NULL, &xo, &yo,
+                                &zo, &oo, &Zo);
+    float param[MO_NPARAM];
+    fill_param(sp, param);
+    calc_setup s;
+    int st = calc_setup_init(&s, param, kept, Zo, xo, yo, zo, sp->ax, sp->ctblengthz);
+    float *x2 = NULL, *y2 = NULL, *z2 = NULL, *occ2 = NULL;
+    int *Z2 = NULL;
+    if (st == MO_OK)
+        st = sorted_copy(kept, Zo, xo, yo, zo, oo, sp->ctblengthz, &x2, &y2, &z2, &occ2, &Z2);
+    if (st == MO_OK) {
+        const int nsl = mo_slice_count(sp->deltaz, sp->ctblengthz);
+        const size_t n = (size_t)sp->nx * sp->ny;
+        double zslice = s.deltaz;
+        int istart = 0;
+        for (int k = 0; k < nsl; k++) {
+            int na = 0;
+            for (int i = istart; i < kept; i++)
+                if (z2[i] < zslice) na++;
+                else break;
+            potential_f64(&x2[istart], &y2[istart], &occ2[istart], &Z2[istart], na, s.ax, s.by,
+                          v + (size_t)k * n, 1, s.nx, s.ny);
+            zslice += s.deltaz;
+            istart += na;
+        }
+    }
+    free(x2);
+    free(y2);
+    free(z2);
+    free(occ2);
+    free(Z2);
+    free(xo);
+    free(yo);
+    free(zo);
+    free(oo);
+    free(Zo);
+    setup_free(&s);
+    return st == MO_OK ? kept : st;
+}
+
+typedef struct {
+    int nx, ny;
+    size_t n;
+    double sigma;
+    double *M;        /* band limit 0/1 */
+    double *p;        /* propagator (complex) with the 2/3 aperture */
+    double *X;        /* ndef free-space multipliers (complex) */
+} stack_ops;
+
+static int stack_setup(const mo_stack_params *sp, int ndef, const double *rprime, stack_ops *o)
+{
+    float param[MO_NPARAM];
+    memset(param, 0, sizeof param);
+    param[MO_pAX] = sp->ax;
+    param[MO_pBY] = sp->by;
+    param[MO_pNX] = (float)sp->nx;
+    param[MO_pNY] = (float)sp->ny;
+    param[MO_pENERGY] = sp->v0;
+    param[MO_pDELTAZ] = sp->deltaz;
+    param[MO_pXCTILT] = sp->ctiltx;
+    param[MO_pYCTILT] = sp->ctilty;
+    calc_setup s;
+    int st = calc_setup_init(&s, param, 0, NULL, NULL, NULL, NULL, sp->ax, 1.0f);
+    if (st) { setup_free(&s); return st; }
+    const int nx = s.nx, ny = s.ny;
+    const size_t n = (size_t)nx * ny;
+    o->nx = nx;
+    o->ny = ny;
+    o->n = n;
+    o->sigma = mo_sigma(sp->v0) / 1000.0;
+    o->M = (double *)malloc(sizeof(double) * n);
+    o->p = (double *)malloc(sizeof(double) * 2 * n);
+    o->X = (double *)malloc(sizeof(double) * 2 * n * (ndef > 0 ? ndef : 1));
+    const double pi = 4.0 * atan(1.0);
+    float k2maxo = sp->aobj / s.wavlen;
+    k2maxo = k2maxo * k2maxo;
+    for (int ix = 0; ix < nx; ix++)
+        for (int iy = 0; iy < ny; iy++) {
+            const size_t i = (size_t)ix * ny + iy;
+            const int keep = (s.ky2[iy] + s.kx2[ix]) < s.k2max;
+            o->M[i] = keep ? 1.0 : 0.0;
+            double tx = pi * s.deltaz * ((double)s.kx2[ix] * s.wavlen - (double)s.kx[ix] * s.tctx);
+            double ty = pi * s.deltaz * ((double)s.ky2[iy] * s.wavlen - (double)s.ky[iy] * s.tcty);
+            /* (cos ty - i sin ty)(cos tx - i sin tx) = exp(-i (tx + ty)) */
+            o->p[2 * i] = keep ? cos(tx + ty) : 0.0;
+            o->p[2 * i + 1] = keep ? -sin(tx + ty) : 0.0;
+            for (int d = 0; d < ndef; d++) {
+                double *x = o->X + 2 * ((size_t)d * n + i);
+                float k2 = s.kx2[ix] + s.ky2[iy];
+                if (k2maxo > 0.0F && !(k2 < k2maxo)) {
+                    x[0] = x[1] = 0.0;
+                } else {
+                    double chi = chi_phase(s.kx[ix], s.ky[iy], s.wavlen, rprime[d], sp->cs3,
+                                           sp->cs5, 0.0, 0.0);
+                    x[0] = cos(chi);
+                    x[1] = -sin(chi);
+                }
+            }
+        }
+    setup_free(&s);
+    return MO_OK;
+}
+
+static void stack_free(stack_ops *o)
+{
+    free(o->M);
+    free(o->p);
+    free(o->X);
+}
+
+/* f <- K[m] f;  m complex (mc) or real (mr), conjugated if conj */
+static void kmul(const stack_ops *o, double *f, const double *mc, const double *mr, int conj)
+{
+    cf_fft_d(f, o->nx, o->ny);
+    for (size_t i = 0; i < o->n; i++) {
+        double a = f[2 * i], b = f[2 * i + 1];
+        if (mr) {
+            f[2 * i] = a * mr[i];
+            f[2 * i + 1] = b * mr[i];
+        } else {
+            double c = mc[2 * i], s = conj ? -mc[2 * i + 1] : mc[2 * i + 1];
+            f[2 * i] = a * c - b * s;
+            f[2 * i + 1] = a * s + b * c;
+        }
+    }
+    cf_ifft_d(f, o->nx, o->ny);
+}
+
+/* Forward through all slices; keeps psi_0..psi_S (psi[k]) and t_k (t[k-1]). */
+static void stack_forward(const stack_ops *o, int S, const double *v, double *psi, double *t)
+{
+    const size_t n = o->n;
+    for (size_t i = 0; i < n; i++) { psi[2 * i] = 1.0; psi[2 * i + 1] = 0.0; }
+    for (int k = 1; k <= S; k++) {
+        double *tk = t + 2 * n * (size_t)(k - 1);
+        const double *vk = v + n * (size_t)(k - 1);
+        for (size_t i = 0; i < n; i++) {
+            tk[2 * i] = cos(o->sigma * vk[i]);
+            tk[2 * i + 1] = sin(o->sigma * vk[i]);
+        }
+        kmul(o, tk, NULL, o->M, 0);
+        const double *pp = psi + 2 * n * (size_t)(k - 1);
+        double *pk = psi + 2 * n * (size_t)k;
+        for (size_t i = 0; i < n; i++) {
+            double a = pp[2 * i], b = pp[2 * i + 1], c = tk[2 * i], d = tk[2 * i + 1];
+            pk[2 * i] = a * c - b * d;
+            pk[2 * i + 1] = a * d + b * c;
+        }
+        kmul(o, pk, o->p, NULL, 0);
+    }
+}
+
+int mo_stack_images_f64(const mo_stack_params *sp, const double *v, int ndef,
+                        const double *rprime, double *images)
+{
+    stack_ops o;
+    int st = stack_setup(sp, ndef, rprime, &o);
+    if (st) return st;
+    const int S = sp->nslices;
+    const size_t n = o.n;
+    double *psi = (double *)malloc(sizeof(double) * 2 * n * (S + 1));
+    double *t = (double *)malloc(sizeof(double) * 2 * n * (S > 0 ? S : 1));
+    double *phi = (double *)malloc(sizeof(double) * 2 * n);
+    stack_forward(&o, S, v, psi, t);
+    for (int d = 0; d < ndef; d++) {
+        memcpy(phi, psi + 2 * n * (size_t)S, sizeof(double) * 2 * n);
+        kmul(&o, phi, o.X + 2 * n * (size_t)d, NULL, 0);
+        for (size_t i = 0; i < n; i++)
+            images[(size_t)d * n + i] = phi[2 * i] * phi[2 * i] + phi[2 * i + 1] * phi[2 * i + 1];
+    }
+    free(psi);
+    free(t);
+    free(phi);
+    stack_free(&o);
+    return MO_OK;
+}
+
+double mo_stack_loss_f64(const mo_stack_params *sp, const double *v, int ndef,
+                         const double *rprime, const float *target)
+{
+    const size_t n = (size_t)sp->nx * sp->ny;
+    double *img = (double *)malloc(sizeof(double) * n * (ndef > 0 ? ndef : 1));
+    mo_stack_images_f64(sp, v, ndef, rprime, img);
+    double L = 0.0;
+    for (size_t i = 0; i < n * ndef; i++) {
+        double r = img[i] - target[i];
+        L += r * r;
+    }
+    free(img);
+    return L;
+}
+
+int mo_stack_adjoint_f64(const mo_stack_params *sp, const double *v, int ndef,
+                         const double *rprime, const float *target, double *grad, double *loss)
+{
+    stack_ops o;
+    int st = stack_setup(sp, ndef, rprime, &o);
+    if (st) return st;
+    const int S = sp->nslices;
+    const size_t n = o.n;
+    double *psi = (double *)malloc(sizeof(double) * 2 * n * (S + 1));
+    double *t = (double *)malloc(sizeof(double) * 2 * n * (S > 0 ? S : 1));
+    double *phi = (double *)malloc(sizeof(double) * 2 * n);
+    double *g = (double *)calloc(2 * n, sizeof(double));   /* dL/d conj(psi_k) */
+    double *gu = (double *)malloc(sizeof(double) * 2 * n);
+    stack_forward(&o, S, v, psi, t);
+    double L = 0.0;
+    for (int d = 0; d < ndef; d++) {
+        memcpy(phi, psi + 2 * n * (size_t)S, sizeof(double) * 2 * n);
+        kmul(&o, phi, o.X + 2 * n * (size_t)d, NULL, 0);
+        for (size_t i = 0; i < n; i++) {
+            double I = phi[2 * i] * phi[2 * i] + phi[2 * i + 1] * phi[2 * i + 1];
+            double r = I - target[(size_t)d * n + i];
+            L += r * r;
+            phi[2 * i] *= 2.0 * r;    /* dL/d conj(phi) = 2 (I - T) phi */
+            phi[2 * i + 1] *= 2.0 * r;
+        }
+        kmul(&o, phi, o.X + 2 * n * (size_t)d, NULL, 1);  /* K[X]^H = K[conj X] */
+        for (size_t i = 0; i < 2 * n; i++) g[i] += phi[i];
+    }
+    for (int k = S; k >= 1; k--) {
+        memcpy(gu, g, sizeof(double) * 2 * n);
+        kmul(&o, gu, o.p, NULL, 1);                       /* g_u = K[conj p] g_psi */
+        const double *tk = t + 2 * n * (size_t)(k - 1);
+        const double *pp = psi + 2 * n * (size_t)(k - 1);
+        for (size_t i = 0; i < n; i++) {
+            double ar = gu[2 * i], ai = gu[2 * i + 1];
+            double tr = tk[2 * i], ti = tk[2 * i + 1], pr = pp[2 * i], pi_ = pp[2 * i + 1];
+            g[2 * i] = ar * tr + ai * ti;                 /* conj(t) g_u */
+            g[2 * i + 1] = ai * tr - ar * ti;
+            gu[2 * i] = ar * pr + ai * pi_;               /* conj(psi_{k-1}) g_u */
+            gu[2 * i + 1] = ai * pr - ar * pi_;
+        }
+        kmul(&o, gu, NULL, o.M, 0);                       /* g_e = K[M] g_t */
+        const double *vk = v + n * (size_t)(k - 1);
+        double *gk = grad + n * (size_t)(k - 1);
+        for (size_t i = 0; i < n; i++) {
+            double er = cos(o.sigma * vk[i]), ei = sin(o.sigma * vk[i]);
+            /* dL/dv = 2 sigma Im(g_e conj(e)) */
+            gk[i] = 2.0 * o.sigma * (gu[2 * i + 1] * er - gu[2 * i] * ei);
+        }
+    }
+    if (loss) *loss = L;
+    free(psi);
+    free(t);
+    free(phi);
+    free(g);
+    free(gu);
+    stack_free(&o);
+    return MO_OK;
 }

@@ -149,6 +149,36 @@ int mo_orientations_f32(const mo_series_params *sp, int nunits, int nthreads, in
                         const float *z, const float *occ, const double *angZ,
                         const double *angY, int ndef, const double *defocus, float *images);
 
+/* Per-slice projected potentials (FP64 sums) of one orientation, sliced as
+ * calculate() slices it: v[mo_slice_count(deltaz, ctblengthz)][nx][ny].
+ * Returns the atoms kept or a negative status. */
+int mo_orientation_potential_f64(const mo_series_params *sp, int natom, const int *Znum,
+                                 const float *x, const float *y, const float *z,
+                                 const float *occ, double angleZ, double angleY, double *v);
+
+/* ---- multislice from per-slice potential stacks, and its adjoint (FP64) ----
+ * Forward model for one orientation given v[k][ix][iy] (V*Angstrom, the
+ * quantity trlayer accumulates, autoslic.cpp:950-984), k = 0..nslices-1:
+ *   e_k = exp(i sigma v_k);  t_k = K[M] e_k   (2/3 band limit, autoslic.cpp:999-1009)
+ *   u_k = psi_{k-1} t_k;     psi_k = K[p] u_k (propagator, slicelib.cpp:811-849)
+ *   phi_d = K[X_d] psi_S;    I_d = |phi_d|^2  (free-space step of mo_defocus_*)
+ * with K[m] f = ifft(m fft(f))/(nx ny) in the cfpix convention and psi_0 = 1.
+ * Loss L = sum_d sum_px (I_d - T_d)^2.  The adjoint returns dL/dv_k. */
+typedef struct {
+    int nx, ny;
+    float ax, by, v0, deltaz, ctiltx, ctilty;
+    int nslices;
+    float aobj;          /* objective aperture, rad (0: none) */
+    double cs3, cs5;     /* Angstrom */
+} mo_stack_params;
+
+int mo_stack_images_f64(const mo_stack_params *p, const double *v, int ndef,
+                        const double *rprime, double *images);
+double mo_stack_loss_f64(const mo_stack_params *p, const double *v, int ndef,
+                         const double *rprime, const float *target);
+int mo_stack_adjoint_f64(const mo_stack_params *p, const double *v, int ndef,
+                         const double *rprime, const float *target, double *grad, double *loss);
+
 #ifdef __cplusplus
 }
 #endif

@@ -60,6 +60,13 @@ def _atoms(Znum, x, y, z, occ):
             np.ascontiguousarray(occ, np.float32))
 
 
+class StackParams(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("ax", C.c_float), ("by", C.c_float),
+                ("v0", C.c_float), ("deltaz", C.c_float), ("ctiltx", C.c_float),
+                ("ctilty", C.c_float), ("nslices", C.c_int), ("aobj", C.c_float),
+                ("cs3", C.c_double), ("cs5", C.c_double)]
+
+
 class Oracle:
     def __init__(self, path=LIB_ORACLE):
         if not os.path.exists(path):
@@ -93,10 +100,17 @@ class Oracle:
             getattr(L, nm).argtypes = [T, C.c_int, C.c_int, C.c_float, C.c_float, C.c_double,
                                        C.c_double, C.c_float, C.c_double, C.c_double, C.c_double,
                                        C.c_double, T]
+        L.mo_orientation_potential_f64.argtypes = [C.POINTER(SeriesParams), C.c_int, _ip, _fp,
+                                                   _fp, _fp, _fp, C.c_double, C.c_double, _dp]
         for nm, T in (("mo_orientation_f32", _fp), ("mo_orientation_f64", _dp)):
             getattr(L, nm).argtypes = [C.POINTER(SeriesParams), C.c_int, _ip, _fp, _fp, _fp, _fp,
                                        C.c_double, C.c_double, C.c_void_p, C.c_int, _dp, T,
                                        C.c_void_p]
+        L.mo_stack_images_f64.argtypes = [C.POINTER(StackParams), _dp, C.c_int, _dp, _dp]
+        L.mo_stack_loss_f64.argtypes = [C.POINTER(StackParams), _dp, C.c_int, _dp, _fp]
+        L.mo_stack_loss_f64.restype = C.c_double
+        L.mo_stack_adjoint_f64.argtypes = [C.POINTER(StackParams), _dp, C.c_int, _dp, _fp, _dp,
+                                           C.POINTER(C.c_double)]
         L.mo_orientations_f32.argtypes = [C.POINTER(SeriesParams), C.c_int, C.c_int, C.c_int,
                                           C.c_long, _ip, _fp, _fp, _fp, _fp, _dp, _dp, C.c_int,
                                           _dp, _fp]
@@ -188,6 +202,44 @@ class Oracle:
             raise RuntimeError("oracle orientation failed: %d" % kept)
         imgs = imgs.reshape(len(defoci), sp.nx, sp.ny)
         return (imgs, ew.reshape(sp.nx, sp.ny, 2), kept) if want_exit else (imgs, kept)
+
+    # -- potential stacks (FP64)
+    def stack_images(self, sp, v, rprime):
+        v = np.ascontiguousarray(v, np.float64)
+        rp = np.ascontiguousarray(rprime, np.float64)
+        out = np.zeros(len(rp) * sp.nx * sp.ny)
+        st = self.L.mo_stack_images_f64(C.byref(sp), v.reshape(-1), len(rp), rp, out)
+        if st:
+            raise RuntimeError("oracle stack images failed: %d" % st)
+        return out.reshape(len(rp), sp.nx, sp.ny)
+
+    def stack_loss(self, sp, v, rprime, target):
+        return self.L.mo_stack_loss_f64(C.byref(sp), np.ascontiguousarray(v, np.float64).reshape(-1),
+                                        len(rprime), np.ascontiguousarray(rprime, np.float64),
+                                        np.ascontiguousarray(target, np.float32).reshape(-1))
+
+    def stack_adjoint(self, sp, v, rprime, target):
+        v = np.ascontiguousarray(v, np.float64)
+        g = np.zeros(v.size)
+        loss = C.c_double()
+        st = self.L.mo_stack_adjoint_f64(C.byref(sp), v.reshape(-1), len(rprime),
+                                         np.ascontiguousarray(rprime, np.float64),
+                                         np.ascontiguousarray(target, np.float32).reshape(-1), g,
+                                         C.byref(loss))
+        if st:
+            raise RuntimeError("oracle stack adjoint failed: %d" % st)
+        return g.reshape(v.shape), loss.value
+
+    def orientation_potential(self, sp, Znum, x, y, z, occ, angleZ, angleY):
+        """FP64 per-slice projected potentials [nslices, nx, ny] of one
+        orientation and the number of atoms kept."""
+        ns = self.slice_count(sp.deltaz, sp.ctblengthz)
+        v = np.zeros(ns * sp.nx * sp.ny)
+        kept = self.L.mo_orientation_potential_f64(C.byref(sp), len(x), *_atoms(Znum, x, y, z, occ),
+                                                   angleZ, angleY, v)
+        if kept < 0:
+            raise RuntimeError("oracle potential failed: %d" % kept)
+        return v.reshape(ns, sp.nx, sp.ny), kept
 
     def orientations_f32(self, sp, Znum, x, y, z, occ, angZ, angY, defoci, nthreads,
                          coord_stride=0):

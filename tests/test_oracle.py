@@ -125,3 +125,65 @@ def test_defocus_properties(oracle):
     i1 = oracle.defocus(pix, 64.0, 64.0, lam, 250.0, fp64=True)
     assert abs(i1.sum() / i0.sum() - 1.0) < 1e-12
     assert rel_l2(i1, i0) > 1e-3  # and it does change the image
+
+
+def stack_params(nx, ny, S, ax=16.0, aobj=0.0, cs3=0.0):
+    from oracle.oracle import StackParams
+    p = StackParams()
+    p.nx, p.ny, p.ax, p.by, p.v0, p.deltaz, p.nslices = nx, ny, ax, ax * ny / nx, 200.0, 1.0, S
+    p.aobj, p.cs3 = aobj, cs3
+    return p
+
+
+def test_stack_adjoint_matches_central_differences(oracle):
+    """The FP64 adjoint of the potential-stack multislice against central
+    finite differences of its own loss (relative error <= 1e-6 per voxel)."""
+    p = stack_params(32, 32, 6, aobj=0.02, cs3=1e6)
+    v = sp.potential_stack(1, 6, 32, 32, seed=7)[0].astype(np.float64)
+    rp = np.array([5.0, 40.0])
+    T = oracle.stack_images(p, sp.perturbed(v, seed=8), rp).astype(np.float32)
+    g, L = oracle.stack_adjoint(p, v, rp, T)
+    assert abs(L / oracle.stack_loss(p, v, rp, T) - 1.0) < 1e-12
+    rng = np.random.default_rng(9)
+    gmax = np.abs(g).max()
+    for _ in range(12):
+        k, i, j = rng.integers(0, 6), rng.integers(0, 32), rng.integers(0, 32)
+        h = 1e-3 * max(1.0, abs(v[k, i, j]))
+        vp = v.copy()
+        vp[k, i, j] += h
+        vm = v.copy()
+        vm[k, i, j] -= h
+        fd = (oracle.stack_loss(p, vp, rp, T) - oracle.stack_loss(p, vm, rp, T)) / (2 * h)
+        assert abs(fd - g[k, i, j]) <= 1e-6 * max(abs(fd), 1e-3 * gmax)
+
+
+def test_stack_images_free_space_is_unitary(oracle):
+    p = stack_params(32, 64, 4)
+    v = sp.potential_stack(1, 4, 32, 64, seed=3)[0]
+    im = oracle.stack_images(p, v, [0.0, 300.0])
+    # no aperture: the propagator and the free-space step keep the total intensity
+    # once the band limit has acted (the transmission is not unitary after it)
+    assert abs(im[1].sum() / im[0].sum() - 1.0) < 1e-12
+    assert rel_l2(im[1], im[0]) > 1e-4
+
+
+def test_stack_of_atom_potentials_reproduces_orientation_images(oracle):
+    """The potential-stack model fed with the atom path's own per-slice
+    potentials gives that path's images (FP64 both; defocus measured from the
+    box centre there, from the exit face here)."""
+    from oracle.oracle import SeriesParams, StackParams
+    spec = sp.random_specimen(300, 32.0, 6.0, 26.0, 1012)
+    atoms = (spec.Znum, spec.x, spec.y, spec.z, spec.occ)
+    sr = SeriesParams()
+    sr.ax, sr.ctblengthz, sr.nx, sr.ny, sr.v0, sr.deltaz = 32.0, 32.0, 64, 64, 300.0, 2.0
+    sr.aobj, sr.cs3, sr.max_slices = 0.02, 1e6, -1
+    defoci = np.array([0.0, 250.0])
+    for angY in (0.0, 0.6):
+        v, kept = oracle.orientation_potential(sr, *atoms, 0.2, angY)
+        ref, k = oracle.orientation(sr, *atoms, 0.2, angY, defoci, fp64=True)
+        assert kept == k
+        p = StackParams()
+        p.nx, p.ny, p.ax, p.by, p.v0, p.deltaz = 64, 64, 32.0, 32.0, 300.0, 2.0
+        p.nslices, p.aobj, p.cs3 = v.shape[0], 0.02, 1e6
+        im = oracle.stack_images(p, v, defoci - 0.5 * 32.0)
+        assert rel_l2(im, ref) < 1e-12

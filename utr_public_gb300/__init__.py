@@ -26,7 +26,8 @@ NPARAM = 200
 EXPORTS = ("msk_create", "msk_destroy", "msk_last_error", "msk_status_string", "msk_calculate",
            "msk_tilt_series", "msk_slice_count", "msk_slice_assign", "msk_sort_by_z",
            "msk_rotate", "msk_potential_table", "msk_set_stream", "msk_profile",
-           "msk_profile_read", "msk_calculate_static", "msk_tilt_series_per_angle")
+           "msk_profile_read", "msk_calculate_static", "msk_tilt_series_per_angle",
+           "msk_stack_images", "msk_stack_adjoint", "msk_potential_stack")
 
 
 class MskError(RuntimeError):
@@ -42,6 +43,15 @@ class Series(C.Structure):
                 ("aobj", C.c_float), ("cs3", C.c_double), ("cs5", C.c_double),
                 ("astig", C.c_double), ("astig_angle", C.c_double), ("dxc", C.c_double),
                 ("dyc", C.c_double), ("dzc", C.c_double), ("nmode", C.c_int),
+                ("max_batch", C.c_int)]
+
+
+class Stack(C.Structure):
+    """msk_stack (include/msk.h): multislice from per-slice potentials."""
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("ax", C.c_float), ("by", C.c_float),
+                ("v0", C.c_float), ("deltaz", C.c_float), ("ctiltx", C.c_float),
+                ("ctilty", C.c_float), ("aobj", C.c_float), ("cs3", C.c_double),
+                ("cs5", C.c_double), ("nslices", C.c_int), ("checkpoint", C.c_int),
                 ("max_batch", C.c_int)]
 
 
@@ -97,6 +107,11 @@ def load():
                                             C.c_int, _dp, _dp, C.c_int, vp, C.c_int, vp, vp, vp]
     L.msk_calculate_static.argtypes = [vp, vp, vp, _fp, C.c_int, vp, vp, vp, vp, vp, C.c_float,
                                        C.c_float, C.c_int]
+    L.msk_stack_images.argtypes = [vp, C.POINTER(Stack), C.c_int, vp, C.c_int, vp, vp]
+    L.msk_stack_adjoint.argtypes = [vp, C.POINTER(Stack), C.c_int, vp, C.c_int, vp, vp, vp,
+                                    C.POINTER(C.c_double)]
+    L.msk_potential_stack.argtypes = [vp, C.POINTER(Series), C.c_int, vp, vp, vp, vp, vp,
+                                      C.c_int, _dp, _dp, vp, vp]
     _lib = L
     return L
 
@@ -268,6 +283,59 @@ class Context:
                                     _ptr(images), _ptr(exitwaves), _ptr(kept))
         self._check(st)
         return (images, exitwaves, kept) if want_exit or exitwaves is not None else (images, kept)
+
+    @staticmethod
+    def _f32(a):
+        if hasattr(a, "data_ptr"):
+            return a
+        return np.ascontiguousarray(a, np.float32)
+
+    def potential_stack(self, series, Znum, x, y, z, occ, angleZ, angleY, v=None):
+        """Per-slice projected potentials v [nangles, nslices, nx, ny] of a tilt
+        series (msk_potential_stack); v may be a preallocated torch CUDA tensor."""
+        angleZ = np.ascontiguousarray(angleZ, np.float64)
+        angleY = np.ascontiguousarray(angleY, np.float64)
+        na = len(angleZ)
+        ns = slice_count(series.deltaz, series.ctblengthz)
+        if v is None:
+            v = np.zeros((na, ns, series.nx, series.ny), np.float32)
+        kept = np.zeros(na, np.int32)
+        arrs = [np.ascontiguousarray(a, dt) for a, dt in
+                ((Znum, np.int32), (x, np.float32), (y, np.float32), (z, np.float32),
+                 (occ, np.float32))]
+        st = self.L.msk_potential_stack(self.h, C.byref(series), len(arrs[1]),
+                                        *[_ptr(a) for a in arrs], na, angleZ, angleY, _ptr(v),
+                                        _ptr(kept))
+        self._check(st)
+        return v, kept
+
+    def stack_images(self, stack, v, defocus, images=None):
+        """Images [nunits, ndef, nx, ny] of potential stacks v [nunits, nslices,
+        nx, ny] (msk_stack_images); v / images may be torch CUDA tensors."""
+        v = self._f32(v)
+        defocus = np.ascontiguousarray(defocus, np.float64)
+        nu = v.shape[0]
+        if images is None:
+            images = np.zeros((nu, len(defocus), stack.nx, stack.ny), np.float32)
+        st = self.L.msk_stack_images(self.h, C.byref(stack), nu, _ptr(v), len(defocus),
+                                     _ptr(defocus), _ptr(images))
+        self._check(st)
+        return images
+
+    def stack_adjoint(self, stack, v, defocus, target, grad=None):
+        """(loss, dL/dv) for L = sum (I - target)^2 (msk_stack_adjoint);
+        grad has v's shape; v / target / grad may be torch CUDA tensors."""
+        v = self._f32(v)
+        target = self._f32(target)
+        defocus = np.ascontiguousarray(defocus, np.float64)
+        nu = v.shape[0]
+        if grad is None:
+            grad = np.zeros(tuple(v.shape), np.float32)
+        loss = C.c_double(0.0)
+        st = self.L.msk_stack_adjoint(self.h, C.byref(stack), nu, _ptr(v), len(defocus),
+                                      _ptr(defocus), _ptr(target), _ptr(grad), C.byref(loss))
+        self._check(st)
+        return loss.value, grad
 
     def tilt_series_per_angle(self, series, Znum, x, y, z, occ, angleZ, angleY, defocus,
                               nconfig=1, displacements=None, images=None):

@@ -625,11 +625,13 @@ struct DevBuf {
 // Kinds of launches for the per-kernel accounting (msk_profile).
 enum Kind {
     kSplat, kKColMask, kTransmit, kKColProp, kFresnel, kIntensity, kExit, kInit, kPlane, kFresTab,
+    kExpv, kAdjTransmit, kGrad, kImGrad, kAccum,
     kKinds
 };
 static const char *const kKindName[kKinds] = {
     "row_splat", "col_bandlimit", "row_transmit", "col_propagate", "col_fresnel",
-    "row_intensity", "row_exit", "row_init", "plane_init", "fresnel_table"};
+    "row_intensity", "row_exit", "row_init", "plane_init", "fresnel_table",
+    "row_expv", "row_adj_transmit", "row_grad", "row_imgrad", "accumulate"};
 
 struct ProfRec {
     int kind;
@@ -654,6 +656,7 @@ struct msk_context {
     DevBuf psi, tbuf, tbuf2, atoms, slice_off, act, tables, imgmeta, wave0, images, exitw, fresnel,
         flags;
     DevBuf pa_v, pa_t, pa_psi, pa_e;  // buffers of the per-orientation comparison form
+    DevBuf stk, stk_v, stk_g, stk_t, stk_img, stk_part, adjtab;  // potential stacks, adjoint
     size_t units_alloc = 0;  // units the psi / tbuf buffers hold
     std::vector<int> zmap = std::vector<int>(104, -1);
 };
@@ -992,7 +995,8 @@ int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode)
             }
             {
                 Prof p(ctx, kTransmit, 24.0 * plane * na, sB);
-                rop->row_transmit(g, units, na, tb, psi, 1.0f / ((float)gp.ny * (float)gp.ny), sB);
+                rop->row_transmit(g, units, na, tb, psi, psi, 1.0f / ((float)gp.ny * (float)gp.ny),
+                                  sB);
             }
             if (overlap) {
                 MSK_CUDA(ctx, cudaEventRecord(ctx->ev_free[k], sB));
@@ -1049,7 +1053,9 @@ void msk_destroy(msk_context *ctx)
     for (cudaEvent_t e : ctx->prof_pool) cudaEventDestroy(e);
     for (DevBuf *b : {&ctx->psi, &ctx->tbuf, &ctx->tbuf2, &ctx->atoms, &ctx->slice_off, &ctx->act, &ctx->tables,
                       &ctx->imgmeta, &ctx->wave0, &ctx->images, &ctx->exitw, &ctx->fresnel,
-                      &ctx->flags, &ctx->pa_v, &ctx->pa_t, &ctx->pa_psi, &ctx->pa_e})
+                      &ctx->flags, &ctx->pa_v, &ctx->pa_t, &ctx->pa_psi, &ctx->pa_e, &ctx->stk,
+                      &ctx->stk_v, &ctx->stk_g, &ctx->stk_t, &ctx->stk_img, &ctx->stk_part,
+                      &ctx->adjtab})
         b->release();
     for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_join, ctx->ev_t[0], ctx->ev_t[1], ctx->ev_free[0],
                           ctx->ev_free[1]})
@@ -1451,6 +1457,418 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
     MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (kept)
         for (int u = 0; u < nunits; u++) kept[u] = ua[u].kept;
+    return flags_check(ctx);
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ potential stacks
+// The multislice of calculate() (autoslic.cpp:838-861) driven by given
+// per-slice projected potentials v_k instead of atoms, from a plane wave, with
+// the free-space step of msk_tilt_series to each detector plane; and the
+// adjoint of an image misfit through it.  Kernels: P1 is k_row_expv (no
+// splat), P2-P4 as in the atom path; the backward pass runs the adjoint of
+// every step in W-states with conjugated propagator and free-space tables
+// (the 2/3 band limit is real and symmetric: its own adjoint).
+
+namespace {
+
+__global__ void k_add_waves(float2 *__restrict__ dst, const float2 *__restrict__ src, size_t n)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const float2 a = dst[i], b = src[i];
+        dst[i] = make_float2(a.x + b.x, a.y + b.y);
+    }
+}
+
+struct StackJob {
+    const msk_stack *s;
+    int nunits, ndef;
+    const float *v;
+    const double *defocus;
+    const float *target;  // adjoint only
+    float *images;        // forward only (may be NULL)
+    float *grad;          // adjoint only
+    double *loss;
+};
+
+Fresnel stack_fresnel(msk_context *ctx, const GridPre &gp, const msk_stack *s, double rprime,
+                      double sign)
+{
+    const double pi = 4.0 * atan(1.0), l = gp.wavlen;
+    float k2maxo = s->aobj / gp.wavlen;
+    k2maxo = k2maxo * k2maxo;
+    Fresnel fr{};
+    fr.a1 = sign * pi * l * rprime;
+    fr.a3 = sign * (pi / 2.0) * s->cs3 * l * l * l;
+    fr.a5 = sign * (pi / 3.0) * s->cs5 * l * l * l * l * l;
+    fr.k2maxo = k2maxo;
+    fr.kx = tables_kx(ctx, gp);
+    fr.ky = tables_ky(ctx, gp);
+    return fr;
+}
+
+int stack_run(msk_context *ctx, const StackJob &J)
+{
+    const msk_stack *s = J.s;
+    const bool adjoint = J.grad != nullptr;
+    if (!s || J.nunits < 1 || J.ndef < 0 || !J.v || (J.ndef > 0 && !J.defocus) ||
+        (adjoint && (J.ndef < 1 || !J.target)) || (!adjoint && J.ndef > 0 && !J.images) ||
+        s->nslices < 1 || s->checkpoint < 0)
+        return fail(ctx, MSK_EINVAL, "bad potential-stack arguments");
+    const int nx = s->nx, ny = s->ny, S = s->nslices, ndef = J.ndef;
+    if (nx < 1 || ny < 1 || s->ax < 0.0f || s->by < 0.0f)
+        return fail(ctx, MSK_EBADSIZE, "bad size parameters");
+    if (!pow2_supported(nx) || !pow2_supported(ny))
+        return fail(ctx, MSK_EUNSUPPORTED, "grid must be a power of two from 16 to 4096");
+    MSK_CUDA(ctx, cudaSetDevice(ctx->device));
+    GridPre gp;
+    if (!grid_pre(gp, nx, ny, s->ax, s->by, s->v0, s->deltaz, s->ctiltx, s->ctilty))
+        return fail(ctx, MSK_EUNSUPPORTED, "band limit is not two index ranges per column");
+    int st = upload_tables(ctx, gp, std::vector<int>());
+    if (st) return st;
+    Geom &g = gp.g;
+    st = flags_reset(ctx, g);
+    if (st) return st;
+    // conjugated propagator for the backward pass
+    Geom gc = g;
+    if (adjoint) {
+        std::vector<float2> pc(nx + ny);
+        for (int i = 0; i < nx; i++) pc[i] = make_float2(gp.propx[i].x, -gp.propx[i].y);
+        for (int i = 0; i < ny; i++) pc[nx + i] = make_float2(gp.propy[i].x, -gp.propy[i].y);
+        MSK_CUDA(ctx, ctx->adjtab.reserve(pc.size() * sizeof(float2)));
+        MSK_CUDA(ctx, cudaMemcpyAsync(ctx->adjtab.p, pc.data(), pc.size() * sizeof(float2),
+                                      cudaMemcpyHostToDevice, ctx->stream));
+        count_copy(ctx, 0, (double)(pc.size() * sizeof(float2)));
+        MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        gc.propx = ctx->adjtab.as<float2>();
+        gc.propy = ctx->adjtab.as<float2>() + nx;
+    }
+
+    const size_t plane = (size_t)nx * ny;
+    const size_t pb = plane * sizeof(float2);
+    const int K = adjoint ? (s->checkpoint > 0 ? std::min(s->checkpoint, S) : std::min(8, S)) : 1;
+    const int nblk = adjoint ? (S + K - 1) / K : 1;
+    // planes per unit: forward W, transmission B, free-space E (+ adjoint:
+    // checkpoints, the block's transmissions and waves, the wave gradient G)
+    const int planes = adjoint ? 3 + nblk + K + (K - 1) : 3;
+    const bool v_dev = is_device_ptr(J.v);
+    const bool g_dev = adjoint && is_device_ptr(J.grad);
+    const bool t_dev = adjoint && is_device_ptr(J.target);
+    const bool i_dev = !adjoint && ndef > 0 && is_device_ptr(J.images);
+    const size_t vb = (size_t)S * plane * sizeof(float);      // one unit's stack
+    const size_t ib = (size_t)ndef * plane * sizeof(float);   // one unit's images
+    const size_t per_unit = planes * pb + (v_dev ? 0 : vb) + (adjoint && !g_dev ? vb : 0) +
+                            (adjoint && !t_dev ? ib : 0) + (!adjoint && !i_dev ? ib : 0);
+    size_t free_b = 0, total_b = 0;
+    MSK_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
+    const size_t budget = std::min<size_t>(free_b / 2, (size_t)64 << 30);
+    int B = (int)std::max<size_t>(1, std::min<size_t>(J.nunits, budget / per_unit));
+    if (s->max_batch > 0) B = std::min(B, s->max_batch);
+
+    MSK_CUDA(ctx, ctx->stk.reserve((size_t)planes * B * pb));
+    float2 *base = ctx->stk.as<float2>();
+    auto grid_at = [&](int i) { return base + (size_t)i * B * plane; };
+    float2 *W = grid_at(0), *E = grid_at(1), *Bt = grid_at(2), *G = nullptr;
+    std::vector<float2 *> ck, Bb, Wb;
+    if (adjoint) {
+        G = grid_at(2);
+        for (int i = 0; i < nblk; i++) ck.push_back(grid_at(3 + i));
+        for (int i = 0; i < K; i++) Bb.push_back(grid_at(3 + nblk + i));
+        for (int i = 0; i < K - 1; i++) Wb.push_back(grid_at(3 + nblk + K + i));
+        Bt = Bb[0];  // the forward pass's transmission: a block buffer, free until the backward
+    }
+    if (!v_dev) MSK_CUDA(ctx, ctx->stk_v.reserve((size_t)B * vb));
+    if (adjoint && !g_dev) MSK_CUDA(ctx, ctx->stk_g.reserve((size_t)B * vb));
+    if (adjoint && !t_dev) MSK_CUDA(ctx, ctx->stk_t.reserve((size_t)B * ib));
+    if (!adjoint && ndef > 0 && !i_dev) MSK_CUDA(ctx, ctx->stk_img.reserve((size_t)B * ib));
+    MSK_CUDA(ctx, ctx->fresnel.reserve((adjoint ? 2 : 1) * pb));
+
+    const SizeOps *rop = size_ops(ny), *cop = size_ops(nx);
+    // one tensor map per grid buffer the column passes touch
+    std::vector<CUtensorMap> maps(planes);
+    for (int i = 0; i < planes; i++) {
+        st = column_map(ctx, &maps[i], grid_at(i), nx, ny, B, cop);
+        if (st) return st;
+    }
+    auto map_of = [&](const float2 *p) -> const CUtensorMap & {
+        return maps[(size_t)(p - base) / ((size_t)B * plane)];
+    };
+    const double P = (double)plane;
+    const float tscale = 1.0f / ((float)ny * (float)ny);
+    // loss partials: one per row-pass CTA (at most one per row) and defocus
+    if (adjoint) MSK_CUDA(ctx, ctx->stk_part.reserve((size_t)ndef * B * nx * sizeof(double)));
+    std::vector<double> partial_host;
+    double loss = 0.0;
+
+    for (int u0 = 0; u0 < J.nunits; u0 += B) {
+        const int nb = std::min(B, J.nunits - u0);
+        const float *vd = v_dev ? J.v + (size_t)u0 * S * plane : ctx->stk_v.as<float>();
+        if (!v_dev) {
+            MSK_CUDA(ctx, cudaMemcpyAsync(ctx->stk_v.p, J.v + (size_t)u0 * S * plane, nb * vb,
+                                          cudaMemcpyHostToDevice, ctx->stream));
+            count_copy(ctx, 0, (double)nb * vb);
+        }
+        const size_t ustride = (size_t)S * plane;
+        auto vslice = [&](int k) { return vd + (size_t)(k - 1) * plane; };  // k = 1..S
+        // P1 + P2 of slice k into buffer `dst`
+        auto transmission = [&](int k, float2 *dst) {
+            {
+                Prof p(ctx, kExpv, 12.0 * P * nb);
+                rop->row_expv(g, nb, vslice(k), ustride, dst, ctx->stream);
+            }
+            Prof p(ctx, kKColMask, 16.0 * P * nb);
+            cop->col_mask(g, map_of(dst), map_of(dst), nullptr, nb, ctx->stream);
+        };
+        // P3 + P4 of one slice: out = W(K[p](iS(in) t))
+        auto step = [&](const float2 *tb, const float2 *in, float2 *out) {
+            {
+                Prof p(ctx, kTransmit, 24.0 * P * nb);
+                rop->row_transmit(g, nullptr, nb, tb, in, out, tscale, ctx->stream);
+            }
+            Prof p(ctx, kKColProp, 16.0 * P * nb);
+            cop->col_prop(g, map_of(out), map_of(out), nullptr, nb, ctx->stream);
+        };
+
+        // forward: W_0 = S(1); checkpoints W_{bK} kept for the backward pass
+        float2 *w0 = adjoint ? ck[0] : W;
+        {
+            Prof p(ctx, kPlane, 8.0 * P * nb);
+            k_plane_init<<<1024, 256, 0, ctx->stream>>>(w0, nullptr, nb, nx, ny);
+        }
+        for (int k = 1; k <= S; k++) {
+            const float2 *in = (adjoint && (k - 1) % K == 0) ? ck[(k - 1) / K] : W;
+            float2 *out = (adjoint && k % K == 0 && k < S) ? ck[k / K] : W;
+            transmission(k, Bt);
+            step(Bt, in, out);
+        }
+
+        // free space to every detector plane; images or the loss and its gradient
+        float *img_d = nullptr;
+        if (!adjoint && ndef > 0)
+            img_d = i_dev ? J.images + (size_t)u0 * ndef * plane : ctx->stk_img.as<float>();
+        const float *tgt = nullptr;
+        if (adjoint) {
+            tgt = t_dev ? J.target + (size_t)u0 * ndef * plane : ctx->stk_t.as<float>();
+            if (!t_dev) {
+                MSK_CUDA(ctx, cudaMemcpyAsync(ctx->stk_t.p, J.target + (size_t)u0 * ndef * plane,
+                                              nb * ib, cudaMemcpyHostToDevice, ctx->stream));
+                count_copy(ctx, 0, (double)nb * ib);
+            }
+        }
+        int nparts = 0;
+        for (int d = 0; d < ndef; d++) {
+            float2 *tab = ctx->fresnel.as<float2>();
+            Fresnel fr = stack_fresnel(ctx, gp, s, J.defocus[d], 1.0);
+            fr.table = tab;
+            {
+                Prof p(ctx, kFresTab, 8.0 * P);
+                k_fresnel_table<<<4 * 152, 256, 0, ctx->stream>>>(
+                    g, fr, 1.0f / ((float)nx * (float)ny), tab);
+            }
+            {
+                Prof p(ctx, kFresnel, 16.0 * P * nb);
+                cop->col_fresnel(g, map_of(W), map_of(E), nullptr, nb, fr, 1.0f, ctx->stream);
+            }
+            if (!adjoint) {
+                // images[u][d] = |iS(E)|^2: one image per unit, no averaging
+                std::vector<int> meta;
+                for (int i = 0; i <= nb; i++) meta.push_back(i);          // img_off
+                for (int i = 0; i < nb; i++) meta.push_back(i);           // img_units
+                for (int i = 0; i < nb; i++) meta.push_back(i * ndef + d);  // img_dst
+                for (int i = 0; i < nb; i++) meta.push_back(0);           // img_flags
+                MSK_CUDA(ctx, ctx->imgmeta.reserve(meta.size() * sizeof(int) * ndef));
+                int *dm = ctx->imgmeta.as<int>() + (size_t)d * meta.size();
+                MSK_CUDA(ctx, cudaMemcpyAsync(dm, meta.data(), meta.size() * sizeof(int),
+                                              cudaMemcpyHostToDevice, ctx->stream));
+                count_copy(ctx, 0, (double)(meta.size() * sizeof(int)));
+                Prof p(ctx, kIntensity, 12.0 * P * nb);
+                rop->row_intensity(g, nb, dm, dm + nb + 1, dm + 2 * nb + 1, dm + 3 * nb + 1, E,
+                                   img_d, 1.0f, ctx->stream);
+                continue;
+            }
+            // G_d = W(2 (I - T) phi), in place in E; partial sums of the loss
+            int np = 0;
+            {
+                Prof p(ctx, kImGrad, 20.0 * P * nb);
+                np = rop->row_imgrad(g, nb, E, tgt + (size_t)d * plane, (size_t)ndef * plane, E,
+                                     ctx->stk_part.as<double>() + nparts, ctx->stream);
+            }
+            nparts += np;
+            // g_psiS += K[conj X] g_phi: conjugate table with the column 1/nx
+            Fresnel fc = stack_fresnel(ctx, gp, s, J.defocus[d], -1.0);
+            fc.table = tab + plane;
+            {
+                Prof p(ctx, kFresTab, 8.0 * P);
+                k_fresnel_table<<<4 * 152, 256, 0, ctx->stream>>>(g, fc, 1.0f / (float)nx,
+                                                                   tab + plane);
+            }
+            {
+                Prof p(ctx, kFresnel, 16.0 * P * nb);
+                cop->col_fresnel(g, map_of(E), map_of(d == 0 ? G : E), nullptr, nb, fc, 1.0f,
+                                 ctx->stream);
+            }
+            if (d > 0) {
+                Prof p(ctx, kAccum, 24.0 * P * nb);
+                k_add_waves<<<8 * 152, 256, 0, ctx->stream>>>(G, E, (size_t)nb * plane);
+            }
+        }
+
+        if (adjoint) {
+            float *gd = g_dev ? J.grad + (size_t)u0 * S * plane : ctx->stk_g.as<float>();
+            // backward, one checkpoint block at a time from the last
+            for (int b = nblk - 1; b >= 0; b--) {
+                const int k0 = b * K, nj = std::min(S, k0 + K) - k0;
+                for (int j = 1; j <= nj; j++) {  // recompute the block's t_k and psi_k
+                    transmission(k0 + j, Bb[j - 1]);
+                    if (j < nj) step(Bb[j - 1], j == 1 ? ck[b] : Wb[j - 2], Wb[j - 1]);
+                }
+                for (int j = nj; j >= 1; j--) {
+                    const int k = k0 + j;
+                    {
+                        Prof p(ctx, kKColProp, 16.0 * P * nb);  // g_u = K[conj p] g_psi
+                        cop->col_prop(gc, map_of(G), map_of(G), nullptr, nb, ctx->stream);
+                    }
+                    {
+                        Prof p(ctx, kAdjTransmit, 40.0 * P * nb);
+                        rop->row_adj_transmit(g, nb, G, Bb[j - 1], j == 1 ? ck[b] : Wb[j - 2],
+                                              ctx->stream);
+                    }
+                    {
+                        Prof p(ctx, kKColMask, 16.0 * P * nb);  // g_e = K[M] g_t
+                        cop->col_mask(g, map_of(Bb[j - 1]), map_of(Bb[j - 1]), nullptr, nb,
+                                      ctx->stream);
+                    }
+                    Prof p(ctx, kGrad, 16.0 * P * nb);
+                    rop->row_grad(g, nb, Bb[j - 1], vslice(k), ustride,
+                                  gd + (size_t)(k - 1) * plane, ctx->stream);
+                }
+            }
+            if (!g_dev) {
+                MSK_CUDA(ctx, cudaMemcpyAsync(J.grad + (size_t)u0 * S * plane, gd, nb * vb,
+                                              cudaMemcpyDeviceToHost, ctx->stream));
+                count_copy(ctx, 1, (double)nb * vb);
+            }
+            partial_host.resize(nparts);
+            MSK_CUDA(ctx, cudaMemcpyAsync(partial_host.data(), ctx->stk_part.p,
+                                          nparts * sizeof(double), cudaMemcpyDeviceToHost,
+                                          ctx->stream));
+            count_copy(ctx, 1, (double)nparts * sizeof(double));
+        } else if (ndef > 0 && !i_dev) {
+            MSK_CUDA(ctx, cudaMemcpyAsync(J.images + (size_t)u0 * ndef * plane, img_d, nb * ib,
+                                          cudaMemcpyDeviceToHost, ctx->stream));
+            count_copy(ctx, 1, (double)nb * ib);
+        }
+        MSK_CUDA(ctx, cudaGetLastError());
+        MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        prof_collect(ctx);
+        for (int i = 0; i < nparts; i++) loss += partial_host[i];  // fixed order
+    }
+    if (J.loss) *J.loss = loss;
+    return flags_check(ctx);
+}
+
+}  // namespace
+
+extern "C" {
+
+int msk_stack_images(msk_context *ctx, const msk_stack *s, int nunits, const float *v,
+                     int ndefocus, const double *defocus, float *images)
+{
+    if (!ctx) return MSK_EINVAL;
+    ctx->err.clear();
+    StackJob J{s, nunits, ndefocus, v, defocus, nullptr, images, nullptr, nullptr};
+    return stack_run(ctx, J);
+}
+
+int msk_stack_adjoint(msk_context *ctx, const msk_stack *s, int nunits, const float *v,
+                      int ndefocus, const double *defocus, const float *target, float *grad,
+                      double *loss)
+{
+    if (!ctx) return MSK_EINVAL;
+    ctx->err.clear();
+    if (!grad) return fail(ctx, MSK_EINVAL, "grad is required");
+    StackJob J{s, nunits, ndefocus, v, defocus, target, nullptr, grad, loss};
+    return stack_run(ctx, J);
+}
+
+int msk_potential_stack(msk_context *ctx, const msk_series *s, int natom, const int *Znum,
+                        const float *x, const float *y, const float *z, const float *occ,
+                        int nangles, const double *angleZ, const double *angleY, float *v,
+                        int *kept)
+{
+    if (!ctx) return MSK_EINVAL;
+    ctx->err.clear();
+    if (!s || natom < 0 || nangles < 1 || !angleZ || !angleY || !v ||
+        (natom > 0 && (!Znum || !x || !y || !z || !occ)))
+        return fail(ctx, MSK_EINVAL, "bad potential-stack arguments");
+    const int nx = s->nx, ny = s->ny;
+    if (nx < 1 || ny < 1 || s->ctblength < 0.0f) return fail(ctx, MSK_EBADSIZE, "bad size parameters");
+    if (!pow2_supported(nx) || !pow2_supported(ny))
+        return fail(ctx, MSK_EUNSUPPORTED, "grid must be a power of two from 16 to 4096");
+    MSK_CUDA(ctx, cudaSetDevice(ctx->device));
+    GridPre gp;
+    if (!grid_pre(gp, nx, ny, s->ctblength, s->ctblength, s->v0, s->deltaz, 0.0f, 0.0f))
+        return fail(ctx, MSK_EUNSUPPORTED, "band limit is not two index ranges per column");
+    const int nslices = slice_count(s->deltaz, s->ctblengthz);
+    std::vector<int> zlist;
+    int st = build_zmap(ctx, natom, Znum, zlist);
+    if (st) return st;
+    st = upload_tables(ctx, gp, zlist);
+    if (st) return st;
+    st = flags_reset(ctx, gp.g);
+    if (st) return st;
+    const size_t plane = (size_t)nx * ny;
+    const size_t ub = (size_t)nslices * plane * sizeof(float);  // one orientation's stack
+    const bool v_dev = is_device_ptr(v);
+    int B = nangles;
+    if (!v_dev) {
+        size_t free_b = 0, total_b = 0;
+        MSK_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
+        const size_t budget = std::min<size_t>(free_b / 2, (size_t)64 << 30);
+        B = (int)std::max<size_t>(1, std::min<size_t>(nangles, budget / ub));
+        if (s->max_batch > 0) B = std::min(B, s->max_batch);
+        MSK_CUDA(ctx, ctx->stk_v.reserve((size_t)B * ub));
+    }
+    const SizeOps *rop = size_ops(ny);
+    std::vector<UnitAtoms> ua(nangles);
+    for (int u0 = 0; u0 < nangles; u0 += B) {
+        const int nb = std::min(B, nangles - u0);
+        parallel_for(nb, host_threads(), [&](int i) {
+            const int a = u0 + i;
+            PrepSpec ps{natom, Znum, x, y, z, occ, s->ctblength, s->ctblengthz, s->deltaz,
+                        nslices, true, angleZ[a], angleY[a], s->dxc, s->dyc, s->dzc, nullptr,
+                        true, ctx->zmap.data()};
+            prep_unit(gp, ps, ua[a]);
+        });
+        for (int i = 0; i < nb; i++)
+            if (ua[u0 + i].status)
+                return fail(ctx, ua[u0 + i].status, msk_status_string(ua[u0 + i].status));
+        Batch b;
+        st = upload_batch(ctx, ua, u0, nb, nslices, b);
+        if (st) return st;
+        float *vd = v_dev ? v + (size_t)u0 * nslices * plane : ctx->stk_v.as<float>();
+        MSK_CUDA(ctx, cudaMemsetAsync(vd, 0, nb * ub, ctx->stream));
+        for (int sl = 0; sl < nslices; sl++) {
+            const int na = b.act_off[sl + 1] - b.act_off[sl];
+            if (na == 0) continue;
+            Prof p(ctx, kSplat, 4.0 * plane * na);
+            rop->splat_potential(gp.g, ctx->act.as<int>() + b.act_off[sl], na, sl, nslices + 1,
+                                 ctx->slice_off.as<int>(), ctx->atoms.as<SplatAtom>(),
+                                 vd + (size_t)sl * plane, (size_t)nslices * plane, ctx->stream);
+        }
+        if (!v_dev) {
+            MSK_CUDA(ctx, cudaMemcpyAsync(v + (size_t)u0 * nslices * plane, vd, nb * ub,
+                                          cudaMemcpyDeviceToHost, ctx->stream));
+            count_copy(ctx, 1, (double)nb * ub);
+        }
+        MSK_CUDA(ctx, cudaGetLastError());
+        MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        prof_collect(ctx);
+    }
+    if (kept)
+        for (int a = 0; a < nangles; a++) kept[a] = ua[a].kept;
     return flags_check(ctx);
 }
 

@@ -15,6 +15,11 @@ struct SizeOps {
     int col_c, col_box_rows;  // column tile width and TMA box height for line length n
     void (*splat)(const Geom &, const int *units, int nunits, int slice, int nsl1,
                   const int *slice_off, const SplatAtom *atoms, float2 *tbuf, cudaStream_t);
+    // the same splat writing the projected potential of the slice (float) to
+    // vout + u * vstride instead of its transmission
+    void (*splat_potential)(const Geom &, const int *units, int nunits, int slice, int nsl1,
+                            const int *slice_off, const SplatAtom *atoms, float *vout,
+                            size_t vstride, cudaStream_t);
     void (*col_mask)(const Geom &, const CUtensorMap &in, const CUtensorMap &out,
                      const int *units, int nunits, cudaStream_t);
     void (*col_prop)(const Geom &, const CUtensorMap &in, const CUtensorMap &out,
@@ -22,7 +27,7 @@ struct SizeOps {
     void (*col_fresnel)(const Geom &, const CUtensorMap &in, const CUtensorMap &out,
                         const int *units, int nunits, const Fresnel &, float scale, cudaStream_t);
     void (*row_transmit)(const Geom &, const int *units, int nunits, const float2 *tbuf,
-                         float2 *psi, float out_scale, cudaStream_t);
+                         const float2 *psi, float2 *out, float out_scale, cudaStream_t);
     void (*row_init)(const Geom &, const int *units, int nunits, const float2 *wave0,
                      float2 *psi, float scale, cudaStream_t);
     void (*row_exit)(const Geom &, const int *units, int nunits, const float2 *psi,
@@ -30,6 +35,16 @@ struct SizeOps {
     void (*row_intensity)(const Geom &, int nimg, const int *img_off, const int *img_units,
                           const int *img_dst, const int *img_flags, const float2 *ebuf,
                           float *images, float nconf, cudaStream_t);
+    // potential stacks and the adjoint (row length n)
+    void (*row_expv)(const Geom &, int nunits, const float *v, size_t ustride, float2 *out,
+                     cudaStream_t);
+    void (*row_adj_transmit)(const Geom &, int nunits, float2 *Gu, float2 *B, const float2 *Wp,
+                             cudaStream_t);
+    void (*row_grad)(const Geom &, int nunits, const float2 *Ge, const float *v, size_t ustride,
+                     float *grad, cudaStream_t);
+    // returns the number of loss partials written
+    int (*row_imgrad)(const Geom &, int nunits, const float2 *E, const float *target,
+                      size_t tstride, float2 *G, double *partial, cudaStream_t);
 };
 
 // Line lengths with kernels: 16 .. 4096, powers of two.
@@ -43,6 +58,8 @@ template <int N> struct Smem {
     static constexpr size_t col = (size_t)ColCfg<N>::C * P::PADN * 8 + 16;
     static constexpr size_t transmit = (size_t)2 * RowCfg<N>::LT * P::PADN * 8 + 16;
     static constexpr size_t row = (size_t)RowCfg<N>::L * P::PADN * 8;
+    static constexpr size_t adj = (size_t)RowCfg<N>::LT * (P::PADN + N) * 8;
+    static constexpr size_t imgrad = row + (size_t)RowCfg<N>::L * P::T * 8;
 };
 
 template <typename K>
@@ -66,10 +83,20 @@ struct Launch {
                       const int *slice_off, const SplatAtom *atoms, float2 *tbuf, cudaStream_t s)
     {
         static std::once_flag f;
-        set_smem(k_row_splat<N>, Smem<N>::splat, f);
+        set_smem(k_row_splat<N, false>, Smem<N>::splat, f);
         const int L = RowCfg<N>::L;
-        k_row_splat<N><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::splat, s>>>(
-            g, units, slice, nsl1, slice_off, atoms, tbuf);
+        k_row_splat<N, false><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::splat, s>>>(
+            g, units, slice, nsl1, slice_off, atoms, tbuf, nullptr, 0);
+    }
+    static void splat_potential(const Geom &g, const int *units, int nunits, int slice, int nsl1,
+                                const int *slice_off, const SplatAtom *atoms, float *vout,
+                                size_t vstride, cudaStream_t s)
+    {
+        static std::once_flag f;
+        set_smem(k_row_splat<N, true>, Smem<N>::splat, f);
+        const int L = RowCfg<N>::L;
+        k_row_splat<N, true><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::splat, s>>>(
+            g, units, slice, nsl1, slice_off, atoms, nullptr, vout, vstride);
     }
     template <int MODE>
     static void col(const Geom &g, const CUtensorMap &in, const CUtensorMap &out,
@@ -99,13 +126,13 @@ struct Launch {
         col<kColFresnel>(g, in, out, units, nunits, fr, scale, s);
     }
     static void row_transmit(const Geom &g, const int *units, int nunits, const float2 *tbuf,
-                             float2 *psi, float out_scale, cudaStream_t s)
+                             const float2 *psi, float2 *out, float out_scale, cudaStream_t s)
     {
         static std::once_flag f;
         set_smem(k_row_transmit<N>, Smem<N>::transmit, f);
         const int L = RowCfg<N>::LT;
         k_row_transmit<N><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::transmit, s>>>(
-            g, units, tbuf, psi, out_scale);
+            g, units, tbuf, psi, out, out_scale);
     }
     static void row_init(const Geom &g, const int *units, int nunits, const float2 *wave0,
                          float2 *psi, float scale, cudaStream_t s)
@@ -136,11 +163,49 @@ struct Launch {
             g, img_off, img_units, img_dst, img_flags, ebuf, images, nconf);
     }
 
+    static void row_expv(const Geom &g, int nunits, const float *v, size_t ustride, float2 *out,
+                         cudaStream_t s)
+    {
+        static std::once_flag f;
+        set_smem(k_row_expv<N>, Smem<N>::row, f);
+        const int L = RowCfg<N>::L;
+        k_row_expv<N><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::row, s>>>(g, v, ustride, out);
+    }
+    static void row_adj_transmit(const Geom &g, int nunits, float2 *Gu, float2 *B,
+                                 const float2 *Wp, cudaStream_t s)
+    {
+        static std::once_flag f;
+        set_smem(k_row_adj_transmit<N>, Smem<N>::adj, f);
+        const int L = RowCfg<N>::LT;
+        k_row_adj_transmit<N><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::adj, s>>>(g, Gu, B, Wp);
+    }
+    static void row_grad(const Geom &g, int nunits, const float2 *Ge, const float *v,
+                         size_t ustride, float *grad, cudaStream_t s)
+    {
+        static std::once_flag f;
+        set_smem(k_row_grad<N>, Smem<N>::row, f);
+        const int L = RowCfg<N>::L;
+        k_row_grad<N><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::row, s>>>(g, Ge, v, ustride,
+                                                                               grad);
+    }
+    static int row_imgrad(const Geom &g, int nunits, const float2 *E, const float *target,
+                          size_t tstride, float2 *G, double *partial, cudaStream_t s)
+    {
+        static std::once_flag f;
+        set_smem(k_row_imgrad<N>, Smem<N>::imgrad, f);
+        const int L = RowCfg<N>::L;
+        const int nb = nunits * row_blocks(g, L);
+        k_row_imgrad<N><<<nb, L * P::T, Smem<N>::imgrad, s>>>(g, E, target, tstride, G, partial);
+        return nb;
+    }
+
     static const SizeOps *ops()
     {
-        static const SizeOps o = {N,        ColCfg<N>::C, ColCfg<N>::BR, splat,
-                                  col_mask, col_prop,     col_fresnel,   row_transmit,
-                                  row_init, row_exit,     row_intensity};
+        static const SizeOps o = {N,        ColCfg<N>::C, ColCfg<N>::BR,    splat,
+                                  splat_potential,
+                                  col_mask, col_prop,     col_fresnel,      row_transmit,
+                                  row_init, row_exit,     row_intensity,    row_expv,
+                                  row_adj_transmit,       row_grad,         row_imgrad};
         return &o;
     }
 };

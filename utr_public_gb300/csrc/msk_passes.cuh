@@ -110,11 +110,11 @@ __device__ __forceinline__ float spline_vz(const Geom &g, const float *knots, co
 // fixed pixel owner, so the sum order per pixel is the atom order and the
 // result is deterministic, with no atomics (autoslic.cpp:950-984 is a racy
 // scatter in the reference).  Then t = exp(i sigma v) and the row FFT.
-template <int NY>
+template <int NY, bool POT>
 __global__ void __launch_bounds__(RowCfg<NY>::L * FftPlan<NY>::T)
 k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
             const int *__restrict__ slice_off, const SplatAtom *__restrict__ atoms,
-            float2 *__restrict__ tbuf)
+            float2 *__restrict__ tbuf, float *__restrict__ vout, size_t vstride)
 {
     using P = FftPlan<NY>;
     constexpr int T = P::T, E = P::E, L = RowCfg<NY>::L, NT = L * T, NW = (NT + 31) / 32;
@@ -193,6 +193,15 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
             }
         }
         __syncthreads();
+    }
+    if constexpr (POT) {
+        // the projected potential itself: vout -> slice `slice` of unit 0
+        if (row_ok) {
+            float *dst = vout + (size_t)u * vstride + (size_t)ix * NY;
+#pragma unroll
+            for (int m = 0; m < E; m++) dst[t + m * T] = vacc[t + m * T];
+        }
+        return;
     }
 
     float2 v[E];
@@ -312,13 +321,13 @@ k_col_pass(const Geom g, const __grid_constant__ CUtensorMap in_map,
 }
 
 // ---------------------------------------------------------------- P3
-// W = S(iS(W) * iS(B)) * out_scale (out_scale = 1/ny^2): wave *= trans
+// W' = S(iS(W) * iS(B)) * out_scale (out_scale = 1/ny^2): wave *= trans
 // (cfpix.cpp:349-372) between the transmission's and the wave's row
-// transforms.
+// transforms.  `out` may be `psi` (in place).
 template <int NY>
 __global__ void __launch_bounds__(RowCfg<NY>::LT * FftPlan<NY>::T, 3)
 k_row_transmit(const Geom g, const int *__restrict__ units, const float2 *__restrict__ tbuf,
-               float2 *__restrict__ psi, float out_scale)
+               const float2 *psi, float2 *out, float out_scale)
 {
     using P = FftPlan<NY>;
     constexpr int T = P::T, E = P::E, L = RowCfg<NY>::LT;
@@ -331,7 +340,7 @@ k_row_transmit(const Geom g, const int *__restrict__ units, const float2 *__rest
     const int tid = threadIdx.x, l = tid / T, t = tid % T;
     const int nx = g.nx;
     const int bpu = (nx + L - 1) / L;
-    const int u = units[blockIdx.x / bpu];
+    const int u = units ? units[blockIdx.x / bpu] : (int)(blockIdx.x / bpu);
     const int ix0 = (blockIdx.x % bpu) * L;
     const int rows = min(L, nx - ix0);
     const uint32_t bytes = (uint32_t)rows * NY * 8u;
@@ -371,7 +380,7 @@ k_row_transmit(const Geom g, const int *__restrict__ units, const float2 *__rest
     fence_proxy_async();
     __syncthreads();
     if (tid == 0) {
-        bulk_store(psi + off, bufW, bytes);
+        bulk_store(out + off, bufW, bytes);
         bulk_commit();
         bulk_wait_read();
     }
@@ -456,6 +465,179 @@ k_row_intensity(const Geom g, const int *__restrict__ img_off, const int *__rest
 #pragma unroll
         for (int m = 0; m < E; m++) dst[t + m * T] = (flags & 2) ? __fdiv_rn(acc[m], nconf) : acc[m];
     }
+}
+
+// ---------------------------------------------------------------- potential stacks
+// Rows of a per-slice potential stack v[u][k][ix][iy] (float, V*Angstrom):
+// A = S(exp(i sigma v)), the transmission before its band limit.  `v` points
+// at slice k of unit 0; units are `ustride` floats apart.
+template <int NY>
+__global__ void __launch_bounds__(RowCfg<NY>::L * FftPlan<NY>::T)
+k_row_expv(const Geom g, const float *__restrict__ v, size_t ustride, float2 *__restrict__ out)
+{
+    using P = FftPlan<NY>;
+    constexpr int T = P::T, E = P::E, L = RowCfg<NY>::L;
+    constexpr bool BLK = RowCfg<NY>::BLK;
+    extern __shared__ __align__(128) unsigned char smem[];
+    float2 *s_lines = reinterpret_cast<float2 *>(smem);
+    const int tid = threadIdx.x, l = tid / T, t = tid % T;
+    const int nx = g.nx;
+    const int bpu = (nx + L - 1) / L;
+    const int u = blockIdx.x / bpu;
+    const int ix = (blockIdx.x % bpu) * L + l;
+    const bool row_ok = ix < nx;
+    const float *src = v + (size_t)u * ustride + (size_t)(row_ok ? ix : 0) * NY;
+    float2 w[E];
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+        const float ph = src[t + m * T] * g.sigma_f;
+        w[m] = make_float2(1.0f, 0.0f);
+        if (__any_sync(0xffffffffu, ph != 0.0f)) w[m] = expi(ph);
+    }
+    fft_line<NY, false, 1, BLK>(w, s_lines + l * P::PADN, 0, t, g.tw_row);
+    if (row_ok) {
+        float2 *dst = out + ((size_t)u * nx + ix) * NY;
+#pragma unroll
+        for (int m = 0; m < E; m++) dst[t + m * T] = w[m];
+    }
+}
+
+// Adjoint of transmit.  In W-states (W(f) = S(f)): from Gu = W(g_u),
+// B = W(t_k), Wp = W(psi_{k-1}):  Gu <- W(conj(t) g_u)  (dL/dconj psi_{k-1})
+// and B <- W(conj(psi_{k-1}) g_u)  (dL/dconj t_k), both in place.
+template <int NY>
+__global__ void __launch_bounds__(RowCfg<NY>::LT * FftPlan<NY>::T)
+k_row_adj_transmit(const Geom g, float2 *Gu, float2 *B, const float2 *__restrict__ Wp)
+{
+    using P = FftPlan<NY>;
+    constexpr int T = P::T, E = P::E, L = RowCfg<NY>::LT;
+    constexpr bool BLK = RowCfg<NY>::BLK;
+    extern __shared__ __align__(128) unsigned char smem[];
+    float2 *s_lines = reinterpret_cast<float2 *>(smem);
+    float2 *s_stash = s_lines + L * P::PADN;
+    const int tid = threadIdx.x, l = tid / T, t = tid % T;
+    const int nx = g.nx;
+    const int bpu = (nx + L - 1) / L;
+    const int u = blockIdx.x / bpu;
+    const int ix = (blockIdx.x % bpu) * L + l;
+    const bool row_ok = ix < nx;
+    const size_t off = ((size_t)u * nx + (row_ok ? ix : 0)) * NY;
+    const float sc = 1.0f / ((float)NY * (float)NY);
+    float2 *buf = s_lines + l * P::PADN;
+    float2 *stash = s_stash + l * NY;
+    float2 a[E];
+#pragma unroll
+    for (int m = 0; m < E; m++) a[m] = Gu[off + t + m * T];
+    fft_line<NY, true, 1, BLK>(a, buf, 0, t, g.tw_row);  // ny g_u
+#pragma unroll
+    for (int m = 0; m < E; m++) stash[t + m * T] = a[m];
+#pragma unroll
+    for (int m = 0; m < E; m++) a[m] = B[off + t + m * T];
+    fft_line<NY, true, 1, BLK>(a, buf, 0, t, g.tw_row);  // ny t
+#pragma unroll
+    for (int m = 0; m < E; m++) a[m] = cmul_conj(stash[t + m * T], a[m]);
+    fft_line<NY, false, 1, BLK>(a, buf, 0, t, g.tw_row);
+    if (row_ok) {
+#pragma unroll
+        for (int m = 0; m < E; m++) Gu[off + t + m * T] = cscale(a[m], sc);
+    }
+#pragma unroll
+    for (int m = 0; m < E; m++) a[m] = Wp[off + t + m * T];
+    fft_line<NY, true, 1, BLK>(a, buf, 0, t, g.tw_row);  // ny psi
+#pragma unroll
+    for (int m = 0; m < E; m++) a[m] = cmul_conj(stash[t + m * T], a[m]);
+    fft_line<NY, false, 1, BLK>(a, buf, 0, t, g.tw_row);
+    if (row_ok) {
+#pragma unroll
+        for (int m = 0; m < E; m++) B[off + t + m * T] = cscale(a[m], sc);
+    }
+}
+
+// dL/dv_k = 2 sigma Im(g_e conj(e_k)), e_k = exp(i sigma v_k), from
+// Ge = W(g_e).  `v` and `grad` point at slice k of unit 0, units `ustride`
+// floats apart.
+template <int NY>
+__global__ void __launch_bounds__(RowCfg<NY>::L * FftPlan<NY>::T)
+k_row_grad(const Geom g, const float2 *__restrict__ Ge, const float *__restrict__ v,
+           size_t ustride, float *__restrict__ grad)
+{
+    using P = FftPlan<NY>;
+    constexpr int T = P::T, E = P::E, L = RowCfg<NY>::L;
+    constexpr bool BLK = RowCfg<NY>::BLK;
+    extern __shared__ __align__(128) unsigned char smem[];
+    float2 *s_lines = reinterpret_cast<float2 *>(smem);
+    const int tid = threadIdx.x, l = tid / T, t = tid % T;
+    const int nx = g.nx;
+    const int bpu = (nx + L - 1) / L;
+    const int u = blockIdx.x / bpu;
+    const int ix = (blockIdx.x % bpu) * L + l;
+    const bool row_ok = ix < nx;
+    const size_t row = (size_t)(row_ok ? ix : 0) * NY;
+    float2 a[E];
+#pragma unroll
+    for (int m = 0; m < E; m++) a[m] = Ge[(size_t)u * nx * NY + row + t + m * T];
+    fft_line<NY, true, 1, BLK>(a, s_lines + l * P::PADN, 0, t, g.tw_row);
+    const float c = 2.0f * g.sigma_f / (float)NY;
+    const float *vr = v + (size_t)u * ustride + row;
+    float *gr = grad + (size_t)u * ustride + row;
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+        const float ph = vr[t + m * T] * g.sigma_f;
+        float2 e = make_float2(1.0f, 0.0f);
+        if (__any_sync(0xffffffffu, ph != 0.0f)) e = expi(ph);
+        if (row_ok) gr[t + m * T] = c * (a[m].y * e.x - a[m].x * e.y);
+    }
+}
+
+// Image residual of the loss L = sum (|phi|^2 - T)^2: from E with
+// phi = iS(E) (the free-space column pass output), G = S(2 (I - T) phi) =
+// W(dL/dconj phi); per-CTA partial sums of (I - T)^2 go to partial[block].
+// G may be Ein: every CTA reads its rows before it writes them.
+template <int NY>
+__global__ void __launch_bounds__(RowCfg<NY>::L * FftPlan<NY>::T)
+k_row_imgrad(const Geom g, const float2 *Ein, const float *__restrict__ target, size_t tstride,
+             float2 *G, double *__restrict__ partial)
+{
+    using P = FftPlan<NY>;
+    constexpr int T = P::T, E = P::E, L = RowCfg<NY>::L, NT = L * T;
+    constexpr bool BLK = RowCfg<NY>::BLK;
+    extern __shared__ __align__(128) unsigned char smem[];
+    float2 *s_lines = reinterpret_cast<float2 *>(smem);
+    double *s_red = reinterpret_cast<double *>(s_lines + L * P::PADN);
+    const int tid = threadIdx.x, l = tid / T, t = tid % T;
+    const int nx = g.nx;
+    const int bpu = (nx + L - 1) / L;
+    const int u = blockIdx.x / bpu;
+    const int ix = (blockIdx.x % bpu) * L + l;
+    const bool row_ok = ix < nx;
+    const size_t row = (size_t)(row_ok ? ix : 0) * NY;
+    float2 a[E];
+#pragma unroll
+    for (int m = 0; m < E; m++) a[m] = Ein[(size_t)u * nx * NY + row + t + m * T];
+    fft_line<NY, true, 1, BLK>(a, s_lines + l * P::PADN, 0, t, g.tw_row);  // phi
+    const float *tr = target + (size_t)u * tstride + row;
+    double acc = 0.0;
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+        const float I = a[m].x * a[m].x + a[m].y * a[m].y;
+        const float r = row_ok ? I - tr[t + m * T] : 0.0f;
+        acc += (double)r * (double)r;
+        a[m] = cscale(a[m], 2.0f * r);
+    }
+    fft_line<NY, false, 1, BLK>(a, s_lines + l * P::PADN, 0, t, g.tw_row);
+    if (row_ok) {
+#pragma unroll
+        for (int m = 0; m < E; m++) G[(size_t)u * nx * NY + row + t + m * T] = a[m];
+    }
+    // fixed-order block reduction: deterministic loss
+    __syncthreads();
+    s_red[tid] = acc;
+    __syncthreads();
+    for (int w = NT / 2; w > 0; w >>= 1) {
+        if (tid < w) s_red[tid] += s_red[tid + w];
+        __syncthreads();
+    }
+    if (tid == 0) partial[blockIdx.x] = s_red[0];
 }
 
 // The free-space multiplier of one detector plane, in double, reduced modulo

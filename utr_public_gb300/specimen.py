@@ -106,3 +106,26 @@ def read_xyz(path):
     f32 = lambda c: a[:, c].astype(np.float32)
     return Specimen(a[:, 0].astype(np.int32), f32(1), f32(2), f32(3), f32(4), f32(5),
                     float(max(ax, by, cz)))
+
+
+def potential_stack(nunits, nslices, nx, ny, blobs=3, peak=60.0, width=2.0, seed=1005):
+    """Synthetic per-slice projected potentials v[nunits, nslices, nx, ny]
+    (V*Angstrom, float32): `blobs` periodic Gaussian peaks per slice, the
+    shape a splatted atom gives, for the potential-stack and adjoint paths."""
+    rng = np.random.default_rng(seed)
+    X, Y = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    v = np.zeros((nunits, nslices, nx, ny), np.float64)
+    for u in range(nunits):
+        for k in range(nslices):
+            for _ in range(blobs):
+                cx, cy = rng.uniform(0, nx), rng.uniform(0, ny)
+                dx = (X - cx + nx / 2) % nx - nx / 2
+                dy = (Y - cy + ny / 2) % ny - ny / 2
+                v[u, k] += peak * np.exp(-(dx * dx + dy * dy) / (2 * width * width))
+    return v.astype(np.float32)
+
+
+def perturbed(v, rel=0.01, seed=1005):
+    """v * (1 + rel N(0, 1)): the potential whose images are the adjoint's target."""
+    rng = np.random.default_rng(seed)
+    return (v * (1.0 + rel * rng.standard_normal(v.shape))).astype(np.float32)
