@@ -184,6 +184,199 @@ def fp64_error_job(result):
         result["error"] = repr(e)
 
 
+ADJ_NX, ADJ_FOV, ADJ_V0, ADJ_NANG, ADJ_CHECKPOINT = 512, 64.0, 200.0, 90, 8
+ADJ_METRIC = ("adjoint slice-steps/s (512², FP32, 64 slices x 90 orientations, forward + "
+              "checkpointed adjoint); dL/dv err vs FP64 adjoint and central differences")
+
+
+def adjoint_check(result, v, S, target, angles, nvox, rp):
+    """FP64 oracle adjoint and central differences (host threads) for a few
+    orientations of the adjoint workload; v[a], target[a] host arrays."""
+    try:
+        from oracle import oracle as orc
+        O = orc.Oracle()
+        p = orc.StackParams()
+        p.nx = p.ny = ADJ_NX
+        p.ax = p.by = ADJ_FOV
+        p.v0, p.deltaz, p.nslices = ADJ_V0, 1.0, S
+        rng = np.random.default_rng(1005)
+        threads = max(1, (os.cpu_count() or 2) - 1)
+        out = []
+        t0 = time.perf_counter()
+        for a in angles:
+            g64, L64 = O.stack_adjoint(p, v[a], rp, target[a])
+            vox = np.stack([rng.integers(0, S, nvox), rng.integers(0, ADJ_NX, nvox),
+                            rng.integers(0, ADJ_NX, nvox)], axis=1)
+            fd = O.stack_fd(p, v[a], rp, target[a], vox, nthreads=threads)
+            out.append({"angle_index": int(a), "grad64": g64, "loss64": L64, "voxels": vox,
+                        "fd": fd})
+        result["cases"] = out
+        result["seconds"] = time.perf_counter() - t0
+        result["threads"] = threads
+    except Exception as e:  # reported, not fatal
+        result["error"] = repr(e)
+
+
+def run_adjoint(args, rank, world, local_rank):
+    """C5: per-orientation potential stacks of the plain specimen (splatted on
+    the GPU), target images from the stacks perturbed by 1% Gaussian noise,
+    L = sum (I - T)^2 at one detector plane, dL/dv with checkpoints every 8
+    slices.  One step = one msk_adjoint call over all 90 orientations."""
+    import torch
+    import utr_public_gb300 as msk
+    from utr_public_gb300 import specimen
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    msk.load()
+    ctx = msk.Context(local_rank)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    spec = specimen.plain_specimen(1001)
+    atoms = (spec.Znum, spec.x, spec.y, spec.z, spec.occ)
+    nang = ADJ_NANG
+    angY = np.deg2rad(2.0 * np.arange(nang))
+    angZ = np.full(nang, 0.1 * rank)
+    s = msk.Series()
+    s.nx = s.ny = ADJ_NX
+    s.ctblength = s.ctblengthz = ADJ_FOV
+    s.v0, s.deltaz = ADJ_V0, 1.0
+    S = msk.slice_count(1.0, ADJ_FOV)
+    v = torch.empty((nang, S, ADJ_NX, ADJ_NX), dtype=torch.float32, device="cuda")
+    with torch.cuda.stream(stream):
+        ctx.potential_stack(s, *atoms, angZ, angY, v=v)
+        gen = torch.Generator(device="cuda")
+        gen.manual_seed(1005 + rank)
+        vt = v * (1.0 + 0.01 * torch.randn(v.shape, generator=gen, device="cuda"))
+    st = msk.Stack()
+    st.nx = st.ny = ADJ_NX
+    st.ax = st.by = ADJ_FOV
+    st.v0, st.deltaz, st.nslices, st.checkpoint = ADJ_V0, 1.0, S, ADJ_CHECKPOINT
+    rp = np.array([0.0 - 0.5 * ADJ_FOV])  # detector defocus 0 from the box centre
+    target = torch.empty((nang, 1, ADJ_NX, ADJ_NX), dtype=torch.float32, device="cuda")
+    ctx.stack_images(st, vt, rp, images=target)
+    grad = torch.empty_like(v)
+    del vt
+    torch.cuda.synchronize()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def timed(fn, k):
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ms = e0.elapsed_time(e1) / k
+        if dist is not None:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    step = lambda: ctx.adjoint(st, v, rp, target, grad=grad)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = Clocks(gpu_index(local_rank))
+    ms = timed(step, args.steps)
+    clk = clocks.stop()
+    steps_per = nang * S
+    value = world * steps_per / (ms / 1000.0)
+    loss_dev, _ = ctx.adjoint(st, v, rp, target, grad=grad)
+    pick = [0, nang // 4]  # the orientations the oracle checks (0 and 44 degrees)
+    g_dev = {a: grad[a].cpu().numpy() for a in pick}
+    # forward alone (images of the same stacks)
+    fimg = torch.empty_like(target)
+    ms_fwd = timed(lambda: ctx.stack_images(st, v, rp, images=fimg), args.steps)
+    # per-kernel attribution of one adjoint call
+    ctx.profile(True)
+    ms_serial = timed(step, 1)
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    # end to end: pinned host stacks, target and gradient
+    hv = torch.empty(v.shape, dtype=torch.float32, pin_memory=True)
+    hv.copy_(v)
+    ht = torch.empty(target.shape, dtype=torch.float32, pin_memory=True)
+    ht.copy_(target)
+    hg = torch.empty(v.shape, dtype=torch.float32, pin_memory=True)
+    k_e2e = max(1, min(args.steps, 2))
+    ctx.adjoint(st, hv, rp, ht, grad=hg)
+    ctx.profile(True)
+    ms_e2e = timed(lambda: ctx.adjoint(st, hv, rp, ht, grad=hg), k_e2e)
+    prof_e2e = ctx.profile_read()
+    ctx.profile(False)
+    h2d = prof_e2e.get("copy_h2d", (0, 0.0, 0.0))[2] / k_e2e
+    d2h = prof_e2e.get("copy_d2h", (0, 0.0, 0.0))[2] / k_e2e
+    same = bool(torch.equal(hg, grad.cpu())) if rank == 0 else None
+    kernels = {k: x for k, x in prof.items() if not k.startswith("copy_")}
+    launches = int(sum(x[0] for x in kernels.values())) * args.steps
+    dom = max(kernels, key=lambda k: kernels[k][1])
+    n_l, t_ms, nbytes = kernels[dom]
+    peak, peak_kind = peaks()
+    achieved = (nbytes / n_l) / (t_ms / n_l / 1000.0) / 1e9
+    if rank != 0:
+        return
+    err = None
+    if not args.no_fp64_check:
+        check = {}
+        adjoint_check(check, {a: v[a].cpu().numpy() for a in pick}, S,
+                      {a: target[a].cpu().numpy() for a in pick}, pick, args.fd_voxels, rp)
+        if "cases" in check:
+            rl2 = lambda a, b: float(np.linalg.norm(np.asarray(a, np.float64) - b) /
+                                     np.linalg.norm(b))
+            cases = []
+            for c in check["cases"]:
+                g = g_dev[c["angle_index"]]
+                ours = np.array([g[k, i, j] for k, i, j in c["voxels"]])
+                cases.append({"orientation_deg": 2.0 * c["angle_index"],
+                              "grad_rel_l2_vs_fp64_adjoint": rl2(g, c["grad64"]),
+                              "grad_rel_l2_vs_central_fd": rl2(ours, c["fd"]),
+                              "fd_voxels": int(len(ours))})
+            err = {"cases": cases, "oracle_seconds": check["seconds"],
+                   "oracle_threads": check["threads"]}
+        else:
+            err = {"error": check.get("error", "not run")}
+    out = {
+        "metric": ADJ_METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "adjoint: plain specimen (2000 atoms, 64 A box), 512^2, 64 "
+                               "slices of 1 A, 200 keV, 90 orientations (2 deg about y), "
+                               "potentials splatted on the GPU, target from v(1 + 0.01 N(0,1)), "
+                               "1 detector plane (defocus 0), checkpoint every 8 slices",
+                   "slice_steps_per_step": steps_per * world,
+                   "l2": "inputs larger than L2 (stacks 6.0 GB per GPU)"},
+        "forward_only": {"value": world * steps_per / (ms_fwd / 1000.0), "unit": UNIT,
+                         "ms": ms_fwd, "adjoint_over_forward_time": ms / ms_fwd},
+        "loss": loss_dev,
+        "e2e": {"value": world * steps_per / (ms_e2e / 1000.0), "unit": UNIT,
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "ms_per_step": ms_e2e, "matches_device_output": same},
+        "gpu_launches": launches * world,
+        "ms_per_step_serialized": ms_serial,
+        "kernels": {k: {"launches": x[0], "ms": round(x[1], 3),
+                        "GBps": round(x[2] / (x[1] / 1000.0) / 1e9, 1) if x[1] > 0 else None}
+                    for k, x in kernels.items()},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "peak_source": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_launch": nbytes / n_l},
+        "clocks": clk,
+        "err_vs_fp64": err,
+    }
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -195,6 +388,11 @@ def main():
     ap.add_argument("--no-per-angle", action="store_true")
     ap.add_argument("--orientations", type=int, default=NANG,
                     help="orientations per step (180 for the headline workload)")
+    ap.add_argument("--workload", default="tilt", choices=["tilt", "adjoint"],
+                    help="tilt: the 180-orientation 1024^2 tilt series (headline); adjoint: "
+                         "the 512^2 potential-stack adjoint over 90 orientations")
+    ap.add_argument("--fd-voxels", type=int, default=32,
+                    help="central-difference voxels per checked orientation (adjoint)")
     ap.add_argument("--profile-run", action="store_true",
                     help="one tilt series and its per-kernel table, for profilers")
     args = ap.parse_args()
@@ -203,6 +401,15 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.workload == "adjoint":
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "metric": ADJ_METRIC,
+                                  "unavailable": "the reference has no adjoint"}))
+            return
+        run_adjoint(args, rank, world, local_rank)
+        return
 
     if args.impl == "reference":
         if world > 1:

@@ -205,7 +205,7 @@ int msk_stack_images(msk_context *ctx, const msk_stack *s, int nunits, const flo
 /*   target: float[nunits][ndefocus][nx][ny], host or device (ndefocus >= 1)
  *   grad out: float[nunits][nslices][nx][ny] = dL/dv, host or device
  *   loss out (may be NULL): L, summed in double in a fixed order */
-int msk_stack_adjoint(msk_context *ctx, const msk_stack *s, int nunits, const float *v,
+int msk_adjoint(msk_context *ctx, const msk_stack *s, int nunits, const float *v,
                       int ndefocus, const double *defocus, const float *target, float *grad,
                       double *loss);
 

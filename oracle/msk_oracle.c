@@ -1284,3 +1284,165 @@ int mo_stack_adjoint_f64(const mo_stack_params *sp, const double *v, int ndef,
     stack_free(&o);
     return MO_OK;
 }
+
+/* Central finite differences of mo_stack_loss_f64 at chosen voxels.
+ * Perturbing v_k at one pixel changes e_k there only, so the band-limited
+ * transmission becomes t_k + c h(. - pixel) with h = K[M] delta (computed
+ * once) and c the exact change of exp(i sigma v).  For fixed transmissions
+ * the slice loop is linear in the wave, so the perturbed wave is psi + d
+ * with d_k = K[p](psi_{k-1} c h(. - pixel)) and d_m = K[p](d_{m-1} t_m)
+ * exactly, and each image changes by dI = 2 Re(conj(phi) dphi) + |dphi|^2.
+ * L(v + h) - L(v - h) = sum (dI+ - dI-) (2 r + dI+ + dI-), r = I - T: the
+ * same central difference as two full evaluations, without the cancellation
+ * of two large sums.  Voxels run on nthreads threads; fd[i] = that difference
+ * / (2 h_i), h_i = h_rel * max(1, |v|). */
+typedef struct {
+    const stack_ops *o;
+    int S, ndef;
+    const double *v, *psi, *t, *hk;
+    const double *phi;  /* base free-space waves [ndef][n] (complex) */
+    const double *res;  /* base residuals I - T [ndef][n] */
+    const int *vox;
+    int nvox;
+    double h_rel;
+    double *fd;
+    int next;
+    pthread_mutex_t lock;
+} fd_job;
+
+/* dI[d][px] for the change dv of v_k at (ix, iy). */
+static void fd_delta(fd_job *J, int k, int ix, int iy, double dv, double *w, double *dphi,
+                     double *dI)
+{
+    const stack_ops *o = J->o;
+    const size_t n = o->n;
+    const int nx = o->nx, ny = o->ny;
+    const double vk = J->v[(size_t)(k - 1) * n + (size_t)ix * ny + iy];
+    const double c_r = cos(o->sigma * (vk + dv)) - cos(o->sigma * vk);
+    const double c_i = sin(o->sigma * (vk + dv)) - sin(o->sigma * vk);
+    const double *pp = J->psi + 2 * n * (size_t)(k - 1);
+    for (int x = 0; x < nx; x++)
+        for (int y = 0; y < ny; y++) {
+            const size_t i = (size_t)x * ny + y;
+            /* h shifted to the pixel: h[(x - ix) mod nx][(y - iy) mod ny] */
+            const size_t hi = (size_t)((x - ix + nx) % nx) * ny + (size_t)((y - iy + ny) % ny);
+            const double hr = J->hk[2 * hi], him = J->hk[2 * hi + 1];
+            const double tr = c_r * hr - c_i * him, ti = c_r * him + c_i * hr;
+            const double a = pp[2 * i], b = pp[2 * i + 1];
+            w[2 * i] = a * tr - b * ti;
+            w[2 * i + 1] = a * ti + b * tr;
+        }
+    kmul(o, w, o->p, NULL, 0);
+    for (int m = k + 1; m <= J->S; m++) {
+        const double *tm = J->t + 2 * n * (size_t)(m - 1);
+        for (size_t i = 0; i < n; i++) {
+            const double a = w[2 * i], b = w[2 * i + 1], c = tm[2 * i], d = tm[2 * i + 1];
+            w[2 * i] = a * c - b * d;
+            w[2 * i + 1] = a * d + b * c;
+        }
+        kmul(o, w, o->p, NULL, 0);
+    }
+    for (int d = 0; d < J->ndef; d++) {
+        memcpy(dphi, w, sizeof(double) * 2 * n);
+        kmul(o, dphi, o->X + 2 * n * (size_t)d, NULL, 0);
+        const double *ph = J->phi + 2 * n * (size_t)d;
+        double *di = dI + n * (size_t)d;
+        for (size_t i = 0; i < n; i++) {
+            const double pr = ph[2 * i], pi_ = ph[2 * i + 1];
+            const double qr = dphi[2 * i], qi = dphi[2 * i + 1];
+            di[i] = 2.0 * (pr * qr + pi_ * qi) + (qr * qr + qi * qi);
+        }
+    }
+}
+
+static void *fd_worker(void *arg)
+{
+    fd_job *J = (fd_job *)arg;
+    const size_t n = J->o->n;
+    const size_t nd = n * (size_t)J->ndef;
+    double *w = (double *)malloc(sizeof(double) * 2 * n);
+    double *dphi = (double *)malloc(sizeof(double) * 2 * n);
+    double *dIp = (double *)malloc(sizeof(double) * (nd > 0 ? nd : 1));
+    double *dIm = (double *)malloc(sizeof(double) * (nd > 0 ? nd : 1));
+    for (;;) {
+        pthread_mutex_lock(&J->lock);
+        const int q = J->next++;
+        pthread_mutex_unlock(&J->lock);
+        if (q >= J->nvox) break;
+        const int k = J->vox[3 * q] + 1, ix = J->vox[3 * q + 1], iy = J->vox[3 * q + 2];
+        const double vk = J->v[(size_t)(k - 1) * n + (size_t)ix * J->o->ny + iy];
+        const double h = J->h_rel * (fabs(vk) > 1.0 ? fabs(vk) : 1.0);
+        fd_delta(J, k, ix, iy, h, w, dphi, dIp);
+        fd_delta(J, k, ix, iy, -h, w, dphi, dIm);
+        double dL = 0.0;
+        for (size_t i = 0; i < nd; i++) dL += (dIp[i] - dIm[i]) * (2.0 * J->res[i] + dIp[i] + dIm[i]);
+        J->fd[q] = dL / (2.0 * h);
+    }
+    free(w);
+    free(dphi);
+    free(dIp);
+    free(dIm);
+    return NULL;
+}
+
+int mo_stack_fd_f64(const mo_stack_params *sp, const double *v, int ndef, const double *rprime,
+                    const float *target, int nvox, const int *vox, double h_rel, int nthreads,
+                    double *fd)
+{
+    stack_ops o;
+    int st = stack_setup(sp, ndef, rprime, &o);
+    if (st) return st;
+    const int S = sp->nslices;
+    const size_t n = o.n;
+    for (int q = 0; q < nvox; q++)
+        if (vox[3 * q] < 0 || vox[3 * q] >= S || vox[3 * q + 1] < 0 || vox[3 * q + 1] >= o.nx ||
+            vox[3 * q + 2] < 0 || vox[3 * q + 2] >= o.ny) {
+            stack_free(&o);
+            return MO_EBADSIZE;
+        }
+    double *psi = (double *)malloc(sizeof(double) * 2 * n * (S + 1));
+    double *t = (double *)malloc(sizeof(double) * 2 * n * (S > 0 ? S : 1));
+    double *hk = (double *)calloc(2 * n, sizeof(double));
+    double *phi = (double *)malloc(sizeof(double) * 2 * n * (ndef > 0 ? ndef : 1));
+    double *res = (double *)malloc(sizeof(double) * n * (ndef > 0 ? ndef : 1));
+    stack_forward(&o, S, v, psi, t);
+    hk[0] = 1.0;
+    kmul(&o, hk, NULL, o.M, 0);
+    for (int d = 0; d < ndef; d++) {
+        double *ph = phi + 2 * n * (size_t)d;
+        memcpy(ph, psi + 2 * n * (size_t)S, sizeof(double) * 2 * n);
+        kmul(&o, ph, o.X + 2 * n * (size_t)d, NULL, 0);
+        for (size_t i = 0; i < n; i++)
+            res[(size_t)d * n + i] = ph[2 * i] * ph[2 * i] + ph[2 * i + 1] * ph[2 * i + 1] -
+                                     target[(size_t)d * n + i];
+    }
+    fd_job J;
+    J.o = &o;
+    J.S = S;
+    J.ndef = ndef;
+    J.v = v;
+    J.psi = psi;
+    J.t = t;
+    J.hk = hk;
+    J.phi = phi;
+    J.res = res;
+    J.vox = vox;
+    J.nvox = nvox;
+    J.h_rel = h_rel;
+    J.fd = fd;
+    J.next = 0;
+    pthread_mutex_init(&J.lock, NULL);
+    if (nthreads < 1) nthreads = 1;
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
+    for (int i = 0; i < nthreads; i++) pthread_create(&th[i], NULL, fd_worker, &J);
+    for (int i = 0; i < nthreads; i++) pthread_join(th[i], NULL);
+    free(th);
+    pthread_mutex_destroy(&J.lock);
+    free(psi);
+    free(t);
+    free(hk);
+    free(phi);
+    free(res);
+    stack_free(&o);
+    return MO_OK;
+}

@@ -178,6 +178,11 @@ double mo_stack_loss_f64(const mo_stack_params *p, const double *v, int ndef,
                          const double *rprime, const float *target);
 int mo_stack_adjoint_f64(const mo_stack_params *p, const double *v, int ndef,
                          const double *rprime, const float *target, double *grad, double *loss);
+/* Central finite differences of the loss at nvox voxels vox[q] = {k, ix, iy}
+ * (k 0-based slice), step h_rel * max(1, |v|), on nthreads threads. */
+int mo_stack_fd_f64(const mo_stack_params *p, const double *v, int ndef, const double *rprime,
+                    const float *target, int nvox, const int *vox, double h_rel, int nthreads,
+                    double *fd);
 
 #ifdef __cplusplus
 }

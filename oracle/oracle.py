@@ -230,6 +230,21 @@ class Oracle:
             raise RuntimeError("oracle stack adjoint failed: %d" % st)
         return g.reshape(v.shape), loss.value
 
+    def stack_fd(self, sp, v, rprime, target, voxels, h_rel=1e-3, nthreads=1):
+        """Central differences dL/dv at voxels [(k, ix, iy), ...] (FP64)."""
+        v = np.ascontiguousarray(v, np.float64)
+        vox = np.ascontiguousarray(voxels, np.int32).reshape(-1)
+        fd = np.zeros(len(vox) // 3)
+        fn = self.L.mo_stack_fd_f64
+        fn.argtypes = [C.POINTER(StackParams), _dp, C.c_int, _dp, _fp, C.c_int, _ip, C.c_double,
+                       C.c_int, _dp]
+        st = fn(C.byref(sp), v.reshape(-1), len(rprime), np.ascontiguousarray(rprime, np.float64),
+                np.ascontiguousarray(target, np.float32).reshape(-1), len(fd), vox, h_rel,
+                nthreads, fd)
+        if st:
+            raise RuntimeError("oracle finite differences failed: %d" % st)
+        return fd
+
     def orientation_potential(self, sp, Znum, x, y, z, occ, angleZ, angleY):
         """FP64 per-slice projected potentials [nslices, nx, ny] of one
         orientation and the number of atoms kept."""

@@ -1,5 +1,5 @@
 """Potential-stack multislice and its adjoint on the GPU (msk_stack_images,
-msk_stack_adjoint) against the FP64 oracle and central finite differences.
+msk_adjoint) against the FP64 oracle and central finite differences.
 
 Tolerances (relative L2):
   * images vs the FP64 oracle:                          1e-5
@@ -64,14 +64,14 @@ def test_stack_images_match_oracle(ctx, msk, oracle, nx, ny, S, aobj, cs3, ctilt
 
 
 @pytest.mark.parametrize("S,checkpoint", [(10, 0), (10, 4), (9, 3), (5, 1), (6, 6)])
-def test_stack_adjoint_matches_oracle(ctx, msk, oracle, S, checkpoint):
+def test_adjoint_matches_oracle(ctx, msk, oracle, S, checkpoint):
     nx = ny = 64
     s = make_stack(msk, nx, ny, S, aobj=0.03, checkpoint=checkpoint)
     v, vt = case(nx, ny, S, 2, 21)
     rp = [10.0, 200.0]
     p = oracle_params(s)
     target = np.stack([oracle.stack_images(p, vt[u], rp) for u in range(2)]).astype(np.float32)
-    loss, g = ctx.stack_adjoint(s, v, rp, target)
+    loss, g = ctx.adjoint(s, v, rp, target)
     L64 = 0.0
     for u in range(2):
         gref, Lu = oracle.stack_adjoint(p, v[u], rp, target[u])
@@ -80,7 +80,7 @@ def test_stack_adjoint_matches_oracle(ctx, msk, oracle, S, checkpoint):
     assert abs(loss / L64 - 1.0) < 1e-4
 
 
-def test_stack_adjoint_matches_finite_differences(ctx, msk, oracle):
+def test_adjoint_matches_finite_differences(ctx, msk, oracle):
     """Central differences of the FP64 oracle loss on random voxels."""
     nx = ny = 64
     S = 12
@@ -89,7 +89,7 @@ def test_stack_adjoint_matches_finite_differences(ctx, msk, oracle):
     rp = [0.0, 150.0]
     p = oracle_params(s)
     target = oracle.stack_images(p, vt[0], rp).astype(np.float32)[None]
-    _, g = ctx.stack_adjoint(s, v, rp, target)
+    _, g = ctx.adjoint(s, v, rp, target)
     v64 = v[0].astype(np.float64)
     rng = np.random.default_rng(32)
     # voxels where the gradient is not negligible: on and near the potential peaks
@@ -108,7 +108,7 @@ def test_stack_adjoint_matches_finite_differences(ctx, msk, oracle):
     assert rel_l2(ours, np.array(fd)) < 2e-3
 
 
-def test_stack_adjoint_batching_and_device_pointers(ctx, msk, oracle):
+def test_adjoint_batching_and_device_pointers(ctx, msk, oracle):
     torch = pytest.importorskip("torch")
     nx = ny = 64
     S = 8
@@ -116,15 +116,15 @@ def test_stack_adjoint_batching_and_device_pointers(ctx, msk, oracle):
     rp = [0.0]
     s = make_stack(msk, nx, ny, S, checkpoint=3)
     target = ctx.stack_images(s, vt, rp)
-    loss_a, ga = ctx.stack_adjoint(s, v, rp, target)
+    loss_a, ga = ctx.adjoint(s, v, rp, target)
     s1 = make_stack(msk, nx, ny, S, checkpoint=3, max_batch=2)
-    loss_b, gb = ctx.stack_adjoint(s1, v, rp, target)
+    loss_b, gb = ctx.adjoint(s1, v, rp, target)
     assert np.array_equal(ga, gb)  # units are independent: bit-equal in any batch
     assert abs(loss_b / loss_a - 1.0) < 1e-12
     dv = torch.from_numpy(v).cuda()
     dt = torch.from_numpy(target).cuda()
     dg = torch.zeros_like(dv)
-    loss_c, _ = ctx.stack_adjoint(s, dv, rp, dt, grad=dg)
+    loss_c, _ = ctx.adjoint(s, dv, rp, dt, grad=dg)
     assert np.array_equal(dg.cpu().numpy(), ga)
     assert loss_c == loss_a
     di = torch.zeros((5, 1, nx, ny), dtype=torch.float32, device="cuda")
@@ -152,7 +152,7 @@ def test_stack_errors(ctx, msk):
     assert e.value.status == msk.MSK_EUNSUPPORTED
     s = make_stack(msk, 32, 32, 2)
     with pytest.raises(msk.MskError) as e:  # the adjoint needs a detector plane
-        ctx.stack_adjoint(s, v, [], np.zeros((1, 0, 32, 32), np.float32))
+        ctx.adjoint(s, v, [], np.zeros((1, 0, 32, 32), np.float32))
     assert e.value.status == msk.MSK_EINVAL
 
 

@@ -146,6 +146,7 @@ def test_stack_adjoint_matches_central_differences(oracle):
     assert abs(L / oracle.stack_loss(p, v, rp, T) - 1.0) < 1e-12
     rng = np.random.default_rng(9)
     gmax = np.abs(g).max()
+    vox, fds = [], []
     for _ in range(12):
         k, i, j = rng.integers(0, 6), rng.integers(0, 32), rng.integers(0, 32)
         h = 1e-3 * max(1.0, abs(v[k, i, j]))
@@ -155,6 +156,11 @@ def test_stack_adjoint_matches_central_differences(oracle):
         vm[k, i, j] -= h
         fd = (oracle.stack_loss(p, vp, rp, T) - oracle.stack_loss(p, vm, rp, T)) / (2 * h)
         assert abs(fd - g[k, i, j]) <= 1e-6 * max(abs(fd), 1e-3 * gmax)
+        vox.append((k, i, j))
+        fds.append(fd)
+    # the incremental finite differences (base waves reused, threads) agree
+    fast = oracle.stack_fd(p, v, rp, T, vox, nthreads=3)
+    assert np.allclose(fast, fds, rtol=1e-6, atol=1e-9 * gmax)  # FD rounding ~1e-8
 
 
 def test_stack_images_free_space_is_unitary(oracle):

@@ -27,7 +27,7 @@ EXPORTS = ("msk_create", "msk_destroy", "msk_last_error", "msk_status_string", "
            "msk_tilt_series", "msk_slice_count", "msk_slice_assign", "msk_sort_by_z",
            "msk_rotate", "msk_potential_table", "msk_set_stream", "msk_profile",
            "msk_profile_read", "msk_calculate_static", "msk_tilt_series_per_angle",
-           "msk_stack_images", "msk_stack_adjoint", "msk_potential_stack")
+           "msk_stack_images", "msk_adjoint", "msk_potential_stack")
 
 
 class MskError(RuntimeError):
@@ -108,7 +108,7 @@ def load():
     L.msk_calculate_static.argtypes = [vp, vp, vp, _fp, C.c_int, vp, vp, vp, vp, vp, C.c_float,
                                        C.c_float, C.c_int]
     L.msk_stack_images.argtypes = [vp, C.POINTER(Stack), C.c_int, vp, C.c_int, vp, vp]
-    L.msk_stack_adjoint.argtypes = [vp, C.POINTER(Stack), C.c_int, vp, C.c_int, vp, vp, vp,
+    L.msk_adjoint.argtypes = [vp, C.POINTER(Stack), C.c_int, vp, C.c_int, vp, vp, vp,
                                     C.POINTER(C.c_double)]
     L.msk_potential_stack.argtypes = [vp, C.POINTER(Series), C.c_int, vp, vp, vp, vp, vp,
                                       C.c_int, _dp, _dp, vp, vp]
@@ -322,8 +322,8 @@ class Context:
         self._check(st)
         return images
 
-    def stack_adjoint(self, stack, v, defocus, target, grad=None):
-        """(loss, dL/dv) for L = sum (I - target)^2 (msk_stack_adjoint);
+    def adjoint(self, stack, v, defocus, target, grad=None):
+        """(loss, dL/dv) for L = sum (I - target)^2 (msk_adjoint);
         grad has v's shape; v / target / grad may be torch CUDA tensors."""
         v = self._f32(v)
         target = self._f32(target)
@@ -332,7 +332,7 @@ class Context:
         if grad is None:
             grad = np.zeros(tuple(v.shape), np.float32)
         loss = C.c_double(0.0)
-        st = self.L.msk_stack_adjoint(self.h, C.byref(stack), nu, _ptr(v), len(defocus),
+        st = self.L.msk_adjoint(self.h, C.byref(stack), nu, _ptr(v), len(defocus),
                                       _ptr(defocus), _ptr(target), _ptr(grad), C.byref(loss))
         self._check(st)
         return loss.value, grad

@@ -1782,7 +1782,7 @@ int msk_stack_images(msk_context *ctx, const msk_stack *s, int nunits, const flo
     return stack_run(ctx, J);
 }
 
-int msk_stack_adjoint(msk_context *ctx, const msk_stack *s, int nunits, const float *v,
+int msk_adjoint(msk_context *ctx, const msk_stack *s, int nunits, const float *v,
                       int ndefocus, const double *defocus, const float *target, float *grad,
                       double *loss)
 {
