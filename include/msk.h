@@ -119,6 +119,32 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
                     const double *defocus, int nconfig, const float *displacements,
                     float *images, float *exitwaves, int *kept);
 
+/* Many specimens in one call: MultisliceT.cpp:398-448 run for each specimen,
+ * with its own atoms, box, grid and orientations; the common beam, slicing,
+ * lens and defocus settings come from `s` (its nx, ny, ctblength,
+ * ctblengthz and max_batch are not read).  All specimens' tables, atoms,
+ * waves and images live in one device arena (in waves of specimens when they
+ * do not fit); specimens run on concurrent streams, longest first.  With
+ * flags & MSK_BATCH_GRAPH the launches are captured into one CUDA graph and
+ * launched once.  Results equal msk_tilt_series per specimen. */
+typedef struct {
+    int natom;
+    const int *Znum;
+    const float *x, *y, *z, *occ;
+    int nx, ny;                       /* this specimen's grid */
+    float ctblength, ctblengthz;      /* this specimen's box, Angstrom */
+    int nangles;
+    const double *angleZ, *angleY;    /* radians */
+    float *images;   /* out: float[nangles][ndefocus][nx][ny], host or device */
+    int *kept;       /* out (may be NULL): int[nangles] */
+} msk_specimen;
+
+enum { MSK_BATCH_GRAPH = 1 };
+
+int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int nspec,
+                          const msk_specimen *spec, int ndefocus, const double *defocus,
+                          int flags);
+
 /* calculate() without any allocation -- no counterpart in the reference.
  * For callers that cannot allocate device memory (a plug-in inside a host
  * framework that owns all device memory through its own pool, or a loop that

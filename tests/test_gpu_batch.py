@@ -1,0 +1,80 @@
+"""msk_tilt_series_batch: specimens of different atom counts, boxes, grids and
+orientation counts in one call (concurrent streams, optionally one CUDA
+graph).  Each specimen's images must equal msk_tilt_series on that specimen
+alone, bit for bit: the same kernels run on the same data, only the order of
+independent launches differs."""
+import numpy as np
+import pytest
+
+from utr_public_gb300 import specimen as sp
+
+pytestmark = pytest.mark.gpu
+
+
+def series(msk, aobj=0.0, cs3=0.0):
+    s = msk.Series()
+    s.v0, s.deltaz, s.aobj, s.cs3 = 300.0, 1.0, aobj, cs3
+    return s
+
+
+def batch_case():
+    out = []
+    for i, (natom, fov, n, nang) in enumerate([(400, 32.0, 64, 3), (600, 48.0, 128, 1),
+                                               (300, 40.0, 64, 2), (900, 64.0, 256, 5),
+                                               (0, 32.0, 32, 2)]):
+        edge = fov / np.sqrt(2.0)
+        lo = 0.5 * (fov - edge)
+        spec = sp.random_specimen(natom, fov, lo, lo + edge, 2000 + i)
+        aY = np.deg2rad(np.linspace(0.0, 170.0, nang))
+        aZ = np.full(nang, 0.05 * i)
+        out.append((spec, n, aZ, aY))
+    return out
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_batch_equals_single_specimen_calls(ctx, msk, graph):
+    cases = batch_case()
+    defoci = [0.0, 300.0]
+    s = series(msk, aobj=0.015, cs3=1e6)
+    imgs, kept = ctx.tilt_series_batch(s, cases, defoci, graph=graph)
+    for (spec, n, aZ, aY), im, k in zip(cases, imgs, kept):
+        s1 = series(msk, aobj=0.015, cs3=1e6)
+        s1.nx = s1.ny = n
+        s1.ctblength = s1.ctblengthz = spec.fov
+        ref, k1 = ctx.tilt_series(s1, spec.Znum, spec.x, spec.y, spec.z, spec.occ, aZ, aY,
+                                  defoci)
+        assert np.array_equal(k, k1)
+        assert np.array_equal(im, ref)
+
+
+def test_batch_device_images_and_repeat(ctx, msk):
+    torch = pytest.importorskip("torch")
+    cases = batch_case()
+    defoci = [50.0]
+    s = series(msk)
+    host, _ = ctx.tilt_series_batch(s, cases, defoci)
+    dev = [torch.zeros((len(aZ), 1, n, n), dtype=torch.float32, device="cuda")
+           for _, n, aZ, _ in cases]
+    ctx.tilt_series_batch(s, cases, defoci, images=dev)
+    for h, d in zip(host, dev):
+        assert np.array_equal(h, d.cpu().numpy())
+    again, _ = ctx.tilt_series_batch(s, cases, defoci)  # the arena is reused
+    for h, a in zip(host, again):
+        assert np.array_equal(h, a)
+
+
+def test_batch_errors(ctx, msk):
+    cases = batch_case()[:2]
+    s = series(msk)
+    bad = [(cases[0][0], 48, cases[0][2], cases[0][3])]
+    with pytest.raises(msk.MskError) as e:
+        ctx.tilt_series_batch(s, bad, [0.0])
+    assert e.value.status == msk.MSK_EUNSUPPORTED
+    spec = sp.random_specimen(10, 32.0, 8.0, 24.0, 7)
+    spec.Znum[3] = 104
+    with pytest.raises(msk.MskError) as e:
+        ctx.tilt_series_batch(s, [cases[1], (spec, 64, [0.0], [0.0])], [0.0])
+    assert e.value.status == msk.MSK_EZNUM
+    # the context stays usable
+    imgs, _ = ctx.tilt_series_batch(s, cases, [0.0])
+    assert all(np.isfinite(i).all() for i in imgs)

@@ -27,7 +27,8 @@ EXPORTS = ("msk_create", "msk_destroy", "msk_last_error", "msk_status_string", "
            "msk_tilt_series", "msk_slice_count", "msk_slice_assign", "msk_sort_by_z",
            "msk_rotate", "msk_potential_table", "msk_set_stream", "msk_profile",
            "msk_profile_read", "msk_calculate_static", "msk_tilt_series_per_angle",
-           "msk_stack_images", "msk_adjoint", "msk_potential_stack")
+           "msk_stack_images", "msk_adjoint", "msk_potential_stack", "msk_tilt_series_batch")
+MSK_BATCH_GRAPH = 1
 
 
 class MskError(RuntimeError):
@@ -53,6 +54,15 @@ class Stack(C.Structure):
                 ("ctilty", C.c_float), ("aobj", C.c_float), ("cs3", C.c_double),
                 ("cs5", C.c_double), ("nslices", C.c_int), ("checkpoint", C.c_int),
                 ("max_batch", C.c_int)]
+
+
+class SpecimenDesc(C.Structure):
+    """msk_specimen (include/msk.h): one specimen of a batch."""
+    _fields_ = [("natom", C.c_int), ("Znum", C.c_void_p), ("x", C.c_void_p), ("y", C.c_void_p),
+                ("z", C.c_void_p), ("occ", C.c_void_p), ("nx", C.c_int), ("ny", C.c_int),
+                ("ctblength", C.c_float), ("ctblengthz", C.c_float), ("nangles", C.c_int),
+                ("angleZ", C.c_void_p), ("angleY", C.c_void_p), ("images", C.c_void_p),
+                ("kept", C.c_void_p)]
 
 
 class KernelStat(C.Structure):
@@ -112,6 +122,8 @@ def load():
                                     C.POINTER(C.c_double)]
     L.msk_potential_stack.argtypes = [vp, C.POINTER(Series), C.c_int, vp, vp, vp, vp, vp,
                                       C.c_int, _dp, _dp, vp, vp]
+    L.msk_tilt_series_batch.argtypes = [vp, C.POINTER(Series), C.c_int, C.POINTER(SpecimenDesc),
+                                        C.c_int, vp, C.c_int]
     _lib = L
     return L
 
@@ -289,6 +301,41 @@ class Context:
         if hasattr(a, "data_ptr"):
             return a
         return np.ascontiguousarray(a, np.float32)
+
+    def tilt_series_batch(self, series, specimens, defocus, graph=True, images=None):
+        """Many specimens in one call (msk_tilt_series_batch).  specimens: list
+        of (Specimen-like with Znum/x/y/z/occ/fov, n, angleZ, angleY[, ctblengthz]);
+        returns (images list [nangles, ndef, n, n] per specimen, kept list).
+        images may be a list of preallocated arrays or torch CUDA tensors."""
+        defocus = np.ascontiguousarray(defocus, np.float64)
+        nd = len(defocus)
+        descs = (SpecimenDesc * len(specimens))()
+        keep, outs, kepts = [], [], []
+        for i, item in enumerate(specimens):
+            sp_, n, aZ, aY = item[:4]
+            zc = item[4] if len(item) > 4 else sp_.fov
+            arrs = [np.ascontiguousarray(a, dt) for a, dt in
+                    ((sp_.Znum, np.int32), (sp_.x, np.float32), (sp_.y, np.float32),
+                     (sp_.z, np.float32), (sp_.occ, np.float32))]
+            aZ = np.ascontiguousarray(aZ, np.float64)
+            aY = np.ascontiguousarray(aY, np.float64)
+            img = images[i] if images is not None else np.zeros((len(aZ), nd, n, n), np.float32)
+            kp = np.zeros(len(aZ), np.int32)
+            keep += arrs + [aZ, aY]
+            outs.append(img)
+            kepts.append(kp)
+            d = descs[i]
+            d.natom = len(arrs[1])
+            d.Znum, d.x, d.y, d.z, d.occ = [_ptr(a) for a in arrs]
+            d.nx = d.ny = n
+            d.ctblength, d.ctblengthz = sp_.fov, zc
+            d.nangles = len(aZ)
+            d.angleZ, d.angleY = _ptr(aZ), _ptr(aY)
+            d.images, d.kept = _ptr(img), _ptr(kp)
+        st = self.L.msk_tilt_series_batch(self.h, C.byref(series), len(specimens), descs, nd,
+                                          _ptr(defocus), MSK_BATCH_GRAPH if graph else 0)
+        self._check(st)
+        return outs, kepts
 
     def potential_stack(self, series, Znum, x, y, z, occ, angleZ, angleY, v=None):
         """Per-slice projected potentials v [nangles, nslices, nx, ny] of a tilt

@@ -341,6 +341,7 @@ struct GridPre {
     double scalex, scaley;  // float-divided pixel pitch, promoted
     double sigma;
     Geom g;                 // device pointers filled at upload
+    const float *d_kx = nullptr, *d_ky = nullptr;  // device kx, ky (free-space step)
     std::vector<float> kx, kx2, ky, ky2;
     std::vector<float2> propx, propy;
 };
@@ -657,6 +658,9 @@ struct msk_context {
         flags;
     DevBuf pa_v, pa_t, pa_psi, pa_e;  // buffers of the per-orientation comparison form
     DevBuf stk, stk_v, stk_g, stk_t, stk_img, stk_part, adjtab;  // potential stacks, adjoint
+    DevBuf arena;                                // specimen batches
+    std::vector<cudaStream_t> lanes;             // concurrent specimens of a batch
+    std::vector<cudaEvent_t> lane_ev;            // lane joins (one per lane) + fork
     size_t units_alloc = 0;  // units the psi / tbuf buffers hold
     std::vector<int> zmap = std::vector<int>(104, -1);
 };
@@ -793,9 +797,14 @@ void prof_collect(msk_context *ctx)
     ctx->prof_pending.clear();
 }
 
-// Compact atomic-number map and device tables (frequency grids, propagator,
-// twiddles, potential spline) for one grid.
-int upload_tables(msk_context *ctx, GridPre &gp, const std::vector<int> &zlist)
+// Device tables of one grid (frequency grids, propagator, twiddles, potential
+// spline, band-limit ranges) laid out in one block of 256-byte aligned pieces.
+struct TableLayout {
+    size_t kx2, ky2, kx, ky, px, py, twr, twc, kn, cf, kb, bytes;
+};
+
+static void build_tables(const GridPre &gp, const std::vector<int> &zlist,
+                         std::vector<unsigned char> &host, TableLayout &o)
 {
     std::vector<float2> twr, twc;
     twiddles(gp.ny, twr);
@@ -812,63 +821,74 @@ int upload_tables(msk_context *ctx, GridPre &gp, const std::vector<int> &zlist)
             coef[(size_t)zi * phys::kN + i] = make_float4((float)L.y[Z][i], (float)L.b[Z][i],
                                                           (float)L.c[Z][i], (float)L.d[Z][i]);
     }
-    // one allocation, 256-byte aligned pieces
     size_t off = 0;
     auto piece = [&](size_t bytes) {
-        size_t o = off;
+        size_t q = off;
         off += (bytes + 255) & ~size_t(255);
-        return o;
+        return q;
     };
-    const size_t o_kx2 = piece(4 * gp.nx), o_ky2 = piece(4 * gp.ny), o_kx = piece(4 * gp.nx),
-                 o_ky = piece(4 * gp.ny), o_px = piece(8 * gp.nx), o_py = piece(8 * gp.ny),
-                 o_twr = piece(8 * twr.size()), o_twc = piece(8 * twc.size()),
-                 o_kn = piece(4 * knots.size()), o_cf = piece(16 * coef.size()),
-                 o_kb = piece(8 * gp.ny);
-    std::vector<unsigned char> host(off);
-    std::memcpy(&host[o_kx2], gp.kx2.data(), 4 * gp.nx);
-    std::memcpy(&host[o_ky2], gp.ky2.data(), 4 * gp.ny);
-    std::memcpy(&host[o_kx], gp.kx.data(), 4 * gp.nx);
-    std::memcpy(&host[o_ky], gp.ky.data(), 4 * gp.ny);
-    std::memcpy(&host[o_px], gp.propx.data(), 8 * gp.nx);
-    std::memcpy(&host[o_py], gp.propy.data(), 8 * gp.ny);
-    std::memcpy(&host[o_twr], twr.data(), 8 * twr.size());
-    std::memcpy(&host[o_twc], twc.data(), 8 * twc.size());
-    std::memcpy(&host[o_kn], knots.data(), 4 * knots.size());
-    std::memcpy(&host[o_cf], coef.data(), 16 * coef.size());
-    std::memcpy(&host[o_kb], gp.kband.data(), 8 * gp.ny);
-    MSK_CUDA(ctx, ctx->tables.reserve(off));
-    MSK_CUDA(ctx, cudaMemcpyAsync(ctx->tables.p, host.data(), off, cudaMemcpyHostToDevice,
+    o.kx2 = piece(4 * gp.nx);
+    o.ky2 = piece(4 * gp.ny);
+    o.kx = piece(4 * gp.nx);
+    o.ky = piece(4 * gp.ny);
+    o.px = piece(8 * gp.nx);
+    o.py = piece(8 * gp.ny);
+    o.twr = piece(8 * twr.size());
+    o.twc = piece(8 * twc.size());
+    o.kn = piece(4 * knots.size());
+    o.cf = piece(16 * coef.size());
+    o.kb = piece(8 * gp.ny);
+    o.bytes = off;
+    host.assign(off, 0);
+    std::memcpy(&host[o.kx2], gp.kx2.data(), 4 * gp.nx);
+    std::memcpy(&host[o.ky2], gp.ky2.data(), 4 * gp.ny);
+    std::memcpy(&host[o.kx], gp.kx.data(), 4 * gp.nx);
+    std::memcpy(&host[o.ky], gp.ky.data(), 4 * gp.ny);
+    std::memcpy(&host[o.px], gp.propx.data(), 8 * gp.nx);
+    std::memcpy(&host[o.py], gp.propy.data(), 8 * gp.ny);
+    std::memcpy(&host[o.twr], twr.data(), 8 * twr.size());
+    std::memcpy(&host[o.twc], twc.data(), 8 * twc.size());
+    std::memcpy(&host[o.kn], knots.data(), 4 * knots.size());
+    std::memcpy(&host[o.cf], coef.data(), 16 * coef.size());
+    std::memcpy(&host[o.kb], gp.kband.data(), 8 * gp.ny);
+}
+
+// Point the grid's Geom (and kx, ky for the free-space step) at a device copy
+// of its table block.
+static void bind_tables(GridPre &gp, const unsigned char *b, const TableLayout &o)
+{
+    Geom &g = gp.g;
+    g.kx2 = reinterpret_cast<const float *>(b + o.kx2);
+    g.ky2 = reinterpret_cast<const float *>(b + o.ky2);
+    g.propx = reinterpret_cast<const float2 *>(b + o.px);
+    g.propy = reinterpret_cast<const float2 *>(b + o.py);
+    g.tw_row = reinterpret_cast<const float2 *>(b + o.twr);
+    g.tw_col = reinterpret_cast<const float2 *>(b + o.twc);
+    g.knots = reinterpret_cast<const float *>(b + o.kn);
+    g.coef = reinterpret_cast<const float4 *>(b + o.cf);
+    g.kband = reinterpret_cast<const int2 *>(b + o.kb);
+    gp.d_kx = reinterpret_cast<const float *>(b + o.kx);
+    gp.d_ky = reinterpret_cast<const float *>(b + o.ky);
+}
+
+// Tables of one grid into the context's table buffer.
+int upload_tables(msk_context *ctx, GridPre &gp, const std::vector<int> &zlist)
+{
+    std::vector<unsigned char> host;
+    TableLayout o;
+    build_tables(gp, zlist, host, o);
+    MSK_CUDA(ctx, ctx->tables.reserve(o.bytes));
+    MSK_CUDA(ctx, cudaMemcpyAsync(ctx->tables.p, host.data(), o.bytes, cudaMemcpyHostToDevice,
                                   ctx->stream));
-    count_copy(ctx, 0, (double)off);
+    count_copy(ctx, 0, (double)o.bytes);
     // the host staging vector must outlive the copy
     MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    unsigned char *b = ctx->tables.as<unsigned char>();
-    Geom &g = gp.g;
-    g.kx2 = reinterpret_cast<const float *>(b + o_kx2);
-    g.ky2 = reinterpret_cast<const float *>(b + o_ky2);
-    g.propx = reinterpret_cast<const float2 *>(b + o_px);
-    g.propy = reinterpret_cast<const float2 *>(b + o_py);
-    g.tw_row = reinterpret_cast<const float2 *>(b + o_twr);
-    g.tw_col = reinterpret_cast<const float2 *>(b + o_twc);
-    g.knots = reinterpret_cast<const float *>(b + o_kn);
-    g.coef = reinterpret_cast<const float4 *>(b + o_cf);
-    g.kband = reinterpret_cast<const int2 *>(b + o_kb);
-    (void)o_kx;
-    (void)o_ky;
+    bind_tables(gp, ctx->tables.as<unsigned char>(), o);
     return MSK_OK;
 }
 
-const float *tables_kx(msk_context *ctx, const GridPre &gp)
-{
-    // kx follows kx2 and ky2 in the table block (see upload_tables)
-    size_t o = ((4 * (size_t)gp.nx + 255) & ~size_t(255)) + ((4 * (size_t)gp.ny + 255) & ~size_t(255));
-    return reinterpret_cast<const float *>(ctx->tables.as<unsigned char>() + o);
-}
-const float *tables_ky(msk_context *ctx, const GridPre &gp)
-{
-    size_t o = ((4 * (size_t)gp.nx + 255) & ~size_t(255)) * 2 + ((4 * (size_t)gp.ny + 255) & ~size_t(255));
-    return reinterpret_cast<const float *>(ctx->tables.as<unsigned char>() + o);
-}
+const float *tables_kx(msk_context *, const GridPre &gp) { return gp.d_kx; }
+const float *tables_ky(msk_context *, const GridPre &gp) { return gp.d_ky; }
 
 bool is_device_ptr(const void *p)
 {
@@ -888,8 +908,10 @@ struct Batch {
     std::vector<int> act;         // active units per slice
 };
 
-int upload_batch(msk_context *ctx, const std::vector<UnitAtoms> &ua, int u0, int nunits,
-                 int nslices, Batch &b)
+// Per-slice atom offsets, active units per slice and the packed atoms of
+// units u0 .. u0+nunits-1.
+void pack_batch(const std::vector<UnitAtoms> &ua, int u0, int nunits, int nslices, Batch &b,
+                std::vector<SplatAtom> &atoms)
 {
     b.nunits = nunits;
     b.nslices = nslices;
@@ -914,13 +936,20 @@ int upload_batch(msk_context *ctx, const std::vector<UnitAtoms> &ua, int u0, int
             if (ua[u0 + i].counts[s] > 0) b.act.push_back(i);
     }
     b.act_off[nslices] = (int)b.act.size();
-    std::vector<SplatAtom> atoms(std::max<size_t>(total, 1));
+    atoms.assign(std::max<size_t>(total, 1), SplatAtom{});
     size_t o = 0;
     for (int i = 0; i < nunits; i++) {
         const auto &a = ua[u0 + i].atoms;
         std::copy(a.begin(), a.end(), atoms.begin() + o);
         o += a.size();
     }
+}
+
+int upload_batch(msk_context *ctx, const std::vector<UnitAtoms> &ua, int u0, int nunits,
+                 int nslices, Batch &b)
+{
+    std::vector<SplatAtom> atoms;
+    pack_batch(ua, u0, nunits, nslices, b, atoms);
     MSK_CUDA(ctx, ctx->atoms.reserve(atoms.size() * sizeof(SplatAtom)));
     MSK_CUDA(ctx, ctx->slice_off.reserve(b.slice_off.size() * sizeof(int)));
     MSK_CUDA(ctx, ctx->act.reserve(std::max<size_t>(b.act.size(), 1) * sizeof(int)));
@@ -1055,11 +1084,13 @@ void msk_destroy(msk_context *ctx)
                       &ctx->imgmeta, &ctx->wave0, &ctx->images, &ctx->exitw, &ctx->fresnel,
                       &ctx->flags, &ctx->pa_v, &ctx->pa_t, &ctx->pa_psi, &ctx->pa_e, &ctx->stk,
                       &ctx->stk_v, &ctx->stk_g, &ctx->stk_t, &ctx->stk_img, &ctx->stk_part,
-                      &ctx->adjtab})
+                      &ctx->adjtab, &ctx->arena})
         b->release();
     for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_join, ctx->ev_t[0], ctx->ev_t[1], ctx->ev_free[0],
                           ctx->ev_free[1]})
         if (e) cudaEventDestroy(e);
+    for (cudaStream_t l : ctx->lanes) cudaStreamDestroy(l);
+    for (cudaEvent_t e : ctx->lane_ev) cudaEventDestroy(e);
     if (ctx->aux) cudaStreamDestroy(ctx->aux);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
@@ -1873,6 +1904,360 @@ int msk_potential_stack(msk_context *ctx, const msk_series *s, int natom, const 
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ specimen batches
+// msk_tilt_series_batch: many specimens -- each with its own atoms, box, grid
+// and orientations -- in one call.  Every specimen keeps its own tables,
+// atoms, waves and images in one device arena; specimens are spread over
+// concurrent streams (longest first onto the least-loaded stream) and, with
+// MSK_BATCH_GRAPH, the whole launch sequence is captured into one CUDA graph
+// and launched once.
+
+namespace {
+
+constexpr int kLanes = 8;
+
+struct SpecPlan {
+    GridPre gp;
+    int nslices = 0, nangles = 0;
+    std::vector<UnitAtoms> ua;
+    Batch b;
+    std::vector<SplatAtom> atoms;
+    std::vector<unsigned char> tables;
+    TableLayout tl;
+    std::vector<int> meta;  // per defocus: img_off[n+1] | units[n] | dst[n] | flags[n]
+    float ctblengthz = 0.0f;
+    size_t o_tab = 0, o_atoms = 0, o_soff = 0, o_act = 0, o_meta = 0;  // upload region
+    size_t o_fres = 0, o_psi = 0, o_tbuf = 0, o_img = 0;               // work region
+    bool img_dev = false;
+    double work = 0.0;
+    int lane = 0;
+};
+
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+int ensure_lanes(msk_context *ctx)
+{
+    while ((int)ctx->lanes.size() < kLanes) {
+        cudaStream_t l = nullptr;
+        MSK_CUDA(ctx, cudaStreamCreateWithFlags(&l, cudaStreamNonBlocking));
+        ctx->lanes.push_back(l);
+    }
+    while ((int)ctx->lane_ev.size() < kLanes + 1) {
+        cudaEvent_t e = nullptr;
+        MSK_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->lane_ev.push_back(e);
+    }
+    return MSK_OK;
+}
+
+// The launches of one specimen on one stream: plane wave, slice loop, then
+// per detector plane the free-space step and the intensity.
+int enqueue_specimen(msk_context *ctx, SpecPlan &P, unsigned char *arena, const msk_series *s,
+                     int ndef, const double *defocus, float *d_images, cudaStream_t st)
+{
+    const GridPre &gp = P.gp;
+    const Geom &g = gp.g;
+    const int nx = gp.nx, ny = gp.ny, na = P.nangles;
+    const size_t plane = (size_t)nx * ny;
+    const SizeOps *rop = size_ops(ny), *cop = size_ops(nx);
+    float2 *psi = reinterpret_cast<float2 *>(arena + P.o_psi);
+    float2 *tb = reinterpret_cast<float2 *>(arena + P.o_tbuf);
+    const int *act = reinterpret_cast<const int *>(arena + P.o_act);
+    const int *soff = reinterpret_cast<const int *>(arena + P.o_soff);
+    const SplatAtom *atoms = reinterpret_cast<const SplatAtom *>(arena + P.o_atoms);
+    CUtensorMap pmap, tmap;
+    int rc = column_map(ctx, &pmap, psi, nx, ny, na, cop);
+    if (rc) return rc;
+    rc = column_map(ctx, &tmap, tb, nx, ny, na, cop);
+    if (rc) return rc;
+    const double pl = (double)plane;
+    {
+        Prof p(ctx, kPlane, 8.0 * pl * na, st);
+        k_plane_init<<<1024, 256, 0, st>>>(psi, nullptr, na, nx, ny);
+    }
+    const int nsl1 = P.nslices + 1;
+    for (int sl = 0; sl < P.nslices; sl++) {
+        const int nact = P.b.act_off[sl + 1] - P.b.act_off[sl];
+        const int *units = act + P.b.act_off[sl];
+        if (nact > 0) {
+            {
+                Prof p(ctx, kSplat, 8.0 * pl * nact, st);
+                rop->splat(g, units, nact, sl, nsl1, soff, atoms, tb, st);
+            }
+            {
+                Prof p(ctx, kKColMask, 16.0 * pl * nact, st);
+                cop->col_mask(g, tmap, tmap, units, nact, st);
+            }
+            Prof p(ctx, kTransmit, 24.0 * pl * nact, st);
+            rop->row_transmit(g, units, nact, tb, psi, psi, 1.0f / ((float)ny * (float)ny), st);
+        }
+        if (s->nmode == 0) {
+            Prof p(ctx, kKColProp, 16.0 * pl * na, st);
+            cop->col_prop(g, pmap, pmap, nullptr, na, st);
+        }
+    }
+    const double pi = 4.0 * atan(1.0), l = gp.wavlen;
+    float k2maxo = s->aobj / gp.wavlen;
+    k2maxo = k2maxo * k2maxo;
+    const size_t nmeta = 4 * (size_t)na + 1;
+    for (int d = 0; d < ndef; d++) {
+        Fresnel fr{};
+        const double rprime = defocus[d] - 0.5 * P.ctblengthz;  // autosliccmd.cpp:1060
+        fr.a1 = pi * l * rprime;
+        fr.a3 = (pi / 2.0) * s->cs3 * l * l * l;
+        fr.a5 = (pi / 3.0) * s->cs5 * l * l * l * l * l;
+        fr.a2c = (pi / 2.0) * l * s->astig * cos(2.0 * s->astig_angle);
+        fr.a2s = (pi / 2.0) * l * s->astig * sin(2.0 * s->astig_angle);
+        fr.k2maxo = k2maxo;
+        fr.kx = gp.d_kx;
+        fr.ky = gp.d_ky;
+        float2 *tab = reinterpret_cast<float2 *>(arena + P.o_fres) + (size_t)d * plane;
+        fr.table = tab;
+        {
+            Prof p(ctx, kFresTab, 8.0 * pl, st);
+            k_fresnel_table<<<4 * 152, 256, 0, st>>>(g, fr, 1.0f / ((float)nx * (float)ny), tab);
+        }
+        {
+            Prof p(ctx, kFresnel, 16.0 * pl * na, st);
+            cop->col_fresnel(g, pmap, tmap, nullptr, na, fr, 1.0f, st);
+        }
+        const int *dm = reinterpret_cast<const int *>(arena + P.o_meta) + (size_t)d * nmeta;
+        Prof p(ctx, kIntensity, 12.0 * pl * na, st);
+        rop->row_intensity(g, na, dm, dm + na + 1, dm + 2 * na + 1, dm + 3 * na + 1, tb, d_images,
+                           1.0f, st);
+    }
+    MSK_CUDA(ctx, cudaGetLastError());
+    return MSK_OK;
+}
+
+}  // namespace
+
+extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int nspec,
+                                     const msk_specimen *spec, int ndefocus,
+                                     const double *defocus, int flags)
+{
+    if (!ctx) return MSK_EINVAL;
+    ctx->err.clear();
+    if (!s || nspec < 1 || !spec || ndefocus < 0 || (ndefocus > 0 && !defocus))
+        return fail(ctx, MSK_EINVAL, "bad batch arguments");
+    for (int i = 0; i < nspec; i++) {
+        const msk_specimen &q = spec[i];
+        if (q.natom < 0 || q.nangles < 1 || !q.angleZ || !q.angleY ||
+            (ndefocus > 0 && !q.images) ||
+            (q.natom > 0 && (!q.Znum || !q.x || !q.y || !q.z || !q.occ)))
+            return fail(ctx, MSK_EINVAL, "bad specimen " + std::to_string(i));
+        if (q.nx < 1 || q.ny < 1 || q.ctblength < 0.0f)
+            return fail(ctx, MSK_EBADSIZE, "bad size parameters of specimen " + std::to_string(i));
+        if (!pow2_supported(q.nx) || !pow2_supported(q.ny))
+            return fail(ctx, MSK_EUNSUPPORTED, "grid must be a power of two from 16 to 4096");
+    }
+    MSK_CUDA(ctx, cudaSetDevice(ctx->device));
+    int st = ensure_lanes(ctx);
+    if (st) return st;
+
+    // one compact Z map over every specimen
+    std::vector<int> allZ;
+    for (int i = 0; i < nspec; i++) allZ.insert(allZ.end(), spec[i].Znum, spec[i].Znum + spec[i].natom);
+    std::vector<int> zlist;
+    st = build_zmap(ctx, (int)allZ.size(), allZ.data(), zlist);
+    if (st) return st;
+
+    // host preparation: grids, then every (specimen, orientation) unit in parallel
+    std::vector<SpecPlan> P(nspec);
+    std::vector<std::pair<int, int>> units;
+    for (int i = 0; i < nspec; i++) {
+        const msk_specimen &q = spec[i];
+        if (!grid_pre(P[i].gp, q.nx, q.ny, q.ctblength, q.ctblength, s->v0, s->deltaz, 0.0f, 0.0f))
+            return fail(ctx, MSK_EUNSUPPORTED, "band limit is not two index ranges per column");
+        P[i].nslices = slice_count(s->deltaz, q.ctblengthz);
+        P[i].nangles = q.nangles;
+        P[i].ctblengthz = q.ctblengthz;
+        P[i].ua.resize(q.nangles);
+        for (int a = 0; a < q.nangles; a++) units.push_back({i, a});
+    }
+    parallel_for((int)units.size(), host_threads(), [&](int k) {
+        const int i = units[k].first, a = units[k].second;
+        const msk_specimen &q = spec[i];
+        PrepSpec ps{q.natom, q.Znum, q.x, q.y, q.z, q.occ, q.ctblength, q.ctblengthz, s->deltaz,
+                    P[i].nslices, true, q.angleZ[a], q.angleY[a], s->dxc, s->dyc, s->dzc,
+                    nullptr, true, ctx->zmap.data()};
+        prep_unit(P[i].gp, ps, P[i].ua[a]);
+    });
+    for (int i = 0; i < nspec; i++)
+        for (int a = 0; a < spec[i].nangles; a++)
+            if (P[i].ua[a].status)
+                return fail(ctx, P[i].ua[a].status, "specimen " + std::to_string(i) + ": " +
+                                                         msk_status_string(P[i].ua[a].status));
+    parallel_for(nspec, host_threads(), [&](int i) {
+        SpecPlan &q = P[i];
+        build_tables(q.gp, zlist, q.tables, q.tl);
+        pack_batch(q.ua, 0, q.nangles, q.nslices, q.b, q.atoms);
+        const int na = q.nangles;
+        q.meta.clear();
+        for (int d = 0; d < ndefocus; d++) {
+            for (int a = 0; a <= na; a++) q.meta.push_back(a);         // img_off
+            for (int a = 0; a < na; a++) q.meta.push_back(a);          // img_units
+            for (int a = 0; a < na; a++) q.meta.push_back(a * ndefocus + d);  // img_dst
+            for (int a = 0; a < na; a++) q.meta.push_back(0);          // img_flags
+        }
+        q.work = (double)na * q.nslices * q.gp.nx * q.gp.ny;
+        q.img_dev = ndefocus > 0 && is_device_ptr(spec[i].images);
+    });
+
+    // waves of specimens whose arena fits the memory budget
+    size_t free_b = 0, total_b = 0;
+    MSK_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
+    const size_t budget = (size_t)((double)(free_b + ctx->arena.cap) * 0.8);
+    auto arena_of = [&](SpecPlan &q, size_t &up, size_t &work) {
+        const size_t plane = (size_t)q.gp.nx * q.gp.ny;
+        q.o_tab = up;
+        up += align256(q.tables.size());
+        q.o_atoms = up;
+        up += align256(q.atoms.size() * sizeof(SplatAtom));
+        q.o_soff = up;
+        up += align256(q.b.slice_off.size() * sizeof(int));
+        q.o_act = up;
+        up += align256(std::max<size_t>(q.b.act.size(), 1) * sizeof(int));
+        q.o_meta = up;
+        up += align256(std::max<size_t>(q.meta.size(), 1) * sizeof(int));
+        q.o_fres = work;
+        work += align256((size_t)std::max(ndefocus, 1) * plane * sizeof(float2));
+        q.o_psi = work;
+        work += align256((size_t)q.nangles * plane * sizeof(float2));
+        q.o_tbuf = work;
+        work += align256((size_t)q.nangles * plane * sizeof(float2));
+        q.o_img = work;
+        if (!q.img_dev) work += align256((size_t)q.nangles * ndefocus * plane * sizeof(float));
+    };
+    const bool graph = (flags & MSK_BATCH_GRAPH) && !ctx->prof_on;
+    int first = 0;
+    while (first < nspec) {
+        // the next wave: as many specimens (in order) as fit
+        int last = first;
+        size_t up = 0, work = 0;
+        for (; last < nspec; last++) {
+            size_t up2 = up, work2 = work;
+            arena_of(P[last], up2, work2);
+            if (last > first && up2 + work2 > budget) break;
+            up = up2;
+            work = work2;
+        }
+        // offsets of the work region follow the upload region
+        for (int i = first; i < last; i++) {
+            P[i].o_fres += align256(up);
+            P[i].o_psi += align256(up);
+            P[i].o_tbuf += align256(up);
+            P[i].o_img += align256(up);
+        }
+        const size_t total = align256(up) + work;
+        MSK_CUDA(ctx, ctx->arena.reserve(total));
+        unsigned char *arena = ctx->arena.as<unsigned char>();
+        std::vector<unsigned char> host(up);
+        for (int i = first; i < last; i++) {
+            SpecPlan &q = P[i];
+            std::memcpy(&host[q.o_tab], q.tables.data(), q.tables.size());
+            if (!q.atoms.empty())
+                std::memcpy(&host[q.o_atoms], q.atoms.data(), q.atoms.size() * sizeof(SplatAtom));
+            std::memcpy(&host[q.o_soff], q.b.slice_off.data(), q.b.slice_off.size() * sizeof(int));
+            if (!q.b.act.empty())
+                std::memcpy(&host[q.o_act], q.b.act.data(), q.b.act.size() * sizeof(int));
+            if (!q.meta.empty())
+                std::memcpy(&host[q.o_meta], q.meta.data(), q.meta.size() * sizeof(int));
+            bind_tables(q.gp, arena + q.o_tab, q.tl);
+        }
+        MSK_CUDA(ctx, cudaMemcpyAsync(arena, host.data(), up, cudaMemcpyHostToDevice, ctx->stream));
+        count_copy(ctx, 0, (double)up);
+        Geom gflag{};
+        st = flags_reset(ctx, gflag);
+        if (st) return st;
+        MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (int i = first; i < last; i++) P[i].gp.g.err = gflag.err;
+
+        // longest specimen first onto the least-loaded lane
+        std::vector<int> order;
+        for (int i = first; i < last; i++) order.push_back(i);
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int a, int b) { return P[a].work > P[b].work; });
+        const int nl = ctx->prof_on ? 1 : kLanes;
+        std::vector<double> load(nl, 0.0);
+        std::vector<std::vector<int>> lane_of(nl);
+        for (int i : order) {
+            const int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+            load[l] += P[i].work;
+            lane_of[l].push_back(i);
+        }
+        cudaGraph_t gr = nullptr;
+        if (graph)
+            MSK_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed));
+        int rc = MSK_OK;
+        if (nl == 1) {
+            for (int i : lane_of[0]) {
+                float *dimg = P[i].img_dev ? spec[i].images : reinterpret_cast<float *>(arena + P[i].o_img);
+                if ((rc = enqueue_specimen(ctx, P[i], arena, s, ndefocus, defocus, dimg, ctx->stream)))
+                    break;
+            }
+        } else {
+            cudaEvent_t fork = ctx->lane_ev[kLanes];
+            if (cudaEventRecord(fork, ctx->stream) != cudaSuccess) rc = fail(ctx, MSK_ECUDA, "fork");
+            for (int l = 0; l < nl && !rc; l++) {
+                if (cudaStreamWaitEvent(ctx->lanes[l], fork, 0) != cudaSuccess) {
+                    rc = fail(ctx, MSK_ECUDA, "lane wait");
+                    break;
+                }
+                for (int i : lane_of[l]) {
+                    float *dimg = P[i].img_dev ? spec[i].images : reinterpret_cast<float *>(arena + P[i].o_img);
+                    if ((rc = enqueue_specimen(ctx, P[i], arena, s, ndefocus, defocus, dimg,
+                                               ctx->lanes[l])))
+                        break;
+                }
+                if (!rc && cudaEventRecord(ctx->lane_ev[l], ctx->lanes[l]) != cudaSuccess)
+                    rc = fail(ctx, MSK_ECUDA, "lane join");
+            }
+            for (int l = 0; l < nl && !rc; l++)
+                if (cudaStreamWaitEvent(ctx->stream, ctx->lane_ev[l], 0) != cudaSuccess)
+                    rc = fail(ctx, MSK_ECUDA, "join wait");
+        }
+        if (graph) {
+            cudaError_t e = cudaStreamEndCapture(ctx->stream, &gr);
+            if (!rc && e != cudaSuccess)
+                rc = fail(ctx, MSK_ECUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+            if (!rc) {
+                cudaGraphExec_t ex = nullptr;
+                e = cudaGraphInstantiate(&ex, gr, 0);
+                if (e == cudaSuccess) e = cudaGraphLaunch(ex, ctx->stream);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+                if (ex) cudaGraphExecDestroy(ex);
+                if (e != cudaSuccess)
+                    rc = fail(ctx, MSK_ECUDA, std::string("graph launch: ") + cudaGetErrorString(e));
+            }
+            if (gr) cudaGraphDestroy(gr);
+        }
+        if (rc) {  // nothing of this wave may still run when the arena is reused
+            for (cudaStream_t l : ctx->lanes) cudaStreamSynchronize(l);
+            cudaStreamSynchronize(ctx->stream);
+            return rc;
+        }
+        // images to host buffers
+        for (int i = first; i < last; i++) {
+            if (ndefocus == 0 || P[i].img_dev) continue;
+            const size_t bytes = (size_t)P[i].nangles * ndefocus * P[i].gp.nx * P[i].gp.ny * sizeof(float);
+            MSK_CUDA(ctx, cudaMemcpyAsync(spec[i].images, arena + P[i].o_img, bytes,
+                                          cudaMemcpyDeviceToHost, ctx->stream));
+            count_copy(ctx, 1, (double)bytes);
+        }
+        MSK_CUDA(ctx, cudaGetLastError());
+        MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        prof_collect(ctx);
+        st = flags_check(ctx);
+        if (st) return st;
+        first = last;
+    }
+    for (int i = 0; i < nspec; i++)
+        if (spec[i].kept)
+            for (int a = 0; a < spec[i].nangles; a++) spec[i].kept[a] = P[i].ua[a].kept;
+    return MSK_OK;
+}
 
 // ------------------------------------------------------------------ allocation-free calculate()
 //
