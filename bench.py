@@ -377,6 +377,134 @@ def run_adjoint(args, rank, world, local_rank):
     print(json.dumps(out))
 
 
+UNEVEN_METRIC = ("uneven-batch slice-steps/s (64 specimens, 5e3-2e5 atoms, 256^2-2048^2, 1-90 "
+                 "orientations, FP32, one CUDA graph)")
+
+
+def run_uneven(args, rank, world, local_rank):
+    """C4: 64 specimens of log-uniform atom count, field of view sqrt(2) x edge,
+    grids drawn from {256, 512, 1024, 2048}, 1..90 orientations evenly over 180
+    degrees, 300 keV, 1 A slices, two detector defoci; one msk_tilt_series_batch
+    call (one CUDA graph) per step."""
+    import torch
+    import utr_public_gb300 as msk
+    from utr_public_gb300 import specimen
+    torch.cuda.set_device(local_rank)
+    msk.load()
+    ctx = msk.Context(local_rank)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    batch = specimen.uneven_batch(64, 1004)
+    cases = []
+    for sp_, n, nang in batch:
+        aY = np.deg2rad(np.arange(nang) * (180.0 / nang))
+        cases.append((sp_, n, np.full(nang, 0.1 * rank), aY))
+    s = msk.Series()
+    s.v0, s.deltaz = V0, DZ
+    defoci = np.array(DEFOCI)
+    imgs = [torch.empty((len(c[2]), len(defoci), c[1], c[1]), dtype=torch.float32, device="cuda")
+            for c in cases]
+    nsl = [msk.slice_count(DZ, c[0].fov) for c in cases]
+    steps = [len(c[2]) * k for c, k in zip(cases, nsl)]
+
+    def timed(fn, k):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / k
+
+    run = lambda graph, sel=None: ctx.tilt_series_batch(
+        s, cases if sel is None else [cases[i] for i in sel], defoci, graph=graph,
+        images=imgs if sel is None else [imgs[i] for i in sel])
+    for _ in range(args.warmup):
+        run(True)
+    clocks = Clocks(gpu_index(local_rank))
+    ms = timed(lambda: run(True), args.steps)
+    clk = clocks.stop()
+    total = sum(steps)
+    value = world * total / (ms / 1000.0)
+    ms_streams = timed(lambda: run(False), 1)
+    per_size = {}
+    for n in (256, 512, 1024, 2048):
+        sel = [i for i, c in enumerate(cases) if c[1] == n]
+        if not sel:
+            continue
+        run(True, sel)
+        t = timed(lambda: run(True, sel), 1)
+        st_ = sum(steps[i] for i in sel)
+        per_size[str(n)] = {"specimens": len(sel), "slice_steps": st_, "ms": t,
+                            "slice_steps_per_s": st_ / (t / 1000.0)}
+    ctx.profile(True)
+    ms_serial = timed(lambda: run(False), 1)
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    kernels = {k: x for k, x in prof.items() if not k.startswith("copy_")}
+    launches = int(sum(x[0] for x in kernels.values())) * args.steps
+    # end to end: host images
+    host = [np.zeros(tuple(t.shape), np.float32) for t in imgs]
+    t0 = time.perf_counter()
+    ctx.tilt_series_batch(s, cases, defoci, graph=True, images=host)
+    ms_e2e = 1000.0 * (time.perf_counter() - t0)
+    same = all(np.array_equal(h, d.cpu().numpy()) for h, d in zip(host, imgs))
+    dom = max(kernels, key=lambda k: kernels[k][1])
+    n_l, t_ms, nbytes = kernels[dom]
+    peak, peak_kind = peaks()
+    achieved = (nbytes / n_l) / (t_ms / n_l / 1000.0) / 1e9
+    if rank != 0:
+        return
+    err = None
+    if not args.no_fp64_check:
+        # FP64 oracle on the smallest-grid specimen's first orientation
+        try:
+            from oracle import oracle as orc
+            i = min(range(len(cases)), key=lambda j: (cases[j][1], cases[j][0].natom))
+            sp_, n, aZ, aY = cases[i]
+            O = orc.Oracle()
+            p = orc.SeriesParams()
+            p.ax, p.ctblengthz, p.nx, p.ny, p.v0, p.deltaz = sp_.fov, sp_.fov, n, n, V0, DZ
+            p.max_slices, p.min_slice = -1, 0
+            ref, _ = O.orientation(p, sp_.Znum, sp_.x, sp_.y, sp_.z, sp_.occ, aZ[0], aY[0],
+                                   defoci, fp64=True)
+            got = imgs[i][0].cpu().numpy()
+            err = {"specimen": i, "grid": n, "natom": sp_.natom,
+                   "image_rel_l2": [float(np.linalg.norm(got[d] - ref[d]) / np.linalg.norm(ref[d]))
+                                    for d in range(len(defoci))]}
+        except Exception as ex:
+            err = {"error": repr(ex)}
+    out = {
+        "metric": UNEVEN_METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "uneven batch: 64 specimens (seed 1004), natom log-uniform "
+                               "5e3..2e5 at 0.1 atoms/A^3, FOV sqrt(2) x edge, grids "
+                               "{256,512,1024,2048}^2, 1..90 orientations over 180 deg, 300 keV, "
+                               "1 A slices, defoci 0 and 500 A",
+                   "slice_steps_per_step": total, "images_per_step": 2 * sum(len(c[2]) for c in cases),
+                   "l2": "inputs larger than L2 (tens of GB of waves)"},
+        "per_size": per_size,
+        "streams_without_graph": {"ms": ms_streams, "value": total / (ms_streams / 1000.0)},
+        "e2e": {"value": total / (ms_e2e / 1000.0), "unit": UNIT, "h2d_bytes_per_step":
+                int(prof.get("copy_h2d", (0, 0, 0))[2]),
+                "d2h_bytes_per_step": int(sum(h.nbytes for h in host)), "ms_per_step": ms_e2e,
+                "matches_device_output": bool(same)},
+        "gpu_launches": launches,
+        "ms_per_step_serialized": ms_serial,
+        "kernels": {k: {"launches": x[0], "ms": round(x[1], 3),
+                        "GBps": round(x[2] / (x[1] / 1000.0) / 1e9, 1) if x[1] > 0 else None}
+                    for k, x in kernels.items()},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                     "traffic": None, "algorithmic_bytes_per_launch": nbytes / n_l},
+        "clocks": clk,
+        "err_vs_fp64": err,
+    }
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -388,7 +516,7 @@ def main():
     ap.add_argument("--no-per-angle", action="store_true")
     ap.add_argument("--orientations", type=int, default=NANG,
                     help="orientations per step (180 for the headline workload)")
-    ap.add_argument("--workload", default="tilt", choices=["tilt", "adjoint"],
+    ap.add_argument("--workload", default="tilt", choices=["tilt", "adjoint", "uneven"],
                     help="tilt: the 180-orientation 1024^2 tilt series (headline); adjoint: "
                          "the 512^2 potential-stack adjoint over 90 orientations")
     ap.add_argument("--fd-voxels", type=int, default=32,
@@ -402,6 +530,14 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
 
+    if args.workload == "uneven":
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "metric": UNEVEN_METRIC,
+                                  "unavailable": "timed for the tilt-series workload only"}))
+            return
+        run_uneven(args, rank, world, local_rank)
+        return
     if args.workload == "adjoint":
         if args.impl == "reference":
             if rank == 0:
