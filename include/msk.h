@@ -151,7 +151,7 @@ int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int nspec,
  * cannot take cudaMalloc's latency and implicit synchronisation).  Same
  * arguments and result as msk_calculate, minus the context, plus the CUDA
  * stream to run on (NULL: the legacy default stream); host pointers; blocks
- * until pix is written.  Its device scratch is a fixed 8.04 MiB array in this
+ * until pix is written.  Its device scratch is a fixed 8.07 MiB array in this
  * library, held by every GPU that loads it until the process exits.
  * Limits: nx*ny <= 512*512, natom <= 65536, <= 4096 slices; beyond them it
  * returns MSK_ETOOLARGE.  The first call on a device looks up the array's

@@ -344,6 +344,7 @@ struct GridPre {
     const float *d_kx = nullptr, *d_ky = nullptr;  // device kx, ky (free-space step)
     std::vector<float> kx, kx2, ky, ky2;
     std::vector<float2> propx, propy;
+    int band_p = 0, band_q = 0;  // in-band columns: iy <= band_p or iy >= band_q
 };
 
 static bool grid_pre(GridPre &gp, int nx, int ny, float ax, float by, float v0, float deltaz,
@@ -405,6 +406,20 @@ static bool grid_pre(GridPre &gp, int nx, int ny, float ax, float by, float v0, 
         }
         gp.kband[iy] = make_int2(A, B);
     }
+    // whole columns outside the band (ky2 >= k2max): iy in (band_p, band_q)
+    {
+        int p = -1, q = ny;
+        while (p + 1 < ny && gp.kband[p + 1].x >= 0) p++;
+        while (q - 1 > p && gp.kband[q - 1].x >= 0) q--;
+        for (int iy = p + 1; iy < q; iy++)
+            if (gp.kband[iy].x >= 0) {  // in-band columns not of that shape: no skipping
+                p = ny - 1;
+                q = ny;
+                break;
+            }
+        gp.band_p = p;
+        gp.band_q = q;
+    }
     // trlayer constants (autoslic.cpp:927-941)
     gp.sigma = phys::sigma(v0) / 1000.0;
     gp.scalex = ax / nx;  // float division, as the reference
@@ -428,6 +443,15 @@ static bool grid_pre(GridPre &gp, int nx, int ny, float ax, float by, float v0, 
     const double dlnr = log(5.0 / 0.01) / (phys::kN - 1);
     g.lut_c0 = (float)(-2.0 * log(0.01));
     g.lut_c1 = (float)(1.0 / (2.0 * dlnr));
+    // column blocks of the column passes (C columns each) holding in-band columns
+    g.band_p = gp.band_p;
+    g.band_q = gp.band_q;
+    const int C = size_ops(nx)->col_c, nblk = ny / C;
+    g.cb_lo = std::min(nblk, (gp.band_p + 1 + C - 1) / C);
+    g.cb_hi0 = std::max(g.cb_lo, gp.band_q / C);
+    g.cb_n = g.cb_lo + (nblk - g.cb_hi0);
+    g.seg_e1 = std::min(ny, (gp.band_p + 2) & ~1);
+    g.seg_s2 = std::max(g.seg_e1, gp.band_q & ~1);
     return true;
 }
 
@@ -720,11 +744,20 @@ int column_map(msk_context *ctx, CUtensorMap *map, void *base, int nx, int ny, s
 
 // Device error flags: cleared at the start of a call, read after its last
 // synchronisation (a bounded wait in a kernel that gave up sets a bit).
+// The same buffer holds, after 256 bytes, kZeroBytes of zeros: the source
+// the row passes fill out-of-band row segments from.
+constexpr size_t kZeroBytes = 4096 * sizeof(float2);
+constexpr size_t kFlagBytes = 256 + kZeroBytes;
+
 int flags_reset(msk_context *ctx, Geom &g)
 {
-    MSK_CUDA(ctx, ctx->flags.reserve(256));
+    if (ctx->flags.cap < kFlagBytes) {
+        MSK_CUDA(ctx, ctx->flags.reserve(kFlagBytes));
+        MSK_CUDA(ctx, cudaMemsetAsync(ctx->flags.p, 0, kFlagBytes, ctx->stream));
+    }
     MSK_CUDA(ctx, cudaMemsetAsync(ctx->flags.p, 0, sizeof(int), ctx->stream));
     g.err = ctx->flags.as<int>();
+    g.zeros = reinterpret_cast<const float2 *>(ctx->flags.as<unsigned char>() + 256);
     return MSK_OK;
 }
 
@@ -978,7 +1011,7 @@ int upload_batch(msk_context *ctx, const std::vector<UnitAtoms> &ua, int u0, int
 // order P3 after its P2 and the reuse of a transmission buffer after the P3
 // that read it.  With per-kernel profiling on, everything runs in order on
 // one stream so that each launch is timed alone.
-int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode)
+int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode, bool w_in_band)
 {
     const SizeOps *rop = size_ops(gp.ny), *cop = size_ops(gp.nx);
     const Geom &g = gp.g;
@@ -1016,7 +1049,7 @@ int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode)
             }
             {
                 Prof p(ctx, kKColMask, 16.0 * plane * na, sA);
-                cop->col_mask(g, tmaps[k], tmaps[k], units, na, sA);
+                cop->col_mask(g, tmaps[k], tmaps[k], units, na, 1, sA);
             }
             if (overlap) {
                 MSK_CUDA(ctx, cudaEventRecord(ctx->ev_t[k], sA));
@@ -1025,7 +1058,7 @@ int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode)
             {
                 Prof p(ctx, kTransmit, 24.0 * plane * na, sB);
                 rop->row_transmit(g, units, na, tb, psi, psi, 1.0f / ((float)gp.ny * (float)gp.ny),
-                                  sB);
+                                  nmode == 0 && w_in_band, sB);
             }
             if (overlap) {
                 MSK_CUDA(ctx, cudaEventRecord(ctx->ev_free[k], sB));
@@ -1034,7 +1067,11 @@ int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode)
         }
         if (nmode == 0) {
             Prof p(ctx, kKColProp, 16.0 * plane * b.nunits, sB);
-            cop->col_prop(g, pmap, pmap, nullptr, b.nunits, sB);
+            // band mode once every wave is zero out of band: from the start for
+            // a plane wave, else after one full pass (the transmit leaves zeros
+            // there, but units without atoms in a slice keep their wave)
+            cop->col_prop(g, pmap, pmap, nullptr, b.nunits, w_in_band ? 1 : 0, sB);
+            w_in_band = true;
         }
     }
     if (overlap) {
@@ -1287,6 +1324,9 @@ int msk_calculate(msk_context *ctx, float *pix, const float *wave0, const float 
     MSK_CUDA(ctx, ctx->psi.reserve(plane * sizeof(float2)));
     MSK_CUDA(ctx, ctx->tbuf.reserve(plane * sizeof(float2)));
     MSK_CUDA(ctx, ctx->tbuf2.reserve(plane * sizeof(float2)));
+    // the splat stores in-band row segments only: the rest must read as zeros
+    MSK_CUDA(ctx, cudaMemsetAsync(ctx->tbuf.p, 0, plane * sizeof(float2), ctx->stream));
+    MSK_CUDA(ctx, cudaMemsetAsync(ctx->tbuf2.p, 0, plane * sizeof(float2), ctx->stream));
     ctx->units_alloc = 1;
     MSK_CUDA(ctx, ctx->wave0.reserve(plane * sizeof(float2)));
     st = flags_reset(ctx, gp.g);
@@ -1300,7 +1340,7 @@ int msk_calculate(msk_context *ctx, float *pix, const float *wave0, const float 
         rop->row_init(gp.g, nullptr, 1, ctx->wave0.as<float2>(), ctx->psi.as<float2>(), 1.0f,
                       ctx->stream);
     }
-    st = run_slices(ctx, gp, b, nmode);
+    st = run_slices(ctx, gp, b, nmode, false);  // any incident wave
     if (st) return st;
     {
         Prof p(ctx, kExit, 16.0 * plane);
@@ -1366,6 +1406,9 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
     MSK_CUDA(ctx, ctx->psi.reserve((size_t)B * plane * sizeof(float2)));
     MSK_CUDA(ctx, ctx->tbuf.reserve((size_t)B * plane * sizeof(float2)));
     MSK_CUDA(ctx, ctx->tbuf2.reserve((size_t)B * plane * sizeof(float2)));
+    // the splat stores in-band row segments only: the rest must read as zeros
+    MSK_CUDA(ctx, cudaMemsetAsync(ctx->tbuf.p, 0, (size_t)B * plane * sizeof(float2), ctx->stream));
+    MSK_CUDA(ctx, cudaMemsetAsync(ctx->tbuf2.p, 0, (size_t)B * plane * sizeof(float2), ctx->stream));
     ctx->units_alloc = B;
     st = flags_reset(ctx, gp.g);
     if (st) return st;
@@ -1404,7 +1447,7 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
             Prof p(ctx, kPlane, 8.0 * plane * nb);
             k_plane_init<<<1024, 256, 0, ctx->stream>>>(psi, nullptr, nb, nx, ny);
         }
-        st = run_slices(ctx, gp, b, s->nmode);
+        st = run_slices(ctx, gp, b, s->nmode, true);  // plane wave: in band
         if (st) return st;
         if (exitwaves) {
             {
@@ -1650,18 +1693,21 @@ int stack_run(msk_context *ctx, const StackJob &J)
                 rop->row_expv(g, nb, vslice(k), ustride, dst, ctx->stream);
             }
             Prof p(ctx, kKColMask, 16.0 * P * nb);
-            cop->col_mask(g, map_of(dst), map_of(dst), nullptr, nb, ctx->stream);
+            cop->col_mask(g, map_of(dst), map_of(dst), nullptr, nb, 1, ctx->stream);
         };
         // P3 + P4 of one slice: out = W(K[p](iS(in) t))
         auto step = [&](const float2 *tb, const float2 *in, float2 *out) {
             {
                 Prof p(ctx, kTransmit, 24.0 * P * nb);
-                rop->row_transmit(g, nullptr, nb, tb, in, out, tscale, ctx->stream);
+                rop->row_transmit(g, nullptr, nb, tb, in, out, tscale, 1, ctx->stream);
             }
             Prof p(ctx, kKColProp, 16.0 * P * nb);
-            cop->col_prop(g, map_of(out), map_of(out), nullptr, nb, ctx->stream);
+            cop->col_prop(g, map_of(out), map_of(out), nullptr, nb, 1, ctx->stream);  // W0 in band
         };
 
+        // the band-mode transmit stores only in-band row segments: every wave
+        // buffer starts as zeros
+        MSK_CUDA(ctx, cudaMemsetAsync(base, 0, (size_t)planes * B * pb, ctx->stream));
         // forward: W_0 = S(1); checkpoints W_{bK} kept for the backward pass
         float2 *w0 = adjoint ? ck[0] : W;
         {
@@ -1759,7 +1805,7 @@ int stack_run(msk_context *ctx, const StackJob &J)
                     const int k = k0 + j;
                     {
                         Prof p(ctx, kKColProp, 16.0 * P * nb);  // g_u = K[conj p] g_psi
-                        cop->col_prop(gc, map_of(G), map_of(G), nullptr, nb, ctx->stream);
+                        cop->col_prop(gc, map_of(G), map_of(G), nullptr, nb, 0, ctx->stream);
                     }
                     {
                         Prof p(ctx, kAdjTransmit, 40.0 * P * nb);
@@ -1768,7 +1814,7 @@ int stack_run(msk_context *ctx, const StackJob &J)
                     }
                     {
                         Prof p(ctx, kKColMask, 16.0 * P * nb);  // g_e = K[M] g_t
-                        cop->col_mask(g, map_of(Bb[j - 1]), map_of(Bb[j - 1]), nullptr, nb,
+                        cop->col_mask(g, map_of(Bb[j - 1]), map_of(Bb[j - 1]), nullptr, nb, 0,
                                       ctx->stream);
                     }
                     Prof p(ctx, kGrad, 16.0 * P * nb);
@@ -1987,14 +2033,15 @@ int enqueue_specimen(msk_context *ctx, SpecPlan &P, unsigned char *arena, const 
             }
             {
                 Prof p(ctx, kKColMask, 16.0 * pl * nact, st);
-                cop->col_mask(g, tmap, tmap, units, nact, st);
+                cop->col_mask(g, tmap, tmap, units, nact, 1, st);
             }
             Prof p(ctx, kTransmit, 24.0 * pl * nact, st);
-            rop->row_transmit(g, units, nact, tb, psi, psi, 1.0f / ((float)ny * (float)ny), st);
+            rop->row_transmit(g, units, nact, tb, psi, psi, 1.0f / ((float)ny * (float)ny),
+                              s->nmode == 0, st);
         }
         if (s->nmode == 0) {
             Prof p(ctx, kKColProp, 16.0 * pl * na, st);
-            cop->col_prop(g, pmap, pmap, nullptr, na, st);
+            cop->col_prop(g, pmap, pmap, nullptr, na, 1, st);  // plane-wave start: in band
         }
     }
     const double pi = 4.0 * atan(1.0), l = gp.wavlen;
@@ -2171,8 +2218,16 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
         Geom gflag{};
         st = flags_reset(ctx, gflag);
         if (st) return st;
+        for (int i = first; i < last; i++) {
+            P[i].gp.g.err = gflag.err;
+            P[i].gp.g.zeros = gflag.zeros;
+            // the splat stores in-band row segments only: the rest reads as zeros
+            MSK_CUDA(ctx, cudaMemsetAsync(arena + P[i].o_tbuf, 0,
+                                          (size_t)P[i].nangles * P[i].gp.nx * P[i].gp.ny *
+                                              sizeof(float2),
+                                          ctx->stream));
+        }
         MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        for (int i = first; i < last; i++) P[i].gp.g.err = gflag.err;
 
         // longest specimen first onto the least-loaded lane
         std::vector<int> order;
@@ -2280,7 +2335,7 @@ constexpr size_t kSTables = (size_t)1 << 20;                          // 1 MiB
 constexpr size_t kSAtoms = (size_t)kStaticAtoms * sizeof(SplatAtom);  // 1 MiB
 constexpr size_t kSSliceOff = 20 << 10;
 constexpr size_t kSAct = 20 << 10;
-constexpr size_t kSFlags = 256;
+constexpr size_t kSFlags = kFlagBytes;  // error flag + zero source
 constexpr size_t kOffPsi = 0, kOffTbuf = kOffPsi + kSGrid, kOffWave0 = kOffTbuf + kSGrid,
                  kOffTables = kOffWave0 + kSGrid, kOffAtoms = kOffTables + kSTables,
                  kOffSliceOff = kOffAtoms + kSAtoms, kOffAct = kOffSliceOff + kSSliceOff,
@@ -2358,6 +2413,11 @@ extern "C" int msk_calculate_static(void *stream, float *pix, const float *wave0
     view(ctx.slice_off, kOffSliceOff, kSSliceOff);
     view(ctx.act, kOffAct, kSAct);
     view(ctx.flags, kOffFlags, kSFlags);
+    // the zero source and the transmission buffer's out-of-band columns must
+    // read as zeros; the scratch holds whatever the last call left
+    if (cudaMemsetAsync(ctx.flags.p, 0, kSFlags, ctx.stream) != cudaSuccess ||
+        cudaMemsetAsync(ctx.tbuf.p, 0, (size_t)nx * ny * sizeof(float2), ctx.stream) != cudaSuccess)
+        return MSK_ECUDA;
     // ctx.tbuf2 stays empty: the slice loop then runs in order on `stream`
 
     GridPre gp;
@@ -2399,7 +2459,7 @@ extern "C" int msk_calculate_static(void *stream, float *pix, const float *wave0
         return MSK_ECUDA;
     const SizeOps *rop = size_ops(ny);
     rop->row_init(gp.g, nullptr, 1, ctx.wave0.as<float2>(), ctx.psi.as<float2>(), 1.0f, ctx.stream);
-    if ((st = run_slices(&ctx, gp, b, nmode))) return st;
+    if ((st = run_slices(&ctx, gp, b, nmode, false))) return st;
     rop->row_exit(gp.g, nullptr, 1, ctx.psi.as<float2>(), ctx.tbuf.as<float2>(), ctx.stream);
     if (cudaGetLastError() != cudaSuccess) return MSK_ECUDA;
     if (cudaMemcpyAsync(pix, ctx.tbuf.p, plane * sizeof(float2), cudaMemcpyDeviceToHost,

@@ -20,14 +20,19 @@ struct SizeOps {
     void (*splat_potential)(const Geom &, const int *units, int nunits, int slice, int nsl1,
                             const int *slice_off, const SplatAtom *atoms, float *vout,
                             size_t vstride, cudaStream_t);
+    // band != 0: only the in-band column blocks (Geom::cb_*); the others must
+    // be zero in the input and stay zero in the output buffer
     void (*col_mask)(const Geom &, const CUtensorMap &in, const CUtensorMap &out,
-                     const int *units, int nunits, cudaStream_t);
+                     const int *units, int nunits, int band, cudaStream_t);
     void (*col_prop)(const Geom &, const CUtensorMap &in, const CUtensorMap &out,
-                     const int *units, int nunits, cudaStream_t);
+                     const int *units, int nunits, int band, cudaStream_t);
     void (*col_fresnel)(const Geom &, const CUtensorMap &in, const CUtensorMap &out,
                         const int *units, int nunits, const Fresnel &, float scale, cudaStream_t);
+    // band != 0: only the in-band row segments are loaded and stored (B and
+    // W must be zero out of band, and `out` too; a propagator pass follows)
     void (*row_transmit)(const Geom &, const int *units, int nunits, const float2 *tbuf,
-                         const float2 *psi, float2 *out, float out_scale, cudaStream_t);
+                         const float2 *psi, float2 *out, float out_scale, int band,
+                         cudaStream_t);
     void (*row_init)(const Geom &, const int *units, int nunits, const float2 *wave0,
                      float2 *psi, float scale, cudaStream_t);
     void (*row_exit)(const Geom &, const int *units, int nunits, const float2 *psi,
@@ -100,39 +105,42 @@ struct Launch {
     }
     template <int MODE>
     static void col(const Geom &g, const CUtensorMap &in, const CUtensorMap &out,
-                    const int *units, int nunits, const Fresnel &fr, float scale, cudaStream_t s)
+                    const int *units, int nunits, const Fresnel &fr, float scale, int band,
+                    cudaStream_t s)
     {
         static std::once_flag f;
         set_smem(k_col_pass<N, MODE>, Smem<N>::col, f);
         const int C = ColCfg<N>::C;
-        k_col_pass<N, MODE><<<nunits * (g.ny / C), ColCfg<N>::NT, Smem<N>::col, s>>>(
-            g, in, out, units, fr, scale);
+        const int bpu = band ? g.cb_n : g.ny / C;
+        k_col_pass<N, MODE><<<nunits * bpu, ColCfg<N>::NT, Smem<N>::col, s>>>(
+            g, in, out, units, fr, scale, band);
     }
     static void col_mask(const Geom &g, const CUtensorMap &in, const CUtensorMap &out,
-                         const int *units, int nunits, cudaStream_t s)
+                         const int *units, int nunits, int band, cudaStream_t s)
     {
-        col<kColMask>(g, in, out, units, nunits, Fresnel{}, 1.0f / (float)g.nx, s);
+        col<kColMask>(g, in, out, units, nunits, Fresnel{}, 1.0f / (float)g.nx, band, s);
     }
     static void col_prop(const Geom &g, const CUtensorMap &in, const CUtensorMap &out,
-                         const int *units, int nunits, cudaStream_t s)
+                         const int *units, int nunits, int band, cudaStream_t s)
     {
-        col<kColProp>(g, in, out, units, nunits, Fresnel{}, 1.0f / (float)g.nx, s);
+        col<kColProp>(g, in, out, units, nunits, Fresnel{}, 1.0f / (float)g.nx, band, s);
     }
     static void col_fresnel(const Geom &g, const CUtensorMap &in, const CUtensorMap &out,
                             const int *units, int nunits, const Fresnel &fr, float scale,
                             cudaStream_t s)
     {
         if (!fr.table) return;  // the pass multiplies by fr.table; nothing to run without it
-        col<kColFresnel>(g, in, out, units, nunits, fr, scale, s);
+        col<kColFresnel>(g, in, out, units, nunits, fr, scale, 0, s);
     }
     static void row_transmit(const Geom &g, const int *units, int nunits, const float2 *tbuf,
-                             const float2 *psi, float2 *out, float out_scale, cudaStream_t s)
+                             const float2 *psi, float2 *out, float out_scale, int band,
+                             cudaStream_t s)
     {
         static std::once_flag f;
         set_smem(k_row_transmit<N>, Smem<N>::transmit, f);
         const int L = RowCfg<N>::LT;
         k_row_transmit<N><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::transmit, s>>>(
-            g, units, tbuf, psi, out, out_scale);
+            g, units, tbuf, psi, out, out_scale, band);
     }
     static void row_init(const Geom &g, const int *units, int nunits, const float2 *wave0,
                          float2 *psi, float scale, cudaStream_t s)

@@ -31,6 +31,41 @@ namespace msk {
 // a mod n in [0, n) for a power-of-two n (every grid size here is one)
 __device__ __forceinline__ int pmod(int a, int n) { return a & (n - 1); }
 
+// Column iy lies outside the band: the band limit and the propagator zero it
+// whole, so a row pass whose output only feeds them may store zeros there.
+__device__ __forceinline__ bool out_of_band(const Geom &g, int iy)
+{
+    return iy > g.band_p && iy < g.band_q;
+}
+
+// Store `rows` dense rows of length NY from shared memory as their in-band
+// segments [0, seg_e1) and [seg_s2, NY); the (at most two) out-of-band
+// elements inside the segments are zeroed first.  Called by every thread;
+// ends with the stores committed and shared memory read.
+template <int NY>
+__device__ __forceinline__ void store_band_rows(const Geom &g, float2 *rows_smem, int rows,
+                                                float2 *dst)
+{
+    const int e1 = g.seg_e1, s2 = g.seg_s2;
+    __syncthreads();  // every element written before the fix-up
+    if (threadIdx.x < 2 * rows) {
+        const int r = threadIdx.x >> 1;
+        const int iy = (threadIdx.x & 1) ? s2 : e1 - 1;
+        if (iy >= 0 && iy < NY && out_of_band(g, iy)) rows_smem[r * NY + iy] = make_float2(0.0f, 0.0f);
+    }
+    fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int r = 0; r < rows; r++) {
+            bulk_store(dst + (size_t)r * NY, rows_smem + r * NY, (uint32_t)e1 * 8u);
+            if (s2 < NY)
+                bulk_store(dst + (size_t)r * NY + s2, rows_smem + r * NY + s2, (uint32_t)(NY - s2) * 8u);
+        }
+        bulk_commit();
+        bulk_wait_read();
+    }
+}
+
 // exp(i*ph), kept out of line: 32 inlined sincosf bodies per thread (with
 // their large-argument paths) overflow the instruction cache of the splat
 static __device__ __noinline__ float2 expi(float ph)
@@ -201,29 +236,22 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
 #pragma unroll
             for (int m = 0; m < E; m++) dst[t + m * T] = vacc[t + m * T];
         }
-        return;
-    }
-
-    float2 v[E];
+    } else {
+        float2 v[E];
 #pragma unroll
-    for (int m = 0; m < E; m++) {
-        // most of a slice is empty: exp(i*0) = 1 exactly, as sincosf(0) gives
-        const float ph = vacc[t + m * T] * g.sigma_f;
-        v[m] = make_float2(1.0f, 0.0f);
-        if (__any_sync(0xffffffffu, ph != 0.0f)) v[m] = expi(ph);
-    }
-    fft_line<NY, false, 1, BLK>(v, s_lines + l * P::PADN, 0, t, g.tw_row);
-    // dense rows into shared memory, then one bulk store of the whole tile
-    __syncthreads();
+        for (int m = 0; m < E; m++) {
+            // most of a slice is empty: exp(i*0) = 1 exactly, as sincosf(0) gives
+            const float ph = vacc[t + m * T] * g.sigma_f;
+            v[m] = make_float2(1.0f, 0.0f);
+            if (__any_sync(0xffffffffu, ph != 0.0f)) v[m] = expi(ph);
+        }
+        fft_line<NY, false, 1, BLK>(v, s_lines + l * P::PADN, 0, t, g.tw_row);
+        // dense rows into shared memory, then their in-band segments to the
+        // buffer (its out-of-band columns hold zeros: the band limit zeroes them)
+        __syncthreads();
 #pragma unroll
-    for (int m = 0; m < E; m++) s_lines[l * NY + t + m * T] = v[m];
-    fence_proxy_async();
-    __syncthreads();
-    if (tid == 0) {
-        const int rows = min(L, nx - ix0);
-        bulk_store(tbuf + ((size_t)u * nx + ix0) * NY, s_lines, (uint32_t)rows * NY * 8u);
-        bulk_commit();
-        bulk_wait_read();
+        for (int m = 0; m < E; m++) s_lines[l * NY + t + m * T] = v[m];
+        store_band_rows<NY>(g, s_lines, min(L, nx - ix0), tbuf + ((size_t)u * nx + ix0) * NY);
     }
 }
 
@@ -242,7 +270,7 @@ template <int NX, int MODE>
 __global__ void __launch_bounds__(ColCfg<NX>::NT, ColMinBlocks<NX, MODE>::value)
 k_col_pass(const Geom g, const __grid_constant__ CUtensorMap in_map,
            const __grid_constant__ CUtensorMap out_map, const int *__restrict__ units,
-           const Fresnel fr, float fscale)
+           const Fresnel fr, float fscale, int band)
 {
     using P = FftPlan<NX>;
     using CC = ColCfg<NX>;
@@ -253,9 +281,12 @@ k_col_pass(const Geom g, const __grid_constant__ CUtensorMap in_map,
 
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
     const int ny = g.ny;
-    const int bpu = ny / C;
+    // band mode: only the column blocks that hold in-band columns (the others
+    // are zero on input and output)
+    const int bpu = band ? g.cb_n : ny / C;
     const int u = units ? units[blockIdx.x / bpu] : (int)(blockIdx.x / bpu);
-    const int cb = blockIdx.x % bpu;
+    int cb = blockIdx.x % bpu;
+    if (band && cb >= g.cb_lo) cb = g.cb_hi0 + (cb - g.cb_lo);
     const int iy = cb * C + c;
     // tile = rows u*NX .. u*NX+NX-1, float columns 2*cb*C .. 2*cb*C+2C-1
     if (tid == 0) {
@@ -327,7 +358,7 @@ k_col_pass(const Geom g, const __grid_constant__ CUtensorMap in_map,
 template <int NY>
 __global__ void __launch_bounds__(RowCfg<NY>::LT * FftPlan<NY>::T, 3)
 k_row_transmit(const Geom g, const int *__restrict__ units, const float2 *__restrict__ tbuf,
-               const float2 *psi, float2 *out, float out_scale)
+               const float2 *psi, float2 *out, float out_scale, int band)
 {
     using P = FftPlan<NY>;
     constexpr int T = P::T, E = P::E, L = RowCfg<NY>::LT;
@@ -345,15 +376,35 @@ k_row_transmit(const Geom g, const int *__restrict__ units, const float2 *__rest
     const int rows = min(L, nx - ix0);
     const uint32_t bytes = (uint32_t)rows * NY * 8u;
     const size_t off = ((size_t)u * nx + ix0) * NY;
+    // band: only the row segments [0, e1) and [s2, NY) move (even bounds, so
+    // every copy is 16-byte aligned); the rest is zero in B and W
+    const int e1 = band ? g.seg_e1 : NY, s2 = band ? g.seg_s2 : NY;
     if (tid == 0) {
         mbar_init(bar, 1);
         fence_mbar_init();
     }
     __syncthreads();
     if (tid == 0) {
-        mbar_arrive_expect_tx(bar, 2u * bytes);
-        bulk_load(bufB, tbuf + off, bytes, bar);
-        bulk_load(bufW, psi + off, bytes, bar);
+        if (band) {  // segments from the buffers, the middle from the zero source
+            mbar_arrive_expect_tx(bar, 2u * bytes);
+            for (int r = 0; r < rows; r++) {
+                const size_t ro = off + (size_t)r * NY;
+                bulk_load(bufB + r * NY, tbuf + ro, (uint32_t)e1 * 8u, bar);
+                bulk_load(bufW + r * NY, psi + ro, (uint32_t)e1 * 8u, bar);
+                if (s2 > e1) {
+                    bulk_load(bufB + r * NY + e1, g.zeros, (uint32_t)(s2 - e1) * 8u, bar);
+                    bulk_load(bufW + r * NY + e1, g.zeros, (uint32_t)(s2 - e1) * 8u, bar);
+                }
+                if (s2 < NY) {
+                    bulk_load(bufB + r * NY + s2, tbuf + ro + s2, (uint32_t)(NY - s2) * 8u, bar);
+                    bulk_load(bufW + r * NY + s2, psi + ro + s2, (uint32_t)(NY - s2) * 8u, bar);
+                }
+            }
+        } else {
+            mbar_arrive_expect_tx(bar, 2u * bytes);
+            bulk_load(bufB, tbuf + off, bytes, bar);
+            bulk_load(bufW, psi + off, bytes, bar);
+        }
     }
     if (!cta_wait(bar, 0, g.err)) {
         cta_drain(bar, 0);
@@ -377,6 +428,11 @@ k_row_transmit(const Geom g, const int *__restrict__ units, const float2 *__rest
     __syncthreads();
 #pragma unroll
     for (int m = 0; m < E; m++) bufW[l * NY + t + m * T] = cscale(v[m], out_scale);
+    if (band) {  // in-band segments only: `out` holds zeros out of band, the
+                 // propagator that follows zeroes those columns
+        store_band_rows<NY>(g, bufW, rows, out + off);
+        return;
+    }
     fence_proxy_async();
     __syncthreads();
     if (tid == 0) {
@@ -398,7 +454,7 @@ k_row_simple(const Geom g, const int *__restrict__ units, const float2 *__restri
              float2 *__restrict__ out, float scale)
 {
     using P = FftPlan<NY>;
-    constexpr int T = P::T, E = P::E, L = RowCfg<NY>::L, NT = L * T;
+    constexpr int T = P::T, E = P::E, L = RowCfg<NY>::L;
     constexpr bool BLK = RowCfg<NY>::BLK;
     extern __shared__ __align__(128) unsigned char smem[];
     float2 *s_lines = reinterpret_cast<float2 *>(smem);
@@ -436,7 +492,7 @@ k_row_intensity(const Geom g, const int *__restrict__ img_off, const int *__rest
                 const float2 *__restrict__ ebuf, float *__restrict__ images, float nconf)
 {
     using P = FftPlan<NY>;
-    constexpr int T = P::T, E = P::E, L = RowCfg<NY>::L, NT = L * T;
+    constexpr int T = P::T, E = P::E, L = RowCfg<NY>::L;
     constexpr bool BLK = RowCfg<NY>::BLK;
     extern __shared__ __align__(128) unsigned char smem[];
     float2 *s_lines = reinterpret_cast<float2 *>(smem);
@@ -495,10 +551,11 @@ k_row_expv(const Geom g, const float *__restrict__ v, size_t ustride, float2 *__
         if (__any_sync(0xffffffffu, ph != 0.0f)) w[m] = expi(ph);
     }
     fft_line<NY, false, 1, BLK>(w, s_lines + l * P::PADN, 0, t, g.tw_row);
-    if (row_ok) {
+    if (row_ok) {  // out-of-band columns as zeros: the band limit zeroes them
         float2 *dst = out + ((size_t)u * nx + ix) * NY;
 #pragma unroll
-        for (int m = 0; m < E; m++) dst[t + m * T] = w[m];
+        for (int m = 0; m < E; m++)
+            dst[t + m * T] = out_of_band(g, t + m * T) ? make_float2(0.0f, 0.0f) : w[m];
     }
 }
 

@@ -25,6 +25,16 @@ struct Geom {
     const float2 *propx;  // [nx] (cos t, -sin t), t = pi dz (kx^2 lambda - kx 2 tan(tilt_x))
     const float2 *propy;  // [ny]
     const int2 *kband;    // [ny] (A, B): kx2[ix] + ky2[iy] < k2max  <=>  ix <= A or ix >= B
+    // Columns iy with ky2[iy] >= k2max are zeroed whole by the band limit and
+    // by the propagator: in band <=> iy <= band_p or iy >= band_q.  Column
+    // passes in band mode run only the column blocks [0, cb_lo) and
+    // [cb_hi0, ny/C) (C columns per block); cb_n blocks per unit.
+    int band_p, band_q;
+    int cb_lo, cb_hi0, cb_n;
+    // Row segments [0, seg_e1) and [seg_s2, ny) with even bounds that cover
+    // the in-band columns: what a band-mode row pass loads and stores.
+    int seg_e1, seg_s2;
+    const float2 *zeros;  // >= 4096 zero complex values: the source of zero fills
     const float2 *tw_row;  // twiddles for line length ny
     const float2 *tw_col;  // twiddles for line length nx
     const float *knots;    // [100] spline knots in r^2
