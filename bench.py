@@ -505,6 +505,204 @@ def run_uneven(args, rank, world, local_rank):
     print(json.dumps(out))
 
 
+PLAIN_METRIC = "plain multislice slice-steps/s (256², FP32, one orientation); err vs FP32 reference and FP64"
+PHONON_METRIC = ("frozen-phonon slice-steps/s (1024², FP32, 60 orientations x 32 configurations); "
+                 "err vs FP64")
+
+
+def _event_timer(torch, stream):
+    def timed(fn, k):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / k
+    return timed
+
+
+def _rl2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def run_plain(args, rank, world, local_rank):
+    """C1: the plain specimen (2000 atoms in [7, 57]^3, 64 A box), 256^2, 2 A slices,
+    200 keV, one orientation, defocus 0: one msk_calculate call per step (host atoms,
+    host exit wave) and the same orientation as a one-orientation msk_tilt_series
+    (image left in HBM)."""
+    import torch
+    import utr_public_gb300 as msk
+    from utr_public_gb300 import specimen
+    torch.cuda.set_device(local_rank)
+    msk.load()
+    ctx = msk.Context(local_rank)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    timed = _event_timer(torch, stream)
+    sp_ = specimen.plain_specimen(1001)
+    atoms = (sp_.Znum, sp_.x, sp_.y, sp_.z, sp_.occ)
+    param = msk.make_param(64.0, 64.0, 256, 256, 200.0, 2.0)
+    nsl = msk.slice_count(2.0, 64.0)
+    s = msk.Series()
+    s.nx = s.ny = 256
+    s.ctblength = s.ctblengthz = 64.0
+    s.v0, s.deltaz = 200.0, 2.0
+    img = torch.empty((1, 1, 256, 256), dtype=torch.float32, device="cuda")
+    step = lambda: ctx.tilt_series(s, *atoms, [0.0], [0.0], [0.0], images=img)
+    calc = lambda: ctx.calculate(param, *atoms, 64.0, 64.0)
+    for _ in range(args.warmup):
+        step()
+        calc()
+    clocks = Clocks(gpu_index(local_rank))
+    ms = timed(step, max(args.steps, 20))
+    clk = clocks.stop()
+    t0 = time.perf_counter()
+    k = max(args.steps, 20)
+    for _ in range(k):
+        pix = calc()
+    ms_e2e = 1000.0 * (time.perf_counter() - t0) / k
+    ctx.profile(True)
+    step()
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    kernels = {kk: x for kk, x in prof.items() if not kk.startswith("copy_")}
+    if rank != 0:
+        return
+    err = {}
+    gold = os.path.join(ROOT, "tests", "golden", "ref_exit_c1_256.npz")
+    if os.path.exists(gold):
+        err["exit_wave_rel_l2_vs_reference_fp32"] = _rl2(pix, np.load(gold)["pix"])
+    cpu = None
+    if not args.no_fp64_check or not args.no_cpu_baseline:
+        from oracle import oracle as orc
+        O = orc.Oracle()
+        if not args.no_fp64_check:
+            ref64 = O.calculate(param, *atoms, 64.0, 64.0, fp64=True)
+            err["exit_wave_rel_l2_vs_fp64"] = _rl2(pix, ref64)
+            lam = O.wavelength(200.0)
+            i64 = O.defocus(ref64, 64.0, 64.0, lam, 0.0 - 32.0, fp64=True)
+            err["image_rel_l2_vs_fp64"] = _rl2(img[0, 0].cpu().numpy(), i64)
+        if not args.no_cpu_baseline:
+            t0 = time.perf_counter()
+            n = 0
+            while time.perf_counter() - t0 < 3.0:
+                O.calculate(param, *atoms, 64.0, 64.0)
+                n += 1
+            dt = time.perf_counter() - t0
+            cpu = {"value": n * nsl / dt, "unit": UNIT, "cores": 1, "kind": "port",
+                   "sample": "%d calculate() calls of this workload on one host thread" % n}
+    print(json.dumps({
+        "metric": PLAIN_METRIC, "value": nsl / (ms / 1000.0), "unit": UNIT, "n_gpus": world,
+        "steps": k, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "plain: 2000 atoms in [7,57]^3 A, 64 A box, 256^2, 2 A slices, "
+                               "200 keV, one orientation, defocus 0 (seed 1001)",
+                   "slice_steps_per_step": nsl,
+                   "l2": "a 0.5 MB problem: L2-resident by nature (one exit wave)"},
+        "e2e": {"value": nsl / (ms_e2e / 1000.0), "unit": UNIT,
+                "h2d_bytes_per_step": int(prof.get("copy_h2d", (0, 0, 0))[2]),
+                "d2h_bytes_per_step": 256 * 256 * 8, "ms_per_step": ms_e2e,
+                "call": "msk_calculate, host atoms and exit wave"},
+        "gpu_launches": int(sum(x[0] for x in kernels.values())) * k,
+        "kernels": {kk: {"launches": x[0], "ms": round(x[1], 4)} for kk, x in kernels.items()},
+        "clocks": clk, "cpu_baseline": cpu, "err": err}))
+
+
+def run_phonon(args, rank, world, local_rank):
+    """C3: the plain specimen in its 64 A box at 1024^2, 1 A slices, 200 keV, 60
+    orientations in 3 degree steps, 32 thermal configurations (x, y, z += N(0,
+    0.08^2), seeds (1003, c)), defocus 0, images averaged over configurations: one
+    msk_tilt_series call per step."""
+    import torch
+    import utr_public_gb300 as msk
+    from utr_public_gb300 import specimen
+    torch.cuda.set_device(local_rank)
+    msk.load()
+    ctx = msk.Context(local_rank)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    timed = _event_timer(torch, stream)
+    sp_ = specimen.plain_specimen(1001)
+    atoms = (sp_.Znum, sp_.x, sp_.y, sp_.z, sp_.occ)
+    nconf, nang = 32, 60
+    disp = specimen.phonon_displacements(sp_, nconf, 0.08, 1003)
+    angY = np.deg2rad(3.0 * np.arange(nang))
+    angZ = np.full(nang, 0.1 * rank)
+    s = msk.Series()
+    s.nx = s.ny = 1024
+    s.ctblength = s.ctblengthz = 64.0
+    s.v0, s.deltaz = 200.0, 1.0
+    nsl = msk.slice_count(1.0, 64.0)
+    img = torch.empty((nang, 1, 1024, 1024), dtype=torch.float32, device="cuda")
+    step = lambda: ctx.tilt_series(s, *atoms, angZ, angY, [0.0], nconfig=nconf,
+                                   displacements=disp, images=img)
+    for _ in range(args.warmup):
+        step()
+    clocks = Clocks(gpu_index(local_rank))
+    ms = timed(step, args.steps)
+    clk = clocks.stop()
+    total = nang * nconf * nsl
+    ctx.profile(True)
+    ms_serial = timed(step, 1)
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    kernels = {kk: x for kk, x in prof.items() if not kk.startswith("copy_")}
+    dom = max(kernels, key=lambda kk: kernels[kk][1])
+    n_l, t_ms, nbytes = kernels[dom]
+    peak, peak_kind = peaks()
+    achieved = (nbytes / n_l) / (t_ms / n_l / 1000.0) / 1e9
+    host = np.zeros((nang, 1, 1024, 1024), np.float32)
+    t0 = time.perf_counter()
+    ctx.tilt_series(s, *atoms, angZ, angY, [0.0], nconfig=nconf, displacements=disp, images=host)
+    ms_e2e = 1000.0 * (time.perf_counter() - t0)
+    same = bool(np.array_equal(host, img.cpu().numpy()))
+    if rank != 0:
+        return
+    err = None
+    if not args.no_fp64_check:
+        # FP64 oracle: the average over the first two configurations of one orientation
+        from oracle import oracle as orc
+        O = orc.Oracle()
+        p = orc.SeriesParams()
+        p.ax, p.ctblengthz, p.nx, p.ny, p.v0, p.deltaz = 64.0, 64.0, 1024, 1024, 200.0, 1.0
+        p.max_slices, p.min_slice = -1, 0
+        a = nang // 3
+        ref = sum(O.orientation(p, *atoms, angZ[a], angY[a], [0.0], fp64=True, disp=disp[c])[0][0]
+                  for c in range(2)) / 2.0
+        got, _ = ctx.tilt_series(s, *atoms, angZ[a:a + 1], angY[a:a + 1], [0.0], nconfig=2,
+                                 displacements=disp[:2])
+        err = {"orientation_deg": float(np.rad2deg(angY[a])), "configurations": 2,
+               "image_rel_l2_vs_fp64": _rl2(got[0, 0], ref)}
+    print(json.dumps({
+        "metric": PHONON_METRIC, "value": world * total / (ms / 1000.0), "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "frozen phonon: plain specimen (2000 atoms, 64 A box), 1024^2, "
+                               "1 A slices, 200 keV, 60 orientations (3 deg about y) x 32 "
+                               "configurations (rms 0.08 A, seeds (1003, c)), defocus 0, images "
+                               "averaged over configurations",
+                   "slice_steps_per_step": total * world, "images_per_step": nang,
+                   "l2": "inputs larger than L2 (1920 waves, 46 GB of buffers)"},
+        "e2e": {"value": world * total / (ms_e2e / 1000.0), "unit": UNIT,
+                "h2d_bytes_per_step": int(prof.get("copy_h2d", (0, 0, 0))[2]),
+                "d2h_bytes_per_step": int(host.nbytes), "ms_per_step": ms_e2e,
+                "matches_device_output": same},
+        "gpu_launches": int(sum(x[0] for x in kernels.values())) * args.steps,
+        "ms_per_step_serialized": ms_serial,
+        "kernels": {kk: {"launches": x[0], "ms": round(x[1], 3),
+                         "GBps": round(x[2] / (x[1] / 1000.0) / 1e9, 1) if x[1] > 0 else None}
+                    for kk, x in kernels.items()},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                     "traffic": None, "algorithmic_bytes_per_launch": nbytes / n_l},
+        "clocks": clk, "err_vs_fp64": err}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -516,8 +714,11 @@ def main():
     ap.add_argument("--no-per-angle", action="store_true")
     ap.add_argument("--orientations", type=int, default=NANG,
                     help="orientations per step (180 for the headline workload)")
-    ap.add_argument("--workload", default="tilt", choices=["tilt", "adjoint", "uneven"],
-                    help="tilt: the 180-orientation 1024^2 tilt series (headline); adjoint: "
+    ap.add_argument("--workload", default="tilt",
+                    choices=["tilt", "adjoint", "uneven", "plain", "phonon"],
+                    help="tilt: the 180-orientation 1024^2 tilt series (headline); plain: one "
+                         "256^2 orientation; phonon: 60 orientations x 32 configurations at "
+                         "1024^2; uneven: 64 specimens of uneven size in one graph; adjoint: "
                          "the 512^2 potential-stack adjoint over 90 orientations")
     ap.add_argument("--fd-voxels", type=int, default=32,
                     help="central-difference voxels per checked orientation (adjoint)")
@@ -530,6 +731,15 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
 
+    if args.workload in ("plain", "phonon"):
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference",
+                                  "metric": PLAIN_METRIC if args.workload == "plain" else PHONON_METRIC,
+                                  "unavailable": "the reference arm is timed on the tilt series"}))
+            return
+        (run_plain if args.workload == "plain" else run_phonon)(args, rank, world, local_rank)
+        return
     if args.workload == "uneven":
         if args.impl == "reference":
             if rank == 0:
