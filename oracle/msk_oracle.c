@@ -11,6 +11,7 @@
 #include "msk_oracle.h"
 
 #include <math.h>
+#include <stdint.h>
 #include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
@@ -353,13 +354,12 @@ static void cf_ifft_d(double *a, int nx, int ny)
     }
 }
 
-/* Transmission function of one slice (autoslic.cpp:917-1013). */
-static void trlayer_f32(const float *x, const float *y, const float *occ, const int *Znum,
-                        int natom, float ax, float by, float kev, float *trans, int nx, int ny,
-                        const float *kx2, const float *ky2, float k2max)
+/* The projected potential of one slice accumulated in float into trans[2j]
+ * (autoslic.cpp:943-984, the loop trlayer and trlayerDW share). */
+static void potential_f32(const float *x, const float *y, const float *occ, const int *Znum,
+                          int natom, float ax, float by, float *trans, int nx, int ny)
 {
     const double rmax = 3.0, rmax2 = rmax * rmax;
-    double scale = mo_sigma(kev) / 1000.0;
     double scalex = ax / nx; /* float division, as in the reference */
     double scaley = by / ny;
     double rmin = ax / ((double)nx);
@@ -393,6 +393,13 @@ static void trlayer_f32(const float *x, const float *y, const float *occ, const 
             }
         }
     }
+}
+
+/* t = exp(i scale v), then the 2/3 band limit (autoslic.cpp:986-1009). */
+static void phase_bandlimit_f32(float *trans, double scale, int nx, int ny, const float *kx2,
+                                const float *ky2, float k2max)
+{
+    size_t n = (size_t)nx * ny;
     for (size_t j = 0; j < n; j++) {
         double vz = scale * trans[2 * j];
         trans[2 * j] = (float)cos(vz);
@@ -405,6 +412,52 @@ static void trlayer_f32(const float *x, const float *y, const float *occ, const 
             if (!(k2 < k2max)) trans[2 * ((size_t)iy + (size_t)ix * ny)] = trans[2 * ((size_t)iy + (size_t)ix * ny) + 1] = 0.0F;
         }
     cf_ifft_f(trans, nx, ny);
+}
+
+/* Transmission function of one slice (autoslic.cpp:917-1013). */
+static void trlayer_f32(const float *x, const float *y, const float *occ, const int *Znum,
+                        int natom, float ax, float by, float kev, float *trans, int nx, int ny,
+                        const float *kx2, const float *ky2, float k2max)
+{
+    potential_f32(x, y, occ, Znum, natom, ax, by, trans, nx, ny);
+    phase_bandlimit_f32(trans, mo_sigma(kev) / 1000.0, nx, ny, kx2, ky2, k2max);
+}
+
+/* Debye-Waller factor of one slice (autoslic.cpp:1049-1056): B averaged
+ * over wobble[0 .. natom-1] -- the caller's first natom entries, as the
+ * reference passes its unsorted wobble array with the slice's atom count. */
+static double dw_bdw(const float *wobble, int natom, float temperature)
+{
+    const double twopi = 2.0 * (4.0 * atan(1.0));
+    double scaleTemp2 = temperature / 300.0;
+    double Bdw = 0;
+    for (int i = 0; i < natom; i++) Bdw += wobble[i] * wobble[i] * scaleTemp2;
+    Bdw /= natom;
+    Bdw *= 2.0 * twopi * twopi;
+    return Bdw;
+}
+
+/* trlayerDW (autoslic.cpp:1039-1160): the potential damped by exp(-B k^2/4)
+ * (FFT, multiply, inverse FFT, real part), then as trlayer. */
+static void trlayerDW_f32(const float *x, const float *y, const float *occ, const int *Znum,
+                          int natom, float ax, float by, float kev, float *trans, int nx, int ny,
+                          const float *kx2, const float *ky2, float k2max, const float *wobble,
+                          float temperature)
+{
+    const double mBdw4 = -0.25 * dw_bdw(wobble, natom, temperature);
+    size_t n = (size_t)nx * ny;
+    potential_f32(x, y, occ, Znum, natom, ax, by, trans, nx, ny);
+    for (size_t j = 0; j < n; j++) trans[2 * j + 1] = 0.0f;
+    cf_fft_f(trans, nx, ny);
+    for (int ix = 0; ix < nx; ix++)
+        for (int iy = 0; iy < ny; iy++) {
+            float k2 = ky2[iy] + kx2[ix];
+            float emM = (float)exp(mBdw4 * k2);
+            trans[2 * ((size_t)iy + (size_t)ix * ny)] *= emM;
+            trans[2 * ((size_t)iy + (size_t)ix * ny) + 1] *= emM;
+        }
+    cf_ifft_f(trans, nx, ny);
+    phase_bandlimit_f32(trans, mo_sigma(kev) / 1000.0, nx, ny, kx2, ky2, k2max);
 }
 
 /* Projected potential of one slice summed in double (the accumulation of
@@ -449,14 +502,43 @@ static void potential_f64(const float *x, const float *y, const float *occ, cons
     }
 }
 
+static void phase_bandlimit_f64(double *trans, double scale, int nx, int ny, const float *kx2,
+                                const float *ky2, float k2max);
+
 /* Same slice in double: potential summed in double, double transform. */
 static void trlayer_f64(const float *x, const float *y, const float *occ, const int *Znum,
                         int natom, float ax, float by, float kev, double *trans, int nx, int ny,
                         const float *kx2, const float *ky2, float k2max)
 {
-    double scale = mo_sigma(kev) / 1000.0;
+    potential_f64(x, y, occ, Znum, natom, ax, by, trans, 2, nx, ny);
+    phase_bandlimit_f64(trans, mo_sigma(kev) / 1000.0, nx, ny, kx2, ky2, k2max);
+}
+
+/* trlayerDW in double (same B, the multiplier exp(-B k^2/4) in double). */
+static void trlayerDW_f64(const float *x, const float *y, const float *occ, const int *Znum,
+                          int natom, float ax, float by, float kev, double *trans, int nx,
+                          int ny, const float *kx2, const float *ky2, float k2max,
+                          const float *wobble, float temperature)
+{
+    const double mBdw4 = -0.25 * dw_bdw(wobble, natom, temperature);
     size_t n = (size_t)nx * ny;
     potential_f64(x, y, occ, Znum, natom, ax, by, trans, 2, nx, ny);
+    for (size_t j = 0; j < n; j++) trans[2 * j + 1] = 0.0;
+    cf_fft_d(trans, nx, ny);
+    for (int ix = 0; ix < nx; ix++)
+        for (int iy = 0; iy < ny; iy++) {
+            double emM = exp(mBdw4 * (double)(ky2[iy] + kx2[ix]));
+            trans[2 * ((size_t)iy + (size_t)ix * ny)] *= emM;
+            trans[2 * ((size_t)iy + (size_t)ix * ny) + 1] *= emM;
+        }
+    cf_ifft_d(trans, nx, ny);
+    phase_bandlimit_f64(trans, mo_sigma(kev) / 1000.0, nx, ny, kx2, ky2, k2max);
+}
+
+static void phase_bandlimit_f64(double *trans, double scale, int nx, int ny, const float *kx2,
+                                const float *ky2, float k2max)
+{
+    size_t n = (size_t)nx * ny;
     for (size_t j = 0; j < n; j++) {
         double vz = scale * trans[2 * j];
         trans[2 * j] = cos(vz);
@@ -584,10 +666,26 @@ static int calc_setup_init(calc_setup *s, const float *param, int natom, const i
     return MO_OK;
 }
 
-/* Sorted working copies of the atoms (autoslic.cpp:689-739). */
-static int sorted_copy(int natom, const int *Znum, const float *x, const float *y,
-                       const float *z, const float *occ, float ctblengthz, float **x2,
-                       float **y2, float **z2, float **occ2, int **Z2)
+/* The Gaussian deviate the thermal wobble draws (autoslic.cpp:707-709 calls
+ * gasdev from the XArrayLibrary, which is not part of the reference): this
+ * project's definition, shared with the driver of the reference build --
+ * two steps of the 64-bit LCG (6364136223846793005, 1442695040888963407) on
+ * the seed, Box-Muller from the top 53 bits. */
+double mo_gasdev(long *idum)
+{
+    uint64_t s = (uint64_t)(*idum) * 6364136223846793005ULL + 1442695040888963407ULL;
+    uint64_t s2 = s * 6364136223846793005ULL + 1442695040888963407ULL;
+    *idum = (long)s2;
+    double u1 = ((s >> 11) + 1.0) / 9007199254740993.0;
+    double u2 = (s2 >> 11) / 9007199254740992.0;
+    return sqrt(-2.0 * log(u1)) * cos(8.0 * atan(1.0) * u2);
+}
+
+/* Sorted working copies of the atoms (autoslic.cpp:689-739), with the random
+ * thermal displacement of lwobble == 1, nwobble > 1 (autoslic.cpp:701-713). */
+static int sorted_copy_th(int natom, const int *Znum, const float *x, const float *y,
+                          const float *z, const float *occ, float ctblengthz, float **x2,
+                          float **y2, float **z2, float **occ2, int **Z2, const mo_thermal *th)
 {
     size_t n = natom > 0 ? (size_t)natom : 1;
     *x2 = (float *)malloc(sizeof(float) * n);
@@ -601,10 +699,25 @@ static int sorted_copy(int natom, const int *Znum, const float *x, const float *
         memcpy(*z2, z, sizeof(float) * natom);
         memcpy(*occ2, occ, sizeof(float) * natom);
         memcpy(*Z2, Znum, sizeof(int) * natom);
+        if (th && th->lwobble == 1 && th->nwobble > 1) {
+            const float scale = (float)sqrt(th->temperature / 300.0);
+            for (int i = 0; i < natom; i++) {
+                (*x2)[i] = x[i] + (float)(th->wobble[i] * mo_gasdev(th->iseed) * scale);
+                (*y2)[i] = y[i] + (float)(th->wobble[i] * mo_gasdev(th->iseed) * scale);
+                (*z2)[i] = z[i] + (float)(th->wobble[i] * mo_gasdev(th->iseed) * scale);
+            }
+        }
         mo_sortByZ(*x2, *y2, *z2, *occ2, *Z2, natom);
         if ((*z2)[0] < 0 || (*z2)[natom - 1] > ctblengthz) return MO_EZSORT;
     }
     return MO_OK;
+}
+
+static int sorted_copy(int natom, const int *Znum, const float *x, const float *y,
+                       const float *z, const float *occ, float ctblengthz, float **x2,
+                       float **y2, float **z2, float **occ2, int **Z2)
+{
+    return sorted_copy_th(natom, Znum, x, y, z, occ, ctblengthz, x2, y2, z2, occ2, Z2, NULL);
 }
 
 /* autoslic::calculate coherent branch (autoslic.cpp:209-869, 666-837). */
@@ -617,10 +730,36 @@ int mo_calculate_f32(float *pix, const float *wave0, const float *param, int nat
                                    ctblengthz, nmode, 0, max_slices);
 }
 
+static int calculate_f32(float *pix, const float *wave0, const float *param, int natom,
+                         const int *Znum, const float *x, const float *y, const float *z,
+                         const float *occ, float ctblength, float ctblengthz, int nmode,
+                         int min_slice, int max_slices, const mo_thermal *th);
+
 int mo_calculate_sample_f32(float *pix, const float *wave0, const float *param, int natom,
                             const int *Znum, const float *x, const float *y, const float *z,
                             const float *occ, float ctblength, float ctblengthz, int nmode,
                             int min_slice, int max_slices)
+{
+    return calculate_f32(pix, wave0, param, natom, Znum, x, y, z, occ, ctblength, ctblengthz,
+                         nmode, min_slice, max_slices, NULL);
+}
+
+int mo_calculate_thermal_f32(float *pix, const float *wave0, const float *param, int natom,
+                             const int *Znum, const float *x, const float *y, const float *z,
+                             const float *occ, const float *wobble, float ctblength,
+                             float ctblengthz, int nmode, int lwobble, long *iseed)
+{
+    mo_thermal th = {wobble, lwobble != 0, 0, param[MO_pTEMPER], iseed};
+    th.nwobble = to_int(param[MO_pNWOBBLE]);
+    if (th.nwobble < 1) th.nwobble = 1;
+    return calculate_f32(pix, wave0, param, natom, Znum, x, y, z, occ, ctblength, ctblengthz,
+                         nmode, 0, -1, &th);
+}
+
+static int calculate_f32(float *pix, const float *wave0, const float *param, int natom,
+                         const int *Znum, const float *x, const float *y, const float *z,
+                         const float *occ, float ctblength, float ctblengthz, int nmode,
+                         int min_slice, int max_slices, const mo_thermal *th)
 {
     calc_setup s;
     int st = calc_setup_init(&s, param, natom, Znum, x, y, z, ctblength, ctblengthz);
@@ -643,7 +782,7 @@ int mo_calculate_sample_f32(float *pix, const float *wave0, const float *param, 
     }
     float *x2, *y2, *z2, *occ2;
     int *Z2;
-    st = sorted_copy(natom, Znum, x, y, z, occ, ctblengthz, &x2, &y2, &z2, &occ2, &Z2);
+    st = sorted_copy_th(natom, Znum, x, y, z, occ, ctblengthz, &x2, &y2, &z2, &occ2, &Z2, th);
     float *wave = (float *)malloc(sizeof(float) * 2 * n);
     float *trans = (float *)malloc(sizeof(float) * 2 * n);
     if (st == MO_OK) {
@@ -663,8 +802,13 @@ int mo_calculate_sample_f32(float *pix, const float *wave0, const float *param, 
                 continue;
             }
             if (na > 0) {
-                trlayer_f32(&x2[istart], &y2[istart], &occ2[istart], &Z2[istart], na, s.ax, s.by,
-                            s.v0, trans, nx, ny, s.kx2, s.ky2, s.k2max);
+                if (th && th->lwobble == 1 && th->nwobble == 1)  /* autoslic.cpp:766-774 */
+                    trlayerDW_f32(&x2[istart], &y2[istart], &occ2[istart], &Z2[istart], na, s.ax,
+                                  s.by, s.v0, trans, nx, ny, s.kx2, s.ky2, s.k2max, th->wobble,
+                                  th->temperature);
+                else
+                    trlayer_f32(&x2[istart], &y2[istart], &occ2[istart], &Z2[istart], na, s.ax,
+                                s.by, s.v0, trans, nx, ny, s.kx2, s.ky2, s.k2max);
                 for (size_t j = 0; j < n; j++) { /* cfpix::operator*= (cfpix.cpp:349-372) */
                     float wr = wave[2 * j], wi = wave[2 * j + 1];
                     float tr = trans[2 * j], ti = trans[2 * j + 1];
@@ -699,10 +843,36 @@ int mo_calculate_sample_f32(float *pix, const float *wave0, const float *param, 
     return st;
 }
 
+static int calculate_f64(double *pix, const double *wave0, const float *param, int natom,
+                         const int *Znum, const float *x, const float *y, const float *z,
+                         const float *occ, float ctblength, float ctblengthz, int nmode,
+                         int max_slices, const mo_thermal *th);
+
 int mo_calculate_f64(double *pix, const double *wave0, const float *param, int natom,
                      const int *Znum, const float *x, const float *y, const float *z,
                      const float *occ, float ctblength, float ctblengthz, int nmode,
                      int max_slices)
+{
+    return calculate_f64(pix, wave0, param, natom, Znum, x, y, z, occ, ctblength, ctblengthz,
+                         nmode, max_slices, NULL);
+}
+
+int mo_calculate_thermal_f64(double *pix, const double *wave0, const float *param, int natom,
+                             const int *Znum, const float *x, const float *y, const float *z,
+                             const float *occ, const float *wobble, float ctblength,
+                             float ctblengthz, int nmode, int lwobble, long *iseed)
+{
+    mo_thermal th = {wobble, lwobble != 0, 0, param[MO_pTEMPER], iseed};
+    th.nwobble = to_int(param[MO_pNWOBBLE]);
+    if (th.nwobble < 1) th.nwobble = 1;
+    return calculate_f64(pix, wave0, param, natom, Znum, x, y, z, occ, ctblength, ctblengthz,
+                         nmode, -1, &th);
+}
+
+static int calculate_f64(double *pix, const double *wave0, const float *param, int natom,
+                         const int *Znum, const float *x, const float *y, const float *z,
+                         const float *occ, float ctblength, float ctblengthz, int nmode,
+                         int max_slices, const mo_thermal *th)
 {
     calc_setup s;
     int st = calc_setup_init(&s, param, natom, Znum, x, y, z, ctblength, ctblengthz);
@@ -724,7 +894,7 @@ int mo_calculate_f64(double *pix, const double *wave0, const float *param, int n
     }
     float *x2, *y2, *z2, *occ2;
     int *Z2;
-    st = sorted_copy(natom, Znum, x, y, z, occ, ctblengthz, &x2, &y2, &z2, &occ2, &Z2);
+    st = sorted_copy_th(natom, Znum, x, y, z, occ, ctblengthz, &x2, &y2, &z2, &occ2, &Z2, th);
     double *wave = (double *)malloc(sizeof(double) * 2 * n);
     double *trans = (double *)malloc(sizeof(double) * 2 * n);
     if (st == MO_OK) {
@@ -738,8 +908,13 @@ int mo_calculate_f64(double *pix, const double *wave0, const float *param, int n
                 if (z2[i] < zslice) na++;
                 else break;
             if (na > 0) {
-                trlayer_f64(&x2[istart], &y2[istart], &occ2[istart], &Z2[istart], na, s.ax, s.by,
-                            s.v0, trans, nx, ny, s.kx2, s.ky2, s.k2max);
+                if (th && th->lwobble == 1 && th->nwobble == 1)
+                    trlayerDW_f64(&x2[istart], &y2[istart], &occ2[istart], &Z2[istart], na, s.ax,
+                                  s.by, s.v0, trans, nx, ny, s.kx2, s.ky2, s.k2max, th->wobble,
+                                  th->temperature);
+                else
+                    trlayer_f64(&x2[istart], &y2[istart], &occ2[istart], &Z2[istart], na, s.ax,
+                                s.by, s.v0, trans, nx, ny, s.kx2, s.ky2, s.k2max);
                 for (size_t j = 0; j < n; j++) {
                     double wr = wave[2 * j], wi = wave[2 * j + 1];
                     double tr = trans[2 * j], ti = trans[2 * j + 1];

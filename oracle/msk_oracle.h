@@ -156,6 +156,27 @@ int mo_orientation_potential_f64(const mo_series_params *sp, int natom, const in
                                  const float *x, const float *y, const float *z,
                                  const float *occ, double angleZ, double angleY, double *v);
 
+/* Thermal options of calculate(): lwobble = 1 with nwobble = param[pNWOBBLE] == 1
+ * takes the Debye-Waller branch (trlayerDW, autoslic.cpp:766-774, 1039-1160) with
+ * temperature = param[pTEMPER]; nwobble > 1 displaces every atom by
+ * wobble * gasdev * sqrt(T/300) before the sort (autoslic.cpp:701-713). */
+typedef struct {
+    const float *wobble;
+    int lwobble, nwobble;
+    float temperature;
+    long *iseed;
+} mo_thermal;
+
+double mo_gasdev(long *idum);
+int mo_calculate_thermal_f32(float *pix, const float *wave0, const float *param, int natom,
+                             const int *Znum, const float *x, const float *y, const float *z,
+                             const float *occ, const float *wobble, float ctblength,
+                             float ctblengthz, int nmode, int lwobble, long *iseed);
+int mo_calculate_thermal_f64(double *pix, const double *wave0, const float *param, int natom,
+                             const int *Znum, const float *x, const float *y, const float *z,
+                             const float *occ, const float *wobble, float ctblength,
+                             float ctblengthz, int nmode, int lwobble, long *iseed);
+
 /* ---- multislice from per-slice potential stacks, and its adjoint (FP64) ----
  * Forward model for one orientation given v[k][ix][iy] (V*Angstrom, the
  * quantity trlayer accumulates, autoslic.cpp:950-984), k = 0..nslices-1:

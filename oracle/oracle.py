@@ -23,6 +23,7 @@ REF_TREE = "/root/reference"
 # param[] offsets (slicelib.hpp:142-240)
 pXCTILT, pYCTILT, pDEFOCUS, pENERGY, pOAPERT = 9, 10, 11, 16, 17
 pDELTAZ, pAX, pBY, pNX, pNY = 30, 101, 102, 104, 105
+pNWOBBLE, pTEMPER = 111, 120
 NPARAM = 200
 
 _fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
@@ -176,6 +177,28 @@ class Oracle:
             raise RuntimeError("oracle calculate failed: %d" % st)
         return pix.reshape(nx, ny, 2)
 
+    def calculate_thermal(self, param, Znum, x, y, z, occ, wobble, ctblength, ctblengthz,
+                          nmode=0, lwobble=1, iseed=-1, wave0=None, fp64=False):
+        """calculate() with its thermal branches; returns (pix, advanced iseed)."""
+        nx, ny = int(param[pNX] + 0.1), int(param[pNY] + 0.1)
+        T = np.float64 if fp64 else np.float32
+        if wave0 is None:
+            wave0 = np.zeros((nx, ny, 2), T)
+            wave0[..., 0] = 1
+        wave0 = np.ascontiguousarray(wave0, T).reshape(-1)
+        pix = np.zeros(2 * nx * ny, T)
+        seed = C.c_long(iseed)
+        fn = self.L.mo_calculate_thermal_f64 if fp64 else self.L.mo_calculate_thermal_f32
+        fn.argtypes = [_dp if fp64 else _fp, _dp if fp64 else _fp, _fp, C.c_int, _ip, _fp, _fp,
+                       _fp, _fp, _fp, C.c_float, C.c_float, C.c_int, C.c_int,
+                       C.POINTER(C.c_long)]
+        st = fn(pix, wave0, np.ascontiguousarray(param, np.float32), len(x),
+                *_atoms(Znum, x, y, z, occ), np.ascontiguousarray(wobble, np.float32),
+                ctblength, ctblengthz, nmode, lwobble, C.byref(seed))
+        if st:
+            raise RuntimeError("oracle calculate failed: %d" % st)
+        return pix.reshape(nx, ny, 2), seed.value
+
     def defocus(self, pix, ax, by, wavlen, rprime, k2maxo=0.0, cs3=0.0, cs5=0.0, astig=0.0,
                 astig_angle=0.0, fp64=False):
         nx, ny = pix.shape[0], pix.shape[1]
@@ -294,7 +317,11 @@ class Reference:
         L.ref_freqn.argtypes = [_fp, _fp, _fp, C.c_int, C.c_double]
         self._planned = None
 
-    def calculate(self, param, Znum, x, y, z, occ, ctblength, ctblengthz, nmode=0, wave0=None):
+    def calculate(self, param, Znum, x, y, z, occ, ctblength, ctblengthz, nmode=0, wave0=None,
+                  wobble=None, lwobble=0, iseed=None):
+        """autoslic::calculate; with lwobble = 1 its thermal branches (param[pNWOBBLE],
+        param[pTEMPER]); iseed: the gasdev seed, returned advanced as the second
+        value when given."""
         param = np.array(param, np.float32)
         nx, ny = int(param[pNX] + 0.1), int(param[pNY] + 0.1)
         if wave0 is None:
@@ -303,10 +330,13 @@ class Reference:
         wave0 = np.ascontiguousarray(wave0, np.float32).reshape(-1)
         pix = np.zeros(2 * nx * ny, np.float32)
         Znum, x, y, z, occ = (a.copy() for a in _atoms(Znum, x, y, z, occ))
-        wob = np.zeros(len(x), np.float32)
+        wob = np.zeros(len(x), np.float32) if wobble is None else \
+            np.ascontiguousarray(wobble, np.float32).copy()
+        seed = C.c_long(-1 if iseed is None else iseed)
         self.L.ref_calculate(pix, wave0, param, len(x), Znum, x, y, z, occ, wob, ctblength,
-                             ctblengthz, nmode, 0, None, 1)
-        return pix.reshape(nx, ny, 2)
+                             ctblengthz, nmode, lwobble, C.addressof(seed), 1)
+        pix = pix.reshape(nx, ny, 2)
+        return pix if iseed is None else (pix, seed.value)
 
     def sort_by_z(self, Znum, x, y, z, occ):
         Znum, x, y, z, occ = (a.copy() for a in _atoms(Znum, x, y, z, occ))

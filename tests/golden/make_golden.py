@@ -12,6 +12,7 @@ Fixtures (seeded synthetic specimens, see utr_public_gb300/specimen.py):
   ref_physics.npz   wavelength/sigma, freqn grids, vzatomLUT samples, bessk0
   ref_sort.npz      sortByZ permutation of the 2000-atom specimen
   ref_exit_*.npz    exit waves of autoslic::calculate (coherent branch)
+  ref_thermal_*.npz exit waves of its thermal branches (lwobble = 1)
 """
 import os
 import sys
@@ -32,6 +33,19 @@ CASES = {
     "rect_64x128": (300, 64.0, 64, 128, 300.0, 1.5, 0, 1007),
     "proj_64": (200, 64.0, 64, 64, 200.0, 2.0, 1, 1008),
 }
+
+
+THERMAL = {
+    # name: (natom subset of the 64 A plain specimen, grid, nwobble, temperature K, iseed)
+    "dw_128": (600, 128, 1, 300.0, -1),
+    "wobble_128": (400, 128, 3, 250.0, -12345),
+}
+
+
+def thermal_wobble(natom):
+    """Per-atom rms displacement at 300 K (A): 0.05, 0.075, 0.1 cycling, so that
+    the slice averages of the Debye-Waller branch depend on which entries count."""
+    return (0.05 + 0.025 * (np.arange(natom) % 3)).astype(np.float32)
 
 
 def case_specimen(natom, seed):
@@ -79,6 +93,20 @@ def main():
                             natom=natom, fov=fov, nx=nx, ny=ny, v0=v0, deltaz=dz, nmode=nmode,
                             seed=seed)
         print("wrote", name, pix.shape)
+
+    # thermal branches of calculate (lwobble = 1): Debye-Waller (nwobble 1) and
+    # random displacements (nwobble > 1, the build's gasdev)
+    for name, (natom, nx, nwob, temp, seed0) in THERMAL.items():
+        Z, x, y, z, occ = case_specimen(natom, 1001)
+        wob = thermal_wobble(natom)
+        param = orc.make_param(64.0, 64.0, nx, nx, 200.0, 2.0)
+        param[orc.pNWOBBLE], param[orc.pTEMPER] = nwob, temp
+        pix, seed1 = R.calculate(param, Z, x, y, z, occ, 64.0, 64.0, wobble=wob, lwobble=1,
+                                 iseed=seed0)
+        np.savez_compressed(os.path.join(HERE, "ref_thermal_%s.npz" % name), pix=pix,
+                            natom=natom, nx=nx, nwobble=nwob, temperature=temp, iseed0=seed0,
+                            iseed1=seed1)
+        print("wrote thermal", name, pix.shape)
 
 
 if __name__ == "__main__":

@@ -193,3 +193,26 @@ def test_stack_of_atom_potentials_reproduces_orientation_images(oracle):
         p.nslices, p.aobj, p.cs3 = v.shape[0], 0.02, 1e6
         im = oracle.stack_images(p, v, defoci - 0.5 * 32.0)
         assert rel_l2(im, ref) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["dw_128", "wobble_128"])
+def test_thermal_branches_match_reference_bit_for_bit(oracle, name):
+    """The oracle's thermal calculate() against the reference's own build:
+    Debye-Waller (nwobble 1) and random displacements (nwobble 3)."""
+    from oracle.oracle import make_param, pNWOBBLE, pTEMPER
+    g = golden("ref_thermal_%s.npz" % name)
+    n, nx = int(g["natom"]), int(g["nx"])
+    s = sp.plain_specimen(1001)
+    wob = (0.05 + 0.025 * (np.arange(n) % 3)).astype(np.float32)
+    param = make_param(64.0, 64.0, nx, nx, 200.0, 2.0)
+    param[pNWOBBLE], param[pTEMPER] = float(g["nwobble"]), float(g["temperature"])
+    atoms = (s.Znum[:n], s.x[:n], s.y[:n], s.z[:n], s.occ[:n])
+    pix, seed = oracle.calculate_thermal(param, *atoms, wob, 64.0, 64.0, iseed=int(g["iseed0"]))
+    assert np.array_equal(pix, g["pix"])
+    assert seed == int(g["iseed1"])
+    pix64, _ = oracle.calculate_thermal(param, *atoms, wob, 64.0, 64.0, iseed=int(g["iseed0"]),
+                                        fp64=True)
+    assert rel_l2(g["pix"], pix64) < 1e-5
+    # the thermal branch changes the result
+    plain = oracle.calculate(param, *atoms, 64.0, 64.0)
+    assert rel_l2(plain, pix64) > 1e-4
