@@ -66,12 +66,24 @@ const char *msk_status_string(int status);
  *                made internally, autoslic.cpp:689-724)
  *   ctblength, ctblengthz: the box (autoslic.cpp:288-303)
  *   nmode:  0 multislice; 1, 2 transmission only (autoslic.cpp:783)
- *   lwobble: must be 0 (the thermal branches are not provided: MSK_EUNSUPPORTED)
+ *   lwobble: 1 takes calculate()'s thermal branches (autoslic.cpp:701-713,
+ *            766-774) with nwobble = param[pNWOBBLE], T = param[pTEMPER] and
+ *            wobble[] = rms displacement at 300 K per atom:
+ *              nwobble == 1: Debye-Waller damping exp(-B k^2/4) of every slice's
+ *                potential (trlayerDW, autoslic.cpp:1039-1160), B averaged over
+ *                wobble[0 .. na-1] of the caller's order as the reference does;
+ *              nwobble > 1: every atom displaced by wobble * gasdev(iseed) *
+ *                sqrt(T/300) in x, y, z before the sort; *iseed advances.  gasdev
+ *                is this library's (the reference's lives in the XArrayLibrary,
+ *                which is not part of it): two steps of the 64-bit LCG
+ *                (6364136223846793005, 1442695040888963407), Box-Muller from the
+ *                top 53 bits.
+ *   iseed:   the displacement seed (nwobble > 1 only; may be NULL otherwise)
  * Host pointers.  Blocks until the result is in pix. */
 int msk_calculate(msk_context *ctx, float *pix, const float *wave0, const float *param,
                   int natom, const int *Znum, const float *x, const float *y, const float *z,
                   const float *occ, const float *wobble, float ctblength, float ctblengthz,
-                  int nmode, int lwobble);
+                  int nmode, int lwobble, long *iseed);
 
 /* One tilt series as MsctKirkland produces it (MultisliceT.cpp:398-448 driving
  * autosliccmd.cpp:711-1224 per orientation): for every orientation, rotate
@@ -100,6 +112,18 @@ typedef struct {
     double dxc, dyc, dzc;  /* rotation centre shift from the box centre, Angstrom */
     int nmode;             /* as in msk_calculate */
     int max_batch;         /* waves in flight at once (0: as many as memory allows) */
+    /* thermal branches, as msk_calculate with nconfig in the role of nwobble:
+     * lwobble = 1 and nconfig == 1 damps every slice's potential by the
+     * Debye-Waller factor; lwobble = 1 and nconfig > 1 without displacements
+     * draws them in the engine, orientation i from the seed `seed - i`, its
+     * configurations in order from that sequence */
+    int lwobble;
+    float temperature;     /* K */
+    const float *wobble;   /* rms displacement at 300 K per atom (host; lwobble = 1) */
+    long seed;
+    /* incident wave: 0 a plane wave; else a spherical wave from a point source
+     * R1 Angstrom before the box centre (autosliccmd.cpp:650-689) */
+    double R1;
 } msk_series;
 
 /*   natom atoms: Znum, x, y, z, occ (host)

@@ -92,9 +92,11 @@ def test_error_statuses(ctx, msk):
     with pytest.raises(msk.MskError) as e:
         ctx.calculate(msk.make_param(32.0, 32.0, 100, 64, 200.0, 2.0), *atoms, 32.0, 32.0)
     assert e.value.status == msk.MSK_EUNSUPPORTED
+    p2 = param.copy()
+    p2[msk.pNWOBBLE] = 2  # random displacements need a seed
     with pytest.raises(msk.MskError) as e:
-        ctx.calculate(param, *atoms, 32.0, 32.0, lwobble=1)
-    assert e.value.status == msk.MSK_EUNSUPPORTED
+        ctx.calculate(p2, *atoms, 32.0, 32.0, lwobble=1)
+    assert e.value.status == msk.MSK_EINVAL
     # the context stays usable after every failure
     pix = ctx.calculate(param, *atoms, 32.0, 32.0)
     assert np.isfinite(pix).all()

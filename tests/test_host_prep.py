@@ -43,7 +43,7 @@ def test_null_context_is_rejected(msk):
     L = msk.load()
     z = np.zeros(200, np.float32)
     assert L.msk_calculate(None, None, None, z, 0, None, None, None, None, None, None, 1.0, 1.0,
-                           0, 0) == msk.MSK_EINVAL
+                           0, 0, None) == msk.MSK_EINVAL
 
 
 def test_sort_matches_reference_and_oracle(msk, oracle):

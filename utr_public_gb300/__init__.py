@@ -44,7 +44,8 @@ class Series(C.Structure):
                 ("aobj", C.c_float), ("cs3", C.c_double), ("cs5", C.c_double),
                 ("astig", C.c_double), ("astig_angle", C.c_double), ("dxc", C.c_double),
                 ("dyc", C.c_double), ("dzc", C.c_double), ("nmode", C.c_int),
-                ("max_batch", C.c_int)]
+                ("max_batch", C.c_int), ("lwobble", C.c_int), ("temperature", C.c_float),
+                ("wobble", C.c_void_p), ("seed", C.c_long), ("R1", C.c_double)]
 
 
 class Stack(C.Structure):
@@ -99,7 +100,7 @@ def load():
     L.msk_status_string.argtypes = [C.c_int]
     L.msk_status_string.restype = C.c_char_p
     L.msk_calculate.argtypes = [vp, vp, vp, _fp, C.c_int, vp, vp, vp, vp, vp, vp, C.c_float,
-                                C.c_float, C.c_int, C.c_int]
+                                C.c_float, C.c_int, C.c_int, C.POINTER(C.c_long)]
     L.msk_tilt_series.argtypes = [vp, C.POINTER(Series), C.c_int, vp, vp, vp, vp, vp, C.c_int,
                                   _dp, _dp, C.c_int, vp, C.c_int, vp, vp, vp, vp]
     L.msk_slice_count.argtypes = [C.c_float, C.c_float]
@@ -252,8 +253,10 @@ class Context:
                                        float(buf[i].bytes)) for i in range(min(n, 16))}
 
     def calculate(self, param, Znum, x, y, z, occ, ctblength, ctblengthz, nmode=0, wave0=None,
-                  wobble=None, lwobble=0):
-        """autoslic::calculate coherent branch; returns the exit wave [nx, ny, 2] float32."""
+                  wobble=None, lwobble=0, iseed=None):
+        """autoslic::calculate coherent branch; returns the exit wave [nx, ny, 2] float32.
+        lwobble = 1 takes its thermal branches (param[pNWOBBLE], param[pTEMPER]); with
+        iseed given (nwobble > 1) returns (exit wave, advanced seed)."""
         param = np.ascontiguousarray(param, np.float32)
         nx, ny = int(param[pNX] + 0.1), int(param[pNY] + 0.1)
         if wave0 is None:
@@ -266,11 +269,12 @@ class Context:
                  (occ, np.float32))]
         wob = np.zeros(len(arrs[1]), np.float32) if wobble is None else \
             np.ascontiguousarray(wobble, np.float32)
+        seed = None if iseed is None else C.c_long(iseed)
         st = self.L.msk_calculate(self.h, _ptr(pix), _ptr(wave0), param, len(arrs[1]),
                                   *[_ptr(a) for a in arrs], _ptr(wob), ctblength, ctblengthz,
-                                  nmode, lwobble)
+                                  nmode, lwobble, None if seed is None else C.byref(seed))
         self._check(st)
-        return pix
+        return pix if seed is None else (pix, seed.value)
 
     def tilt_series(self, series, Znum, x, y, z, occ, angleZ, angleY, defocus, nconfig=1,
                     displacements=None, images=None, exitwaves=None, want_exit=False):

@@ -494,9 +494,26 @@ static bool twiddles(int n, std::vector<float2> &out)
 struct UnitAtoms {
     std::vector<SplatAtom> atoms;
     std::vector<int> counts;  // per slice
+    std::vector<float> dw;    // Debye-Waller branch: -B/4 per slice
     int kept = 0;
     int status = MSK_OK;
 };
+
+// This library's gasdev: the reference draws its thermal displacements with
+// gasdev from the XArrayLibrary (autoslic.cpp:707-709), which is not part of
+// the reference.  Two steps of the 64-bit LCG (6364136223846793005,
+// 1442695040888963407) on the seed, Box-Muller from the top 53 bits.
+static double gasdev(long *idum)
+{
+    uint64_t s = (uint64_t)(*idum) * 6364136223846793005ULL + 1442695040888963407ULL;
+    uint64_t s2 = s * 6364136223846793005ULL + 1442695040888963407ULL;
+    *idum = (long)s2;
+    double u1 = ((s >> 11) + 1.0) / 9007199254740993.0;
+    double u2 = (s2 >> 11) / 9007199254740992.0;
+    return sqrt(-2.0 * log(u1)) * cos(8.0 * atan(1.0) * u2);
+}
+
+enum { kThermNone = 0, kThermDW = 1, kThermRandom = 2 };
 
 struct PrepSpec {
     int natom;
@@ -509,6 +526,12 @@ struct PrepSpec {
     const float *disp;  // [3][natom] or null
     bool drop_outside;
     const int *zmap;    // Z -> compact index
+    // thermal branches of calculate (lwobble = 1): kThermDW (nwobble 1) or
+    // kThermRandom (nwobble > 1, displacements drawn from *iseed)
+    int thermal = kThermNone;
+    const float *wobble = nullptr;  // rms displacement at 300 K per atom
+    float temperature = 0.0f;
+    long *iseed = nullptr;
 };
 
 static void prep_unit(const GridPre &gp, const PrepSpec &ps, UnitAtoms &out)
@@ -517,6 +540,8 @@ static void prep_unit(const GridPre &gp, const PrepSpec &ps, UnitAtoms &out)
     std::vector<float> x(ps.x, ps.x + n0), y(ps.y, ps.y + n0), z(ps.z, ps.z + n0),
         occ(ps.occ, ps.occ + n0);
     std::vector<int> Z(ps.Znum, ps.Znum + n0);
+    std::vector<float> wob;
+    if (ps.thermal != kThermNone) wob.assign(ps.wobble, ps.wobble + n0);
     if (ps.rotate)
         rotate(ps.ctblength, ps.dxc, ps.dyc, ps.dzc, ps.angZ, ps.angY, n0, x.data(), y.data(),
                z.data());
@@ -539,6 +564,7 @@ static void prep_unit(const GridPre &gp, const PrepSpec &ps, UnitAtoms &out)
             z[n] = z[k];
             occ[n] = occ[k];
             Z[n] = Z[k];
+            if (!wob.empty()) wob[n] = wob[k];  // autosliccmd.cpp:806-818 keeps wobble along
             n++;
         }
     } else if (n > 0) {
@@ -563,6 +589,14 @@ static void prep_unit(const GridPre &gp, const PrepSpec &ps, UnitAtoms &out)
             out.status = MSK_EZNUM;
             return;
         }
+    if (ps.thermal == kThermRandom) {  // autoslic.cpp:701-713, before the sort
+        const float scale = (float)sqrt(ps.temperature / 300.0);
+        for (int i = 0; i < n; i++) {
+            x[i] = x[i] + (float)(wob[i] * gasdev(ps.iseed) * scale);
+            y[i] = y[i] + (float)(wob[i] * gasdev(ps.iseed) * scale);
+            z[i] = z[i] + (float)(wob[i] * gasdev(ps.iseed) * scale);
+        }
+    }
     sort_by_z(x.data(), y.data(), z.data(), occ.data(), Z.data(), n);
     if (n > 0 && (z[0] < 0 || z[n - 1] > ps.ctblengthz)) {  // autoslic.cpp:734-739
         out.status = MSK_EZSORT;
@@ -572,6 +606,23 @@ static void prep_unit(const GridPre &gp, const PrepSpec &ps, UnitAtoms &out)
     slice_counts(ps.deltaz, ps.ctblengthz, n, z.data(), ps.nslices, out.counts.data());
     int used = 0;
     for (int s = 0; s < ps.nslices; s++) used += out.counts[s];
+    if (ps.thermal == kThermDW) {
+        // trlayerDW's B for a slice of na atoms (autoslic.cpp:1049-1056): the
+        // mean over wobble[0 .. na-1] of the caller's (unsorted) order
+        const double twopi = 2.0 * (4.0 * atan(1.0));
+        const double scaleTemp2 = ps.temperature / 300.0;
+        std::vector<double> pre(n + 1, 0.0);
+        for (int i = 0; i < n; i++) pre[i + 1] = pre[i] + wob[i] * wob[i] * scaleTemp2;
+        out.dw.assign(ps.nslices, 0.0f);
+        for (int s = 0; s < ps.nslices; s++) {
+            const int na = out.counts[s];
+            if (na == 0) continue;
+            double Bdw = pre[na];
+            Bdw /= na;
+            Bdw *= 2.0 * twopi * twopi;
+            out.dw[s] = (float)(-0.25 * Bdw);
+        }
+    }
     out.atoms.resize(used);
     for (int i = 0; i < used; i++) {
         // trlayer's pixel of the atom (autoslic.cpp:952-953) and the offset
@@ -617,6 +668,39 @@ static int host_threads()
 
 }  // namespace msk
 
+// Spherical incident wave of MsctKirkland (autosliccmd.cpp:650-689): a point
+// source R1 before the box centre, defined on the entrance surface (R1in =
+// R1 - ctblength/2): amplitude 1/sqrt(1 + r^2/R1in^2), phase
+// 2 pi/lambda sqrt(r^2 + R1in^2) - the phase at the grid corner, r measured
+// from pixel (nx/2, ny/2); values computed in double, stored as float.
+static void spherical_wave(int nx, int ny, float ctblength, float v0, double R1,
+                           std::vector<float2> &w)
+{
+    const double pi = 4.0 * atan(1.0);
+    const double R1in = R1 - 0.5 * ctblength;
+    const double R12 = R1in * R1in, aR12 = 1.0 / R12;
+    const double tPIdlambda = 2.0 * pi / msk::phys::wavelength(v0);
+    const double xst = ctblength / nx, yst = ctblength / ny;  // float divisions
+    const int nx2 = nx / 2, ny2 = ny / 2;
+    const double phamax =
+        tPIdlambda * sqrt(xst * xst * nx2 * nx2 + yst * yst * ny2 * ny2 + R12);
+    w.resize((size_t)nx * ny);
+    for (int j = 0; j < ny; j++) {
+        double yy = double(j - ny2) * yst;
+        yy *= yy;
+        const double yyR12 = yy + R12;
+        for (int i = 0; i < nx; i++) {
+            double xx = double(i - nx2) * xst;
+            xx *= xx;
+            const float amp = float(1.0 / sqrt(1.0 + (xx + yy) * aR12));
+            xx += yyR12;
+            const float pha = float(tPIdlambda * sqrt(xx) - phamax);
+            w[(size_t)i * ny + j] = make_float2(float(amp * cos((double)pha)),
+                                                float(amp * sin((double)pha)));
+        }
+    }
+}
+
 // ------------------------------------------------------------------ context
 
 using namespace msk;
@@ -650,13 +734,14 @@ struct DevBuf {
 // Kinds of launches for the per-kernel accounting (msk_profile).
 enum Kind {
     kSplat, kKColMask, kTransmit, kKColProp, kFresnel, kIntensity, kExit, kInit, kPlane, kFresTab,
-    kExpv, kAdjTransmit, kGrad, kImGrad, kAccum,
+    kExpv, kAdjTransmit, kGrad, kImGrad, kAccum, kDW, kDWExp,
     kKinds
 };
 static const char *const kKindName[kKinds] = {
     "row_splat", "col_bandlimit", "row_transmit", "col_propagate", "col_fresnel",
     "row_intensity", "row_exit", "row_init", "plane_init", "fresnel_table",
-    "row_expv", "row_adj_transmit", "row_grad", "row_imgrad", "accumulate"};
+    "row_expv", "row_adj_transmit", "row_grad", "row_imgrad", "accumulate", "col_debye_waller",
+    "row_dw_phase"};
 
 struct ProfRec {
     int kind;
@@ -683,6 +768,7 @@ struct msk_context {
     DevBuf pa_v, pa_t, pa_psi, pa_e;  // buffers of the per-orientation comparison form
     DevBuf stk, stk_v, stk_g, stk_t, stk_img, stk_part, adjtab;  // potential stacks, adjoint
     DevBuf arena;                                // specimen batches
+    DevBuf dwbuf;                                // Debye-Waller -B/4 per (unit, slice)
     std::vector<cudaStream_t> lanes;             // concurrent specimens of a batch
     std::vector<cudaEvent_t> lane_ev;            // lane joins (one per lane) + fork
     size_t units_alloc = 0;  // units the psi / tbuf buffers hold
@@ -939,6 +1025,7 @@ struct Batch {
     std::vector<int> slice_off;   // [nunits][nslices+1] absolute atom offsets
     std::vector<int> act_off;     // [nslices+1]
     std::vector<int> act;         // active units per slice
+    std::vector<float> dw;        // Debye-Waller branch: [nunits][nslices] -B/4 (else empty)
 };
 
 // Per-slice atom offsets, active units per slice and the packed atoms of
@@ -976,6 +1063,12 @@ void pack_batch(const std::vector<UnitAtoms> &ua, int u0, int nunits, int nslice
         std::copy(a.begin(), a.end(), atoms.begin() + o);
         o += a.size();
     }
+    b.dw.clear();
+    if (nunits > 0 && !ua[u0].dw.empty()) {
+        b.dw.assign((size_t)nunits * nslices, 0.0f);
+        for (int i = 0; i < nunits; i++)
+            std::copy(ua[u0 + i].dw.begin(), ua[u0 + i].dw.end(), b.dw.begin() + (size_t)i * nslices);
+    }
 }
 
 int upload_batch(msk_context *ctx, const std::vector<UnitAtoms> &ua, int u0, int nunits,
@@ -996,6 +1089,12 @@ int upload_batch(msk_context *ctx, const std::vector<UnitAtoms> &ua, int u0, int
     if (!b.act.empty())
         MSK_CUDA(ctx, cudaMemcpyAsync(ctx->act.p, b.act.data(), b.act.size() * sizeof(int),
                                       cudaMemcpyHostToDevice, ctx->stream));
+    if (!b.dw.empty()) {
+        MSK_CUDA(ctx, ctx->dwbuf.reserve(b.dw.size() * sizeof(float)));
+        MSK_CUDA(ctx, cudaMemcpyAsync(ctx->dwbuf.p, b.dw.data(), b.dw.size() * sizeof(float),
+                                      cudaMemcpyHostToDevice, ctx->stream));
+        count_copy(ctx, 0, (double)(b.dw.size() * sizeof(float)));
+    }
     MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return MSK_OK;
 }
@@ -1015,7 +1114,12 @@ int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode, b
 {
     const SizeOps *rop = size_ops(gp.ny), *cop = size_ops(gp.nx);
     const Geom &g = gp.g;
-    const bool overlap = !ctx->prof_on && ctx->tbuf2.cap >= ctx->tbuf.cap;
+    // Debye-Waller branch: the second transmission buffer holds the potential's
+    // spectrum, so the two slice chains run in order on one stream
+    const bool dw = !b.dw.empty();
+    if (dw && ctx->tbuf2.cap < ctx->tbuf.cap)
+        return fail(ctx, MSK_EUNSUPPORTED, "the Debye-Waller branch needs a second buffer");
+    const bool overlap = !dw && !ctx->prof_on && ctx->tbuf2.cap >= ctx->tbuf.cap;
     cudaStream_t sA = ctx->stream, sB = overlap ? ctx->aux : ctx->stream;
     float2 *psi = ctx->psi.as<float2>();
     float2 *tbs[2] = {ctx->tbuf.as<float2>(), overlap ? ctx->tbuf2.as<float2>() : ctx->tbuf.as<float2>()};
@@ -1028,6 +1132,11 @@ int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode, b
     if (st) return st;
     st = column_map(ctx, &pmap, psi, gp.nx, gp.ny, ctx->units_alloc, cop);
     if (st) return st;
+    CUtensorMap smap;
+    if (dw) {
+        st = column_map(ctx, &smap, ctx->tbuf2.p, gp.nx, gp.ny, ctx->units_alloc, cop);
+        if (st) return st;
+    }
     const double plane = (double)gp.nx * gp.ny;
     if (overlap) {
         MSK_CUDA(ctx, cudaEventRecord(ctx->ev_fork, sA));
@@ -1042,7 +1151,20 @@ int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode, b
             const int k = overlap ? (uses++ & 1) : 0;
             float2 *tb = tbs[k];
             if (overlap && pending_free[k]) MSK_CUDA(ctx, cudaStreamWaitEvent(sA, ctx->ev_free[k], 0));
-            {
+            if (dw) {  // trlayerDW: S(v), damping, then A = S(exp(i sigma v'))
+                float2 *spec = ctx->tbuf2.as<float2>();
+                {
+                    Prof p(ctx, kSplat, 8.0 * plane * na, sA);
+                    rop->splat_spec(g, units, na, sl, nsl1, ctx->slice_off.as<int>(),
+                                    ctx->atoms.as<SplatAtom>(), spec, sA);
+                }
+                {
+                    Prof p(ctx, kDW, 16.0 * plane * na, sA);
+                    cop->col_dw(g, smap, units, na, ctx->dwbuf.as<float>() + sl, b.nslices, sA);
+                }
+                Prof p(ctx, kDWExp, 16.0 * plane * na, sA);
+                rop->row_dwexp(g, units, na, spec, tb, sA);
+            } else {
                 Prof p(ctx, kSplat, 8.0 * plane * na, sA);
                 rop->splat(g, units, na, sl, nsl1, ctx->slice_off.as<int>(),
                            ctx->atoms.as<SplatAtom>(), tb, sA);
@@ -1121,7 +1243,7 @@ void msk_destroy(msk_context *ctx)
                       &ctx->imgmeta, &ctx->wave0, &ctx->images, &ctx->exitw, &ctx->fresnel,
                       &ctx->flags, &ctx->pa_v, &ctx->pa_t, &ctx->pa_psi, &ctx->pa_e, &ctx->stk,
                       &ctx->stk_v, &ctx->stk_g, &ctx->stk_t, &ctx->stk_img, &ctx->stk_part,
-                      &ctx->adjtab, &ctx->arena})
+                      &ctx->adjtab, &ctx->arena, &ctx->dwbuf})
         b->release();
     for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_join, ctx->ev_t[0], ctx->ev_t[1], ctx->ev_free[0],
                           ctx->ev_free[1]})
@@ -1268,15 +1390,21 @@ static int build_zmap(msk_context *ctx, int natom, const int *Znum, std::vector<
 int msk_calculate(msk_context *ctx, float *pix, const float *wave0, const float *param,
                   int natom, const int *Znum, const float *x, const float *y, const float *z,
                   const float *occ, const float *wobble, float ctblength, float ctblengthz,
-                  int nmode, int lwobble)
+                  int nmode, int lwobble, long *iseed)
 {
-    (void)wobble;
     if (!ctx) return MSK_EINVAL;
     ctx->err.clear();
     if (!pix || !wave0 || !param || natom < 0 ||
         (natom > 0 && (!Znum || !x || !y || !z || !occ)))
         return fail(ctx, MSK_EINVAL, "null pointer or negative atom count");
-    if (lwobble) return fail(ctx, MSK_EUNSUPPORTED, "thermal (lwobble) branches are not provided");
+    // thermal branches (autoslic.cpp:250-254, 701-713, 766-774)
+    int nwobble = (int)(param[MSK_pNWOBBLE] + 0.1F);
+    if (nwobble < 1) nwobble = 1;
+    const int thermal = !lwobble ? kThermNone : (nwobble == 1 ? kThermDW : kThermRandom);
+    if (thermal != kThermNone && natom > 0 && !wobble)
+        return fail(ctx, MSK_EINVAL, "lwobble needs the wobble array");
+    if (thermal == kThermRandom && !iseed)
+        return fail(ctx, MSK_EINVAL, "random thermal displacements need iseed");
     const float ax = param[MSK_pAX], by = param[MSK_pBY];
     const int nx = (int)(param[MSK_pNX] + 0.1F), ny = (int)(param[MSK_pNY] + 0.1F);
     if (nx < 1 || ny < 1 || ax < 0.0 || by < 0.0)
@@ -1313,6 +1441,10 @@ int msk_calculate(msk_context *ctx, float *pix, const float *wave0, const float 
     std::vector<UnitAtoms> ua(1);
     PrepSpec ps{natom, Znum, x, y, z, occ, ctblength, ctblengthz, param[MSK_pDELTAZ], nslices,
                 false, 0, 0, 0, 0, 0, nullptr, false, ctx->zmap.data()};
+    ps.thermal = thermal;
+    ps.wobble = wobble;
+    ps.temperature = param[MSK_pTEMPER];
+    ps.iseed = iseed;
     prep_unit(gp, ps, ua[0]);
     if (ua[0].status) return fail(ctx, ua[0].status, msk_status_string(ua[0].status));
     int st = upload_tables(ctx, gp, zlist);
@@ -1365,7 +1497,8 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
     ctx->err.clear();
     if (!s || natom < 0 || nangles < 1 || ndefocus < 0 || nconfig < 1 || !angleZ || !angleY ||
         (ndefocus > 0 && (!defocus || !images)) ||
-        (natom > 0 && (!Znum || !x || !y || !z || !occ)) || (nconfig > 1 && !displacements))
+        (natom > 0 && (!Znum || !x || !y || !z || !occ)) ||
+        (nconfig > 1 && !displacements && !s->lwobble))
         return fail(ctx, MSK_EINVAL, "bad tilt-series arguments");
     const int nx = s->nx, ny = s->ny;
     if (nx < 1 || ny < 1 || s->ctblength < 0.0f) return fail(ctx, MSK_EBADSIZE, "bad size parameters");
@@ -1418,6 +1551,28 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
     st = column_map(ctx, &tmap, ctx->tbuf.p, nx, ny, B, size_ops(nx));
     if (st) return st;
 
+    // thermal branches: Debye-Waller with one configuration, displacements
+    // drawn in the engine with several (when the caller gives none)
+    const int thermal = !s->lwobble ? kThermNone
+                        : nconfig == 1 ? kThermDW
+                        : displacements ? kThermNone : kThermRandom;
+    if (thermal != kThermNone && natom > 0 && !s->wobble)
+        return fail(ctx, MSK_EINVAL, "lwobble needs the wobble array");
+    std::vector<long> seeds;
+    if (thermal == kThermRandom)
+        for (int a = 0; a < nangles; a++) seeds.push_back(s->seed - a);
+    // incident wave: a plane wave, or MsctKirkland's spherical wave
+    const bool spherical = s->R1 != 0.0;
+    if (spherical) {
+        std::vector<float2> w0;
+        spherical_wave(nx, ny, s->ctblength, s->v0, s->R1, w0);
+        MSK_CUDA(ctx, ctx->wave0.reserve(plane * sizeof(float2)));
+        MSK_CUDA(ctx, cudaMemcpyAsync(ctx->wave0.p, w0.data(), plane * sizeof(float2),
+                                      cudaMemcpyHostToDevice, ctx->stream));
+        count_copy(ctx, 0, (double)(plane * sizeof(float2)));
+        MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+
     const float wavlen = gp.wavlen;
     float k2maxo = s->aobj / wavlen;  // autosliccmd.cpp:1042-1043
     k2maxo = k2maxo * k2maxo;
@@ -1428,14 +1583,29 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
     const SizeOps *rop = size_ops(ny), *cop = size_ops(nx);
     for (int u0 = 0; u0 < nunits; u0 += B) {
         const int nb = std::min(B, nunits - u0);
-        parallel_for(nb, host_threads(), [&](int i) {
-            const int u = u0 + i, a = u / nconfig, c = u % nconfig;
+        auto prep = [&](int u) {
+            const int a = u / nconfig, c = u % nconfig;
             PrepSpec ps{natom, Znum, x, y, z, occ, s->ctblength, s->ctblengthz, s->deltaz,
                         nslices, true, angleZ[a], angleY[a], s->dxc, s->dyc, s->dzc,
                         displacements ? displacements + (size_t)c * 3 * natom : nullptr, true,
                         ctx->zmap.data()};
+            ps.thermal = thermal;
+            ps.wobble = s->wobble;
+            ps.temperature = s->temperature;
+            ps.iseed = thermal == kThermRandom ? &seeds[a] : nullptr;
             prep_unit(gp, ps, ua[u]);
-        });
+        };
+        if (thermal == kThermRandom) {
+            // one orientation's configurations in order (they draw from one sequence)
+            const int a0 = u0 / nconfig, a1 = (u0 + nb - 1) / nconfig;
+            parallel_for(a1 - a0 + 1, host_threads(), [&](int k) {
+                const int a = a0 + k;
+                for (int u = std::max(u0, a * nconfig); u < std::min(u0 + nb, (a + 1) * nconfig); u++)
+                    prep(u);
+            });
+        } else {
+            parallel_for(nb, host_threads(), [&](int i) { prep(u0 + i); });
+        }
         for (int i = 0; i < nb; i++)
             if (ua[u0 + i].status)
                 return fail(ctx, ua[u0 + i].status, msk_status_string(ua[u0 + i].status));
@@ -1443,11 +1613,14 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
         st = upload_batch(ctx, ua, u0, nb, nslices, b);
         if (st) return st;
         float2 *psi = ctx->psi.as<float2>(), *tb = ctx->tbuf.as<float2>();
-        {
+        if (spherical) {
+            Prof p(ctx, kInit, 8.0 * plane * (nb + 1));
+            rop->row_init(gp.g, nullptr, nb, ctx->wave0.as<float2>(), psi, 1.0f, ctx->stream);
+        } else {
             Prof p(ctx, kPlane, 8.0 * plane * nb);
             k_plane_init<<<1024, 256, 0, ctx->stream>>>(psi, nullptr, nb, nx, ny);
         }
-        st = run_slices(ctx, gp, b, s->nmode, true);  // plane wave: in band
+        st = run_slices(ctx, gp, b, s->nmode, !spherical);  // a plane wave is in band
         if (st) return st;
         if (exitwaves) {
             {
@@ -2088,6 +2261,8 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
     ctx->err.clear();
     if (!s || nspec < 1 || !spec || ndefocus < 0 || (ndefocus > 0 && !defocus))
         return fail(ctx, MSK_EINVAL, "bad batch arguments");
+    if (s->lwobble || s->R1 != 0.0)
+        return fail(ctx, MSK_EUNSUPPORTED, "batches take plane waves without thermal branches");
     for (int i = 0; i < nspec; i++) {
         const msk_specimen &q = spec[i];
         if (q.natom < 0 || q.nangles < 1 || !q.angleZ || !q.angleY ||
@@ -2603,6 +2778,8 @@ extern "C" int msk_tilt_series_per_angle(msk_context *ctx, const msk_series *s, 
         (ndefocus > 0 && (!defocus || !images)) ||
         (natom > 0 && (!Znum || !x || !y || !z || !occ)) || (nconfig > 1 && !displacements))
         return fail(ctx, MSK_EINVAL, "bad tilt-series arguments");
+    if (s->lwobble || s->R1 != 0.0)
+        return fail(ctx, MSK_EUNSUPPORTED, "the comparison form takes plane waves without thermal branches");
     const int nx = s->nx, ny = s->ny;
     if (!pow2_supported(nx) || !pow2_supported(ny))
         return fail(ctx, MSK_EUNSUPPORTED, "grid must be a power of two from 16 to 4096");

@@ -20,6 +20,14 @@ struct SizeOps {
     void (*splat_potential)(const Geom &, const int *units, int nunits, int slice, int nsl1,
                             const int *slice_off, const SplatAtom *atoms, float *vout,
                             size_t vstride, cudaStream_t);
+    // Debye-Waller branch: S(v) to `spec`, the damping column pass on it
+    // (in place), then A = S(exp(i sigma v')) into `tbuf`
+    void (*splat_spec)(const Geom &, const int *units, int nunits, int slice, int nsl1,
+                       const int *slice_off, const SplatAtom *atoms, float2 *spec, cudaStream_t);
+    void (*col_dw)(const Geom &, const CUtensorMap &spec, const int *units, int nunits,
+                   const float *dw, int dw_stride, cudaStream_t);
+    void (*row_dwexp)(const Geom &, const int *units, int nunits, const float2 *spec,
+                      float2 *tbuf, cudaStream_t);
     // band != 0: only the in-band column blocks (Geom::cb_*); the others must
     // be zero in the input and stay zero in the output buffer
     void (*col_mask)(const Geom &, const CUtensorMap &in, const CUtensorMap &out,
@@ -88,9 +96,9 @@ struct Launch {
                       const int *slice_off, const SplatAtom *atoms, float2 *tbuf, cudaStream_t s)
     {
         static std::once_flag f;
-        set_smem(k_row_splat<N, false>, Smem<N>::splat, f);
+        set_smem(k_row_splat<N, kSplatTrans>, Smem<N>::splat, f);
         const int L = RowCfg<N>::L;
-        k_row_splat<N, false><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::splat, s>>>(
+        k_row_splat<N, kSplatTrans><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::splat, s>>>(
             g, units, slice, nsl1, slice_off, atoms, tbuf, nullptr, 0);
     }
     static void splat_potential(const Geom &g, const int *units, int nunits, int slice, int nsl1,
@@ -98,10 +106,29 @@ struct Launch {
                                 size_t vstride, cudaStream_t s)
     {
         static std::once_flag f;
-        set_smem(k_row_splat<N, true>, Smem<N>::splat, f);
+        set_smem(k_row_splat<N, kSplatPot>, Smem<N>::splat, f);
         const int L = RowCfg<N>::L;
-        k_row_splat<N, true><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::splat, s>>>(
+        k_row_splat<N, kSplatPot><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::splat, s>>>(
             g, units, slice, nsl1, slice_off, atoms, nullptr, vout, vstride);
+    }
+    static void splat_spec(const Geom &g, const int *units, int nunits, int slice, int nsl1,
+                           const int *slice_off, const SplatAtom *atoms, float2 *spec,
+                           cudaStream_t s)
+    {
+        static std::once_flag f;
+        set_smem(k_row_splat<N, kSplatSpec>, Smem<N>::splat, f);
+        const int L = RowCfg<N>::L;
+        k_row_splat<N, kSplatSpec><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::splat, s>>>(
+            g, units, slice, nsl1, slice_off, atoms, spec, nullptr, 0);
+    }
+    static void row_dwexp(const Geom &g, const int *units, int nunits, const float2 *spec,
+                          float2 *tbuf, cudaStream_t s)
+    {
+        static std::once_flag f;
+        set_smem(k_row_dwexp<N>, Smem<N>::row, f);
+        const int L = RowCfg<N>::L;
+        k_row_dwexp<N><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::row, s>>>(g, units, spec,
+                                                                                tbuf);
     }
     template <int MODE>
     static void col(const Geom &g, const CUtensorMap &in, const CUtensorMap &out,
@@ -124,6 +151,14 @@ struct Launch {
                          const int *units, int nunits, int band, cudaStream_t s)
     {
         col<kColProp>(g, in, out, units, nunits, Fresnel{}, 1.0f / (float)g.nx, band, s);
+    }
+    static void col_dw(const Geom &g, const CUtensorMap &spec, const int *units, int nunits,
+                       const float *dw, int dw_stride, cudaStream_t s)
+    {
+        Fresnel fr{};
+        fr.dw = dw;
+        fr.dw_stride = dw_stride;
+        col<kColDW>(g, spec, spec, units, nunits, fr, 1.0f / (float)g.nx, 0, s);
     }
     static void col_fresnel(const Geom &g, const CUtensorMap &in, const CUtensorMap &out,
                             const int *units, int nunits, const Fresnel &fr, float scale,
@@ -210,7 +245,7 @@ struct Launch {
     static const SizeOps *ops()
     {
         static const SizeOps o = {N,        ColCfg<N>::C, ColCfg<N>::BR,    splat,
-                                  splat_potential,
+                                  splat_potential, splat_spec, col_dw, row_dwexp,
                                   col_mask, col_prop,     col_fresnel,      row_transmit,
                                   row_init, row_exit,     row_intensity,    row_expv,
                                   row_adj_transmit,       row_grad,         row_imgrad};

@@ -145,7 +145,13 @@ __device__ __forceinline__ float spline_vz(const Geom &g, const float *knots, co
 // fixed pixel owner, so the sum order per pixel is the atom order and the
 // result is deterministic, with no atomics (autoslic.cpp:950-984 is a racy
 // scatter in the reference).  Then t = exp(i sigma v) and the row FFT.
-template <int NY, bool POT>
+// MODE kSplatTrans: A = S(exp(i sigma v)), in-band row segments to tbuf
+//      kSplatPot:   v itself (float) to vout + u * vstride
+//      kSplatSpec:  S(v) (v as a complex field), whole rows to tbuf (the
+//                   Debye-Waller branch filters it before the phase)
+enum { kSplatTrans = 0, kSplatPot = 1, kSplatSpec = 2 };
+
+template <int NY, int MODE>
 __global__ void __launch_bounds__(RowCfg<NY>::L * FftPlan<NY>::T)
 k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
             const int *__restrict__ slice_off, const SplatAtom *__restrict__ atoms,
@@ -229,12 +235,28 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
         }
         __syncthreads();
     }
-    if constexpr (POT) {
+    if constexpr (MODE == kSplatPot) {
         // the projected potential itself: vout -> slice `slice` of unit 0
         if (row_ok) {
             float *dst = vout + (size_t)u * vstride + (size_t)ix * NY;
 #pragma unroll
             for (int m = 0; m < E; m++) dst[t + m * T] = vacc[t + m * T];
+        }
+    } else if constexpr (MODE == kSplatSpec) {
+        float2 v[E];
+#pragma unroll
+        for (int m = 0; m < E; m++) v[m] = make_float2(vacc[t + m * T], 0.0f);
+        fft_line<NY, false, 1, BLK>(v, s_lines + l * P::PADN, 0, t, g.tw_row);
+        __syncthreads();
+#pragma unroll
+        for (int m = 0; m < E; m++) s_lines[l * NY + t + m * T] = v[m];
+        fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+            bulk_store(tbuf + ((size_t)u * nx + ix0) * NY, s_lines,
+                       (uint32_t)min(L, nx - ix0) * NY * 8u);
+            bulk_commit();
+            bulk_wait_read();
         }
     } else {
         float2 v[E];
@@ -264,7 +286,9 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
 //   MODE 1: Fresnel propagator p_y then p_x with the 2/3 aperture
 //           (slicelib.cpp:811-849)
 //   MODE 2: free-space step exp(-i chi) with the objective aperture
-enum { kColMask = 0, kColProp = 1, kColFresnel = 2 };
+//   MODE 3: Debye-Waller damping (float)exp(-B k^2/4) of a potential's
+//           spectrum (autoslic.cpp:1098-1106), -B/4 per unit in fr.dw
+enum { kColMask = 0, kColProp = 1, kColFresnel = 2, kColDW = 3 };
 
 template <int NX, int MODE>
 __global__ void __launch_bounds__(ColCfg<NX>::NT, ColMinBlocks<NX, MODE>::value)
@@ -330,6 +354,14 @@ k_col_pass(const Geom g, const __grid_constant__ CUtensorMap in_map,
             } else {
                 v[m] = make_float2(0.0f, 0.0f);
             }
+        }
+    } else if constexpr (MODE == kColDW) {
+        const float mb4 = __ldg(&fr.dw[(size_t)u * fr.dw_stride]);
+        const float ky2 = __ldg(&g.ky2[iy]);
+#pragma unroll
+        for (int m = 0; m < E; m++) {
+            const float k2 = __fadd_rn(ky2, __ldg(&g.kx2[t + m * T]));
+            v[m] = cscale(v[m], expf(mb4 * k2) * fscale);
         }
     } else {
         const float2 *tab = fr.table + iy;
@@ -557,6 +589,46 @@ k_row_expv(const Geom g, const float *__restrict__ v, size_t ustride, float2 *__
         for (int m = 0; m < E; m++)
             dst[t + m * T] = out_of_band(g, t + m * T) ? make_float2(0.0f, 0.0f) : w[m];
     }
+}
+
+// Debye-Waller branch, last step (autoslic.cpp:1107-1118): from C = the
+// damped spectrum after the column pass (iF(D F(S v))/nx), the damped
+// potential v' = Re(iS(C))/ny, t = exp(i sigma v'), A = S(t) stored as the
+// in-band row segments of `out` (as the splat stores them).
+template <int NY>
+__global__ void __launch_bounds__(RowCfg<NY>::L * FftPlan<NY>::T)
+k_row_dwexp(const Geom g, const int *__restrict__ units, const float2 *__restrict__ spec,
+            float2 *__restrict__ out)
+{
+    using P = FftPlan<NY>;
+    constexpr int T = P::T, E = P::E, L = RowCfg<NY>::L;
+    constexpr bool BLK = RowCfg<NY>::BLK;
+    extern __shared__ __align__(128) unsigned char smem[];
+    float2 *s_lines = reinterpret_cast<float2 *>(smem);
+    const int tid = threadIdx.x, l = tid / T, t = tid % T;
+    const int nx = g.nx;
+    const int bpu = (nx + L - 1) / L;
+    const int u = units[blockIdx.x / bpu];
+    const int ix0 = (blockIdx.x % bpu) * L;
+    const int ix = ix0 + l;
+    const bool row_ok = ix < nx;
+    const float2 *src = spec + ((size_t)u * nx + (row_ok ? ix : 0)) * NY;
+    float2 w[E];
+#pragma unroll
+    for (int m = 0; m < E; m++) w[m] = src[t + m * T];
+    fft_line<NY, true, 1, BLK>(w, s_lines + l * P::PADN, 0, t, g.tw_row);
+    const float sc = g.sigma_f / (float)NY;
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+        const float ph = w[m].x * sc;
+        w[m] = make_float2(1.0f, 0.0f);
+        if (__any_sync(0xffffffffu, ph != 0.0f)) w[m] = expi(ph);
+    }
+    fft_line<NY, false, 1, BLK>(w, s_lines + l * P::PADN, 0, t, g.tw_row);
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < E; m++) s_lines[l * NY + t + m * T] = w[m];
+    store_band_rows<NY>(g, s_lines, min(L, nx - ix0), out + ((size_t)u * nx + ix0) * NY);
 }
 
 // Adjoint of transmit.  In W-states (W(f) = S(f)): from Gu = W(g_u),

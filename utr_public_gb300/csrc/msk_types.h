@@ -67,6 +67,10 @@ struct Fresnel {
     const float *kx;  // [nx]
     const float *ky;  // [ny]
     const float2 *table;
+    // Debye-Waller column pass (kColDW): -B/4 per (unit, slice) at
+    // dw[u * dw_stride] (the caller offsets dw to the slice)
+    const float *dw;
+    int dw_stride;
 };
 
 }  // namespace msk

@@ -58,7 +58,7 @@ void autoslic::calculate(cfpix &pix, cfpix &wave0, cfpix &depthpix, float param[
                          float ycross, float dfdelt, float ctblength, float ctblengthz,
                          int nfftwinit, int nmode)
 {
-    (void)depthpix; (void)multiMode; (void)iseed; (void)beams; (void)hb; (void)kb;
+    (void)depthpix; (void)multiMode; (void)beams; (void)hb; (void)kb;
     (void)nbeams; (void)ycross; (void)dfdelt; (void)nfftwinit;
     if (lpartl || lbeams || lcross)
         throw std::runtime_error("autoslic (GPU): only the coherent branch is provided");
@@ -69,7 +69,7 @@ void autoslic::calculate(cfpix &pix, cfpix &wave0, cfpix &depthpix, float param[
     // cfpix keeps interleaved complex floats, x-major: &re(0,0) is its data
     const int st = msk_calculate(thread_context(), &pix.re(0, 0), &wave0.re(0, 0), param, natom,
                                  Znum, x, y, z, occ, wobble, ctblength, ctblengthz, nmode,
-                                 lwobble);
+                                 lwobble, iseed);
     if (st != MSK_OK)
         throw std::runtime_error(std::string("autoslic (GPU): ") + msk_last_error(thread_context()));
 }
