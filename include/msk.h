@@ -124,6 +124,16 @@ typedef struct {
     /* incident wave: 0 a plane wave; else a spherical wave from a point source
      * R1 Angstrom before the box centre (autosliccmd.cpp:650-689) */
     double R1;
+    /* image plane (autosliccmd.cpp:1119-1143): rotation[d] (radians; NULL: none)
+     * about the optic axis through the box centre + (dxc, dyc), then a shift by
+     * (xshift, yshift) Angstrom rounded to whole pixels, both applied to the
+     * propagated amplitude of detector plane d before |psi|^2.  The reference
+     * calls the missing XArrayLibrary for them; this library's definitions:
+     * Catmull-Rom bicubic interpolation, out(p) = in(c + R(-theta)(p - c)) with
+     * the atom rotation's R, and values outside the image taken as the mean of
+     * the 5-pixel border (per real and imaginary part). */
+    const double *rotation;
+    double xshift, yshift;
 } msk_series;
 
 /*   natom atoms: Znum, x, y, z, occ (host)

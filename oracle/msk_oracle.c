@@ -1033,6 +1033,110 @@ int mo_defocus_f64(const double *pix, int nx, int ny, float ax, float by, double
     return MO_OK;
 }
 
+/* The image-plane rotation and shift of autosliccmd.cpp:1119-1143 with this
+ * project's definitions of the missing XArrayLibrary calls (NormAverEdge(5),
+ * XArray2DSpln::Rotate, XArray2DMove::Move): fill = the mean of each part over
+ * the 5-pixel border; out(p) = in(c + R(-theta)(p - c)) by Catmull-Rom bicubic
+ * interpolation, grid points outside reading the fill; then out(ix, iy) =
+ * in(ix - sx, iy - sy), fill outside.  amp: complex [nx][ny], in place. */
+static double cr_weight(double t, int k)
+{
+    double t2 = t * t, t3 = t2 * t;
+    switch (k) {
+    case 0: return 0.5 * (-t3 + 2.0 * t2 - t);
+    case 1: return 0.5 * (3.0 * t3 - 5.0 * t2 + 2.0);
+    case 2: return 0.5 * (-3.0 * t3 + 4.0 * t2 + t);
+    default: return 0.5 * (t3 - t2);
+    }
+}
+
+void mo_image_plane_f64(double *amp, int nx, int ny, double xst, double yst, double xc,
+                        double yc, double theta, int sx, int sy)
+{
+    size_t n = (size_t)nx * ny;
+    double fr = 0.0, fi = 0.0;
+    long cnt = 0;
+    for (int ix = 0; ix < nx; ix++)
+        for (int iy = 0; iy < ny; iy++)
+            if (ix < 5 || ix >= nx - 5 || iy < 5 || iy >= ny - 5) {
+                fr += amp[2 * ((size_t)ix * ny + iy)];
+                fi += amp[2 * ((size_t)ix * ny + iy) + 1];
+                cnt++;
+            }
+    if (cnt) {
+        fr /= cnt;
+        fi /= cnt;
+    }
+    double *rot = (double *)malloc(sizeof(double) * 2 * n);
+    const double c = cos(theta), sn = sin(theta);
+    for (int ix = 0; ix < nx; ix++)
+        for (int iy = 0; iy < ny; iy++) {
+            double *o = rot + 2 * ((size_t)ix * ny + iy);
+            if (theta == 0.0) {
+                o[0] = amp[2 * ((size_t)ix * ny + iy)];
+                o[1] = amp[2 * ((size_t)ix * ny + iy) + 1];
+                continue;
+            }
+            double dx = ix * xst - xc, dy = iy * yst - yc;
+            double fx = (xc + c * dx + sn * dy) / xst, fy = (yc - sn * dx + c * dy) / yst;
+            int x0 = (int)floor(fx), y0 = (int)floor(fy);
+            double tx = fx - x0, ty = fy - y0, ar = 0.0, ai = 0.0;
+            for (int a = 0; a < 4; a++)
+                for (int b = 0; b < 4; b++) {
+                    int xx = x0 - 1 + a, yy = y0 - 1 + b;
+                    double w = cr_weight(tx, a) * cr_weight(ty, b);
+                    int in = xx >= 0 && xx < nx && yy >= 0 && yy < ny;
+                    ar += w * (in ? amp[2 * ((size_t)xx * ny + yy)] : fr);
+                    ai += w * (in ? amp[2 * ((size_t)xx * ny + yy) + 1] : fi);
+                }
+            o[0] = ar;
+            o[1] = ai;
+        }
+    for (int ix = 0; ix < nx; ix++)
+        for (int iy = 0; iy < ny; iy++) {
+            int jx = ix - sx, jy = iy - sy;
+            double *o = amp + 2 * ((size_t)ix * ny + iy);
+            if (jx >= 0 && jx < nx && jy >= 0 && jy < ny) {
+                o[0] = rot[2 * ((size_t)jx * ny + jy)];
+                o[1] = rot[2 * ((size_t)jx * ny + jy) + 1];
+            } else {
+                o[0] = fr;
+                o[1] = fi;
+            }
+        }
+    free(rot);
+}
+
+/* mo_defocus_f64's free-space step, returning the complex amplitude. */
+int mo_defocus_amp_f64(const double *pix, int nx, int ny, float ax, float by, double wavlen,
+                       double rprime, float k2maxo, double cs3, double cs5, double *amp)
+{
+    size_t n = (size_t)nx * ny;
+    float *kx = (float *)malloc(sizeof(float) * 3 * nx), *ky = (float *)malloc(sizeof(float) * 3 * ny);
+    mo_freqn(kx, kx + nx, kx + 2 * nx, nx, ax);
+    mo_freqn(ky, ky + ny, ky + 2 * ny, ny, by);
+    memcpy(amp, pix, sizeof(double) * 2 * n);
+    cf_fft_d(amp, nx, ny);
+    for (int ix = 0; ix < nx; ix++)
+        for (int iy = 0; iy < ny; iy++) {
+            double *e = amp + 2 * ((size_t)iy + (size_t)ix * ny);
+            float k2 = kx[nx + ix] + ky[ny + iy];
+            if (k2maxo > 0.0F && !(k2 < k2maxo)) {
+                e[0] = e[1] = 0.0;
+                continue;
+            }
+            double chi = chi_phase(kx[ix], ky[iy], wavlen, rprime, cs3, cs5, 0.0, 0.0);
+            double cc = cos(chi), sn = sin(chi);
+            double re = e[0], im = e[1];
+            e[0] = re * cc + im * sn;
+            e[1] = im * cc - re * sn;
+        }
+    cf_ifft_d(amp, nx, ny);
+    free(kx);
+    free(ky);
+    return MO_OK;
+}
+
 /* --------------------------------------------------- per-orientation worker */
 
 static void fill_param(const mo_series_params *sp, float *param)

@@ -156,6 +156,14 @@ int mo_orientation_potential_f64(const mo_series_params *sp, int natom, const in
                                  const float *x, const float *y, const float *z,
                                  const float *occ, double angleZ, double angleY, double *v);
 
+/* Image plane of a detector (autosliccmd.cpp:1119-1143, this project's
+ * definitions of the missing XArrayLibrary calls): rotation by theta about
+ * (xc, yc), then a whole-pixel shift (sx, sy), in place on amp [nx][ny]. */
+void mo_image_plane_f64(double *amp, int nx, int ny, double xst, double yst, double xc,
+                        double yc, double theta, int sx, int sy);
+int mo_defocus_amp_f64(const double *pix, int nx, int ny, float ax, float by, double wavlen,
+                       double rprime, float k2maxo, double cs3, double cs5, double *amp);
+
 /* Thermal options of calculate(): lwobble = 1 with nwobble = param[pNWOBBLE] == 1
  * takes the Debye-Waller branch (trlayerDW, autoslic.cpp:766-774, 1039-1160) with
  * temperature = param[pTEMPER]; nwobble > 1 displaces every atom by

@@ -199,6 +199,24 @@ class Oracle:
             raise RuntimeError("oracle calculate failed: %d" % st)
         return pix.reshape(nx, ny, 2), seed.value
 
+    def image_plane(self, pix64, ax, wavlen, rprime, theta, xc, yc, sx, sy, k2maxo=0.0,
+                    cs3=0.0, cs5=0.0):
+        """FP64 image of a detector plane with the image-plane rotation and shift."""
+        nx, ny = pix64.shape[0], pix64.shape[1]
+        amp = np.zeros(2 * nx * ny)
+        self.L.mo_defocus_amp_f64.argtypes = [_dp, C.c_int, C.c_int, C.c_float, C.c_float,
+                                              C.c_double, C.c_double, C.c_float, C.c_double,
+                                              C.c_double, _dp]
+        self.L.mo_image_plane_f64.argtypes = [_dp, C.c_int, C.c_int, C.c_double, C.c_double,
+                                              C.c_double, C.c_double, C.c_double, C.c_int,
+                                              C.c_int]
+        self.L.mo_defocus_amp_f64(np.ascontiguousarray(pix64, np.float64).reshape(-1), nx, ny, ax,
+                                  ax, wavlen, rprime, k2maxo, cs3, cs5, amp)
+        st = np.float64(np.float32(ax) / np.float32(nx))
+        self.L.mo_image_plane_f64(amp, nx, ny, st, st, xc, yc, theta, sx, sy)
+        a = amp.reshape(nx, ny, 2)
+        return a[..., 0] ** 2 + a[..., 1] ** 2
+
     def defocus(self, pix, ax, by, wavlen, rprime, k2maxo=0.0, cs3=0.0, cs5=0.0, astig=0.0,
                 astig_angle=0.0, fp64=False):
         nx, ny = pix.shape[0], pix.shape[1]

@@ -118,3 +118,34 @@ def test_spherical_incident_wave(ctx, msk, oracle):
     _, plane, _ = ctx.tilt_series(series(msk, 128, 64.0), spec.Znum, spec.x, spec.y, spec.z,
                                   spec.occ, [0.0], [0.0], [0.0], want_exit=True)
     assert rel_l2(ew[0, 0], plane[0, 0]) > 1e-3
+
+
+def test_image_plane_rotation_and_shift(ctx, msk, oracle):
+    """Rotation about the optic axis and a whole-pixel shift of the propagated
+    amplitude (autosliccmd.cpp:1119-1143, this library's definitions) against
+    the FP64 oracle, per detector plane; planes without them are unchanged."""
+    from oracle.oracle import SeriesParams
+    spec = sp.random_specimen(500, 64.0, 10.0, 54.0, 1024)
+    atoms = (spec.Znum, spec.x, spec.y, spec.z, spec.occ)
+    s = series(msk, 128, 64.0)
+    s.dxc, s.dyc = 1.5, -2.0
+    rot = np.array([0.3, 0.0, -1.1])
+    s.rotation = rot.ctypes.data
+    s.xshift, s.yshift = 1.3, -0.7
+    defoci = np.array([0.0, 150.0, 40.0])
+    angY, angZ = np.deg2rad([25.0]), np.array([0.2])
+    imgs, ew, _ = ctx.tilt_series(s, *atoms, angZ, angY, defoci, want_exit=True)
+    p = SeriesParams()
+    p.ax, p.ctblengthz, p.nx, p.ny, p.v0, p.deltaz = 64.0, 64.0, 128, 128, 200.0, 2.0
+    p.dxc, p.dyc, p.max_slices = 1.5, -2.0, -1
+    _, ew64, _ = oracle.orientation(p, *atoms, angZ[0], angY[0], defoci, fp64=True,
+                                    want_exit=True)
+    st = float(np.float32(64.0) / np.float32(128))
+    lam = oracle.wavelength(200.0)
+    sx, sy = int(np.floor(1.3 / st + 0.5)), int(np.floor(-0.7 / st + 0.5))
+    for d in range(3):
+        ref = oracle.image_plane(ew64, 64.0, lam, defoci[d] - 32.0, rot[d], 32.0 + 1.5,
+                                 32.0 - 2.0, sx, sy)
+        assert rel_l2(imgs[0, d], ref) < 1e-5, d
+    plain, _ = ctx.tilt_series(series(msk, 128, 64.0), *atoms, angZ, angY, defoci)
+    assert rel_l2(imgs[0, 1], plain[0, 1]) > 1e-3  # the shift acts on every plane

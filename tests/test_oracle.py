@@ -216,3 +216,31 @@ def test_thermal_branches_match_reference_bit_for_bit(oracle, name):
     # the thermal branch changes the result
     plain = oracle.calculate(param, *atoms, 64.0, 64.0)
     assert rel_l2(plain, pix64) > 1e-4
+
+
+def test_image_plane_rotation_and_shift_definitions(oracle):
+    """The oracle's image-plane operations: a whole-pixel shift moves the field
+    exactly, a quarter turn about a pixel centre permutes pixels, zero does
+    nothing."""
+    import ctypes as C
+    n = 32
+    rng = np.random.default_rng(5)
+    amp = rng.standard_normal((n, n, 2))
+    L = oracle.L
+    L.mo_image_plane_f64.argtypes = [np.ctypeslib.ndpointer(np.float64), C.c_int, C.c_int,
+                                     C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                     C.c_int, C.c_int]
+    a = amp.copy()
+    L.mo_image_plane_f64(a.reshape(-1), n, n, 0.5, 0.5, 8.0, 8.0, 0.0, 0, 0)
+    assert np.array_equal(a, amp)
+    a = amp.copy()
+    L.mo_image_plane_f64(a.reshape(-1), n, n, 0.5, 0.5, 8.0, 8.0, 0.0, 3, -2)
+    assert np.array_equal(a[3:, :n - 2], amp[:n - 3, 2:])
+    edge = np.ones((n, n), bool)
+    edge[5:n - 5, 5:n - 5] = False
+    assert np.allclose(a[0, 0], amp[edge].mean(axis=0))
+    a = amp.copy()
+    L.mo_image_plane_f64(a.reshape(-1), n, n, 0.5, 0.5, 8.0, 8.0, np.pi / 2, 0, 0)
+    # out(ix, iy) = in(c + R(-90)(p - c)): in pixels (cx = cy = 16) -> (16 + (iy-16), 16 - (ix-16))
+    ix, iy = 20, 9
+    assert np.allclose(a[ix, iy], amp[16 + (iy - 16), 16 - (ix - 16)], atol=1e-12)

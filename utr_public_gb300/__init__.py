@@ -45,7 +45,8 @@ class Series(C.Structure):
                 ("astig", C.c_double), ("astig_angle", C.c_double), ("dxc", C.c_double),
                 ("dyc", C.c_double), ("dzc", C.c_double), ("nmode", C.c_int),
                 ("max_batch", C.c_int), ("lwobble", C.c_int), ("temperature", C.c_float),
-                ("wobble", C.c_void_p), ("seed", C.c_long), ("R1", C.c_double)]
+                ("wobble", C.c_void_p), ("seed", C.c_long), ("R1", C.c_double),
+                ("rotation", C.c_void_p), ("xshift", C.c_double), ("yshift", C.c_double)]
 
 
 class Stack(C.Structure):

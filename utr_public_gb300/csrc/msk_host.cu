@@ -86,6 +86,136 @@ __global__ void k_fresnel_table(const Geom g, const Fresnel fr, float scale, flo
     }
 }
 
+// ------------------------------------------------------------------ image plane
+// The rotation about the optic axis and the XY shift MsctKirkland applies to
+// the propagated amplitude of a detector plane (autosliccmd.cpp:1119-1143,
+// XArray2DSpln::Rotate, XArray2DMove::Move and NormAverEdge(5) from the
+// XArrayLibrary, which is not part of the reference).  This library's
+// definitions, per component (real, imaginary):
+//   fill   = the mean over the pixels within 5 of any edge;
+//   rotate = out(p) = in(c + R(-theta)(p - c)), p = (ix*xst, iy*yst), c the
+//            rotation centre, R(t) = [[cos t, -sin t], [sin t, cos t]] (the atom
+//            rotation of autosliccmd.cpp:734-736), Catmull-Rom bicubic
+//            interpolation on the pixel grid, grid points outside the image
+//            reading the fill value;
+//   shift  = out(ix, iy) = in(ix - sx, iy - sy), fill outside, (sx, sy) the shift
+//            rounded to whole pixels.
+
+// Per unit: the edge means of the real and imaginary parts, in double.
+__global__ void k_edge_mean(const float2 *__restrict__ phi, int nx, int ny, int border,
+                            float2 *__restrict__ mean)
+{
+    const int u = blockIdx.x;
+    const float2 *p = phi + (size_t)u * nx * ny;
+    double sr = 0.0, si = 0.0;
+    long long cnt = 0;
+    for (int i = threadIdx.x; i < nx * ny; i += blockDim.x) {
+        const int ix = i / ny, iy = i % ny;
+        if (ix < border || ix >= nx - border || iy < border || iy >= ny - border) {
+            sr += p[i].x;
+            si += p[i].y;
+            cnt++;
+        }
+    }
+    __shared__ double s_r[256], s_i[256];
+    __shared__ long long s_c[256];
+    s_r[threadIdx.x] = sr;
+    s_i[threadIdx.x] = si;
+    s_c[threadIdx.x] = cnt;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+            s_r[threadIdx.x] += s_r[threadIdx.x + w];
+            s_i[threadIdx.x] += s_i[threadIdx.x + w];
+            s_c[threadIdx.x] += s_c[threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        mean[u] = s_c[0] ? make_float2((float)(s_r[0] / s_c[0]), (float)(s_i[0] / s_c[0]))
+                         : make_float2(0.0f, 0.0f);
+}
+
+__device__ __forceinline__ float catmull_rom(float t, int k)
+{
+    // weights of the samples at -1, 0, 1, 2 for a fractional position t
+    const float t2 = t * t, t3 = t2 * t;
+    switch (k) {
+    case 0: return 0.5f * (-t3 + 2.0f * t2 - t);
+    case 1: return 0.5f * (3.0f * t3 - 5.0f * t2 + 2.0f);
+    case 2: return 0.5f * (-3.0f * t3 + 4.0f * t2 + t);
+    default: return 0.5f * (t3 - t2);
+    }
+}
+
+__global__ void k_rotate_shift(const float2 *__restrict__ in, float2 *__restrict__ out,
+                               int nunits, int nx, int ny, double xst, double yst, double xc,
+                               double yc, double cth, double sth, int rotate, int sx, int sy,
+                               const float2 *__restrict__ fill)
+{
+    const size_t plane = (size_t)nx * ny;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < plane * nunits;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const int u = (int)(i / plane), r = (int)(i % plane);
+        const int ix = r / ny - sx, iy = r % ny - sy;
+        const float2 f = fill[u];
+        const float2 *src = in + (size_t)u * plane;
+        float2 v = f;
+        if (ix >= 0 && ix < nx && iy >= 0 && iy < ny) {
+            if (!rotate) {
+                v = src[(size_t)ix * ny + iy];
+            } else {
+                const double dx = ix * xst - xc, dy = iy * yst - yc;
+                const double fx = (xc + cth * dx + sth * dy) / xst;  // R(-theta)
+                const double fy = (yc - sth * dx + cth * dy) / yst;
+                const int x0 = (int)floor(fx), y0 = (int)floor(fy);
+                const float tx = (float)(fx - x0), ty = (float)(fy - y0);
+                float ar = 0.0f, ai = 0.0f;
+                for (int a = 0; a < 4; a++) {
+                    const int xx = x0 - 1 + a;
+                    const float wx = catmull_rom(tx, a);
+                    for (int b = 0; b < 4; b++) {
+                        const int yy = y0 - 1 + b;
+                        const float w = wx * catmull_rom(ty, b);
+                        const float2 q = (xx >= 0 && xx < nx && yy >= 0 && yy < ny)
+                                             ? src[(size_t)xx * ny + yy]
+                                             : f;
+                        ar += w * q.x;
+                        ai += w * q.y;
+                    }
+                }
+                v = make_float2(ar, ai);
+            }
+        }
+        out[i] = v;
+    }
+}
+
+// Images from real-space amplitudes: images[dst[i]] (+)= sum over the units
+// img_units[img_off[i] .. img_off[i+1]) of |a|^2, divided by nconf when
+// flags & 2 (the bookkeeping of k_row_intensity).
+__global__ void k_intensity_direct(int nimg, const int *__restrict__ img_off,
+                                   const int *__restrict__ img_units,
+                                   const int *__restrict__ img_dst,
+                                   const int *__restrict__ img_flags,
+                                   const float2 *__restrict__ amp, float *__restrict__ images,
+                                   size_t plane, float nconf)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < plane * nimg;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const int img = (int)(i / plane);
+        const size_t r = i % plane;
+        float *dst = images + (size_t)img_dst[img] * plane + r;
+        const int fl = img_flags[img];
+        float acc = (fl & 1) ? *dst : 0.0f;
+        for (int k = img_off[img]; k < img_off[img + 1]; k++) {
+            const float2 a = amp[(size_t)img_units[k] * plane + r];
+            acc += a.x * a.x + a.y * a.y;
+        }
+        *dst = (fl & 2) ? __fdiv_rn(acc, nconf) : acc;
+    }
+}
+
 // ------------------------------------------------------------------ physics
 // Restatements of the reference's slicelib routines used to build tables.
 namespace phys {
@@ -734,14 +864,14 @@ struct DevBuf {
 // Kinds of launches for the per-kernel accounting (msk_profile).
 enum Kind {
     kSplat, kKColMask, kTransmit, kKColProp, kFresnel, kIntensity, kExit, kInit, kPlane, kFresTab,
-    kExpv, kAdjTransmit, kGrad, kImGrad, kAccum, kDW, kDWExp,
+    kExpv, kAdjTransmit, kGrad, kImGrad, kAccum, kDW, kDWExp, kRotShift,
     kKinds
 };
 static const char *const kKindName[kKinds] = {
     "row_splat", "col_bandlimit", "row_transmit", "col_propagate", "col_fresnel",
     "row_intensity", "row_exit", "row_init", "plane_init", "fresnel_table",
     "row_expv", "row_adj_transmit", "row_grad", "row_imgrad", "accumulate", "col_debye_waller",
-    "row_dw_phase"};
+    "row_dw_phase", "image_rotate_shift"};
 
 struct ProfRec {
     int kind;
@@ -769,6 +899,7 @@ struct msk_context {
     DevBuf stk, stk_v, stk_g, stk_t, stk_img, stk_part, adjtab;  // potential stacks, adjoint
     DevBuf arena;                                // specimen batches
     DevBuf dwbuf;                                // Debye-Waller -B/4 per (unit, slice)
+    DevBuf imgfill;                              // image-plane fill values per unit
     std::vector<cudaStream_t> lanes;             // concurrent specimens of a batch
     std::vector<cudaEvent_t> lane_ev;            // lane joins (one per lane) + fork
     size_t units_alloc = 0;  // units the psi / tbuf buffers hold
@@ -1243,7 +1374,7 @@ void msk_destroy(msk_context *ctx)
                       &ctx->imgmeta, &ctx->wave0, &ctx->images, &ctx->exitw, &ctx->fresnel,
                       &ctx->flags, &ctx->pa_v, &ctx->pa_t, &ctx->pa_psi, &ctx->pa_e, &ctx->stk,
                       &ctx->stk_v, &ctx->stk_g, &ctx->stk_t, &ctx->stk_img, &ctx->stk_part,
-                      &ctx->adjtab, &ctx->arena, &ctx->dwbuf})
+                      &ctx->adjtab, &ctx->arena, &ctx->dwbuf, &ctx->imgfill})
         b->release();
     for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_join, ctx->ev_t[0], ctx->ev_t[1], ctx->ev_free[0],
                           ctx->ev_free[1]})
@@ -1573,6 +1704,11 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
         MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     }
 
+    // image plane: rotation centre and shift (autosliccmd.cpp:1046, 1137-1141)
+    const double xst = s->ctblength / nx, yst = s->ctblength / ny;  // float divisions
+    const double xcen = 0.5 * (0.0 + s->ctblength) + s->dxc, ycen = 0.5 * (0.0 + s->ctblength) + s->dyc;
+    const int sxp = (int)floor(s->xshift / xst + 0.5), syp = (int)floor(s->yshift / yst + 0.5);
+
     const float wavlen = gp.wavlen;
     float k2maxo = s->aobj / wavlen;  // autosliccmd.cpp:1042-1043
     k2maxo = k2maxo * k2maxo;
@@ -1686,9 +1822,31 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
                 count_copy(ctx, 0, (double)(meta.size() * sizeof(int)));
                 const int *d_off = dm, *d_units = dm + off.size(),
                           *d_dst = d_units + units.size(), *d_flags = d_dst + nimg;
-                Prof p(ctx, kIntensity, 8.0 * plane * units.size() + 4.0 * plane * nimg);
-                rop->row_intensity(gp.g, nimg, d_off, d_units, d_dst, d_flags, tb, d_images,
-                                   (float)nconfig, ctx->stream);
+                const double rot = s->rotation ? s->rotation[d] : 0.0;
+                if (rot != 0.0 || sxp != 0 || syp != 0) {
+                    // the amplitude in real space, rotated and shifted, then |.|^2
+                    float2 *phi = ctx->tbuf2.as<float2>();
+                    {
+                        Prof p(ctx, kExit, 16.0 * plane * nb);
+                        rop->row_inverse(gp.g, nb, tb, phi, 1.0f, ctx->stream);
+                    }
+                    MSK_CUDA(ctx, ctx->imgfill.reserve((size_t)nb * sizeof(float2)));
+                    k_edge_mean<<<nb, 256, 0, ctx->stream>>>(phi, nx, ny, 5,
+                                                             ctx->imgfill.as<float2>());
+                    {
+                        Prof p(ctx, kRotShift, 16.0 * plane * nb);
+                        k_rotate_shift<<<8 * 152, 256, 0, ctx->stream>>>(
+                            phi, tb, nb, nx, ny, xst, yst, xcen, ycen, cos(rot), sin(rot),
+                            rot != 0.0, sxp, syp, ctx->imgfill.as<float2>());
+                    }
+                    Prof p(ctx, kIntensity, 8.0 * plane * units.size() + 4.0 * plane * nimg);
+                    k_intensity_direct<<<8 * 152, 256, 0, ctx->stream>>>(
+                        nimg, d_off, d_units, d_dst, d_flags, tb, d_images, plane, (float)nconfig);
+                } else {
+                    Prof p(ctx, kIntensity, 8.0 * plane * units.size() + 4.0 * plane * nimg);
+                    rop->row_intensity(gp.g, nimg, d_off, d_units, d_dst, d_flags, tb, d_images,
+                                       (float)nconfig, ctx->stream);
+                }
             }
         }
         MSK_CUDA(ctx, cudaGetLastError());
@@ -2261,8 +2419,9 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
     ctx->err.clear();
     if (!s || nspec < 1 || !spec || ndefocus < 0 || (ndefocus > 0 && !defocus))
         return fail(ctx, MSK_EINVAL, "bad batch arguments");
-    if (s->lwobble || s->R1 != 0.0)
-        return fail(ctx, MSK_EUNSUPPORTED, "batches take plane waves without thermal branches");
+    if (s->lwobble || s->R1 != 0.0 || s->rotation || s->xshift != 0.0 || s->yshift != 0.0)
+        return fail(ctx, MSK_EUNSUPPORTED,
+                    "batches take plane waves without thermal branches or image rotation");
     for (int i = 0; i < nspec; i++) {
         const msk_specimen &q = spec[i];
         if (q.natom < 0 || q.nangles < 1 || !q.angleZ || !q.angleY ||
@@ -2778,8 +2937,9 @@ extern "C" int msk_tilt_series_per_angle(msk_context *ctx, const msk_series *s, 
         (ndefocus > 0 && (!defocus || !images)) ||
         (natom > 0 && (!Znum || !x || !y || !z || !occ)) || (nconfig > 1 && !displacements))
         return fail(ctx, MSK_EINVAL, "bad tilt-series arguments");
-    if (s->lwobble || s->R1 != 0.0)
-        return fail(ctx, MSK_EUNSUPPORTED, "the comparison form takes plane waves without thermal branches");
+    if (s->lwobble || s->R1 != 0.0 || s->rotation || s->xshift != 0.0 || s->yshift != 0.0)
+        return fail(ctx, MSK_EUNSUPPORTED,
+                    "the comparison form takes plane waves without thermal branches or image rotation");
     const int nx = s->nx, ny = s->ny;
     if (!pow2_supported(nx) || !pow2_supported(ny))
         return fail(ctx, MSK_EUNSUPPORTED, "grid must be a power of two from 16 to 4096");

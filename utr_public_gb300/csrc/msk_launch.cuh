@@ -45,6 +45,9 @@ struct SizeOps {
                      float2 *psi, float scale, cudaStream_t);
     void (*row_exit)(const Geom &, const int *units, int nunits, const float2 *psi,
                      float2 *out, cudaStream_t);
+    // out = iS(in) * scale (the real-space wave of a W-state, unnormalised)
+    void (*row_inverse)(const Geom &, int nunits, const float2 *in, float2 *out, float scale,
+                        cudaStream_t);
     void (*row_intensity)(const Geom &, int nimg, const int *img_off, const int *img_units,
                           const int *img_dst, const int *img_flags, const float2 *ebuf,
                           float *images, float nconf, cudaStream_t);
@@ -186,6 +189,15 @@ struct Launch {
         k_row_simple<N, kRowInit><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::row, s>>>(
             g, units, wave0, psi, scale);
     }
+    static void row_inverse(const Geom &g, int nunits, const float2 *in, float2 *out,
+                            float scale, cudaStream_t s)
+    {
+        static std::once_flag f;
+        set_smem(k_row_simple<N, kRowExit>, Smem<N>::row, f);
+        const int L = RowCfg<N>::L;
+        k_row_simple<N, kRowExit><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::row, s>>>(
+            g, nullptr, in, out, scale);
+    }
     static void row_exit(const Geom &g, const int *units, int nunits, const float2 *psi,
                          float2 *out, cudaStream_t s)
     {
@@ -247,7 +259,7 @@ struct Launch {
         static const SizeOps o = {N,        ColCfg<N>::C, ColCfg<N>::BR,    splat,
                                   splat_potential, splat_spec, col_dw, row_dwexp,
                                   col_mask, col_prop,     col_fresnel,      row_transmit,
-                                  row_init, row_exit,     row_intensity,    row_expv,
+                                  row_init, row_exit,     row_inverse, row_intensity, row_expv,
                                   row_adj_transmit,       row_grad,         row_imgrad};
         return &o;
     }
