@@ -283,6 +283,39 @@ int msk_potential_stack(msk_context *ctx, const msk_series *s, int natom, const 
                         int nangles, const double *angleZ, const double *angleY, float *v,
                         int *kept);
 
+/* MsctKirkland's files (the reference reads and writes them through its
+ * XArrayLibrary, which is not part of it).  Images are [nx][ny] (iy fastest)
+ * and are written with rows along y, x fastest, as the reference transposes
+ * its cfpix data before writing (autosliccmd.cpp:1053-1055); little-endian.
+ *   GRD (ReadmeMsctKirkland.txt): "DSBB", nx ny (short), xlo xhi ylo yhi zlo zhi
+ *        (double; z = the value range), the values (float)
+ *   GRC: -5 (short), wavelength (double), nx ny (short), xlo xhi ylo yhi
+ *        (double), re im pairs (float)
+ *   TIFF32: baseline TIFF, one strip of 32-bit IEEE floats
+ * MSK_EINVAL when the file cannot be written. */
+int msk_write_grd(const char *path, const float *img, int nx, int ny, double xlo, double xhi,
+                  double ylo, double yhi);
+int msk_write_grc(const char *path, const float *amp, int nx, int ny, double wavelength,
+                  double xlo, double xhi, double ylo, double yhi);
+int msk_write_tiff32(const char *path, const float *img, int nx, int ny);
+
+/* MsctKirkland's orientation file (its parameter 17, ".txt" or ".relionnew"):
+ * angles[2i], angles[2i+1] = rotations about Z and Y' (degrees) of orientation
+ * i; its detector planes [plane_off[i], plane_off[i+1]) with planes[5k..5k+4] =
+ * {Z'' rotation (degrees), defocus from the object centre, astigmatism,
+ * astigmatism angle (degrees), 0}; shifts[2i], shifts[2i+1] = image shift along
+ * x and y.  Call first with null arrays: *nangles and *nplanes receive the
+ * counts; then with arrays of those sizes (plane_off: nangles + 1) and the
+ * counts as capacities.  ".txt": "//" comment lines, then per line the Z and
+ * Y' angles and (Z'' angle, defocus) pairs.  ".relionnew": index, name, x
+ * shift, y shift, defocus U, defocus V, astigmatism angle, rot, tilt, psi per
+ * line; every number but the astigmatism angle changes sign (the readme's
+ * rule); defocus = (U + V)/2, astigmatism = (U - V)/2 (this library's reading;
+ * the reference's reader is in the missing XArrayLibrary).  MSK_EINVAL on a
+ * malformed file or an unknown extension. */
+int msk_read_orientations(const char *path, int *nangles, int *nplanes, double *angles,
+                          int *plane_off, double *planes, double *shifts);
+
 /* Number of slice-steps calculate() runs for a box of depth ctblengthz
  * (autoslic.cpp:747-830: zslice = dz, dz + dz, ... while < ctblengthz + dz). */
 int msk_slice_count(float deltaz, float ctblengthz);

@@ -27,7 +27,8 @@ EXPORTS = ("msk_create", "msk_destroy", "msk_last_error", "msk_status_string", "
            "msk_tilt_series", "msk_slice_count", "msk_slice_assign", "msk_sort_by_z",
            "msk_rotate", "msk_potential_table", "msk_set_stream", "msk_profile",
            "msk_profile_read", "msk_calculate_static", "msk_tilt_series_per_angle",
-           "msk_stack_images", "msk_adjoint", "msk_potential_stack", "msk_tilt_series_batch")
+           "msk_stack_images", "msk_adjoint", "msk_potential_stack", "msk_tilt_series_batch",
+           "msk_write_grd", "msk_write_grc", "msk_write_tiff32", "msk_read_orientations")
 MSK_BATCH_GRAPH = 1
 
 
@@ -126,6 +127,11 @@ def load():
                                       C.c_int, _dp, _dp, vp, vp]
     L.msk_tilt_series_batch.argtypes = [vp, C.POINTER(Series), C.c_int, C.POINTER(SpecimenDesc),
                                         C.c_int, vp, C.c_int]
+    L.msk_write_grd.argtypes = [C.c_char_p, _fp, C.c_int, C.c_int] + [C.c_double] * 4
+    L.msk_write_grc.argtypes = [C.c_char_p, _fp, C.c_int, C.c_int] + [C.c_double] * 5
+    L.msk_write_tiff32.argtypes = [C.c_char_p, _fp, C.c_int, C.c_int]
+    L.msk_read_orientations.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), vp,
+                                        vp, vp, vp]
     _lib = L
     return L
 
@@ -138,6 +144,48 @@ def _ptr(a):
     if hasattr(a, "data_ptr"):  # torch tensor (device or host)
         return a.data_ptr()
     return a.ctypes.data
+
+
+def _io_check(st, path):
+    if st:
+        raise MskError(st, "cannot write or read %s" % path)
+
+
+def write_grd(path, img, xlo, xhi, ylo, yhi):
+    """Image [nx, ny] to a binary GRD file (msk_write_grd)."""
+    img = np.ascontiguousarray(img, np.float32)
+    _io_check(load().msk_write_grd(os.fsencode(path), img.reshape(-1), img.shape[0],
+                                   img.shape[1], xlo, xhi, ylo, yhi), path)
+
+
+def write_grc(path, amp, wavelength, xlo, xhi, ylo, yhi):
+    """Complex amplitude [nx, ny, 2] to a GRC file (msk_write_grc)."""
+    amp = np.ascontiguousarray(amp, np.float32)
+    _io_check(load().msk_write_grc(os.fsencode(path), amp.reshape(-1), amp.shape[0],
+                                   amp.shape[1], wavelength, xlo, xhi, ylo, yhi), path)
+
+
+def write_tiff32(path, img):
+    """Image [nx, ny] to a 32-bit float TIFF (msk_write_tiff32)."""
+    img = np.ascontiguousarray(img, np.float32)
+    _io_check(load().msk_write_tiff32(os.fsencode(path), img.reshape(-1), img.shape[0],
+                                      img.shape[1]), path)
+
+
+def read_orientations(path):
+    """(angles [n, 2] degrees, list of per-orientation plane arrays [k, 5], shifts
+    [n, 2]) from a MsctKirkland orientation file (msk_read_orientations)."""
+    L = load()
+    na, npl = C.c_int(0), C.c_int(0)
+    _io_check(L.msk_read_orientations(os.fsencode(path), C.byref(na), C.byref(npl), None, None,
+                                      None, None), path)
+    angles = np.zeros((na.value, 2))
+    off = np.zeros(na.value + 1, np.int32)
+    planes = np.zeros((max(npl.value, 1), 5))
+    shifts = np.zeros((na.value, 2))
+    _io_check(L.msk_read_orientations(os.fsencode(path), C.byref(na), C.byref(npl), _ptr(angles),
+                                      _ptr(off), _ptr(planes), _ptr(shifts)), path)
+    return angles, [planes[off[i]:off[i + 1]] for i in range(na.value)], shifts
 
 
 def make_param(ax, by, nx, ny, v0, deltaz, ctiltx=0.0, ctilty=0.0):

@@ -2,7 +2,7 @@
 
     python -m utr_public_gb300._build          # or __graft_entry__.build()
 
-Every .cu file under csrc/ compiles in parallel to an object in _build/,
+Every .cu and .cpp file under csrc/ compiles in parallel to an object in _build/,
 then the objects link into utr_public_gb300/libmsk.so with the CUDA runtime
 linked statically.  Host code is compiled with -ffp-contract=off so that the
 reference-exact host arithmetic rounds the same on x86-64 and aarch64.
@@ -33,7 +33,7 @@ def nvcc():
 
 
 def _sources():
-    return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
 
 
 def _deps():
@@ -56,7 +56,7 @@ def build(verbose=False, jobs=None):
     todo = []
     objs = []
     for src in _sources():
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(BUILD, os.path.splitext(os.path.basename(src))[0] + ".o")
         objs.append(obj)
         if _stale(obj, [src] + deps):
             todo.append((src, obj))
