@@ -179,6 +179,29 @@ int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int nspec,
                           const msk_specimen *spec, int ndefocus, const double *defocus,
                           int flags);
 
+/* The tilt series with its own detector planes per orientation, as
+ * MsctKirkland's orientation files give them (MultisliceT.cpp:264-285; see
+ * msk_read_orientations): orientation i images planes [plane_off[i],
+ * plane_off[i+1]) of `planes`, its images shifted by shifts[2i], shifts[2i+1]
+ * Angstrom (NULL: none); images[k] (float[plane_off[nangles]][nx][ny], host or
+ * device) is the image of plane k.  The lens settings other than astigmatism
+ * (aobj, cs3, cs5) and everything else come from `s`; its astig, astig_angle,
+ * rotation, xshift and yshift are not read.  Planes with equal parameters in
+ * different orientations share one free-space table and pass. */
+typedef struct {
+    double defocus;       /* Angstrom from the box centre */
+    double rotation;      /* about the optic axis, radians (the image-plane rotation) */
+    double astig;         /* two-fold astigmatism, Angstrom */
+    double astig_angle;   /* radians */
+} msk_plane;
+
+int msk_tilt_series_planes(msk_context *ctx, const msk_series *s, int natom, const int *Znum,
+                           const float *x, const float *y, const float *z, const float *occ,
+                           int nangles, const double *angleZ, const double *angleY,
+                           const int *plane_off, const msk_plane *planes, const double *shifts,
+                           int nconfig, const float *displacements, float *images,
+                           float *exitwaves, int *kept);
+
 /* calculate() without any allocation -- no counterpart in the reference.
  * For callers that cannot allocate device memory (a plug-in inside a host
  * framework that owns all device memory through its own pool, or a loop that

@@ -28,7 +28,8 @@ EXPORTS = ("msk_create", "msk_destroy", "msk_last_error", "msk_status_string", "
            "msk_rotate", "msk_potential_table", "msk_set_stream", "msk_profile",
            "msk_profile_read", "msk_calculate_static", "msk_tilt_series_per_angle",
            "msk_stack_images", "msk_adjoint", "msk_potential_stack", "msk_tilt_series_batch",
-           "msk_write_grd", "msk_write_grc", "msk_write_tiff32", "msk_read_orientations")
+           "msk_write_grd", "msk_write_grc", "msk_write_tiff32", "msk_read_orientations",
+           "msk_tilt_series_planes")
 MSK_BATCH_GRAPH = 1
 
 
@@ -66,6 +67,12 @@ class SpecimenDesc(C.Structure):
                 ("ctblength", C.c_float), ("ctblengthz", C.c_float), ("nangles", C.c_int),
                 ("angleZ", C.c_void_p), ("angleY", C.c_void_p), ("images", C.c_void_p),
                 ("kept", C.c_void_p)]
+
+
+class Plane(C.Structure):
+    """msk_plane (include/msk.h): one detector plane of one orientation."""
+    _fields_ = [("defocus", C.c_double), ("rotation", C.c_double), ("astig", C.c_double),
+                ("astig_angle", C.c_double)]
 
 
 class KernelStat(C.Structure):
@@ -127,6 +134,8 @@ def load():
                                       C.c_int, _dp, _dp, vp, vp]
     L.msk_tilt_series_batch.argtypes = [vp, C.POINTER(Series), C.c_int, C.POINTER(SpecimenDesc),
                                         C.c_int, vp, C.c_int]
+    L.msk_tilt_series_planes.argtypes = [vp, C.POINTER(Series), C.c_int, vp, vp, vp, vp, vp,
+                                         C.c_int, _dp, _dp, vp, vp, vp, C.c_int, vp, vp, vp, vp]
     L.msk_write_grd.argtypes = [C.c_char_p, _fp, C.c_int, C.c_int] + [C.c_double] * 4
     L.msk_write_grc.argtypes = [C.c_char_p, _fp, C.c_int, C.c_int] + [C.c_double] * 5
     L.msk_write_tiff32.argtypes = [C.c_char_p, _fp, C.c_int, C.c_int]
@@ -436,6 +445,54 @@ class Context:
                                       _ptr(defocus), _ptr(target), _ptr(grad), C.byref(loss))
         self._check(st)
         return loss.value, grad
+
+    def tilt_series_planes(self, series, Znum, x, y, z, occ, angleZ, angleY, planes,
+                           shifts=None, nconfig=1, displacements=None, images=None,
+                           want_exit=False):
+        """Tilt series with per-orientation detector planes (msk_tilt_series_planes).
+        planes: per orientation a sequence of (defocus, rotation, astig, astig_angle)
+        rows (radians); shifts [nangles, 2] Angstrom.  Returns (images [total planes,
+        nx, ny], kept) or (images, exit waves, kept) with want_exit."""
+        angleZ = np.ascontiguousarray(angleZ, np.float64)
+        angleY = np.ascontiguousarray(angleY, np.float64)
+        na = len(angleZ)
+        off = np.zeros(na + 1, np.int32)
+        rows = []
+        for a in range(na):
+            pa = np.asarray(planes[a], np.float64).reshape(-1, 4)
+            rows.extend(pa)
+            off[a + 1] = off[a] + len(pa)
+        total = int(off[-1])
+        arr = (Plane * max(total, 1))()
+        for k, r in enumerate(rows):
+            arr[k].defocus, arr[k].rotation, arr[k].astig, arr[k].astig_angle = map(float, r)
+        sh = None if shifts is None else np.ascontiguousarray(shifts, np.float64).reshape(-1)
+        if images is None:
+            images = np.zeros((total, series.nx, series.ny), np.float32)
+        exitwaves = np.zeros((na, nconfig, series.nx, series.ny, 2), np.float32) \
+            if want_exit else None
+        kept = np.zeros(na * nconfig, np.int32)
+        arrs = [np.ascontiguousarray(a, dt) for a, dt in
+                ((Znum, np.int32), (x, np.float32), (y, np.float32), (z, np.float32),
+                 (occ, np.float32))]
+        disp = None if displacements is None else np.ascontiguousarray(displacements, np.float32)
+        st = self.L.msk_tilt_series_planes(self.h, C.byref(series), len(arrs[1]),
+                                           *[_ptr(a) for a in arrs], na, angleZ, angleY,
+                                           _ptr(off), C.addressof(arr), _ptr(sh), nconfig,
+                                           _ptr(disp), _ptr(images), _ptr(exitwaves),
+                                           _ptr(kept))
+        self._check(st)
+        return (images, exitwaves, kept) if want_exit else (images, kept)
+
+    def tilt_series_from_file(self, series, Znum, x, y, z, occ, path, **kw):
+        """The tilt series a MsctKirkland orientation file (.txt or .relionnew)
+        describes: its angles and Z'' rotations in degrees, defoci from the object
+        centre, astigmatism and image shifts; images in file order."""
+        angles, planes, shifts = read_orientations(path)
+        rad = np.pi / 180.0
+        pl = [np.stack([p[:, 1], p[:, 0] * rad, p[:, 2], p[:, 3] * rad], axis=1) for p in planes]
+        return self.tilt_series_planes(series, Znum, x, y, z, occ, angles[:, 0] * rad,
+                                       angles[:, 1] * rad, pl, shifts=shifts, **kw)
 
     def tilt_series_per_angle(self, series, Znum, x, y, z, occ, angleZ, angleY, defocus,
                               nconfig=1, displacements=None, images=None):

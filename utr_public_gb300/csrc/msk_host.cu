@@ -6,6 +6,7 @@
 // boundaries, frequency grids, propagator tables) is compiled with
 // -ffp-contract=off so that x86-64 and aarch64 give the same bits.
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -102,10 +103,10 @@ __global__ void k_fresnel_table(const Geom g, const Fresnel fr, float scale, flo
 //            rounded to whole pixels.
 
 // Per unit: the edge means of the real and imaginary parts, in double.
-__global__ void k_edge_mean(const float2 *__restrict__ phi, int nx, int ny, int border,
-                            float2 *__restrict__ mean)
+__global__ void k_edge_mean(const float2 *__restrict__ phi, const int *__restrict__ units, int nx,
+                            int ny, int border, float2 *__restrict__ mean)
 {
-    const int u = blockIdx.x;
+    const int u = units ? units[blockIdx.x] : (int)blockIdx.x;
     const float2 *p = phi + (size_t)u * nx * ny;
     double sr = 0.0, si = 0.0;
     long long cnt = 0;
@@ -149,14 +150,16 @@ __device__ __forceinline__ float catmull_rom(float t, int k)
 }
 
 __global__ void k_rotate_shift(const float2 *__restrict__ in, float2 *__restrict__ out,
-                               int nunits, int nx, int ny, double xst, double yst, double xc,
-                               double yc, double cth, double sth, int rotate, int sx, int sy,
+                               const int *__restrict__ units, int nunits, int nx, int ny,
+                               double xst, double yst, double xc, double yc, double cth,
+                               double sth, int rotate, int sx, int sy,
                                const float2 *__restrict__ fill)
 {
     const size_t plane = (size_t)nx * ny;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < plane * nunits;
          i += (size_t)gridDim.x * blockDim.x) {
-        const int u = (int)(i / plane), r = (int)(i % plane);
+        const int ui = (int)(i / plane), r = (int)(i % plane);
+        const int u = units ? units[ui] : ui;
         const int ix = r / ny - sx, iy = r % ny - sy;
         const float2 f = fill[u];
         const float2 *src = in + (size_t)u * plane;
@@ -187,7 +190,7 @@ __global__ void k_rotate_shift(const float2 *__restrict__ in, float2 *__restrict
                 v = make_float2(ar, ai);
             }
         }
-        out[i] = v;
+        out[(size_t)u * plane + r] = v;
     }
 }
 
@@ -1618,19 +1621,34 @@ int msk_calculate(msk_context *ctx, float *pix, const float *wave0, const float 
     return flags_check(ctx);
 }
 
-int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int *Znum,
-                    const float *x, const float *y, const float *z, const float *occ,
-                    int nangles, const double *angleZ, const double *angleY, int ndefocus,
-                    const double *defocus, int nconfig, const float *displacements,
-                    float *images, float *exitwaves, int *kept)
+}  // extern "C"
+
+namespace {
+
+// Detector planes per orientation: orientation a images planes
+// [off[a], off[a+1]) of `p`, shifted by shift[2a], shift[2a+1] Angstrom;
+// images[k] is the image of plane k.
+struct PlaneDesc {
+    double defocus, rotation, astig, astig_angle;
+};
+struct PlaneList {
+    int total = 0;
+    std::vector<int> off;
+    std::vector<PlaneDesc> p;
+    std::vector<double> shift;
+};
+
+int tilt_series_impl(msk_context *ctx, const msk_series *s, int natom, const int *Znum,
+                     const float *x, const float *y, const float *z, const float *occ,
+                     int nangles, const double *angleZ, const double *angleY,
+                     const PlaneList &pl, int nconfig, const float *displacements,
+                     float *images, float *exitwaves, int *kept)
 {
-    if (!ctx) return MSK_EINVAL;
-    ctx->err.clear();
-    if (!s || natom < 0 || nangles < 1 || ndefocus < 0 || nconfig < 1 || !angleZ || !angleY ||
-        (ndefocus > 0 && (!defocus || !images)) ||
-        (natom > 0 && (!Znum || !x || !y || !z || !occ)) ||
+    if (!s || natom < 0 || nangles < 1 || nconfig < 1 || !angleZ || !angleY ||
+        (pl.total > 0 && !images) || (natom > 0 && (!Znum || !x || !y || !z || !occ)) ||
         (nconfig > 1 && !displacements && !s->lwobble))
         return fail(ctx, MSK_EINVAL, "bad tilt-series arguments");
+    const int ndefocus = pl.total;  // images in all
     const int nx = s->nx, ny = s->ny;
     if (nx < 1 || ny < 1 || s->ctblength < 0.0f) return fail(ctx, MSK_EBADSIZE, "bad size parameters");
     if (!pow2_supported(nx) || !pow2_supported(ny))
@@ -1654,7 +1672,7 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
     // psi + t per unit; the image and exit-wave outputs are held separately
     const bool img_dev = ndefocus > 0 && is_device_ptr(images);
     const bool ew_dev = exitwaves && is_device_ptr(exitwaves);
-    const size_t img_bytes = (size_t)nangles * ndefocus * plane * sizeof(float);
+    const size_t img_bytes = (size_t)ndefocus * plane * sizeof(float);
     size_t budget = free_b - std::min(free_b, (size_t)(img_dev ? 0 : img_bytes));
     budget = std::min<size_t>(budget / 2, (size_t)64 << 30);
     // psi and two transmission buffers per unit in flight
@@ -1707,7 +1725,6 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
     // image plane: rotation centre and shift (autosliccmd.cpp:1046, 1137-1141)
     const double xst = s->ctblength / nx, yst = s->ctblength / ny;  // float divisions
     const double xcen = 0.5 * (0.0 + s->ctblength) + s->dxc, ycen = 0.5 * (0.0 + s->ctblength) + s->dyc;
-    const int sxp = (int)floor(s->xshift / xst + 0.5), syp = (int)floor(s->yshift / yst + 0.5);
 
     const float wavlen = gp.wavlen;
     float k2maxo = s->aobj / wavlen;  // autosliccmd.cpp:1042-1043
@@ -1770,82 +1787,122 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
             if (!ew_dev) count_copy(ctx, 1, (double)nb * plane * sizeof(float2));
         }
         if (ndefocus > 0) {
-            // one image per angle in this batch; its configurations in order
+            // this batch's orientations: their units (configurations in order) and
+            // whether their images continue or finish a configuration average
             const int a_first = u0 / nconfig, a_last = (u0 + nb - 1) / nconfig;
-            const int nimg = a_last - a_first + 1;
-            std::vector<int> meta;  // img_off[nimg+1] | img_units | img_dst[nimg] | img_flags[nimg]
-            std::vector<int> off(nimg + 1), units, flags(nimg);
+            const int na_b = a_last - a_first + 1;
+            std::vector<std::vector<int>> aunits(na_b);
+            std::vector<int> aflags(na_b);
+            int kmax = 0;
             for (int a = a_first; a <= a_last; a++) {
                 const int c0 = std::max(u0, a * nconfig), c1 = std::min(u0 + nb, (a + 1) * nconfig);
-                off[a - a_first] = (int)units.size();
-                for (int u = c0; u < c1; u++) units.push_back(u - u0);
+                for (int u = c0; u < c1; u++) aunits[a - a_first].push_back(u - u0);
                 int f = 0;
                 if (c0 > a * nconfig) f |= 1;                        // continue a partial sum
                 if (c1 == (a + 1) * nconfig && nconfig > 1) f |= 2;   // last configuration
-                flags[a - a_first] = f;
+                aflags[a - a_first] = f;
+                kmax = std::max(kmax, pl.off[a + 1] - pl.off[a]);
             }
-            off[nimg] = (int)units.size();
-            const size_t nmeta = off.size() + units.size() + 2 * (size_t)nimg;
-            MSK_CUDA(ctx, ctx->imgmeta.reserve(nmeta * sizeof(int) * (size_t)ndefocus));
-            for (int d = 0; d < ndefocus; d++) {
-                const double rprime = defocus[d] - 0.5 * s->ctblengthz;  // autosliccmd.cpp:1060
-                Fresnel fr{};
-                fr.a1 = pi * l * rprime;
-                fr.a3 = (pi / 2.0) * s->cs3 * l * l * l;
-                fr.a5 = (pi / 3.0) * s->cs5 * l * l * l * l * l;
-                fr.a2c = (pi / 2.0) * l * s->astig * cos(2.0 * s->astig_angle);
-                fr.a2s = (pi / 2.0) * l * s->astig * sin(2.0 * s->astig_angle);
-                fr.k2maxo = k2maxo;
-                fr.kx = tables_kx(ctx, gp);
-                fr.ky = tables_ky(ctx, gp);
-                // psi_d = iS(iF(exp(-i chi) F(W)))/N: the multiplier (with 1/N)
-                // once per plane, then one column pass per wave
-                MSK_CUDA(ctx, ctx->fresnel.reserve(plane * sizeof(float2)));
-                fr.table = ctx->fresnel.as<float2>();
-                {
-                    Prof p(ctx, kFresTab, 8.0 * plane);
-                    k_fresnel_table<<<4 * 152, 256, 0, ctx->stream>>>(
-                        gp.g, fr, 1.0f / ((float)nx * (float)ny), ctx->fresnel.as<float2>());
+            MSK_CUDA(ctx, ctx->fresnel.reserve(plane * sizeof(float2)));
+            MSK_CUDA(ctx, ctx->imgfill.reserve((size_t)B * sizeof(float2)));
+            for (int k = 0; k < kmax; k++) {
+                // the k-th plane of every orientation, grouped by equal free-space
+                // and image-plane parameters: one table and one pass per group
+                struct Group {
+                    std::array<double, 6> key;
+                    std::vector<int> ori;  // orientation indices within the batch
+                    size_t o_units, o_off, o_dst, o_flags;
+                    int n_units;
+                };
+                std::vector<Group> groups;
+                for (int a = a_first; a <= a_last; a++) {
+                    if (pl.off[a + 1] - pl.off[a] <= k) continue;
+                    const PlaneDesc &q = pl.p[pl.off[a] + k];
+                    const std::array<double, 6> key = {
+                        q.defocus, q.astig, q.astig_angle, q.rotation,
+                        floor(pl.shift[2 * a] / xst + 0.5), floor(pl.shift[2 * a + 1] / yst + 0.5)};
+                    size_t gi = 0;
+                    while (gi < groups.size() && groups[gi].key != key) gi++;
+                    if (gi == groups.size()) groups.push_back(Group{key, {}, 0, 0, 0, 0, 0});
+                    groups[gi].ori.push_back(a - a_first);
                 }
-                {
-                    Prof p(ctx, kFresnel, 16.0 * plane * nb);
-                    cop->col_fresnel(gp.g, pmap, tmap, nullptr, nb, fr, 1.0f, ctx->stream);
+                // per group: img_off[n+1] | img_units | img_dst[n] | img_flags[n]
+                std::vector<int> meta;
+                for (Group &gr : groups) {
+                    const int n = (int)gr.ori.size();
+                    gr.o_off = meta.size();
+                    int cnt = 0;
+                    for (int oa : gr.ori) {
+                        meta.push_back(cnt);
+                        cnt += (int)aunits[oa].size();
+                    }
+                    meta.push_back(cnt);
+                    gr.o_units = meta.size();
+                    gr.n_units = cnt;
+                    for (int oa : gr.ori) meta.insert(meta.end(), aunits[oa].begin(), aunits[oa].end());
+                    gr.o_dst = meta.size();
+                    for (int oa : gr.ori) meta.push_back(pl.off[a_first + oa] + k);
+                    gr.o_flags = meta.size();
+                    for (int oa : gr.ori) meta.push_back(aflags[oa]);
+                    (void)n;
                 }
-                meta.clear();
-                meta.insert(meta.end(), off.begin(), off.end());
-                meta.insert(meta.end(), units.begin(), units.end());
-                for (int a = a_first; a <= a_last; a++) meta.push_back(a * ndefocus + d);
-                meta.insert(meta.end(), flags.begin(), flags.end());
-                int *dm = ctx->imgmeta.as<int>() + (size_t)d * nmeta;
-                MSK_CUDA(ctx, cudaMemcpyAsync(dm, meta.data(), meta.size() * sizeof(int),
+                MSK_CUDA(ctx, ctx->imgmeta.reserve(meta.size() * sizeof(int)));
+                MSK_CUDA(ctx, cudaMemcpyAsync(ctx->imgmeta.p, meta.data(), meta.size() * sizeof(int),
                                               cudaMemcpyHostToDevice, ctx->stream));
                 count_copy(ctx, 0, (double)(meta.size() * sizeof(int)));
-                const int *d_off = dm, *d_units = dm + off.size(),
-                          *d_dst = d_units + units.size(), *d_flags = d_dst + nimg;
-                const double rot = s->rotation ? s->rotation[d] : 0.0;
-                if (rot != 0.0 || sxp != 0 || syp != 0) {
-                    // the amplitude in real space, rotated and shifted, then |.|^2
-                    float2 *phi = ctx->tbuf2.as<float2>();
+                const int *dm = ctx->imgmeta.as<int>();
+                for (const Group &gr : groups) {
+                    const int nimg = (int)gr.ori.size(), nu = gr.n_units;
+                    const int *d_off = dm + gr.o_off, *d_units = dm + gr.o_units,
+                              *d_dst = dm + gr.o_dst, *d_flags = dm + gr.o_flags;
+                    const double rprime = gr.key[0] - 0.5 * s->ctblengthz;  // autosliccmd.cpp:1060
+                    Fresnel fr{};
+                    fr.a1 = pi * l * rprime;
+                    fr.a3 = (pi / 2.0) * s->cs3 * l * l * l;
+                    fr.a5 = (pi / 3.0) * s->cs5 * l * l * l * l * l;
+                    fr.a2c = (pi / 2.0) * l * gr.key[1] * cos(2.0 * gr.key[2]);
+                    fr.a2s = (pi / 2.0) * l * gr.key[1] * sin(2.0 * gr.key[2]);
+                    fr.k2maxo = k2maxo;
+                    fr.kx = tables_kx(ctx, gp);
+                    fr.ky = tables_ky(ctx, gp);
+                    // psi_d = iS(iF(exp(-i chi) F(W)))/N: the multiplier (with 1/N)
+                    // once per group, then one column pass over its waves
+                    fr.table = ctx->fresnel.as<float2>();
                     {
-                        Prof p(ctx, kExit, 16.0 * plane * nb);
-                        rop->row_inverse(gp.g, nb, tb, phi, 1.0f, ctx->stream);
+                        Prof p(ctx, kFresTab, 8.0 * plane);
+                        k_fresnel_table<<<4 * 152, 256, 0, ctx->stream>>>(
+                            gp.g, fr, 1.0f / ((float)nx * (float)ny), ctx->fresnel.as<float2>());
                     }
-                    MSK_CUDA(ctx, ctx->imgfill.reserve((size_t)nb * sizeof(float2)));
-                    k_edge_mean<<<nb, 256, 0, ctx->stream>>>(phi, nx, ny, 5,
-                                                             ctx->imgfill.as<float2>());
                     {
-                        Prof p(ctx, kRotShift, 16.0 * plane * nb);
-                        k_rotate_shift<<<8 * 152, 256, 0, ctx->stream>>>(
-                            phi, tb, nb, nx, ny, xst, yst, xcen, ycen, cos(rot), sin(rot),
-                            rot != 0.0, sxp, syp, ctx->imgfill.as<float2>());
+                        Prof p(ctx, kFresnel, 16.0 * plane * nu);
+                        cop->col_fresnel(gp.g, pmap, tmap, d_units, nu, fr, 1.0f, ctx->stream);
                     }
-                    Prof p(ctx, kIntensity, 8.0 * plane * units.size() + 4.0 * plane * nimg);
-                    k_intensity_direct<<<8 * 152, 256, 0, ctx->stream>>>(
-                        nimg, d_off, d_units, d_dst, d_flags, tb, d_images, plane, (float)nconfig);
-                } else {
-                    Prof p(ctx, kIntensity, 8.0 * plane * units.size() + 4.0 * plane * nimg);
-                    rop->row_intensity(gp.g, nimg, d_off, d_units, d_dst, d_flags, tb, d_images,
-                                       (float)nconfig, ctx->stream);
+                    const double rot = gr.key[3];
+                    const int sxp = (int)gr.key[4], syp = (int)gr.key[5];
+                    if (rot != 0.0 || sxp != 0 || syp != 0) {
+                        // the amplitude in real space, rotated and shifted, then |.|^2
+                        float2 *phi = ctx->tbuf2.as<float2>();
+                        {
+                            Prof p(ctx, kExit, 16.0 * plane * nu);
+                            rop->row_inverse(gp.g, d_units, nu, tb, phi, 1.0f, ctx->stream);
+                        }
+                        k_edge_mean<<<nu, 256, 0, ctx->stream>>>(phi, d_units, nx, ny, 5,
+                                                                 ctx->imgfill.as<float2>());
+                        {
+                            Prof p(ctx, kRotShift, 16.0 * plane * nu);
+                            k_rotate_shift<<<8 * 152, 256, 0, ctx->stream>>>(
+                                phi, tb, d_units, nu, nx, ny, xst, yst, xcen, ycen, cos(rot),
+                                sin(rot), rot != 0.0, sxp, syp, ctx->imgfill.as<float2>());
+                        }
+                        Prof p(ctx, kIntensity, 8.0 * plane * nu + 4.0 * plane * nimg);
+                        k_intensity_direct<<<8 * 152, 256, 0, ctx->stream>>>(
+                            nimg, d_off, d_units, d_dst, d_flags, tb, d_images, plane,
+                            (float)nconfig);
+                    } else {
+                        Prof p(ctx, kIntensity, 8.0 * plane * nu + 4.0 * plane * nimg);
+                        rop->row_intensity(gp.g, nimg, d_off, d_units, d_dst, d_flags, tb,
+                                           d_images, (float)nconfig, ctx->stream);
+                    }
                 }
             }
         }
@@ -1863,6 +1920,65 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
     if (kept)
         for (int u = 0; u < nunits; u++) kept[u] = ua[u].kept;
     return flags_check(ctx);
+}
+
+}  // namespace
+
+extern "C" {
+
+int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int *Znum,
+                    const float *x, const float *y, const float *z, const float *occ,
+                    int nangles, const double *angleZ, const double *angleY, int ndefocus,
+                    const double *defocus, int nconfig, const float *displacements,
+                    float *images, float *exitwaves, int *kept)
+{
+    if (!ctx) return MSK_EINVAL;
+    ctx->err.clear();
+    if (!s || nangles < 1 || ndefocus < 0 || (ndefocus > 0 && (!defocus || !images)))
+        return fail(ctx, MSK_EINVAL, "bad tilt-series arguments");
+    // the same planes for every orientation: image [a][d] is plane a * ndefocus + d
+    PlaneList pl;
+    pl.total = nangles * ndefocus;
+    for (int a = 0; a <= nangles; a++) pl.off.push_back(a * ndefocus);
+    for (int a = 0; a < nangles; a++) {
+        for (int d = 0; d < ndefocus; d++)
+            pl.p.push_back(PlaneDesc{defocus[d], s->rotation ? s->rotation[d] : 0.0, s->astig,
+                                     s->astig_angle});
+        pl.shift.push_back(s->xshift);
+        pl.shift.push_back(s->yshift);
+    }
+    return tilt_series_impl(ctx, s, natom, Znum, x, y, z, occ, nangles, angleZ, angleY, pl,
+                            nconfig, displacements, images, exitwaves, kept);
+}
+
+int msk_tilt_series_planes(msk_context *ctx, const msk_series *s, int natom, const int *Znum,
+                           const float *x, const float *y, const float *z, const float *occ,
+                           int nangles, const double *angleZ, const double *angleY,
+                           const int *plane_off, const msk_plane *planes, const double *shifts,
+                           int nconfig, const float *displacements, float *images,
+                           float *exitwaves, int *kept)
+{
+    if (!ctx) return MSK_EINVAL;
+    ctx->err.clear();
+    if (!s || nangles < 1 || !plane_off || plane_off[0] != 0)
+        return fail(ctx, MSK_EINVAL, "bad plane lists");
+    PlaneList pl;
+    for (int a = 0; a <= nangles; a++) {
+        if (a > 0 && plane_off[a] < plane_off[a - 1])
+            return fail(ctx, MSK_EINVAL, "plane_off must not decrease");
+        pl.off.push_back(plane_off[a]);
+    }
+    pl.total = plane_off[nangles];
+    if (pl.total > 0 && (!planes || !images)) return fail(ctx, MSK_EINVAL, "bad plane lists");
+    for (int k = 0; k < pl.total; k++)
+        pl.p.push_back(PlaneDesc{planes[k].defocus, planes[k].rotation, planes[k].astig,
+                                 planes[k].astig_angle});
+    for (int a = 0; a < nangles; a++) {
+        pl.shift.push_back(shifts ? shifts[2 * a] : 0.0);
+        pl.shift.push_back(shifts ? shifts[2 * a + 1] : 0.0);
+    }
+    return tilt_series_impl(ctx, s, natom, Znum, x, y, z, occ, nangles, angleZ, angleY, pl,
+                            nconfig, displacements, images, exitwaves, kept);
 }
 
 }  // extern "C"

@@ -46,8 +46,8 @@ struct SizeOps {
     void (*row_exit)(const Geom &, const int *units, int nunits, const float2 *psi,
                      float2 *out, cudaStream_t);
     // out = iS(in) * scale (the real-space wave of a W-state, unnormalised)
-    void (*row_inverse)(const Geom &, int nunits, const float2 *in, float2 *out, float scale,
-                        cudaStream_t);
+    void (*row_inverse)(const Geom &, const int *units, int nunits, const float2 *in,
+                        float2 *out, float scale, cudaStream_t);
     void (*row_intensity)(const Geom &, int nimg, const int *img_off, const int *img_units,
                           const int *img_dst, const int *img_flags, const float2 *ebuf,
                           float *images, float nconf, cudaStream_t);
@@ -189,14 +189,14 @@ struct Launch {
         k_row_simple<N, kRowInit><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::row, s>>>(
             g, units, wave0, psi, scale);
     }
-    static void row_inverse(const Geom &g, int nunits, const float2 *in, float2 *out,
-                            float scale, cudaStream_t s)
+    static void row_inverse(const Geom &g, const int *units, int nunits, const float2 *in,
+                            float2 *out, float scale, cudaStream_t s)
     {
         static std::once_flag f;
         set_smem(k_row_simple<N, kRowExit>, Smem<N>::row, f);
         const int L = RowCfg<N>::L;
         k_row_simple<N, kRowExit><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::row, s>>>(
-            g, nullptr, in, out, scale);
+            g, units, in, out, scale);
     }
     static void row_exit(const Geom &g, const int *units, int nunits, const float2 *psi,
                          float2 *out, cudaStream_t s)
