@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstring>
 #include <functional>
+#include <map>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -579,10 +580,12 @@ static bool grid_pre(GridPre &gp, int nx, int ny, float ax, float by, float v0, 
     // column blocks of the column passes (C columns each) holding in-band columns
     g.band_p = gp.band_p;
     g.band_q = gp.band_q;
-    const int C = size_ops(nx)->col_c, nblk = ny / C;
-    g.cb_lo = std::min(nblk, (gp.band_p + 1 + C - 1) / C);
-    g.cb_hi0 = std::max(g.cb_lo, gp.band_q / C);
-    g.cb_n = g.cb_lo + (nblk - g.cb_hi0);
+    for (int v = 0; v < 2; v++) {
+        const int C = size_ops(nx)->col_c[v], nblk = ny / C;
+        g.cb_lo[v] = std::min(nblk, (gp.band_p + 1 + C - 1) / C);
+        g.cb_hi0[v] = std::max(g.cb_lo[v], gp.band_q / C);
+        g.cb_n[v] = g.cb_lo[v] + (nblk - g.cb_hi0[v]);
+    }
     g.seg_e1 = std::min(ny, (gp.band_p + 2) & ~1);
     g.seg_s2 = std::max(g.seg_e1, gp.band_q & ~1);
     return true;
@@ -903,6 +906,8 @@ struct msk_context {
     DevBuf arena;                                // specimen batches
     DevBuf dwbuf;                                // Debye-Waller -B/4 per (unit, slice)
     DevBuf imgfill;                              // image-plane fill values per unit
+    DevBuf tune;                                 // scratch grid of the column tuner
+    bool no_tune = false;                        // column tiles fixed at variant 0
     std::vector<cudaStream_t> lanes;             // concurrent specimens of a batch
     std::vector<cudaEvent_t> lane_ev;            // lane joins (one per lane) + fork
     size_t units_alloc = 0;  // units the psi / tbuf buffers hold
@@ -944,21 +949,23 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
     return fn;
 }
 
-// 2D view of a wave buffer for the column passes: rows = units * nx, each
-// row ny complex64 = 2*ny floats; box = the pass's column tile.
-int column_map(msk_context *ctx, CUtensorMap *map, void *base, int nx, int ny, size_t units,
-               const SizeOps *cop)
+// 2D view of a wave buffer for the column passes of tile variant v: rows =
+// units * nx, each row ny complex64 = 2*ny floats; box = the variant's
+// column tile.
+int column_map(msk_context *ctx, ColView *view, void *base, int nx, int ny, size_t units,
+               const SizeOps *cop, int v)
 {
     auto enc = tensor_map_encoder();
     if (!enc) return fail(ctx, MSK_ECUDA, "cuTensorMapEncodeTiled is not available");
     const cuuint64_t dims[2] = {(cuuint64_t)2 * ny, (cuuint64_t)units * nx};
     const cuuint64_t strides[1] = {(cuuint64_t)ny * 8};
-    const cuuint32_t box[2] = {(cuuint32_t)(2 * cop->col_c), (cuuint32_t)cop->col_box_rows};
+    const cuuint32_t box[2] = {(cuuint32_t)(2 * cop->col_c[v]), (cuuint32_t)cop->col_box_rows};
     const cuuint32_t estr[2] = {1, 1};
-    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+    CUresult r = enc(&view->map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box,
+                     estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(ctx, MSK_ECUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    view->v = v;
     return MSK_OK;
 }
 
@@ -1048,6 +1055,77 @@ void prof_collect(msk_context *ctx)
         ctx->prof_pool.push_back(r.b);
     }
     ctx->prof_pending.clear();
+}
+
+// The column tile of each pass (ColCfg variant), per device, grid and pass:
+// the first time a pass runs on a grid, both widths run on a scratch grid
+// (three timed launches each, after one untimed) and the faster is kept for the
+// life of the process.  The widths compute every column identically, so the
+// choice changes speed only.  MSK_COL_TILE=0 or 1 in the environment fixes it.
+struct ColChoices {
+    std::mutex m;
+    std::map<std::array<int, 4>, int> v;  // (device, nx, ny, pass) -> variant
+};
+ColChoices &col_choices()
+{
+    static ColChoices c;
+    return c;
+}
+
+int col_variant(msk_context *ctx, const GridPre &gp, int mode)
+{
+    if (ctx->no_tune) return 0;
+    static const char *forced = getenv("MSK_COL_TILE");
+    if (forced && (forced[0] == '0' || forced[0] == '1') && forced[1] == 0) return forced[0] - '0';
+    const std::array<int, 4> key = {ctx->device, gp.nx, gp.ny, mode};
+    ColChoices &cc = col_choices();
+    std::lock_guard<std::mutex> lock(cc.m);
+    auto it = cc.v.find(key);
+    if (it != cc.v.end()) return it->second;
+    const SizeOps *cop = size_ops(gp.nx);
+    const size_t plane = (size_t)gp.nx * gp.ny;
+    const int U = (int)std::max<size_t>(2, std::min<size_t>(64, ((size_t)256 << 20) / (plane * 8)));
+    int choice = 0;
+    float ms[2] = {0.0f, 0.0f};
+    bool ok = ctx->tune.reserve((size_t)(U + 1) * plane * sizeof(float2)) == cudaSuccess &&
+              cudaMemsetAsync(ctx->tune.p, 0, (size_t)(U + 1) * plane * sizeof(float2),
+                              ctx->stream) == cudaSuccess;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ok = ok && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess;
+    float2 *grid = ctx->tune.as<float2>();
+    Fresnel fr{};
+    fr.table = grid + (size_t)U * plane;  // zeros
+    fr.dw = reinterpret_cast<const float *>(grid + (size_t)U * plane);
+    fr.dw_stride = 1;
+    const Geom &g = gp.g;
+    for (int v = 0; v < 2 && ok; v++) {
+        ColView view;
+        if (column_map(ctx, &view, grid, gp.nx, gp.ny, U, cop, v) != MSK_OK) {
+            ok = false;
+            break;
+        }
+        auto launch = [&] {
+            switch (mode) {
+            case kColMask: cop->col_mask(g, view, view, nullptr, U, 1, ctx->stream); break;
+            case kColProp: cop->col_prop(g, view, view, nullptr, U, 1, ctx->stream); break;
+            case kColFresnel: cop->col_fresnel(g, view, view, nullptr, U, fr, 1.0f, ctx->stream); break;
+            default: cop->col_dw(g, view, nullptr, U, fr.dw, 1, ctx->stream); break;
+            }
+        };
+        launch();
+        ok = cudaEventRecord(e0, ctx->stream) == cudaSuccess;
+        for (int r = 0; r < 3; r++) launch();
+        ok = ok && cudaEventRecord(e1, ctx->stream) == cudaSuccess &&
+             cudaEventSynchronize(e1) == cudaSuccess &&
+             cudaEventElapsedTime(&ms[v], e0, e1) == cudaSuccess &&
+             cudaGetLastError() == cudaSuccess;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (ok && ms[1] < 0.97f * ms[0]) choice = 1;  // keep the default unless clearly slower
+    if (!ok) cudaGetLastError();
+    cc.v[key] = choice;
+    return choice;
 }
 
 // Device tables of one grid (frequency grids, propagator, twiddles, potential
@@ -1259,16 +1337,18 @@ int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode, b
     float2 *tbs[2] = {ctx->tbuf.as<float2>(), overlap ? ctx->tbuf2.as<float2>() : ctx->tbuf.as<float2>()};
     const int *act = ctx->act.as<int>();
     const int nsl1 = b.nslices + 1;
-    CUtensorMap tmaps[2], pmap;
-    int st = column_map(ctx, &tmaps[0], tbs[0], gp.nx, gp.ny, ctx->units_alloc, cop);
+    ColView tmaps[2], pmap;
+    const int vm = col_variant(ctx, gp, kColMask), vp = col_variant(ctx, gp, kColProp);
+    int st = column_map(ctx, &tmaps[0], tbs[0], gp.nx, gp.ny, ctx->units_alloc, cop, vm);
     if (st) return st;
-    st = column_map(ctx, &tmaps[1], tbs[1], gp.nx, gp.ny, ctx->units_alloc, cop);
+    st = column_map(ctx, &tmaps[1], tbs[1], gp.nx, gp.ny, ctx->units_alloc, cop, vm);
     if (st) return st;
-    st = column_map(ctx, &pmap, psi, gp.nx, gp.ny, ctx->units_alloc, cop);
+    st = column_map(ctx, &pmap, psi, gp.nx, gp.ny, ctx->units_alloc, cop, vp);
     if (st) return st;
-    CUtensorMap smap;
+    ColView smap;
     if (dw) {
-        st = column_map(ctx, &smap, ctx->tbuf2.p, gp.nx, gp.ny, ctx->units_alloc, cop);
+        st = column_map(ctx, &smap, ctx->tbuf2.p, gp.nx, gp.ny, ctx->units_alloc, cop,
+                        col_variant(ctx, gp, kColDW));
         if (st) return st;
     }
     const double plane = (double)gp.nx * gp.ny;
@@ -1377,7 +1457,7 @@ void msk_destroy(msk_context *ctx)
                       &ctx->imgmeta, &ctx->wave0, &ctx->images, &ctx->exitw, &ctx->fresnel,
                       &ctx->flags, &ctx->pa_v, &ctx->pa_t, &ctx->pa_psi, &ctx->pa_e, &ctx->stk,
                       &ctx->stk_v, &ctx->stk_g, &ctx->stk_t, &ctx->stk_img, &ctx->stk_part,
-                      &ctx->adjtab, &ctx->arena, &ctx->dwbuf, &ctx->imgfill})
+                      &ctx->adjtab, &ctx->arena, &ctx->dwbuf, &ctx->imgfill, &ctx->tune})
         b->release();
     for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_join, ctx->ev_t[0], ctx->ev_t[1], ctx->ev_free[0],
                           ctx->ev_free[1]})
@@ -1694,10 +1774,11 @@ int tilt_series_impl(msk_context *ctx, const msk_series *s, int natom, const int
     ctx->units_alloc = B;
     st = flags_reset(ctx, gp.g);
     if (st) return st;
-    CUtensorMap pmap, tmap;
-    st = column_map(ctx, &pmap, ctx->psi.p, nx, ny, B, size_ops(nx));
+    ColView pmap, tmap;  // the free-space pass's views
+    const int vf = col_variant(ctx, gp, kColFresnel);
+    st = column_map(ctx, &pmap, ctx->psi.p, nx, ny, B, size_ops(nx), vf);
     if (st) return st;
-    st = column_map(ctx, &tmap, ctx->tbuf.p, nx, ny, B, size_ops(nx));
+    st = column_map(ctx, &tmap, ctx->tbuf.p, nx, ny, B, size_ops(nx), vf);
     if (st) return st;
 
     // thermal branches: Debye-Waller with one configuration, displacements
@@ -2107,14 +2188,19 @@ int stack_run(msk_context *ctx, const StackJob &J)
     MSK_CUDA(ctx, ctx->fresnel.reserve((adjoint ? 2 : 1) * pb));
 
     const SizeOps *rop = size_ops(ny), *cop = size_ops(nx);
-    // one tensor map per grid buffer the column passes touch
-    std::vector<CUtensorMap> maps(planes);
-    for (int i = 0; i < planes; i++) {
-        st = column_map(ctx, &maps[i], grid_at(i), nx, ny, B, cop);
-        if (st) return st;
+    // one view per grid buffer the column passes touch and tile variant
+    const int vmask = col_variant(ctx, gp, kColMask), vprop = col_variant(ctx, gp, kColProp),
+              vfres = col_variant(ctx, gp, kColFresnel);
+    std::vector<ColView> maps[2];
+    for (int v = 0; v < 2; v++) {
+        maps[v].resize(planes);
+        for (int i = 0; i < planes; i++) {
+            st = column_map(ctx, &maps[v][i], grid_at(i), nx, ny, B, cop, v);
+            if (st) return st;
+        }
     }
-    auto map_of = [&](const float2 *p) -> const CUtensorMap & {
-        return maps[(size_t)(p - base) / ((size_t)B * plane)];
+    auto map_of = [&](const float2 *p, int v) -> const ColView & {
+        return maps[v][(size_t)(p - base) / ((size_t)B * plane)];
     };
     const double P = (double)plane;
     const float tscale = 1.0f / ((float)ny * (float)ny);
@@ -2140,7 +2226,7 @@ int stack_run(msk_context *ctx, const StackJob &J)
                 rop->row_expv(g, nb, vslice(k), ustride, dst, ctx->stream);
             }
             Prof p(ctx, kKColMask, 16.0 * P * nb);
-            cop->col_mask(g, map_of(dst), map_of(dst), nullptr, nb, 1, ctx->stream);
+            cop->col_mask(g, map_of(dst, vmask), map_of(dst, vmask), nullptr, nb, 1, ctx->stream);
         };
         // P3 + P4 of one slice: out = W(K[p](iS(in) t))
         auto step = [&](const float2 *tb, const float2 *in, float2 *out) {
@@ -2149,7 +2235,8 @@ int stack_run(msk_context *ctx, const StackJob &J)
                 rop->row_transmit(g, nullptr, nb, tb, in, out, tscale, 1, ctx->stream);
             }
             Prof p(ctx, kKColProp, 16.0 * P * nb);
-            cop->col_prop(g, map_of(out), map_of(out), nullptr, nb, 1, ctx->stream);  // W0 in band
+            cop->col_prop(g, map_of(out, vprop), map_of(out, vprop), nullptr, nb, 1,
+                          ctx->stream);  // W0 in band
         };
 
         // the band-mode transmit stores only in-band row segments: every wave
@@ -2193,7 +2280,8 @@ int stack_run(msk_context *ctx, const StackJob &J)
             }
             {
                 Prof p(ctx, kFresnel, 16.0 * P * nb);
-                cop->col_fresnel(g, map_of(W), map_of(E), nullptr, nb, fr, 1.0f, ctx->stream);
+                cop->col_fresnel(g, map_of(W, vfres), map_of(E, vfres), nullptr, nb, fr, 1.0f,
+                                 ctx->stream);
             }
             if (!adjoint) {
                 // images[u][d] = |iS(E)|^2: one image per unit, no averaging
@@ -2230,7 +2318,7 @@ int stack_run(msk_context *ctx, const StackJob &J)
             }
             {
                 Prof p(ctx, kFresnel, 16.0 * P * nb);
-                cop->col_fresnel(g, map_of(E), map_of(d == 0 ? G : E), nullptr, nb, fc, 1.0f,
+                cop->col_fresnel(g, map_of(E, vfres), map_of(d == 0 ? G : E, vfres), nullptr, nb, fc, 1.0f,
                                  ctx->stream);
             }
             if (d > 0) {
@@ -2252,7 +2340,8 @@ int stack_run(msk_context *ctx, const StackJob &J)
                     const int k = k0 + j;
                     {
                         Prof p(ctx, kKColProp, 16.0 * P * nb);  // g_u = K[conj p] g_psi
-                        cop->col_prop(gc, map_of(G), map_of(G), nullptr, nb, 0, ctx->stream);
+                        cop->col_prop(gc, map_of(G, vprop), map_of(G, vprop), nullptr, nb, 0,
+                                      ctx->stream);
                     }
                     {
                         Prof p(ctx, kAdjTransmit, 40.0 * P * nb);
@@ -2261,7 +2350,7 @@ int stack_run(msk_context *ctx, const StackJob &J)
                     }
                     {
                         Prof p(ctx, kKColMask, 16.0 * P * nb);  // g_e = K[M] g_t
-                        cop->col_mask(g, map_of(Bb[j - 1]), map_of(Bb[j - 1]), nullptr, nb, 0,
+                        cop->col_mask(g, map_of(Bb[j - 1], vmask), map_of(Bb[j - 1], vmask), nullptr, nb, 0,
                                       ctx->stream);
                     }
                     Prof p(ctx, kGrad, 16.0 * P * nb);
@@ -2459,10 +2548,17 @@ int enqueue_specimen(msk_context *ctx, SpecPlan &P, unsigned char *arena, const 
     const int *act = reinterpret_cast<const int *>(arena + P.o_act);
     const int *soff = reinterpret_cast<const int *>(arena + P.o_soff);
     const SplatAtom *atoms = reinterpret_cast<const SplatAtom *>(arena + P.o_atoms);
-    CUtensorMap pmap, tmap;
-    int rc = column_map(ctx, &pmap, psi, nx, ny, na, cop);
+    // views for each pass's tile variant (chosen before any capture begins)
+    const int vm = col_variant(ctx, gp, kColMask), vp = col_variant(ctx, gp, kColProp),
+              vf = col_variant(ctx, gp, kColFresnel);
+    ColView pmap, tmap, pmapf, tmapf;
+    int rc = column_map(ctx, &pmap, psi, nx, ny, na, cop, vp);
     if (rc) return rc;
-    rc = column_map(ctx, &tmap, tb, nx, ny, na, cop);
+    rc = column_map(ctx, &tmap, tb, nx, ny, na, cop, vm);
+    if (rc) return rc;
+    rc = column_map(ctx, &pmapf, psi, nx, ny, na, cop, vf);
+    if (rc) return rc;
+    rc = column_map(ctx, &tmapf, tb, nx, ny, na, cop, vf);
     if (rc) return rc;
     const double pl = (double)plane;
     {
@@ -2514,7 +2610,7 @@ int enqueue_specimen(msk_context *ctx, SpecPlan &P, unsigned char *arena, const 
         }
         {
             Prof p(ctx, kFresnel, 16.0 * pl * na, st);
-            cop->col_fresnel(g, pmap, tmap, nullptr, na, fr, 1.0f, st);
+            cop->col_fresnel(g, pmapf, tmapf, nullptr, na, fr, 1.0f, st);
         }
         const int *dm = reinterpret_cast<const int *>(arena + P.o_meta) + (size_t)d * nmeta;
         Prof p(ctx, kIntensity, 12.0 * pl * na, st);
@@ -2692,6 +2788,10 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
             load[l] += P[i].work;
             lane_of[l].push_back(i);
         }
+        // the column tuner runs launches of its own: settle every choice first
+        for (int i = first; i < last; i++)
+            for (int mode : {(int)kColMask, (int)kColProp, (int)kColFresnel})
+                (void)col_variant(ctx, P[i].gp, mode);
         cudaGraph_t gr = nullptr;
         if (graph)
             MSK_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed));
@@ -2850,6 +2950,7 @@ extern "C" int msk_calculate_static(void *stream, float *pix, const float *wave0
     msk_context ctx;
     ctx.device = dev;
     ctx.stream = (cudaStream_t)stream;
+    ctx.no_tune = true;  // the tuner would allocate: the default column tiles
     unsigned char *base = static_cast<unsigned char *>(sc.ptr);
     auto view = [&](DevBuf &b, size_t off, size_t bytes) {
         b.p = base + off;

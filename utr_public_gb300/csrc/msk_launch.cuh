@@ -10,9 +10,16 @@
 
 namespace msk {
 
+// A column pass's view of a wave buffer: the TMA map (its box as wide as the
+// pass's column tile) and the tile variant it was encoded for.
+struct ColView {
+    CUtensorMap map;
+    int v;
+};
+
 struct SizeOps {
     int n;
-    int col_c, col_box_rows;  // column tile width and TMA box height for line length n
+    int col_c[2], col_box_rows;  // column tile widths (per variant), TMA box height
     void (*splat)(const Geom &, const int *units, int nunits, int slice, int nsl1,
                   const int *slice_off, const SplatAtom *atoms, float2 *tbuf, cudaStream_t);
     // the same splat writing the projected potential of the slice (float) to
@@ -24,17 +31,17 @@ struct SizeOps {
     // (in place), then A = S(exp(i sigma v')) into `tbuf`
     void (*splat_spec)(const Geom &, const int *units, int nunits, int slice, int nsl1,
                        const int *slice_off, const SplatAtom *atoms, float2 *spec, cudaStream_t);
-    void (*col_dw)(const Geom &, const CUtensorMap &spec, const int *units, int nunits,
+    void (*col_dw)(const Geom &, const ColView &spec, const int *units, int nunits,
                    const float *dw, int dw_stride, cudaStream_t);
     void (*row_dwexp)(const Geom &, const int *units, int nunits, const float2 *spec,
                       float2 *tbuf, cudaStream_t);
     // band != 0: only the in-band column blocks (Geom::cb_*); the others must
     // be zero in the input and stay zero in the output buffer
-    void (*col_mask)(const Geom &, const CUtensorMap &in, const CUtensorMap &out,
+    void (*col_mask)(const Geom &, const ColView &in, const ColView &out,
                      const int *units, int nunits, int band, cudaStream_t);
-    void (*col_prop)(const Geom &, const CUtensorMap &in, const CUtensorMap &out,
+    void (*col_prop)(const Geom &, const ColView &in, const ColView &out,
                      const int *units, int nunits, int band, cudaStream_t);
-    void (*col_fresnel)(const Geom &, const CUtensorMap &in, const CUtensorMap &out,
+    void (*col_fresnel)(const Geom &, const ColView &in, const ColView &out,
                         const int *units, int nunits, const Fresnel &, float scale, cudaStream_t);
     // band != 0: only the in-band row segments are loaded and stored (B and
     // W must be zero out of band, and `out` too; a propagator pass follows)
@@ -71,7 +78,7 @@ template <int N> struct Smem {
     static constexpr int NTS = RowCfg<N>::L * P::T;
     static constexpr size_t splat = (size_t)RowCfg<N>::L * P::PADN * 8 + NTS * 16 + 128 * 4 +
                                     ((NTS + 31) / 32 + 1) * 4;
-    static constexpr size_t col = (size_t)ColCfg<N>::C * P::PADN * 8 + 16;
+    template <int V> static constexpr size_t col() { return (size_t)ColCfg<N, V>::C * P::PADN * 8 + 16; }
     static constexpr size_t transmit = (size_t)2 * RowCfg<N>::LT * P::PADN * 8 + 16;
     static constexpr size_t row = (size_t)RowCfg<N>::L * P::PADN * 8;
     static constexpr size_t adj = (size_t)RowCfg<N>::LT * (P::PADN + N) * 8;
@@ -133,29 +140,40 @@ struct Launch {
         k_row_dwexp<N><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::row, s>>>(g, units, spec,
                                                                                 tbuf);
     }
-    template <int MODE>
-    static void col(const Geom &g, const CUtensorMap &in, const CUtensorMap &out,
-                    const int *units, int nunits, const Fresnel &fr, float scale, int band,
-                    cudaStream_t s)
+    template <int MODE, int V>
+    static void colv(const Geom &g, const CUtensorMap &in, const CUtensorMap &out,
+                     const int *units, int nunits, const Fresnel &fr, float scale, int band,
+                     cudaStream_t s)
     {
         static std::once_flag f;
-        set_smem(k_col_pass<N, MODE>, Smem<N>::col, f);
-        const int C = ColCfg<N>::C;
-        const int bpu = band ? g.cb_n : g.ny / C;
-        k_col_pass<N, MODE><<<nunits * bpu, ColCfg<N>::NT, Smem<N>::col, s>>>(
+        set_smem(k_col_pass<N, MODE, V>, Smem<N>::template col<V>(), f);
+        const int C = ColCfg<N, V>::C;
+        const int bpu = band ? g.cb_n[V] : g.ny / C;
+        k_col_pass<N, MODE, V><<<nunits * bpu, ColCfg<N, V>::NT, Smem<N>::template col<V>(), s>>>(
             g, in, out, units, fr, scale, band);
     }
-    static void col_mask(const Geom &g, const CUtensorMap &in, const CUtensorMap &out,
+    // in and out must be views of the same tile variant (the kernel's box)
+    template <int MODE>
+    static void col(const Geom &g, const ColView &in, const ColView &out, const int *units,
+                    int nunits, const Fresnel &fr, float scale, int band, cudaStream_t s)
+    {
+        if (in.v != out.v) return;
+        if (in.v == 1)
+            colv<MODE, 1>(g, in.map, out.map, units, nunits, fr, scale, band, s);
+        else
+            colv<MODE, 0>(g, in.map, out.map, units, nunits, fr, scale, band, s);
+    }
+    static void col_mask(const Geom &g, const ColView &in, const ColView &out,
                          const int *units, int nunits, int band, cudaStream_t s)
     {
         col<kColMask>(g, in, out, units, nunits, Fresnel{}, 1.0f / (float)g.nx, band, s);
     }
-    static void col_prop(const Geom &g, const CUtensorMap &in, const CUtensorMap &out,
+    static void col_prop(const Geom &g, const ColView &in, const ColView &out,
                          const int *units, int nunits, int band, cudaStream_t s)
     {
         col<kColProp>(g, in, out, units, nunits, Fresnel{}, 1.0f / (float)g.nx, band, s);
     }
-    static void col_dw(const Geom &g, const CUtensorMap &spec, const int *units, int nunits,
+    static void col_dw(const Geom &g, const ColView &spec, const int *units, int nunits,
                        const float *dw, int dw_stride, cudaStream_t s)
     {
         Fresnel fr{};
@@ -163,7 +181,7 @@ struct Launch {
         fr.dw_stride = dw_stride;
         col<kColDW>(g, spec, spec, units, nunits, fr, 1.0f / (float)g.nx, 0, s);
     }
-    static void col_fresnel(const Geom &g, const CUtensorMap &in, const CUtensorMap &out,
+    static void col_fresnel(const Geom &g, const ColView &in, const ColView &out,
                             const int *units, int nunits, const Fresnel &fr, float scale,
                             cudaStream_t s)
     {
@@ -256,7 +274,7 @@ struct Launch {
 
     static const SizeOps *ops()
     {
-        static const SizeOps o = {N,        ColCfg<N>::C, ColCfg<N>::BR,    splat,
+        static const SizeOps o = {N,        {ColCfg<N, 0>::C, ColCfg<N, 1>::C}, ColCfg<N>::BR, splat,
                                   splat_potential, splat_spec, col_dw, row_dwexp,
                                   col_mask, col_prop,     col_fresnel,      row_transmit,
                                   row_init, row_exit,     row_inverse, row_intensity, row_expv,

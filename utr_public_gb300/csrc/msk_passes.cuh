@@ -83,9 +83,13 @@ template <int NY> struct RowCfg {
     static constexpr bool BLK = T > 32;
 };
 // Columns per CTA for the column passes, and the TMA boxes of a column tile.
-template <int NX> struct ColCfg {
+// Two widths per line length, chosen per pass at run time by timing both
+// (the column tuner of the host code): V = 0 the width that gives a 128-thread
+// CTA (clamped to 2..16), V = 1 half of it, or twice where half would be < 2.
+template <int NX, int V = 0> struct ColCfg {
     static constexpr int T = FftPlan<NX>::T;
-    static constexpr int C = (128 / T) < 2 ? 2 : ((128 / T) > 16 ? 16 : 128 / T);
+    static constexpr int C0 = (128 / T) < 2 ? 2 : ((128 / T) > 16 ? 16 : 128 / T);
+    static constexpr int C = V == 0 ? C0 : (C0 / 2 >= 2 ? C0 / 2 : 2 * C0);
     static constexpr int NT = C * T;
     static constexpr int BR = NX < 256 ? NX : 256;  // rows per box (TMA boxes are <= 256)
     static constexpr int NBOX = NX / BR;
@@ -113,8 +117,8 @@ __device__ __forceinline__ void cta_drain(uint64_t *bar, uint32_t parity)
 // Resident CTAs per SM the column pass is compiled for (its register budget):
 // the propagator pass fits 128 registers, the band-limit and free-space
 // passes need ~168 to stay free of spills at 1024 points.
-template <int NX, int MODE> struct ColMinBlocks {
-    static constexpr int per = (MODE == 1 ? 512 : 384) / ColCfg<NX>::NT;
+template <int NX, int MODE, int V> struct ColMinBlocks {
+    static constexpr int per = (MODE == 1 ? 512 : 384) / ColCfg<NX, V>::NT;
     static constexpr int value = per > 0 ? per : 1;
 };
 
@@ -290,14 +294,14 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
 //           spectrum (autoslic.cpp:1098-1106), -B/4 per unit in fr.dw
 enum { kColMask = 0, kColProp = 1, kColFresnel = 2, kColDW = 3 };
 
-template <int NX, int MODE>
-__global__ void __launch_bounds__(ColCfg<NX>::NT, ColMinBlocks<NX, MODE>::value)
+template <int NX, int MODE, int V>
+__global__ void __launch_bounds__(ColCfg<NX, V>::NT, ColMinBlocks<NX, MODE, V>::value)
 k_col_pass(const Geom g, const __grid_constant__ CUtensorMap in_map,
            const __grid_constant__ CUtensorMap out_map, const int *__restrict__ units,
            const Fresnel fr, float fscale, int band)
 {
     using P = FftPlan<NX>;
-    using CC = ColCfg<NX>;
+    using CC = ColCfg<NX, V>;
     constexpr int T = P::T, E = P::E, C = CC::C;
     extern __shared__ __align__(128) unsigned char smem[];
     float2 *buf = reinterpret_cast<float2 *>(smem);                       // PADN*C
@@ -307,10 +311,10 @@ k_col_pass(const Geom g, const __grid_constant__ CUtensorMap in_map,
     const int ny = g.ny;
     // band mode: only the column blocks that hold in-band columns (the others
     // are zero on input and output)
-    const int bpu = band ? g.cb_n : ny / C;
+    const int bpu = band ? g.cb_n[V] : ny / C;
     const int u = units ? units[blockIdx.x / bpu] : (int)(blockIdx.x / bpu);
     int cb = blockIdx.x % bpu;
-    if (band && cb >= g.cb_lo) cb = g.cb_hi0 + (cb - g.cb_lo);
+    if (band && cb >= g.cb_lo[V]) cb = g.cb_hi0[V] + (cb - g.cb_lo[V]);
     const int iy = cb * C + c;
     // tile = rows u*NX .. u*NX+NX-1, float columns 2*cb*C .. 2*cb*C+2C-1
     if (tid == 0) {

@@ -28,9 +28,10 @@ struct Geom {
     // Columns iy with ky2[iy] >= k2max are zeroed whole by the band limit and
     // by the propagator: in band <=> iy <= band_p or iy >= band_q.  Column
     // passes in band mode run only the column blocks [0, cb_lo) and
-    // [cb_hi0, ny/C) (C columns per block); cb_n blocks per unit.
+    // [cb_hi0, ny/C) (C columns per block); cb_n blocks per unit; one set per
+    // column-tile variant.
     int band_p, band_q;
-    int cb_lo, cb_hi0, cb_n;
+    int cb_lo[2], cb_hi0[2], cb_n[2];
     // Row segments [0, seg_e1) and [seg_s2, ny) with even bounds that cover
     // the in-band columns: what a band-mode row pass loads and stores.
     int seg_e1, seg_s2;
