@@ -81,6 +81,9 @@ template <int NY> struct RowCfg {
     static constexpr int L = (256 / T) > 0 ? 256 / T : 1;   // P1 and the row utilities
     static constexpr int LT = (128 / T) > 0 ? 128 / T : 1;  // P3 (two tiles in flight)
     static constexpr bool BLK = T > 32;
+    // resident CTAs per SM the latency-bound utilities are compiled for
+    // (80 registers a thread at 256 threads); fewer where that would spill
+    static constexpr int MB = NY <= 1024 ? 3 : 2;
 };
 // Columns per CTA for the column passes, and the TMA boxes of a column tile.
 // Two widths per line length, chosen per pass at run time by timing both
@@ -564,7 +567,7 @@ k_row_intensity(const Geom g, const int *__restrict__ img_off, const int *__rest
 // A = S(exp(i sigma v)), the transmission before its band limit.  `v` points
 // at slice k of unit 0; units are `ustride` floats apart.
 template <int NY>
-__global__ void __launch_bounds__(RowCfg<NY>::L * FftPlan<NY>::T)
+__global__ void __launch_bounds__(RowCfg<NY>::L * FftPlan<NY>::T, RowCfg<NY>::MB)
 k_row_expv(const Geom g, const float *__restrict__ v, size_t ustride, float2 *__restrict__ out)
 {
     using P = FftPlan<NY>;
@@ -577,8 +580,7 @@ k_row_expv(const Geom g, const float *__restrict__ v, size_t ustride, float2 *__
     const int bpu = (nx + L - 1) / L;
     const int u = blockIdx.x / bpu;
     const int ix = (blockIdx.x % bpu) * L + l;
-    const bool row_ok = ix < nx;
-    const float *src = v + (size_t)u * ustride + (size_t)(row_ok ? ix : 0) * NY;
+    const float *src = v + (size_t)u * ustride + (size_t)(ix < nx ? ix : 0) * NY;
     float2 w[E];
 #pragma unroll
     for (int m = 0; m < E; m++) {
@@ -587,7 +589,7 @@ k_row_expv(const Geom g, const float *__restrict__ v, size_t ustride, float2 *__
         if (__any_sync(0xffffffffu, ph != 0.0f)) w[m] = expi(ph);
     }
     fft_line<NY, false, 1, BLK>(w, s_lines + l * P::PADN, 0, t, g.tw_row);
-    if (row_ok) {  // out-of-band columns as zeros: the band limit zeroes them
+    if (ix < nx) {  // out-of-band columns as zeros: the band limit zeroes them
         float2 *dst = out + ((size_t)u * nx + ix) * NY;
 #pragma unroll
         for (int m = 0; m < E; m++)
@@ -690,7 +692,7 @@ k_row_adj_transmit(const Geom g, float2 *Gu, float2 *B, const float2 *__restrict
 // Ge = W(g_e).  `v` and `grad` point at slice k of unit 0, units `ustride`
 // floats apart.
 template <int NY>
-__global__ void __launch_bounds__(RowCfg<NY>::L * FftPlan<NY>::T)
+__global__ void __launch_bounds__(RowCfg<NY>::L * FftPlan<NY>::T, RowCfg<NY>::MB)
 k_row_grad(const Geom g, const float2 *__restrict__ Ge, const float *__restrict__ v,
            size_t ustride, float *__restrict__ grad)
 {
