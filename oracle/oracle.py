@@ -8,6 +8,8 @@ shipped package never imports it.
   reference's hot path (msk_oracle.c): FP32 mirror and FP64 oracle.
 * ``Reference`` wraps ``oracle/_ref/libautoslic_ref.so``, the reference's own
   TemsimLibrary sources compiled here (only where the reference tree exists).
+* ``UtrReference`` wraps ``oracle/_ref/libutr_ref.so``, the reference's own
+  PhaseRetrieval/UTR.h templates compiled here.
 """
 import ctypes as C
 import os
@@ -18,6 +20,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_ORACLE = os.path.join(HERE, "liboracle.so")
 LIB_REF = os.path.join(HERE, "_ref", "libautoslic_ref.so")
+LIB_UTR_REF = os.path.join(HERE, "_ref", "libutr_ref.so")
 REF_TREE = "/root/reference"
 
 # param[] offsets (slicelib.hpp:142-240)
@@ -68,6 +71,29 @@ class StackParams(C.Structure):
                 ("cs3", C.c_double), ("cs5", C.c_double)]
 
 
+class UtrParams(C.Structure):
+    """msk_utr (include/msk_utr.h): UTR.exe's reconstruction parameters."""
+    _fields_ = [("modality", C.c_int), ("f1", C.c_double), ("f2", C.c_double),
+                ("nx", C.c_int), ("ny", C.c_int), ("xst", C.c_double), ("zlo", C.c_double),
+                ("zhi", C.c_double), ("dzextra", C.c_double), ("dxc", C.c_double),
+                ("dyc", C.c_double), ("dzc", C.c_double), ("wl", C.c_double),
+                ("aobj", C.c_double), ("cs3", C.c_double), ("cs5", C.c_double),
+                ("ctf_mode", C.c_int), ("escc", C.c_int), ("asigma", C.c_double),
+                ("nsr", C.c_double), ("epsilon", C.c_double), ("inv_laplace", C.c_int)]
+
+
+class UtrGeom(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int)] + \
+        [(n, C.c_double) for n in ("xst", "xlo", "xhi", "ylo", "yhi", "zlo", "zhi", "fxst", "fyst",
+                                   "fzst", "fxlo", "fylo", "fzlo", "xc", "yc", "zc")] + \
+        [("ic", C.c_long), ("jc", C.c_long), ("kc", C.c_long)] + \
+        [(n, C.c_double) for n in ("wl", "ee", "k2maxo", "cs3", "cs5", "zout_aver")] + \
+        [("rot_y_only", C.c_int), ("rot_z_only", C.c_int), ("rot_z2_only", C.c_int)]
+
+
+_GRID_ARGS = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double] + [C.c_float] * 6
+
+
 class Oracle:
     def __init__(self, path=LIB_ORACLE):
         if not os.path.exists(path):
@@ -115,6 +141,25 @@ class Oracle:
         L.mo_orientations_f32.argtypes = [C.POINTER(SeriesParams), C.c_int, C.c_int, C.c_int,
                                           C.c_long, _ip, _fp, _fp, _fp, _fp, _dp, _dp, C.c_int,
                                           _dp, _fp]
+        # UTR reconstruction
+        L.mo_utr_geom_make.argtypes = [C.POINTER(UtrParams), C.c_int, _dp, _dp,
+                                       C.POINTER(UtrGeom)]
+        L.mo_utr_k2four_f32.argtypes = [_fp, C.c_int, C.c_int, C.c_double, C.c_double, _fp]
+        L.mo_utr_k2four_f64.argtypes = [_fp, C.c_int, C.c_int, C.c_double, C.c_double, _dp]
+        L.mo_utr_grid_f32.argtypes = [_fp] + _GRID_ARGS + [_fp, C.c_double, C.c_int, C.c_int,
+                                                            _fp, _fp]
+        L.mo_utr_grid_acc64.argtypes = [_fp] + _GRID_ARGS + [_fp, C.c_double, C.c_int, C.c_int,
+                                                              _dp, _dp]
+        L.mo_utr_grid_f64.argtypes = [_dp] + _GRID_ARGS + [_dp, C.c_double, C.c_int, C.c_int,
+                                                            _dp, _dp]
+        for nm, T in (("mo_utr_ctf3d_f32", _fp), ("mo_utr_ctf3d_f64", _dp)):
+            getattr(L, nm).argtypes = [T, C.c_int, C.c_int, C.c_int] + [C.c_double] * 13 + \
+                [C.c_int]
+        for nm, T in (("mo_utr_invlap3d_f32", _fp), ("mo_utr_invlap3d_f64", _dp)):
+            getattr(L, nm).argtypes = [T, C.c_int, C.c_int, C.c_int] + [C.c_double] * 5
+        L.mo_utr_reconstruct_f64.argtypes = [C.POINTER(UtrParams), C.c_int, _dp, _dp, _fp, _dp,
+                                             C.c_int]
+        L.mo_utr_finish_f64.argtypes = [C.POINTER(UtrParams), C.c_int, _dp, _dp, _dp, _dp, _dp]
 
     # -- physics
     def wavelength(self, kev):
@@ -312,6 +357,118 @@ class Oracle:
         return imgs.reshape(nunits, len(defoci), sp.nx, sp.ny)
 
 
+    # -- UTR reconstruction
+    def utr_geom(self, p, angles, defocus):
+        g = UtrGeom()
+        ang = np.ascontiguousarray(angles, np.float64).reshape(-1)
+        st = self.L.mo_utr_geom_make(C.byref(p), len(ang) // 2, ang,
+                                     np.ascontiguousarray(defocus, np.float64), C.byref(g))
+        if st:
+            raise ValueError("bad UTR parameters")
+        return g
+
+    def utr_k2four(self, img, f1=1.0, f2=0.0, f64=True):
+        img = np.ascontiguousarray(img, np.float32)
+        ny, nx = img.shape
+        if f64:
+            out = np.zeros((ny, nx, 2), np.float64)
+            self.L.mo_utr_k2four_f64(img, nx, ny, f1, f2, out)
+        else:
+            out = np.zeros((ny, nx, 2), np.float32)
+            self.L.mo_utr_k2four_f32(img, nx, ny, f1, f2, out)
+        return out
+
+    def utr_grid(self, k2four, nz, angleY, angleZ, fx, fc, wl, rotshift, escc, mode="f32",
+                 v3=None, samp3=None):
+        """One image into (v3, samp3); fx = (fxlo, fxst, fylo, fyst, fzlo, fzst) as floats;
+        mode "f32" (float sums), "acc64" (float products, double sums) or "f64"
+        (double spectrum and phase; fc = the three imaginary parts)."""
+        ny, nx = k2four.shape[:2]
+        T = np.float32 if mode == "f32" else np.float64
+        if v3 is None:
+            v3 = np.zeros((nz, ny, nx, 2), T)
+            samp3 = np.zeros((nz, ny, nx), T)
+        fn = {"f32": self.L.mo_utr_grid_f32, "acc64": self.L.mo_utr_grid_acc64,
+              "f64": self.L.mo_utr_grid_f64}[mode]
+        kt = np.float64 if mode == "f64" else np.float32
+        fn(np.ascontiguousarray(k2four, kt), nx, ny, nz, angleY, angleZ, *[float(v) for v in fx],
+           np.ascontiguousarray(fc, kt), wl, int(rotshift), int(escc), v3, samp3)
+        return v3, samp3
+
+    def utr_ctf3d(self, v3, wl, box, defocdist, q2max, cs3, cs5, sigma, epsilon, escc):
+        """box = (zlo, zhi, ylo, yhi, xlo, xhi); v3 [nz][ny][nx][2], changed in place."""
+        nz, ny, nx = v3.shape[:3]
+        fn = self.L.mo_utr_ctf3d_f32 if v3.dtype == np.float32 else self.L.mo_utr_ctf3d_f64
+        if fn(v3, nx, ny, nz, wl, *box, defocdist, q2max, cs3, cs5, sigma, epsilon, int(escc)):
+            raise ValueError("CTFcorrection3D: bad sizes or evanescent waves")
+        return v3
+
+    def utr_invlap3d(self, v3, zaper, yaper, xaper, alpha, norm):
+        nz, ny, nx = v3.shape[:3]
+        fn = self.L.mo_utr_invlap3d_f32 if v3.dtype == np.float32 else self.L.mo_utr_invlap3d_f64
+        if fn(v3, nx, ny, nz, zaper, yaper, xaper, alpha, norm):
+            raise ValueError("InverseMLaplacian3D: bad arguments")
+        return v3
+
+    def utr_reconstruct(self, p, angles, defocus, images, nthreads=1):
+        g = self.utr_geom(p, angles, defocus)
+        vol = np.zeros((g.nz, p.ny, p.nx), np.float64)
+        ang = np.ascontiguousarray(angles, np.float64).reshape(-1)
+        st = self.L.mo_utr_reconstruct_f64(C.byref(p), len(ang) // 2, ang,
+                                           np.ascontiguousarray(defocus, np.float64),
+                                           np.ascontiguousarray(images, np.float32), vol,
+                                           nthreads)
+        if st:
+            raise ValueError("oracle reconstruction failed")
+        return vol
+
+    def utr_finish(self, p, angles, defocus, v3, samp3):
+        g = self.utr_geom(p, angles, defocus)
+        vol = np.zeros((g.nz, p.ny, p.nx), np.float64)
+        ang = np.ascontiguousarray(angles, np.float64).reshape(-1)
+        v = np.array(v3, np.float64)
+        if self.L.mo_utr_finish_f64(C.byref(p), len(ang) // 2, ang,
+                                    np.ascontiguousarray(defocus, np.float64), v,
+                                    np.ascontiguousarray(samp3, np.float64), vol):
+            raise ValueError("oracle finish failed")
+        return vol
+
+
+class UtrReference:
+    """The reference's own PhaseRetrieval/UTR.h templates compiled here (oracle/_ref)."""
+
+    def __init__(self, path=LIB_UTR_REF):
+        L = C.CDLL(path)
+        self.L = L
+        L.ref_utr_grid_f.argtypes = [_fp] + _GRID_ARGS + [_fp, C.c_double, C.c_int, C.c_int,
+                                                           _fp, _fp]
+        L.ref_utr_ctf3d_f.argtypes = [_fp, C.c_int, C.c_int, C.c_int] + [C.c_double] * 13 + \
+            [C.c_int]
+        L.ref_utr_invlap3d_f.argtypes = [_fp, C.c_int, C.c_int, C.c_int] + [C.c_double] * 5
+
+    def grid(self, k2four, nz, angleY, angleZ, fx, fc, wl, rotshift, escc, v3=None, samp3=None):
+        ny, nx = k2four.shape[:2]
+        if v3 is None:
+            v3 = np.zeros((nz, ny, nx, 2), np.float32)
+            samp3 = np.zeros((nz, ny, nx), np.float32)
+        self.L.ref_utr_grid_f(np.ascontiguousarray(k2four, np.float32), nx, ny, nz, angleY,
+                              angleZ, *[float(v) for v in fx],
+                              np.ascontiguousarray(fc, np.float32), wl, int(rotshift),
+                              int(escc), v3, samp3)
+        return v3, samp3
+
+    def ctf3d(self, v3, wl, box, defocdist, q2max, cs3, cs5, sigma, epsilon, escc):
+        nz, ny, nx = v3.shape[:3]
+        self.L.ref_utr_ctf3d_f(v3, nx, ny, nz, wl, *box, defocdist, q2max, cs3, cs5, sigma,
+                               epsilon, int(escc))
+        return v3
+
+    def invlap3d(self, v3, zaper, yaper, xaper, alpha, norm):
+        nz, ny, nx = v3.shape[:3]
+        self.L.ref_utr_invlap3d_f(v3, nx, ny, nz, zaper, yaper, xaper, alpha, norm)
+        return v3
+
+
 class Reference:
     """The reference's own code compiled here (oracle/_ref)."""
 
@@ -372,3 +529,7 @@ class Reference:
 
 def reference_available():
     return os.path.exists(LIB_REF)
+
+
+def utr_reference_available():
+    return os.path.exists(LIB_UTR_REF)

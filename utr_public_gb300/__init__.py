@@ -29,7 +29,8 @@ EXPORTS = ("msk_create", "msk_destroy", "msk_last_error", "msk_status_string", "
            "msk_profile_read", "msk_calculate_static", "msk_tilt_series_per_angle",
            "msk_stack_images", "msk_adjoint", "msk_potential_stack", "msk_tilt_series_batch",
            "msk_write_grd", "msk_write_grc", "msk_write_tiff32", "msk_read_orientations",
-           "msk_tilt_series_planes")
+           "msk_tilt_series_planes", "msk_utr_depth", "msk_utr_reconstruct", "msk_utr_grid",
+           "msk_utr_ctf_correction3d", "msk_utr_inverse_mlaplacian3d")
 MSK_BATCH_GRAPH = 1
 
 
@@ -49,6 +50,28 @@ class Series(C.Structure):
                 ("max_batch", C.c_int), ("lwobble", C.c_int), ("temperature", C.c_float),
                 ("wobble", C.c_void_p), ("seed", C.c_long), ("R1", C.c_double),
                 ("rotation", C.c_void_p), ("xshift", C.c_double), ("yshift", C.c_double)]
+
+
+class Utr(C.Structure):
+    """msk_utr (include/msk_utr.h): UTR.exe's reconstruction parameters, in the
+    units of its ".txt" parameter file (ReadmeUTR.txt; bracketed: its lines).
+    modality [1], f1 f2 [7], nx ny [8], xst [9], zlo zhi dzextra [10],
+    dxc dyc dzc [11], wl [12], aobj (mrad) [13], cs3 cs5 (mm) [14],
+    ctf_mode (0, 2 or 4) [15], escc [16], asigma [17], nsr [18], epsilon [19],
+    inv_laplace [22]."""
+    _fields_ = [("modality", C.c_int), ("f1", C.c_double), ("f2", C.c_double),
+                ("nx", C.c_int), ("ny", C.c_int), ("xst", C.c_double), ("zlo", C.c_double),
+                ("zhi", C.c_double), ("dzextra", C.c_double), ("dxc", C.c_double),
+                ("dyc", C.c_double), ("dzc", C.c_double), ("wl", C.c_double),
+                ("aobj", C.c_double), ("cs3", C.c_double), ("cs5", C.c_double),
+                ("ctf_mode", C.c_int), ("escc", C.c_int), ("asigma", C.c_double),
+                ("nsr", C.c_double), ("epsilon", C.c_double), ("inv_laplace", C.c_int)]
+
+    def __init__(self, **kw):
+        super().__init__()
+        self.f1 = 1.0
+        for k, v in kw.items():
+            setattr(self, k, v)
 
 
 class Stack(C.Structure):
@@ -141,6 +164,13 @@ def load():
     L.msk_write_tiff32.argtypes = [C.c_char_p, _fp, C.c_int, C.c_int]
     L.msk_read_orientations.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), vp,
                                         vp, vp, vp]
+    L.msk_utr_depth.argtypes = [C.POINTER(Utr)]
+    L.msk_utr_reconstruct.argtypes = [vp, C.POINTER(Utr), C.c_int, _dp, _dp, vp, vp]
+    L.msk_utr_grid.argtypes = [vp, C.POINTER(Utr), C.c_int, _dp, vp, vp, vp]
+    L.msk_utr_ctf_correction3d.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int] + \
+        [C.c_double] * 13 + [C.c_int]
+    L.msk_utr_inverse_mlaplacian3d.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int] + \
+        [C.c_double] * 5
     _lib = L
     return L
 
@@ -445,6 +475,62 @@ class Context:
                                       _ptr(defocus), _ptr(target), _ptr(grad), C.byref(loss))
         self._check(st)
         return loss.value, grad
+
+    # -- UTR reconstruction (include/msk_utr.h)
+    def utr_depth(self, utr):
+        nz = self.L.msk_utr_depth(C.byref(utr))
+        if nz < 0:
+            raise MskError(nz, "bad UTR geometry")
+        return nz
+
+    def utr_reconstruct(self, utr, angles, defocus, images, volume=None):
+        """3D potential (TEM) or beta (X-ray) [nz, ny, nx] from one defocused
+        image per orientation (msk_utr_reconstruct).  angles [nangles, 2]: Z
+        and Y' rotations in degrees; defocus [nangles]; images [nangles, ny,
+        nx] (x fastest, flat-field corrected); images / volume may be torch
+        CUDA tensors."""
+        ang = np.ascontiguousarray(angles, np.float64).reshape(-1, 2)
+        defocus = np.ascontiguousarray(defocus, np.float64)
+        images = self._f32(images)
+        if volume is None:
+            volume = np.zeros((self.utr_depth(utr), utr.ny, utr.nx), np.float32)
+        st = self.L.msk_utr_reconstruct(self.h, C.byref(utr), len(ang), ang.reshape(-1),
+                                        defocus, _ptr(images), _ptr(volume))
+        self._check(st)
+        return volume
+
+    def utr_grid(self, utr, angles, k2four, v3=None, samp3=None):
+        """CT_3Dgridding of centred spectra k2four [nangles, ny, nx, 2] into a
+        zeroed volume (msk_utr_grid): (v3 [nz, ny, nx, 2], samp3 [nz, ny, nx])."""
+        ang = np.ascontiguousarray(angles, np.float64).reshape(-1, 2)
+        k2four = self._f32(k2four)
+        nz = self.utr_depth(utr)
+        if v3 is None:
+            v3 = np.zeros((nz, utr.ny, utr.nx, 2), np.float32)
+        if samp3 is None:
+            samp3 = np.zeros((nz, utr.ny, utr.nx), np.float32)
+        st = self.L.msk_utr_grid(self.h, C.byref(utr), len(ang), ang.reshape(-1), _ptr(k2four),
+                                 _ptr(v3), _ptr(samp3))
+        self._check(st)
+        return v3, samp3
+
+    def utr_ctf_correction3d(self, v3, wl, box, defocdist, q2max, cs3, cs5, sigma, epsilon,
+                             escc):
+        """CTFcorrection3D on a centred complex volume [nz, ny, nx, 2], in place;
+        box = (zlo, zhi, ylo, yhi, xlo, xhi), cs in length units."""
+        nz, ny, nx = v3.shape[:3]
+        st = self.L.msk_utr_ctf_correction3d(self.h, _ptr(v3), nx, ny, nz, wl, *box, defocdist,
+                                             q2max, cs3, cs5, sigma, epsilon, int(escc))
+        self._check(st)
+        return v3
+
+    def utr_inverse_mlaplacian3d(self, v3, zaper, yaper, xaper, alpha, norm):
+        """InverseMLaplacian3D on a centred complex volume [nz, ny, nx, 2], in place."""
+        nz, ny, nx = v3.shape[:3]
+        st = self.L.msk_utr_inverse_mlaplacian3d(self.h, _ptr(v3), nx, ny, nz, zaper, yaper,
+                                                 xaper, alpha, norm)
+        self._check(st)
+        return v3
 
     def tilt_series_planes(self, series, Znum, x, y, z, occ, angleZ, angleY, planes,
                            shifts=None, nconfig=1, displacements=None, images=None,

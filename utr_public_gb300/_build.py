@@ -38,7 +38,7 @@ def _sources():
 
 def _deps():
     return (glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h")) +
-            glob.glob(os.path.join(CSRC, "*.inc")) + [os.path.join(ROOT, "include", "msk.h")])
+            glob.glob(os.path.join(CSRC, "*.inc")) + glob.glob(os.path.join(ROOT, "include", "*.h")))
 
 
 def _stale(target, inputs):

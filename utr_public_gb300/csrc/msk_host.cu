@@ -23,6 +23,7 @@
 #include <dlfcn.h>
 
 #include "msk.h"
+#include "msk_ctx.h"
 #include "msk_launch.cuh"
 
 namespace msk {
@@ -609,7 +610,7 @@ static void twiddles_n(std::vector<float2> &out)
     if (P::S == 3) fill(P::TW2, P::NS3, P::R3);
 }
 
-static bool twiddles(int n, std::vector<float2> &out)
+bool twiddles(int n, std::vector<float2> &out)
 {
     switch (n) {
     case 16: twiddles_n<16>(out); return true;
@@ -841,94 +842,23 @@ static void spherical_wave(int nx, int ny, float ctblength, float v0, double R1,
 
 using namespace msk;
 
-namespace {
-
-struct DevBuf {
-    void *p = nullptr;
-    size_t cap = 0;
-    cudaError_t reserve(size_t bytes)
-    {
-        if (bytes <= cap) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-        cudaError_t e = cudaMalloc(&p, bytes);
-        if (e == cudaSuccess) cap = bytes;
-        return e;
-    }
-    template <typename T> T *as() const { return reinterpret_cast<T *>(p); }
-    void release()
-    {
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-    }
-};
-
-}  // namespace
-
-// Kinds of launches for the per-kernel accounting (msk_profile).
-enum Kind {
-    kSplat, kKColMask, kTransmit, kKColProp, kFresnel, kIntensity, kExit, kInit, kPlane, kFresTab,
-    kExpv, kAdjTransmit, kGrad, kImGrad, kAccum, kDW, kDWExp, kRotShift,
-    kKinds
-};
-static const char *const kKindName[kKinds] = {
+namespace msk {
+const char *const kKindName[kKinds] = {
     "row_splat", "col_bandlimit", "row_transmit", "col_propagate", "col_fresnel",
     "row_intensity", "row_exit", "row_init", "plane_init", "fresnel_table",
     "row_expv", "row_adj_transmit", "row_grad", "row_imgrad", "accumulate", "col_debye_waller",
-    "row_dw_phase", "image_rotate_shift"};
+    "row_dw_phase", "image_rotate_shift",
+    "utr_image_rows", "utr_image_cols", "utr_grid", "utr_fourier_rows", "utr_volume_cols",
+    "utr_final_cols", "utr_pointwise"};
+}  // namespace msk
 
-struct ProfRec {
-    int kind;
-    cudaEvent_t a, b;
-    double bytes;
-};
-
-struct msk_context {
-    int device = 0;
-    cudaStream_t stream = nullptr;      // the stream work goes to
-    cudaStream_t own_stream = nullptr;  // created with the context
-    cudaStream_t aux = nullptr;         // second stream: the wave chain of the slice loop
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_t[2] = {}, ev_free[2] = {};
-    bool prof_on = false;
-    std::vector<ProfRec> prof_pending;
-    std::vector<cudaEvent_t> prof_pool;
-    long long prof_launches[kKinds] = {};
-    double prof_ms[kKinds] = {}, prof_bytes[kKinds] = {};
-    long long copies[2] = {};      // host-to-device, device-to-host copies while profiling
-    double copy_bytes[2] = {};
-    std::string err;
-    DevBuf psi, tbuf, tbuf2, atoms, slice_off, act, tables, imgmeta, wave0, images, exitw, fresnel,
-        flags;
-    DevBuf pa_v, pa_t, pa_psi, pa_e;  // buffers of the per-orientation comparison form
-    DevBuf stk, stk_v, stk_g, stk_t, stk_img, stk_part, adjtab;  // potential stacks, adjoint
-    DevBuf arena;                                // specimen batches
-    DevBuf dwbuf;                                // Debye-Waller -B/4 per (unit, slice)
-    DevBuf imgfill;                              // image-plane fill values per unit
-    DevBuf tune;                                 // scratch grid of the column tuner
-    bool no_tune = false;                        // column tiles fixed at variant 0
-    std::vector<cudaStream_t> lanes;             // concurrent specimens of a batch
-    std::vector<cudaEvent_t> lane_ev;            // lane joins (one per lane) + fork
-    size_t units_alloc = 0;  // units the psi / tbuf buffers hold
-    std::vector<int> zmap = std::vector<int>(104, -1);
-};
-
-namespace {
+namespace msk {
 
 int fail(msk_context *ctx, int code, const std::string &msg)
 {
     if (ctx) ctx->err = msg;
     return code;
 }
-
-#define MSK_CUDA(ctx, call)                                                                     \
-    do {                                                                                        \
-        cudaError_t e_ = (call);                                                                \
-        if (e_ != cudaSuccess)                                                                  \
-            return fail(ctx, e_ == cudaErrorMemoryAllocation ? MSK_ENOMEM : MSK_ECUDA,          \
-                        std::string(#call) + ": " + cudaGetErrorString(e_));                    \
-    } while (0)
 
 bool pow2_supported(int n) { return size_ops(n) != nullptr; }
 
@@ -997,42 +927,6 @@ int flags_check(msk_context *ctx)
     return MSK_OK;
 }
 
-// Brackets one launch with events when profiling is on.
-struct Prof {
-    msk_context *ctx;
-    int kind;
-    double bytes;
-    cudaEvent_t a = nullptr;
-    static cudaEvent_t get(msk_context *c)
-    {
-        if (!c->prof_pool.empty()) {
-            cudaEvent_t e = c->prof_pool.back();
-            c->prof_pool.pop_back();
-            return e;
-        }
-        cudaEvent_t e = nullptr;
-        cudaEventCreate(&e);
-        return e;
-    }
-    cudaStream_t st;
-    Prof(msk_context *c, int k, double b, cudaStream_t stream = nullptr)
-        : ctx(c), kind(k), bytes(b), st(stream ? stream : c->stream)
-    {
-        if (ctx->prof_on) {
-            a = get(ctx);
-            cudaEventRecord(a, st);
-        }
-    }
-    ~Prof()
-    {
-        if (a) {
-            cudaEvent_t b = get(ctx);
-            cudaEventRecord(b, st);
-            ctx->prof_pending.push_back({kind, a, b, bytes});
-        }
-    }
-};
-
 // Host<->device copy accounting (dir 0: to the device, 1: to the host).
 void count_copy(msk_context *ctx, int dir, double bytes)
 {
@@ -1056,6 +950,10 @@ void prof_collect(msk_context *ctx)
     }
     ctx->prof_pending.clear();
 }
+
+}  // namespace msk
+
+namespace {
 
 // The column tile of each pass (ColCfg variant), per device, grid and pass:
 // the first time a pass runs on a grid, both widths run on a scratch grid
@@ -1221,6 +1119,9 @@ int upload_tables(msk_context *ctx, GridPre &gp, const std::vector<int> &zlist)
 const float *tables_kx(msk_context *, const GridPre &gp) { return gp.d_kx; }
 const float *tables_ky(msk_context *, const GridPre &gp) { return gp.d_ky; }
 
+}  // namespace
+
+namespace msk {
 bool is_device_ptr(const void *p)
 {
     cudaPointerAttributes a;
@@ -1230,6 +1131,9 @@ bool is_device_ptr(const void *p)
     }
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
+}  // namespace msk
+
+namespace {
 
 // A batch of units (waves) with their atoms uploaded: the slice loop.
 struct Batch {
@@ -1457,7 +1361,9 @@ void msk_destroy(msk_context *ctx)
                       &ctx->imgmeta, &ctx->wave0, &ctx->images, &ctx->exitw, &ctx->fresnel,
                       &ctx->flags, &ctx->pa_v, &ctx->pa_t, &ctx->pa_psi, &ctx->pa_e, &ctx->stk,
                       &ctx->stk_v, &ctx->stk_g, &ctx->stk_t, &ctx->stk_img, &ctx->stk_part,
-                      &ctx->adjtab, &ctx->arena, &ctx->dwbuf, &ctx->imgfill, &ctx->tune})
+                      &ctx->adjtab, &ctx->arena, &ctx->dwbuf, &ctx->imgfill, &ctx->tune,
+                      &ctx->utr_img, &ctx->utr_k2, &ctx->utr_acc, &ctx->utr_vol, &ctx->utr_out,
+                      &ctx->utr_tab})
         b->release();
     for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_join, ctx->ev_t[0], ctx->ev_t[1], ctx->ev_free[0],
                           ctx->ev_free[1]})
