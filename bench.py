@@ -377,6 +377,179 @@ def run_adjoint(args, rank, world, local_rank):
     print(json.dumps(out))
 
 
+UTR_METRIC = ("UTR reconstruction voxels/s (1024^3 volume, CTF-3D, from the 180 x 1024^2 tilt "
+              "series, FP32)")
+UTR_UNIT = "voxels/s"
+
+
+def utr_params(msk, n, xst):
+    """UTR parameters of the reconstruction workload: an n^3 volume of voxel
+    edge xst spanning the 160 A box, 300 keV, CTF-3D with the Ewald sphere
+    correction, objective aperture 40 mrad, NSR 0.03, epsilon 1e-4 (the
+    readme's example values), beta/delta 0.05."""
+    u = msk.Utr()
+    u.modality, u.f1, u.f2, u.nx, u.ny, u.xst = 0, 1.0, 0.0, n, n, xst
+    u.zlo, u.zhi = -0.5 * n * xst, 0.5 * n * xst
+    u.wl, u.aobj, u.ctf_mode, u.escc = 0.01968749, 40.0, 4, 1
+    u.asigma, u.nsr, u.epsilon = 0.05, 0.03, 1e-4
+    return u
+
+
+def utr_cpu_sample(msk, imgs_small, ang, df, n, threads):
+    """The oracle's FP64 restatement of UTR.cpp on the host cores: the whole
+    reconstruction of an n^3 volume from the block-averaged images."""
+    from oracle import oracle as orc
+    O = orc.Oracle()
+    u = utr_params(msk, n, FOV / n)
+    p = orc.UtrParams()
+    for name, _ in p._fields_:
+        setattr(p, name, getattr(u, name))
+    t0 = time.perf_counter()
+    vol = O.utr_reconstruct(p, ang, df, imgs_small, nthreads=threads)
+    return vol, time.perf_counter() - t0
+
+
+def run_utr(args, rank, world, local_rank):
+    """UTR reconstruction: the 180-orientation tilt series (defocus 500 A
+    plane, simulated by this library's multislice, untimed) reconstructed
+    into a 1024^3 volume.  One step = one msk_utr_reconstruct call."""
+    import torch
+    import utr_public_gb300 as msk
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    msk.load()
+    ctx = msk.Context(local_rank)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    spec, angZ, angY, _ = workload(rank, NANG)
+    s = msk.Series()
+    s.nx = s.ny = NX
+    s.ctblength = s.ctblengthz = FOV
+    s.v0, s.deltaz = V0, DZ
+    timgs = torch.empty((NANG, 1, NX, NX), dtype=torch.float32, device="cuda")
+    ctx.tilt_series(s, spec.Znum, spec.x, spec.y, spec.z, spec.occ, angZ, angY, [500.0],
+                    images=timgs)
+    torch.cuda.synchronize()
+    # MsctKirkland's images are [nx][ny] (y fastest); UTR reads rows along y
+    imgs = timgs[:, 0].transpose(1, 2).contiguous()
+    del timgs
+    n = args.utr_n
+    if n != NX:  # a smaller volume: the images block-averaged to n^2
+        f = NX // n
+        imgs = imgs.reshape(NANG, n, f, n, f).mean(dim=(2, 4)).contiguous()
+    ang = np.stack([np.rad2deg(angZ), np.rad2deg(angY)], axis=1)
+    df = np.full(NANG, 500.0)
+    u = utr_params(msk, n, FOV / n)
+    nz = ctx.utr_depth(u)
+    vol = torch.empty((nz, n, n), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def timed(fn, k):
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ms = e0.elapsed_time(e1) / k
+        if dist is not None:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    step = lambda: ctx.utr_reconstruct(u, ang, df, imgs, volume=vol)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = Clocks(gpu_index(local_rank))
+    ms = timed(step, args.steps)
+    clk = clocks.stop()
+    nvox = n * n * nz
+    value = world * nvox / (ms / 1000.0)
+    ctx.profile(True)
+    ms_serial = timed(step, 1)
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    # end to end: pinned host images in, the host volume out
+    himg = torch.empty(imgs.shape, dtype=torch.float32, pin_memory=True)
+    himg.copy_(imgs)
+    hvol = torch.empty(vol.shape, dtype=torch.float32, pin_memory=True)
+    k_e2e = max(1, min(args.steps, 2))
+    ctx.utr_reconstruct(u, ang, df, himg, volume=hvol)
+    ctx.profile(True)
+    ms_e2e = timed(lambda: ctx.utr_reconstruct(u, ang, df, himg, volume=hvol), k_e2e)
+    prof_e2e = ctx.profile_read()
+    ctx.profile(False)
+    h2d = prof_e2e.get("copy_h2d", (0, 0.0, 0.0))[2] / k_e2e
+    d2h = prof_e2e.get("copy_d2h", (0, 0.0, 0.0))[2] / k_e2e
+    same = bool(torch.equal(hvol, vol.cpu())) if rank == 0 else None
+    kernels = {k: x for k, x in prof.items() if not k.startswith("copy_")}
+    launches = int(sum(x[0] for x in kernels.values())) * args.steps
+    dom = max(kernels, key=lambda k: kernels[k][1])
+    n_l, t_ms, nbytes = kernels[dom]
+    peak, peak_kind = peaks()
+    achieved = (nbytes / n_l) / (t_ms / n_l / 1000.0) / 1e9
+    if rank != 0:
+        return
+    # FP64 oracle on a bounded sample: the same images block-averaged 4 x 4
+    # to 256^2, a 256^3 volume; the GPU reconstructs the same sample
+    cpu, err = None, None
+    if not args.no_cpu_baseline and n % 4 == 0:
+        small = imgs.reshape(NANG, n // 4, 4, n // 4, 4).mean(dim=(2, 4)).contiguous()
+        small_np = small.cpu().numpy()
+        threads = os.cpu_count() or 1
+        m = n // 4
+        ref, dt = utr_cpu_sample(msk, small_np, ang, df, m, threads)
+        sample = ("180 images block-averaged to %d^2, a %d^3 volume (voxel %.4g A), the whole "
+                  "reconstruction" % (m, m, FOV / m))
+        cpu = {"value": m ** 3 / dt, "unit": UTR_UNIT, "cores": threads, "kind": "port",
+               "sample": sample, "seconds": dt}
+        us = utr_params(msk, m, FOV / m)
+        got = ctx.utr_reconstruct(us, ang, df, small_np)
+        err = {"volume_rel_l2_vs_fp64_%d" % m: float(np.linalg.norm(got - ref) /
+                                                   np.linalg.norm(ref))}
+    out = {
+        "metric": UTR_METRIC, "value": value, "unit": UTR_UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "UTR reconstruction: 180 orientations (1 deg about y) x %d^2 "
+                               "images at defocus 500 A of the 20000-atom tilt specimen, %d^3 "
+                               "volume of %.4g A voxels, CTF-3D + Ewald sphere correction, "
+                               "aperture 40 mrad, NSR 0.03, epsilon 1e-4" % (n, n, FOV / n),
+                   "voxels_per_step": nvox * world, "images_per_step": NANG * world,
+                   "l2": "inputs larger than L2 (34 GB of gridding sums per GPU)"},
+        "images_per_s": world * NANG / (ms / 1000.0),
+        "e2e": {"value": world * nvox / (ms_e2e / 1000.0), "unit": UTR_UNIT,
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "ms_per_step": ms_e2e, "matches_device_output": same},
+        "gpu_launches": launches * world,
+        "ms_per_step_serialized": ms_serial,
+        "kernels": {k: {"launches": x[0], "ms": round(x[1], 3),
+                        "GBps": round(x[2] / (x[1] / 1000.0) / 1e9, 1) if x[1] > 0 else None}
+                    for k, x in kernels.items()},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "peak_source": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_launch": nbytes / n_l},
+        "clocks": clk,
+        "cpu_baseline": cpu,
+        "err_vs_fp64": err,
+    }
+    print(json.dumps(out))
+
+
 UNEVEN_METRIC = ("uneven-batch slice-steps/s (64 specimens, 5e3-2e5 atoms, 256^2-2048^2, 1-90 "
                  "orientations, FP32, one CUDA graph)")
 
@@ -715,13 +888,16 @@ def main():
     ap.add_argument("--orientations", type=int, default=NANG,
                     help="orientations per step (180 for the headline workload)")
     ap.add_argument("--workload", default="tilt",
-                    choices=["tilt", "adjoint", "uneven", "plain", "phonon"],
+                    choices=["tilt", "adjoint", "uneven", "plain", "phonon", "utr"],
                     help="tilt: the 180-orientation 1024^2 tilt series (headline); plain: one "
                          "256^2 orientation; phonon: 60 orientations x 32 configurations at "
                          "1024^2; uneven: 64 specimens of uneven size in one graph; adjoint: "
-                         "the 512^2 potential-stack adjoint over 90 orientations")
+                         "the 512^2 potential-stack adjoint over 90 orientations; utr: the UTR "
+                         "reconstruction of the tilt series into a 1024^3 volume")
     ap.add_argument("--fd-voxels", type=int, default=32,
                     help="central-difference voxels per checked orientation (adjoint)")
+    ap.add_argument("--utr-n", type=int, default=NX,
+                    help="volume edge of the utr workload (images block-averaged to it)")
     ap.add_argument("--profile-run", action="store_true",
                     help="one tilt series and its per-kernel table, for profilers")
     args = ap.parse_args()
@@ -747,6 +923,16 @@ def main():
                                   "unavailable": "timed for the tilt-series workload only"}))
             return
         run_uneven(args, rank, world, local_rank)
+        return
+    if args.workload == "utr":
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "metric": UTR_METRIC,
+                                  "unavailable": "UTR.exe needs XArrayLibrary, which the reference "
+                                                 "does not include; the oracle port is timed as "
+                                                 "cpu_baseline"}))
+            return
+        run_utr(args, rank, world, local_rank)
         return
     if args.workload == "adjoint":
         if args.impl == "reference":
