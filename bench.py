@@ -424,6 +424,22 @@ def run_utr(args, rank, world, local_rank):
     ctx = msk.Context(local_rank)
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
+    if args.profile_run:
+        # for profilers: seeded smooth images, no multislice, a handful of calls
+        n = args.utr_n
+        g = torch.Generator(device="cuda")
+        g.manual_seed(7)
+        low = torch.randn((NANG, 1, n // 16, n // 16), generator=g, device="cuda")
+        imgs = (1.0 + 0.05 * torch.nn.functional.interpolate(low, size=(n, n), mode="bilinear",
+                                                             align_corners=False))[:, 0].contiguous()
+        ang = np.stack([np.zeros(NANG), np.arange(NANG, dtype=np.float64)], axis=1)
+        u = utr_params(msk, n, FOV / n)
+        vol = torch.empty((ctx.utr_depth(u), n, n), dtype=torch.float32, device="cuda")
+        for _ in range(2):
+            ctx.utr_reconstruct(u, ang, np.full(NANG, 500.0), imgs, volume=vol)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_run": "utr", "n": n, "volume_abs_sum": float(vol.abs().sum())}))
+        return
     spec, angZ, angY, _ = workload(rank, NANG)
     s = msk.Series()
     s.nx = s.ny = NX

@@ -6,13 +6,13 @@
 // nz x ny x nx):
 //   images   float   [nimg][ny][nx]     (the caller's, or a staged copy)
 //   k2       complex [nimg][ny][nx]     centred image spectra
-//   acc      UtrAcc  [nz][ny][nx]       fixed-point gridding sums (32 B)
+//   acc      UtrAcc  [nz][ny][nx]       gridding sums (re, im, weight, -), 16 B
 //   vol      complex [nz][ny][nx]       the spectrum, then its inverse in place
 //   out      float   [nz][ny][nx]       the caller's, or a staged copy
-// Gridding sums are int64 fixed point (atomic adds are exact and order-free,
-// so the result does not depend on the schedule); the scale is a power of
-// two chosen from the largest spectrum magnitude, with headroom for 16
-// contributions per image and voxel.
+// The gridding sums are float, as the reference accumulates them, with one
+// 16-byte vector atomic per voxel update: the summation order (and so the last
+// bits) follows the schedule, as in the reference's threaded loop over
+// orientations.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -64,26 +64,19 @@ struct UtrGridP {
     const float *tabs;  // [nimg][xxx2 | xsy | xcy (nx each) | yyy2 | ysz | ycz (ny each)]
     const float *scal;  // [nimg][kScal]
     float fxlo, fxst, fylo, fyst, fzlo, fzst;
-    int rotshift, escc, hb;
-    const unsigned *maxbits;
+    int rotshift, escc;
     UtrAcc *acc;
 };
-
-__device__ __forceinline__ void red_add(long long *p, long long v)
-{
-    atomicAdd(reinterpret_cast<unsigned long long *>(p), (unsigned long long)v);
-}
 
 // CT_3Dgridding (UTR.h:199-307) of every pixel of every image: the pixel's
 // frequency coordinates rotated back (about Y' then Z), on the Ewald sphere
 // with the curvature correction, the enclosing voxel cell, and trilinear
 // weights, all in float with the reference's operation order; each of the
-// eight corners gets weight * value and the weight, as fixed-point atomics.
+// eight corners gets (weight * value, weight) by one vector atomic.
 __global__ void __launch_bounds__(256) k_utr_grid(const UtrGridP p)
 {
     const size_t npix = (size_t)p.nx * p.ny, total = npix * p.nimg;
     const size_t nxny = npix;
-    const float vs = utr_pow2f(utr_vexp(*p.maxbits, p.hb)), ws = utr_pow2f(61 - p.hb);
     const int tstride = 3 * p.nx + 3 * p.ny;
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total;
          q += (size_t)gridDim.x * blockDim.x) {
@@ -130,37 +123,25 @@ __global__ void __launch_bounds__(256) k_utr_grid(const UtrGridP p)
 #pragma unroll
                 for (int e = 0; e < 2; e++) {
                     const float w = __fmul_rn(__fmul_rn(dx[e], dy[b]), dz[zc]);
+                    // a zero weight adds exact zeros: skip it (for a tilt about y
+                    // alone the pixel rows fall on voxel rows, dy1 = 0)
+                    if (w == 0.0f) continue;
                     UtrAcc *v = p.acc + (size_t)(nn + zc) * nxny + (size_t)(jj + b) * p.nx + (ii + e);
-                    red_add(&v->re, __float2ll_rn(__fmul_rn(__fmul_rn(cd.x, w), vs)));
-                    red_add(&v->im, __float2ll_rn(__fmul_rn(__fmul_rn(cd.y, w), vs)));
-                    red_add(&v->w, __float2ll_rn(__fmul_rn(w, ws)));
+                    atomicAdd(reinterpret_cast<float4 *>(v),
+                              make_float4(__fmul_rn(cd.x, w), __fmul_rn(cd.y, w), w, 0.0f));
                 }
     }
 }
 
-// max |re|, |im| of complex data (for spectra the caller supplies)
-__global__ void k_utr_maxabs(const float2 *__restrict__ a, size_t n, unsigned *maxbits)
+// gridding sums -> the caller's V3, Samp3 (msk_utr_grid)
+__global__ void k_utr_acc_split(const UtrAcc *__restrict__ acc, size_t n, float2 *__restrict__ v3,
+                                float *__restrict__ samp3)
 {
-    float mx = 0.0f;
-    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
-         q += (size_t)gridDim.x * blockDim.x) {
-        const float2 v = a[q];
-        mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
-    }
-    const unsigned bits = __reduce_max_sync(0xffffffffu, __float_as_uint(mx));
-    if ((threadIdx.x & 31) == 0) atomicMax(maxbits, bits);
-}
-
-// gridding sums -> float volumes (msk_utr_grid)
-__global__ void k_utr_acc_float(const UtrAcc *__restrict__ acc, size_t n, const unsigned *maxbits,
-                                int hb, float2 *__restrict__ v3, float *__restrict__ samp3)
-{
-    const float vinv = utr_pow2f(-utr_vexp(*maxbits, hb)), winv = utr_pow2f(-(61 - hb));
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
          q += (size_t)gridDim.x * blockDim.x) {
         const UtrAcc a = acc[q];
-        v3[q] = make_float2(__fmul_rn(__ll2float_rn(a.re), vinv), __fmul_rn(__ll2float_rn(a.im), vinv));
-        samp3[q] = __fmul_rn(__ll2float_rn(a.w), winv);
+        v3[q] = make_float2(a.re, a.im);
+        samp3[q] = a.w;
     }
 }
 
@@ -265,11 +246,22 @@ int make_geo(msk_context *ctx, const msk_utr *p, int nangles, const double *angl
     return MSK_OK;
 }
 
+// Host tables of one 3D correction (uploaded with the call's other tables).
+struct CorrTabs {
+    std::vector<double> lx, cx, ilx;
+    std::vector<float> cxf;
+    std::vector<float2> ex, ey, ez;
+};
+
+// (cos, sin) of a double phase, rounded to float
+float2 expi_d(double ph) { return make_float2((float)cos(ph), (float)sin(ph)); }
+
 // CTFcorrection3D's constants (UTR.h:27-83); MSK_EINVAL where it throws.
+// The phase of voxel (k, j, i) is fac2 (ksi_i + eta_j + zeta_k) - omega (+ the
+// Cs terms of ksi^2): its exponential is a product of per-axis factors.
 int ctf_setup(UtrFourier &f, int nx, int ny, int nz, double wl, double zlo, double zhi,
               double ylo, double yhi, double xlo, double xhi, double defocdist, double q2max,
-              double cs3, double cs5, double sigma, double epsilon, int escc,
-              std::vector<double> &cx, std::vector<double> &cfx)
+              double cs3, double cs5, double sigma, double epsilon, int escc, CorrTabs &t)
 {
     if ((nx & 1) || (ny & 1) || (nz & 1)) return MSK_EINVAL;
     const double xst = (xhi - xlo) / nx, yst = (yhi - ylo) / ny, zst = (zhi - zlo) / ny;
@@ -278,23 +270,36 @@ int ctf_setup(UtrFourier &f, int nx, int ny, int nz, double wl, double zlo, doub
     const double dksi2 = 1.0 / ((xhi - xlo) * (xhi - xlo));
     f.deta2 = 1.0 / ((yhi - ylo) * (yhi - ylo));
     f.dzeta2 = 1.0 / ((zhi - zlo) * (zhi - zlo));
-    f.fac2 = kPi * wl * defocdist;
+    const double fac2 = kPi * wl * defocdist;
     if (epsilon <= 0)
-        epsilon = 0.1 * pow(fabs(f.fac2) * std::min(dksi2, std::min(f.deta2, f.dzeta2)), 2);
-    f.eps = epsilon;
+        epsilon = 0.1 * pow(fabs(fac2) * std::min(dksi2, std::min(f.deta2, f.dzeta2)), 2);
+    f.eps = (float)epsilon;
     f.fac3 = kPi * pow(wl, 3) / 2.0 * cs3;
     f.fac5 = kPi * pow(wl, 5) / 3.0 * cs5;
-    f.omega = atan(sigma);
+    const double omega = atan(sigma);
     f.c35 = (cs3 != 0) || (cs5 != 0);
     f.aper = q2max > 0;
     f.q2max = q2max;
+    f.q2maxf = (float)q2max;
     f.escc = escc;
-    cx.resize(nx);
-    cfx.resize(nx);
+    t.cx.resize(nx);
+    t.cxf.resize(nx);
+    t.ex.resize(nx);
     for (int i = 0; i < nx; i++) {
         const int i1 = i - nx / 2;
-        cx[i] = dksi2 * i1 * i1;
-        cfx[i] = f.fac2 * cx[i];
+        t.cx[i] = dksi2 * i1 * i1;
+        t.cxf[i] = (float)t.cx[i];
+        t.ex[i] = expi_d(fac2 * t.cx[i]);
+    }
+    t.ey.resize(ny);
+    for (int j = 0; j < ny; j++) {
+        const int j1 = j - ny / 2;
+        t.ey[j] = expi_d(fac2 * (f.deta2 * j1 * j1));
+    }
+    t.ez.resize(nz);
+    for (int k = 0; k < nz; k++) {
+        const int k1 = k - nz / 2;
+        t.ez[k] = expi_d(fac2 * (f.dzeta2 * k1 * k1) - omega);
     }
     f.corr = 4;
     return MSK_OK;
@@ -368,39 +373,94 @@ void grid_tables(const msk_utr *p, const Geo &g, int nangles, const double *angl
     }
 }
 
-int headroom_bits(int nangles) { return 5 + ilog2i(std::max(1, nangles)); }
-
 bool sizes_ok(int n) { return utr_ops(n) != nullptr && size_ops(n) != nullptr; }
 
+// 2D view of `units` blocks of `lines` rows x `width` complex64 for a UTR
+// column pass over lines of length `lines` (box: its UtrColCfg tile).
+int utr_column_map(msk_context *ctx, ColView *view, void *base, int lines, size_t width,
+                   size_t units)
+{
+    auto enc = tensor_map_encoder();
+    if (!enc) return fail(ctx, MSK_ECUDA, "cuTensorMapEncodeTiled is not available");
+    const UtrOps *op = utr_ops(lines);
+    const cuuint64_t dims[2] = {(cuuint64_t)2 * width, (cuuint64_t)units * lines};
+    const cuuint64_t strides[1] = {(cuuint64_t)width * 8};
+    const cuuint32_t box[2] = {(cuuint32_t)(2 * op->col_c), (cuuint32_t)op->col_box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(&view->map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box,
+                     estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        return fail(ctx, MSK_ECUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    view->v = 0;
+    return MSK_OK;
+}
+
 // Device scratch of one call: tables at fixed offsets in ctx->utr_tab.
-struct TabLayout {
-    size_t maxbits, tw_x, tw_y, tw_z, lx, cx, cfx, ilx, ex, ey, ez, tabs, scal, total;
+// Device tables of one call, packed into ctx->utr_tab (256-byte aligned).
+struct TabPack {
+    std::vector<unsigned char> host;
+    size_t put(const void *p, size_t bytes)
+    {
+        const size_t at = host.size();
+        host.resize(at + ((bytes + 255) & ~(size_t)255));
+        if (bytes) std::memcpy(host.data() + at, p, bytes);
+        return at;
+    }
+    template <typename T> size_t put(const std::vector<T> &v) { return put(v.data(), v.size() * sizeof(T)); }
 };
 
-TabLayout tab_layout(int nx, int ny, int nz, size_t ntabs, size_t nscal, size_t ntw = 0)
+// The 3D-correction tables of `t` into the pack, pointers resolved against `base`.
+struct CorrOffsets {
+    size_t lx, cx, cxf, ilx, ex, ey, ez;
+};
+CorrOffsets put_corr(TabPack &pk, CorrTabs &t, int nx, int ny, int nz)
 {
-    TabLayout o{};
-    size_t at = 0;
-    auto put = [&](size_t bytes) {
-        const size_t here = at;
-        at += (bytes + 255) & ~(size_t)255;
-        return here;
-    };
-    o.maxbits = put(256);
-    o.tw_x = put(sizeof(float2) * std::max<size_t>(ntw, 2 * (size_t)nx));
-    o.tw_y = put(sizeof(float2) * std::max<size_t>(ntw, 2 * (size_t)ny));
-    o.tw_z = put(sizeof(float2) * std::max<size_t>(ntw, 2 * (size_t)nz));
-    o.lx = put(sizeof(double) * nx);
-    o.cx = put(sizeof(double) * nx);
-    o.cfx = put(sizeof(double) * nx);
-    o.ilx = put(sizeof(double) * nx);
-    o.ex = put(sizeof(double) * nx);
-    o.ey = put(sizeof(double) * ny);
-    o.ez = put(sizeof(double) * nz);
-    o.tabs = put(sizeof(float) * ntabs);
-    o.scal = put(sizeof(float) * nscal);
-    o.total = at;
+    if (t.lx.empty()) t.lx.assign(nx, 0.0);
+    if (t.cx.empty()) t.cx.assign(nx, 0.0);
+    if (t.cxf.empty()) t.cxf.assign(nx, 0.0f);
+    if (t.ilx.empty()) t.ilx.assign(nx, 0.0);
+    if (t.ex.empty()) t.ex.assign(nx, make_float2(1.0f, 0.0f));
+    if (t.ey.empty()) t.ey.assign(ny, make_float2(1.0f, 0.0f));
+    if (t.ez.empty()) t.ez.assign(nz, make_float2(1.0f, 0.0f));
+    CorrOffsets o;
+    o.lx = pk.put(t.lx);
+    o.cx = pk.put(t.cx);
+    o.cxf = pk.put(t.cxf);
+    o.ilx = pk.put(t.ilx);
+    o.ex = pk.put(t.ex);
+    o.ey = pk.put(t.ey);
+    o.ez = pk.put(t.ez);
     return o;
+}
+void bind_corr(UtrFourier &f, const unsigned char *base, const CorrOffsets &o)
+{
+    f.lx = reinterpret_cast<const double *>(base + o.lx);
+    f.cx = reinterpret_cast<const double *>(base + o.cx);
+    f.cxf = reinterpret_cast<const float *>(base + o.cxf);
+    f.ilx = reinterpret_cast<const double *>(base + o.ilx);
+    f.ex = reinterpret_cast<const float2 *>(base + o.ex);
+    f.ey = reinterpret_cast<const float2 *>(base + o.ey);
+    f.ez = reinterpret_cast<const float2 *>(base + o.ez);
+}
+
+// Uploads a pack into ctx->utr_tab; returns its device base (null on failure).
+unsigned char *upload_pack(msk_context *ctx, const TabPack &pk, int *st)
+{
+    *st = MSK_OK;
+    cudaError_t e = ctx->utr_tab.reserve(std::max<size_t>(pk.host.size(), 256));
+    if (e != cudaSuccess) {
+        *st = fail(ctx, e == cudaErrorMemoryAllocation ? MSK_ENOMEM : MSK_ECUDA, "table allocation failed");
+        return nullptr;
+    }
+    e = cudaMemcpyAsync(ctx->utr_tab.p, pk.host.data(), pk.host.size(), cudaMemcpyHostToDevice,
+                        ctx->stream);
+    if (e != cudaSuccess) {
+        *st = fail(ctx, MSK_ECUDA, std::string("table upload: ") + cudaGetErrorString(e));
+        return nullptr;
+    }
+    count_copy(ctx, 0, (double)pk.host.size());
+    return ctx->utr_tab.as<unsigned char>();
 }
 
 int upload(msk_context *ctx, void *dst, const void *src, size_t bytes)
@@ -417,8 +477,9 @@ int grid_blocks(size_t n)
 }
 
 // Images (device) -> centred spectra in ctx->utr_k2 and the magnitude bound.
+// Images (device) -> centred spectra in ctx->utr_k2.
 int spectra(msk_context *ctx, const msk_utr *p, int nangles, const float *img_d,
-            const float2 *tw_x, const float2 *tw_y, unsigned *maxbits)
+            const float2 *tw_x, const float2 *tw_y)
 {
     const int nx = p->nx, ny = p->ny;
     const size_t plane = (size_t)nx * ny;
@@ -438,7 +499,7 @@ int spectra(msk_context *ctx, const msk_utr *p, int nangles, const float *img_d,
         utr_ops(nx)->img_rows(ip, img_d, k2, ctx->stream);
     }
     ColView view;
-    int st = column_map(ctx, &view, k2, ny, nx, (size_t)nangles, size_ops(ny), 0);
+    int st = utr_column_map(ctx, &view, k2, ny, nx, (size_t)nangles);
     if (st) return st;
     Geom gdummy{};
     st = flags_reset(ctx, gdummy);
@@ -447,14 +508,13 @@ int spectra(msk_context *ctx, const msk_utr *p, int nangles, const float *img_d,
     cp.width = nx;
     cp.tw = tw_y;
     cp.err = gdummy.err;
-    cp.maxbits = maxbits;
     Prof pr(ctx, kUtrImgCols, 16.0 * plane * nangles);
     utr_ops(ny)->col_img(cp, view.map, view.map, nangles, ctx->stream);
     return MSK_OK;
 }
 
 int grid_launch(msk_context *ctx, const msk_utr *p, const Geo &g, int nangles, const float2 *k2,
-                const float *tabs_d, const float *scal_d, const unsigned *maxbits, UtrAcc *acc)
+                const float *tabs_d, const float *scal_d, UtrAcc *acc)
 {
     UtrGridP gp{};
     gp.nx = g.nx;
@@ -472,8 +532,6 @@ int grid_launch(msk_context *ctx, const msk_utr *p, const Geo &g, int nangles, c
     gp.fzst = (float)g.fzst;
     gp.rotshift = p->dxc != 0 || p->dyc != 0 || p->dzc != 0;
     gp.escc = p->escc != 0;
-    gp.hb = headroom_bits(nangles);
-    gp.maxbits = maxbits;
     gp.acc = acc;
     const size_t n = (size_t)g.nx * g.ny * nangles;
     Prof pr(ctx, kUtrGrid, 8.0 * n);
@@ -535,14 +593,14 @@ int msk_utr_reconstruct(msk_context *ctx, const msk_utr *p, int nangles, const d
     fr.nx = nx;
     fr.ny = ny;
     fr.nz = nz;
-    fr.hb = headroom_bits(nangles);
-    fr.nsr = p->nsr * sqrt((double)nx * ny);
-    std::vector<double> cx, cfx, lx, ilx(nx, 0.0);
+    fr.nsr = (float)(p->nsr * sqrt((double)nx * ny));
+    fr.inv_nsr = fr.nsr != 0.0f ? (float)(1.0 / (p->nsr * sqrt((double)nx * ny))) : 0.0f;
+    CorrTabs ct;
     if (g.zout != 0) {
         if (p->ctf_mode == 2) {
             const double alpha = -4.0 * kPi * p->asigma / (g.zout * p->wl);
             const double norm = -alpha * sqrt(1.0 + p->asigma * p->asigma) / p->asigma;
-            if (invlap_setup(nx, ny, nz, g.zhi - g.zlo, g.yhi - g.ylo, g.xhi - g.ylo, alpha, lx,
+            if (invlap_setup(nx, ny, nz, g.zhi - g.zlo, g.yhi - g.ylo, g.xhi - g.ylo, alpha, ct.lx,
                              fr.ly, fr.lz))
                 return fail(ctx, MSK_EINVAL, "InverseMLaplacian3D: alpha <= 0 or a zero aperture");
             fr.corr = 2;
@@ -550,13 +608,13 @@ int msk_utr_reconstruct(msk_context *ctx, const msk_utr *p, int nangles, const d
             fr.lnorm = norm;
         } else if (p->ctf_mode == 4) {
             if (ctf_setup(fr, nx, ny, nz, p->wl, g.zlo, g.zhi, g.ylo, g.yhi, g.xlo, g.xhi, g.zout,
-                          g.k2maxo, g.cs3, g.cs5, p->asigma, p->epsilon, p->escc, cx, cfx))
+                          g.k2maxo, g.cs3, g.cs5, p->asigma, p->epsilon, p->escc, ct))
                 return fail(ctx, MSK_EINVAL, "CTFcorrection3D: evanescent waves present");
         }
     }
     if (p->inv_laplace && p->ctf_mode != 1 && p->ctf_mode != 2) {
-        if (invlap_setup(nx, ny, nz, g.zhi - g.zlo, g.yhi - g.ylo, g.xhi - g.ylo, p->epsilon, ilx,
-                         fr.ily, fr.ilz))
+        if (invlap_setup(nx, ny, nz, g.zhi - g.zlo, g.yhi - g.ylo, g.xhi - g.ylo, p->epsilon,
+                         ct.ilx, fr.ily, fr.ilz))
             return fail(ctx, MSK_EINVAL, "inverse Laplacian filter: epsilon must be positive");
         fr.invlap = 1;
         fr.ilalpha = p->epsilon;
@@ -564,13 +622,10 @@ int msk_utr_reconstruct(msk_context *ctx, const msk_utr *p, int nangles, const d
     }
     fr.nyq = 1;
     fr.modulate = 1;
-    if (lx.empty()) lx.assign(nx, 0.0);
-    if (cx.empty()) {
-        cx.assign(nx, 0.0);
-        cfx.assign(nx, 0.0);
-    }
 
-    // output stage (UTR.cpp:1235-1278)
+    // output stage (UTR.cpp:1235-1278): the mask radius, exp(dtemp d^2) per
+    // axis (1 for an axis the mask leaves out) and the output scale
+    const bool use_y = !g.rot_y_only, use_z = !(g.rot_z_only || g.rot_z2_only);
     const long long nxd2 = nx / 2, nyd2 = ny / 2, nzd2 = nz / 2;
     const long long nxR2 = g.ic <= nxd2 ? g.ic * g.ic : (nx - g.ic) * (nx - g.ic);
     const long long nyR2 = g.jc <= nyd2 ? g.jc * g.jc : (ny - g.jc) * (ny - g.jc);
@@ -580,48 +635,32 @@ int msk_utr_reconstruct(msk_context *ctx, const msk_utr *p, int nangles, const d
     else if (g.rot_z_only || g.rot_z2_only) nR2 = std::min(nxR2, nyR2);
     else nR2 = std::min(std::min(nxR2, nyR2), nzR2);
     const double dtemp = 2.0 / (double)(g.kc * g.kc + g.jc * g.jc + g.ic * g.ic);
-    std::vector<double> ex(nx), ey(ny), ez(nz);
-    for (int i = 0; i < nx; i++) ex[i] = exp(dtemp * (double)((i - g.ic) * (i - g.ic)));
-    for (int j = 0; j < ny; j++) ey[j] = exp(dtemp * (double)((j - g.jc) * (j - g.jc)));
-    for (int k = 0; k < nz; k++) ez[k] = exp(dtemp * (double)((k - g.kc) * (k - g.kc)));
+    std::vector<float> mx(nx), my(ny), mz(nz);
+    for (int i = 0; i < nx; i++) mx[i] = (float)exp(dtemp * (double)((i - g.ic) * (i - g.ic)));
+    for (int j = 0; j < ny; j++) my[j] = use_y ? (float)exp(dtemp * (double)((j - g.jc) * (j - g.jc))) : 1.0f;
+    for (int k = 0; k < nz; k++) mz[k] = use_z ? (float)exp(dtemp * (double)((k - g.kc) * (k - g.kc))) : 1.0f;
     const double fnorm =
         p->modality == 0
             ? g.ee * p->wl / (2.0 * kPi * sqrt(1.0 + p->asigma * p->asigma) * g.xst)
             : p->asigma * p->wl / (4.0 * kPi * sqrt(1.0 + p->asigma * p->asigma) * g.xst);
 
+    // tables
     std::vector<float> tabs, scal;
     grid_tables(p, g, nangles, angles, tabs, scal);
     std::vector<float2> twx, twy, twz;
     if (!twiddles(nx, twx) || !twiddles(ny, twy) || !twiddles(nz, twz))
         return fail(ctx, MSK_EUNSUPPORTED, "no FFT for this size");
-
-    const TabLayout o = tab_layout(nx, ny, nz, tabs.size(), scal.size(),
-                                   std::max(twx.size(), std::max(twy.size(), twz.size())));
-    MSK_CUDA(ctx, ctx->utr_tab.reserve(o.total));
-    unsigned char *tb = ctx->utr_tab.as<unsigned char>();
-    MSK_CUDA(ctx, cudaMemsetAsync(tb + o.maxbits, 0, 256, ctx->stream));
-    if ((st = upload(ctx, tb + o.tw_x, twx.data(), twx.size() * sizeof(float2))) ||
-        (st = upload(ctx, tb + o.tw_y, twy.data(), twy.size() * sizeof(float2))) ||
-        (st = upload(ctx, tb + o.tw_z, twz.data(), twz.size() * sizeof(float2))) ||
-        (st = upload(ctx, tb + o.lx, lx.data(), nx * sizeof(double))) ||
-        (st = upload(ctx, tb + o.cx, cx.data(), nx * sizeof(double))) ||
-        (st = upload(ctx, tb + o.cfx, cfx.data(), nx * sizeof(double))) ||
-        (st = upload(ctx, tb + o.ilx, ilx.data(), nx * sizeof(double))) ||
-        (st = upload(ctx, tb + o.ex, ex.data(), nx * sizeof(double))) ||
-        (st = upload(ctx, tb + o.ey, ey.data(), ny * sizeof(double))) ||
-        (st = upload(ctx, tb + o.ez, ez.data(), nz * sizeof(double))) ||
-        (st = upload(ctx, tb + o.tabs, tabs.data(), tabs.size() * sizeof(float))) ||
-        (st = upload(ctx, tb + o.scal, scal.data(), scal.size() * sizeof(float))))
-        return st;
-    unsigned *maxbits = reinterpret_cast<unsigned *>(tb + o.maxbits);
-    const float2 *tw_x = reinterpret_cast<const float2 *>(tb + o.tw_x);
-    const float2 *tw_y = reinterpret_cast<const float2 *>(tb + o.tw_y);
-    const float2 *tw_z = reinterpret_cast<const float2 *>(tb + o.tw_z);
-    fr.maxbits = maxbits;
-    fr.lx = reinterpret_cast<const double *>(tb + o.lx);
-    fr.cx = reinterpret_cast<const double *>(tb + o.cx);
-    fr.cfx = reinterpret_cast<const double *>(tb + o.cfx);
-    fr.ilx = reinterpret_cast<const double *>(tb + o.ilx);
+    TabPack pk;
+    const size_t o_twx = pk.put(twx), o_twy = pk.put(twy), o_twz = pk.put(twz);
+    const CorrOffsets oc = put_corr(pk, ct, nx, ny, nz);
+    const size_t o_mx = pk.put(mx), o_my = pk.put(my), o_mz = pk.put(mz);
+    const size_t o_tabs = pk.put(tabs), o_scal = pk.put(scal);
+    unsigned char *tb = upload_pack(ctx, pk, &st);
+    if (!tb) return st;
+    const float2 *tw_x = reinterpret_cast<const float2 *>(tb + o_twx);
+    const float2 *tw_y = reinterpret_cast<const float2 *>(tb + o_twy);
+    const float2 *tw_z = reinterpret_cast<const float2 *>(tb + o_twz);
+    bind_corr(fr, tb, oc);
 
     // images in, spectra, gridding
     const size_t plane = (size_t)nx * ny, nvox = plane * nz;
@@ -631,27 +670,27 @@ int msk_utr_reconstruct(msk_context *ctx, const msk_utr *p, int nangles, const d
         if ((st = upload(ctx, ctx->utr_img.p, images, sizeof(float) * plane * nangles))) return st;
         img_d = ctx->utr_img.as<float>();
     }
-    if ((st = spectra(ctx, p, nangles, img_d, tw_x, tw_y, maxbits))) return st;
+    if ((st = spectra(ctx, p, nangles, img_d, tw_x, tw_y))) return st;
     MSK_CUDA(ctx, ctx->utr_acc.reserve(sizeof(UtrAcc) * nvox));
     UtrAcc *acc = ctx->utr_acc.as<UtrAcc>();
     MSK_CUDA(ctx, cudaMemsetAsync(acc, 0, sizeof(UtrAcc) * nvox, ctx->stream));
     if ((st = grid_launch(ctx, p, g, nangles, ctx->utr_k2.as<float2>(),
-                          reinterpret_cast<const float *>(tb + o.tabs),
-                          reinterpret_cast<const float *>(tb + o.scal), maxbits, acc)))
+                          reinterpret_cast<const float *>(tb + o_tabs),
+                          reinterpret_cast<const float *>(tb + o_scal), acc)))
         return st;
 
     // Fourier-space processing and the inverse 3D transform
     MSK_CUDA(ctx, ctx->utr_vol.reserve(sizeof(float2) * nvox));
     float2 *vol = ctx->utr_vol.as<float2>();
     {
-        Prof pr(ctx, kUtrFourier, 40.0 * nvox);
+        Prof pr(ctx, kUtrFourier, 24.0 * nvox);
         utr_ops(nx)->fourier_rows(fr, tw_x, acc, vol, ny * nz, ctx->stream);
     }
     Geom gdummy{};
     if ((st = flags_reset(ctx, gdummy))) return st;
     ColView vy, vz;
-    if ((st = column_map(ctx, &vy, vol, ny, nx, (size_t)nz, size_ops(ny), 0))) return st;
-    if ((st = column_map(ctx, &vz, vol, nz, nx * ny, 1, size_ops(nz), 0))) return st;
+    if ((st = utr_column_map(ctx, &vy, vol, ny, nx, (size_t)nz))) return st;
+    if ((st = utr_column_map(ctx, &vz, vol, nz, (size_t)nx * ny, 1))) return st;
     UtrCol cy{};
     cy.width = nx;
     cy.tw = tw_y;
@@ -680,11 +719,11 @@ int msk_utr_reconstruct(msk_context *ctx, const msk_utr *p, int nangles, const d
     cz.jc = g.jc;
     cz.kc = g.kc;
     cz.nr2 = nR2;
-    cz.use_y = !g.rot_y_only;
-    cz.use_z = !(g.rot_z_only || g.rot_z2_only);
-    cz.ex = reinterpret_cast<const double *>(tb + o.ex);
-    cz.ey = reinterpret_cast<const double *>(tb + o.ey);
-    cz.ez = reinterpret_cast<const double *>(tb + o.ez);
+    cz.use_y = use_y;
+    cz.use_z = use_z;
+    cz.ex = reinterpret_cast<const float *>(tb + o_mx);
+    cz.ey = reinterpret_cast<const float *>(tb + o_my);
+    cz.ez = reinterpret_cast<const float *>(tb + o_mz);
     {
         Prof pr(ctx, kUtrFinal, 12.0 * nvox);
         utr_ops(nz)->col_final(cz, vz.map, 1, ctx->stream);
@@ -715,14 +754,10 @@ int msk_utr_grid(msk_context *ctx, const msk_utr *p, int nangles, const double *
     MSK_CUDA(ctx, cudaSetDevice(ctx->device));
     std::vector<float> tabs, scal;
     grid_tables(p, g, nangles, angles, tabs, scal);
-    const TabLayout o = tab_layout(2, 2, 2, tabs.size(), scal.size());
-    MSK_CUDA(ctx, ctx->utr_tab.reserve(o.total));
-    unsigned char *tb = ctx->utr_tab.as<unsigned char>();
-    MSK_CUDA(ctx, cudaMemsetAsync(tb + o.maxbits, 0, 256, ctx->stream));
-    if ((st = upload(ctx, tb + o.tabs, tabs.data(), tabs.size() * sizeof(float))) ||
-        (st = upload(ctx, tb + o.scal, scal.data(), scal.size() * sizeof(float))))
-        return st;
-    unsigned *maxbits = reinterpret_cast<unsigned *>(tb + o.maxbits);
+    TabPack pk;
+    const size_t o_tabs = pk.put(tabs), o_scal = pk.put(scal);
+    unsigned char *tb = upload_pack(ctx, pk, &st);
+    if (!tb) return st;
     const size_t plane = (size_t)g.nx * g.ny, nvox = plane * g.nz;
     const float2 *k2_d = reinterpret_cast<const float2 *>(k2four);
     if (!is_device_ptr(k2four)) {
@@ -730,12 +765,11 @@ int msk_utr_grid(msk_context *ctx, const msk_utr *p, int nangles, const double *
         if ((st = upload(ctx, ctx->utr_k2.p, k2four, sizeof(float2) * plane * nangles))) return st;
         k2_d = ctx->utr_k2.as<float2>();
     }
-    k_utr_maxabs<<<grid_blocks(plane * nangles), 256, 0, ctx->stream>>>(k2_d, plane * nangles, maxbits);
     MSK_CUDA(ctx, ctx->utr_acc.reserve(sizeof(UtrAcc) * nvox));
     UtrAcc *acc = ctx->utr_acc.as<UtrAcc>();
     MSK_CUDA(ctx, cudaMemsetAsync(acc, 0, sizeof(UtrAcc) * nvox, ctx->stream));
-    if ((st = grid_launch(ctx, p, g, nangles, k2_d, reinterpret_cast<const float *>(tb + o.tabs),
-                          reinterpret_cast<const float *>(tb + o.scal), maxbits, acc)))
+    if ((st = grid_launch(ctx, p, g, nangles, k2_d, reinterpret_cast<const float *>(tb + o_tabs),
+                          reinterpret_cast<const float *>(tb + o_scal), acc)))
         return st;
     const bool vdev = is_device_ptr(v3), sdev = is_device_ptr(samp3);
     float2 *v_d = reinterpret_cast<float2 *>(v3);
@@ -746,9 +780,8 @@ int msk_utr_grid(msk_context *ctx, const msk_utr *p, int nangles, const double *
         if (!sdev) s_d = reinterpret_cast<float *>(ctx->utr_vol.as<float2>() + nvox);
     }
     {
-        Prof pr(ctx, kUtrPoint, 44.0 * nvox);
-        k_utr_acc_float<<<grid_blocks(nvox), 256, 0, ctx->stream>>>(acc, nvox, maxbits,
-                                                                     headroom_bits(nangles), v_d, s_d);
+        Prof pr(ctx, kUtrPoint, 28.0 * nvox);
+        k_utr_acc_split<<<grid_blocks(nvox), 256, 0, ctx->stream>>>(acc, nvox, v_d, s_d);
     }
     MSK_CUDA(ctx, cudaGetLastError());
     if (!vdev) {
@@ -770,19 +803,15 @@ namespace {
 
 // One pointwise pass over a caller's complex volume, staged through the
 // context when it is in host memory.
-int point_pass(msk_context *ctx, float *v3, size_t nvox, UtrFourier &f,
-               const std::vector<double> &tab_a, const std::vector<double> &tab_b)
+int point_pass(msk_context *ctx, float *v3, size_t nvox, UtrFourier &f, CorrTabs &t)
 {
     MSK_CUDA(ctx, cudaSetDevice(ctx->device));
-    const TabLayout o = tab_layout(f.nx, 2, 2, 0, 0);
-    MSK_CUDA(ctx, ctx->utr_tab.reserve(o.total));
-    unsigned char *tb = ctx->utr_tab.as<unsigned char>();
+    TabPack pk;
+    const CorrOffsets oc = put_corr(pk, t, f.nx, f.ny, f.nz);
     int st;
-    if ((st = upload(ctx, tb + o.lx, tab_a.data(), f.nx * sizeof(double))) ||
-        (st = upload(ctx, tb + o.cfx, tab_b.data(), f.nx * sizeof(double))))
-        return st;
-    f.lx = f.cx = f.ilx = reinterpret_cast<const double *>(tb + o.lx);
-    f.cfx = reinterpret_cast<const double *>(tb + o.cfx);
+    unsigned char *tb = upload_pack(ctx, pk, &st);
+    if (!tb) return st;
+    bind_corr(f, tb, oc);
     float2 *v_d = reinterpret_cast<float2 *>(v3);
     const bool dev = is_device_ptr(v3);
     if (!dev) {
@@ -820,11 +849,11 @@ int msk_utr_ctf_correction3d(msk_context *ctx, float *v3, int nx, int ny, int nz
     f.nx = nx;
     f.ny = ny;
     f.nz = nz;
-    std::vector<double> cx, cfx;
+    CorrTabs t;
     if (ctf_setup(f, nx, ny, nz, wl, zlo, zhi, ylo, yhi, xlo, xhi, defocdist, q2max, cs3, cs5,
-                  sigma, epsilon, escc, cx, cfx))
+                  sigma, epsilon, escc, t))
         return fail(ctx, MSK_EINVAL, "CTFcorrection3D: odd sizes or evanescent waves");
-    return point_pass(ctx, v3, (size_t)nx * ny * nz, f, cx, cfx);
+    return point_pass(ctx, v3, (size_t)nx * ny * nz, f, t);
 }
 
 int msk_utr_inverse_mlaplacian3d(msk_context *ctx, float *v3, int nx, int ny, int nz,
@@ -838,13 +867,13 @@ int msk_utr_inverse_mlaplacian3d(msk_context *ctx, float *v3, int nx, int ny, in
     f.nx = nx;
     f.ny = ny;
     f.nz = nz;
-    std::vector<double> lx;
-    if (invlap_setup(nx, ny, nz, zaper, yaper, xaper, alpha, lx, f.ly, f.lz))
+    CorrTabs t;
+    if (invlap_setup(nx, ny, nz, zaper, yaper, xaper, alpha, t.lx, f.ly, f.lz))
         return fail(ctx, MSK_EINVAL, "InverseMLaplacian3D: alpha <= 0, a zero aperture or odd sizes");
     f.corr = 2;
     f.lalpha = alpha;
     f.lnorm = norm;
-    return point_pass(ctx, v3, (size_t)nx * ny * nz, f, lx, lx);
+    return point_pass(ctx, v3, (size_t)nx * ny * nz, f, t);
 }
 
 }  // extern "C"

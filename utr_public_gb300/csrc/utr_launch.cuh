@@ -11,6 +11,7 @@ namespace msk {
 
 struct UtrOps {
     int n;
+    int col_c, col_box_rows;  // column tile width and TMA box height (UtrColCfg)
     // rows of images (x lines of length n)
     void (*img_rows)(const UtrImg &, const float *img, float2 *k2, cudaStream_t);
     // rows of the volume (x lines of length n): gridding sums -> inverse FFT
@@ -48,10 +49,9 @@ template <int N> struct UtrLaunch {
                     cudaStream_t s)
     {
         static std::once_flag f;
-        set_smem(k_utr_col<N, MODE>, Smem<N>::template col<0>(), f);
-        const int C = ColCfg<N, 0>::C;
-        k_utr_col<N, MODE><<<units * (p.width / C), ColCfg<N, 0>::NT, Smem<N>::template col<0>(), s>>>(
-            p, in, out);
+        using CC = UtrColCfg<N>;
+        set_smem(k_utr_col<N, MODE>, CC::SMEM, f);
+        k_utr_col<N, MODE><<<units * (p.width / CC::C), CC::NT, CC::SMEM, s>>>(p, in, out);
     }
     static void col_img(const UtrCol &p, const CUtensorMap &in, const CUtensorMap &out, int units,
                         cudaStream_t s)
@@ -69,7 +69,8 @@ template <int N> struct UtrLaunch {
     }
     static const UtrOps *ops()
     {
-        static const UtrOps o = {N, img_rows, fourier_rows, col_img, col_vol, col_final};
+        static const UtrOps o = {N,       UtrColCfg<N>::C, UtrColCfg<N>::BR, img_rows,
+                                 fourier_rows, col_img, col_vol, col_final};
         return &o;
     }
 };

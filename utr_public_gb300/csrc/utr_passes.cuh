@@ -8,9 +8,8 @@
 //
 // Image spectra (UTR.cpp:989-996):  k_utr_img_rows (normalise, threshold,
 //   log, (-1)^(x+y), FFT along x, FFTW's forward sign) then k_utr_col<N,
-//   kUtrColImg> (FFT along y, (-1)^(kx+ky), the maximum |re|, |im| for the
-//   fixed-point scale of the gridding).
-// Volume inverse (UTR.cpp:1200-1272): k_utr_fourier_rows (fixed-point sums ->
+//   kUtrColImg> (FFT along y, (-1)^(kx+ky)).
+// Volume inverse (UTR.cpp:1200-1272): k_utr_fourier_rows (gridding sums ->
 //   sampling normalisation, SNR filter, 3D correction, (-1)^(i+j+k), inverse
 //   FFT along x), k_utr_col<N, kUtrColVol> (along y, in place), k_utr_col<N,
 //   kUtrColFinal> (along z, then (-1)^(x+y+z), the real part / (nx ny nz), the
@@ -26,25 +25,30 @@
 
 namespace msk {
 
-// One voxel of the gridding sums: fixed-point real part, imaginary part and
-// weight (int64, two's complement through unsigned atomics), padded to 32 B.
-struct __align__(32) UtrAcc {
-    long long re, im, w, pad;
+// One voxel of the gridding sums (float, as the reference accumulates them):
+// real part, imaginary part, weight -- one 16-byte vector atomic per update.
+struct __align__(16) UtrAcc {
+    float re, im, w, pad;
 };
 
 // Per-voxel Fourier-space processing of UTR.cpp:1052-1217 and UTR.h:15-175.
 struct UtrFourier {
     int nx, ny, nz;
-    const unsigned *maxbits;  // bits of max |re|, |im| over every spectrum
-    int hb;                   // headroom bits of the fixed-point sums
-    double nsr;               // dInputNSR * sqrt(nx * ny); 0: plain normalisation
+    float nsr;                // dInputNSR * sqrt(nx * ny); 0: plain normalisation
+    float inv_nsr;            // 1 / nsr
     int corr;                 // 0 none, 2 TIE-Hom (inverse Laplacian), 4 CTF
     // InverseMLaplacian3D of the 3D TIE-Hom step: den = lx[i] + (j1 j1 ly + (k1 k1 lz + alpha))
     const double *lx;         // [nx] (dksi2 * i1) * i1
     double ly, lz, lalpha, lnorm;
-    // CTFcorrection3D: tables [nx] of (dksi2 * i1) * i1 and fac2 times it
-    const double *cx, *cfx;
-    double fac2, fac3, fac5, omega, eps, deta2, dzeta2, q2max;
+    // CTFcorrection3D: the phase dtemp = fac2 ksi^2 - omega (+ the Cs terms) of
+    // voxel (k, j, i) is a sum of per-axis parts; exp(i dtemp) = ex[i] ey[j]
+    // ez[k] from tables made in double (ez holds -omega).  cx: [nx] (dksi2 *
+    // i1) * i1 for the aperture test and the Cs terms.
+    const float2 *ex, *ey, *ez;
+    const double *cx;
+    const float *cxf;  // cx in float
+    double fac3, fac5, deta2, dzeta2, q2max;
+    float eps, q2maxf;
     int aper, c35, escc;
     // the optional inverse Laplacian filter (parameter 22), as lx/ly/lz
     int invlap;
@@ -53,19 +57,6 @@ struct UtrFourier {
     int nyq;       // apply the Hermitian step's factor on the x-Nyquist plane
     int modulate;  // multiply by (-1)^(i+j+k) for the centred inverse
 };
-
-__device__ __forceinline__ float utr_pow2f(int e)
-{
-    e = max(-126, min(127, e));
-    return __int_as_float((e + 127) << 23);
-}
-
-// 2^-scale of the fixed-point sums: s_v = 61 - hb - E with max < 2^E
-__device__ __forceinline__ int utr_vexp(unsigned maxbits, int hb)
-{
-    const int e = maxbits ? (int)((maxbits >> 23) & 0xff) - 127 + 1 : 0;
-    return max(-100, min(100, 61 - hb - e));
-}
 
 __device__ __forceinline__ float2 cmul_rn(float2 a, float2 b)
 {
@@ -90,7 +81,9 @@ __device__ __forceinline__ void sincos_reduced(double ph, float *s, float *c)
 
 // Row constants of the 3D corrections for row (k, j).
 struct UtrRow {
-    double eta2, eta2fac2;  // CTF
+    double eta2;            // CTF: the (j, k) part of ksi^2
+    float eta2f;
+    float2 e;               // CTF: ey[j] ez[k]
     double lden, ilden;     // inverse Laplacians: the (j, k) part of the denominator
 };
 
@@ -99,10 +92,10 @@ __device__ __forceinline__ UtrRow utr_row(const UtrFourier &f, int k, int j)
     UtrRow r;
     const int k1 = k - f.nz / 2, j1 = j - f.ny / 2;
     const double zeta2 = dmul(dmul(f.dzeta2, (double)k1), (double)k1);
-    const double zeta2fac2 = dadd(dmul(f.fac2, zeta2), -f.omega);
     const double eta2 = dmul(dmul(f.deta2, (double)j1), (double)j1);
-    r.eta2fac2 = dadd(dmul(f.fac2, eta2), zeta2fac2);
     r.eta2 = dadd(eta2, zeta2);
+    r.eta2f = (float)r.eta2;
+    r.e = f.corr == 4 ? cmul_rn(__ldg(&f.ey[j]), __ldg(&f.ez[k])) : make_float2(1.0f, 0.0f);
     r.lden = dadd(dmul((double)(j1 * j1), f.ly), dadd(dmul((double)(k1 * k1), f.lz), f.lalpha));
     r.ilden = dadd(dmul((double)(j1 * j1), f.ily), dadd(dmul((double)(k1 * k1), f.ilz), f.ilalpha));
     return r;
@@ -112,31 +105,42 @@ __device__ __forceinline__ UtrRow utr_row(const UtrFourier &f, int k, int j)
 __device__ __forceinline__ float2 utr_correct(const UtrFourier &f, const UtrRow &r, int i, float2 v)
 {
     if (f.corr == 4) {
-        double ksi2 = __ldg(&f.cx[i]);
-        const double ksi2fac2 = dadd(__ldg(&f.cfx[i]), r.eta2fac2);
-        ksi2 = dadd(ksi2, r.eta2);
-        if (!f.aper || ksi2 < f.q2max) {
-            double dtemp = ksi2fac2;
-            if (f.c35) {
-                const double k4 = dmul(ksi2, ksi2);
-                dtemp = dadd(dtemp, dadd(dmul(dmul(f.fac3, ksi2), ksi2), dmul(f.fac5, dmul(k4, ksi2))));
+        bool in = true;
+        double ksi2 = 0.0;
+        if (f.c35) ksi2 = dadd(__ldg(&f.cx[i]), r.eta2);
+        if (f.aper) {
+            // ksi^2 < q2max in double (UTR.h:106); decided in float away from
+            // the boundary
+            const float kf = __fadd_rn(__ldg(&f.cxf[i]), r.eta2f), qf = f.q2maxf;
+            if (fabsf(kf - qf) > 1e-5f * qf) {
+                in = kf < qf;
+            } else {
+                if (!f.c35) ksi2 = dadd(__ldg(&f.cx[i]), r.eta2);
+                in = ksi2 < f.q2max;
             }
-            float s, c;
-            sincos_reduced(dtemp, &s, &c);
-            const float epsf = (float)f.eps;
-            const float sinreg = __fdiv_rn(s, __fadd_rn(__fmul_rn(s, s), epsf));
+        }
+        if (in) {
+            float2 e = cmul_rn(__ldg(&f.ex[i]), r.e);  // (cos, sin) of the phase
+            if (f.c35) {
+                float s, c;
+                const double k4 = dmul(ksi2, ksi2);
+                sincos_reduced(dadd(dmul(dmul(f.fac3, ksi2), ksi2), dmul(f.fac5, dmul(k4, ksi2))),
+                               &s, &c);
+                e = cmul_rn(e, make_float2(c, s));
+            }
+            const float sinreg = __fdividef(e.y, fmaf(e.y, e.y, f.eps));
             float cosreg = 0.0f;
-            if (f.escc) cosreg = __fdiv_rn(c, __fadd_rn(__fmul_rn(c, c), epsf));
+            if (f.escc) cosreg = __fdividef(e.x, fmaf(e.x, e.x, f.eps));
             v = cmul_rn(v, make_float2(sinreg, -cosreg));
         }
     } else if (f.corr == 2) {
         const double den = dadd(__ldg(&f.lx[i]), r.lden);
-        const float sc = __fdiv_rn((float)f.lnorm, (float)den);
+        const float sc = __fdividef((float)f.lnorm, (float)den);
         v = make_float2(__fmul_rn(v.x, sc), __fmul_rn(v.y, sc));
     }
     if (f.invlap) {
         const double den = dadd(__ldg(&f.ilx[i]), r.ilden);
-        const float sc = __fdiv_rn((float)f.ilnorm, (float)den);
+        const float sc = __fdividef((float)f.ilnorm, (float)den);
         v = make_float2(__fmul_rn(v.x, sc), __fmul_rn(v.y, sc));
     }
     return v;
@@ -147,12 +151,12 @@ __device__ __forceinline__ float2 utr_correct(const UtrFourier &f, const UtrRow 
 __device__ __forceinline__ float2 utr_filter(const UtrFourier &f, float2 v, float x)
 {
     if (x == 0.0f) return make_float2(0.0f, 0.0f);
-    float s = __fdiv_rn(1.0f, x);
-    if (f.nsr != 0.0) {
-        const float den = __double2float_rn(__dmul_rn(f.nsr, (double)__fsqrt_rn(x)));
-        const float y = __fdiv_rn(hypotf(v.x, v.y), den);
+    float s = __frcp_rn(x);  // 1/x, correctly rounded as the reference's division
+    if (f.nsr != 0.0f) {
+        // y = |v| / (nsr sqrt(x)), the SNR of the coefficient
+        const float y = sqrtf(fmaf(v.x, v.x, v.y * v.y)) * rsqrtf(x) * f.inv_nsr;
         const float a = atanf(__fmul_rn(100.0f, __fsub_rn(y, 1.41421354f)));
-        s = __fmul_rn(s, __fadd_rn(0.5f, __fdiv_rn(a, 3.14159274f)));
+        s = __fmul_rn(s, fmaf(a, 0.318309873f, 0.5f));  // 0.5 + atan / pi
     }
     return make_float2(__fmul_rn(v.x, s), __fmul_rn(v.y, s));
 }
@@ -219,7 +223,7 @@ k_utr_img_rows(const UtrImg p, const float *__restrict__ img, float2 *__restrict
 // Row (k, j) of the volume: the gridding sums -> the processed spectrum ->
 // inverse FFT along x (FFTW's backward sign) into vol.
 template <int NX>
-__global__ void __launch_bounds__(RowCfg<NX>::L * FftPlan<NX>::T)
+__global__ void __launch_bounds__(RowCfg<NX>::L * FftPlan<NX>::T, RowCfg<NX>::MB)
 k_utr_fourier_rows(const UtrFourier f, const float2 *__restrict__ tw, const UtrAcc *__restrict__ acc,
                    float2 *__restrict__ vol)
 {
@@ -234,7 +238,6 @@ k_utr_fourier_rows(const UtrFourier f, const float2 *__restrict__ tw, const UtrA
     const bool ok = row < nrows;
     const int rr = ok ? row : 0;
     const int k = rr / f.ny, j = rr % f.ny;
-    const float vinv = utr_pow2f(-utr_vexp(*f.maxbits, f.hb)), winv = utr_pow2f(-(61 - f.hb));
     const UtrRow r = utr_row(f, k, j);
     const UtrAcc *src = acc + (size_t)rr * NX;
     float2 w[E];
@@ -242,9 +245,7 @@ k_utr_fourier_rows(const UtrFourier f, const float2 *__restrict__ tw, const UtrA
     for (int m = 0; m < E; m++) {
         const int i = t + m * T;
         const UtrAcc a = src[i];
-        float2 v = make_float2(__fmul_rn(__ll2float_rn(a.re), vinv), __fmul_rn(__ll2float_rn(a.im), vinv));
-        const float x = __fmul_rn(__ll2float_rn(a.w), winv);
-        v = utr_filter(f, v, x);
+        float2 v = utr_filter(f, make_float2(a.re, a.im), a.w);
         v = utr_correct(f, r, i, v);
         if (f.nyq && i == 0) {
             const float q = utr_nyquist_factor(k, j, f.ny, f.nz);
@@ -264,27 +265,39 @@ k_utr_fourier_rows(const UtrFourier f, const float2 *__restrict__ tw, const UtrA
 // ---------------------------------------------------------------- column passes
 enum { kUtrColImg = 0, kUtrColVol = 1, kUtrColFinal = 2 };
 
+// Column tiles of the UTR passes: C lines of N points with 256 threads
+// (capped at 16 lines), so that every row of a tile is C * 8 >= 32 bytes:
+// the z pass reads lines whose points lie nx * ny * 8 bytes apart.
+template <int N> struct UtrColCfg {
+    static constexpr int T = FftPlan<N>::T;
+    static constexpr int C = (256 / T) < 2 ? 2 : ((256 / T) > 16 ? 16 : 256 / T);
+    static constexpr int NT = C * T;
+    static constexpr int BR = N < 256 ? N : 256;  // rows per TMA box
+    static constexpr int NBOX = N / BR;
+    static constexpr uint32_t TILE_BYTES = (uint32_t)N * C * 8;
+    static constexpr size_t SMEM = (size_t)C * FftPlan<N>::PADN * 8 + 16;
+};
+
 struct UtrCol {
     int width;  // complex columns of the 2D view
     const float2 *tw;
     int *err;
-    unsigned *maxbits;  // kUtrColImg
     // kUtrColFinal: the volume [nz][ny][nx] (width = nx * ny, lines = nz)
     float *out;
     int nx, ny, nxlog;
     float inv_n, fnorm;
     long long ic, jc, kc, nr2;
     int use_y, use_z;
-    const double *ex, *ey, *ez;  // exp(dtemp * d^2) per axis
+    const float *ex, *ey, *ez;  // exp(dtemp * d^2) per axis (1 for an axis left out)
 };
 
 template <int N, int MODE>
-__global__ void __launch_bounds__(ColCfg<N, 0>::NT)
+__global__ void __launch_bounds__(UtrColCfg<N>::NT)
 k_utr_col(const UtrCol p, const __grid_constant__ CUtensorMap in_map,
           const __grid_constant__ CUtensorMap out_map)
 {
     using P = FftPlan<N>;
-    using CC = ColCfg<N, 0>;
+    using CC = UtrColCfg<N>;
     constexpr int T = P::T, E = P::E, C = CC::C;
     extern __shared__ __align__(128) unsigned char smem[];
     float2 *buf = reinterpret_cast<float2 *>(smem);
@@ -315,7 +328,7 @@ k_utr_col(const UtrCol p, const __grid_constant__ CUtensorMap in_map,
     if constexpr (MODE == kUtrColFinal) {
         const int x = col & (p.nx - 1), y = col >> p.nxlog;
         const long long dx = x - p.ic, dy = y - p.jc;
-        const double fxy = __dmul_rn(__ldg(&p.ex[x]), p.use_y ? __ldg(&p.ey[y]) : 1.0);
+        const float fxy = __fmul_rn(__ldg(&p.ex[x]), __ldg(&p.ey[y]));
 #pragma unroll
         for (int m = 0; m < E; m++) {
             const int z = t + m * T;
@@ -327,23 +340,16 @@ k_utr_col(const UtrCol p, const __grid_constant__ CUtensorMap in_map,
             if (ii2 > p.nr2) {
                 r = 0.0f;
             } else {
-                const double e = __dmul_rn(fxy, p.use_z ? __ldg(&p.ez[z]) : 1.0);
-                r = __fmul_rn(__fmul_rn(r, __double2float_rn(e)), p.fnorm);
+                r = __fmul_rn(__fmul_rn(r, __fmul_rn(fxy, __ldg(&p.ez[z]))), p.fnorm);
             }
             p.out[((size_t)z * p.ny * p.nx) + col] = r;
         }
         return;
     } else {
         if constexpr (MODE == kUtrColImg) {
-            float mx = 0.0f;
 #pragma unroll
-            for (int m = 0; m < E; m++) {
+            for (int m = 0; m < E; m++)
                 if ((col + t + m * T) & 1) v[m] = make_float2(-v[m].x, -v[m].y);
-                mx = fmaxf(mx, fmaxf(fabsf(v[m].x), fabsf(v[m].y)));
-            }
-            constexpr unsigned kLanes = CC::NT >= 32 ? 0xffffffffu : ((1u << CC::NT) - 1u);
-            const unsigned bits = __reduce_max_sync(kLanes, __float_as_uint(mx));
-            if ((tid & 31) == 0) atomicMax(p.maxbits, bits);
         }
         __syncthreads();  // every thread is done with the exchange layout
 #pragma unroll
