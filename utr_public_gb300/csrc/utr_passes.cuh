@@ -89,15 +89,19 @@ struct UtrRow {
 
 __device__ __forceinline__ UtrRow utr_row(const UtrFourier &f, int k, int j)
 {
-    UtrRow r;
+    UtrRow r{};
     const int k1 = k - f.nz / 2, j1 = j - f.ny / 2;
-    const double zeta2 = dmul(dmul(f.dzeta2, (double)k1), (double)k1);
-    const double eta2 = dmul(dmul(f.deta2, (double)j1), (double)j1);
-    r.eta2 = dadd(eta2, zeta2);
-    r.eta2f = (float)r.eta2;
-    r.e = f.corr == 4 ? cmul_rn(__ldg(&f.ey[j]), __ldg(&f.ez[k])) : make_float2(1.0f, 0.0f);
-    r.lden = dadd(dmul((double)(j1 * j1), f.ly), dadd(dmul((double)(k1 * k1), f.lz), f.lalpha));
-    r.ilden = dadd(dmul((double)(j1 * j1), f.ily), dadd(dmul((double)(k1 * k1), f.ilz), f.ilalpha));
+    if (f.corr == 4) {  // (the FP64 pipe is narrow: only what the mode uses)
+        const double zeta2 = dmul(dmul(f.dzeta2, (double)k1), (double)k1);
+        const double eta2 = dmul(dmul(f.deta2, (double)j1), (double)j1);
+        r.eta2 = dadd(eta2, zeta2);
+        r.eta2f = (float)r.eta2;
+        r.e = cmul_rn(__ldg(&f.ey[j]), __ldg(&f.ez[k]));
+    }
+    if (f.corr == 2)
+        r.lden = dadd(dmul((double)(j1 * j1), f.ly), dadd(dmul((double)(k1 * k1), f.lz), f.lalpha));
+    if (f.invlap)
+        r.ilden = dadd(dmul((double)(j1 * j1), f.ily), dadd(dmul((double)(k1 * k1), f.ilz), f.ilalpha));
     return r;
 }
 
@@ -240,8 +244,10 @@ k_utr_fourier_rows(const UtrFourier f, const float2 *__restrict__ tw, const UtrA
     const int k = rr / f.ny, j = rr % f.ny;
     const UtrRow r = utr_row(f, k, j);
     const UtrAcc *src = acc + (size_t)rr * NX;
-    float2 w[E];
-#pragma unroll
+    float2 *line = s_lines + l * P::PADN;
+    // per-voxel work in a rolled loop (one copy of the code: the unrolled form
+    // overflowed the instruction cache), staged in the line's shared buffer
+#pragma unroll 1
     for (int m = 0; m < E; m++) {
         const int i = t + m * T;
         const UtrAcc a = src[i];
@@ -252,9 +258,13 @@ k_utr_fourier_rows(const UtrFourier f, const float2 *__restrict__ tw, const UtrA
             v = make_float2(v.x * q, v.y * q);
         }
         if (f.modulate && ((i + j + k) & 1)) v = make_float2(-v.x, -v.y);
-        w[m] = v;
+        line[i] = v;
     }
-    fft_line<NX, false, 1, BLK>(w, s_lines + l * P::PADN, 0, t, tw);
+    group_sync<BLK>();
+    float2 w[E];
+#pragma unroll
+    for (int m = 0; m < E; m++) w[m] = line[t + m * T];
+    fft_line<NX, false, 1, BLK>(w, line, 0, t, tw);
     if (ok) {
         float2 *dst = vol + (size_t)rr * NX;
 #pragma unroll
