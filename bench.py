@@ -759,6 +759,15 @@ def run_plain(args, rank, world, local_rank):
     prof = ctx.profile_read()
     ctx.profile(False)
     kernels = {kk: x for kk, x in prof.items() if not kk.startswith("copy_")}
+    # the dominant kernel against the HBM copy peak (a 0.5 MB problem: the
+    # launches are latency-bound, the fraction is low by nature)
+    dom = max(kernels, key=lambda kk: kernels[kk][1])
+    n_l, t_ms, nbytes = kernels[dom]
+    peak, peak_kind = peaks()
+    achieved = (nbytes / n_l) / (t_ms / n_l / 1000.0) / 1e9
+    roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+            "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+            "traffic": None, "algorithmic_bytes_per_launch": nbytes / n_l}
     if rank != 0:
         return
     err = {}
@@ -798,6 +807,7 @@ def run_plain(args, rank, world, local_rank):
                 "call": "msk_calculate, host atoms and exit wave"},
         "gpu_launches": int(sum(x[0] for x in kernels.values())) * k,
         "kernels": {kk: {"launches": x[0], "ms": round(x[1], 4)} for kk, x in kernels.items()},
+        "roofline": roof,
         "clocks": clk, "cpu_baseline": cpu, "err": err}))
 
 
