@@ -1665,6 +1665,20 @@ int tilt_series_impl(msk_context *ctx, const msk_series *s, int natom, const int
     int B = (int)std::max<size_t>(1, std::min<size_t>(nunits, budget / (3 * plane * sizeof(float2))));
     if (s->max_batch > 0) B = std::min(B, s->max_batch);
     if (nconfig > 1 && B > nconfig) B = (B / nconfig) * nconfig;  // whole angles per batch
+    // batch bounds: a large call starts with a small batch (~1/16 of the
+    // units) so that only its host preparation is exposed; each later batch is
+    // prepared on the host while the GPU runs the one before
+    std::vector<int> bounds = {0};
+    {
+        int first = B;
+        if (s->max_batch <= 0 && nunits >= 32) {
+            first = std::min(B, std::max(8, (nunits + 15) / 16));
+            if (nconfig > 1) first = std::max(nconfig, (first / nconfig) * nconfig);
+            first = std::min(first, B);
+        }
+        bounds.push_back(std::min(first, nunits));
+        while (bounds.back() < nunits) bounds.push_back(std::min(nunits, bounds.back() + B));
+    }
 
     float *d_images = images;
     if (ndefocus > 0 && !img_dev) {
@@ -1721,8 +1735,7 @@ int tilt_series_impl(msk_context *ctx, const msk_series *s, int natom, const int
 
     std::vector<UnitAtoms> ua(nunits);
     const SizeOps *rop = size_ops(ny), *cop = size_ops(nx);
-    for (int u0 = 0; u0 < nunits; u0 += B) {
-        const int nb = std::min(B, nunits - u0);
+    auto prep_batch = [&](int u0, int nb) {
         auto prep = [&](int u) {
             const int a = u / nconfig, c = u % nconfig;
             PrepSpec ps{natom, Znum, x, y, z, occ, s->ctblength, s->ctblengthz, s->deltaz,
@@ -1746,6 +1759,10 @@ int tilt_series_impl(msk_context *ctx, const msk_series *s, int natom, const int
         } else {
             parallel_for(nb, host_threads(), [&](int i) { prep(u0 + i); });
         }
+    };
+    prep_batch(0, bounds[1]);
+    for (size_t bi = 0; bi + 1 < bounds.size(); bi++) {
+        const int u0 = bounds[bi], nb = bounds[bi + 1] - bounds[bi];
         for (int i = 0; i < nb; i++)
             if (ua[u0 + i].status)
                 return fail(ctx, ua[u0 + i].status, msk_status_string(ua[u0 + i].status));
@@ -1894,9 +1911,11 @@ int tilt_series_impl(msk_context *ctx, const msk_series *s, int natom, const int
             }
         }
         MSK_CUDA(ctx, cudaGetLastError());
-        MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        prof_collect(ctx);
+        // the next batch's atoms while this one runs (its upload waits for it)
+        if (bi + 2 < bounds.size()) prep_batch(bounds[bi + 1], bounds[bi + 2] - bounds[bi + 1]);
     }
+    MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    prof_collect(ctx);
     if (ndefocus > 0 && !img_dev)
     {
         MSK_CUDA(ctx, cudaMemcpyAsync(images, d_images, img_bytes, cudaMemcpyDeviceToHost,
