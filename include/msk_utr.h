@@ -20,6 +20,7 @@
  *   - every pointer may be host or device memory;
  *   - nx, ny and the volume depth nz: powers of two from 16 to 4096;
  *   - status codes and the context are those of msk.h.
+ * zlo = zhi = 0 with modality 1 selects the ".xri" default z range [xlo, xhi].
  */
 #ifndef MSK_UTR_H
 #define MSK_UTR_H
@@ -68,7 +69,9 @@ int msk_utr_reconstruct(msk_context *ctx, const msk_utr *p, int nangles, const d
 
 /* CT_3Dgridding (UTR.h:199-307) of nangles centred image spectra into a
  * zeroed volume: v3 = sum of weight * K2four, samp3 = sum of weights,
- * accumulated exactly (fixed point) and rounded to float once.
+ * accumulated in float as the reference does (by atomics: the order of the
+ * sums, and so their last bits, follow the schedule, as in the reference's
+ * threaded loop over orientations).
  *   k2four: complex [nangles][ny][nx]; v3 out: complex [nz][ny][nx];
  *   samp3 out: float [nz][ny][nx] */
 int msk_utr_grid(msk_context *ctx, const msk_utr *p, int nangles, const double *angles,

@@ -141,3 +141,17 @@ def test_reconstruction_linear_in_log_images(oracle):
     assert rel_l2(v2, 2.0 * v1) < 1e-5  # the images are rounded to float
     # flat images reconstruct to zero
     assert not oracle.utr_reconstruct(p, ang, df, np.ones_like(g, np.float32)).any()
+
+
+def test_library_depth_matches_oracle(msk, oracle):
+    # msk_utr_depth is host code: no GPU needed
+    L = msk.load()
+    for kw in (dict(nx=64, ny=32, xst=0.457, zlo=3.6, zhi=-3.7), dict(nx=32, ny=32, xst=0.5),
+               dict(modality=1, asigma=-0.01, zlo=0.0, zhi=0.0, nx=32, ny=32, xst=0.5)):
+        p = uc.params(**kw)
+        u = msk.Utr()
+        for name, _ in p._fields_:
+            setattr(u, name, getattr(p, name))
+        assert L.msk_utr_depth(u) == oracle.utr_geom(p, [[0, 0]], [0.0]).nz
+    bad = msk.Utr(nx=32, ny=32, xst=0.0, zlo=-1.0, zhi=1.0, wl=0.02)
+    assert L.msk_utr_depth(bad) == -8

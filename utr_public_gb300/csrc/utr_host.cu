@@ -396,7 +396,6 @@ int utr_column_map(msk_context *ctx, ColView *view, void *base, int lines, size_
     return MSK_OK;
 }
 
-// Device scratch of one call: tables at fixed offsets in ctx->utr_tab.
 // Device tables of one call, packed into ctx->utr_tab (256-byte aligned).
 struct TabPack {
     std::vector<unsigned char> host;
