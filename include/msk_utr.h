@@ -67,6 +67,18 @@ int msk_utr_depth(const msk_utr *p);
 int msk_utr_reconstruct(msk_context *ctx, const msk_utr *p, int nangles, const double *angles,
                         const double *defocus, const float *images, float *volume);
 
+/* msk_utr_reconstruct with each image's Z'' rotation and shift undone first
+ * (UTR.cpp:920-940, the orientation file's Z'' angle and the .relionnew
+ * shifts): the normalised image is shifted back by whole pixels, then
+ * rotated by -Z'' about the rotation centre (Catmull-Rom bicubic), the mean
+ * of its pixels within 5 of an edge filling in (XArray2DMove, XArray2DSpln:
+ * XArrayLibrary is not part of the reference; this library's definitions).
+ *   zrot: [nangles] Z'' angles (degrees), may be NULL
+ *   shifts: [nangles][2] x, y shifts, may be NULL */
+int msk_utr_reconstruct_planes(msk_context *ctx, const msk_utr *p, int nangles,
+                               const double *angles, const double *defocus, const double *zrot,
+                               const double *shifts, const float *images, float *volume);
+
 /* CT_3Dgridding (UTR.h:199-307) of nangles centred image spectra into a
  * zeroed volume: v3 = sum of weight * K2four, samp3 = sum of weights,
  * accumulated in float as the reference does (by atomics: the order of the

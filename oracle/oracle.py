@@ -157,8 +157,8 @@ class Oracle:
                 [C.c_int]
         for nm, T in (("mo_utr_invlap3d_f32", _fp), ("mo_utr_invlap3d_f64", _dp)):
             getattr(L, nm).argtypes = [T, C.c_int, C.c_int, C.c_int] + [C.c_double] * 5
-        L.mo_utr_reconstruct_f64.argtypes = [C.POINTER(UtrParams), C.c_int, _dp, _dp, _fp, _dp,
-                                             C.c_int]
+        L.mo_utr_reconstruct_f64.argtypes = [C.POINTER(UtrParams), C.c_int, _dp, _dp, C.c_void_p,
+                                             C.c_void_p, _fp, _dp, C.c_int]
         L.mo_utr_finish_f64.argtypes = [C.POINTER(UtrParams), C.c_int, _dp, _dp, _dp, _dp, _dp]
 
     # -- physics
@@ -410,12 +410,16 @@ class Oracle:
             raise ValueError("InverseMLaplacian3D: bad arguments")
         return v3
 
-    def utr_reconstruct(self, p, angles, defocus, images, nthreads=1):
+    def utr_reconstruct(self, p, angles, defocus, images, nthreads=1, zrot=None, shifts=None):
         g = self.utr_geom(p, angles, defocus)
         vol = np.zeros((g.nz, p.ny, p.nx), np.float64)
         ang = np.ascontiguousarray(angles, np.float64).reshape(-1)
+        zr = None if zrot is None else np.ascontiguousarray(zrot, np.float64)
+        sh = None if shifts is None else np.ascontiguousarray(shifts, np.float64).reshape(-1)
         st = self.L.mo_utr_reconstruct_f64(C.byref(p), len(ang) // 2, ang,
                                            np.ascontiguousarray(defocus, np.float64),
+                                           None if zr is None else zr.ctypes.data,
+                                           None if sh is None else sh.ctypes.data,
                                            np.ascontiguousarray(images, np.float32), vol,
                                            nthreads)
         if st:

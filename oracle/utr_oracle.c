@@ -17,7 +17,13 @@
  *     spectrum kx = 0 .. nx/2 (centred indices nx/2 .. nx-1 and 0): complex
  *     inverse transforms along z and y, then a real inverse along x that
  *     reads the real parts of its kx = 0 and kx = nx/2 terms; GetRealXArray3D
- *     shuffles back and divides by nx*ny*nz (UTR.cpp:1266-1272).
+ *     shuffles back and divides by nx*ny*nz (UTR.cpp:1266-1272);
+ *   - NormAverEdge(5), XArray2DMove::Move and XArray2DSpln::Rotate of the
+ *     input images (UTR.cpp:920-940): the mean over the pixels within 5 of any
+ *     edge; out(j, i) = in(j - dy, i - dx); out(p) = in(c + R(-t)(p - c)) by
+ *     Catmull-Rom bicubic interpolation, R(t) = [[cos t, -sin t], [sin t,
+ *     cos t]] on (x, y) = (i, j), both reading the edge mean outside the
+ *     image (the definitions this library uses for MsctKirkland's image plane).
  */
 #include "utr_oracle.h"
 
@@ -124,6 +130,77 @@ static void shuffle2_d(double *a, int nx, int ny)
         }
     memcpy(a, t, sizeof(double) * 2 * (size_t)nx * ny);
     free(t);
+}
+
+static double cr_w(double t, int k)
+{
+    const double t2 = t * t, t3 = t2 * t;
+    switch (k) {
+    case 0: return 0.5 * (-t3 + 2.0 * t2 - t);
+    case 1: return 0.5 * (3.0 * t3 - 5.0 * t2 + 2.0);
+    case 2: return 0.5 * (-3.0 * t3 + 4.0 * t2 + t);
+    default: return 0.5 * (t3 - t2);
+    }
+}
+
+/* UTR.cpp:920-940 on a normalised image [ny][nx] in place: the edge mean,
+ * the shift (dx, dy) pixels, then the rotation by `t` about (cx, cy) (pixels),
+ * as defined in the file header (UTR rotates by -Z'': t = -Z'') */
+void mo_utr_image_plane_f64(double *img, int nx, int ny, double cx, double cy, double t,
+                            long dx, long dy)
+{
+    const size_t n = (size_t)nx * ny;
+    double f = 0.0;
+    long cnt = 0;
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++)
+            if (i < 5 || i >= nx - 5 || j < 5 || j >= ny - 5) {
+                f += img[(size_t)j * nx + i];
+                cnt++;
+            }
+    if (cnt) f /= cnt;
+    double *s1 = (double *)malloc(sizeof(double) * n);
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            const long jj = j - dy, ii = i - dx;
+            s1[(size_t)j * nx + i] =
+                (jj >= 0 && jj < ny && ii >= 0 && ii < nx) ? img[(size_t)jj * nx + ii] : f;
+        }
+    if (t == 0.0) {
+        memcpy(img, s1, sizeof(double) * n);
+        free(s1);
+        return;
+    }
+    const double c = cos(t), sn = sin(t);
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            const double ddx = i - cx, ddy = j - cy;
+            const double fx = cx + c * ddx + sn * ddy, fy = cy - sn * ddx + c * ddy;  /* R(-t) */
+            const int x0 = (int)floor(fx), y0 = (int)floor(fy);
+            const double tx = fx - x0, ty = fy - y0;
+            double acc = 0.0;
+            for (int b = 0; b < 4; b++)
+                for (int a = 0; a < 4; a++) {
+                    const int xx = x0 - 1 + a, yy = y0 - 1 + b;
+                    const double w = cr_w(tx, a) * cr_w(ty, b);
+                    acc += w * ((xx >= 0 && xx < nx && yy >= 0 && yy < ny) ? s1[(size_t)yy * nx + xx] : f);
+                }
+            img[(size_t)j * nx + i] = acc;
+        }
+    free(s1);
+}
+
+/* the log-FFT of a normalised double image (UTR.cpp:989-996) */
+static void k2four_from_norm(double *k2, const double *v, int nx, int ny)
+{
+    const size_t n = (size_t)nx * ny;
+    for (size_t q = 0; q < n; q++) {
+        k2[2 * q] = v[q] > 0.0 ? log(v[q]) : 0.0;
+        k2[2 * q + 1] = 0.0;
+    }
+    shuffle2_d(k2, nx, ny);
+    ocfft2d_d(k2, ny, nx, -1);
+    shuffle2_d(k2, nx, ny);
 }
 
 /* UTR.cpp:940-950 (normalisation, threshold) and 989-996 (Log0, complex,
@@ -574,7 +651,7 @@ static void centre_phase(const msk_utr *p, double angleY, double angleZ, double 
 typedef struct {
     const msk_utr *p;
     const mo_utr_geom *g;
-    const double *angles;
+    const double *angles, *zrot, *shifts;
     const float *images;
     int a0, a1;
     double *v3, *samp3;
@@ -586,10 +663,28 @@ static void *grid_worker(void *arg)
     const mo_utr_geom *g = J->g;
     const int nx = g->nx, ny = g->ny;
     double *k2 = (double *)malloc(sizeof(double) * 2 * (size_t)nx * ny);
+    double *nv = (double *)malloc(sizeof(double) * (size_t)nx * ny);
     const int rotshift = J->p->dxc != 0 || J->p->dyc != 0 || J->p->dzc != 0;
+    const double cx = (g->xc - g->xlo) / g->xst, cy = (g->yc - g->ylo) / g->xst;
     for (int a = J->a0; a < J->a1; a++) {
         const double angleZ = J->angles[2 * a] * kPi / 180.0, angleY = J->angles[2 * a + 1] * kPi / 180.0;
-        mo_utr_k2four_f64(J->images + (size_t)a * nx * ny, nx, ny, J->p->f1, J->p->f2, k2);
+        const double z2 = J->zrot ? J->zrot[a] : 0.0;
+        const double shx = J->shifts ? J->shifts[2 * a] : 0.0, shy = J->shifts ? J->shifts[2 * a + 1] : 0.0;
+        if (z2 != 0.0 || shx != 0.0 || shy != 0.0) {
+            /* UTR.cpp:940-948 then 920-940: normalise, shift and rotate back */
+            const float *im = J->images + (size_t)a * nx * ny;
+            for (size_t q = 0; q < (size_t)nx * ny; q++) {
+                double v = im[q];
+                if (J->p->f1 != 1.0) v /= J->p->f1;
+                if (J->p->f2 != 0.0) v += J->p->f2;
+                nv[q] = v < 0.0 ? 0.0 : v;
+            }
+            mo_utr_image_plane_f64(nv, nx, ny, cx, cy, -z2 * kPi / 180.0,
+                                   (long)floor(-shx / g->xst + 0.5), (long)floor(-shy / g->xst + 0.5));
+            k2four_from_norm(k2, nv, nx, ny);
+        } else {
+            mo_utr_k2four_f64(J->images + (size_t)a * nx * ny, nx, ny, J->p->f1, J->p->f2, k2);
+        }
         double fd[3];
         float ff[6];
         centre_phase(J->p, angleY, angleZ, fd, ff);
@@ -597,6 +692,7 @@ static void *grid_worker(void *arg)
                         (float)g->fylo, (float)g->fyst, (float)g->fzlo, (float)g->fzst, fd, g->wl,
                         rotshift, J->p->escc, J->v3, J->samp3);
     }
+    free(nv);
     free(k2);
     return NULL;
 }
@@ -693,11 +789,10 @@ static void c2r3_f64(const double *v3, int nx, int ny, int nz, double *out)
     free(hs);
 }
 
-int mo_utr_finish_f64(const msk_utr *p, int nangles, const double *angles,
-                      const double *defocus, double *v3, const double *samp3, double *volume)
+static int utr_finish_geom(const msk_utr *p, const mo_utr_geom *gp, double *v3,
+                           const double *samp3, double *volume)
 {
-    mo_utr_geom g;
-    if (mo_utr_geom_make(p, nangles, angles, defocus, &g)) return -1;
+    const mo_utr_geom g = *gp;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     normalise_f64(p, &g, v3, samp3);
     /* UTR.cpp:1177-1201 */
@@ -756,12 +851,23 @@ int mo_utr_finish_f64(const msk_utr *p, int nangles, const double *angles,
     return 0;
 }
 
-int mo_utr_reconstruct_f64(const msk_utr *p, int nangles, const double *angles,
-                           const double *defocus, const float *images, double *volume,
-                           int nthreads)
+int mo_utr_finish_f64(const msk_utr *p, int nangles, const double *angles,
+                      const double *defocus, double *v3, const double *samp3, double *volume)
 {
     mo_utr_geom g;
     if (mo_utr_geom_make(p, nangles, angles, defocus, &g)) return -1;
+    return utr_finish_geom(p, &g, v3, samp3, volume);
+}
+
+int mo_utr_reconstruct_f64(const msk_utr *p, int nangles, const double *angles,
+                           const double *defocus, const double *zrot, const double *shifts,
+                           const float *images, double *volume, int nthreads)
+{
+    mo_utr_geom g;
+    if (mo_utr_geom_make(p, nangles, angles, defocus, &g)) return -1;
+    if (zrot) /* UTR.cpp:221: a Z'' rotation (from the second orientation on) */
+        for (int i = 1; i < nangles; i++)
+            if (zrot[i] != 0) g.rot_y_only = g.rot_z_only = 0;
     if (p->ctf_mode == 1 || p->ctf_mode == 3) return -1; /* XArrayLibrary's 2D filters */
     const size_t nv = (size_t)g.nx * g.ny * g.nz;
     if (nthreads < 1) nthreads = 1;
@@ -772,6 +878,8 @@ int mo_utr_reconstruct_f64(const msk_utr *p, int nangles, const double *angles,
         jobs[t].p = p;
         jobs[t].g = &g;
         jobs[t].angles = angles;
+        jobs[t].zrot = zrot;
+        jobs[t].shifts = shifts;
         jobs[t].images = images;
         jobs[t].a0 = (int)((long)nangles * t / nthreads);
         jobs[t].a1 = (int)((long)nangles * (t + 1) / nthreads);
@@ -787,7 +895,7 @@ int mo_utr_reconstruct_f64(const msk_utr *p, int nangles, const double *angles,
         free(jobs[t].v3);
         free(jobs[t].samp3);
     }
-    const int st = mo_utr_finish_f64(p, nangles, angles, defocus, v3, samp3, volume);
+    const int st = utr_finish_geom(p, &g, v3, samp3, volume);
     free(v3);
     free(samp3);
     free(jobs);

@@ -78,10 +78,18 @@ int mo_utr_invlap3d_f64(double *v3, int nx, int ny, int nz, double zaper, double
  * an FFTW-style complex-to-real inverse 3D FFT of the half spectrum, the
  * sphere mask and the output scale.  volume: double [nz][ny][nx].
  * nthreads: host threads for the gridding (its sums are per-thread partial
- * volumes added in thread order, so the result does not depend on timing). */
+ * volumes added in thread order, so the result does not depend on timing).
+ * zrot, shifts (may be NULL): the Z'' rotation (degrees) and the x, y shift
+ * of each image, undone before its spectrum (UTR.cpp:920-940). */
 int mo_utr_reconstruct_f64(const msk_utr *p, int nangles, const double *angles,
-                           const double *defocus, const float *images, double *volume,
-                           int nthreads);
+                           const double *defocus, const double *zrot, const double *shifts,
+                           const float *images, double *volume, int nthreads);
+
+/* UTR.cpp:920-940 on a normalised image [ny][nx] (definitions in the
+ * utr_oracle.c header): zrot (degrees, may be NULL) and shifts ([n][2] x, y,
+ * may be NULL) in mo_utr_reconstruct_f64 select it per image. */
+void mo_utr_image_plane_f64(double *img, int nx, int ny, double cx, double cy, double t,
+                            long dx, long dy);
 
 /* Only the Fourier-space and output stages of mo_utr_reconstruct_f64, from
  * gridded sums: v3 complex, samp3 [nz][ny][nx] (v3 is overwritten). */

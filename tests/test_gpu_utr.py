@@ -117,3 +117,23 @@ def test_reconstruction_errors(ctx, msk):
         assert e.value.status == status, kw
     # flat images: log 1 = 0 everywhere
     assert not ctx.utr_reconstruct(p, ang, df, imgs).any()
+
+
+def test_reconstruction_with_image_planes_matches_oracle(ctx, msk, oracle):
+    # Z'' rotations and shifts of the input images, undone before the spectra
+    p = uc.params(nx=64, ny=64, nz=32, ctf_mode=4, escc=1, dxc=0.4, dyc=-0.3)
+    na = 24
+    ang = uc.tilt_angles(na)
+    df = np.full(na, 70.0)
+    imgs = uc.images(p, na, seed=31)
+    zrot = np.linspace(-25.0, 25.0, na)
+    shifts = np.stack([np.linspace(-1.6, 1.6, na), np.linspace(0.9, -0.9, na)], axis=1)
+    want = oracle.utr_reconstruct(p, ang, df, imgs, nthreads=8, zrot=zrot, shifts=shifts)
+    got = ctx.utr_reconstruct(as_msk(msk, p), ang, df, imgs, zrot=zrot, shifts=shifts)
+    assert rel_l2(got, want) <= 1e-4
+    plain = ctx.utr_reconstruct(as_msk(msk, p), ang, df, imgs)
+    assert rel_l2(plain, want) > 1e-3  # the planes change the reconstruction
+    # shifts alone (no rotation) take the whole-pixel path
+    want_s = oracle.utr_reconstruct(p, ang, df, imgs, nthreads=8, shifts=shifts)
+    got_s = ctx.utr_reconstruct(as_msk(msk, p), ang, df, imgs, shifts=shifts)
+    assert rel_l2(got_s, want_s) <= 1e-4

@@ -155,3 +155,48 @@ def test_library_depth_matches_oracle(msk, oracle):
         assert L.msk_utr_depth(u) == oracle.utr_geom(p, [[0, 0]], [0.0]).nz
     bad = msk.Utr(nx=32, ny=32, xst=0.0, zlo=-1.0, zhi=1.0, wl=0.02)
     assert L.msk_utr_depth(bad) == -8
+
+
+def test_image_plane_definitions(oracle):
+    L = oracle.L
+    import ctypes as C
+    L.mo_utr_image_plane_f64.argtypes = [np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS"),
+                                         C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                         C.c_long, C.c_long]
+    rng = np.random.default_rng(4)
+    img = 1.0 + 0.1 * rng.standard_normal((24, 32))
+    edge = np.ones_like(img, bool)
+    edge[5:-5, 5:-5] = False
+    f = img[edge].mean()
+    # a pure shift: whole pixels, the edge mean coming in
+    a = img.copy()
+    L.mo_utr_image_plane_f64(a, 32, 24, 16.0, 12.0, 0.0, 3, -2)
+    assert np.array_equal(a[:22, 3:], img[2:, :29])
+    assert np.allclose(a[:, :3], f, rtol=1e-14) and np.allclose(a[22:], f, rtol=1e-14)
+    # a rotation by t then -t about the same centre: a smooth interior comes back
+    y, x = np.mgrid[0:24, 0:32]
+    sm = 1.0 + 0.2 * np.exp(-((x - 14.0) ** 2 + (y - 11.0) ** 2) / 18.0)
+    b = sm.copy()
+    L.mo_utr_image_plane_f64(b, 32, 24, 16.0, 12.0, 0.3, 0, 0)
+    assert np.abs(b - sm).max() > 1e-2
+    L.mo_utr_image_plane_f64(b, 32, 24, 16.0, 12.0, -0.3, 0, 0)
+    assert np.abs(b - sm)[8:16, 10:22].max() < 0.05 * np.abs(sm - 1).max()
+    # a quarter turn of the sample grid is exact away from the edges
+    sq = 1.0 + 0.1 * rng.standard_normal((32, 32))
+    c = sq.copy()
+    L.mo_utr_image_plane_f64(c, 32, 32, 16.0, 16.0, np.pi / 2, 0, 0)
+    # out(i, j) = in(c + R(-t)(p - c)): for t = pi/2, x' = cx + (j - cy), y' = cy - (i - cx)
+    j, i = 20, 10
+    assert abs(c[j, i] - sq[int(16 - (i - 16)), int(16 + (j - 16))]) < 1e-9
+
+
+def test_zero_planes_equal_plain_reconstruction(oracle):
+    p = uc.params(nx=32, ny=32, nz=16)
+    ang = uc.tilt_angles(8)
+    df = np.full(8, 40.0)
+    imgs = uc.images(p, 8, seed=9)
+    a = oracle.utr_reconstruct(p, ang, df, imgs)
+    b = oracle.utr_reconstruct(p, ang, df, imgs, zrot=np.zeros(8), shifts=np.zeros((8, 2)))
+    assert np.array_equal(a, b)
+    c = oracle.utr_reconstruct(p, ang, df, imgs, zrot=np.linspace(0, 20, 8))
+    assert rel_l2(c, a) > 1e-3

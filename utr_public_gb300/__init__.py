@@ -29,7 +29,8 @@ EXPORTS = ("msk_create", "msk_destroy", "msk_last_error", "msk_status_string", "
            "msk_profile_read", "msk_calculate_static", "msk_tilt_series_per_angle",
            "msk_stack_images", "msk_adjoint", "msk_potential_stack", "msk_tilt_series_batch",
            "msk_write_grd", "msk_write_grc", "msk_write_tiff32", "msk_read_orientations",
-           "msk_tilt_series_planes", "msk_utr_depth", "msk_utr_reconstruct", "msk_utr_grid",
+           "msk_tilt_series_planes", "msk_utr_depth", "msk_utr_reconstruct",
+           "msk_utr_reconstruct_planes", "msk_utr_grid",
            "msk_utr_ctf_correction3d", "msk_utr_inverse_mlaplacian3d")
 MSK_BATCH_GRAPH = 1
 
@@ -166,6 +167,8 @@ def load():
                                         vp, vp, vp]
     L.msk_utr_depth.argtypes = [C.POINTER(Utr)]
     L.msk_utr_reconstruct.argtypes = [vp, C.POINTER(Utr), C.c_int, _dp, _dp, vp, vp]
+    L.msk_utr_reconstruct_planes.argtypes = [vp, C.POINTER(Utr), C.c_int, _dp, _dp, vp, vp, vp,
+                                             vp]
     L.msk_utr_grid.argtypes = [vp, C.POINTER(Utr), C.c_int, _dp, vp, vp, vp]
     L.msk_utr_ctf_correction3d.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int] + \
         [C.c_double] * 13 + [C.c_int]
@@ -483,19 +486,28 @@ class Context:
             raise MskError(nz, "bad UTR geometry")
         return nz
 
-    def utr_reconstruct(self, utr, angles, defocus, images, volume=None):
+    def utr_reconstruct(self, utr, angles, defocus, images, volume=None, zrot=None, shifts=None):
         """3D potential (TEM) or beta (X-ray) [nz, ny, nx] from one defocused
-        image per orientation (msk_utr_reconstruct).  angles [nangles, 2]: Z
-        and Y' rotations in degrees; defocus [nangles]; images [nangles, ny,
-        nx] (x fastest, flat-field corrected); images / volume may be torch
-        CUDA tensors."""
+        image per orientation (msk_utr_reconstruct, or msk_utr_reconstruct_planes
+        with zrot / shifts).  angles [nangles, 2]: Z and Y' rotations in degrees;
+        defocus [nangles]; zrot [nangles] Z'' angles in degrees and shifts
+        [nangles, 2] x, y image shifts, undone first; images [nangles, ny, nx]
+        (x fastest, flat-field corrected); images / volume may be torch CUDA
+        tensors."""
         ang = np.ascontiguousarray(angles, np.float64).reshape(-1, 2)
         defocus = np.ascontiguousarray(defocus, np.float64)
         images = self._f32(images)
         if volume is None:
             volume = np.zeros((self.utr_depth(utr), utr.ny, utr.nx), np.float32)
-        st = self.L.msk_utr_reconstruct(self.h, C.byref(utr), len(ang), ang.reshape(-1),
-                                        defocus, _ptr(images), _ptr(volume))
+        if zrot is None and shifts is None:
+            st = self.L.msk_utr_reconstruct(self.h, C.byref(utr), len(ang), ang.reshape(-1),
+                                            defocus, _ptr(images), _ptr(volume))
+        else:
+            zr = None if zrot is None else np.ascontiguousarray(zrot, np.float64)
+            sh = None if shifts is None else np.ascontiguousarray(shifts, np.float64).reshape(-1)
+            st = self.L.msk_utr_reconstruct_planes(self.h, C.byref(utr), len(ang),
+                                                   ang.reshape(-1), defocus, _ptr(zr), _ptr(sh),
+                                                   _ptr(images), _ptr(volume))
         self._check(st)
         return volume
 

@@ -81,7 +81,7 @@ struct msk_context {
     msk::DevBuf dwbuf;                                // Debye-Waller -B/4 per (unit, slice)
     msk::DevBuf imgfill;                              // image-plane fill values per unit
     msk::DevBuf tune;                                 // scratch grid of the column tuner
-    msk::DevBuf utr_img, utr_k2, utr_acc, utr_vol, utr_out, utr_tab;  // UTR reconstruction
+    msk::DevBuf utr_img, utr_k2, utr_acc, utr_vol, utr_out, utr_tab, utr_stage;  // UTR reconstruction
     bool no_tune = false;                             // column tiles fixed at variant 0
     std::vector<cudaStream_t> lanes;                  // concurrent specimens of a batch
     std::vector<cudaEvent_t> lane_ev;                 // lane joins (one per lane) + fork

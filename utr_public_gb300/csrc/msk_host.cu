@@ -1363,7 +1363,7 @@ void msk_destroy(msk_context *ctx)
                       &ctx->stk_v, &ctx->stk_g, &ctx->stk_t, &ctx->stk_img, &ctx->stk_part,
                       &ctx->adjtab, &ctx->arena, &ctx->dwbuf, &ctx->imgfill, &ctx->tune,
                       &ctx->utr_img, &ctx->utr_k2, &ctx->utr_acc, &ctx->utr_vol, &ctx->utr_out,
-                      &ctx->utr_tab})
+                      &ctx->utr_tab, &ctx->utr_stage})
         b->release();
     for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_join, ctx->ev_t[0], ctx->ev_t[1], ctx->ev_free[0],
                           ctx->ev_free[1]})

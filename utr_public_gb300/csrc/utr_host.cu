@@ -133,6 +133,119 @@ __global__ void __launch_bounds__(256) k_utr_grid(const UtrGridP p)
     }
 }
 
+// ------------------------------------------------------------------ input image plane
+// UTR.cpp:920-950 for images with a Z'' rotation or a shift: the normalised
+// image (input / f1 + f2, negatives to 0), its edge mean (NormAverEdge(5)),
+// the shift by whole pixels, then the rotation back by -Z'' (XArray2DMove,
+// XArray2DSpln::Rotate; XArrayLibrary is not part of the reference, so these
+// are this library's definitions, those of MsctKirkland's image plane):
+//   shift:  s(j, i) = v(j - dy, i - dx), the edge mean outside;
+//   rotate: out(p) = s(c + R(-t)(p - c)), t = -Z'', Catmull-Rom bicubic on
+//           (x, y) = (i, j), the edge mean outside, c the rotation centre.
+struct UtrPlaneP {
+    int nx, ny, nimg;
+    float f1, f2;
+    int use_f1, use_f2;
+    double cx, cy;          // rotation centre in pixels
+    const double *par;      // [nimg][4]: cos t, sin t, dx, dy
+    const int *op;          // [nimg]: 0 none, 1 shift only, 2 rotate (and shift)
+    const float *fill;      // [nimg] edge means
+};
+
+__device__ __forceinline__ float utr_norm(const UtrPlaneP &p, float v)
+{
+    if (p.use_f1) v = __fdiv_rn(v, p.f1);
+    if (p.use_f2) v = __fadd_rn(v, p.f2);
+    return v < 0.0f ? 0.0f : v;
+}
+
+// One CTA per image: the mean of the normalised pixels within 5 of an edge.
+__global__ void __launch_bounds__(256) k_utr_edge_mean(const UtrPlaneP p, const float *__restrict__ img,
+                                                       float *__restrict__ fill)
+{
+    const int a = blockIdx.x;
+    if (!p.op[a]) return;
+    const float *src = img + (size_t)a * p.nx * p.ny;
+    double sum = 0.0;
+    long long cnt = 0;
+    for (int q = threadIdx.x; q < p.nx * p.ny; q += blockDim.x) {
+        const int j = q / p.nx, i = q - j * p.nx;
+        if (i < 5 || i >= p.nx - 5 || j < 5 || j >= p.ny - 5) {
+            sum += utr_norm(p, src[q]);
+            cnt++;
+        }
+    }
+    __shared__ double s_sum[256];
+    __shared__ long long s_cnt[256];
+    s_sum[threadIdx.x] = sum;
+    s_cnt[threadIdx.x] = cnt;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            s_sum[threadIdx.x] += s_sum[threadIdx.x + o];
+            s_cnt[threadIdx.x] += s_cnt[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) fill[a] = s_cnt[0] ? (float)(s_sum[0] / (double)s_cnt[0]) : 0.0f;
+}
+
+__device__ __forceinline__ float cr_weight_f(float t, int k)
+{
+    // Catmull-Rom weights of the samples at -1, 0, 1, 2 for a fraction t
+    const float t2 = t * t, t3 = t2 * t;
+    switch (k) {
+    case 0: return 0.5f * (-t3 + 2.0f * t2 - t);
+    case 1: return 0.5f * (3.0f * t3 - 5.0f * t2 + 2.0f);
+    case 2: return 0.5f * (-3.0f * t3 + 4.0f * t2 + t);
+    default: return 0.5f * (t3 - t2);
+    }
+}
+
+// Normalised images with their plane operations into `out` (every image).
+__global__ void k_utr_img_plane(const UtrPlaneP p, const float *__restrict__ img,
+                                float *__restrict__ out)
+{
+    const size_t plane = (size_t)p.nx * p.ny;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < plane * p.nimg;
+         q += (size_t)gridDim.x * blockDim.x) {
+        const int a = (int)(q / plane);
+        const int r = (int)(q - (size_t)a * plane);
+        const int j = r / p.nx, i = r - j * p.nx;
+        const float *src = img + (size_t)a * plane;
+        const int op = p.op[a];
+        if (!op) {
+            out[q] = utr_norm(p, src[r]);
+            continue;
+        }
+        const double *pr = p.par + 4 * (size_t)a;
+        const long dx = (long)pr[2], dy = (long)pr[3];
+        const float f = p.fill[a];
+        // the shifted image s at (yy, xx), the edge mean outside
+        auto sval = [&](long yy, long xx) -> float {
+            if (yy < 0 || yy >= p.ny || xx < 0 || xx >= p.nx) return f;
+            const long sy = yy - dy, sx = xx - dx;
+            if (sy < 0 || sy >= p.ny || sx < 0 || sx >= p.nx) return f;
+            return utr_norm(p, src[(size_t)sy * p.nx + sx]);
+        };
+        if (op == 1) {
+            out[q] = sval(j, i);
+            continue;
+        }
+        const double c = pr[0], sn = pr[1];
+        const double ddx = i - p.cx, ddy = j - p.cy;
+        const double fx = p.cx + c * ddx + sn * ddy, fy = p.cy - sn * ddx + c * ddy;  // R(-t)
+        const long x0 = (long)floor(fx), y0 = (long)floor(fy);
+        const float tx = (float)(fx - x0), ty = (float)(fy - y0);
+        float acc = 0.0f;
+        for (int b = 0; b < 4; b++) {
+            const float wy = cr_weight_f(ty, b);
+            for (int e = 0; e < 4; e++) acc += cr_weight_f(tx, e) * wy * sval(y0 - 1 + b, x0 - 1 + e);
+        }
+        out[q] = acc;
+    }
+}
+
 // gridding sums -> the caller's V3, Samp3 (msk_utr_grid)
 __global__ void k_utr_acc_split(const UtrAcc *__restrict__ acc, size_t n, float2 *__restrict__ v3,
                                 float *__restrict__ samp3)
@@ -196,7 +309,7 @@ int depth_of(const msk_utr *p, double *zlo_out, double *zhi_out)
 }
 
 int make_geo(msk_context *ctx, const msk_utr *p, int nangles, const double *angles,
-             const double *defocus, Geo &g)
+             const double *defocus, Geo &g, const double *zrot = nullptr)
 {
     const int nz = depth_of(p, &g.zlo, &g.zhi);
     if (nz < 0) return fail(ctx, MSK_EINVAL, "bad UTR geometry (pixel size, sizes or z range)");
@@ -243,6 +356,9 @@ int make_geo(msk_context *ctx, const msk_utr *p, int nangles, const double *angl
     }
     zav /= nangles;
     g.zout = zav - p->dzextra;
+    if (zrot)  // UTR.cpp:221: a Z'' rotation (from the second orientation on)
+        for (int i = 1; i < nangles; i++)
+            if (zrot[i] != 0) g.rot_y_only = g.rot_z_only = false;
     return MSK_OK;
 }
 
@@ -574,13 +690,21 @@ int msk_utr_depth(const msk_utr *p) { return depth_of(p, nullptr, nullptr); }
 int msk_utr_reconstruct(msk_context *ctx, const msk_utr *p, int nangles, const double *angles,
                         const double *defocus, const float *images, float *volume)
 {
+    return msk_utr_reconstruct_planes(ctx, p, nangles, angles, defocus, nullptr, nullptr, images,
+                                      volume);
+}
+
+int msk_utr_reconstruct_planes(msk_context *ctx, const msk_utr *p, int nangles,
+                               const double *angles, const double *defocus, const double *zrot,
+                               const double *shifts, const float *images, float *volume)
+{
     if (!ctx) return MSK_EINVAL;
     ctx->err.clear();
     int st = check_params(ctx, p, nangles, angles, defocus);
     if (st) return st;
     if (!images || !volume) return fail(ctx, MSK_EINVAL, "null image or volume pointer");
     Geo g{};
-    st = make_geo(ctx, p, nangles, angles, defocus, g);
+    st = make_geo(ctx, p, nangles, angles, defocus, g, zrot);
     if (st) return st;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     if (!sizes_ok(nx) || !sizes_ok(ny) || !sizes_ok(nz))
@@ -649,7 +773,27 @@ int msk_utr_reconstruct(msk_context *ctx, const msk_utr *p, int nangles, const d
     std::vector<float2> twx, twy, twz;
     if (!twiddles(nx, twx) || !twiddles(ny, twy) || !twiddles(nz, twz))
         return fail(ctx, MSK_EUNSUPPORTED, "no FFT for this size");
+    // input image planes (UTR.cpp:920-940): per image the operation, cos and
+    // sin of t = -Z'', and the whole-pixel shift back
+    std::vector<int> pop(nangles, 0);
+    std::vector<double> ppar(4 * (size_t)nangles, 0.0);
+    bool any_plane = false;
+    for (int a = 0; a < nangles; a++) {
+        const double z2 = zrot ? zrot[a] : 0.0;
+        const double shx = shifts ? shifts[2 * a] : 0.0, shy = shifts ? shifts[2 * a + 1] : 0.0;
+        if (z2 == 0.0 && shx == 0.0 && shy == 0.0) continue;
+        const double t = -z2 * kPi / 180.0;
+        pop[a] = z2 != 0.0 ? 2 : 1;
+        ppar[4 * a] = cos(t);
+        ppar[4 * a + 1] = sin(t);
+        ppar[4 * a + 2] = floor(-shx / p->xst + 0.5);
+        ppar[4 * a + 3] = floor(-shy / p->xst + 0.5);
+        any_plane = true;
+    }
     TabPack pk;
+    const size_t o_pop = pk.put(pop), o_ppar = pk.put(ppar);
+    std::vector<float> fill0(nangles, 0.0f);
+    const size_t o_fill = pk.put(fill0);
     const size_t o_twx = pk.put(twx), o_twy = pk.put(twy), o_twz = pk.put(twz);
     const CorrOffsets oc = put_corr(pk, ct, nx, ny, nz);
     const size_t o_mx = pk.put(mx), o_my = pk.put(my), o_mz = pk.put(mz);
@@ -669,7 +813,35 @@ int msk_utr_reconstruct(msk_context *ctx, const msk_utr *p, int nangles, const d
         if ((st = upload(ctx, ctx->utr_img.p, images, sizeof(float) * plane * nangles))) return st;
         img_d = ctx->utr_img.as<float>();
     }
-    if ((st = spectra(ctx, p, nangles, img_d, tw_x, tw_y))) return st;
+    if (any_plane) {
+        UtrPlaneP pp{};
+        pp.nx = nx;
+        pp.ny = ny;
+        pp.nimg = nangles;
+        pp.f1 = (float)p->f1;
+        pp.f2 = (float)p->f2;
+        pp.use_f1 = p->f1 != 1.0;
+        pp.use_f2 = p->f2 != 0.0;
+        pp.cx = (((g.xhi + g.xlo) / 2.0 + p->dxc) - g.xlo) / p->xst;
+        pp.cy = (((g.yhi + g.ylo) / 2.0 + p->dyc) - g.ylo) / p->xst;
+        pp.par = reinterpret_cast<const double *>(tb + o_ppar);
+        pp.op = reinterpret_cast<const int *>(tb + o_pop);
+        float *fill = reinterpret_cast<float *>(tb + o_fill);
+        pp.fill = fill;
+        MSK_CUDA(ctx, ctx->utr_stage.reserve(sizeof(float) * plane * nangles));
+        float *staged = ctx->utr_stage.as<float>();
+        {
+            Prof pr(ctx, kUtrPoint, 8.0 * plane * nangles);
+            k_utr_edge_mean<<<nangles, 256, 0, ctx->stream>>>(pp, img_d, fill);
+            k_utr_img_plane<<<grid_blocks(plane * nangles), 256, 0, ctx->stream>>>(pp, img_d, staged);
+        }
+        msk_utr q = *p;  // the staged images are normalised
+        q.f1 = 1.0;
+        q.f2 = 0.0;
+        if ((st = spectra(ctx, &q, nangles, staged, tw_x, tw_y))) return st;
+    } else if ((st = spectra(ctx, p, nangles, img_d, tw_x, tw_y))) {
+        return st;
+    }
     MSK_CUDA(ctx, ctx->utr_acc.reserve(sizeof(UtrAcc) * nvox));
     UtrAcc *acc = ctx->utr_acc.as<UtrAcc>();
     MSK_CUDA(ctx, cudaMemsetAsync(acc, 0, sizeof(UtrAcc) * nvox, ctx->stream));
