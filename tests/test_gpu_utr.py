@@ -46,6 +46,29 @@ def test_gridding_sums_match_oracle(ctx, msk, oracle):
     assert np.abs(s3 - S).max() < 1e-5 * S.max()
 
 
+@pytest.mark.parametrize("escc", [0, 1])
+def test_tilt_series_gridding_matches_oracle(ctx, msk, oracle, escc):
+    # tilts about Y' alone take the per-plane tile form
+    p = uc.params(nx=128, ny=32, nz=64, escc=escc, dxc=0.3 * escc)
+    ang = uc.tilt_angles(37, span=185.0)
+    rng = np.random.default_rng(12 + escc)
+    k2 = rng.standard_normal((37, 32, 128, 2)).astype(np.float32)
+    v3, s3 = ctx.utr_grid(as_msk(msk, p), ang, k2)
+    g = oracle.utr_geom(p, ang, np.zeros(37))
+    fx = tuple(np.float32(v) for v in (g.fxlo, g.fxst, g.fylo, g.fyst, g.fzlo, g.fzst))
+    V = np.zeros((g.nz, 32, 128, 2))
+    S = np.zeros((g.nz, 32, 128))
+    for a, (az, ay) in enumerate(ang):
+        Y = np.deg2rad(ay)
+        fa = np.float32([2 * np.pi * p.dxc * (1 - np.cos(Y)), 0.0, -2 * np.pi * p.dxc * np.sin(Y)])
+        fc = np.zeros(6, np.float32)
+        fc[1::2] = -fa
+        oracle.utr_grid(k2[a], g.nz, Y, 0.0, fx, fc, WL, escc, escc, mode="acc64", v3=V, samp3=S)
+    assert (S > 0).sum() > 10000
+    assert rel_l2(s3, S) < 1e-6
+    assert rel_l2(v3, V) < 1e-6
+
+
 def test_ctf_and_laplacian_match_reference_restatement(ctx, oracle):
     rng = np.random.default_rng(5)
     v = rng.standard_normal((16, 32, 64, 2)).astype(np.float32)
