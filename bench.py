@@ -310,12 +310,13 @@ def run_adjoint(args, rank, world, local_rank):
     hg = torch.empty(v.shape, dtype=torch.float32, pin_memory=True)
     k_e2e = max(1, min(args.steps, 2))
     ctx.adjoint(st, hv, rp, ht, grad=hg)
-    ctx.profile(True)
     ms_e2e = timed(lambda: ctx.adjoint(st, hv, rp, ht, grad=hg), k_e2e)
+    ctx.profile(True)  # the copied bytes, from one more call (not the timed ones)
+    ctx.adjoint(st, hv, rp, ht, grad=hg)
     prof_e2e = ctx.profile_read()
     ctx.profile(False)
-    h2d = prof_e2e.get("copy_h2d", (0, 0.0, 0.0))[2] / k_e2e
-    d2h = prof_e2e.get("copy_d2h", (0, 0.0, 0.0))[2] / k_e2e
+    h2d = prof_e2e.get("copy_h2d", (0, 0.0, 0.0))[2]
+    d2h = prof_e2e.get("copy_d2h", (0, 0.0, 0.0))[2]
     same = bool(torch.equal(hg, grad.cpu())) if rank == 0 else None
     kernels = {k: x for k, x in prof.items() if not k.startswith("copy_")}
     launches = int(sum(x[0] for x in kernels.values())) * args.steps
@@ -503,13 +504,16 @@ def run_utr(args, rank, world, local_rank):
     hvol = torch.empty(vol.shape, dtype=torch.float32, pin_memory=True)
     k_e2e = max(1, min(args.steps, 2))
     ctx.utr_reconstruct(u, ang, df, himg, volume=hvol)
-    ctx.profile(True)
     ms_e2e = timed(lambda: ctx.utr_reconstruct(u, ang, df, himg, volume=hvol), k_e2e)
+    ctx.profile(True)  # the copied bytes, from one more call (not the timed ones)
+    ctx.utr_reconstruct(u, ang, df, himg, volume=hvol)
     prof_e2e = ctx.profile_read()
     ctx.profile(False)
-    h2d = prof_e2e.get("copy_h2d", (0, 0.0, 0.0))[2] / k_e2e
-    d2h = prof_e2e.get("copy_d2h", (0, 0.0, 0.0))[2] / k_e2e
-    same = bool(torch.equal(hvol, vol.cpu())) if rank == 0 else None
+    h2d = prof_e2e.get("copy_h2d", (0, 0.0, 0.0))[2]
+    d2h = prof_e2e.get("copy_d2h", (0, 0.0, 0.0))[2]
+    # the gridding sums are float atomics: equal to the device run to rounding
+    same = (float(torch.linalg.vector_norm(hvol - vol.cpu()) / torch.linalg.vector_norm(hvol))
+            < 1e-6) if rank == 0 else None
     kernels = {k: x for k, x in prof.items() if not k.startswith("copy_")}
     launches = int(sum(x[0] for x in kernels.values())) * args.steps
     dom = max(kernels, key=lambda k: kernels[k][1])
@@ -633,12 +637,12 @@ def run_uneven(args, rank, world, local_rank):
     ctx.profile(False)
     kernels = {k: x for k, x in prof.items() if not k.startswith("copy_")}
     launches = int(sum(x[0] for x in kernels.values())) * args.steps
-    # end to end: host images
-    host = [np.zeros(tuple(t.shape), np.float32) for t in imgs]
+    # end to end: pinned host images
+    host = [torch.empty(tuple(t.shape), dtype=torch.float32, pin_memory=True) for t in imgs]
     t0 = time.perf_counter()
     ctx.tilt_series_batch(s, cases, defoci, graph=True, images=host)
     ms_e2e = 1000.0 * (time.perf_counter() - t0)
-    same = all(np.array_equal(h, d.cpu().numpy()) for h, d in zip(host, imgs))
+    same = all(torch.equal(h, d.cpu()) for h, d in zip(host, imgs))
     dom = max(kernels, key=lambda k: kernels[k][1])
     n_l, t_ms, nbytes = kernels[dom]
     peak, peak_kind = peaks()
@@ -678,7 +682,7 @@ def run_uneven(args, rank, world, local_rank):
         "streams_without_graph": {"ms": ms_streams, "value": total / (ms_streams / 1000.0)},
         "e2e": {"value": total / (ms_e2e / 1000.0), "unit": UNIT, "h2d_bytes_per_step":
                 int(prof.get("copy_h2d", (0, 0, 0))[2]),
-                "d2h_bytes_per_step": int(sum(h.nbytes for h in host)), "ms_per_step": ms_e2e,
+                "d2h_bytes_per_step": int(sum(h.numel() * 4 for h in host)), "ms_per_step": ms_e2e,
                 "matches_device_output": bool(same)},
         "gpu_launches": launches,
         "ms_per_step_serialized": ms_serial,
@@ -854,11 +858,11 @@ def run_phonon(args, rank, world, local_rank):
     n_l, t_ms, nbytes = kernels[dom]
     peak, peak_kind = peaks()
     achieved = (nbytes / n_l) / (t_ms / n_l / 1000.0) / 1e9
-    host = np.zeros((nang, 1, 1024, 1024), np.float32)
+    host = torch.empty((nang, 1, 1024, 1024), dtype=torch.float32, pin_memory=True)
     t0 = time.perf_counter()
     ctx.tilt_series(s, *atoms, angZ, angY, [0.0], nconfig=nconf, displacements=disp, images=host)
     ms_e2e = 1000.0 * (time.perf_counter() - t0)
-    same = bool(np.array_equal(host, img.cpu().numpy()))
+    same = bool(torch.equal(host, img.cpu()))
     if rank != 0:
         return
     err = None
@@ -889,7 +893,7 @@ def run_phonon(args, rank, world, local_rank):
                    "l2": "inputs larger than L2 (1920 waves, 46 GB of buffers)"},
         "e2e": {"value": world * total / (ms_e2e / 1000.0), "unit": UNIT,
                 "h2d_bytes_per_step": int(prof.get("copy_h2d", (0, 0, 0))[2]),
-                "d2h_bytes_per_step": int(host.nbytes), "ms_per_step": ms_e2e,
+                "d2h_bytes_per_step": int(host.numel() * 4), "ms_per_step": ms_e2e,
                 "matches_device_output": same},
         "gpu_launches": int(sum(x[0] for x in kernels.values())) * args.steps,
         "ms_per_step_serialized": ms_serial,
@@ -1048,16 +1052,19 @@ def main():
     prof = ctx.profile_read()
     ctx.profile(False)
 
-    # end to end: host buffers (pinned), copies inside the timed region
+    # end to end: host buffers (pinned), copies inside the timed region, the
+    # library's normal schedule; the copied bytes from one more, profiled call
+    # (profiling serialises the passes, so it is not the timed one)
     host_images = torch.empty((nang, len(defoci), NX, NX), dtype=torch.float32, pin_memory=True)
     step(host_images)
-    ctx.profile(True)
     ms_e2e = timed(host_images, max(1, min(args.steps, 3)))
+    ctx.profile(True)
+    step(host_images)
+    torch.cuda.synchronize()
     prof_e2e = ctx.profile_read()
     ctx.profile(False)
-    k_e2e = max(1, min(args.steps, 3))
-    h2d = prof_e2e.get("copy_h2d", (0, 0.0, 0.0))[2] / k_e2e
-    d2h = prof_e2e.get("copy_d2h", (0, 0.0, 0.0))[2] / k_e2e
+    h2d = prof_e2e.get("copy_h2d", (0, 0.0, 0.0))[2]
+    d2h = prof_e2e.get("copy_d2h", (0, 0.0, 0.0))[2]
     e2e_value = world * steps_per / (ms_e2e / 1000.0)
     if rank == 0:
         same = torch.equal(host_images, images.cpu())
