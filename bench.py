@@ -184,9 +184,9 @@ def fp64_error_job(result):
         result["error"] = repr(e)
 
 
-ADJ_NX, ADJ_FOV, ADJ_V0, ADJ_NANG, ADJ_CHECKPOINT = 512, 64.0, 200.0, 90, 8
+ADJ_NX, ADJ_FOV, ADJ_V0, ADJ_NANG, ADJ_CHECKPOINT = 512, 64.0, 200.0, 90, 0
 ADJ_METRIC = ("adjoint slice-steps/s (512², FP32, 64 slices x 90 orientations, forward + "
-              "checkpointed adjoint); dL/dv err vs FP64 adjoint and central differences")
+              "adjoint); dL/dv err vs FP64 adjoint and central differences")
 
 
 def adjoint_check(result, v, S, target, angles, nvox, rp):
@@ -220,7 +220,10 @@ def adjoint_check(result, v, S, target, angles, nvox, rp):
 def run_adjoint(args, rank, world, local_rank):
     """C5: per-orientation potential stacks of the plain specimen (splatted on
     the GPU), target images from the stacks perturbed by 1% Gaussian noise,
-    L = sum (I - T)^2 at one detector plane, dL/dv with checkpoints every 8
+    L = sum (I - T)^2 at one detector plane, dL/dv with every wave and transmission
+    of the forward pass kept in HBM (checkpoint 0: 264 MiB per orientation,
+    24.9 GB, no recomputation); with
+    --adj-checkpoint K a checkpoint every K
     slices.  One step = one msk_adjoint call over all 90 orientations."""
     import torch
     import utr_public_gb300 as msk
@@ -253,7 +256,7 @@ def run_adjoint(args, rank, world, local_rank):
     st = msk.Stack()
     st.nx = st.ny = ADJ_NX
     st.ax = st.by = ADJ_FOV
-    st.v0, st.deltaz, st.nslices, st.checkpoint = ADJ_V0, 1.0, S, ADJ_CHECKPOINT
+    st.v0, st.deltaz, st.nslices, st.checkpoint = ADJ_V0, 1.0, S, args.adj_checkpoint
     rp = np.array([0.0 - 0.5 * ADJ_FOV])  # detector defocus 0 from the box centre
     target = torch.empty((nang, 1, ADJ_NX, ADJ_NX), dtype=torch.float32, device="cuda")
     ctx.stack_images(st, vt, rp, images=target)
@@ -354,7 +357,10 @@ def run_adjoint(args, rank, world, local_rank):
         "config": {"workload": "adjoint: plain specimen (2000 atoms, 64 A box), 512^2, 64 "
                                "slices of 1 A, 200 keV, 90 orientations (2 deg about y), "
                                "potentials splatted on the GPU, target from v(1 + 0.01 N(0,1)), "
-                               "1 detector plane (defocus 0), checkpoint every 8 slices",
+                               "1 detector plane (defocus 0), " + (
+                                   "every wave and transmission kept (checkpoint 0)"
+                                   if args.adj_checkpoint == 0 else
+                                   "checkpoint every %d slices" % args.adj_checkpoint),
                    "slice_steps_per_step": steps_per * world,
                    "l2": "inputs larger than L2 (stacks 6.0 GB per GPU)"},
         "forward_only": {"value": world * steps_per / (ms_fwd / 1000.0), "unit": UNIT,
@@ -924,6 +930,9 @@ def main():
                          "1024^2; uneven: 64 specimens of uneven size in one graph; adjoint: "
                          "the 512^2 potential-stack adjoint over 90 orientations; utr: the UTR "
                          "reconstruction of the tilt series into a 1024^3 volume")
+    ap.add_argument("--adj-checkpoint", type=int, default=ADJ_CHECKPOINT,
+                    help="adjoint: slices per checkpoint (0: keep every wave and transmission "
+                         "when memory allows)")
     ap.add_argument("--fd-voxels", type=int, default=32,
                     help="central-difference voxels per checked orientation (adjoint)")
     ap.add_argument("--utr-n", type=int, default=NX,

@@ -262,9 +262,13 @@ int msk_tilt_series_per_angle(msk_context *ctx, const msk_series *s, int natom, 
  * propagator) with v_k supplied instead of splatted from atoms, from a plane
  * wave psi_0 = 1, then the free-space step of msk_tilt_series to each
  * detector plane and I = |psi|^2.  The adjoint returns dL/dv for the image
- * misfit L = sum over units, planes, pixels of (I - target)^2; its backward
- * pass keeps the wave every `checkpoint` slices and recomputes the waves
- * inside a block from its checkpoint.  The reference has no adjoint. */
+ * misfit L = sum over units, planes, pixels of (I - target)^2.  With
+ * checkpoint 0 the forward pass keeps every wave and transmission (2S + 4
+ * grids per unit) when at least min(nunits, 32) units fit in memory at once,
+ * and the backward pass recomputes nothing; otherwise (and with checkpoint
+ * K > 0) it keeps the wave every K slices (8 for checkpoint 0) and recomputes
+ * the waves inside a block from its checkpoint.  The reference has no
+ * adjoint. */
 typedef struct {
     int nx, ny;            /* grid */
     float ax, by;          /* cell size, Angstrom (param[pAX], param[pBY]) */
@@ -274,7 +278,7 @@ typedef struct {
     float aobj;            /* objective aperture semi-angle, rad (0: none) */
     double cs3, cs5;       /* spherical aberrations, Angstrom */
     int nslices;           /* slices per stack (>= 1) */
-    int checkpoint;        /* slices per checkpoint block of the adjoint (0: 8) */
+    int checkpoint;        /* slices per checkpoint block of the adjoint (0: keep all) */
     int max_batch;         /* units in flight at once (0: as many as memory allows) */
 } msk_stack;
 

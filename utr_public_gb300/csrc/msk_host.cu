@@ -2075,22 +2075,33 @@ int stack_run(msk_context *ctx, const StackJob &J)
 
     const size_t plane = (size_t)nx * ny;
     const size_t pb = plane * sizeof(float2);
-    const int K = adjoint ? (s->checkpoint > 0 ? std::min(s->checkpoint, S) : std::min(8, S)) : 1;
-    const int nblk = adjoint ? (S + K - 1) / K : 1;
-    // planes per unit: forward W, transmission B, free-space E (+ adjoint:
-    // checkpoints, the block's transmissions and waves, the wave gradient G)
-    const int planes = adjoint ? 3 + nblk + K + (K - 1) : 3;
     const bool v_dev = is_device_ptr(J.v);
     const bool g_dev = adjoint && is_device_ptr(J.grad);
     const bool t_dev = adjoint && is_device_ptr(J.target);
     const bool i_dev = !adjoint && ndef > 0 && is_device_ptr(J.images);
     const size_t vb = (size_t)S * plane * sizeof(float);      // one unit's stack
     const size_t ib = (size_t)ndef * plane * sizeof(float);   // one unit's images
-    const size_t per_unit = planes * pb + (v_dev ? 0 : vb) + (adjoint && !g_dev ? vb : 0) +
-                            (adjoint && !t_dev ? ib : 0) + (!adjoint && !i_dev ? ib : 0);
+    const size_t staged = (v_dev ? 0 : vb) + (adjoint && !g_dev ? vb : 0) +
+                          (adjoint && !t_dev ? ib : 0) + (!adjoint && !i_dev ? ib : 0);
     size_t free_b = 0, total_b = 0;
     MSK_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
     const size_t budget = std::min<size_t>(free_b / 2, (size_t)64 << 30);
+    // Adjoint with checkpoint 0: keep every wave and every transmission of the
+    // forward pass (2S + 3 planes a unit) when memory holds at least 32 units
+    // (or all of them) at once -- the backward pass then recomputes nothing;
+    // otherwise a checkpoint every K slices (8 by default) with the waves and
+    // transmissions of a block recomputed from its checkpoint.
+    const size_t keep_unit = (size_t)(2 * S + 3) * pb + staged;
+    const bool keep = adjoint && s->checkpoint == 0 &&
+                      budget / keep_unit >= (size_t)std::min(J.nunits, 32) &&
+                      (s->max_batch <= 0 || s->max_batch >= std::min(J.nunits, 32));
+    const int K = !adjoint ? 1 : keep ? 1 : (s->checkpoint > 0 ? std::min(s->checkpoint, S) : std::min(8, S));
+    const int nblk = adjoint ? (S + K - 1) / K : 1;
+    // planes per unit: forward W, transmission B, free-space E (+ adjoint:
+    // checkpoints, the block's transmissions and waves, the wave gradient G;
+    // keeping everything: the S + 1 waves and the S transmissions, G)
+    const int planes = keep ? 2 * S + 4 : adjoint ? 3 + nblk + K + (K - 1) : 3;
+    const size_t per_unit = planes * pb + staged;
     int B = (int)std::max<size_t>(1, std::min<size_t>(J.nunits, budget / per_unit));
     if (s->max_batch > 0) B = std::min(B, s->max_batch);
 
@@ -2098,8 +2109,13 @@ int stack_run(msk_context *ctx, const StackJob &J)
     float2 *base = ctx->stk.as<float2>();
     auto grid_at = [&](int i) { return base + (size_t)i * B * plane; };
     float2 *W = grid_at(0), *E = grid_at(1), *Bt = grid_at(2), *G = nullptr;
-    std::vector<float2 *> ck, Bb, Wb;
-    if (adjoint) {
+    std::vector<float2 *> ck, Bb, Wb, waves, trans;
+    if (keep) {
+        G = grid_at(2);
+        for (int k = 0; k <= S; k++) waves.push_back(grid_at(3 + k));          // W_0 .. W_S
+        for (int k = 1; k <= S; k++) trans.push_back(grid_at(3 + S + k));      // B_1 .. B_S
+        W = waves[S];  // the exit wave the free-space step reads
+    } else if (adjoint) {
         G = grid_at(2);
         for (int i = 0; i < nblk; i++) ck.push_back(grid_at(3 + i));
         for (int i = 0; i < K; i++) Bb.push_back(grid_at(3 + nblk + i));
@@ -2167,13 +2183,19 @@ int stack_run(msk_context *ctx, const StackJob &J)
         // the band-mode transmit stores only in-band row segments: every wave
         // buffer starts as zeros
         MSK_CUDA(ctx, cudaMemsetAsync(base, 0, (size_t)planes * B * pb, ctx->stream));
-        // forward: W_0 = S(1); checkpoints W_{bK} kept for the backward pass
-        float2 *w0 = adjoint ? ck[0] : W;
+        // forward: W_0 = S(1); checkpoints W_{bK} (or every wave and
+        // transmission) kept for the backward pass
+        float2 *w0 = keep ? waves[0] : adjoint ? ck[0] : W;
         {
             Prof p(ctx, kPlane, 8.0 * P * nb);
             k_plane_init<<<1024, 256, 0, ctx->stream>>>(w0, nullptr, nb, nx, ny);
         }
         for (int k = 1; k <= S; k++) {
+            if (keep) {
+                transmission(k, trans[k - 1]);
+                step(trans[k - 1], waves[k - 1], waves[k]);
+                continue;
+            }
             const float2 *in = (adjoint && (k - 1) % K == 0) ? ck[(k - 1) / K] : W;
             float2 *out = (adjoint && k % K == 0 && k < S) ? ck[k / K] : W;
             transmission(k, Bt);
@@ -2254,8 +2276,28 @@ int stack_run(msk_context *ctx, const StackJob &J)
 
         if (adjoint) {
             float *gd = g_dev ? J.grad + (size_t)u0 * S * plane : ctx->stk_g.as<float>();
+            // backward with every wave and transmission kept: slice by slice
+            for (int k = keep ? S : 0; k >= 1; k--) {
+                {
+                    Prof p(ctx, kKColProp, 16.0 * P * nb);  // g_u = K[conj p] g_psi
+                    cop->col_prop(gc, map_of(G, vprop), map_of(G, vprop), nullptr, nb, 0,
+                                  ctx->stream);
+                }
+                {
+                    Prof p(ctx, kAdjTransmit, 40.0 * P * nb);
+                    rop->row_adj_transmit(g, nb, G, trans[k - 1], waves[k - 1], ctx->stream);
+                }
+                {
+                    Prof p(ctx, kKColMask, 16.0 * P * nb);  // g_e = K[M] g_t
+                    cop->col_mask(g, map_of(trans[k - 1], vmask), map_of(trans[k - 1], vmask),
+                                  nullptr, nb, 0, ctx->stream);
+                }
+                Prof p(ctx, kGrad, 16.0 * P * nb);
+                rop->row_grad(g, nb, trans[k - 1], vslice(k), ustride,
+                              gd + (size_t)(k - 1) * plane, ctx->stream);
+            }
             // backward, one checkpoint block at a time from the last
-            for (int b = nblk - 1; b >= 0; b--) {
+            for (int b = keep ? -1 : nblk - 1; b >= 0; b--) {
                 const int k0 = b * K, nj = std::min(S, k0 + K) - k0;
                 for (int j = 1; j <= nj; j++) {  // recompute the block's t_k and psi_k
                     transmission(k0 + j, Bb[j - 1]);
