@@ -184,7 +184,7 @@ def fp64_error_job(result):
         result["error"] = repr(e)
 
 
-ADJ_NX, ADJ_FOV, ADJ_V0, ADJ_NANG, ADJ_CHECKPOINT = 512, 64.0, 200.0, 90, 0
+ADJ_NX, ADJ_FOV, ADJ_V0, ADJ_NANG, ADJ_CHECKPOINT = 512, 64.0, 200.0, 90, 8
 ADJ_METRIC = ("adjoint slice-steps/s (512², FP32, 64 slices x 90 orientations, forward + "
               "adjoint); dL/dv err vs FP64 adjoint and central differences")
 
@@ -220,11 +220,11 @@ def adjoint_check(result, v, S, target, angles, nvox, rp):
 def run_adjoint(args, rank, world, local_rank):
     """C5: per-orientation potential stacks of the plain specimen (splatted on
     the GPU), target images from the stacks perturbed by 1% Gaussian noise,
-    L = sum (I - T)^2 at one detector plane, dL/dv with every wave and transmission
-    of the forward pass kept in HBM (checkpoint 0: 264 MiB per orientation,
-    24.9 GB, no recomputation); with
-    --adj-checkpoint K a checkpoint every K
-    slices.  One step = one msk_adjoint call over all 90 orientations."""
+    L = sum (I - T)^2 at one detector plane, dL/dv with a checkpoint every 8
+    slices (--adj-checkpoint K: every K).  One step = one msk_adjoint call over
+    all 90 orientations.  `keep_all` times the same call with checkpoint 0, every
+    wave and transmission of the forward pass kept in HBM (264 MiB per
+    orientation, 24.9 GB) and nothing recomputed."""
     import torch
     import utr_public_gb300 as msk
     from utr_public_gb300 import specimen
@@ -297,6 +297,15 @@ def run_adjoint(args, rank, world, local_rank):
     loss_dev, _ = ctx.adjoint(st, v, rp, target, grad=grad)
     pick = [0, nang // 4]  # the orientations the oracle checks (0 and 44 degrees)
     g_dev = {a: grad[a].cpu().numpy() for a in pick}
+    keep_all = None
+    if args.adj_checkpoint != 0:  # the same call keeping every wave and transmission
+        st.checkpoint = 0
+        for _ in range(2):
+            step()
+        ms_keep = timed(step, args.steps)
+        st.checkpoint = args.adj_checkpoint
+        keep_all = {"value": world * steps_per / (ms_keep / 1000.0), "unit": UNIT,
+                    "ms_per_step": ms_keep, "checkpoint": 0}
     # forward alone (images of the same stacks)
     fimg = torch.empty_like(target)
     ms_fwd = timed(lambda: ctx.stack_images(st, v, rp, images=fimg), args.steps)
@@ -363,6 +372,7 @@ def run_adjoint(args, rank, world, local_rank):
                                    "checkpoint every %d slices" % args.adj_checkpoint),
                    "slice_steps_per_step": steps_per * world,
                    "l2": "inputs larger than L2 (stacks 6.0 GB per GPU)"},
+        "keep_all": keep_all,
         "forward_only": {"value": world * steps_per / (ms_fwd / 1000.0), "unit": UNIT,
                          "ms": ms_fwd, "adjoint_over_forward_time": ms / ms_fwd},
         "loss": loss_dev,
@@ -933,7 +943,7 @@ def main():
     ap.add_argument("--adj-checkpoint", type=int, default=ADJ_CHECKPOINT,
                     help="adjoint: slices per checkpoint (0: keep every wave and transmission "
                          "when memory allows)")
-    ap.add_argument("--fd-voxels", type=int, default=32,
+    ap.add_argument("--fd-voxels", type=int, default=256,
                     help="central-difference voxels per checked orientation (adjoint)")
     ap.add_argument("--utr-n", type=int, default=NX,
                     help="volume edge of the utr workload (images block-averaged to it)")

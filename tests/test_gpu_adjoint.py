@@ -3,15 +3,16 @@ msk_adjoint) against the FP64 oracle and central finite differences.
 
 Tolerances (relative L2):
   * images vs the FP64 oracle:                          1e-5
-  * dL/dv vs the FP64 oracle adjoint:                   2e-3
+  * dL/dv vs the FP64 oracle adjoint:                   1e-3
   * dL/dv vs central finite differences of the FP64
-    oracle loss, over the sampled voxels:               2e-3
+    oracle loss, over the sampled voxels:               1e-3
   * loss vs the FP64 oracle loss:                       1e-4
 dL/dv is linear in the residuals I - T.  A 1% perturbation of the potential
-moves the images by only ~1e-4..1e-3 of their value, while the FP32 forward
-pass leaves ~1e-6 relative error in I, so the residuals -- and dL/dv with
-them -- carry ~1e-3 relative error: the FP32 floor of this loss, measured
-at 0.7e-3..1.4e-3 on 64^2..256^2 grids with 10..64 slices.
+moves the images by only ~1e-4..1e-3 of their value, so the residuals carry
+the forward pass's error in I magnified by 1e3..1e4.  The stack path keeps
+its waves in the scattered form (psi = 1 + phi), which leaves ~1e-7 relative
+error in I instead of the ~1e-6 of FP32 waves psi; dL/dv then stays within
+1e-3 of the FP64 adjoint and of central differences.
 """
 import numpy as np
 import pytest
@@ -76,7 +77,7 @@ def test_adjoint_matches_oracle(ctx, msk, oracle, S, checkpoint):
     for u in range(2):
         gref, Lu = oracle.stack_adjoint(p, v[u], rp, target[u])
         L64 += Lu
-        assert rel_l2(g[u], gref) < 2e-3
+        assert rel_l2(g[u], gref) < 1e-3
     assert abs(loss / L64 - 1.0) < 1e-4
 
 
@@ -105,7 +106,38 @@ def test_adjoint_matches_finite_differences(ctx, msk, oracle):
         fd.append((oracle.stack_loss(p, vp, rp, target[0]) -
                    oracle.stack_loss(p, vm, rp, target[0])) / (2 * h))
     ours = np.array([g[0][k, i, j] for k, i, j in pick])
-    assert rel_l2(ours, np.array(fd)) < 2e-3
+    assert rel_l2(ours, np.array(fd)) < 1e-3
+
+
+def test_adjoint_splatted_specimen_finite_differences(ctx, msk, oracle):
+    """The adjoint workload's setting at 128^2: potentials splatted from a
+    random specimen, the target from v (1 + 0.01 N(0, 1)), one detector plane;
+    dL/dv against the FP64 adjoint and central differences on 128 random
+    voxels (within 1e-3 of both)."""
+    import os
+    spec = sp.random_specimen(600, 32.0, 4.0, 28.0, 1021)
+    s = msk.Series()
+    s.nx = s.ny = 128
+    s.ctblength = s.ctblengthz = 32.0
+    s.v0, s.deltaz = 200.0, 1.0
+    v, _ = ctx.potential_stack(s, spec.Znum, spec.x, spec.y, spec.z, spec.occ,
+                               np.array([0.0, 0.3]), np.array([0.0, 0.7]))
+    S = v.shape[1]
+    vt = sp.perturbed(v, seed=1022)
+    st = make_stack(msk, 128, 128, S, ax=32.0, checkpoint=8)
+    rp = [-16.0]
+    target = ctx.stack_images(st, vt, rp)
+    _, g = ctx.adjoint(st, v, rp, target)
+    p = oracle_params(st)
+    rng = np.random.default_rng(1023)
+    for u in range(2):
+        gref, _ = oracle.stack_adjoint(p, v[u], rp, target[u])
+        assert rel_l2(g[u], gref) < 1e-3
+        vox = np.stack([rng.integers(0, S, 128), rng.integers(0, 128, 128),
+                        rng.integers(0, 128, 128)], axis=1)
+        fd = oracle.stack_fd(p, v[u], rp, target[u], vox, nthreads=os.cpu_count() or 1)
+        ours = np.array([g[u][k, i, j] for k, i, j in vox])
+        assert rel_l2(ours, fd) < 1e-3
 
 
 def test_adjoint_batching_and_device_pointers(ctx, msk, oracle):
@@ -133,11 +165,11 @@ def test_adjoint_batching_and_device_pointers(ctx, msk, oracle):
 
 
 def test_stack_zero_potential_is_plane_wave(ctx, msk):
-    """v = 0: every transmission is 1 and the image 1, up to the rounding of
-    the transforms of a constant."""
+    """v = 0: every transmission is 1 and the image exactly 1 (the scattered
+    parts tau and phi are exactly zero throughout)."""
     s = make_stack(msk, 32, 32, 4)
-    im = ctx.stack_images(s, np.zeros((2, 4, 32, 32), np.float32), [0.0])
-    assert np.allclose(im, 1.0, rtol=0, atol=1e-5)
+    im = ctx.stack_images(s, np.zeros((2, 4, 32, 32), np.float32), [0.0, 50.0])
+    assert np.all(im == 1.0)
 
 
 def test_stack_errors(ctx, msk):

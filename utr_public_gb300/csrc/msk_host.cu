@@ -1996,7 +1996,11 @@ int msk_tilt_series_planes(msk_context *ctx, const msk_series *s, int natom, con
 // adjoint of an image misfit through it.  Kernels: P1 is k_row_expv (no
 // splat), P2-P4 as in the atom path; the backward pass runs the adjoint of
 // every step in W-states with conjugated propagator and free-space tables
-// (the 2/3 band limit is real and symmetric: its own adjoint).
+// (the 2/3 band limit is real and symmetric: its own adjoint).  Waves and
+// transmissions are carried in the scattered form (phi = psi - 1, tau = t - 1;
+// k_row_transmit<N, true>), which keeps the FP32 rounding of the images ~10x
+// below that of psi and t themselves: the adjoint's residuals I - T are a few
+// 1e-4 of I.
 
 namespace {
 
@@ -2144,7 +2148,7 @@ int stack_run(msk_context *ctx, const StackJob &J)
         return maps[v][(size_t)(p - base) / ((size_t)B * plane)];
     };
     const double P = (double)plane;
-    const float tscale = 1.0f / ((float)ny * (float)ny);
+    const float tscale = 1.0f / (float)ny;  // scattered-form transmit: S(n phi') / ny
     // loss partials: one per row-pass CTA (at most one per row) and defocus
     if (adjoint) MSK_CUDA(ctx, ctx->stk_part.reserve((size_t)ndef * B * nx * sizeof(double)));
     std::vector<double> partial_host;
@@ -2173,23 +2177,18 @@ int stack_run(msk_context *ctx, const StackJob &J)
         auto step = [&](const float2 *tb, const float2 *in, float2 *out) {
             {
                 Prof p(ctx, kTransmit, 24.0 * P * nb);
-                rop->row_transmit(g, nullptr, nb, tb, in, out, tscale, 1, ctx->stream);
+                rop->row_transmit_scat(g, nullptr, nb, tb, in, out, tscale, 1, ctx->stream);
             }
             Prof p(ctx, kKColProp, 16.0 * P * nb);
             cop->col_prop(g, map_of(out, vprop), map_of(out, vprop), nullptr, nb, 1,
                           ctx->stream);  // W0 in band
         };
 
-        // the band-mode transmit stores only in-band row segments: every wave
-        // buffer starts as zeros
-        MSK_CUDA(ctx, cudaMemsetAsync(base, 0, (size_t)planes * B * pb, ctx->stream));
-        // forward: W_0 = S(1); checkpoints W_{bK} (or every wave and
+        // every buffer starts as zeros: the band-mode transmit stores only
+        // in-band row segments, and W_0 = S(phi_0) = 0 (psi_0 = 1, the
+        // scattered form); checkpoints W_{bK} (or every wave and
         // transmission) kept for the backward pass
-        float2 *w0 = keep ? waves[0] : adjoint ? ck[0] : W;
-        {
-            Prof p(ctx, kPlane, 8.0 * P * nb);
-            k_plane_init<<<1024, 256, 0, ctx->stream>>>(w0, nullptr, nb, nx, ny);
-        }
+        MSK_CUDA(ctx, cudaMemsetAsync(base, 0, (size_t)planes * B * pb, ctx->stream));
         for (int k = 1; k <= S; k++) {
             if (keep) {
                 transmission(k, trans[k - 1]);
@@ -2231,7 +2230,7 @@ int stack_run(msk_context *ctx, const StackJob &J)
                                  ctx->stream);
             }
             if (!adjoint) {
-                // images[u][d] = |iS(E)|^2: one image per unit, no averaging
+                // images[u][d] = |1 + iS(E)|^2: one image per unit, no averaging
                 std::vector<int> meta;
                 for (int i = 0; i <= nb; i++) meta.push_back(i);          // img_off
                 for (int i = 0; i < nb; i++) meta.push_back(i);           // img_units
@@ -2243,11 +2242,11 @@ int stack_run(msk_context *ctx, const StackJob &J)
                                               cudaMemcpyHostToDevice, ctx->stream));
                 count_copy(ctx, 0, (double)(meta.size() * sizeof(int)));
                 Prof p(ctx, kIntensity, 12.0 * P * nb);
-                rop->row_intensity(g, nb, dm, dm + nb + 1, dm + 2 * nb + 1, dm + 3 * nb + 1, E,
-                                   img_d, 1.0f, ctx->stream);
+                rop->row_intensity_scat(g, nb, dm, dm + nb + 1, dm + 2 * nb + 1, dm + 3 * nb + 1,
+                                        E, img_d, 1.0f, ctx->stream);
                 continue;
             }
-            // G_d = W(2 (I - T) phi), in place in E; partial sums of the loss
+            // G_d = W(2 (I - T) psi), in place in E; partial sums of the loss
             int np = 0;
             {
                 Prof p(ctx, kImGrad, 20.0 * P * nb);

@@ -48,6 +48,10 @@ struct SizeOps {
     void (*row_transmit)(const Geom &, const int *units, int nunits, const float2 *tbuf,
                          const float2 *psi, float2 *out, float out_scale, int band,
                          cudaStream_t);
+    // the same in the scattered form (phi, tau; the potential-stack path)
+    void (*row_transmit_scat)(const Geom &, const int *units, int nunits, const float2 *tbuf,
+                              const float2 *psi, float2 *out, float out_scale, int band,
+                              cudaStream_t);
     void (*row_init)(const Geom &, const int *units, int nunits, const float2 *wave0,
                      float2 *psi, float scale, cudaStream_t);
     void (*row_exit)(const Geom &, const int *units, int nunits, const float2 *psi,
@@ -58,7 +62,10 @@ struct SizeOps {
     void (*row_intensity)(const Geom &, int nimg, const int *img_off, const int *img_units,
                           const int *img_dst, const int *img_flags, const float2 *ebuf,
                           float *images, float nconf, cudaStream_t);
-    // potential stacks and the adjoint (row length n)
+    // potential stacks and the adjoint (row length n), all in the scattered form
+    void (*row_intensity_scat)(const Geom &, int nimg, const int *img_off, const int *img_units,
+                               const int *img_dst, const int *img_flags, const float2 *ebuf,
+                               float *images, float nconf, cudaStream_t);
     void (*row_expv)(const Geom &, int nunits, const float *v, size_t ustride, float2 *out,
                      cudaStream_t);
     void (*row_adj_transmit)(const Geom &, int nunits, float2 *Gu, float2 *B, const float2 *Wp,
@@ -188,14 +195,15 @@ struct Launch {
         if (!fr.table) return;  // the pass multiplies by fr.table; nothing to run without it
         col<kColFresnel>(g, in, out, units, nunits, fr, scale, 0, s);
     }
-    static void row_transmit(const Geom &g, const int *units, int nunits, const float2 *tbuf,
-                             const float2 *psi, float2 *out, float out_scale, int band,
-                             cudaStream_t s)
+    template <bool SCAT>
+    static void row_transmit_t(const Geom &g, const int *units, int nunits, const float2 *tbuf,
+                               const float2 *psi, float2 *out, float out_scale, int band,
+                               cudaStream_t s)
     {
         static std::once_flag f;
-        set_smem(k_row_transmit<N>, Smem<N>::transmit, f);
+        set_smem(k_row_transmit<N, SCAT>, Smem<N>::transmit, f);
         const int L = RowCfg<N>::LT;
-        k_row_transmit<N><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::transmit, s>>>(
+        k_row_transmit<N, SCAT><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::transmit, s>>>(
             g, units, tbuf, psi, out, out_scale, band);
     }
     static void row_init(const Geom &g, const int *units, int nunits, const float2 *wave0,
@@ -225,14 +233,15 @@ struct Launch {
         k_row_simple<N, kRowExit><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::row, s>>>(
             g, units, psi, out, 1.0f / (float)g.ny);
     }
-    static void row_intensity(const Geom &g, int nimg, const int *img_off, const int *img_units,
-                              const int *img_dst, const int *img_flags, const float2 *ebuf,
-                              float *images, float nconf, cudaStream_t s)
+    template <bool SCAT>
+    static void row_intensity_t(const Geom &g, int nimg, const int *img_off,
+                                const int *img_units, const int *img_dst, const int *img_flags,
+                                const float2 *ebuf, float *images, float nconf, cudaStream_t s)
     {
         static std::once_flag f;
-        set_smem(k_row_intensity<N>, Smem<N>::row, f);
+        set_smem(k_row_intensity<N, SCAT>, Smem<N>::row, f);
         const int L = RowCfg<N>::L;
-        k_row_intensity<N><<<nimg * row_blocks(g, L), L * P::T, Smem<N>::row, s>>>(
+        k_row_intensity<N, SCAT><<<nimg * row_blocks(g, L), L * P::T, Smem<N>::row, s>>>(
             g, img_off, img_units, img_dst, img_flags, ebuf, images, nconf);
     }
 
@@ -276,8 +285,9 @@ struct Launch {
     {
         static const SizeOps o = {N,        {ColCfg<N, 0>::C, ColCfg<N, 1>::C}, ColCfg<N>::BR, splat,
                                   splat_potential, splat_spec, col_dw, row_dwexp,
-                                  col_mask, col_prop,     col_fresnel,      row_transmit,
-                                  row_init, row_exit,     row_inverse, row_intensity, row_expv,
+                                  col_mask, col_prop,     col_fresnel,      row_transmit_t<false>,
+                                  row_transmit_t<true>,   row_init, row_exit, row_inverse,
+                                  row_intensity_t<false>, row_intensity_t<true>, row_expv,
                                   row_adj_transmit,       row_grad,         row_imgrad};
         return &o;
     }

@@ -18,6 +18,15 @@
 // With unnormalised transforms these scalings are exactly the reference's
 // fft / ifft-with-1/(nx*ny) pairs.  An empty slice is P4 alone: the
 // wave's row iFFT and FFT around a missing transmit cancel.
+//
+// Scattered form (the potential-stack path and its adjoint): the buffers hold
+// phi = psi - 1 and tau = t - 1 instead of psi and t.  The band limit, the
+// propagator and the free-space multiplier are 1 at k = 0, so they map 1 to 1
+// and act on phi and tau alone; the transmit becomes phi' = phi + (tau +
+// phi tau) and I = |1 + phi|^2.  Same FP32 arithmetic, but every rounding
+// scales with |phi| (the scattered part) instead of with the unit plane
+// wave, which leaves ~10x less error in I -- the figure the image residuals
+// I - T of the adjoint's loss, a few 1e-4 of I, depend on.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -73,6 +82,36 @@ static __device__ __noinline__ float2 expi(float ph)
     float s, c;
     sincosf(ph, &s, &c);
     return make_float2(c, s);
+}
+
+// exp(i*ph) - 1 = (-2 sin^2(ph/2), 2 sin(ph/2) cos(ph/2)): both parts with a
+// relative error of a few ulp of their own size (no cancellation against 1)
+static __device__ __noinline__ float2 expm1i(float ph)
+{
+    float s, c;
+    sincosf(0.5f * ph, &s, &c);
+    return make_float2(-2.0f * s * s, 2.0f * s * c);
+}
+
+// phi' = phi + (tau + phi tau) of the scattered form, on a = n phi, b = n tau
+// (row transforms of W-states), inv_n = 1/n: returns n phi'
+__device__ __forceinline__ float2 scat_transmit(float2 a, float2 b, float inv_n)
+{
+    const float2 ab = cscale(cmul(a, b), inv_n);
+    return make_float2(a.x + (b.x + ab.x), a.y + (b.y + ab.y));
+}
+
+// conj(1 + x) g on c = n g, x = n x', inv_n = 1/n: returns n conj(1 + x') g
+__device__ __forceinline__ float2 scat_conj_mul(float2 c, float2 x, float inv_n)
+{
+    const float2 cx = cscale(cmul_conj(c, x), inv_n);
+    return make_float2(c.x + cx.x, c.y + cx.y);
+}
+
+// |1 + phi|^2 - 1 = phi_r (2 + phi_r) + phi_i^2, without forming 1 + phi
+__device__ __forceinline__ float scat_dI(float2 phi)
+{
+    return fmaf(phi.x, phi.x + 2.0f, phi.y * phi.y);
 }
 
 // Rows (lines of length NY) per CTA for the row passes.
@@ -393,8 +432,9 @@ k_col_pass(const Geom g, const __grid_constant__ CUtensorMap in_map,
 // ---------------------------------------------------------------- P3
 // W' = S(iS(W) * iS(B)) * out_scale (out_scale = 1/ny^2): wave *= trans
 // (cfpix.cpp:349-372) between the transmission's and the wave's row
-// transforms.  `out` may be `psi` (in place).
-template <int NY>
+// transforms.  `out` may be `psi` (in place).  SCAT: the scattered form,
+// W = S(phi), B = S(tau_bl), out = S(phi + tau + phi tau) * out_scale * ny.
+template <int NY, bool SCAT = false>
 __global__ void __launch_bounds__(RowCfg<NY>::LT * FftPlan<NY>::T, 3)
 k_row_transmit(const Geom g, const int *__restrict__ units, const float2 *__restrict__ tbuf,
                const float2 *psi, float2 *out, float out_scale, int band)
@@ -462,7 +502,9 @@ k_row_transmit(const Geom g, const int *__restrict__ units, const float2 *__rest
     __syncthreads();
     fft_line<NY, true, 1, BLK>(v, bufW + l * P::PADN, 0, t, g.tw_row);
 #pragma unroll
-    for (int m = 0; m < E; m++) v[m] = cmul(v[m], bufB[l * NY + t + m * T]);
+    for (int m = 0; m < E; m++)
+        v[m] = SCAT ? scat_transmit(v[m], bufB[l * NY + t + m * T], 1.0f / (float)NY)
+                    : cmul(v[m], bufB[l * NY + t + m * T]);
     fft_line<NY, false, 1, BLK>(v, bufW + l * P::PADN, 0, t, g.tw_row);
     __syncthreads();
 #pragma unroll
@@ -524,7 +566,8 @@ k_row_simple(const Geom g, const int *__restrict__ units, const float2 *__restri
 //                                           whose free-space waves make image i
 //   img_dst[i]: destination image index; img_flags[i]: 1 = add onto the
 //   partial sum already stored, 2 = divide by nconf after adding.
-template <int NY>
+// SCAT: the waves are the scattered parts phi of psi = 1 + phi.
+template <int NY, bool SCAT = false>
 __global__ void __launch_bounds__(RowCfg<NY>::L * FftPlan<NY>::T)
 k_row_intensity(const Geom g, const int *__restrict__ img_off, const int *__restrict__ img_units,
                 const int *__restrict__ img_dst, const int *__restrict__ img_flags,
@@ -554,7 +597,8 @@ k_row_intensity(const Geom g, const int *__restrict__ img_off, const int *__rest
         for (int m = 0; m < E; m++) v[m] = src[t + m * T];
         fft_line<NY, true, 1, BLK>(v, s_lines + l * P::PADN, 0, t, g.tw_row);
 #pragma unroll
-        for (int m = 0; m < E; m++) acc[m] += v[m].x * v[m].x + v[m].y * v[m].y;
+        for (int m = 0; m < E; m++)
+            acc[m] += SCAT ? 1.0f + scat_dI(v[m]) : v[m].x * v[m].x + v[m].y * v[m].y;
     }
     if (row_ok) {
 #pragma unroll
@@ -564,8 +608,9 @@ k_row_intensity(const Geom g, const int *__restrict__ img_off, const int *__rest
 
 // ---------------------------------------------------------------- potential stacks
 // Rows of a per-slice potential stack v[u][k][ix][iy] (float, V*Angstrom):
-// A = S(exp(i sigma v)), the transmission before its band limit.  `v` points
-// at slice k of unit 0; units are `ustride` floats apart.
+// A = S(exp(i sigma v) - 1), the scattered part tau of the transmission
+// before its band limit.  `v` points at slice k of unit 0; units are
+// `ustride` floats apart.
 template <int NY>
 __global__ void __launch_bounds__(RowCfg<NY>::L * FftPlan<NY>::T, RowCfg<NY>::MB)
 k_row_expv(const Geom g, const float *__restrict__ v, size_t ustride, float2 *__restrict__ out)
@@ -585,8 +630,8 @@ k_row_expv(const Geom g, const float *__restrict__ v, size_t ustride, float2 *__
 #pragma unroll
     for (int m = 0; m < E; m++) {
         const float ph = src[t + m * T] * g.sigma_f;
-        w[m] = make_float2(1.0f, 0.0f);
-        if (__any_sync(0xffffffffu, ph != 0.0f)) w[m] = expi(ph);
+        w[m] = make_float2(0.0f, 0.0f);
+        if (__any_sync(0xffffffffu, ph != 0.0f)) w[m] = expm1i(ph);
     }
     fft_line<NY, false, 1, BLK>(w, s_lines + l * P::PADN, 0, t, g.tw_row);
     if (ix < nx) {  // out-of-band columns as zeros: the band limit zeroes them
@@ -637,9 +682,10 @@ k_row_dwexp(const Geom g, const int *__restrict__ units, const float2 *__restric
     store_band_rows<NY>(g, s_lines, min(L, nx - ix0), out + ((size_t)u * nx + ix0) * NY);
 }
 
-// Adjoint of transmit.  In W-states (W(f) = S(f)): from Gu = W(g_u),
-// B = W(t_k), Wp = W(psi_{k-1}):  Gu <- W(conj(t) g_u)  (dL/dconj psi_{k-1})
-// and B <- W(conj(psi_{k-1}) g_u)  (dL/dconj t_k), both in place.
+// Adjoint of transmit, scattered form.  In W-states (W(f) = S(f)): from
+// Gu = W(g_u), B = W(tau_k), Wp = W(phi_{k-1}):  Gu <- W(conj(1 + tau) g_u)
+// (dL/dconj psi_{k-1}) and B <- W(conj(1 + phi_{k-1}) g_u) (dL/dconj t_k),
+// both in place.
 template <int NY>
 __global__ void __launch_bounds__(RowCfg<NY>::LT * FftPlan<NY>::T)
 k_row_adj_transmit(const Geom g, float2 *Gu, float2 *B, const float2 *__restrict__ Wp)
@@ -657,7 +703,7 @@ k_row_adj_transmit(const Geom g, float2 *Gu, float2 *B, const float2 *__restrict
     const int ix = (blockIdx.x % bpu) * L + l;
     const bool row_ok = ix < nx;
     const size_t off = ((size_t)u * nx + (row_ok ? ix : 0)) * NY;
-    const float sc = 1.0f / ((float)NY * (float)NY);
+    const float sc = 1.0f / (float)NY, inv_n = 1.0f / (float)NY;
     float2 *buf = s_lines + l * P::PADN;
     float2 *stash = s_stash + l * NY;
     float2 a[E];
@@ -668,9 +714,9 @@ k_row_adj_transmit(const Geom g, float2 *Gu, float2 *B, const float2 *__restrict
     for (int m = 0; m < E; m++) stash[t + m * T] = a[m];
 #pragma unroll
     for (int m = 0; m < E; m++) a[m] = B[off + t + m * T];
-    fft_line<NY, true, 1, BLK>(a, buf, 0, t, g.tw_row);  // ny t
+    fft_line<NY, true, 1, BLK>(a, buf, 0, t, g.tw_row);  // ny tau
 #pragma unroll
-    for (int m = 0; m < E; m++) a[m] = cmul_conj(stash[t + m * T], a[m]);
+    for (int m = 0; m < E; m++) a[m] = scat_conj_mul(stash[t + m * T], a[m], inv_n);
     fft_line<NY, false, 1, BLK>(a, buf, 0, t, g.tw_row);
     if (row_ok) {
 #pragma unroll
@@ -678,9 +724,9 @@ k_row_adj_transmit(const Geom g, float2 *Gu, float2 *B, const float2 *__restrict
     }
 #pragma unroll
     for (int m = 0; m < E; m++) a[m] = Wp[off + t + m * T];
-    fft_line<NY, true, 1, BLK>(a, buf, 0, t, g.tw_row);  // ny psi
+    fft_line<NY, true, 1, BLK>(a, buf, 0, t, g.tw_row);  // ny phi
 #pragma unroll
-    for (int m = 0; m < E; m++) a[m] = cmul_conj(stash[t + m * T], a[m]);
+    for (int m = 0; m < E; m++) a[m] = scat_conj_mul(stash[t + m * T], a[m], inv_n);
     fft_line<NY, false, 1, BLK>(a, buf, 0, t, g.tw_row);
     if (row_ok) {
 #pragma unroll
@@ -724,9 +770,10 @@ k_row_grad(const Geom g, const float2 *__restrict__ Ge, const float *__restrict_
     }
 }
 
-// Image residual of the loss L = sum (|phi|^2 - T)^2: from E with
-// phi = iS(E) (the free-space column pass output), G = S(2 (I - T) phi) =
-// W(dL/dconj phi); per-CTA partial sums of (I - T)^2 go to partial[block].
+// Image residual of the loss L = sum (|psi|^2 - T)^2, scattered form: from E
+// with phi = iS(E) (the free-space column pass output, psi = 1 + phi),
+// r = I - T = (1 - T) + (|1 + phi|^2 - 1), G = S(2 r psi) = W(dL/dconj psi);
+// per-CTA partial sums of r^2 go to partial[block].
 // G may be Ein: every CTA reads its rows before it writes them.
 template <int NY>
 __global__ void __launch_bounds__(RowCfg<NY>::L * FftPlan<NY>::T)
@@ -754,10 +801,9 @@ k_row_imgrad(const Geom g, const float2 *Ein, const float *__restrict__ target, 
     double acc = 0.0;
 #pragma unroll
     for (int m = 0; m < E; m++) {
-        const float I = a[m].x * a[m].x + a[m].y * a[m].y;
-        const float r = row_ok ? I - tr[t + m * T] : 0.0f;
+        const float r = row_ok ? (1.0f - tr[t + m * T]) + scat_dI(a[m]) : 0.0f;
         acc += (double)r * (double)r;
-        a[m] = cscale(a[m], 2.0f * r);
+        a[m] = make_float2(2.0f * r * (1.0f + a[m].x), 2.0f * r * a[m].y);
     }
     fft_line<NY, false, 1, BLK>(a, s_lines + l * P::PADN, 0, t, g.tw_row);
     if (row_ok) {
