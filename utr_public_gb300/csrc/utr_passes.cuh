@@ -246,11 +246,17 @@ k_utr_fourier_rows(const UtrFourier f, const float2 *__restrict__ tw, const UtrA
     const UtrAcc *src = acc + (size_t)rr * NX;
     float2 *line = s_lines + l * P::PADN;
     // per-voxel work in a rolled loop (one copy of the code: the unrolled form
-    // overflowed the instruction cache), staged in the line's shared buffer
+    // overflowed the instruction cache), staged in the line's shared buffer;
+    // the sums are loaded three iterations ahead (four 16-byte loads in flight
+    // a thread: one alone left the pass waiting on HBM latency)
+    UtrAcc a1 = src[t], a2 = src[t + T], a3 = src[t + 2 * T];
 #pragma unroll 1
     for (int m = 0; m < E; m++) {
         const int i = t + m * T;
-        const UtrAcc a = src[i];
+        const UtrAcc a = a1;
+        a1 = a2;
+        a2 = a3;
+        if (m + 3 < E) a3 = src[i + 3 * T];
         float2 v = utr_filter(f, make_float2(a.re, a.im), a.w);
         v = utr_correct(f, r, i, v);
         if (f.nyq && i == 0) {
