@@ -47,6 +47,17 @@ __device__ __forceinline__ bool out_of_band(const Geom &g, int iy)
     return iy > g.band_p && iy < g.band_q;
 }
 
+// True when no thread of the line group holds a non-zero `nz`: a warp vote
+// for lines of <= 32 threads (several lines a warp below 32: the group
+// transforms share warp barriers), a CTA vote for larger lines (their
+// transforms use CTA barriers).  Uniform over everything a line FFT syncs.
+template <bool BLK>
+__device__ __forceinline__ bool group_none(bool nz)
+{
+    if constexpr (BLK) return !__syncthreads_or(nz);
+    else return !__any_sync(0xffffffffu, nz);
+}
+
 // Store `rows` dense rows of length NY from shared memory as their in-band
 // segments [0, seg_e1) and [seg_s2, NY); the (at most two) out-of-band
 // elements inside the segments are zeroed first.  Called by every thread;
@@ -290,9 +301,14 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
         }
     } else if constexpr (MODE == kSplatSpec) {
         float2 v[E];
+        bool nz = false;
 #pragma unroll
-        for (int m = 0; m < E; m++) v[m] = make_float2(vacc[t + m * T], 0.0f);
-        fft_line<NY, false, 1, BLK>(v, s_lines + l * P::PADN, 0, t, g.tw_row);
+        for (int m = 0; m < E; m++) {
+            v[m] = make_float2(vacc[t + m * T], 0.0f);
+            nz |= v[m].x != 0.0f;
+        }
+        if (!group_none<BLK>(nz))  // S(0) = 0: rows without atoms skip the transform
+            fft_line<NY, false, 1, BLK>(v, s_lines + l * P::PADN, 0, t, g.tw_row);
         __syncthreads();
 #pragma unroll
         for (int m = 0; m < E; m++) s_lines[l * NY + t + m * T] = v[m];
@@ -306,14 +322,24 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
         }
     } else {
         float2 v[E];
+        bool nz = false;
 #pragma unroll
         for (int m = 0; m < E; m++) {
             // most of a slice is empty: exp(i*0) = 1 exactly, as sincosf(0) gives
             const float ph = vacc[t + m * T] * g.sigma_f;
             v[m] = make_float2(1.0f, 0.0f);
+            nz |= ph != 0.0f;
             if (__any_sync(0xffffffffu, ph != 0.0f)) v[m] = expi(ph);
         }
-        fft_line<NY, false, 1, BLK>(v, s_lines + l * P::PADN, 0, t, g.tw_row);
+        if (group_none<BLK>(nz)) {
+            // rows without atoms: t = 1 and S(t) = NY at iy = 0, 0 elsewhere
+            // (what the transform of ones gives, every step exact)
+#pragma unroll
+            for (int m = 0; m < E; m++)
+                v[m] = make_float2(m == 0 && t == 0 ? (float)NY : 0.0f, 0.0f);
+        } else {
+            fft_line<NY, false, 1, BLK>(v, s_lines + l * P::PADN, 0, t, g.tw_row);
+        }
         // dense rows into shared memory, then their in-band segments to the
         // buffer (its out-of-band columns hold zeros: the band limit zeroes them)
         __syncthreads();
@@ -627,13 +653,16 @@ k_row_expv(const Geom g, const float *__restrict__ v, size_t ustride, float2 *__
     const int ix = (blockIdx.x % bpu) * L + l;
     const float *src = v + (size_t)u * ustride + (size_t)(ix < nx ? ix : 0) * NY;
     float2 w[E];
+    bool nz = false;
 #pragma unroll
     for (int m = 0; m < E; m++) {
         const float ph = src[t + m * T] * g.sigma_f;
         w[m] = make_float2(0.0f, 0.0f);
+        nz |= ph != 0.0f;
         if (__any_sync(0xffffffffu, ph != 0.0f)) w[m] = expm1i(ph);
     }
-    fft_line<NY, false, 1, BLK>(w, s_lines + l * P::PADN, 0, t, g.tw_row);
+    if (!group_none<BLK>(nz))  // S(0) = 0: empty rows skip the transform
+        fft_line<NY, false, 1, BLK>(w, s_lines + l * P::PADN, 0, t, g.tw_row);
     if (ix < nx) {  // out-of-band columns as zeros: the band limit zeroes them
         float2 *dst = out + ((size_t)u * nx + ix) * NY;
 #pragma unroll
