@@ -63,7 +63,9 @@ struct msk_context {
     int device = 0;
     cudaStream_t stream = nullptr;      // the stream work goes to
     cudaStream_t own_stream = nullptr;  // created with the context
-    cudaStream_t aux = nullptr;         // second stream: the wave chain of the slice loop
+    cudaStream_t aux = nullptr;         // second stream: the wave chain of the slice loop,
+                                        // the potential stacks' copies in
+    cudaStream_t aux2 = nullptr;        // third stream: the potential stacks' copies out
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_t[2] = {}, ev_free[2] = {};
     bool prof_on = false;
     std::vector<msk::ProfRec> prof_pending;
@@ -83,6 +85,8 @@ struct msk_context {
     msk::DevBuf tune;                                 // scratch grid of the column tuner
     msk::DevBuf utr_img, utr_k2, utr_acc, utr_vol, utr_out, utr_tab, utr_stage;  // UTR reconstruction
     bool no_tune = false;                             // column tiles fixed at variant 0
+    cudaEvent_t stk_ev[7] = {};                       // potential stacks: copy / kernel handoffs
+    std::vector<cudaEvent_t> stk_sev;                 // the same per slice (2 per slice)
     std::vector<cudaStream_t> lanes;                  // concurrent specimens of a batch
     std::vector<cudaEvent_t> lane_ev;                 // lane joins (one per lane) + fork
     size_t units_alloc = 0;  // units the psi / tbuf buffers hold

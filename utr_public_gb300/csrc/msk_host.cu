@@ -1338,6 +1338,7 @@ int msk_create(int device, msk_context **out)
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->aux2, cudaStreamNonBlocking);
     for (cudaEvent_t *ev : {&ctx->ev_fork, &ctx->ev_join, &ctx->ev_t[0], &ctx->ev_t[1],
                             &ctx->ev_free[0], &ctx->ev_free[1]})
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
@@ -1368,9 +1369,13 @@ void msk_destroy(msk_context *ctx)
     for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_join, ctx->ev_t[0], ctx->ev_t[1], ctx->ev_free[0],
                           ctx->ev_free[1]})
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->stk_ev)
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->stk_sev) cudaEventDestroy(e);
     for (cudaStream_t l : ctx->lanes) cudaStreamDestroy(l);
     for (cudaEvent_t e : ctx->lane_ev) cudaEventDestroy(e);
     if (ctx->aux) cudaStreamDestroy(ctx->aux);
+    if (ctx->aux2) cudaStreamDestroy(ctx->aux2);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }
@@ -2087,15 +2092,23 @@ int stack_run(msk_context *ctx, const StackJob &J)
     const size_t ib = (size_t)ndef * plane * sizeof(float);   // one unit's images
     const size_t staged = (v_dev ? 0 : vb) + (adjoint && !g_dev ? vb : 0) +
                           (adjoint && !t_dev ? ib : 0) + (!adjoint && !i_dev ? ib : 0);
+    // Host buffers: the copies in and out run on two more streams, slice by
+    // slice -- slice k of every unit of a batch (one 2D copy) goes in ahead of
+    // the forward pass's slice k, and dL/dv_k goes out as soon as the backward
+    // pass has written it -- so the kernels wait only for the first slice and
+    // the host only for the last.  Several batches (when memory is short) use
+    // two sets of staging buffers.
+    const bool host_io = staged > 0;
+    const int nslot_max = host_io ? 2 : 1;
     size_t free_b = 0, total_b = 0;
     MSK_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
     const size_t budget = std::min<size_t>(free_b / 2, (size_t)64 << 30);
     // Adjoint with checkpoint 0: keep every wave and every transmission of the
-    // forward pass (2S + 3 planes a unit) when memory holds at least 32 units
+    // forward pass (2S + 4 planes a unit) when memory holds at least 32 units
     // (or all of them) at once -- the backward pass then recomputes nothing;
     // otherwise a checkpoint every K slices (8 by default) with the waves and
     // transmissions of a block recomputed from its checkpoint.
-    const size_t keep_unit = (size_t)(2 * S + 3) * pb + staged;
+    const size_t keep_unit = (size_t)(2 * S + 4) * pb + nslot_max * staged;
     const bool keep = adjoint && s->checkpoint == 0 &&
                       budget / keep_unit >= (size_t)std::min(J.nunits, 32) &&
                       (s->max_batch <= 0 || s->max_batch >= std::min(J.nunits, 32));
@@ -2105,9 +2118,11 @@ int stack_run(msk_context *ctx, const StackJob &J)
     // checkpoints, the block's transmissions and waves, the wave gradient G;
     // keeping everything: the S + 1 waves and the S transmissions, G)
     const int planes = keep ? 2 * S + 4 : adjoint ? 3 + nblk + K + (K - 1) : 3;
-    const size_t per_unit = planes * pb + staged;
+    const size_t per_unit = planes * pb + nslot_max * staged;
     int B = (int)std::max<size_t>(1, std::min<size_t>(J.nunits, budget / per_unit));
     if (s->max_batch > 0) B = std::min(B, s->max_batch);
+    const int nbat = (J.nunits + B - 1) / B;
+    const int nslot = nbat > 1 ? nslot_max : 1;
 
     MSK_CUDA(ctx, ctx->stk.reserve((size_t)planes * B * pb));
     float2 *base = ctx->stk.as<float2>();
@@ -2126,10 +2141,31 @@ int stack_run(msk_context *ctx, const StackJob &J)
         for (int i = 0; i < K - 1; i++) Wb.push_back(grid_at(3 + nblk + K + i));
         Bt = Bb[0];  // the forward pass's transmission: a block buffer, free until the backward
     }
-    if (!v_dev) MSK_CUDA(ctx, ctx->stk_v.reserve((size_t)B * vb));
-    if (adjoint && !g_dev) MSK_CUDA(ctx, ctx->stk_g.reserve((size_t)B * vb));
-    if (adjoint && !t_dev) MSK_CUDA(ctx, ctx->stk_t.reserve((size_t)B * ib));
-    if (!adjoint && ndef > 0 && !i_dev) MSK_CUDA(ctx, ctx->stk_img.reserve((size_t)B * ib));
+    if (!v_dev) MSK_CUDA(ctx, ctx->stk_v.reserve((size_t)nslot * B * vb));
+    if (adjoint && !g_dev) MSK_CUDA(ctx, ctx->stk_g.reserve((size_t)nslot * B * vb));
+    if (adjoint && !t_dev) MSK_CUDA(ctx, ctx->stk_t.reserve((size_t)nslot * B * ib));
+    if (!adjoint && ndef > 0 && !i_dev) MSK_CUDA(ctx, ctx->stk_img.reserve((size_t)nslot * B * ib));
+    // staging of batch b: slot b % nslot
+    auto slot_of = [&](const DevBuf &buf, size_t per, int b) {
+        return reinterpret_cast<float *>(buf.as<char>() + (size_t)(b % nslot) * B * per);
+    };
+    if (host_io && !ctx->stk_ev[0])
+        for (cudaEvent_t &e : ctx->stk_ev)
+            MSK_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    while (host_io && ctx->stk_sev.size() < (size_t)2 * S) {
+        cudaEvent_t e = nullptr;
+        MSK_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->stk_sev.push_back(e);
+    }
+    cudaEvent_t *ev_sin = host_io ? ctx->stk_sev.data() : nullptr;    // slice k of v is in
+    cudaEvent_t *ev_sout = host_io ? ctx->stk_sev.data() + S : nullptr;  // dL/dv_k is written
+    cudaEvent_t *ev_in = ctx->stk_ev, *ev_done = ctx->stk_ev + 2, *ev_out = ctx->stk_ev + 4;
+    cudaStream_t cin = host_io ? ctx->aux : ctx->stream, cout = host_io ? ctx->aux2 : ctx->stream;
+    // slice-by-slice copies are 2D copies with a unit's stack as the pitch;
+    // beyond the device's largest pitch whole batches go in and out instead
+    int max_pitch = 0;
+    MSK_CUDA(ctx, cudaDeviceGetAttribute(&max_pitch, cudaDevAttrMaxPitch, ctx->device));
+    const bool by_slice = vb <= (size_t)max_pitch;
     MSK_CUDA(ctx, ctx->fresnel.reserve((adjoint ? 2 : 1) * pb));
 
     const SizeOps *rop = size_ops(ny), *cop = size_ops(nx);
@@ -2150,18 +2186,56 @@ int stack_run(msk_context *ctx, const StackJob &J)
     const double P = (double)plane;
     const float tscale = 1.0f / (float)ny;  // scattered-form transmit: S(n phi') / ny
     // loss partials: one per row-pass CTA (at most one per row) and defocus
-    if (adjoint) MSK_CUDA(ctx, ctx->stk_part.reserve((size_t)ndef * B * nx * sizeof(double)));
+    // (every batch's, kept on the device and summed on the host at the end)
+    if (adjoint)
+        MSK_CUDA(ctx, ctx->stk_part.reserve((size_t)ndef * J.nunits * nx * sizeof(double)));
     std::vector<double> partial_host;
     double loss = 0.0;
+    int part_off = 0;
 
-    for (int u0 = 0; u0 < J.nunits; u0 += B) {
-        const int nb = std::min(B, J.nunits - u0);
-        const float *vd = v_dev ? J.v + (size_t)u0 * S * plane : ctx->stk_v.as<float>();
+    // the host inputs of batch b into its staging slot, on the copy-in stream
+    // once the kernels of batch b - nslot (the slot's last reader) are done;
+    // v slice by slice, each slice of every unit of the batch one 2D copy
+    // (rows: the units, S planes apart)
+    auto upload = [&](int b) -> int {
+        const int u0 = b * B, nb = std::min(B, J.nunits - u0);
+        if (host_io && b >= nslot) MSK_CUDA(ctx, cudaStreamWaitEvent(cin, ev_done[b % nslot], 0));
         if (!v_dev) {
-            MSK_CUDA(ctx, cudaMemcpyAsync(ctx->stk_v.p, J.v + (size_t)u0 * S * plane, nb * vb,
-                                          cudaMemcpyHostToDevice, ctx->stream));
+            float *dst = slot_of(ctx->stk_v, vb, b);
+            if (!by_slice)
+                MSK_CUDA(ctx, cudaMemcpyAsync(dst, J.v + (size_t)u0 * S * plane, nb * vb,
+                                              cudaMemcpyHostToDevice, cin));
+            for (int k = 0; k < S; k++) {
+                if (by_slice)
+                    MSK_CUDA(ctx, cudaMemcpy2DAsync(dst + (size_t)k * plane, vb,
+                                                    J.v + ((size_t)u0 * S + k) * plane, vb,
+                                                    plane * sizeof(float), nb,
+                                                    cudaMemcpyHostToDevice, cin));
+                MSK_CUDA(ctx, cudaEventRecord(ev_sin[k], cin));
+            }
             count_copy(ctx, 0, (double)nb * vb);
         }
+        if (adjoint && !t_dev) {
+            MSK_CUDA(ctx, cudaMemcpyAsync(slot_of(ctx->stk_t, ib, b),
+                                          J.target + (size_t)u0 * ndef * plane, nb * ib,
+                                          cudaMemcpyHostToDevice, cin));
+            count_copy(ctx, 0, (double)nb * ib);
+        }
+        if (host_io) MSK_CUDA(ctx, cudaEventRecord(ev_in[b % nslot], cin));
+        return MSK_OK;
+    };
+    if (host_io) {  // the copies start after the work already queued on the library's stream
+        MSK_CUDA(ctx, cudaEventRecord(ctx->stk_ev[6], ctx->stream));
+        MSK_CUDA(ctx, cudaStreamWaitEvent(cin, ctx->stk_ev[6], 0));
+        MSK_CUDA(ctx, cudaStreamWaitEvent(cout, ctx->stk_ev[6], 0));
+    }
+    if ((st = upload(0))) return st;
+
+    for (int b = 0; b < nbat; b++) {
+        const int u0 = b * B, nb = std::min(B, J.nunits - u0), sl = b % nslot;
+        // the slot's outputs of batch b - nslot copied out before they are overwritten
+        if (host_io && b >= nslot) MSK_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ev_out[sl], 0));
+        const float *vd = v_dev ? J.v + (size_t)u0 * S * plane : slot_of(ctx->stk_v, vb, b);
         const size_t ustride = (size_t)S * plane;
         auto vslice = [&](int k) { return vd + (size_t)(k - 1) * plane; };  // k = 1..S
         // P1 + P2 of slice k into buffer `dst`
@@ -2184,12 +2258,17 @@ int stack_run(msk_context *ctx, const StackJob &J)
                           ctx->stream);  // W0 in band
         };
 
-        // every buffer starts as zeros: the band-mode transmit stores only
+        // the wave buffers start as zeros: the band-mode transmit stores only
         // in-band row segments, and W_0 = S(phi_0) = 0 (psi_0 = 1, the
         // scattered form); checkpoints W_{bK} (or every wave and
-        // transmission) kept for the backward pass
-        MSK_CUDA(ctx, cudaMemsetAsync(base, 0, (size_t)planes * B * pb, ctx->stream));
+        // transmission) kept for the backward pass.  Keeping everything, only
+        // the S + 1 wave planes (the transmissions' row pass writes whole rows).
+        if (keep)
+            MSK_CUDA(ctx, cudaMemsetAsync(waves[0], 0, (size_t)(S + 1) * B * pb, ctx->stream));
+        else
+            MSK_CUDA(ctx, cudaMemsetAsync(base, 0, (size_t)planes * B * pb, ctx->stream));
         for (int k = 1; k <= S; k++) {
+            if (!v_dev) MSK_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ev_sin[k - 1], 0));
             if (keep) {
                 transmission(k, trans[k - 1]);
                 step(trans[k - 1], waves[k - 1], waves[k]);
@@ -2200,20 +2279,17 @@ int stack_run(msk_context *ctx, const StackJob &J)
             transmission(k, Bt);
             step(Bt, in, out);
         }
+        // the next batch's inputs go in while this one runs (after this batch's
+        // waits on the per-slice events are queued)
+        if (b + 1 < nbat && (st = upload(b + 1))) return st;
+        if (host_io) MSK_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ev_in[sl], 0));  // the target
 
         // free space to every detector plane; images or the loss and its gradient
         float *img_d = nullptr;
         if (!adjoint && ndef > 0)
-            img_d = i_dev ? J.images + (size_t)u0 * ndef * plane : ctx->stk_img.as<float>();
+            img_d = i_dev ? J.images + (size_t)u0 * ndef * plane : slot_of(ctx->stk_img, ib, b);
         const float *tgt = nullptr;
-        if (adjoint) {
-            tgt = t_dev ? J.target + (size_t)u0 * ndef * plane : ctx->stk_t.as<float>();
-            if (!t_dev) {
-                MSK_CUDA(ctx, cudaMemcpyAsync(ctx->stk_t.p, J.target + (size_t)u0 * ndef * plane,
-                                              nb * ib, cudaMemcpyHostToDevice, ctx->stream));
-                count_copy(ctx, 0, (double)nb * ib);
-            }
-        }
+        if (adjoint) tgt = t_dev ? J.target + (size_t)u0 * ndef * plane : slot_of(ctx->stk_t, ib, b);
         int nparts = 0;
         for (int d = 0; d < ndef; d++) {
             float2 *tab = ctx->fresnel.as<float2>();
@@ -2251,7 +2327,7 @@ int stack_run(msk_context *ctx, const StackJob &J)
             {
                 Prof p(ctx, kImGrad, 20.0 * P * nb);
                 np = rop->row_imgrad(g, nb, E, tgt + (size_t)d * plane, (size_t)ndef * plane, E,
-                                     ctx->stk_part.as<double>() + nparts, ctx->stream);
+                                     ctx->stk_part.as<double>() + part_off + nparts, ctx->stream);
             }
             nparts += np;
             // g_psiS += K[conj X] g_phi: conjugate table with the column 1/nx
@@ -2274,7 +2350,18 @@ int stack_run(msk_context *ctx, const StackJob &J)
         }
 
         if (adjoint) {
-            float *gd = g_dev ? J.grad + (size_t)u0 * S * plane : ctx->stk_g.as<float>();
+            float *gd = g_dev ? J.grad + (size_t)u0 * S * plane : slot_of(ctx->stk_g, vb, b);
+            // dL/dv_k of every unit of the batch to the host (one 2D copy) once written
+            auto grad_out = [&](int k) -> int {
+                if (g_dev || !by_slice) return MSK_OK;
+                MSK_CUDA(ctx, cudaEventRecord(ev_sout[k - 1], ctx->stream));
+                MSK_CUDA(ctx, cudaStreamWaitEvent(cout, ev_sout[k - 1], 0));
+                MSK_CUDA(ctx, cudaMemcpy2DAsync(J.grad + ((size_t)u0 * S + (k - 1)) * plane, vb,
+                                                gd + (size_t)(k - 1) * plane, vb,
+                                                plane * sizeof(float), nb, cudaMemcpyDeviceToHost,
+                                                cout));
+                return MSK_OK;
+            };
             // backward with every wave and transmission kept: slice by slice
             for (int k = keep ? S : 0; k >= 1; k--) {
                 {
@@ -2291,16 +2378,19 @@ int stack_run(msk_context *ctx, const StackJob &J)
                     cop->col_mask(g, map_of(trans[k - 1], vmask), map_of(trans[k - 1], vmask),
                                   nullptr, nb, 0, ctx->stream);
                 }
-                Prof p(ctx, kGrad, 16.0 * P * nb);
-                rop->row_grad(g, nb, trans[k - 1], vslice(k), ustride,
-                              gd + (size_t)(k - 1) * plane, ctx->stream);
+                {
+                    Prof p(ctx, kGrad, 16.0 * P * nb);
+                    rop->row_grad(g, nb, trans[k - 1], vslice(k), ustride,
+                                  gd + (size_t)(k - 1) * plane, ctx->stream);
+                }
+                if ((st = grad_out(k))) return st;
             }
             // backward, one checkpoint block at a time from the last
-            for (int b = keep ? -1 : nblk - 1; b >= 0; b--) {
-                const int k0 = b * K, nj = std::min(S, k0 + K) - k0;
+            for (int blk = keep ? -1 : nblk - 1; blk >= 0; blk--) {
+                const int k0 = blk * K, nj = std::min(S, k0 + K) - k0;
                 for (int j = 1; j <= nj; j++) {  // recompute the block's t_k and psi_k
                     transmission(k0 + j, Bb[j - 1]);
-                    if (j < nj) step(Bb[j - 1], j == 1 ? ck[b] : Wb[j - 2], Wb[j - 1]);
+                    if (j < nj) step(Bb[j - 1], j == 1 ? ck[blk] : Wb[j - 2], Wb[j - 1]);
                 }
                 for (int j = nj; j >= 1; j--) {
                     const int k = k0 + j;
@@ -2311,7 +2401,7 @@ int stack_run(msk_context *ctx, const StackJob &J)
                     }
                     {
                         Prof p(ctx, kAdjTransmit, 40.0 * P * nb);
-                        rop->row_adj_transmit(g, nb, G, Bb[j - 1], j == 1 ? ck[b] : Wb[j - 2],
+                        rop->row_adj_transmit(g, nb, G, Bb[j - 1], j == 1 ? ck[blk] : Wb[j - 2],
                                               ctx->stream);
                     }
                     {
@@ -2319,30 +2409,48 @@ int stack_run(msk_context *ctx, const StackJob &J)
                         cop->col_mask(g, map_of(Bb[j - 1], vmask), map_of(Bb[j - 1], vmask), nullptr, nb, 0,
                                       ctx->stream);
                     }
-                    Prof p(ctx, kGrad, 16.0 * P * nb);
-                    rop->row_grad(g, nb, Bb[j - 1], vslice(k), ustride,
-                                  gd + (size_t)(k - 1) * plane, ctx->stream);
+                    {
+                        Prof p(ctx, kGrad, 16.0 * P * nb);
+                        rop->row_grad(g, nb, Bb[j - 1], vslice(k), ustride,
+                                      gd + (size_t)(k - 1) * plane, ctx->stream);
+                    }
+                    if ((st = grad_out(k))) return st;
                 }
             }
-            if (!g_dev) {
-                MSK_CUDA(ctx, cudaMemcpyAsync(J.grad + (size_t)u0 * S * plane, gd, nb * vb,
-                                              cudaMemcpyDeviceToHost, ctx->stream));
-                count_copy(ctx, 1, (double)nb * vb);
+        }
+        part_off += nparts;
+        // the host outputs of batch b, on the copy-out stream once its kernels are done
+        if (host_io) {
+            MSK_CUDA(ctx, cudaEventRecord(ev_done[sl], ctx->stream));
+            MSK_CUDA(ctx, cudaStreamWaitEvent(cout, ev_done[sl], 0));
+            if (adjoint && !g_dev) {
+                if (!by_slice)
+                    MSK_CUDA(ctx, cudaMemcpyAsync(J.grad + (size_t)u0 * S * plane,
+                                                  slot_of(ctx->stk_g, vb, b), nb * vb,
+                                                  cudaMemcpyDeviceToHost, cout));
+                count_copy(ctx, 1, (double)nb * vb);  // (by slice: copied as written)
             }
-            partial_host.resize(nparts);
-            MSK_CUDA(ctx, cudaMemcpyAsync(partial_host.data(), ctx->stk_part.p,
-                                          nparts * sizeof(double), cudaMemcpyDeviceToHost,
-                                          ctx->stream));
-            count_copy(ctx, 1, (double)nparts * sizeof(double));
-        } else if (ndef > 0 && !i_dev) {
-            MSK_CUDA(ctx, cudaMemcpyAsync(J.images + (size_t)u0 * ndef * plane, img_d, nb * ib,
-                                          cudaMemcpyDeviceToHost, ctx->stream));
-            count_copy(ctx, 1, (double)nb * ib);
+            if (!adjoint && ndef > 0 && !i_dev) {
+                MSK_CUDA(ctx, cudaMemcpyAsync(J.images + (size_t)u0 * ndef * plane, img_d, nb * ib,
+                                              cudaMemcpyDeviceToHost, cout));
+                count_copy(ctx, 1, (double)nb * ib);
+            }
+            MSK_CUDA(ctx, cudaEventRecord(ev_out[sl], cout));
         }
         MSK_CUDA(ctx, cudaGetLastError());
-        MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        prof_collect(ctx);
-        for (int i = 0; i < nparts; i++) loss += partial_host[i];  // fixed order
+    }
+    if (host_io) {
+        MSK_CUDA(ctx, cudaStreamSynchronize(cin));
+        MSK_CUDA(ctx, cudaStreamSynchronize(cout));
+    }
+    MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    prof_collect(ctx);
+    if (adjoint) {
+        partial_host.resize(part_off);
+        MSK_CUDA(ctx, cudaMemcpy(partial_host.data(), ctx->stk_part.p, part_off * sizeof(double),
+                                 cudaMemcpyDeviceToHost));
+        count_copy(ctx, 1, (double)part_off * sizeof(double));
+        for (int i = 0; i < part_off; i++) loss += partial_host[i];  // fixed order
     }
     if (J.loss) *J.loss = loss;
     return flags_check(ctx);
