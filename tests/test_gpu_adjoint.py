@@ -52,6 +52,7 @@ def case(nx, ny, S, nunits, seed):
     (64, 64, 10, 0.0, 0.0, (0.0, 0.0)),
     (64, 128, 7, 0.02, 1e6, (0.0, 0.0)),
     (128, 64, 5, 0.0, 0.0, (0.01, -0.02)),
+    (32, 4096, 3, 0.0, 0.0, (0.0, 0.0)),
 ])
 def test_stack_images_match_oracle(ctx, msk, oracle, nx, ny, S, aobj, cs3, ctilt):
     s = make_stack(msk, nx, ny, S, aobj=aobj, cs3=cs3, ctilt=ctilt)

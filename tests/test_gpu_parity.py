@@ -38,7 +38,8 @@ def test_calculate_matches_reference_golden(ctx, msk, oracle, name):
 @pytest.mark.parametrize("nx,ny,fov,dz", [(16, 16, 8.0, 2.0), (32, 32, 16.0, 2.0),
                                           (32, 64, 20.0, 1.0), (64, 32, 20.0, 1.0),
                                           (512, 512, 64.0, 2.0), (128, 2048, 64.0, 4.0),
-                                          (2048, 64, 64.0, 4.0), (4096, 32, 64.0, 8.0)])
+                                          (2048, 64, 64.0, 4.0), (4096, 32, 64.0, 8.0),
+                                          (32, 4096, 64.0, 8.0)])
 def test_calculate_grid_sizes(ctx, msk, oracle, nx, ny, fov, dz):
     s = sp.random_specimen(120, fov, 0.1 * fov, 0.9 * fov, 4242 + nx + ny)
     atoms = (s.Znum, s.x, s.y, s.z, s.occ)

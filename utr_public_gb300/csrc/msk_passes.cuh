@@ -104,19 +104,19 @@ static __device__ __noinline__ float2 expm1i(float ph)
     return make_float2(-2.0f * s * s, 2.0f * s * c);
 }
 
-// phi' = phi + (tau + phi tau) of the scattered form, on a = n phi, b = n tau
-// (row transforms of W-states), inv_n = 1/n: returns n phi'
+// phi' = phi + tau (1 + phi) of the scattered form, on a = n phi, b = n tau
+// (row transforms of W-states), inv_n = 1/n: returns n phi'.  Rounding 1 + phi
+// costs eps |tau| in the product, as small as the other roundings.
 __device__ __forceinline__ float2 scat_transmit(float2 a, float2 b, float inv_n)
 {
-    const float2 ab = cscale(cmul(a, b), inv_n);
-    return make_float2(a.x + (b.x + ab.x), a.y + (b.y + ab.y));
+    const float2 bc = cmul(b, make_float2(fmaf(a.x, inv_n, 1.0f), a.y * inv_n));
+    return make_float2(a.x + bc.x, a.y + bc.y);
 }
 
 // conj(1 + x) g on c = n g, x = n x', inv_n = 1/n: returns n conj(1 + x') g
 __device__ __forceinline__ float2 scat_conj_mul(float2 c, float2 x, float inv_n)
 {
-    const float2 cx = cscale(cmul_conj(c, x), inv_n);
-    return make_float2(c.x + cx.x, c.y + cx.y);
+    return cmul_conj(c, make_float2(fmaf(x.x, inv_n, 1.0f), x.y * inv_n));
 }
 
 // |1 + phi|^2 - 1 = phi_r (2 + phi_r) + phi_i^2, without forming 1 + phi
