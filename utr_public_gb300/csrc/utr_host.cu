@@ -593,13 +593,15 @@ int grid_blocks(size_t n)
 
 // Images (device) -> centred spectra in ctx->utr_k2 and the magnitude bound.
 // Images (device) -> centred spectra in ctx->utr_k2.
-int spectra(msk_context *ctx, const msk_utr *p, int nangles, const float *img_d,
-            const float2 *tw_x, const float2 *tw_y)
+// Images a0 .. a0 + nangles - 1 (img_d points at image a0) -> their spectra in
+// ctx->utr_k2, which the caller has reserved for every image; err: the
+// call's device error flag.
+int spectra(msk_context *ctx, const msk_utr *p, int a0, int nangles, const float *img_d,
+            const float2 *tw_x, const float2 *tw_y, int *err)
 {
     const int nx = p->nx, ny = p->ny;
     const size_t plane = (size_t)nx * ny;
-    MSK_CUDA(ctx, ctx->utr_k2.reserve(sizeof(float2) * plane * nangles));
-    float2 *k2 = ctx->utr_k2.as<float2>();
+    float2 *k2 = ctx->utr_k2.as<float2>() + (size_t)a0 * plane;
     UtrImg ip{};
     ip.nx = nx;
     ip.ny = ny;
@@ -616,13 +618,10 @@ int spectra(msk_context *ctx, const msk_utr *p, int nangles, const float *img_d,
     ColView view;
     int st = utr_column_map(ctx, &view, k2, ny, nx, (size_t)nangles);
     if (st) return st;
-    Geom gdummy{};
-    st = flags_reset(ctx, gdummy);
-    if (st) return st;
     UtrCol cp{};
     cp.width = nx;
     cp.tw = tw_y;
-    cp.err = gdummy.err;
+    cp.err = err;
     Prof pr(ctx, kUtrImgCols, 16.0 * plane * nangles);
     utr_ops(ny)->col_img(cp, view.map, view.map, nangles, ctx->stream);
     return MSK_OK;
@@ -719,6 +718,8 @@ int msk_utr_reconstruct_planes(msk_context *ctx, const msk_utr *p, int nangles,
     fr.nsr = (float)(p->nsr * sqrt((double)nx * ny));
     fr.inv_nsr = fr.nsr != 0.0f ? (float)(1.0 / (p->nsr * sqrt((double)nx * ny))) : 0.0f;
     CorrTabs ct;
+    // the x extent passed to InverseMLaplacian3D is xhi - ylo, as UTR.cpp:1186
+    // and 1200 pass it (equal to xhi - xlo for the square images it reads)
     if (g.zout != 0) {
         if (p->ctf_mode == 2) {
             const double alpha = -4.0 * kPi * p->asigma / (g.zout * p->wl);
@@ -807,48 +808,82 @@ int msk_utr_reconstruct_planes(msk_context *ctx, const msk_utr *p, int nangles,
 
     // images in, spectra, gridding
     const size_t plane = (size_t)nx * ny, nvox = plane * nz;
-    const float *img_d = images;
-    if (!is_device_ptr(images)) {
-        MSK_CUDA(ctx, ctx->utr_img.reserve(sizeof(float) * plane * nangles));
-        if ((st = upload(ctx, ctx->utr_img.p, images, sizeof(float) * plane * nangles))) return st;
-        img_d = ctx->utr_img.as<float>();
-    }
-    if (any_plane) {
-        UtrPlaneP pp{};
-        pp.nx = nx;
-        pp.ny = ny;
-        pp.nimg = nangles;
-        pp.f1 = (float)p->f1;
-        pp.f2 = (float)p->f2;
-        pp.use_f1 = p->f1 != 1.0;
-        pp.use_f2 = p->f2 != 0.0;
-        pp.cx = (((g.xhi + g.xlo) / 2.0 + p->dxc) - g.xlo) / p->xst;
-        pp.cy = (((g.yhi + g.ylo) / 2.0 + p->dyc) - g.ylo) / p->xst;
-        pp.par = reinterpret_cast<const double *>(tb + o_ppar);
-        pp.op = reinterpret_cast<const int *>(tb + o_pop);
-        float *fill = reinterpret_cast<float *>(tb + o_fill);
-        pp.fill = fill;
-        MSK_CUDA(ctx, ctx->utr_stage.reserve(sizeof(float) * plane * nangles));
-        float *staged = ctx->utr_stage.as<float>();
-        {
-            Prof pr(ctx, kUtrPoint, 8.0 * plane * nangles);
-            k_utr_edge_mean<<<nangles, 256, 0, ctx->stream>>>(pp, img_d, fill);
-            k_utr_img_plane<<<grid_blocks(plane * nangles), 256, 0, ctx->stream>>>(pp, img_d, staged);
-        }
-        msk_utr q = *p;  // the staged images are normalised
-        q.f1 = 1.0;
-        q.f2 = 0.0;
-        if ((st = spectra(ctx, &q, nangles, staged, tw_x, tw_y))) return st;
-    } else if ((st = spectra(ctx, p, nangles, img_d, tw_x, tw_y))) {
-        return st;
-    }
+    Geom gflags{};  // the call's device error flag, cleared once
+    if ((st = flags_reset(ctx, gflags))) return st;
+    MSK_CUDA(ctx, ctx->utr_k2.reserve(sizeof(float2) * plane * nangles));
     MSK_CUDA(ctx, ctx->utr_acc.reserve(sizeof(UtrAcc) * nvox));
     UtrAcc *acc = ctx->utr_acc.as<UtrAcc>();
     MSK_CUDA(ctx, cudaMemsetAsync(acc, 0, sizeof(UtrAcc) * nvox, ctx->stream));
-    if ((st = grid_launch(ctx, p, g, nangles, ctx->utr_k2.as<float2>(),
-                          reinterpret_cast<const float *>(tb + o_tabs),
-                          reinterpret_cast<const float *>(tb + o_scal), acc)))
-        return st;
+    const float *tabs_d = reinterpret_cast<const float *>(tb + o_tabs);
+    const float *scal_d = reinterpret_cast<const float *>(tb + o_scal);
+    const int tstride = 3 * nx + 3 * ny;
+    const float *img_d = images;
+    const bool img_host = !is_device_ptr(images);
+    if (img_host) {
+        MSK_CUDA(ctx, ctx->utr_img.reserve(sizeof(float) * plane * nangles));
+        img_d = ctx->utr_img.as<float>();
+    }
+    if (img_host && !any_plane) {
+        // host images in chunks on the copy-in stream: each chunk's spectra
+        // and gridding run while the next chunk comes in
+        const int nch = std::min(nangles, 8), per = (nangles + nch - 1) / nch;
+        if (!ctx->stk_ev[0])
+            for (cudaEvent_t &e : ctx->stk_ev)
+                MSK_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        MSK_CUDA(ctx, cudaEventRecord(ctx->stk_ev[6], ctx->stream));
+        MSK_CUDA(ctx, cudaStreamWaitEvent(ctx->aux, ctx->stk_ev[6], 0));
+        for (int a0 = 0, c = 0; a0 < nangles; a0 += per, c++) {
+            const int na = std::min(per, nangles - a0);
+            float *dst = ctx->utr_img.as<float>() + (size_t)a0 * plane;
+            MSK_CUDA(ctx, cudaMemcpyAsync(dst, images + (size_t)a0 * plane,
+                                          sizeof(float) * plane * na, cudaMemcpyHostToDevice,
+                                          ctx->aux));
+            count_copy(ctx, 0, (double)sizeof(float) * plane * na);
+            cudaEvent_t ev = ctx->stk_ev[c & 1];
+            MSK_CUDA(ctx, cudaEventRecord(ev, ctx->aux));
+            MSK_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ev, 0));
+            if ((st = spectra(ctx, p, a0, na, dst, tw_x, tw_y, gflags.err))) return st;
+            if ((st = grid_launch(ctx, p, g, na, ctx->utr_k2.as<float2>() + (size_t)a0 * plane,
+                                  tabs_d + (size_t)a0 * tstride, scal_d + (size_t)a0 * kScal,
+                                  acc)))
+                return st;
+        }
+    } else {
+        if (img_host &&
+            (st = upload(ctx, ctx->utr_img.p, images, sizeof(float) * plane * nangles)))
+            return st;
+        if (any_plane) {
+            UtrPlaneP pp{};
+            pp.nx = nx;
+            pp.ny = ny;
+            pp.nimg = nangles;
+            pp.f1 = (float)p->f1;
+            pp.f2 = (float)p->f2;
+            pp.use_f1 = p->f1 != 1.0;
+            pp.use_f2 = p->f2 != 0.0;
+            pp.cx = (((g.xhi + g.xlo) / 2.0 + p->dxc) - g.xlo) / p->xst;
+            pp.cy = (((g.yhi + g.ylo) / 2.0 + p->dyc) - g.ylo) / p->xst;
+            pp.par = reinterpret_cast<const double *>(tb + o_ppar);
+            pp.op = reinterpret_cast<const int *>(tb + o_pop);
+            float *fill = reinterpret_cast<float *>(tb + o_fill);
+            pp.fill = fill;
+            MSK_CUDA(ctx, ctx->utr_stage.reserve(sizeof(float) * plane * nangles));
+            float *staged = ctx->utr_stage.as<float>();
+            {
+                Prof pr(ctx, kUtrPoint, 8.0 * plane * nangles);
+                k_utr_edge_mean<<<nangles, 256, 0, ctx->stream>>>(pp, img_d, fill);
+                k_utr_img_plane<<<grid_blocks(plane * nangles), 256, 0, ctx->stream>>>(pp, img_d, staged);
+            }
+            msk_utr q = *p;  // the staged images are normalised
+            q.f1 = 1.0;
+            q.f2 = 0.0;
+            if ((st = spectra(ctx, &q, 0, nangles, staged, tw_x, tw_y, gflags.err))) return st;
+        } else if ((st = spectra(ctx, p, 0, nangles, img_d, tw_x, tw_y, gflags.err))) {
+            return st;
+        }
+        if ((st = grid_launch(ctx, p, g, nangles, ctx->utr_k2.as<float2>(), tabs_d, scal_d, acc)))
+            return st;
+    }
 
     // Fourier-space processing and the inverse 3D transform
     MSK_CUDA(ctx, ctx->utr_vol.reserve(sizeof(float2) * nvox));
@@ -857,15 +892,13 @@ int msk_utr_reconstruct_planes(msk_context *ctx, const msk_utr *p, int nangles,
         Prof pr(ctx, kUtrFourier, 24.0 * nvox);
         utr_ops(nx)->fourier_rows(fr, tw_x, acc, vol, ny * nz, ctx->stream);
     }
-    Geom gdummy{};
-    if ((st = flags_reset(ctx, gdummy))) return st;
     ColView vy, vz;
     if ((st = utr_column_map(ctx, &vy, vol, ny, nx, (size_t)nz))) return st;
     if ((st = utr_column_map(ctx, &vz, vol, nz, (size_t)nx * ny, 1))) return st;
     UtrCol cy{};
     cy.width = nx;
     cy.tw = tw_y;
-    cy.err = gdummy.err;
+    cy.err = gflags.err;
     {
         Prof pr(ctx, kUtrVolCols, 16.0 * nvox);
         utr_ops(ny)->col_vol(cy, vy.map, vy.map, nz, ctx->stream);
@@ -879,7 +912,7 @@ int msk_utr_reconstruct_planes(msk_context *ctx, const msk_utr *p, int nangles,
     UtrCol cz{};
     cz.width = nx * ny;
     cz.tw = tw_z;
-    cz.err = gdummy.err;
+    cz.err = gflags.err;
     cz.out = out_d;
     cz.nx = nx;
     cz.ny = ny;
@@ -895,15 +928,40 @@ int msk_utr_reconstruct_planes(msk_context *ctx, const msk_utr *p, int nangles,
     cz.ex = reinterpret_cast<const float *>(tb + o_mx);
     cz.ey = reinterpret_cast<const float *>(tb + o_my);
     cz.ez = reinterpret_cast<const float *>(tb + o_mz);
-    {
-        Prof pr(ctx, kUtrFinal, 12.0 * nvox);
-        utr_ops(nz)->col_final(cz, vz.map, 1, ctx->stream);
+    // A host volume goes out in chunks of rows y: chunk c's z pass, then its
+    // copy (nz rows of the chunk's ny/nch x nx floats, one 2D copy) on the
+    // copy-out stream while the z pass of chunk c + 1 runs.
+    const int nch = out_dev ? 1 : std::min(8, ny);
+    const int cpc = utr_ops(nz)->col_c;                       // columns per block
+    const int ncb = (int)((size_t)nx * (ny / nch) / cpc);     // blocks per chunk
+    if (!out_dev && !ctx->stk_ev[0])
+        for (cudaEvent_t &e : ctx->stk_ev)
+            MSK_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    if (!out_dev) {  // the copies start after the work already queued on the library's stream
+        MSK_CUDA(ctx, cudaEventRecord(ctx->stk_ev[6], ctx->stream));
+        MSK_CUDA(ctx, cudaStreamWaitEvent(ctx->aux2, ctx->stk_ev[6], 0));
+    }
+    for (int c = 0; c < nch; c++) {
+        cz.cb0 = c * ncb;
+        cz.ncb = nch > 1 ? ncb : 0;
+        {
+            Prof pr(ctx, kUtrFinal, 12.0 * nvox / nch);
+            utr_ops(nz)->col_final(cz, vz.map, 1, ctx->stream);
+        }
+        if (!out_dev) {
+            const size_t y0 = (size_t)c * (ny / nch), pitch = sizeof(float) * plane;
+            cudaEvent_t ev = ctx->stk_ev[c & 1];
+            MSK_CUDA(ctx, cudaEventRecord(ev, ctx->stream));
+            MSK_CUDA(ctx, cudaStreamWaitEvent(ctx->aux2, ev, 0));
+            MSK_CUDA(ctx, cudaMemcpy2DAsync(volume + y0 * nx, pitch, out_d + y0 * nx, pitch,
+                                            sizeof(float) * nx * (ny / nch), nz,
+                                            cudaMemcpyDeviceToHost, ctx->aux2));
+        }
     }
     MSK_CUDA(ctx, cudaGetLastError());
     if (!out_dev) {
-        MSK_CUDA(ctx, cudaMemcpyAsync(volume, out_d, sizeof(float) * nvox, cudaMemcpyDeviceToHost,
-                                      ctx->stream));
         count_copy(ctx, 1, (double)sizeof(float) * nvox);
+        MSK_CUDA(ctx, cudaStreamSynchronize(ctx->aux2));
     }
     MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     prof_collect(ctx);

@@ -51,7 +51,8 @@ template <int N> struct UtrLaunch {
         static std::once_flag f;
         using CC = UtrColCfg<N>;
         set_smem(k_utr_col<N, MODE>, CC::SMEM, f);
-        k_utr_col<N, MODE><<<units * (p.width / CC::C), CC::NT, CC::SMEM, s>>>(p, in, out);
+        const int bpu = p.ncb > 0 ? p.ncb : p.width / CC::C;
+        k_utr_col<N, MODE><<<units * bpu, CC::NT, CC::SMEM, s>>>(p, in, out);
     }
     static void col_img(const UtrCol &p, const CUtensorMap &in, const CUtensorMap &out, int units,
                         cudaStream_t s)

@@ -296,6 +296,7 @@ template <int N> struct UtrColCfg {
 
 struct UtrCol {
     int width;  // complex columns of the 2D view
+    int cb0, ncb;  // column blocks cb0 .. cb0 + ncb - 1 of each unit (ncb 0: all)
     const float2 *tw;
     int *err;
     // kUtrColFinal: the volume [nz][ny][nx] (width = nx * ny, lines = nz)
@@ -319,8 +320,8 @@ k_utr_col(const UtrCol p, const __grid_constant__ CUtensorMap in_map,
     float2 *buf = reinterpret_cast<float2 *>(smem);
     uint64_t *bar = reinterpret_cast<uint64_t *>(buf + P::PADN * C);
     const int tid = threadIdx.x, c = tid % C, t = tid / C;
-    const int bpu = p.width / C;
-    const int u = blockIdx.x / bpu, cb = blockIdx.x % bpu;
+    const int bpu = p.ncb > 0 ? p.ncb : p.width / C;
+    const int u = blockIdx.x / bpu, cb = blockIdx.x % bpu + p.cb0;
     const int col = cb * C + c;
     if (tid == 0) {
         mbar_init(bar, 1);
