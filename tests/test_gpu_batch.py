@@ -63,6 +63,23 @@ def test_batch_device_images_and_repeat(ctx, msk):
         assert np.array_equal(h, a)
 
 
+@pytest.mark.parametrize("graph", [True, False])
+def test_batch_pinned_host_images(ctx, msk, graph):
+    """Page-locked host images are copied on each specimen's lane (inside the
+    graph when there is one); they equal the pageable and device results."""
+    torch = pytest.importorskip("torch")
+    cases = batch_case()
+    defoci = [0.0, 120.0]
+    s = series(msk, aobj=0.02)
+    ref, _ = ctx.tilt_series_batch(s, cases, defoci, graph=graph)
+    pinned = [torch.full((len(aZ), 2, n, n), -1.0, dtype=torch.float32).pin_memory()
+              for _, n, aZ, _ in cases]
+    for _ in range(2):  # a second call reuses the arena
+        ctx.tilt_series_batch(s, cases, defoci, graph=graph, images=pinned)
+        for r, h in zip(ref, pinned):
+            assert np.array_equal(r, h.numpy())
+
+
 def test_batch_errors(ctx, msk):
     cases = batch_case()[:2]
     s = series(msk)

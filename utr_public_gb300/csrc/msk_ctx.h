@@ -110,6 +110,7 @@ bool pow2_supported(int n);
 // Stockham stage twiddles of the line FFT of length n (false: no kernels for n).
 bool twiddles(int n, std::vector<float2> &out);
 bool is_device_ptr(const void *p);
+bool is_pinned_host(const void *p);
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point.
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();

@@ -1131,6 +1131,18 @@ bool is_device_ptr(const void *p)
     }
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
+
+// Page-locked host memory (cudaHostAlloc / cudaHostRegister): a copy to it
+// may be captured into a graph and runs asynchronously.
+bool is_pinned_host(const void *p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
 }  // namespace msk
 
 namespace {
@@ -2586,6 +2598,7 @@ struct SpecPlan {
     size_t o_tab = 0, o_atoms = 0, o_soff = 0, o_act = 0, o_meta = 0;  // upload region
     size_t o_fres = 0, o_psi = 0, o_tbuf = 0, o_img = 0;               // work region
     bool img_dev = false;
+    bool img_pinned = false;  // host images in page-locked memory: copied on the lane
     double work = 0.0;
     int lane = 0;
 };
@@ -2770,6 +2783,7 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
         }
         q.work = (double)na * q.nslices * q.gp.nx * q.gp.ny;
         q.img_dev = ndefocus > 0 && is_device_ptr(spec[i].images);
+        q.img_pinned = ndefocus > 0 && !q.img_dev && is_pinned_host(spec[i].images);
     });
 
     // waves of specimens whose arena fits the memory budget
@@ -2870,11 +2884,23 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
         if (graph)
             MSK_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed));
         int rc = MSK_OK;
+        // a specimen's images to page-locked host memory on its own lane, as
+        // soon as they are made (beside the other lanes' kernels)
+        auto images_out = [&](int i, cudaStream_t st_) -> int {
+            if (ndefocus == 0 || !P[i].img_pinned) return MSK_OK;
+            const size_t bytes = (size_t)P[i].nangles * ndefocus * P[i].gp.nx * P[i].gp.ny * sizeof(float);
+            if (cudaMemcpyAsync(spec[i].images, arena + P[i].o_img, bytes, cudaMemcpyDeviceToHost,
+                                st_) != cudaSuccess)
+                return fail(ctx, MSK_ECUDA, "image copy");
+            count_copy(ctx, 1, (double)bytes);
+            return MSK_OK;
+        };
         if (nl == 1) {
             for (int i : lane_of[0]) {
                 float *dimg = P[i].img_dev ? spec[i].images : reinterpret_cast<float *>(arena + P[i].o_img);
                 if ((rc = enqueue_specimen(ctx, P[i], arena, s, ndefocus, defocus, dimg, ctx->stream)))
                     break;
+                if ((rc = images_out(i, ctx->stream))) break;
             }
         } else {
             cudaEvent_t fork = ctx->lane_ev[kLanes];
@@ -2889,6 +2915,7 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
                     if ((rc = enqueue_specimen(ctx, P[i], arena, s, ndefocus, defocus, dimg,
                                                ctx->lanes[l])))
                         break;
+                    if ((rc = images_out(i, ctx->lanes[l]))) break;
                 }
                 if (!rc && cudaEventRecord(ctx->lane_ev[l], ctx->lanes[l]) != cudaSuccess)
                     rc = fail(ctx, MSK_ECUDA, "lane join");
@@ -2917,9 +2944,9 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
             cudaStreamSynchronize(ctx->stream);
             return rc;
         }
-        // images to host buffers
+        // images to pageable host buffers
         for (int i = first; i < last; i++) {
-            if (ndefocus == 0 || P[i].img_dev) continue;
+            if (ndefocus == 0 || P[i].img_dev || P[i].img_pinned) continue;
             const size_t bytes = (size_t)P[i].nangles * ndefocus * P[i].gp.nx * P[i].gp.ny * sizeof(float);
             MSK_CUDA(ctx, cudaMemcpyAsync(spec[i].images, arena + P[i].o_img, bytes,
                                           cudaMemcpyDeviceToHost, ctx->stream));
