@@ -32,6 +32,18 @@ def test_abi_exports_every_declared_symbol(msk):
     assert set(msk.EXPORTS) <= set(names)
 
 
+def test_missing_library_fails_loudly(monkeypatch):
+    """Without libmsk.so the package raises at load: there is no CPU
+    fallback for any call."""
+    import utr_public_gb300 as m
+    monkeypatch.setattr(m, "_lib", None)
+    monkeypatch.setattr(m, "LIB_PATH", os.path.join(ROOT, "no_such_dir", "libmsk.so"))
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        m.load()
+    with pytest.raises(RuntimeError):
+        m.Context(0)
+
+
 def test_status_strings(msk):
     L = msk.load()
     for st in (0, -1, -2, -3, -4, -5, -6, -7, -8):
