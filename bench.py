@@ -136,6 +136,23 @@ def cpu_sample(threads, slices=(60, 70), spec=None):
     return steps / dt, dt, steps
 
 
+def oracle_slice_count():
+    """Slices of the tilt-series workload (the reference's slice scan)."""
+    from oracle import oracle as orc
+    return int(orc.Oracle().slice_count(DZ, FOV))
+
+
+def tilt_config(nang, nslices, world):
+    """The `config` of the tilt-series line, shared by both arms."""
+    return {"workload": "tilt series 1024^2, 160 A box, 20000 atoms in a 120^3 A cube, "
+                        "300 keV, 1 A slices, 180 orientations (1 deg about y) x 2 "
+                        "defoci (0, 500 A); seeded synthetic specimen",
+            "orientations": nang,
+            "slice_steps_per_step": nang * nslices * world, "images_per_step": nang * 2 * world,
+            "l2": "inputs larger than L2 (wave and transmission buffers 2.9 GB per GPU)",
+            "parallelism": "weak: one tilt series per GPU"}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -155,8 +172,7 @@ def run_reference(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": "tilt series 1024^2, 160 A box, 20000 atoms, 300 keV, 1 A slices, "
-                               "180 orientations x 2 defoci", "sample": sample},
+        "config": dict(tilt_config(NANG, oracle_slice_count(), world), sample=sample),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -1157,13 +1173,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "tilt series 1024^2, 160 A box, 20000 atoms in a 120^3 A cube, "
-                               "300 keV, 1 A slices, 180 orientations (1 deg about y) x 2 "
-                               "defoci (0, 500 A); seeded synthetic specimen",
-                   "orientations": nang,
-                   "slice_steps_per_step": steps_per * world, "images_per_step": nang * 2 * world,
-                   "l2": "inputs larger than L2 (wave and transmission buffers 2.9 GB per GPU)",
-                   "parallelism": "weak: one tilt series per GPU"},
+        "config": tilt_config(nang, nslices, world),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": ms_e2e,
                 "matches_device_output": bool(same)},
