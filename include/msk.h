@@ -155,8 +155,10 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
 
 /* Many specimens in one call: MultisliceT.cpp:398-448 run for each specimen,
  * with its own atoms, box, grid and orientations; the common beam, slicing,
- * lens and defocus settings come from `s` (its nx, ny, ctblength,
- * ctblengthz and max_batch are not read).  All specimens' tables, atoms,
+ * lens, incident wave (R1), image plane (rotation, xshift, yshift) and defocus
+ * settings come from `s` (its nx, ny, ctblength, ctblengthz and max_batch are
+ * not read; lwobble = 1: MSK_EUNSUPPORTED, the thermal branches run through
+ * msk_tilt_series).  All specimens' tables, atoms,
  * waves and images live in one device arena (in waves of specimens when they
  * do not fit); specimens run on concurrent streams, longest first.  With
  * flags & MSK_BATCH_GRAPH the launches are captured into one CUDA graph and

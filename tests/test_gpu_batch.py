@@ -80,12 +80,42 @@ def test_batch_pinned_host_images(ctx, msk, graph):
             assert np.array_equal(r, h.numpy())
 
 
+@pytest.mark.parametrize("graph", [True, False])
+def test_batch_spherical_wave_and_image_plane(ctx, msk, graph):
+    """A spherical incident wave and a rotated, shifted image plane: each
+    specimen's images equal msk_tilt_series on that specimen, bit for bit."""
+    cases = batch_case()
+    defoci = [0.0, 200.0]
+    rot = np.array([0.0, 0.3])
+    s = series(msk, aobj=0.02)
+    s.R1 = 4000.0
+    s.rotation = rot.ctypes.data
+    s.xshift, s.yshift = 1.1, -0.6
+    imgs, _ = ctx.tilt_series_batch(s, cases, defoci, graph=graph)
+    for spec, n, aZ, aY in cases:
+        s1 = series(msk, aobj=0.02)
+        s1.R1 = 4000.0
+        s1.rotation = rot.ctypes.data
+        s1.xshift, s1.yshift = 1.1, -0.6
+        s1.nx = s1.ny = n
+        s1.ctblength = s1.ctblengthz = spec.fov
+        ref, _ = ctx.tilt_series(s1, spec.Znum, spec.x, spec.y, spec.z, spec.occ, aZ, aY,
+                                 defoci)
+        im = imgs.pop(0)
+        assert np.array_equal(im, ref)
+
+
 def test_batch_errors(ctx, msk):
     cases = batch_case()[:2]
     s = series(msk)
     bad = [(cases[0][0], 48, cases[0][2], cases[0][3])]
     with pytest.raises(msk.MskError) as e:
         ctx.tilt_series_batch(s, bad, [0.0])
+    assert e.value.status == msk.MSK_EUNSUPPORTED
+    sw = series(msk)
+    sw.lwobble = 1  # the thermal branches run through msk_tilt_series
+    with pytest.raises(msk.MskError) as e:
+        ctx.tilt_series_batch(sw, cases, [0.0])
     assert e.value.status == msk.MSK_EUNSUPPORTED
     spec = sp.random_specimen(10, 32.0, 8.0, 24.0, 7)
     spec.Znum[3] = 104

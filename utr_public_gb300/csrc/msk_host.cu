@@ -2594,9 +2594,10 @@ struct SpecPlan {
     std::vector<unsigned char> tables;
     TableLayout tl;
     std::vector<int> meta;  // per defocus: img_off[n+1] | units[n] | dst[n] | flags[n]
-    float ctblengthz = 0.0f;
-    size_t o_tab = 0, o_atoms = 0, o_soff = 0, o_act = 0, o_meta = 0;  // upload region
-    size_t o_fres = 0, o_psi = 0, o_tbuf = 0, o_img = 0;               // work region
+    float ctblength = 0.0f, ctblengthz = 0.0f;
+    std::vector<float2> wave0;  // spherical incident wave (empty: a plane wave)
+    size_t o_tab = 0, o_atoms = 0, o_soff = 0, o_act = 0, o_meta = 0, o_w0 = 0;  // upload region
+    size_t o_fres = 0, o_psi = 0, o_tbuf = 0, o_img = 0, o_phi = 0, o_fill = 0;  // work region
     bool img_dev = false;
     bool img_pinned = false;  // host images in page-locked memory: copied on the lane
     double work = 0.0;
@@ -2648,9 +2649,16 @@ int enqueue_specimen(msk_context *ctx, SpecPlan &P, unsigned char *arena, const 
     rc = column_map(ctx, &tmapf, tb, nx, ny, na, cop, vf);
     if (rc) return rc;
     const double pl = (double)plane;
-    {
+    // incident wave: a plane wave (in band from the start) or the specimen's
+    // spherical wave (in band after the first propagator pass), as msk_tilt_series
+    bool w_in_band = P.wave0.empty();
+    if (w_in_band) {
         Prof p(ctx, kPlane, 8.0 * pl * na, st);
         k_plane_init<<<1024, 256, 0, st>>>(psi, nullptr, na, nx, ny);
+    } else {
+        Prof p(ctx, kInit, 8.0 * pl * (na + 1), st);
+        rop->row_init(g, nullptr, na, reinterpret_cast<const float2 *>(arena + P.o_w0), psi, 1.0f,
+                      st);
     }
     const int nsl1 = P.nslices + 1;
     for (int sl = 0; sl < P.nslices; sl++) {
@@ -2667,13 +2675,18 @@ int enqueue_specimen(msk_context *ctx, SpecPlan &P, unsigned char *arena, const 
             }
             Prof p(ctx, kTransmit, 24.0 * pl * nact, st);
             rop->row_transmit(g, units, nact, tb, psi, psi, 1.0f / ((float)ny * (float)ny),
-                              s->nmode == 0, st);
+                              s->nmode == 0 && w_in_band, st);
         }
         if (s->nmode == 0) {
             Prof p(ctx, kKColProp, 16.0 * pl * na, st);
-            cop->col_prop(g, pmap, pmap, nullptr, na, 1, st);  // plane-wave start: in band
+            cop->col_prop(g, pmap, pmap, nullptr, na, w_in_band ? 1 : 0, st);
+            w_in_band = true;
         }
     }
+    // image plane (autosliccmd.cpp:1119-1143): rotation centre and whole-pixel shift
+    const double xst = P.ctblength / nx, yst = P.ctblength / ny;  // float divisions
+    const double xcen = 0.5 * P.ctblength + s->dxc, ycen = 0.5 * P.ctblength + s->dyc;
+    const int sxp = (int)floor(s->xshift / xst + 0.5), syp = (int)floor(s->yshift / yst + 0.5);
     const double pi = 4.0 * atan(1.0), l = gp.wavlen;
     float k2maxo = s->aobj / gp.wavlen;
     k2maxo = k2maxo * k2maxo;
@@ -2700,6 +2713,27 @@ int enqueue_specimen(msk_context *ctx, SpecPlan &P, unsigned char *arena, const 
             cop->col_fresnel(g, pmapf, tmapf, nullptr, na, fr, 1.0f, st);
         }
         const int *dm = reinterpret_cast<const int *>(arena + P.o_meta) + (size_t)d * nmeta;
+        const double rot = s->rotation ? s->rotation[d] : 0.0;
+        if (rot != 0.0 || sxp != 0 || syp != 0) {
+            // the amplitude in real space, rotated and shifted, then |.|^2
+            float2 *phi = reinterpret_cast<float2 *>(arena + P.o_phi);
+            float2 *fill = reinterpret_cast<float2 *>(arena + P.o_fill);
+            {
+                Prof p(ctx, kExit, 16.0 * pl * na, st);
+                rop->row_inverse(g, nullptr, na, tb, phi, 1.0f, st);
+            }
+            k_edge_mean<<<na, 256, 0, st>>>(phi, nullptr, nx, ny, 5, fill);
+            {
+                Prof p(ctx, kRotShift, 16.0 * pl * na, st);
+                k_rotate_shift<<<8 * 152, 256, 0, st>>>(phi, tb, nullptr, na, nx, ny, xst, yst, xcen,
+                                                        ycen, cos(rot), sin(rot), rot != 0.0, sxp,
+                                                        syp, fill);
+            }
+            Prof p(ctx, kIntensity, 12.0 * pl * na, st);
+            k_intensity_direct<<<8 * 152, 256, 0, st>>>(na, dm, dm + na + 1, dm + 2 * na + 1,
+                                                        dm + 3 * na + 1, tb, d_images, plane, 1.0f);
+            continue;
+        }
         Prof p(ctx, kIntensity, 12.0 * pl * na, st);
         rop->row_intensity(g, na, dm, dm + na + 1, dm + 2 * na + 1, dm + 3 * na + 1, tb, d_images,
                            1.0f, st);
@@ -2718,9 +2752,8 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
     ctx->err.clear();
     if (!s || nspec < 1 || !spec || ndefocus < 0 || (ndefocus > 0 && !defocus))
         return fail(ctx, MSK_EINVAL, "bad batch arguments");
-    if (s->lwobble || s->R1 != 0.0 || s->rotation || s->xshift != 0.0 || s->yshift != 0.0)
-        return fail(ctx, MSK_EUNSUPPORTED,
-                    "batches take plane waves without thermal branches or image rotation");
+    if (s->lwobble)
+        return fail(ctx, MSK_EUNSUPPORTED, "batches take no thermal branches");
     for (int i = 0; i < nspec; i++) {
         const msk_specimen &q = spec[i];
         if (q.natom < 0 || q.nangles < 1 || !q.angleZ || !q.angleY ||
@@ -2752,6 +2785,7 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
             return fail(ctx, MSK_EUNSUPPORTED, "band limit is not two index ranges per column");
         P[i].nslices = slice_count(s->deltaz, q.ctblengthz);
         P[i].nangles = q.nangles;
+        P[i].ctblength = q.ctblength;
         P[i].ctblengthz = q.ctblengthz;
         P[i].ua.resize(q.nangles);
         for (int a = 0; a < q.nangles; a++) units.push_back({i, a});
@@ -2784,7 +2818,12 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
         q.work = (double)na * q.nslices * q.gp.nx * q.gp.ny;
         q.img_dev = ndefocus > 0 && is_device_ptr(spec[i].images);
         q.img_pinned = ndefocus > 0 && !q.img_dev && is_pinned_host(spec[i].images);
+        if (s->R1 != 0.0) spherical_wave(q.gp.nx, q.gp.ny, q.ctblength, s->v0, s->R1, q.wave0);
     });
+    // image-plane rotation or shift of some detector plane: per specimen a real-space
+    // scratch grid per orientation and the edge means
+    bool image_plane = s->xshift != 0.0 || s->yshift != 0.0;
+    for (int d = 0; d < ndefocus && s->rotation; d++) image_plane |= s->rotation[d] != 0.0;
 
     // waves of specimens whose arena fits the memory budget
     size_t free_b = 0, total_b = 0;
@@ -2802,6 +2841,8 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
         up += align256(std::max<size_t>(q.b.act.size(), 1) * sizeof(int));
         q.o_meta = up;
         up += align256(std::max<size_t>(q.meta.size(), 1) * sizeof(int));
+        q.o_w0 = up;
+        up += align256(q.wave0.size() * sizeof(float2));
         q.o_fres = work;
         work += align256((size_t)std::max(ndefocus, 1) * plane * sizeof(float2));
         q.o_psi = work;
@@ -2810,6 +2851,10 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
         work += align256((size_t)q.nangles * plane * sizeof(float2));
         q.o_img = work;
         if (!q.img_dev) work += align256((size_t)q.nangles * ndefocus * plane * sizeof(float));
+        q.o_phi = work;
+        if (image_plane) work += align256((size_t)q.nangles * plane * sizeof(float2));
+        q.o_fill = work;
+        if (image_plane) work += align256((size_t)q.nangles * sizeof(float2));
     };
     const bool graph = (flags & MSK_BATCH_GRAPH) && !ctx->prof_on;
     int first = 0;
@@ -2830,6 +2875,8 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
             P[i].o_psi += align256(up);
             P[i].o_tbuf += align256(up);
             P[i].o_img += align256(up);
+            P[i].o_phi += align256(up);
+            P[i].o_fill += align256(up);
         }
         const size_t total = align256(up) + work;
         MSK_CUDA(ctx, ctx->arena.reserve(total));
@@ -2845,6 +2892,8 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
                 std::memcpy(&host[q.o_act], q.b.act.data(), q.b.act.size() * sizeof(int));
             if (!q.meta.empty())
                 std::memcpy(&host[q.o_meta], q.meta.data(), q.meta.size() * sizeof(int));
+            if (!q.wave0.empty())
+                std::memcpy(&host[q.o_w0], q.wave0.data(), q.wave0.size() * sizeof(float2));
             bind_tables(q.gp, arena + q.o_tab, q.tl);
         }
         MSK_CUDA(ctx, cudaMemcpyAsync(arena, host.data(), up, cudaMemcpyHostToDevice, ctx->stream));
