@@ -1004,7 +1004,7 @@ int col_variant(msk_context *ctx, const GridPre &gp, int mode)
         }
         auto launch = [&] {
             switch (mode) {
-            case kColMask: cop->col_mask(g, view, view, nullptr, U, 1, ctx->stream); break;
+            case kColMask: cop->col_mask(g, view, view, nullptr, U, 1, 1.0f, ctx->stream); break;
             case kColProp: cop->col_prop(g, view, view, nullptr, U, 1, ctx->stream); break;
             case kColFresnel: cop->col_fresnel(g, view, view, nullptr, U, fr, 1.0f, ctx->stream); break;
             default: cop->col_dw(g, view, nullptr, U, fr.dw, 1, ctx->stream); break;
@@ -1301,7 +1301,9 @@ int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode, b
             }
             {
                 Prof p(ctx, kKColMask, 16.0 * plane * na, sA);
-                cop->col_mask(g, tmaps[k], tmaps[k], units, na, 1, sA);
+                // B = S(t_bl) / ny^2: the transmit's 1/ny^2, exact, carried here
+                cop->col_mask(g, tmaps[k], tmaps[k], units, na, 1,
+                              1.0f / ((float)gp.ny * (float)gp.ny), sA);
             }
             if (overlap) {
                 MSK_CUDA(ctx, cudaEventRecord(ctx->ev_t[k], sA));
@@ -1309,8 +1311,7 @@ int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode, b
             }
             {
                 Prof p(ctx, kTransmit, 24.0 * plane * na, sB);
-                rop->row_transmit(g, units, na, tb, psi, psi, 1.0f / ((float)gp.ny * (float)gp.ny),
-                                  nmode == 0 && w_in_band, sB);
+                rop->row_transmit(g, units, na, tb, psi, psi, 1.0f, nmode == 0 && w_in_band, sB);
             }
             if (overlap) {
                 MSK_CUDA(ctx, cudaEventRecord(ctx->ev_free[k], sB));
@@ -2257,7 +2258,8 @@ int stack_run(msk_context *ctx, const StackJob &J)
                 rop->row_expv(g, nb, vslice(k), ustride, dst, ctx->stream);
             }
             Prof p(ctx, kKColMask, 16.0 * P * nb);
-            cop->col_mask(g, map_of(dst, vmask), map_of(dst, vmask), nullptr, nb, 1, ctx->stream);
+            cop->col_mask(g, map_of(dst, vmask), map_of(dst, vmask), nullptr, nb, 1, 1.0f,
+                          ctx->stream);
         };
         // P3 + P4 of one slice: out = W(K[p](iS(in) t))
         auto step = [&](const float2 *tb, const float2 *in, float2 *out) {
@@ -2388,7 +2390,7 @@ int stack_run(msk_context *ctx, const StackJob &J)
                 {
                     Prof p(ctx, kKColMask, 16.0 * P * nb);  // g_e = K[M] g_t
                     cop->col_mask(g, map_of(trans[k - 1], vmask), map_of(trans[k - 1], vmask),
-                                  nullptr, nb, 0, ctx->stream);
+                                  nullptr, nb, 0, 1.0f, ctx->stream);
                 }
                 {
                     Prof p(ctx, kGrad, 16.0 * P * nb);
@@ -2419,7 +2421,7 @@ int stack_run(msk_context *ctx, const StackJob &J)
                     {
                         Prof p(ctx, kKColMask, 16.0 * P * nb);  // g_e = K[M] g_t
                         cop->col_mask(g, map_of(Bb[j - 1], vmask), map_of(Bb[j - 1], vmask), nullptr, nb, 0,
-                                      ctx->stream);
+                                      1.0f, ctx->stream);
                     }
                     {
                         Prof p(ctx, kGrad, 16.0 * P * nb);
@@ -2671,11 +2673,11 @@ int enqueue_specimen(msk_context *ctx, SpecPlan &P, unsigned char *arena, const 
             }
             {
                 Prof p(ctx, kKColMask, 16.0 * pl * nact, st);
-                cop->col_mask(g, tmap, tmap, units, nact, 1, st);
+                // B = S(t_bl) / ny^2: the transmit's 1/ny^2, exact, carried here
+                cop->col_mask(g, tmap, tmap, units, nact, 1, 1.0f / ((float)ny * (float)ny), st);
             }
             Prof p(ctx, kTransmit, 24.0 * pl * nact, st);
-            rop->row_transmit(g, units, nact, tb, psi, psi, 1.0f / ((float)ny * (float)ny),
-                              s->nmode == 0 && w_in_band, st);
+            rop->row_transmit(g, units, nact, tb, psi, psi, 1.0f, s->nmode == 0 && w_in_band, st);
         }
         if (s->nmode == 0) {
             Prof p(ctx, kKColProp, 16.0 * pl * na, st);

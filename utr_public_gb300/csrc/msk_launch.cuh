@@ -36,9 +36,10 @@ struct SizeOps {
     void (*row_dwexp)(const Geom &, const int *units, int nunits, const float2 *spec,
                       float2 *tbuf, cudaStream_t);
     // band != 0: only the in-band column blocks (Geom::cb_*); the others must
-    // be zero in the input and stay zero in the output buffer
+    // be zero in the input and stay zero in the output buffer.  col_mask scales
+    // its output by post / nx (post: a power of two the next pass would apply)
     void (*col_mask)(const Geom &, const ColView &in, const ColView &out,
-                     const int *units, int nunits, int band, cudaStream_t);
+                     const int *units, int nunits, int band, float post, cudaStream_t);
     void (*col_prop)(const Geom &, const ColView &in, const ColView &out,
                      const int *units, int nunits, int band, cudaStream_t);
     void (*col_fresnel)(const Geom &, const ColView &in, const ColView &out,
@@ -171,9 +172,9 @@ struct Launch {
             colv<MODE, 0>(g, in.map, out.map, units, nunits, fr, scale, band, s);
     }
     static void col_mask(const Geom &g, const ColView &in, const ColView &out,
-                         const int *units, int nunits, int band, cudaStream_t s)
+                         const int *units, int nunits, int band, float post, cudaStream_t s)
     {
-        col<kColMask>(g, in, out, units, nunits, Fresnel{}, 1.0f / (float)g.nx, band, s);
+        col<kColMask>(g, in, out, units, nunits, Fresnel{}, post / (float)g.nx, band, s);
     }
     static void col_prop(const Geom &g, const ColView &in, const ColView &out,
                          const int *units, int nunits, int band, cudaStream_t s)

@@ -533,8 +533,13 @@ k_row_transmit(const Geom g, const int *__restrict__ units, const float2 *__rest
                     : cmul(v[m], bufB[l * NY + t + m * T]);
     fft_line<NY, false, 1, BLK>(v, bufW + l * P::PADN, 0, t, g.tw_row);
     __syncthreads();
+    if (out_scale == 1.0f) {  // the scale already carried by B (no multiply)
 #pragma unroll
-    for (int m = 0; m < E; m++) bufW[l * NY + t + m * T] = cscale(v[m], out_scale);
+        for (int m = 0; m < E; m++) bufW[l * NY + t + m * T] = v[m];
+    } else {
+#pragma unroll
+        for (int m = 0; m < E; m++) bufW[l * NY + t + m * T] = cscale(v[m], out_scale);
+    }
     if (band) {  // in-band segments only: `out` holds zeros out of band, the
                  // propagator that follows zeroes those columns
         store_band_rows<NY>(g, bufW, rows, out + off);
