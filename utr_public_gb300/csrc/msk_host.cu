@@ -514,7 +514,8 @@ static bool grid_pre(GridPre &gp, int nx, int ny, float ax, float by, float v0, 
     gp.propy.resize(ny);
     for (int ix = 0; ix < nx; ix++) {
         const double t = scale * (gp.kx2[ix] * gp.wavlen - gp.kx[ix] * tctx);
-        gp.propx[ix] = make_float2((float)cos(t), (float)-sin(t));
+        // with the propagator pass's 1/nx (a power of two: exact)
+        gp.propx[ix] = make_float2((float)cos(t) / (float)nx, (float)-sin(t) / (float)nx);
     }
     for (int iy = 0; iy < ny; iy++) {
         const double t = scale * (gp.ky2[iy] * gp.wavlen - gp.ky[iy] * tcty);
@@ -3397,7 +3398,7 @@ extern "C" int msk_tilt_series_per_angle(msk_context *ctx, const msk_series *s, 
             }
             if (s->nmode == 0) {
                 FFT(psi, CUFFT_INVERSE);
-                k_plain_kmul<1><<<G, TB, 0, sm>>>(g, invN, psi);
+                k_plain_kmul<1><<<G, TB, 0, sm>>>(g, invN * (float)nx, psi);  // propx holds 1/nx
                 FFT(psi, CUFFT_FORWARD);
             }
         }

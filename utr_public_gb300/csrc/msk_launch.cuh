@@ -179,7 +179,8 @@ struct Launch {
     static void col_prop(const Geom &g, const ColView &in, const ColView &out,
                          const int *units, int nunits, int band, cudaStream_t s)
     {
-        col<kColProp>(g, in, out, units, nunits, Fresnel{}, 1.0f / (float)g.nx, band, s);
+        // the 1/nx of the column transforms is in the propx table
+        col<kColProp>(g, in, out, units, nunits, Fresnel{}, 1.0f, band, s);
     }
     static void col_dw(const Geom &g, const ColView &spec, const int *units, int nunits,
                        const float *dw, int dw_stride, cudaStream_t s)

@@ -414,18 +414,15 @@ k_col_pass(const Geom g, const __grid_constant__ CUtensorMap in_map,
             v[m] = (ix <= ab.x || ix >= ab.y) ? cscale(v[m], fscale) : make_float2(0.0f, 0.0f);
         }
     } else if constexpr (MODE == kColProp) {
-        // kx2 < k2max and kx2 + ky2 < k2max: the same index set as the band limit
+        // kx2 < k2max and kx2 + ky2 < k2max: the same index set as the band
+        // limit; propx carries the 1/nx of the transforms (fscale is 1)
         const int2 ab = __ldg(&g.kband[iy]);
-        const float2 py = cscale(__ldg(&g.propy[iy]), 1.0f);
+        const float2 py = __ldg(&g.propy[iy]);
 #pragma unroll
         for (int m = 0; m < E; m++) {
             const int ix = t + m * T;
-            if (ix <= ab.x || ix >= ab.y) {
-                const float2 w = cmul(cmul(v[m], py), __ldg(&g.propx[ix]));
-                v[m] = cscale(w, fscale);
-            } else {
-                v[m] = make_float2(0.0f, 0.0f);
-            }
+            v[m] = (ix <= ab.x || ix >= ab.y) ? cmul(cmul(v[m], py), __ldg(&g.propx[ix]))
+                                              : make_float2(0.0f, 0.0f);
         }
     } else if constexpr (MODE == kColDW) {
         const float mb4 = __ldg(&fr.dw[(size_t)u * fr.dw_stride]);

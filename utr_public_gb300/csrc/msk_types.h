@@ -22,7 +22,7 @@ struct Geom {
     float lut_c0, lut_c1;  // knot index of r^2 ~ (log(r^2) + lut_c0) * lut_c1
     const float *kx2;   // [nx] kx^2 (freqn, float)
     const float *ky2;   // [ny]
-    const float2 *propx;  // [nx] (cos t, -sin t), t = pi dz (kx^2 lambda - kx 2 tan(tilt_x))
+    const float2 *propx;  // [nx] (cos t, -sin t) / nx, t = pi dz (kx^2 lambda - kx 2 tan(tilt_x))
     const float2 *propy;  // [ny]
     const int2 *kband;    // [ny] (A, B): kx2[ix] + ky2[iy] < k2max  <=>  ix <= A or ix >= B
     // Columns iy with ky2[iy] >= k2max are zeroed whole by the band limit and
