@@ -494,14 +494,15 @@ bool sizes_ok(int n) { return utr_ops(n) != nullptr && size_ops(n) != nullptr; }
 // 2D view of `units` blocks of `lines` rows x `width` complex64 for a UTR
 // column pass over lines of length `lines` (box: its UtrColCfg tile).
 int utr_column_map(msk_context *ctx, ColView *view, void *base, int lines, size_t width,
-                   size_t units)
+                   size_t units, bool final_pass = false)
 {
     auto enc = tensor_map_encoder();
     if (!enc) return fail(ctx, MSK_ECUDA, "cuTensorMapEncodeTiled is not available");
     const UtrOps *op = utr_ops(lines);
     const cuuint64_t dims[2] = {(cuuint64_t)2 * width, (cuuint64_t)units * lines};
     const cuuint64_t strides[1] = {(cuuint64_t)width * 8};
-    const cuuint32_t box[2] = {(cuuint32_t)(2 * op->col_c), (cuuint32_t)op->col_box_rows};
+    const cuuint32_t box[2] = {(cuuint32_t)(2 * (final_pass ? op->col_c_final : op->col_c)),
+                               (cuuint32_t)op->col_box_rows};
     const cuuint32_t estr[2] = {1, 1};
     CUresult r = enc(&view->map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box,
                      estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -894,7 +895,7 @@ int msk_utr_reconstruct_planes(msk_context *ctx, const msk_utr *p, int nangles,
     }
     ColView vy, vz;
     if ((st = utr_column_map(ctx, &vy, vol, ny, nx, (size_t)nz))) return st;
-    if ((st = utr_column_map(ctx, &vz, vol, nz, (size_t)nx * ny, 1))) return st;
+    if ((st = utr_column_map(ctx, &vz, vol, nz, (size_t)nx * ny, 1, true))) return st;
     UtrCol cy{};
     cy.width = nx;
     cy.tw = tw_y;
@@ -932,7 +933,7 @@ int msk_utr_reconstruct_planes(msk_context *ctx, const msk_utr *p, int nangles,
     // copy (nz rows of the chunk's ny/nch x nx floats, one 2D copy) on the
     // copy-out stream while the z pass of chunk c + 1 runs.
     const int nch = out_dev ? 1 : std::min(8, ny);
-    const int cpc = utr_ops(nz)->col_c;                       // columns per block
+    const int cpc = utr_ops(nz)->col_c_final;                 // columns per block
     const int ncb = (int)((size_t)nx * (ny / nch) / cpc);     // blocks per chunk
     if (!out_dev && !ctx->stk_ev[0])
         for (cudaEvent_t &e : ctx->stk_ev)

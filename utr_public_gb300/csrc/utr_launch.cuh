@@ -12,6 +12,7 @@ namespace msk {
 struct UtrOps {
     int n;
     int col_c, col_box_rows;  // column tile width and TMA box height (UtrColCfg)
+    int col_c_final;          // the final z pass's tile width (UtrColCfg<n, true>)
     // rows of images (x lines of length n)
     void (*img_rows)(const UtrImg &, const float *img, float2 *k2, cudaStream_t);
     // rows of the volume (x lines of length n): gridding sums -> inverse FFT
@@ -49,7 +50,7 @@ template <int N> struct UtrLaunch {
                     cudaStream_t s)
     {
         static std::once_flag f;
-        using CC = UtrColCfg<N>;
+        using CC = UtrColCfg<N, MODE == kUtrColFinal>;
         set_smem(k_utr_col<N, MODE>, CC::SMEM, f);
         const int bpu = p.ncb > 0 ? p.ncb : p.width / CC::C;
         k_utr_col<N, MODE><<<units * bpu, CC::NT, CC::SMEM, s>>>(p, in, out);
@@ -70,7 +71,8 @@ template <int N> struct UtrLaunch {
     }
     static const UtrOps *ops()
     {
-        static const UtrOps o = {N,       UtrColCfg<N>::C, UtrColCfg<N>::BR, img_rows,
+        static const UtrOps o = {N,       UtrColCfg<N>::C, UtrColCfg<N>::BR, UtrColCfg<N, true>::C,
+                                 img_rows,
                                  fourier_rows, col_img, col_vol, col_final};
         return &o;
     }

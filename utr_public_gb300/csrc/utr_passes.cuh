@@ -282,11 +282,13 @@ k_utr_fourier_rows(const UtrFourier f, const float2 *__restrict__ tw, const UtrA
 enum { kUtrColImg = 0, kUtrColVol = 1, kUtrColFinal = 2 };
 
 // Column tiles of the UTR passes: C lines of N points with 256 threads
-// (capped at 16 lines), so that every row of a tile is C * 8 >= 32 bytes:
-// the z pass reads lines whose points lie nx * ny * 8 bytes apart.
-template <int N> struct UtrColCfg {
+// (capped at 16 lines), so that every row of a tile is C * 8 >= 32 bytes;
+// WIDE (the final z pass, whose line points lie nx * ny * 8 bytes apart):
+// 512 threads, twice the lines, 128-byte tile rows at 1024 points.
+template <int N, bool WIDE = false> struct UtrColCfg {
     static constexpr int T = FftPlan<N>::T;
-    static constexpr int C = (256 / T) < 2 ? 2 : ((256 / T) > 16 ? 16 : 256 / T);
+    static constexpr int TH = WIDE ? 512 : 256;
+    static constexpr int C = (TH / T) < 2 ? 2 : ((TH / T) > 16 ? 16 : TH / T);
     static constexpr int NT = C * T;
     static constexpr int BR = N < 256 ? N : 256;  // rows per TMA box
     static constexpr int NBOX = N / BR;
@@ -309,12 +311,12 @@ struct UtrCol {
 };
 
 template <int N, int MODE>
-__global__ void __launch_bounds__(UtrColCfg<N>::NT)
+__global__ void __launch_bounds__(UtrColCfg<N, MODE == kUtrColFinal>::NT)
 k_utr_col(const UtrCol p, const __grid_constant__ CUtensorMap in_map,
           const __grid_constant__ CUtensorMap out_map)
 {
     using P = FftPlan<N>;
-    using CC = UtrColCfg<N>;
+    using CC = UtrColCfg<N, MODE == kUtrColFinal>;
     constexpr int T = P::T, E = P::E, C = CC::C;
     extern __shared__ __align__(128) unsigned char smem[];
     float2 *buf = reinterpret_cast<float2 *>(smem);
