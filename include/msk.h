@@ -155,10 +155,11 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
 
 /* Many specimens in one call: MultisliceT.cpp:398-448 run for each specimen,
  * with its own atoms, box, grid and orientations; the common beam, slicing,
- * lens, incident wave (R1), image plane (rotation, xshift, yshift) and defocus
- * settings come from `s` (its nx, ny, ctblength, ctblengthz and max_batch are
- * not read; lwobble = 1: MSK_EUNSUPPORTED, the thermal branches run through
- * msk_tilt_series).  All specimens' tables, atoms,
+ * lens, incident wave (R1), image plane (rotation, xshift, yshift), thermal
+ * and defocus settings come from `s` (its nx, ny, ctblength, ctblengthz,
+ * max_batch and wobble are not read).  One configuration per orientation:
+ * lwobble = 1 is the Debye-Waller branch, with each specimen's wobble
+ * (msk_tilt_series with nconfig = 1).  All specimens' tables, atoms,
  * waves and images live in one device arena (in waves of specimens when they
  * do not fit); specimens run on concurrent streams, longest first.  With
  * flags & MSK_BATCH_GRAPH the launches are captured into one CUDA graph and
@@ -173,6 +174,7 @@ typedef struct {
     const double *angleZ, *angleY;    /* radians */
     float *images;   /* out: float[nangles][ndefocus][nx][ny], host or device */
     int *kept;       /* out (may be NULL): int[nangles] */
+    const float *wobble;  /* rms displacement at 300 K per atom (host; s->lwobble = 1) */
 } msk_specimen;
 
 enum { MSK_BATCH_GRAPH = 1 };

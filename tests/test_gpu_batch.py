@@ -105,6 +105,27 @@ def test_batch_spherical_wave_and_image_plane(ctx, msk, graph):
         assert np.array_equal(im, ref)
 
 
+def test_batch_debye_waller(ctx, msk):
+    """lwobble = 1 (one configuration: the Debye-Waller branch) with each
+    specimen's wobble: images equal msk_tilt_series on that specimen."""
+    cases = batch_case()
+    for i, (spec, _, _, _) in enumerate(cases):
+        spec.wobble = (0.03 + 0.02 * ((np.arange(spec.natom) + i) % 5)).astype(np.float32)
+    defoci = [0.0, 150.0]
+    s = series(msk)
+    s.lwobble, s.temperature = 1, 290.0
+    imgs, _ = ctx.tilt_series_batch(s, cases, defoci)
+    for (spec, n, aZ, aY), im in zip(cases, imgs):
+        s1 = series(msk)
+        s1.lwobble, s1.temperature = 1, 290.0
+        s1.wobble = spec.wobble.ctypes.data
+        s1.nx = s1.ny = n
+        s1.ctblength = s1.ctblengthz = spec.fov
+        ref, _ = ctx.tilt_series(s1, spec.Znum, spec.x, spec.y, spec.z, spec.occ, aZ, aY,
+                                 defoci)
+        assert np.array_equal(im, ref)
+
+
 def test_batch_errors(ctx, msk):
     cases = batch_case()[:2]
     s = series(msk)
@@ -113,10 +134,12 @@ def test_batch_errors(ctx, msk):
         ctx.tilt_series_batch(s, bad, [0.0])
     assert e.value.status == msk.MSK_EUNSUPPORTED
     sw = series(msk)
-    sw.lwobble = 1  # the thermal branches run through msk_tilt_series
+    sw.lwobble = 1  # the Debye-Waller branch needs each specimen's wobble
+    for spec, _, _, _ in cases:
+        spec.wobble = None
     with pytest.raises(msk.MskError) as e:
         ctx.tilt_series_batch(sw, cases, [0.0])
-    assert e.value.status == msk.MSK_EUNSUPPORTED
+    assert e.value.status == msk.MSK_EINVAL
     spec = sp.random_specimen(10, 32.0, 8.0, 24.0, 7)
     spec.Znum[3] = 104
     with pytest.raises(msk.MskError) as e:

@@ -90,7 +90,7 @@ class SpecimenDesc(C.Structure):
                 ("z", C.c_void_p), ("occ", C.c_void_p), ("nx", C.c_int), ("ny", C.c_int),
                 ("ctblength", C.c_float), ("ctblengthz", C.c_float), ("nangles", C.c_int),
                 ("angleZ", C.c_void_p), ("angleY", C.c_void_p), ("images", C.c_void_p),
-                ("kept", C.c_void_p)]
+                ("kept", C.c_void_p), ("wobble", C.c_void_p)]
 
 
 class Plane(C.Structure):
@@ -399,7 +399,8 @@ class Context:
 
     def tilt_series_batch(self, series, specimens, defocus, graph=True, images=None):
         """Many specimens in one call (msk_tilt_series_batch).  specimens: list
-        of (Specimen-like with Znum/x/y/z/occ/fov, n, angleZ, angleY[, ctblengthz]);
+        of (Specimen-like with Znum/x/y/z/occ/fov and, for series.lwobble = 1, a
+        float32 `wobble` per atom, n, angleZ, angleY[, ctblengthz]);
         returns (images list [nangles, ndef, n, n] per specimen, kept list).
         images may be a list of preallocated arrays or torch CUDA tensors."""
         defocus = np.ascontiguousarray(defocus, np.float64)
@@ -427,6 +428,11 @@ class Context:
             d.nangles = len(aZ)
             d.angleZ, d.angleY = _ptr(aZ), _ptr(aY)
             d.images, d.kept = _ptr(img), _ptr(kp)
+            wob = getattr(sp_, "wobble", None)
+            if wob is not None:
+                wob = np.ascontiguousarray(wob, np.float32)
+                keep.append(wob)
+                d.wobble = _ptr(wob)
         st = self.L.msk_tilt_series_batch(self.h, C.byref(series), len(specimens), descs, nd,
                                           _ptr(defocus), MSK_BATCH_GRAPH if graph else 0)
         self._check(st)

@@ -2601,6 +2601,7 @@ struct SpecPlan {
     std::vector<float2> wave0;  // spherical incident wave (empty: a plane wave)
     size_t o_tab = 0, o_atoms = 0, o_soff = 0, o_act = 0, o_meta = 0, o_w0 = 0;  // upload region
     size_t o_fres = 0, o_psi = 0, o_tbuf = 0, o_img = 0, o_phi = 0, o_fill = 0;  // work region
+    size_t o_dw = 0, o_spec = 0;  // Debye-Waller branch: -B/4 per (unit, slice); S(v) grids
     bool img_dev = false;
     bool img_pinned = false;  // host images in page-locked memory: copied on the lane
     double work = 0.0;
@@ -2642,7 +2643,7 @@ int enqueue_specimen(msk_context *ctx, SpecPlan &P, unsigned char *arena, const 
     // views for each pass's tile variant (chosen before any capture begins)
     const int vm = col_variant(ctx, gp, kColMask), vp = col_variant(ctx, gp, kColProp),
               vf = col_variant(ctx, gp, kColFresnel);
-    ColView pmap, tmap, pmapf, tmapf;
+    ColView pmap, tmap, pmapf, tmapf, smap;
     int rc = column_map(ctx, &pmap, psi, nx, ny, na, cop, vp);
     if (rc) return rc;
     rc = column_map(ctx, &tmap, tb, nx, ny, na, cop, vm);
@@ -2651,6 +2652,12 @@ int enqueue_specimen(msk_context *ctx, SpecPlan &P, unsigned char *arena, const 
     if (rc) return rc;
     rc = column_map(ctx, &tmapf, tb, nx, ny, na, cop, vf);
     if (rc) return rc;
+    // Debye-Waller branch (trlayerDW): S(v) of each unit in its own grid
+    const bool dw = !P.b.dw.empty();
+    float2 *spec = reinterpret_cast<float2 *>(arena + P.o_spec);
+    const float *dwf = reinterpret_cast<const float *>(arena + P.o_dw);
+    if (dw && (rc = column_map(ctx, &smap, spec, nx, ny, na, cop, col_variant(ctx, gp, kColDW))))
+        return rc;
     const double pl = (double)plane;
     // incident wave: a plane wave (in band from the start) or the specimen's
     // spherical wave (in band after the first propagator pass), as msk_tilt_series
@@ -2668,7 +2675,18 @@ int enqueue_specimen(msk_context *ctx, SpecPlan &P, unsigned char *arena, const 
         const int nact = P.b.act_off[sl + 1] - P.b.act_off[sl];
         const int *units = act + P.b.act_off[sl];
         if (nact > 0) {
-            {
+            if (dw) {  // S(v), the damping, then A = S(exp(i sigma v')), as run_slices
+                {
+                    Prof p(ctx, kSplat, 8.0 * pl * nact, st);
+                    rop->splat_spec(g, units, nact, sl, nsl1, soff, atoms, spec, st);
+                }
+                {
+                    Prof p(ctx, kDW, 16.0 * pl * nact, st);
+                    cop->col_dw(g, smap, units, nact, dwf + sl, P.nslices, st);
+                }
+                Prof p(ctx, kDWExp, 16.0 * pl * nact, st);
+                rop->row_dwexp(g, units, nact, spec, tb, st);
+            } else {
                 Prof p(ctx, kSplat, 8.0 * pl * nact, st);
                 rop->splat(g, units, nact, sl, nsl1, soff, atoms, tb, st);
             }
@@ -2755,10 +2773,10 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
     ctx->err.clear();
     if (!s || nspec < 1 || !spec || ndefocus < 0 || (ndefocus > 0 && !defocus))
         return fail(ctx, MSK_EINVAL, "bad batch arguments");
-    if (s->lwobble)
-        return fail(ctx, MSK_EUNSUPPORTED, "batches take no thermal branches");
     for (int i = 0; i < nspec; i++) {
         const msk_specimen &q = spec[i];
+        if (s->lwobble && q.natom > 0 && !q.wobble)
+            return fail(ctx, MSK_EINVAL, "lwobble needs each specimen's wobble array");
         if (q.natom < 0 || q.nangles < 1 || !q.angleZ || !q.angleY ||
             (ndefocus > 0 && !q.images) ||
             (q.natom > 0 && (!q.Znum || !q.x || !q.y || !q.z || !q.occ)))
@@ -2799,6 +2817,11 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
         PrepSpec ps{q.natom, q.Znum, q.x, q.y, q.z, q.occ, q.ctblength, q.ctblengthz, s->deltaz,
                     P[i].nslices, true, q.angleZ[a], q.angleY[a], s->dxc, s->dyc, s->dzc,
                     nullptr, true, ctx->zmap.data()};
+        if (s->lwobble) {  // one configuration: the Debye-Waller branch
+            ps.thermal = kThermDW;
+            ps.wobble = q.wobble;
+            ps.temperature = s->temperature;
+        }
         prep_unit(P[i].gp, ps, P[i].ua[a]);
     });
     for (int i = 0; i < nspec; i++)
@@ -2846,6 +2869,8 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
         up += align256(std::max<size_t>(q.meta.size(), 1) * sizeof(int));
         q.o_w0 = up;
         up += align256(q.wave0.size() * sizeof(float2));
+        q.o_dw = up;
+        up += align256(q.b.dw.size() * sizeof(float));
         q.o_fres = work;
         work += align256((size_t)std::max(ndefocus, 1) * plane * sizeof(float2));
         q.o_psi = work;
@@ -2858,6 +2883,8 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
         if (image_plane) work += align256((size_t)q.nangles * plane * sizeof(float2));
         q.o_fill = work;
         if (image_plane) work += align256((size_t)q.nangles * sizeof(float2));
+        q.o_spec = work;
+        if (!q.b.dw.empty()) work += align256((size_t)q.nangles * plane * sizeof(float2));
     };
     const bool graph = (flags & MSK_BATCH_GRAPH) && !ctx->prof_on;
     int first = 0;
@@ -2880,6 +2907,7 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
             P[i].o_img += align256(up);
             P[i].o_phi += align256(up);
             P[i].o_fill += align256(up);
+            P[i].o_spec += align256(up);
         }
         const size_t total = align256(up) + work;
         MSK_CUDA(ctx, ctx->arena.reserve(total));
@@ -2897,6 +2925,8 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
                 std::memcpy(&host[q.o_meta], q.meta.data(), q.meta.size() * sizeof(int));
             if (!q.wave0.empty())
                 std::memcpy(&host[q.o_w0], q.wave0.data(), q.wave0.size() * sizeof(float2));
+            if (!q.b.dw.empty())
+                std::memcpy(&host[q.o_dw], q.b.dw.data(), q.b.dw.size() * sizeof(float));
             bind_tables(q.gp, arena + q.o_tab, q.tl);
         }
         MSK_CUDA(ctx, cudaMemcpyAsync(arena, host.data(), up, cudaMemcpyHostToDevice, ctx->stream));
@@ -2930,7 +2960,7 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
         }
         // the column tuner runs launches of its own: settle every choice first
         for (int i = first; i < last; i++)
-            for (int mode : {(int)kColMask, (int)kColProp, (int)kColFresnel})
+            for (int mode : {(int)kColMask, (int)kColProp, (int)kColFresnel, (int)kColDW})
                 (void)col_variant(ctx, P[i].gp, mode);
         cudaGraph_t gr = nullptr;
         if (graph)
