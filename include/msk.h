@@ -157,9 +157,10 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
  * with its own atoms, box, grid and orientations; the common beam, slicing,
  * lens, incident wave (R1), image plane (rotation, xshift, yshift), thermal
  * and defocus settings come from `s` (its nx, ny, ctblength, ctblengthz,
- * max_batch and wobble are not read).  One configuration per orientation:
- * lwobble = 1 is the Debye-Waller branch, with each specimen's wobble
- * (msk_tilt_series with nconfig = 1).  All specimens' tables, atoms,
+ * max_batch and wobble are not read).  With lwobble = 1 and one configuration
+ * per orientation the Debye-Waller branch, with several (nconfig) random
+ * displacements, each with the specimen's wobble: msk_tilt_series with that
+ * nconfig and no displacements.  All specimens' tables, atoms,
  * waves and images live in one device arena (in waves of specimens when they
  * do not fit); specimens run on concurrent streams, longest first.  With
  * flags & MSK_BATCH_GRAPH the launches are captured into one CUDA graph and
@@ -173,8 +174,12 @@ typedef struct {
     int nangles;
     const double *angleZ, *angleY;    /* radians */
     float *images;   /* out: float[nangles][ndefocus][nx][ny], host or device */
-    int *kept;       /* out (may be NULL): int[nangles] */
+    int *kept;       /* out (may be NULL): int[nangles] (see nconfig) */
     const float *wobble;  /* rms displacement at 300 K per atom (host; s->lwobble = 1) */
+    int nconfig;          /* thermal configurations per orientation (0, 1: one); > 1 needs
+                           * s->lwobble = 1: random displacements drawn in the engine as
+                           * msk_tilt_series does, images averaged; kept then holds
+                           * int[nangles * nconfig] */
 } msk_specimen;
 
 enum { MSK_BATCH_GRAPH = 1 };

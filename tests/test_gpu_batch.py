@@ -126,6 +126,29 @@ def test_batch_debye_waller(ctx, msk):
         assert np.array_equal(im, ref)
 
 
+def test_batch_thermal_configurations(ctx, msk):
+    """lwobble = 1 with three configurations per orientation (random
+    displacements from seed - orientation, images averaged): each specimen
+    equals msk_tilt_series with nconfig = 3, bit for bit."""
+    cases = batch_case()
+    for i, (spec, _, _, _) in enumerate(cases):
+        spec.wobble = (0.04 + 0.02 * ((np.arange(spec.natom) + i) % 3)).astype(np.float32)
+    defoci = [0.0, 150.0]
+    s = series(msk)
+    s.lwobble, s.temperature, s.seed = 1, 300.0, 4711
+    imgs, kept = ctx.tilt_series_batch(s, cases, defoci, nconfig=3)
+    for (spec, n, aZ, aY), im, k in zip(cases, imgs, kept):
+        s1 = series(msk)
+        s1.lwobble, s1.temperature, s1.seed = 1, 300.0, 4711
+        s1.wobble = spec.wobble.ctypes.data
+        s1.nx = s1.ny = n
+        s1.ctblength = s1.ctblengthz = spec.fov
+        ref, k1 = ctx.tilt_series(s1, spec.Znum, spec.x, spec.y, spec.z, spec.occ, aZ, aY,
+                                  defoci, nconfig=3)
+        assert np.array_equal(k, k1)
+        assert np.array_equal(im, ref)
+
+
 def test_batch_errors(ctx, msk):
     cases = batch_case()[:2]
     s = series(msk)

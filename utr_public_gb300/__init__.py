@@ -90,7 +90,7 @@ class SpecimenDesc(C.Structure):
                 ("z", C.c_void_p), ("occ", C.c_void_p), ("nx", C.c_int), ("ny", C.c_int),
                 ("ctblength", C.c_float), ("ctblengthz", C.c_float), ("nangles", C.c_int),
                 ("angleZ", C.c_void_p), ("angleY", C.c_void_p), ("images", C.c_void_p),
-                ("kept", C.c_void_p), ("wobble", C.c_void_p)]
+                ("kept", C.c_void_p), ("wobble", C.c_void_p), ("nconfig", C.c_int)]
 
 
 class Plane(C.Structure):
@@ -397,11 +397,13 @@ class Context:
             return a
         return np.ascontiguousarray(a, np.float32)
 
-    def tilt_series_batch(self, series, specimens, defocus, graph=True, images=None):
+    def tilt_series_batch(self, series, specimens, defocus, graph=True, images=None, nconfig=1):
         """Many specimens in one call (msk_tilt_series_batch).  specimens: list
         of (Specimen-like with Znum/x/y/z/occ/fov and, for series.lwobble = 1, a
         float32 `wobble` per atom, n, angleZ, angleY[, ctblengthz]);
         returns (images list [nangles, ndef, n, n] per specimen, kept list).
+        nconfig > 1 (with series.lwobble = 1): thermal configurations per
+        orientation, images averaged; kept then [nangles * nconfig].
         images may be a list of preallocated arrays or torch CUDA tensors."""
         defocus = np.ascontiguousarray(defocus, np.float64)
         nd = len(defocus)
@@ -416,7 +418,7 @@ class Context:
             aZ = np.ascontiguousarray(aZ, np.float64)
             aY = np.ascontiguousarray(aY, np.float64)
             img = images[i] if images is not None else np.zeros((len(aZ), nd, n, n), np.float32)
-            kp = np.zeros(len(aZ), np.int32)
+            kp = np.zeros(len(aZ) * max(1, nconfig), np.int32)
             keep += arrs + [aZ, aY]
             outs.append(img)
             kepts.append(kp)
@@ -428,6 +430,7 @@ class Context:
             d.nangles = len(aZ)
             d.angleZ, d.angleY = _ptr(aZ), _ptr(aY)
             d.images, d.kept = _ptr(img), _ptr(kp)
+            d.nconfig = nconfig
             wob = getattr(sp_, "wobble", None)
             if wob is not None:
                 wob = np.ascontiguousarray(wob, np.float32)

@@ -2591,6 +2591,7 @@ constexpr int kLanes = 8;
 struct SpecPlan {
     GridPre gp;
     int nslices = 0, nangles = 0;
+    int nconf = 1, nunits = 0;  // thermal configurations per orientation; units = both
     std::vector<UnitAtoms> ua;
     Batch b;
     std::vector<SplatAtom> atoms;
@@ -2632,7 +2633,8 @@ int enqueue_specimen(msk_context *ctx, SpecPlan &P, unsigned char *arena, const 
 {
     const GridPre &gp = P.gp;
     const Geom &g = gp.g;
-    const int nx = gp.nx, ny = gp.ny, na = P.nangles;
+    // units u = a * nconf + c (orientation a, configuration c); images per orientation
+    const int nx = gp.nx, ny = gp.ny, na = P.nunits, nimg = P.nangles, nconf = P.nconf;
     const size_t plane = (size_t)nx * ny;
     const SizeOps *rop = size_ops(ny), *cop = size_ops(nx);
     float2 *psi = reinterpret_cast<float2 *>(arena + P.o_psi);
@@ -2711,7 +2713,8 @@ int enqueue_specimen(msk_context *ctx, SpecPlan &P, unsigned char *arena, const 
     const double pi = 4.0 * atan(1.0), l = gp.wavlen;
     float k2maxo = s->aobj / gp.wavlen;
     k2maxo = k2maxo * k2maxo;
-    const size_t nmeta = 4 * (size_t)na + 1;
+    // per plane: img_off[nimg + 1] | img_units[na] | img_dst[nimg] | img_flags[nimg]
+    const size_t nmeta = (size_t)3 * nimg + 1 + na;
     for (int d = 0; d < ndef; d++) {
         Fresnel fr{};
         const double rprime = defocus[d] - 0.5 * P.ctblengthz;  // autosliccmd.cpp:1060
@@ -2734,6 +2737,8 @@ int enqueue_specimen(msk_context *ctx, SpecPlan &P, unsigned char *arena, const 
             cop->col_fresnel(g, pmapf, tmapf, nullptr, na, fr, 1.0f, st);
         }
         const int *dm = reinterpret_cast<const int *>(arena + P.o_meta) + (size_t)d * nmeta;
+        const int *d_off = dm, *d_units = dm + nimg + 1, *d_dst = dm + nimg + 1 + na,
+                  *d_flags = dm + 2 * nimg + 1 + na;
         const double rot = s->rotation ? s->rotation[d] : 0.0;
         if (rot != 0.0 || sxp != 0 || syp != 0) {
             // the amplitude in real space, rotated and shifted, then |.|^2
@@ -2750,14 +2755,14 @@ int enqueue_specimen(msk_context *ctx, SpecPlan &P, unsigned char *arena, const 
                                                         ycen, cos(rot), sin(rot), rot != 0.0, sxp,
                                                         syp, fill);
             }
-            Prof p(ctx, kIntensity, 12.0 * pl * na, st);
-            k_intensity_direct<<<8 * 152, 256, 0, st>>>(na, dm, dm + na + 1, dm + 2 * na + 1,
-                                                        dm + 3 * na + 1, tb, d_images, plane, 1.0f);
+            Prof p(ctx, kIntensity, 8.0 * pl * na + 4.0 * pl * nimg, st);
+            k_intensity_direct<<<8 * 152, 256, 0, st>>>(nimg, d_off, d_units, d_dst, d_flags, tb,
+                                                        d_images, plane, (float)nconf);
             continue;
         }
-        Prof p(ctx, kIntensity, 12.0 * pl * na, st);
-        rop->row_intensity(g, na, dm, dm + na + 1, dm + 2 * na + 1, dm + 3 * na + 1, tb, d_images,
-                           1.0f, st);
+        Prof p(ctx, kIntensity, 8.0 * pl * na + 4.0 * pl * nimg, st);
+        rop->row_intensity(g, nimg, d_off, d_units, d_dst, d_flags, tb, d_images, (float)nconf,
+                           st);
     }
     MSK_CUDA(ctx, cudaGetLastError());
     return MSK_OK;
@@ -2777,6 +2782,9 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
         const msk_specimen &q = spec[i];
         if (s->lwobble && q.natom > 0 && !q.wobble)
             return fail(ctx, MSK_EINVAL, "lwobble needs each specimen's wobble array");
+        if (q.nconfig < 0 || (q.nconfig > 1 && !s->lwobble))
+            return fail(ctx, MSK_EINVAL, "several configurations need lwobble = 1 (bad specimen " +
+                                             std::to_string(i) + ")");
         if (q.natom < 0 || q.nangles < 1 || !q.angleZ || !q.angleY ||
             (ndefocus > 0 && !q.images) ||
             (q.natom > 0 && (!q.Znum || !q.x || !q.y || !q.z || !q.occ)))
@@ -2806,42 +2814,50 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
             return fail(ctx, MSK_EUNSUPPORTED, "band limit is not two index ranges per column");
         P[i].nslices = slice_count(s->deltaz, q.ctblengthz);
         P[i].nangles = q.nangles;
+        P[i].nconf = std::max(1, q.nconfig);
+        P[i].nunits = q.nangles * P[i].nconf;
         P[i].ctblength = q.ctblength;
         P[i].ctblengthz = q.ctblengthz;
-        P[i].ua.resize(q.nangles);
+        P[i].ua.resize(P[i].nunits);
         for (int a = 0; a < q.nangles; a++) units.push_back({i, a});
     }
     parallel_for((int)units.size(), host_threads(), [&](int k) {
         const int i = units[k].first, a = units[k].second;
         const msk_specimen &q = spec[i];
-        PrepSpec ps{q.natom, q.Znum, q.x, q.y, q.z, q.occ, q.ctblength, q.ctblengthz, s->deltaz,
-                    P[i].nslices, true, q.angleZ[a], q.angleY[a], s->dxc, s->dyc, s->dzc,
-                    nullptr, true, ctx->zmap.data()};
-        if (s->lwobble) {  // one configuration: the Debye-Waller branch
-            ps.thermal = kThermDW;
-            ps.wobble = q.wobble;
-            ps.temperature = s->temperature;
+        // one configuration with lwobble: the Debye-Waller branch; several: random
+        // displacements, orientation a's configurations in order from seed - a
+        long seed = s->seed - a;
+        for (int c = 0; c < P[i].nconf; c++) {
+            PrepSpec ps{q.natom, q.Znum, q.x, q.y, q.z, q.occ, q.ctblength, q.ctblengthz,
+                        s->deltaz, P[i].nslices, true, q.angleZ[a], q.angleY[a], s->dxc, s->dyc,
+                        s->dzc, nullptr, true, ctx->zmap.data()};
+            if (s->lwobble) {
+                ps.thermal = P[i].nconf == 1 ? kThermDW : kThermRandom;
+                ps.wobble = q.wobble;
+                ps.temperature = s->temperature;
+                ps.iseed = P[i].nconf == 1 ? nullptr : &seed;
+            }
+            prep_unit(P[i].gp, ps, P[i].ua[(size_t)a * P[i].nconf + c]);
         }
-        prep_unit(P[i].gp, ps, P[i].ua[a]);
     });
     for (int i = 0; i < nspec; i++)
-        for (int a = 0; a < spec[i].nangles; a++)
-            if (P[i].ua[a].status)
-                return fail(ctx, P[i].ua[a].status, "specimen " + std::to_string(i) + ": " +
-                                                         msk_status_string(P[i].ua[a].status));
+        for (int u = 0; u < P[i].nunits; u++)
+            if (P[i].ua[u].status)
+                return fail(ctx, P[i].ua[u].status, "specimen " + std::to_string(i) + ": " +
+                                                         msk_status_string(P[i].ua[u].status));
     parallel_for(nspec, host_threads(), [&](int i) {
         SpecPlan &q = P[i];
         build_tables(q.gp, zlist, q.tables, q.tl);
-        pack_batch(q.ua, 0, q.nangles, q.nslices, q.b, q.atoms);
-        const int na = q.nangles;
+        pack_batch(q.ua, 0, q.nunits, q.nslices, q.b, q.atoms);
+        const int na = q.nangles, nc = q.nconf;
         q.meta.clear();
         for (int d = 0; d < ndefocus; d++) {
-            for (int a = 0; a <= na; a++) q.meta.push_back(a);         // img_off
-            for (int a = 0; a < na; a++) q.meta.push_back(a);          // img_units
+            for (int a = 0; a <= na; a++) q.meta.push_back(a * nc);    // img_off
+            for (int u = 0; u < q.nunits; u++) q.meta.push_back(u);    // img_units
             for (int a = 0; a < na; a++) q.meta.push_back(a * ndefocus + d);  // img_dst
-            for (int a = 0; a < na; a++) q.meta.push_back(0);          // img_flags
+            for (int a = 0; a < na; a++) q.meta.push_back(nc > 1 ? 2 : 0);    // img_flags: mean
         }
-        q.work = (double)na * q.nslices * q.gp.nx * q.gp.ny;
+        q.work = (double)q.nunits * q.nslices * q.gp.nx * q.gp.ny;
         q.img_dev = ndefocus > 0 && is_device_ptr(spec[i].images);
         q.img_pinned = ndefocus > 0 && !q.img_dev && is_pinned_host(spec[i].images);
         if (s->R1 != 0.0) spherical_wave(q.gp.nx, q.gp.ny, q.ctblength, s->v0, s->R1, q.wave0);
@@ -2874,17 +2890,17 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
         q.o_fres = work;
         work += align256((size_t)std::max(ndefocus, 1) * plane * sizeof(float2));
         q.o_psi = work;
-        work += align256((size_t)q.nangles * plane * sizeof(float2));
+        work += align256((size_t)q.nunits * plane * sizeof(float2));
         q.o_tbuf = work;
-        work += align256((size_t)q.nangles * plane * sizeof(float2));
+        work += align256((size_t)q.nunits * plane * sizeof(float2));
         q.o_img = work;
         if (!q.img_dev) work += align256((size_t)q.nangles * ndefocus * plane * sizeof(float));
         q.o_phi = work;
-        if (image_plane) work += align256((size_t)q.nangles * plane * sizeof(float2));
+        if (image_plane) work += align256((size_t)q.nunits * plane * sizeof(float2));
         q.o_fill = work;
-        if (image_plane) work += align256((size_t)q.nangles * sizeof(float2));
+        if (image_plane) work += align256((size_t)q.nunits * sizeof(float2));
         q.o_spec = work;
-        if (!q.b.dw.empty()) work += align256((size_t)q.nangles * plane * sizeof(float2));
+        if (!q.b.dw.empty()) work += align256((size_t)q.nunits * plane * sizeof(float2));
     };
     const bool graph = (flags & MSK_BATCH_GRAPH) && !ctx->prof_on;
     int first = 0;
@@ -2939,7 +2955,7 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
             P[i].gp.g.zeros = gflag.zeros;
             // the splat stores in-band row segments only: the rest reads as zeros
             MSK_CUDA(ctx, cudaMemsetAsync(arena + P[i].o_tbuf, 0,
-                                          (size_t)P[i].nangles * P[i].gp.nx * P[i].gp.ny *
+                                          (size_t)P[i].nunits * P[i].gp.nx * P[i].gp.ny *
                                               sizeof(float2),
                                           ctx->stream));
         }
@@ -3043,7 +3059,7 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
     }
     for (int i = 0; i < nspec; i++)
         if (spec[i].kept)
-            for (int a = 0; a < spec[i].nangles; a++) spec[i].kept[a] = P[i].ua[a].kept;
+            for (int u = 0; u < P[i].nunits; u++) spec[i].kept[u] = P[i].ua[u].kept;
     return MSK_OK;
 }
 
