@@ -176,10 +176,12 @@ typedef struct {
     float *images;   /* out: float[nangles][ndefocus][nx][ny], host or device */
     int *kept;       /* out (may be NULL): int[nangles] (see nconfig) */
     const float *wobble;  /* rms displacement at 300 K per atom (host; s->lwobble = 1) */
-    int nconfig;          /* thermal configurations per orientation (0, 1: one); > 1 needs
-                           * s->lwobble = 1: random displacements drawn in the engine as
-                           * msk_tilt_series does, images averaged; kept then holds
-                           * int[nangles * nconfig] */
+    int nconfig;          /* thermal configurations per orientation (0, 1: one), images
+                           * averaged; kept then holds int[nangles * nconfig] */
+    const float *displacements;  /* float[nconfig][3][natom] added to x, y, z after the
+                                  * rotation (host, may be NULL), as msk_tilt_series; NULL
+                                  * with nconfig > 1 needs s->lwobble = 1 (drawn in the
+                                  * engine) */
 } msk_specimen;
 
 enum { MSK_BATCH_GRAPH = 1 };

@@ -149,6 +149,25 @@ def test_batch_thermal_configurations(ctx, msk):
         assert np.array_equal(im, ref)
 
 
+def test_batch_given_displacements(ctx, msk):
+    """Two configurations per orientation from caller-given displacements:
+    each specimen equals msk_tilt_series with the same displacements."""
+    cases = batch_case()
+    rng = np.random.default_rng(77)
+    disp = [(0.05 * rng.standard_normal((2, 3, spec.natom))).astype(np.float32)
+            for spec, _, _, _ in cases]
+    defoci = [0.0, 150.0]
+    s = series(msk, aobj=0.02)
+    imgs, _ = ctx.tilt_series_batch(s, cases, defoci, nconfig=2, displacements=disp)
+    for (spec, n, aZ, aY), im, dd in zip(cases, imgs, disp):
+        s1 = series(msk, aobj=0.02)
+        s1.nx = s1.ny = n
+        s1.ctblength = s1.ctblengthz = spec.fov
+        ref, _ = ctx.tilt_series(s1, spec.Znum, spec.x, spec.y, spec.z, spec.occ, aZ, aY,
+                                 defoci, nconfig=2, displacements=dd)
+        assert np.array_equal(im, ref)
+
+
 def test_batch_errors(ctx, msk):
     cases = batch_case()[:2]
     s = series(msk)

@@ -90,7 +90,8 @@ class SpecimenDesc(C.Structure):
                 ("z", C.c_void_p), ("occ", C.c_void_p), ("nx", C.c_int), ("ny", C.c_int),
                 ("ctblength", C.c_float), ("ctblengthz", C.c_float), ("nangles", C.c_int),
                 ("angleZ", C.c_void_p), ("angleY", C.c_void_p), ("images", C.c_void_p),
-                ("kept", C.c_void_p), ("wobble", C.c_void_p), ("nconfig", C.c_int)]
+                ("kept", C.c_void_p), ("wobble", C.c_void_p), ("nconfig", C.c_int),
+                ("displacements", C.c_void_p)]
 
 
 class Plane(C.Structure):
@@ -397,13 +398,15 @@ class Context:
             return a
         return np.ascontiguousarray(a, np.float32)
 
-    def tilt_series_batch(self, series, specimens, defocus, graph=True, images=None, nconfig=1):
+    def tilt_series_batch(self, series, specimens, defocus, graph=True, images=None, nconfig=1,
+                          displacements=None):
         """Many specimens in one call (msk_tilt_series_batch).  specimens: list
         of (Specimen-like with Znum/x/y/z/occ/fov and, for series.lwobble = 1, a
         float32 `wobble` per atom, n, angleZ, angleY[, ctblengthz]);
         returns (images list [nangles, ndef, n, n] per specimen, kept list).
-        nconfig > 1 (with series.lwobble = 1): thermal configurations per
-        orientation, images averaged; kept then [nangles * nconfig].
+        nconfig > 1: thermal configurations per orientation, images averaged
+        (kept then [nangles * nconfig]), drawn in the engine (series.lwobble =
+        1) or given: displacements, per specimen float32 [nconfig, 3, natom].
         images may be a list of preallocated arrays or torch CUDA tensors."""
         defocus = np.ascontiguousarray(defocus, np.float64)
         nd = len(defocus)
@@ -431,6 +434,10 @@ class Context:
             d.angleZ, d.angleY = _ptr(aZ), _ptr(aY)
             d.images, d.kept = _ptr(img), _ptr(kp)
             d.nconfig = nconfig
+            if displacements is not None and displacements[i] is not None:
+                disp = np.ascontiguousarray(displacements[i], np.float32)
+                keep.append(disp)
+                d.displacements = _ptr(disp)
             wob = getattr(sp_, "wobble", None)
             if wob is not None:
                 wob = np.ascontiguousarray(wob, np.float32)

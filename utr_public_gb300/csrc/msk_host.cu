@@ -2780,9 +2780,9 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
         return fail(ctx, MSK_EINVAL, "bad batch arguments");
     for (int i = 0; i < nspec; i++) {
         const msk_specimen &q = spec[i];
-        if (s->lwobble && q.natom > 0 && !q.wobble)
+        if (s->lwobble && !(q.nconfig > 1 && q.displacements) && q.natom > 0 && !q.wobble)
             return fail(ctx, MSK_EINVAL, "lwobble needs each specimen's wobble array");
-        if (q.nconfig < 0 || (q.nconfig > 1 && !s->lwobble))
+        if (q.nconfig < 0 || (q.nconfig > 1 && !s->lwobble && !q.displacements))
             return fail(ctx, MSK_EINVAL, "several configurations need lwobble = 1 (bad specimen " +
                                              std::to_string(i) + ")");
         if (q.natom < 0 || q.nangles < 1 || !q.angleZ || !q.angleY ||
@@ -2824,18 +2824,25 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
     parallel_for((int)units.size(), host_threads(), [&](int k) {
         const int i = units[k].first, a = units[k].second;
         const msk_specimen &q = spec[i];
-        // one configuration with lwobble: the Debye-Waller branch; several: random
-        // displacements, orientation a's configurations in order from seed - a
+        // the thermal branch as msk_tilt_series chooses it: none without lwobble,
+        // Debye-Waller with one configuration, none with given displacements, else
+        // random displacements, orientation a's configurations in order from seed - a
         long seed = s->seed - a;
-        for (int c = 0; c < P[i].nconf; c++) {
+        const int nc = P[i].nconf;
+        const int thermal = !s->lwobble ? kThermNone
+                            : nc == 1 ? kThermDW
+                            : q.displacements ? kThermNone : kThermRandom;
+        for (int c = 0; c < nc; c++) {
+            const float *disp =
+                q.displacements ? q.displacements + (size_t)c * 3 * q.natom : nullptr;
             PrepSpec ps{q.natom, q.Znum, q.x, q.y, q.z, q.occ, q.ctblength, q.ctblengthz,
                         s->deltaz, P[i].nslices, true, q.angleZ[a], q.angleY[a], s->dxc, s->dyc,
-                        s->dzc, nullptr, true, ctx->zmap.data()};
-            if (s->lwobble) {
-                ps.thermal = P[i].nconf == 1 ? kThermDW : kThermRandom;
+                        s->dzc, disp, true, ctx->zmap.data()};
+            if (thermal != kThermNone) {
+                ps.thermal = thermal;
                 ps.wobble = q.wobble;
                 ps.temperature = s->temperature;
-                ps.iseed = P[i].nconf == 1 ? nullptr : &seed;
+                ps.iseed = thermal == kThermRandom ? &seed : nullptr;
             }
             prep_unit(P[i].gp, ps, P[i].ua[(size_t)a * P[i].nconf + c]);
         }
