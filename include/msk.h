@@ -182,6 +182,8 @@ typedef struct {
                                   * rotation (host, may be NULL), as msk_tilt_series; NULL
                                   * with nconfig > 1 needs s->lwobble = 1 (drawn in the
                                   * engine) */
+    float *exitwaves;  /* out (may be NULL): complex [nangles][nconfig][nx][ny], host or
+                        * device, as msk_tilt_series */
 } msk_specimen;
 
 enum { MSK_BATCH_GRAPH = 1 };

@@ -168,6 +168,29 @@ def test_batch_given_displacements(ctx, msk):
         assert np.array_equal(im, ref)
 
 
+@pytest.mark.parametrize("pinned", [False, True])
+def test_batch_exit_waves(ctx, msk, pinned):
+    """Exit waves out of the batch (pageable or page-locked host memory,
+    graph capture): equal to msk_tilt_series's, bit for bit."""
+    torch = pytest.importorskip("torch")
+    cases = batch_case()
+    defoci = [0.0]
+    s = series(msk, aobj=0.02)
+    ews = None
+    if pinned:
+        ews = [torch.zeros((len(aZ), 1, n, n, 2), dtype=torch.float32).pin_memory()
+               for _, n, aZ, _ in cases]
+    imgs, _, ew = ctx.tilt_series_batch(s, cases, defoci, exitwaves=ews, want_exit=True)
+    for (spec, n, aZ, aY), e in zip(cases, ew):
+        s1 = series(msk, aobj=0.02)
+        s1.nx = s1.ny = n
+        s1.ctblength = s1.ctblengthz = spec.fov
+        _, ref, _ = ctx.tilt_series(s1, spec.Znum, spec.x, spec.y, spec.z, spec.occ, aZ, aY,
+                                    defoci, want_exit=True)
+        e = e.numpy() if pinned else e
+        assert np.array_equal(e.reshape(ref.shape), ref)
+
+
 def test_batch_errors(ctx, msk):
     cases = batch_case()[:2]
     s = series(msk)

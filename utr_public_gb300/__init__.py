@@ -91,7 +91,7 @@ class SpecimenDesc(C.Structure):
                 ("ctblength", C.c_float), ("ctblengthz", C.c_float), ("nangles", C.c_int),
                 ("angleZ", C.c_void_p), ("angleY", C.c_void_p), ("images", C.c_void_p),
                 ("kept", C.c_void_p), ("wobble", C.c_void_p), ("nconfig", C.c_int),
-                ("displacements", C.c_void_p)]
+                ("displacements", C.c_void_p), ("exitwaves", C.c_void_p)]
 
 
 class Plane(C.Structure):
@@ -399,7 +399,7 @@ class Context:
         return np.ascontiguousarray(a, np.float32)
 
     def tilt_series_batch(self, series, specimens, defocus, graph=True, images=None, nconfig=1,
-                          displacements=None):
+                          displacements=None, exitwaves=None, want_exit=False):
         """Many specimens in one call (msk_tilt_series_batch).  specimens: list
         of (Specimen-like with Znum/x/y/z/occ/fov and, for series.lwobble = 1, a
         float32 `wobble` per atom, n, angleZ, angleY[, ctblengthz]);
@@ -407,11 +407,13 @@ class Context:
         nconfig > 1: thermal configurations per orientation, images averaged
         (kept then [nangles * nconfig]), drawn in the engine (series.lwobble =
         1) or given: displacements, per specimen float32 [nconfig, 3, natom].
+        want_exit (or preallocated exitwaves, per specimen [nangles, nconfig, n,
+        n, 2] float32 arrays or torch tensors): also returns the exit waves.
         images may be a list of preallocated arrays or torch CUDA tensors."""
         defocus = np.ascontiguousarray(defocus, np.float64)
         nd = len(defocus)
         descs = (SpecimenDesc * len(specimens))()
-        keep, outs, kepts = [], [], []
+        keep, outs, kepts, ews = [], [], [], []
         for i, item in enumerate(specimens):
             sp_, n, aZ, aY = item[:4]
             zc = item[4] if len(item) > 4 else sp_.fov
@@ -434,6 +436,11 @@ class Context:
             d.angleZ, d.angleY = _ptr(aZ), _ptr(aY)
             d.images, d.kept = _ptr(img), _ptr(kp)
             d.nconfig = nconfig
+            if exitwaves is not None or want_exit:
+                ew = (exitwaves[i] if exitwaves is not None else
+                      np.zeros((len(aZ), max(1, nconfig), n, n, 2), np.float32))
+                ews.append(ew)
+                d.exitwaves = _ptr(ew)
             if displacements is not None and displacements[i] is not None:
                 disp = np.ascontiguousarray(displacements[i], np.float32)
                 keep.append(disp)
@@ -446,7 +453,7 @@ class Context:
         st = self.L.msk_tilt_series_batch(self.h, C.byref(series), len(specimens), descs, nd,
                                           _ptr(defocus), MSK_BATCH_GRAPH if graph else 0)
         self._check(st)
-        return outs, kepts
+        return (outs, kepts, ews) if ews else (outs, kepts)
 
     def potential_stack(self, series, Znum, x, y, z, occ, angleZ, angleY, v=None):
         """Per-slice projected potentials v [nangles, nslices, nx, ny] of a tilt

@@ -2605,6 +2605,9 @@ struct SpecPlan {
     size_t o_dw = 0, o_spec = 0;  // Debye-Waller branch: -B/4 per (unit, slice); S(v) grids
     bool img_dev = false;
     bool img_pinned = false;  // host images in page-locked memory: copied on the lane
+    float *ew = nullptr;      // exit waves out (may be null)
+    bool ew_dev = false, ew_pinned = false;
+    size_t o_ew = 0;          // work region: pageable-host exit waves, staged
     double work = 0.0;
     int lane = 0;
 };
@@ -2704,6 +2707,23 @@ int enqueue_specimen(msk_context *ctx, SpecPlan &P, unsigned char *arena, const 
             Prof p(ctx, kKColProp, 16.0 * pl * na, st);
             cop->col_prop(g, pmap, pmap, nullptr, na, w_in_band ? 1 : 0, st);
             w_in_band = true;
+        }
+    }
+    // exit waves (psi = iS(W)/ny): into a device destination directly, else
+    // through the transmission buffer (free until the free-space step) to
+    // page-locked host memory on this stream or to the arena for a later copy
+    if (P.ew) {
+        const size_t ewb = (size_t)na * plane * sizeof(float2);
+        float2 *dst = P.ew_dev ? reinterpret_cast<float2 *>(P.ew) : tb;
+        {
+            Prof p(ctx, kExit, 16.0 * pl * na, st);
+            rop->row_exit(g, nullptr, na, psi, dst, st);
+        }
+        if (P.ew_pinned) {
+            MSK_CUDA(ctx, cudaMemcpyAsync(P.ew, tb, ewb, cudaMemcpyDeviceToHost, st));
+            count_copy(ctx, 1, (double)ewb);
+        } else if (!P.ew_dev) {
+            MSK_CUDA(ctx, cudaMemcpyAsync(arena + P.o_ew, tb, ewb, cudaMemcpyDeviceToDevice, st));
         }
     }
     // image plane (autosliccmd.cpp:1119-1143): rotation centre and whole-pixel shift
@@ -2867,6 +2887,9 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
         q.work = (double)q.nunits * q.nslices * q.gp.nx * q.gp.ny;
         q.img_dev = ndefocus > 0 && is_device_ptr(spec[i].images);
         q.img_pinned = ndefocus > 0 && !q.img_dev && is_pinned_host(spec[i].images);
+        q.ew = spec[i].exitwaves;
+        q.ew_dev = q.ew && is_device_ptr(q.ew);
+        q.ew_pinned = q.ew && !q.ew_dev && is_pinned_host(q.ew);
         if (s->R1 != 0.0) spherical_wave(q.gp.nx, q.gp.ny, q.ctblength, s->v0, s->R1, q.wave0);
     });
     // image-plane rotation or shift of some detector plane: per specimen a real-space
@@ -2908,6 +2931,9 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
         if (image_plane) work += align256((size_t)q.nunits * sizeof(float2));
         q.o_spec = work;
         if (!q.b.dw.empty()) work += align256((size_t)q.nunits * plane * sizeof(float2));
+        q.o_ew = work;
+        if (q.ew && !q.ew_dev && !q.ew_pinned)
+            work += align256((size_t)q.nunits * plane * sizeof(float2));
     };
     const bool graph = (flags & MSK_BATCH_GRAPH) && !ctx->prof_on;
     int first = 0;
@@ -2931,6 +2957,7 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
             P[i].o_phi += align256(up);
             P[i].o_fill += align256(up);
             P[i].o_spec += align256(up);
+            P[i].o_ew += align256(up);
         }
         const size_t total = align256(up) + work;
         MSK_CUDA(ctx, ctx->arena.reserve(total));
@@ -3049,8 +3076,14 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
             cudaStreamSynchronize(ctx->stream);
             return rc;
         }
-        // images to pageable host buffers
+        // images and exit waves to pageable host buffers
         for (int i = first; i < last; i++) {
+            if (P[i].ew && !P[i].ew_dev && !P[i].ew_pinned) {
+                const size_t ewb = (size_t)P[i].nunits * P[i].gp.nx * P[i].gp.ny * sizeof(float2);
+                MSK_CUDA(ctx, cudaMemcpyAsync(P[i].ew, arena + P[i].o_ew, ewb,
+                                              cudaMemcpyDeviceToHost, ctx->stream));
+                count_copy(ctx, 1, (double)ewb);
+            }
             if (ndefocus == 0 || P[i].img_dev || P[i].img_pinned) continue;
             const size_t bytes = (size_t)P[i].nangles * ndefocus * P[i].gp.nx * P[i].gp.ny * sizeof(float);
             MSK_CUDA(ctx, cudaMemcpyAsync(spec[i].images, arena + P[i].o_img, bytes,
