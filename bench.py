@@ -181,7 +181,7 @@ def run_reference(args, rank, world):
 
 def fp64_error_job(result):
     """Relative L2 error of one orientation (45 degrees) of the workload vs the
-    FP64 oracle -- runs on a host thread while the GPU is timed."""
+    FP64 oracle (run after the timed regions)."""
     try:
         from oracle import oracle as orc
         import utr_public_gb300 as msk
