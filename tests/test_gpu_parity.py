@@ -2,7 +2,7 @@
 oracle.  Tolerances (relative L2 over the whole grid):
   * exit wave vs the reference's FP32 CPU result (golden):  2e-5
   * exit wave and images vs the FP64 oracle:                1e-5 at these sizes
-    (the benchmark spec's bound is 1e-4)
+    (the path's accuracy target is 1e-4)
 Bit-exact where the arithmetic is exact (plane wave through an empty box).
 """
 import numpy as np

@@ -57,7 +57,7 @@ constexpr int kMetaBits = 13;
 constexpr uint32_t kMetaMask = (1u << kMetaBits) - 1u;
 constexpr int kMaxZidx = 64;
 
-// Free-space step to one detector plane (this build's FresnelA definition):
+// Free-space step to one detector plane (this library's FresnelA definition):
 // chi = a1 k^2 + a3 k^4 + a5 k^6 + a2c (kx^2 - ky^2) + a2s 2 kx ky,
 // multiplier exp(-i chi) where k^2 < k2maxo (k2maxo == 0: everywhere).
 // k_fresnel_table evaluates it once per plane in double into `table`
