@@ -668,7 +668,8 @@ static int calc_setup_init(calc_setup *s, const float *param, int natom, const i
 
 /* The Gaussian deviate the thermal wobble draws (autoslic.cpp:707-709 calls
  * gasdev from the XArrayLibrary, which is not part of the reference): this
- * project's definition, shared with the driver of the reference build --
+ * project's definition, shared with oracle/ref_driver.cpp (the harness of
+ * the reference build) --
  * two steps of the 64-bit LCG (6364136223846793005, 1442695040888963407) on
  * the seed, Box-Muller from the top 53 bits. */
 double mo_gasdev(long *idum)

@@ -2,8 +2,9 @@
  * msk_oracle.h -- CPU restatement of the reference's multislice hot path.
  *
  * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
- * cpu_baseline leg of bench.py load this library, and only as the checker
- * (or as the timed CPU baseline); the shipped library never calls it.
+ * cpu_baseline leg of bench.py load this library, and only as the reference
+ * the GPU results are compared with (or as the timed CPU baseline); the
+ * shipped library never calls it.
  *
  * Two arithmetic variants of the same method:
  *   *_f32  mirrors the reference's own float/double mix operation by

@@ -1,7 +1,8 @@
 """ctypes access to the test oracle.  TEST INFRASTRUCTURE ONLY.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
-this module, and only as the checker (or the timed CPU baseline).  The
+this module, and only as the reference the GPU results are compared with (or
+the timed CPU baseline).  The
 shipped package never imports it.
 
 * ``Oracle`` wraps ``oracle/liboracle.so``, the C restatement of the

@@ -2,8 +2,8 @@
  * utr_oracle.h -- CPU restatement of UTR.exe's reconstruction core
  * (MultisliceCppTest/PhaseRetrieval/UTR.cpp, UTR.h).
  *
- * TEST INFRASTRUCTURE ONLY: the checker of the GPU reconstruction in
- * libmsk.so; nothing in the shipped library links this file.
+ * TEST INFRASTRUCTURE ONLY: what the GPU reconstruction in libmsk.so is
+ * compared with; nothing in the shipped library links this file.
  *
  * Layouts as in msk_utr.h: images [ny][nx], volumes [nz][ny][nx] (x
  * fastest), complex data interleaved, Fourier volumes centred.
