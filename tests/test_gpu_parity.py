@@ -213,3 +213,30 @@ def test_per_angle_form_matches_batched(ctx, msk, oracle):
         for d in range(2):
             assert rel_l2(pa[a, d], ref[d]) < 1e-5
             assert rel_l2(imgs[a, d], pa[a, d]) < 1e-5
+
+
+def test_full_size_tilt_series(ctx, msk, oracle):
+    """The tilt-series workload at its full size (20000 atoms, 1024^2, 160 slices of
+    1 A, 300 keV, defoci 0 and 500 A): the 45-degree orientation of a four-orientation
+    call against the FP64 oracle (exit wave and images within 1e-5), and that
+    orientation computed alone equal to it bit for bit (units are independent)."""
+    from oracle.oracle import SeriesParams
+    spec = sp.tilt_specimen(1002)
+    atoms = (spec.Znum, spec.x, spec.y, spec.z, spec.occ)
+    s = msk.Series()
+    s.nx = s.ny = 1024
+    s.ctblength = s.ctblengthz = 160.0
+    s.v0, s.deltaz = 300.0, 1.0
+    angY = np.deg2rad([0.0, 45.0, 90.0, 135.0])
+    defoci = [0.0, 500.0]
+    imgs, ew, _ = ctx.tilt_series(s, *atoms, np.zeros(4), angY, defoci, want_exit=True)
+    one, ew1, _ = ctx.tilt_series(s, *atoms, [0.0], angY[1:2], defoci, want_exit=True)
+    assert np.array_equal(one[0], imgs[1]) and np.array_equal(ew1[0], ew[1])
+    sr = SeriesParams()
+    sr.ax, sr.ctblengthz, sr.nx, sr.ny, sr.v0, sr.deltaz = 160.0, 160.0, 1024, 1024, 300.0, 1.0
+    sr.max_slices, sr.min_slice = -1, 0
+    ref_img, ref_ew, _ = oracle.orientation(sr, *atoms, 0.0, angY[1], np.array(defoci),
+                                            fp64=True, want_exit=True)
+    assert rel_l2(ew[1, 0], ref_ew) < 1e-5
+    for d in range(2):
+        assert rel_l2(imgs[1, d], ref_img[d]) < 1e-5
