@@ -61,8 +61,11 @@ def test_calculate_with_tilt_and_incident_wave(ctx, msk, oracle):
     assert rel_l2(pix, ref64) < 1e-5
 
 
-def test_empty_box_keeps_plane_wave_exactly(ctx, msk):
-    param = msk.make_param(32.0, 32.0, 64, 64, 200.0, 2.0)
+@pytest.mark.parametrize("n", [64, 4096])
+def test_empty_box_keeps_plane_wave_exactly(ctx, msk, n):
+    """An empty box at the smallest test grid and at the largest grid in both
+    dimensions: every transform of the plane wave is exact, so it stays 1."""
+    param = msk.make_param(32.0, 32.0, n, n, 200.0, 8.0 if n > 1024 else 2.0)
     e = np.zeros(0, np.float32)
     pix = ctx.calculate(param, e.astype(np.int32), e, e, e, e, 32.0, 32.0)
     assert np.all(pix[..., 0] == 1.0) and np.all(pix[..., 1] == 0.0)
