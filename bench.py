@@ -1126,6 +1126,22 @@ def main():
             per_angle = {"value": pa_val, "unit": UNIT, "orientations_timed": int(len(sub)),
                          "ms": pa_ms, "batched_over_per_angle": value / pa_val,
                          "images_rel_l2_vs_batched": same}
+            # this library's own fused passes, one orientation at a time (max_batch 1):
+            # the batching's share of the gain, apart from the fusion's
+            s1 = msk.Series()
+            for f, _ in msk.Series._fields_:
+                setattr(s1, f, getattr(s, f))
+            s1.max_batch = 1
+            ctx.tilt_series(s1, *atoms, angZ[sub[:1]], angY[sub[:1]], defoci, images=pa_imgs[:1])
+            torch.cuda.synchronize()
+            e0.record(stream)
+            ctx.tilt_series(s1, *atoms, angZ[sub], angY[sub], defoci, images=pa_imgs)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            f_ms = e0.elapsed_time(e1)
+            f_val = len(sub) * nslices / (f_ms / 1000.0)
+            per_angle["fused_one_at_a_time"] = {"value": f_val, "ms": f_ms,
+                                                "batched_over_it": value / f_val}
         except Exception as ex:  # reported, not fatal
             per_angle = {"error": repr(ex)}
 
