@@ -191,6 +191,39 @@ def test_batch_exit_waves(ctx, msk, pinned):
         assert np.array_equal(e.reshape(ref.shape), ref)
 
 
+@pytest.mark.parametrize("graph", [True, False])
+def test_batch_features_together(ctx, msk, graph):
+    """Spherical incident wave, three thermal configurations drawn in the engine,
+    a rotated and shifted image plane and exit waves in one batch: each specimen
+    equals msk_tilt_series on it, bit for bit."""
+    cases = batch_case()
+    for i, (spec, _, _, _) in enumerate(cases):
+        spec.wobble = (0.03 + 0.01 * ((np.arange(spec.natom) + i) % 4)).astype(np.float32)
+    defoci = [0.0, 220.0]
+    rot = np.array([0.25, 0.0])
+
+    def setup(s):
+        s.R1 = 3500.0
+        s.rotation = rot.ctypes.data
+        s.xshift, s.yshift = -0.8, 0.5
+        s.lwobble, s.temperature, s.seed = 1, 300.0, 99
+        return s
+
+    s = setup(series(msk, aobj=0.02, cs3=5e5))
+    imgs, kept, ews = ctx.tilt_series_batch(s, cases, defoci, graph=graph, nconfig=3,
+                                            want_exit=True)
+    for (spec, n, aZ, aY), im, k, ew in zip(cases, imgs, kept, ews):
+        s1 = setup(series(msk, aobj=0.02, cs3=5e5))
+        s1.wobble = spec.wobble.ctypes.data
+        s1.nx = s1.ny = n
+        s1.ctblength = s1.ctblengthz = spec.fov
+        ref, ref_ew, k1 = ctx.tilt_series(s1, spec.Znum, spec.x, spec.y, spec.z, spec.occ, aZ,
+                                          aY, defoci, nconfig=3, want_exit=True)
+        assert np.array_equal(k, k1)
+        assert np.array_equal(im, ref)
+        assert np.array_equal(ew.reshape(ref_ew.shape), ref_ew)
+
+
 def test_batch_errors(ctx, msk):
     cases = batch_case()[:2]
     s = series(msk)
