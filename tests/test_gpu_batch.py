@@ -238,6 +238,10 @@ def test_batch_errors(ctx, msk):
     with pytest.raises(msk.MskError) as e:
         ctx.tilt_series_batch(sw, cases, [0.0])
     assert e.value.status == msk.MSK_EINVAL
+    # several configurations need displacements: drawn (lwobble) or given
+    with pytest.raises(msk.MskError) as e:
+        ctx.tilt_series_batch(s, cases, [0.0], nconfig=2)
+    assert e.value.status == msk.MSK_EINVAL
     spec = sp.random_specimen(10, 32.0, 8.0, 24.0, 7)
     spec.Znum[3] = 104
     with pytest.raises(msk.MskError) as e:
