@@ -161,11 +161,11 @@ def run_reference(args, rank, world):
         cpu_sample(threads, (60, 62))
     vals, total = [], 0.0
     for _ in range(args.steps):
-        v, dt, _ = cpu_sample(threads, (60, 64))
+        v, dt, _ = cpu_sample(threads, (60, 80))
         vals.append(v)
         total += dt
     v = float(np.median(vals))
-    sample = ("%d orientations x slices 61-64 of the 180-orientation 1024^2 tilt series, one "
+    sample = ("%d orientations x slices 61-80 of the 180-orientation 1024^2 tilt series, one "
               "orientation per thread" % threads)
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
@@ -1166,9 +1166,9 @@ def main():
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        v, dt, n = cpu_sample(threads)
+        v, dt, n = cpu_sample(threads, (40, 160))  # ~10 s of CPU work on 16 cores
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": "%d orientations x slices 61-70 (%d slice-steps, %.1f s) of this "
+               "sample": "%d orientations x slices 41-160 (%d slice-steps, %.1f s) of this "
                          "workload, one orientation per thread" % (threads, n, dt)}
     err = None
     if not args.no_fp64_check:
