@@ -220,7 +220,9 @@ def adjoint_check(result, v, S, target, angles, nvox, rp):
         out = []
         t0 = time.perf_counter()
         for a in angles:
+            ta = time.perf_counter()
             g64, L64 = O.stack_adjoint(p, v[a], rp, target[a])
+            result.setdefault("adjoint_s", []).append(time.perf_counter() - ta)
             vox = np.stack([rng.integers(0, S, nvox), rng.integers(0, ADJ_NX, nvox),
                             rng.integers(0, ADJ_NX, nvox)], axis=1)
             fd = O.stack_fd(p, v[a], rp, target[a], vox, nthreads=threads)
@@ -355,6 +357,7 @@ def run_adjoint(args, rank, world, local_rank):
     if rank != 0:
         return
     err = None
+    cpu = None
     if not args.no_fp64_check:
         check = {}
         adjoint_check(check, {a: v[a].cpu().numpy() for a in pick}, S,
@@ -372,6 +375,11 @@ def run_adjoint(args, rank, world, local_rank):
                               "fd_voxels": int(len(ours))})
             err = {"cases": cases, "oracle_seconds": check["seconds"],
                    "oracle_threads": check["threads"]}
+            t1 = min(check["adjoint_s"])
+            cpu = {"value": S / t1, "unit": UNIT, "cores": 1, "kind": "port",
+                   "sample": "the FP64 oracle's forward + adjoint of one orientation (%d slices, "
+                             "512^2) on one host thread, %.1f s (the reference has no adjoint)"
+                             % (S, t1)}
         else:
             err = {"error": check.get("error", "not run")}
     out = {
@@ -389,6 +397,7 @@ def run_adjoint(args, rank, world, local_rank):
                    "slice_steps_per_step": steps_per * world,
                    "l2": "inputs larger than L2 (stacks 6.0 GB per GPU)"},
         "keep_all": keep_all,
+        "cpu_baseline": cpu,
         "forward_only": {"value": world * steps_per / (ms_fwd / 1000.0), "unit": UNIT,
                          "ms": ms_fwd, "adjoint_over_forward_time": ms / ms_fwd},
         "loss": loss_dev,
