@@ -153,6 +153,15 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
                     const double *defocus, int nconfig, const float *displacements,
                     float *images, float *exitwaves, int *kept);
 
+/* One detector plane of one orientation (msk_tilt_series_planes,
+ * msk_tilt_series_batch). */
+typedef struct {
+    double defocus;       /* Angstrom from the box centre */
+    double rotation;      /* about the optic axis, radians (the image-plane rotation) */
+    double astig;         /* two-fold astigmatism, Angstrom */
+    double astig_angle;   /* radians */
+} msk_plane;
+
 /* Many specimens in one call: MultisliceT.cpp:398-448 run for each specimen,
  * with its own atoms, box, grid and orientations; the common beam, slicing,
  * lens, incident wave (R1), image plane (rotation, xshift, yshift), thermal
@@ -164,7 +173,8 @@ int msk_tilt_series(msk_context *ctx, const msk_series *s, int natom, const int 
  * waves and images live in one device arena (in waves of specimens when they
  * do not fit); specimens run on concurrent streams, longest first.  With
  * flags & MSK_BATCH_GRAPH the launches are captured into one CUDA graph and
- * launched once.  Results equal msk_tilt_series per specimen. */
+ * launched once.  Results equal msk_tilt_series (msk_tilt_series_planes for
+ * a specimen with its own plane lists) per specimen. */
 typedef struct {
     int natom;
     const int *Znum;
@@ -184,6 +194,15 @@ typedef struct {
                                   * engine) */
     float *exitwaves;  /* out (may be NULL): complex [nangles][nconfig][nx][ny], host or
                         * device, as msk_tilt_series */
+    const int *plane_off;     /* (may be NULL) this specimen's own detector planes per
+                               * orientation, as msk_tilt_series_planes takes them:
+                               * orientation a images planes [plane_off[a], plane_off[a+1])
+                               * of `planes`, shifted by shifts[2a], shifts[2a+1] Angstrom
+                               * (NULL: none); images then float[plane_off[nangles]][nx][ny].
+                               * The call's ndefocus, defocus and s's rotation, astig,
+                               * astig_angle, xshift and yshift are not read for it. */
+    const msk_plane *planes;
+    const double *shifts;
 } msk_specimen;
 
 enum { MSK_BATCH_GRAPH = 1 };
@@ -201,13 +220,6 @@ int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int nspec,
  * (aobj, cs3, cs5) and everything else come from `s`; its astig, astig_angle,
  * rotation, xshift and yshift are not read.  Planes with equal parameters in
  * different orientations share one free-space table and pass. */
-typedef struct {
-    double defocus;       /* Angstrom from the box centre */
-    double rotation;      /* about the optic axis, radians (the image-plane rotation) */
-    double astig;         /* two-fold astigmatism, Angstrom */
-    double astig_angle;   /* radians */
-} msk_plane;
-
 int msk_tilt_series_planes(msk_context *ctx, const msk_series *s, int natom, const int *Znum,
                            const float *x, const float *y, const float *z, const float *occ,
                            int nangles, const double *angleZ, const double *angleY,

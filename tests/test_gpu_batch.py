@@ -224,6 +224,52 @@ def test_batch_features_together(ctx, msk, graph):
         assert np.array_equal(ew.reshape(ref_ew.shape), ref_ew)
 
 
+@pytest.mark.parametrize("graph", [True, False])
+def test_batch_per_orientation_planes(ctx, msk, graph):
+    """Specimens with their own detector planes per orientation (as orientation
+    files give them: defocus, rotation, astigmatism and an image shift per
+    orientation; a plane every orientation shares, planes only some have, an
+    orientation without planes) beside a specimen on the call's common defoci:
+    each equals msk_tilt_series_planes (msk_tilt_series) on it alone, bit for
+    bit."""
+    cases = batch_case()
+    defoci = [0.0, 150.0]
+    planes, shifts = [], []
+    for i, (spec, n, aZ, aY) in enumerate(cases):
+        if i == 1:
+            planes.append(None)
+            shifts.append(None)
+            continue
+        pa = []
+        for a in range(len(aZ)):
+            rows = [(0.0, 0.0, 0.0, 0.0)]
+            if (a + i) % 3 != 2:
+                rows.append((100.0 + 40.0 * (a % 2), 0.3 * (a % 2), 25.0 * (i % 2), 0.4))
+            if a == 0:
+                rows.append((-60.0, 0.0, 0.0, 0.0))
+            pa.append(rows)
+        if i == 2:
+            pa[1] = []
+        planes.append(pa)
+        shifts.append(np.array([[0.7 * (a % 2), -0.4 * a] for a in range(len(aZ))]))
+    s = series(msk, aobj=0.015, cs3=1e6)
+    imgs, kept = ctx.tilt_series_batch(s, cases, defoci, graph=graph, planes=planes,
+                                       shifts=shifts)
+    for (spec, n, aZ, aY), pa, sh, im, k in zip(cases, planes, shifts, imgs, kept):
+        s1 = series(msk, aobj=0.015, cs3=1e6)
+        s1.nx = s1.ny = n
+        s1.ctblength = s1.ctblengthz = spec.fov
+        if pa is None:
+            ref, k1 = ctx.tilt_series(s1, spec.Znum, spec.x, spec.y, spec.z, spec.occ, aZ, aY,
+                                      defoci)
+        else:
+            ref, k1 = ctx.tilt_series_planes(s1, spec.Znum, spec.x, spec.y, spec.z, spec.occ,
+                                             aZ, aY, pa, shifts=sh)
+        assert np.array_equal(k, k1)
+        assert im.shape == ref.shape
+        assert np.array_equal(im, ref)
+
+
 def test_batch_errors(ctx, msk):
     cases = batch_case()[:2]
     s = series(msk)

@@ -91,13 +91,30 @@ class SpecimenDesc(C.Structure):
                 ("ctblength", C.c_float), ("ctblengthz", C.c_float), ("nangles", C.c_int),
                 ("angleZ", C.c_void_p), ("angleY", C.c_void_p), ("images", C.c_void_p),
                 ("kept", C.c_void_p), ("wobble", C.c_void_p), ("nconfig", C.c_int),
-                ("displacements", C.c_void_p), ("exitwaves", C.c_void_p)]
+                ("displacements", C.c_void_p), ("exitwaves", C.c_void_p),
+                ("plane_off", C.c_void_p), ("planes", C.c_void_p), ("shifts", C.c_void_p)]
 
 
 class Plane(C.Structure):
     """msk_plane (include/msk.h): one detector plane of one orientation."""
     _fields_ = [("defocus", C.c_double), ("rotation", C.c_double), ("astig", C.c_double),
                 ("astig_angle", C.c_double)]
+
+
+def _plane_arrays(planes, na):
+    """Per-orientation plane rows (defocus, rotation, astig, astig_angle) as
+    the C arrays plane_off int32[na + 1] and msk_plane[total]."""
+    off = np.zeros(na + 1, np.int32)
+    rows = []
+    for a in range(na):
+        pa = np.asarray(planes[a], np.float64).reshape(-1, 4)
+        rows.extend(pa)
+        off[a + 1] = off[a] + len(pa)
+    total = int(off[-1])
+    arr = (Plane * max(total, 1))()
+    for k, r in enumerate(rows):
+        arr[k].defocus, arr[k].rotation, arr[k].astig, arr[k].astig_angle = map(float, r)
+    return off, arr, total
 
 
 class KernelStat(C.Structure):
@@ -399,7 +416,8 @@ class Context:
         return np.ascontiguousarray(a, np.float32)
 
     def tilt_series_batch(self, series, specimens, defocus, graph=True, images=None, nconfig=1,
-                          displacements=None, exitwaves=None, want_exit=False):
+                          displacements=None, exitwaves=None, want_exit=False, planes=None,
+                          shifts=None):
         """Many specimens in one call (msk_tilt_series_batch).  specimens: list
         of (Specimen-like with Znum/x/y/z/occ/fov and, for series.lwobble = 1, a
         float32 `wobble` per atom, n, angleZ, angleY[, ctblengthz]);
@@ -409,7 +427,11 @@ class Context:
         1) or given: displacements, per specimen float32 [nconfig, 3, natom].
         want_exit (or preallocated exitwaves, per specimen [nangles, nconfig, n,
         n, 2] float32 arrays or torch tensors): also returns the exit waves.
-        images may be a list of preallocated arrays or torch CUDA tensors."""
+        images may be a list of preallocated arrays or torch CUDA tensors.
+        planes (per specimen None or, per orientation, rows of (defocus,
+        rotation, astig, astig_angle) as tilt_series_planes takes them) and
+        shifts (per specimen None or [nangles, 2] Angstrom): that specimen's
+        own detector planes; its images are then [total planes, n, n]."""
         defocus = np.ascontiguousarray(defocus, np.float64)
         nd = len(defocus)
         descs = (SpecimenDesc * len(specimens))()
@@ -422,7 +444,14 @@ class Context:
                      (sp_.z, np.float32), (sp_.occ, np.float32))]
             aZ = np.ascontiguousarray(aZ, np.float64)
             aY = np.ascontiguousarray(aY, np.float64)
-            img = images[i] if images is not None else np.zeros((len(aZ), nd, n, n), np.float32)
+            pl_i = planes[i] if planes is not None else None
+            if pl_i is not None:
+                off, parr, total = _plane_arrays(pl_i, len(aZ))
+                keep += [off, parr]
+                shape = (total, n, n)
+            else:
+                shape = (len(aZ), nd, n, n)
+            img = images[i] if images is not None else np.zeros(shape, np.float32)
             kp = np.zeros(len(aZ) * max(1, nconfig), np.int32)
             keep += arrs + [aZ, aY]
             outs.append(img)
@@ -436,6 +465,12 @@ class Context:
             d.angleZ, d.angleY = _ptr(aZ), _ptr(aY)
             d.images, d.kept = _ptr(img), _ptr(kp)
             d.nconfig = nconfig
+            if pl_i is not None:
+                d.plane_off, d.planes = _ptr(off), C.addressof(parr)
+                if shifts is not None and shifts[i] is not None:
+                    sh = np.ascontiguousarray(shifts[i], np.float64).reshape(-1)
+                    keep.append(sh)
+                    d.shifts = _ptr(sh)
             if exitwaves is not None or want_exit:
                 ew = (exitwaves[i] if exitwaves is not None else
                       np.zeros((len(aZ), max(1, nconfig), n, n, 2), np.float32))
@@ -577,16 +612,7 @@ class Context:
         angleZ = np.ascontiguousarray(angleZ, np.float64)
         angleY = np.ascontiguousarray(angleY, np.float64)
         na = len(angleZ)
-        off = np.zeros(na + 1, np.int32)
-        rows = []
-        for a in range(na):
-            pa = np.asarray(planes[a], np.float64).reshape(-1, 4)
-            rows.extend(pa)
-            off[a + 1] = off[a] + len(pa)
-        total = int(off[-1])
-        arr = (Plane * max(total, 1))()
-        for k, r in enumerate(rows):
-            arr[k].defocus, arr[k].rotation, arr[k].astig, arr[k].astig_angle = map(float, r)
+        off, arr, total = _plane_arrays(planes, na)
         sh = None if shifts is None else np.ascontiguousarray(shifts, np.float64).reshape(-1)
         if images is None:
             images = np.zeros((total, series.nx, series.ny), np.float32)

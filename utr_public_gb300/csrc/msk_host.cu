@@ -2588,6 +2588,68 @@ namespace {
 
 constexpr int kLanes = 8;
 
+// Detector planes of one specimen that share their free-space and image-plane
+// parameters: one multiplier table and one pass over the group's units.
+struct ImgGroup {
+    double defocus, astig, astig_angle, rotation;
+    int sxp, syp;   // whole-pixel image shift
+    int nimg, nu;   // images (orientations) and units of the group
+    bool all;       // every unit of the specimen, in order: passes take no unit list
+    size_t o_meta;  // in the meta: img_off[nimg + 1] | img_units[nu] | img_dst[nimg] | img_flags[nimg]
+};
+
+bool same_plane(const ImgGroup &a, const ImgGroup &b)
+{
+    return a.defocus == b.defocus && a.astig == b.astig && a.astig_angle == b.astig_angle &&
+           a.rotation == b.rotation && a.sxp == b.sxp && a.syp == b.syp;
+}
+
+// The detector planes of one specimen's units (u = a * nc + c), grouped as
+// msk_tilt_series groups them: the k-th plane of every orientation that has
+// one, by equal parameters.
+void group_planes(const PlaneList &pl, int na, int nc, double xst, double yst,
+                  std::vector<ImgGroup> &groups, std::vector<int> &meta)
+{
+    groups.clear();
+    meta.clear();
+    int kmax = 0;
+    for (int a = 0; a < na; a++) kmax = std::max(kmax, pl.off[a + 1] - pl.off[a]);
+    for (int k = 0; k < kmax; k++) {
+        const size_t g0 = groups.size();
+        std::vector<std::vector<int>> ori;
+        for (int a = 0; a < na; a++) {
+            if (pl.off[a + 1] - pl.off[a] <= k) continue;
+            const PlaneDesc &d = pl.p[pl.off[a] + k];
+            ImgGroup key{};
+            key.defocus = d.defocus;
+            key.astig = d.astig;
+            key.astig_angle = d.astig_angle;
+            key.rotation = d.rotation;
+            key.sxp = (int)floor(pl.shift[2 * a] / xst + 0.5);
+            key.syp = (int)floor(pl.shift[2 * a + 1] / yst + 0.5);
+            size_t gi = g0;
+            while (gi < groups.size() && !same_plane(groups[gi], key)) gi++;
+            if (gi == groups.size()) {
+                groups.push_back(key);
+                ori.emplace_back();
+            }
+            ori[gi - g0].push_back(a);
+        }
+        for (size_t j = 0; j < ori.size(); j++) {
+            ImgGroup &gr = groups[g0 + j];
+            gr.nimg = (int)ori[j].size();
+            gr.nu = gr.nimg * nc;
+            gr.all = gr.nimg == na;
+            gr.o_meta = meta.size();
+            for (int i = 0; i <= gr.nimg; i++) meta.push_back(i * nc);           // img_off
+            for (int a : ori[j])
+                for (int c = 0; c < nc; c++) meta.push_back(a * nc + c);          // img_units
+            for (int a : ori[j]) meta.push_back(pl.off[a] + k);                   // img_dst
+            for (size_t i = 0; i < ori[j].size(); i++) meta.push_back(nc > 1 ? 2 : 0);  // mean
+        }
+    }
+}
+
 struct SpecPlan {
     GridPre gp;
     int nslices = 0, nangles = 0;
@@ -2597,7 +2659,10 @@ struct SpecPlan {
     std::vector<SplatAtom> atoms;
     std::vector<unsigned char> tables;
     TableLayout tl;
-    std::vector<int> meta;  // per defocus: img_off[n+1] | units[n] | dst[n] | flags[n]
+    std::vector<ImgGroup> groups;  // detector planes
+    std::vector<int> meta;         // the groups' image lists
+    int nimages = 0;               // images of the specimen
+    bool image_plane = false;      // some plane rotated or shifted
     float ctblength = 0.0f, ctblengthz = 0.0f;
     std::vector<float2> wave0;  // spherical incident wave (empty: a plane wave)
     size_t o_tab = 0, o_atoms = 0, o_soff = 0, o_act = 0, o_meta = 0, o_w0 = 0;  // upload region
@@ -2630,14 +2695,14 @@ int ensure_lanes(msk_context *ctx)
 }
 
 // The launches of one specimen on one stream: plane wave, slice loop, then
-// per detector plane the free-space step and the intensity.
+// per group of detector planes the free-space step and the intensity.
 int enqueue_specimen(msk_context *ctx, SpecPlan &P, unsigned char *arena, const msk_series *s,
-                     int ndef, const double *defocus, float *d_images, cudaStream_t st)
+                     float *d_images, cudaStream_t st)
 {
     const GridPre &gp = P.gp;
     const Geom &g = gp.g;
     // units u = a * nconf + c (orientation a, configuration c); images per orientation
-    const int nx = gp.nx, ny = gp.ny, na = P.nunits, nimg = P.nangles, nconf = P.nconf;
+    const int nx = gp.nx, ny = gp.ny, na = P.nunits, nconf = P.nconf;
     const size_t plane = (size_t)nx * ny;
     const SizeOps *rop = size_ops(ny), *cop = size_ops(nx);
     float2 *psi = reinterpret_cast<float2 *>(arena + P.o_psi);
@@ -2726,63 +2791,63 @@ int enqueue_specimen(msk_context *ctx, SpecPlan &P, unsigned char *arena, const 
             MSK_CUDA(ctx, cudaMemcpyAsync(arena + P.o_ew, tb, ewb, cudaMemcpyDeviceToDevice, st));
         }
     }
-    // image plane (autosliccmd.cpp:1119-1143): rotation centre and whole-pixel shift
+    // image plane (autosliccmd.cpp:1119-1143): rotation centre
     const double xst = P.ctblength / nx, yst = P.ctblength / ny;  // float divisions
     const double xcen = 0.5 * P.ctblength + s->dxc, ycen = 0.5 * P.ctblength + s->dyc;
-    const int sxp = (int)floor(s->xshift / xst + 0.5), syp = (int)floor(s->yshift / yst + 0.5);
     const double pi = 4.0 * atan(1.0), l = gp.wavlen;
     float k2maxo = s->aobj / gp.wavlen;
     k2maxo = k2maxo * k2maxo;
-    // per plane: img_off[nimg + 1] | img_units[na] | img_dst[nimg] | img_flags[nimg]
-    const size_t nmeta = (size_t)3 * nimg + 1 + na;
-    for (int d = 0; d < ndef; d++) {
+    const int *meta = reinterpret_cast<const int *>(arena + P.o_meta);
+    for (size_t gi = 0; gi < P.groups.size(); gi++) {
+        const ImgGroup &gr = P.groups[gi];
+        const int ni = gr.nimg, nu = gr.nu;
         Fresnel fr{};
-        const double rprime = defocus[d] - 0.5 * P.ctblengthz;  // autosliccmd.cpp:1060
+        const double rprime = gr.defocus - 0.5 * P.ctblengthz;  // autosliccmd.cpp:1060
         fr.a1 = pi * l * rprime;
         fr.a3 = (pi / 2.0) * s->cs3 * l * l * l;
         fr.a5 = (pi / 3.0) * s->cs5 * l * l * l * l * l;
-        fr.a2c = (pi / 2.0) * l * s->astig * cos(2.0 * s->astig_angle);
-        fr.a2s = (pi / 2.0) * l * s->astig * sin(2.0 * s->astig_angle);
+        fr.a2c = (pi / 2.0) * l * gr.astig * cos(2.0 * gr.astig_angle);
+        fr.a2s = (pi / 2.0) * l * gr.astig * sin(2.0 * gr.astig_angle);
         fr.k2maxo = k2maxo;
         fr.kx = gp.d_kx;
         fr.ky = gp.d_ky;
-        float2 *tab = reinterpret_cast<float2 *>(arena + P.o_fres) + (size_t)d * plane;
+        float2 *tab = reinterpret_cast<float2 *>(arena + P.o_fres) + gi * plane;
         fr.table = tab;
+        // a group of every unit in order takes no unit list
+        const int *d_off = meta + gr.o_meta, *d_units = d_off + ni + 1,
+                  *d_dst = d_units + nu, *d_flags = d_dst + ni;
+        const int *ulist = gr.all ? nullptr : d_units;
         {
             Prof p(ctx, kFresTab, 8.0 * pl, st);
             k_fresnel_table<<<4 * 152, 256, 0, st>>>(g, fr, 1.0f / ((float)nx * (float)ny), tab);
         }
         {
-            Prof p(ctx, kFresnel, 16.0 * pl * na, st);
-            cop->col_fresnel(g, pmapf, tmapf, nullptr, na, fr, 1.0f, st);
+            Prof p(ctx, kFresnel, 16.0 * pl * nu, st);
+            cop->col_fresnel(g, pmapf, tmapf, ulist, nu, fr, 1.0f, st);
         }
-        const int *dm = reinterpret_cast<const int *>(arena + P.o_meta) + (size_t)d * nmeta;
-        const int *d_off = dm, *d_units = dm + nimg + 1, *d_dst = dm + nimg + 1 + na,
-                  *d_flags = dm + 2 * nimg + 1 + na;
-        const double rot = s->rotation ? s->rotation[d] : 0.0;
-        if (rot != 0.0 || sxp != 0 || syp != 0) {
+        const double rot = gr.rotation;
+        if (rot != 0.0 || gr.sxp != 0 || gr.syp != 0) {
             // the amplitude in real space, rotated and shifted, then |.|^2
             float2 *phi = reinterpret_cast<float2 *>(arena + P.o_phi);
             float2 *fill = reinterpret_cast<float2 *>(arena + P.o_fill);
             {
-                Prof p(ctx, kExit, 16.0 * pl * na, st);
-                rop->row_inverse(g, nullptr, na, tb, phi, 1.0f, st);
+                Prof p(ctx, kExit, 16.0 * pl * nu, st);
+                rop->row_inverse(g, ulist, nu, tb, phi, 1.0f, st);
             }
-            k_edge_mean<<<na, 256, 0, st>>>(phi, nullptr, nx, ny, 5, fill);
+            k_edge_mean<<<nu, 256, 0, st>>>(phi, ulist, nx, ny, 5, fill);
             {
-                Prof p(ctx, kRotShift, 16.0 * pl * na, st);
-                k_rotate_shift<<<8 * 152, 256, 0, st>>>(phi, tb, nullptr, na, nx, ny, xst, yst, xcen,
-                                                        ycen, cos(rot), sin(rot), rot != 0.0, sxp,
-                                                        syp, fill);
+                Prof p(ctx, kRotShift, 16.0 * pl * nu, st);
+                k_rotate_shift<<<8 * 152, 256, 0, st>>>(phi, tb, ulist, nu, nx, ny, xst, yst, xcen,
+                                                        ycen, cos(rot), sin(rot), rot != 0.0,
+                                                        gr.sxp, gr.syp, fill);
             }
-            Prof p(ctx, kIntensity, 8.0 * pl * na + 4.0 * pl * nimg, st);
-            k_intensity_direct<<<8 * 152, 256, 0, st>>>(nimg, d_off, d_units, d_dst, d_flags, tb,
+            Prof p(ctx, kIntensity, 8.0 * pl * nu + 4.0 * pl * ni, st);
+            k_intensity_direct<<<8 * 152, 256, 0, st>>>(ni, d_off, d_units, d_dst, d_flags, tb,
                                                         d_images, plane, (float)nconf);
             continue;
         }
-        Prof p(ctx, kIntensity, 8.0 * pl * na + 4.0 * pl * nimg, st);
-        rop->row_intensity(g, nimg, d_off, d_units, d_dst, d_flags, tb, d_images, (float)nconf,
-                           st);
+        Prof p(ctx, kIntensity, 8.0 * pl * nu + 4.0 * pl * ni, st);
+        rop->row_intensity(g, ni, d_off, d_units, d_dst, d_flags, tb, d_images, (float)nconf, st);
     }
     MSK_CUDA(ctx, cudaGetLastError());
     return MSK_OK;
@@ -2806,9 +2871,18 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
             return fail(ctx, MSK_EINVAL, "several configurations need lwobble = 1 (bad specimen " +
                                              std::to_string(i) + ")");
         if (q.natom < 0 || q.nangles < 1 || !q.angleZ || !q.angleY ||
-            (ndefocus > 0 && !q.images) ||
             (q.natom > 0 && (!q.Znum || !q.x || !q.y || !q.z || !q.occ)))
             return fail(ctx, MSK_EINVAL, "bad specimen " + std::to_string(i));
+        int nimg = q.nangles * ndefocus;
+        if (q.plane_off) {
+            bool ok = q.plane_off[0] == 0;
+            for (int a = 0; a < q.nangles && ok; a++) ok = q.plane_off[a + 1] >= q.plane_off[a];
+            if (!ok) return fail(ctx, MSK_EINVAL, "bad plane lists of specimen " + std::to_string(i));
+            nimg = q.plane_off[q.nangles];
+            if (nimg > 0 && !q.planes)
+                return fail(ctx, MSK_EINVAL, "bad plane lists of specimen " + std::to_string(i));
+        }
+        if (nimg > 0 && !q.images) return fail(ctx, MSK_EINVAL, "bad specimen " + std::to_string(i));
         if (q.nx < 1 || q.ny < 1 || q.ctblength < 0.0f)
             return fail(ctx, MSK_EBADSIZE, "bad size parameters of specimen " + std::to_string(i));
         if (!pow2_supported(q.nx) || !pow2_supported(q.ny))
@@ -2876,27 +2950,41 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
         SpecPlan &q = P[i];
         build_tables(q.gp, zlist, q.tables, q.tl);
         pack_batch(q.ua, 0, q.nunits, q.nslices, q.b, q.atoms);
+        // detector planes: the specimen's own lists, else the call's defoci with
+        // s's image plane for every orientation (as msk_tilt_series builds them)
+        const msk_specimen &sp = spec[i];
         const int na = q.nangles, nc = q.nconf;
-        q.meta.clear();
-        for (int d = 0; d < ndefocus; d++) {
-            for (int a = 0; a <= na; a++) q.meta.push_back(a * nc);    // img_off
-            for (int u = 0; u < q.nunits; u++) q.meta.push_back(u);    // img_units
-            for (int a = 0; a < na; a++) q.meta.push_back(a * ndefocus + d);  // img_dst
-            for (int a = 0; a < na; a++) q.meta.push_back(nc > 1 ? 2 : 0);    // img_flags: mean
+        PlaneList pl;
+        for (int a = 0; a <= na; a++) pl.off.push_back(sp.plane_off ? sp.plane_off[a] : a * ndefocus);
+        pl.total = pl.off[na];
+        for (int a = 0; a < na; a++) {
+            if (sp.plane_off) {
+                for (int k = pl.off[a]; k < pl.off[a + 1]; k++)
+                    pl.p.push_back(PlaneDesc{sp.planes[k].defocus, sp.planes[k].rotation,
+                                             sp.planes[k].astig, sp.planes[k].astig_angle});
+                pl.shift.push_back(sp.shifts ? sp.shifts[2 * a] : 0.0);
+                pl.shift.push_back(sp.shifts ? sp.shifts[2 * a + 1] : 0.0);
+            } else {
+                for (int d = 0; d < ndefocus; d++)
+                    pl.p.push_back(PlaneDesc{defocus[d], s->rotation ? s->rotation[d] : 0.0,
+                                             s->astig, s->astig_angle});
+                pl.shift.push_back(s->xshift);
+                pl.shift.push_back(s->yshift);
+            }
         }
+        group_planes(pl, na, nc, q.ctblength / q.gp.nx, q.ctblength / q.gp.ny, q.groups, q.meta);
+        q.nimages = pl.total;
+        q.image_plane = false;
+        for (const ImgGroup &gr : q.groups)
+            q.image_plane |= gr.rotation != 0.0 || gr.sxp != 0 || gr.syp != 0;
         q.work = (double)q.nunits * q.nslices * q.gp.nx * q.gp.ny;
-        q.img_dev = ndefocus > 0 && is_device_ptr(spec[i].images);
-        q.img_pinned = ndefocus > 0 && !q.img_dev && is_pinned_host(spec[i].images);
+        q.img_dev = q.nimages > 0 && is_device_ptr(spec[i].images);
+        q.img_pinned = q.nimages > 0 && !q.img_dev && is_pinned_host(spec[i].images);
         q.ew = spec[i].exitwaves;
         q.ew_dev = q.ew && is_device_ptr(q.ew);
         q.ew_pinned = q.ew && !q.ew_dev && is_pinned_host(q.ew);
         if (s->R1 != 0.0) spherical_wave(q.gp.nx, q.gp.ny, q.ctblength, s->v0, s->R1, q.wave0);
     });
-    // image-plane rotation or shift of some detector plane: per specimen a real-space
-    // scratch grid per orientation and the edge means
-    bool image_plane = s->xshift != 0.0 || s->yshift != 0.0;
-    for (int d = 0; d < ndefocus && s->rotation; d++) image_plane |= s->rotation[d] != 0.0;
-
     // waves of specimens whose arena fits the memory budget
     size_t free_b = 0, total_b = 0;
     MSK_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
@@ -2918,17 +3006,19 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
         q.o_dw = up;
         up += align256(q.b.dw.size() * sizeof(float));
         q.o_fres = work;
-        work += align256((size_t)std::max(ndefocus, 1) * plane * sizeof(float2));
+        work += align256(std::max<size_t>(q.groups.size(), 1) * plane * sizeof(float2));
         q.o_psi = work;
         work += align256((size_t)q.nunits * plane * sizeof(float2));
         q.o_tbuf = work;
         work += align256((size_t)q.nunits * plane * sizeof(float2));
         q.o_img = work;
-        if (!q.img_dev) work += align256((size_t)q.nangles * ndefocus * plane * sizeof(float));
+        if (!q.img_dev) work += align256((size_t)q.nimages * plane * sizeof(float));
+        // a rotated or shifted image plane: a real-space scratch grid per unit and
+        // the edge means
         q.o_phi = work;
-        if (image_plane) work += align256((size_t)q.nunits * plane * sizeof(float2));
+        if (q.image_plane) work += align256((size_t)q.nunits * plane * sizeof(float2));
         q.o_fill = work;
-        if (image_plane) work += align256((size_t)q.nunits * sizeof(float2));
+        if (q.image_plane) work += align256((size_t)q.nunits * sizeof(float2));
         q.o_spec = work;
         if (!q.b.dw.empty()) work += align256((size_t)q.nunits * plane * sizeof(float2));
         q.o_ew = work;
@@ -3019,8 +3109,8 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
         // a specimen's images to page-locked host memory on its own lane, as
         // soon as they are made (beside the other lanes' kernels)
         auto images_out = [&](int i, cudaStream_t st_) -> int {
-            if (ndefocus == 0 || !P[i].img_pinned) return MSK_OK;
-            const size_t bytes = (size_t)P[i].nangles * ndefocus * P[i].gp.nx * P[i].gp.ny * sizeof(float);
+            if (P[i].nimages == 0 || !P[i].img_pinned) return MSK_OK;
+            const size_t bytes = (size_t)P[i].nimages * P[i].gp.nx * P[i].gp.ny * sizeof(float);
             if (cudaMemcpyAsync(spec[i].images, arena + P[i].o_img, bytes, cudaMemcpyDeviceToHost,
                                 st_) != cudaSuccess)
                 return fail(ctx, MSK_ECUDA, "image copy");
@@ -3030,7 +3120,7 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
         if (nl == 1) {
             for (int i : lane_of[0]) {
                 float *dimg = P[i].img_dev ? spec[i].images : reinterpret_cast<float *>(arena + P[i].o_img);
-                if ((rc = enqueue_specimen(ctx, P[i], arena, s, ndefocus, defocus, dimg, ctx->stream)))
+                if ((rc = enqueue_specimen(ctx, P[i], arena, s, dimg, ctx->stream)))
                     break;
                 if ((rc = images_out(i, ctx->stream))) break;
             }
@@ -3044,8 +3134,7 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
                 }
                 for (int i : lane_of[l]) {
                     float *dimg = P[i].img_dev ? spec[i].images : reinterpret_cast<float *>(arena + P[i].o_img);
-                    if ((rc = enqueue_specimen(ctx, P[i], arena, s, ndefocus, defocus, dimg,
-                                               ctx->lanes[l])))
+                    if ((rc = enqueue_specimen(ctx, P[i], arena, s, dimg, ctx->lanes[l])))
                         break;
                     if ((rc = images_out(i, ctx->lanes[l]))) break;
                 }
@@ -3084,8 +3173,8 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
                                               cudaMemcpyDeviceToHost, ctx->stream));
                 count_copy(ctx, 1, (double)ewb);
             }
-            if (ndefocus == 0 || P[i].img_dev || P[i].img_pinned) continue;
-            const size_t bytes = (size_t)P[i].nangles * ndefocus * P[i].gp.nx * P[i].gp.ny * sizeof(float);
+            if (P[i].nimages == 0 || P[i].img_dev || P[i].img_pinned) continue;
+            const size_t bytes = (size_t)P[i].nimages * P[i].gp.nx * P[i].gp.ny * sizeof(float);
             MSK_CUDA(ctx, cudaMemcpyAsync(spec[i].images, arena + P[i].o_img, bytes,
                                           cudaMemcpyDeviceToHost, ctx->stream));
             count_copy(ctx, 1, (double)bytes);
