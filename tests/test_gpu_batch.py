@@ -293,6 +293,19 @@ def test_batch_errors(ctx, msk):
     with pytest.raises(msk.MskError) as e:
         ctx.tilt_series_batch(s, [cases[1], (spec, 64, [0.0], [0.0])], [0.0])
     assert e.value.status == msk.MSK_EZNUM
+    # a specimen's plane offsets must start at 0 and not decrease (checked on the host)
+    good = msk._plane_arrays
+
+    def bad_offsets(planes, na):
+        off, arr, total = good(planes, na)
+        off[1] = off[2] + 1
+        return off, arr, total
+
+    with pytest.MonkeyPatch.context() as mp:
+        mp.setattr(msk, "_plane_arrays", bad_offsets)
+        with pytest.raises(msk.MskError) as e:
+            ctx.tilt_series_batch(s, cases[:1], [0.0], planes=[[[(0.0, 0, 0, 0)]] * 3])
+    assert e.value.status == msk.MSK_EINVAL
     # the context stays usable
     imgs, _ = ctx.tilt_series_batch(s, cases, [0.0])
     assert all(np.isfinite(i).all() for i in imgs)
