@@ -257,7 +257,7 @@ def run_adjoint(args, rank, world, local_rank):
     ctx.set_stream(stream.cuda_stream)
     spec = specimen.plain_specimen(1001)
     atoms = (spec.Znum, spec.x, spec.y, spec.z, spec.occ)
-    nang = ADJ_NANG
+    nang = args.adj_orientations
     angY = np.deg2rad(2.0 * np.arange(nang))
     angZ = np.full(nang, 0.1 * rank)
     s = msk.Series()
@@ -388,14 +388,15 @@ def run_adjoint(args, rank, world, local_rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": "adjoint: plain specimen (2000 atoms, 64 A box), 512^2, 64 "
-                               "slices of 1 A, 200 keV, 90 orientations (2 deg about y), "
+                               "slices of 1 A, 200 keV, %d orientations (2 deg about y), " % nang +
                                "potentials splatted on the GPU, target from v(1 + 0.01 N(0,1)), "
                                "1 detector plane (defocus 0), " + (
                                    "every wave and transmission kept (checkpoint 0)"
                                    if args.adj_checkpoint == 0 else
                                    "checkpoint every %d slices" % args.adj_checkpoint),
                    "slice_steps_per_step": steps_per * world,
-                   "l2": "inputs larger than L2 (stacks 6.0 GB per GPU)"},
+                   "l2": "inputs larger than L2 (stacks %.1f GB per GPU)"
+                         % (nang * S * ADJ_NX * ADJ_NX * 4 / 1e9)},
         "keep_all": keep_all,
         "cpu_baseline": cpu,
         "forward_only": {"value": world * steps_per / (ms_fwd / 1000.0), "unit": UNIT,
@@ -969,6 +970,9 @@ def main():
     ap.add_argument("--adj-checkpoint", type=int, default=ADJ_CHECKPOINT,
                     help="adjoint: slices per checkpoint (0: keep every wave and transmission "
                          "when memory allows)")
+    ap.add_argument("--adj-orientations", type=int, default=ADJ_NANG,
+                    help="adjoint: orientations per step (90 for the adjoint workload; fewer "
+                         "keep a profiler capture within a few GB)")
     ap.add_argument("--fd-voxels", type=int, default=256,
                     help="central-difference voxels per checked orientation (adjoint)")
     ap.add_argument("--utr-n", type=int, default=NX,

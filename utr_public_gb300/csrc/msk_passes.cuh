@@ -656,9 +656,14 @@ k_row_expv(const Geom g, const float *__restrict__ v, size_t ustride, float2 *__
     const float *src = v + (size_t)u * ustride + (size_t)(ix < nx ? ix : 0) * NY;
     float2 w[E];
     bool nz = false;
+    // every load in flight before the first vote on a value (a vote per load
+    // would send them out one memory latency apart); the potentials wait in
+    // the real parts
+#pragma unroll
+    for (int m = 0; m < E; m++) w[m].x = src[t + m * T];
 #pragma unroll
     for (int m = 0; m < E; m++) {
-        const float ph = src[t + m * T] * g.sigma_f;
+        const float ph = w[m].x * g.sigma_f;
         w[m] = make_float2(0.0f, 0.0f);
         nz |= ph != 0.0f;
         if (__any_sync(0xffffffffu, ph != 0.0f)) w[m] = expm1i(ph);
@@ -792,12 +797,22 @@ k_row_grad(const Geom g, const float2 *__restrict__ Ge, const float *__restrict_
     const float c = 2.0f * g.sigma_f / (float)NY;
     const float *vr = v + (size_t)u * ustride + row;
     float *gr = grad + (size_t)u * ustride + row;
+    // the potentials in groups of G loads in flight before their votes (the
+    // transformed row holds the registers a whole line would need)
+    constexpr int G = E < 8 ? E : 8;
 #pragma unroll
-    for (int m = 0; m < E; m++) {
-        const float ph = vr[t + m * T] * g.sigma_f;
-        float2 e = make_float2(1.0f, 0.0f);
-        if (__any_sync(0xffffffffu, ph != 0.0f)) e = expi(ph);
-        if (row_ok) gr[t + m * T] = c * (a[m].y * e.x - a[m].x * e.y);
+    for (int m0 = 0; m0 < E; m0 += G) {
+        float vv[G];
+#pragma unroll
+        for (int j = 0; j < G; j++) vv[j] = vr[t + (m0 + j) * T];
+#pragma unroll
+        for (int j = 0; j < G; j++) {
+            const int m = m0 + j;
+            const float ph = vv[j] * g.sigma_f;
+            float2 e = make_float2(1.0f, 0.0f);
+            if (__any_sync(0xffffffffu, ph != 0.0f)) e = expi(ph);
+            if (row_ok) gr[t + m * T] = c * (a[m].y * e.x - a[m].x * e.y);
+        }
     }
 }
 
