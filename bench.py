@@ -694,21 +694,32 @@ def run_uneven(args, rank, world, local_rank):
         return
     err = None
     if not args.no_fp64_check:
-        # FP64 oracle on the smallest-grid specimen's first orientation
+        # FP64 oracle on one specimen per grid size (the one with the fewest atoms),
+        # its first orientation; the four checks run on host threads
         try:
+            import concurrent.futures as cf
             from oracle import oracle as orc
-            i = min(range(len(cases)), key=lambda j: (cases[j][1], cases[j][0].natom))
-            sp_, n, aZ, aY = cases[i]
             O = orc.Oracle()
-            p = orc.SeriesParams()
-            p.ax, p.ctblengthz, p.nx, p.ny, p.v0, p.deltaz = sp_.fov, sp_.fov, n, n, V0, DZ
-            p.max_slices, p.min_slice = -1, 0
-            ref, _ = O.orientation(p, sp_.Znum, sp_.x, sp_.y, sp_.z, sp_.occ, aZ[0], aY[0],
-                                   defoci, fp64=True)
-            got = imgs[i][0].cpu().numpy()
-            err = {"specimen": i, "grid": n, "natom": sp_.natom,
-                   "image_rel_l2": [float(np.linalg.norm(got[d] - ref[d]) / np.linalg.norm(ref[d]))
-                                    for d in range(len(defoci))]}
+
+            def check(n):
+                sel = [j for j in range(len(cases)) if cases[j][1] == n]
+                i = min(sel, key=lambda j: cases[j][0].natom)
+                sp_, _, aZ, aY = cases[i]
+                p = orc.SeriesParams()
+                p.ax, p.ctblengthz, p.nx, p.ny, p.v0, p.deltaz = sp_.fov, sp_.fov, n, n, V0, DZ
+                p.max_slices, p.min_slice = -1, 0
+                ref, _ = O.orientation(p, sp_.Znum, sp_.x, sp_.y, sp_.z, sp_.occ, aZ[0], aY[0],
+                                       defoci, fp64=True)
+                got = imgs[i][0].cpu().numpy()
+                return {"specimen": i, "grid": n, "natom": sp_.natom,
+                        "slices": msk.slice_count(DZ, sp_.fov),
+                        "image_rel_l2": [float(np.linalg.norm(got[d] - ref[d]) /
+                                               np.linalg.norm(ref[d])) for d in range(len(defoci))]}
+
+            sizes = sorted({c[1] for c in cases})
+            with cf.ThreadPoolExecutor(len(sizes)) as ex:
+                err = {"per_grid": list(ex.map(check, sizes))}
+            err["max_image_rel_l2"] = max(max(e["image_rel_l2"]) for e in err["per_grid"])
         except Exception as ex:
             err = {"error": repr(ex)}
     out = {

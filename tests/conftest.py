@@ -45,6 +45,11 @@ def golden(name):
 
 
 def rel_l2(a, b):
-    a = np.asarray(a, np.float64)
-    b = np.asarray(b, np.float64)
+    """Relative L2 distance ||a - b|| / ||b|| over every element.  Complex
+    arrays are compared as complex128 (real and imaginary parts both count);
+    interleaved (..., 2) float arrays as they are."""
+    a, b = np.asarray(a), np.asarray(b)
+    dt = np.complex128 if (np.iscomplexobj(a) or np.iscomplexobj(b)) else np.float64
+    a = a.astype(dt)
+    b = b.astype(dt)
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))

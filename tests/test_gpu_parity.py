@@ -200,6 +200,21 @@ def test_full_grid_thin_slab(ctx, msk, oracle):
     assert rel_l2(pix, ref64) < 1e-5
 
 
+@pytest.mark.parametrize("n,fov", [(2048, 200.0), (4096, 256.0)])
+def test_large_grid_thin_slab(ctx, msk, oracle, n, fov):
+    """The uneven batch's largest grid (2048^2) and the largest supported grid
+    (4096^2), both with atoms, on a slab of five 1 A slices that the FP64 oracle
+    finishes in seconds: every line length of the row and column passes at
+    full width in both dimensions."""
+    spec = sp.random_specimen(600, fov, 0.1 * fov, 0.9 * fov, 777 + n)
+    spec.z[:] = np.float32(1.0) + (spec.z - np.float32(0.1 * fov)) * np.float32(3.0 / (0.8 * fov))
+    atoms = (spec.Znum, spec.x, spec.y, spec.z, spec.occ)
+    param = msk.make_param(fov, fov, n, n, 300.0, 1.0)
+    pix = ctx.calculate(param, *atoms, fov, 5.0)
+    ref64 = oracle.calculate(param, *atoms, fov, 5.0, fp64=True)
+    assert rel_l2(pix, ref64) < 1e-5
+
+
 def test_per_angle_form_matches_batched(ctx, msk, oracle):
     """The per-orientation comparison form computes the same images."""
     spec = sp.random_specimen(500, 64.0, 10.0, 54.0, 1014)
@@ -220,9 +235,13 @@ def test_per_angle_form_matches_batched(ctx, msk, oracle):
 
 def test_full_size_tilt_series(ctx, msk, oracle):
     """The tilt-series workload at its full size (20000 atoms, 1024^2, 160 slices of
-    1 A, 300 keV, defoci 0 and 500 A): the 45-degree orientation of a four-orientation
-    call against the FP64 oracle (exit wave and images within 1e-5), and that
-    orientation computed alone equal to it bit for bit (units are independent)."""
+    1 A, 300 keV, defoci 0 and 500 A): the 45-, 90- and 135-degree orientations of a
+    four-orientation call against the FP64 oracle (exit waves and images within 1e-5;
+    at 45 and 135 degrees the box rule drops the cube's corner atoms, and the kept
+    counts must agree), and the 45-degree orientation computed alone equal to it bit
+    for bit (units are independent).  The oracle's orientations run on host threads
+    (its calls release the interpreter lock)."""
+    import concurrent.futures as cf
     from oracle.oracle import SeriesParams
     spec = sp.tilt_specimen(1002)
     atoms = (spec.Znum, spec.x, spec.y, spec.z, spec.occ)
@@ -232,14 +251,22 @@ def test_full_size_tilt_series(ctx, msk, oracle):
     s.v0, s.deltaz = 300.0, 1.0
     angY = np.deg2rad([0.0, 45.0, 90.0, 135.0])
     defoci = [0.0, 500.0]
-    imgs, ew, _ = ctx.tilt_series(s, *atoms, np.zeros(4), angY, defoci, want_exit=True)
+    imgs, ew, kept = ctx.tilt_series(s, *atoms, np.zeros(4), angY, defoci, want_exit=True)
     one, ew1, _ = ctx.tilt_series(s, *atoms, [0.0], angY[1:2], defoci, want_exit=True)
     assert np.array_equal(one[0], imgs[1]) and np.array_equal(ew1[0], ew[1])
     sr = SeriesParams()
     sr.ax, sr.ctblengthz, sr.nx, sr.ny, sr.v0, sr.deltaz = 160.0, 160.0, 1024, 1024, 300.0, 1.0
     sr.max_slices, sr.min_slice = -1, 0
-    ref_img, ref_ew, _ = oracle.orientation(sr, *atoms, 0.0, angY[1], np.array(defoci),
-                                            fp64=True, want_exit=True)
-    assert rel_l2(ew[1, 0], ref_ew) < 1e-5
-    for d in range(2):
-        assert rel_l2(imgs[1, d], ref_img[d]) < 1e-5
+
+    def ref(a):
+        return oracle.orientation(sr, *atoms, 0.0, angY[a], np.array(defoci), fp64=True,
+                                  want_exit=True)
+
+    with cf.ThreadPoolExecutor(3) as ex:
+        refs = dict(zip((1, 2, 3), ex.map(ref, (1, 2, 3))))
+    for a, (ref_img, ref_ew, k) in refs.items():
+        assert kept[a] == k, a
+        assert rel_l2(ew[a, 0], ref_ew) < 1e-5, a
+        for d in range(2):
+            assert rel_l2(imgs[a, d], ref_img[d]) < 1e-5, (a, d)
+    assert kept[1] < 20000 and kept[3] < 20000 and kept[2] == 20000
