@@ -10,8 +10,10 @@
 //
 // The class layout comes from the reference's header, so autosliccmd.cpp
 // (autosliccmd.cpp:936-937) calls it unchanged.  Only the coherent branch is
-// provided (lpartl = lbeams = lcross = 0, no thermal wobble); everything else,
-// and every error the reference answers with exit(0), becomes an exception.
+// provided (lpartl = lbeams = lcross = 0), with its thermal branches (lwobble,
+// iseed and wobble are forwarded to msk_calculate); the partial-coherence,
+// beam and cross-section branches, and every error the reference answers with
+// exit(0), become an exception.
 #include <cstring>
 #include <stdexcept>
 #include <string>
