@@ -99,3 +99,32 @@ def test_orientations_errors(msk, tmp_path):
     other.write_text("1 2\n")
     with pytest.raises(msk.MskError):
         msk.read_orientations(other)
+
+
+SHIPPED = "DefocusRand108_2_NEW2.txt"
+
+
+def shipped_numpy():
+    """The reference's shipped orientation file parsed by numpy: two '//'
+    header lines, then 108 lines of six tab-separated numbers (Z, Y', then the
+    Z'' rotation and defocus of each of two detector planes)."""
+    import os
+    from conftest import GOLDEN
+    return np.loadtxt(os.path.join(GOLDEN, SHIPPED), comments="//", delimiter="\t")
+
+
+def test_reads_the_reference_orientation_file(msk):
+    """msk_read_orientations on the file the reference ships beside MsctKirkland
+    (MultisliceCppTest/MsctKirkland/DefocusRand108_2_NEW2.txt; its readers,
+    MultisliceT.cpp:264-277): every angle and plane equal to numpy's parse."""
+    import os
+    from conftest import GOLDEN
+    want = shipped_numpy()
+    assert want.shape == (108, 6)
+    angles, planes, shifts = msk.read_orientations(os.path.join(GOLDEN, SHIPPED))
+    assert angles.shape == (108, 2) and np.array_equal(angles, want[:, :2])
+    assert len(planes) == 108 and all(p.shape == (2, 5) for p in planes)
+    pl = np.stack(planes)
+    assert np.array_equal(pl[:, :, 0], want[:, [2, 4]])   # Z'' rotations
+    assert np.array_equal(pl[:, :, 1], want[:, [3, 5]])   # defoci
+    assert not pl[:, :, 2:].any() and not shifts.any()     # no astigmatism, no shifts
