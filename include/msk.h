@@ -230,11 +230,14 @@ int msk_tilt_series_planes(msk_context *ctx, const msk_series *s, int natom, con
 /* calculate() without any allocation -- no counterpart in the reference.
  * For callers that cannot allocate device memory (a plug-in inside a host
  * framework that owns all device memory through its own pool, or a loop that
- * cannot take cudaMalloc's latency and implicit synchronisation).  Same
- * arguments and result as msk_calculate, minus the context, plus the CUDA
- * stream to run on (NULL: the legacy default stream); host pointers; blocks
- * until pix is written.  Its device scratch is a fixed 8.07 MiB array in this
- * library, held by every GPU that loads it until the process exits.
+ * cannot take cudaMalloc's latency and implicit synchronisation).  The
+ * arguments and result of msk_calculate's coherent branch: no context, and no
+ * thermal branch (msk_calculate's wobble, lwobble and iseed are not taken);
+ * plus the CUDA stream to run on (NULL: the legacy default stream); host
+ * pointers; blocks until pix is written.  Its device scratch is a fixed
+ * 8.07 MiB array in this library, held by every GPU that loads it until the
+ * process exits; no call allocates device memory (a buffer that would have to
+ * grow fails the call with MSK_ENOMEM instead; msk_device_allocations counts).
  * Limits: nx*ny <= 512*512, natom <= 65536, <= 4096 slices; beyond them it
  * returns MSK_ETOOLARGE.  The first call on a device looks up the array's
  * device address (cudaGetSymbolAddress) with that device current; make that
@@ -246,6 +249,11 @@ int msk_calculate_static(void *stream, float *pix, const float *wave0, const flo
                          int natom, const int *Znum, const float *x, const float *y,
                          const float *z, const float *occ, float ctblength, float ctblengthz,
                          int nmode);
+
+/* Device allocations (cudaMalloc) this library has made in this process so far,
+ * over every context -- no counterpart in the reference; lets a caller check
+ * that a run of msk_calculate_static calls allocated nothing. */
+long long msk_device_allocations(void);
 
 /* Use the caller's CUDA stream (a cudaStream_t) for this context's work
  * instead of the context's own; NULL restores the context's stream. */

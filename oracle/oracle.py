@@ -22,7 +22,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_ORACLE = os.path.join(HERE, "liboracle.so")
 LIB_REF = os.path.join(HERE, "_ref", "libautoslic_ref.so")
 LIB_UTR_REF = os.path.join(HERE, "_ref", "libutr_ref.so")
-REF_TREE = "/root/reference"
+# The reference tree (timg021/UTR_public sources) for the recipe that compiles
+# its own code: MSK_REFERENCE_TREE, or the tree a previous build recorded.
+REF_RECORD = os.path.join(HERE, "_ref", "tree.txt")
 
 # param[] offsets (slicelib.hpp:142-240)
 pXCTILT, pYCTILT, pDEFOCUS, pENERGY, pOAPERT = 9, 10, 11, 16, 17
@@ -35,13 +37,31 @@ _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 
 
-def build(with_ref=None):
-    """Compile liboracle.so (and oracle/_ref when the reference tree exists)."""
+def reference_tree(tree=None):
+    """The reference source tree to compile from, or None: `tree`, else the
+    MSK_REFERENCE_TREE environment variable, else the tree recorded by the last
+    build of oracle/_ref; only a tree that holds TemsimLibrary counts."""
+    cands = [tree, os.environ.get("MSK_REFERENCE_TREE")]
+    if os.path.exists(REF_RECORD):
+        with open(REF_RECORD) as f:
+            cands.append(f.read().strip())
+    for t in cands:
+        if t and os.path.isdir(os.path.join(t, "TemsimLibrary")):
+            return t
+    return None
+
+
+def build(with_ref=None, tree=None):
+    """Compile liboracle.so, and oracle/_ref from the reference tree (see
+    reference_tree) when there is one; with_ref=True requires it."""
     subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
-    if with_ref is None:
-        with_ref = os.path.isdir(os.path.join(REF_TREE, "TemsimLibrary"))
-    if with_ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + REF_TREE], check=True)
+    ref = reference_tree(tree)
+    if with_ref and ref is None:
+        raise RuntimeError("the reference tree is needed: set MSK_REFERENCE_TREE")
+    if ref is not None and with_ref is not False:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + ref], check=True)
+        with open(REF_RECORD, "w") as f:
+            f.write(ref + "\n")
 
 
 class SeriesParams(C.Structure):

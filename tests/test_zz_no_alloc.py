@@ -4,8 +4,8 @@ pool, or a loop that cannot afford cudaMalloc's latency and implicit
 synchronisation).  Its scratch is a fixed array compiled into libmsk.so, so
 this file checks, through the C ABI, that consecutive calls of different
 sizes -- each reusing what the previous call left in that array -- give the
-same exit wave as msk_calculate, and that sizes beyond the array's limits are
-refused.  It is collected last so that a run stopping at its first failure
+same exit wave as msk_calculate while the library's device-allocation count
+stays unchanged, and that sizes beyond the array's limits are refused.  It is collected last so that a run stopping at its first failure
 has already run every other test; it also passes alone in a fresh process.
 """
 import numpy as np
@@ -34,12 +34,23 @@ def cases(msk):
 
 def test_static_entry_matches_calculate_on_consecutive_calls(ctx, msk):
     big, small = cases(msk)
-    # big, then a smaller grid over what the big call left behind, then big again
-    for param, atoms, box, boxz in (big, small, big):
-        ref = ctx.calculate(param, *atoms, box, boxz)
+    seq = (big, small, big)  # a smaller grid over what the big call left, then big again
+    refs = [ctx.calculate(param, *atoms, box, boxz) for param, atoms, box, boxz in seq]
+    # the counter counts: a new context's first call allocates its buffers
+    n0 = msk.device_allocations()
+    c2 = msk.Context(0)
+    try:
+        c2.calculate(*small[:1], *small[1], small[2], small[3])
+    finally:
+        c2.close()
+    assert msk.device_allocations() > n0
+    # ... and the entry point allocates nothing, on any of its calls
+    n1 = msk.device_allocations()
+    for (param, atoms, box, boxz), ref in zip(seq, refs):
         out = msk.calculate_static(param, *atoms, box, boxz)
         assert np.isfinite(out).all()
         assert rel_l2(out, ref) < TOL
+    assert msk.device_allocations() == n1
 
 
 def test_static_entry_refuses_sizes_beyond_its_scratch(msk):

@@ -31,7 +31,8 @@ EXPORTS = ("msk_create", "msk_destroy", "msk_last_error", "msk_status_string", "
            "msk_write_grd", "msk_write_grc", "msk_write_tiff32", "msk_read_orientations",
            "msk_tilt_series_planes", "msk_utr_depth", "msk_utr_reconstruct",
            "msk_utr_reconstruct_planes", "msk_utr_grid",
-           "msk_utr_ctf_correction3d", "msk_utr_inverse_mlaplacian3d")
+           "msk_utr_ctf_correction3d", "msk_utr_inverse_mlaplacian3d",
+           "msk_device_allocations")
 MSK_BATCH_GRAPH = 1
 
 
@@ -169,6 +170,8 @@ def load():
                                             C.c_int, _dp, _dp, C.c_int, vp, C.c_int, vp, vp, vp]
     L.msk_calculate_static.argtypes = [vp, vp, vp, _fp, C.c_int, vp, vp, vp, vp, vp, C.c_float,
                                        C.c_float, C.c_int]
+    L.msk_device_allocations.argtypes = []
+    L.msk_device_allocations.restype = C.c_longlong
     L.msk_stack_images.argtypes = [vp, C.POINTER(Stack), C.c_int, vp, C.c_int, vp, vp]
     L.msk_adjoint.argtypes = [vp, C.POINTER(Stack), C.c_int, vp, C.c_int, vp, vp, vp,
                                     C.POINTER(C.c_double)]
@@ -313,6 +316,11 @@ def calculate_static(param, Znum, x, y, z, occ, ctblength, ctblengthz, nmode=0, 
     if st:
         raise MskError(st, L.msk_status_string(st).decode())
     return pix
+
+
+def device_allocations():
+    """Device allocations libmsk has made in this process (msk_device_allocations)."""
+    return int(load().msk_device_allocations())
 
 
 # ------------------------------------------------------------------ context

@@ -8,7 +8,9 @@ reference's for the projected potential to match; this script only changes
 their layout into a C array initialiser.  Run it from a tree that has the
 reference sources:
 
-    python utr_public_gb300/csrc/gen_kirkland_fparams.py /root/reference
+    python utr_public_gb300/csrc/gen_kirkland_fparams.py <reference tree>
+
+(or with the tree in MSK_REFERENCE_TREE).
 """
 import os
 import re
@@ -44,4 +46,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    tree = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MSK_REFERENCE_TREE")
+    if not tree:
+        raise SystemExit("usage: gen_kirkland_fparams.py <reference tree>")
+    main(tree)

@@ -7,6 +7,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -18,26 +19,48 @@
 
 namespace msk {
 
-// A device allocation that only grows.
+// Device allocations made by the library in this process (every one goes
+// through DevBuf::reserve); msk_device_allocations() reports it.
+extern std::atomic<long long> g_device_allocs;
+// Set on a host thread while a call that must not allocate runs on it
+// (msk_calculate_static): a DevBuf that would have to grow fails instead.
+extern thread_local bool t_no_alloc;
+
+// A device allocation that only grows -- or, when `borrowed`, a view of
+// memory the library does not own (a region of a fixed array), which never
+// grows and is never freed.
 struct DevBuf {
     void *p = nullptr;
     size_t cap = 0;
+    bool borrowed = false;
     cudaError_t reserve(size_t bytes)
     {
         if (bytes <= cap) return cudaSuccess;
+        if (borrowed || t_no_alloc) return cudaErrorMemoryAllocation;
         if (p) cudaFree(p);
         p = nullptr;
         cap = 0;
         cudaError_t e = cudaMalloc(&p, bytes);
-        if (e == cudaSuccess) cap = bytes;
+        if (e == cudaSuccess) {
+            cap = bytes;
+            g_device_allocs.fetch_add(1, std::memory_order_relaxed);
+        }
         return e;
+    }
+    // a view of `bytes` bytes at `q`, owned elsewhere
+    void borrow(void *q, size_t bytes)
+    {
+        p = q;
+        cap = bytes;
+        borrowed = true;
     }
     template <typename T> T *as() const { return reinterpret_cast<T *>(p); }
     void release()
     {
-        if (p) cudaFree(p);
+        if (p && !borrowed) cudaFree(p);
         p = nullptr;
         cap = 0;
+        borrowed = false;
     }
 };
 

@@ -844,6 +844,9 @@ static void spherical_wave(int nx, int ny, float ctblength, float v0, double R1,
 using namespace msk;
 
 namespace msk {
+std::atomic<long long> g_device_allocs{0};
+thread_local bool t_no_alloc = false;
+
 const char *const kKindName[kKinds] = {
     "row_splat", "col_bandlimit", "row_transmit", "col_propagate", "col_fresnel",
     "row_intensity", "row_exit", "row_init", "plane_init", "fresnel_table",
@@ -3227,13 +3230,22 @@ static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
 
 namespace {
 
+// The array's device address per device, looked up on the first call that
+// succeeds on that device (a failed lookup is retried by the next call).
 struct StaticScratch {
-    std::once_flag once;
+    std::mutex m;
     void *ptr = nullptr;
-    cudaError_t err = cudaSuccess;
 };
 constexpr int kStaticDevices = 64;
 StaticScratch g_static[kStaticDevices];
+
+// Marks the calling host thread as one whose library calls must not allocate
+// device memory, for the guard's lifetime.
+struct NoAllocScope {
+    bool prev;
+    NoAllocScope() : prev(t_no_alloc) { t_no_alloc = true; }
+    ~NoAllocScope() { t_no_alloc = prev; }
+};
 
 // Bytes upload_tables() needs for this grid (its 256-byte aligned pieces).
 size_t static_table_bytes(int nx, int ny, int nz)
@@ -3270,20 +3282,31 @@ extern "C" int msk_calculate_static(void *stream, float *pix, const float *wave0
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kStaticDevices) return MSK_ECUDA;
     StaticScratch &sc = g_static[dev];
-    std::call_once(sc.once, [&] { sc.err = cudaGetSymbolAddress(&sc.ptr, g_static_scratch); });
-    if (sc.err != cudaSuccess || !sc.ptr) return MSK_ECUDA;
+    void *scratch = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(sc.m);
+        if (!sc.ptr) {
+            void *q = nullptr;
+            if (cudaGetSymbolAddress(&q, g_static_scratch) != cudaSuccess || !q) {
+                cudaGetLastError();  // not sticky: the next call tries again
+                return MSK_ECUDA;
+            }
+            sc.ptr = q;
+        }
+        scratch = sc.ptr;
+    }
 
-    // A context on the stack whose buffers are views of the scratch; with
-    // every view as large as the call needs, no reserve() below allocates.
+    // A context on the stack whose buffers are borrowed views of the scratch.
+    // A view never grows, and while this call runs no other buffer of this
+    // thread may allocate either: a size beyond a view fails the call
+    // (MSK_ENOMEM) instead of calling cudaMalloc.
+    NoAllocScope no_alloc;
     msk_context ctx;
     ctx.device = dev;
     ctx.stream = (cudaStream_t)stream;
     ctx.no_tune = true;  // the tuner would allocate: the default column tiles
-    unsigned char *base = static_cast<unsigned char *>(sc.ptr);
-    auto view = [&](DevBuf &b, size_t off, size_t bytes) {
-        b.p = base + off;
-        b.cap = bytes;
-    };
+    unsigned char *base = static_cast<unsigned char *>(scratch);
+    auto view = [&](DevBuf &b, size_t off, size_t bytes) { b.borrow(base + off, bytes); };
     view(ctx.psi, kOffPsi, kSGrid);
     view(ctx.tbuf, kOffTbuf, kSGrid);
     view(ctx.wave0, kOffWave0, kSGrid);
@@ -3345,6 +3368,11 @@ extern "C" int msk_calculate_static(void *stream, float *pix, const float *wave0
                         ctx.stream) != cudaSuccess)
         return MSK_ECUDA;
     return flags_check(&ctx);
+}
+
+extern "C" long long msk_device_allocations(void)
+{
+    return g_device_allocs.load(std::memory_order_relaxed);
 }
 
 // ------------------------------------------------------------------ per-orientation form
