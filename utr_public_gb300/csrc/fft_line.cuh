@@ -40,16 +40,6 @@ __device__ __forceinline__ float2 cmul_conj(float2 a, float2 b)  // a * conj(b)
 }
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 
-// cos / sin of 2*pi*k/32, k < 16 (only these occur in a radix-2 DIT of size <= 32)
-__device__ constexpr float kTwC[16] = {1.0f, 0.98078528f, 0.923879533f, 0.831469612f,
-                                       0.707106781f, 0.555570233f, 0.382683432f, 0.195090322f,
-                                       0.0f, -0.195090322f, -0.382683432f, -0.555570233f,
-                                       -0.707106781f, -0.831469612f, -0.923879533f, -0.98078528f};
-__device__ constexpr float kTwS[16] = {0.0f, 0.195090322f, 0.382683432f, 0.555570233f,
-                                       0.707106781f, 0.831469612f, 0.923879533f, 0.98078528f,
-                                       1.0f, 0.98078528f, 0.923879533f, 0.831469612f,
-                                       0.707106781f, 0.555570233f, 0.382683432f, 0.195090322f};
-
 __host__ __device__ constexpr int ilog2(int n)
 {
     int b = 0;
@@ -63,45 +53,77 @@ __host__ __device__ __forceinline__ constexpr int brev(int x, int bits)
     return r;
 }
 
-// b * exp(+-2 pi i k/32), k < 16 known at compile time
-template <int K, bool INV>
-__device__ __forceinline__ float2 twc(float2 b)
+// cos(pi k/16), k = 0..16, to 20 significant digits (exact mathematical values:
+// cos(pi/16), cos(pi/8) = sqrt(2 + sqrt 2)/2, cos(3 pi/16), sqrt(1/2), ...).
+__host__ __device__ constexpr double cos16(int k)
 {
+    constexpr double c[9] = {1.0,
+                             0.98078528040323044913,
+                             0.92387953251128675613,
+                             0.83146961230254523708,
+                             0.70710678118654752440,
+                             0.55557023301960222474,
+                             0.38268343236508977173,
+                             0.19509032201612826785,
+                             0.0};
+    return k <= 8 ? c[k] : -c[16 - k];
+}
+__host__ __device__ constexpr double sin16(int k) { return k <= 8 ? cos16(8 - k) : cos16(k - 8); }
+__host__ __device__ constexpr double dabs(double x) { return x < 0 ? -x : x; }
+
+// The radix-2 butterfly (a, b) -> (a + w b, a - w b) with the twiddle
+// w = exp(+-2 pi i K/32) = c + i s (K < 16 known at compile time) folded into
+// fused multiply-adds (the tangent form of the FMA-optimised FFT, Linzer and
+// Feig 1993 / Goedecker 1997): with |c| >= |s|, w b = c (b + i (s/c) b); else
+// w b = s ((c/s) b + i b).  Two FMAs form the bracket and four apply the common
+// factor with the sums: 6 operations against the 8 of a complex multiply
+// followed by two complex additions.  K = 0 and K = 8 (w = +-i) take 4 adds.
+template <int K, bool INV>
+__host__ __device__ __forceinline__ void bfly(float2 &a, float2 &b)
+{
+    const float2 u = a;
     if constexpr (K == 0) {
-        return b;
+        a = make_float2(u.x + b.x, u.y + b.y);
+        b = make_float2(u.x - b.x, u.y - b.y);
     } else if constexpr (K == 8) {
-        return INV ? make_float2(b.y, -b.x) : make_float2(-b.y, b.x);
+        // w b = (-b.y, b.x) forward, (b.y, -b.x) inverse
+        const float2 wb = INV ? make_float2(b.y, -b.x) : make_float2(-b.y, b.x);
+        a = make_float2(u.x + wb.x, u.y + wb.y);
+        b = make_float2(u.x - wb.x, u.y - wb.y);
     } else {
-        constexpr float c = kTwC[K];
-        constexpr float s = INV ? -kTwS[K] : kTwS[K];
-        return make_float2(b.x * c - b.y * s, b.x * s + b.y * c);
+        constexpr double c = cos16(K), s = INV ? -sin16(K) : sin16(K);
+        constexpr bool TAN = dabs(c) >= dabs(s);
+        constexpr float r = (float)(TAN ? s / c : c / s);  // tan or cot of the angle
+        constexpr float m = (float)(TAN ? c : s);
+        float2 t;
+        if constexpr (TAN) t = make_float2(fmaf(-r, b.y, b.x), fmaf(r, b.x, b.y));
+        else t = make_float2(fmaf(r, b.x, -b.y), fmaf(r, b.y, b.x));
+        a = make_float2(fmaf(m, t.x, u.x), fmaf(m, t.y, u.y));
+        b = make_float2(fmaf(-m, t.x, u.x), fmaf(-m, t.y, u.y));
     }
 }
 
 // In-register DFT of R points v[0], v[S], ..., v[(R-1)*S], natural order in
 // and out.  Radix-2 decimation in time, all indices compile-time.
 template <int R, bool INV, int S, int LEN = 2>
-__device__ __forceinline__ void dft_levels(float2 *a)
+__host__ __device__ __forceinline__ void dft_levels(float2 *a)
 {
     if constexpr (LEN <= R) {
 #pragma unroll
         for (int i = 0; i < R; i += LEN) {
 #pragma unroll
             for (int j = 0; j < LEN / 2; j++) {
-                // twiddle exp(+-2 pi i j/LEN) = kTw[j * 32/LEN]
-                float2 u = a[i + j];
-                float2 w;
+                // twiddle exp(+-2 pi i j/LEN) = exp(+-2 pi i K/32), K = j * 32/LEN
+                float2 &x = a[i + j], &y = a[i + j + LEN / 2];
                 switch (j * (32 / LEN)) {
-#define MSK_TWCASE(K) case K: w = twc<K, INV>(a[i + j + LEN / 2]); break;
-                    MSK_TWCASE(0) MSK_TWCASE(1) MSK_TWCASE(2) MSK_TWCASE(3)
-                    MSK_TWCASE(4) MSK_TWCASE(5) MSK_TWCASE(6) MSK_TWCASE(7)
-                    MSK_TWCASE(8) MSK_TWCASE(9) MSK_TWCASE(10) MSK_TWCASE(11)
-                    MSK_TWCASE(12) MSK_TWCASE(13) MSK_TWCASE(14) MSK_TWCASE(15)
-#undef MSK_TWCASE
-                    default: w = a[i + j + LEN / 2]; break;
+#define MSK_BFCASE(K) case K: bfly<K, INV>(x, y); break;
+                    MSK_BFCASE(0) MSK_BFCASE(1) MSK_BFCASE(2) MSK_BFCASE(3)
+                    MSK_BFCASE(4) MSK_BFCASE(5) MSK_BFCASE(6) MSK_BFCASE(7)
+                    MSK_BFCASE(8) MSK_BFCASE(9) MSK_BFCASE(10) MSK_BFCASE(11)
+                    MSK_BFCASE(12) MSK_BFCASE(13) MSK_BFCASE(14) MSK_BFCASE(15)
+#undef MSK_BFCASE
+                    default: break;
                 }
-                a[i + j] = cadd(u, w);
-                a[i + j + LEN / 2] = csub(u, w);
             }
         }
         dft_levels<R, INV, S, LEN * 2>(a);
@@ -109,7 +131,7 @@ __device__ __forceinline__ void dft_levels(float2 *a)
 }
 
 template <int R, bool INV, int S>
-__device__ __forceinline__ void dft(float2 *v)
+__host__ __device__ __forceinline__ void dft(float2 *v)
 {
     static_assert(R >= 1 && R <= 32 && (R & (R - 1)) == 0, "radix");
     if constexpr (R == 1) return;
@@ -168,18 +190,23 @@ __device__ __forceinline__ void fft_stage(float2 (&v)[FftPlan<N>::E], float2 *bu
         for (int r = 0; r < R; r++) v[k + r * KB] = buf[pidx<N>(b + r * (N / R)) * C + c];
     }
     if constexpr (!LAST) group_sync<BLOCK>();
+    const float4 *tw4 = reinterpret_cast<const float4 *>(tw);
 #pragma unroll
     for (int k = 0; k < KB; k++) {
         const int b = t + k * T;
         const int j = b % NS;
-        // twiddles in groups of 8: the empty asm keeps the compiler from
-        // hoisting all R-1 loads (2 registers each) ahead of the multiplies
+        // twiddles of r = 2p+1 and 2p+2 in one 16-byte load, in groups of four
+        // loads: the empty asm keeps the compiler from hoisting all of them
+        // (4 registers each) ahead of the multiplies
 #pragma unroll
-        for (int r0 = 1; r0 < R; r0 += 8) {
+        for (int p0 = 0; p0 < R / 2; p0 += 4) {
 #pragma unroll
-            for (int r = r0; r < r0 + 8 && r < R; r++) {
-                const float2 w = __ldg(&tw[r * NS + j]);
-                v[k + r * KB] = INV ? cmul_conj(v[k + r * KB], w) : cmul(v[k + r * KB], w);
+            for (int p = p0; p < p0 + 4 && p < R / 2; p++) {
+                const float4 w2 = __ldg(&tw4[p * NS + j]);
+                const int r1 = 2 * p + 1, r2 = 2 * p + 2;
+                const float2 w = make_float2(w2.x, w2.y), w_ = make_float2(w2.z, w2.w);
+                v[k + r1 * KB] = INV ? cmul_conj(v[k + r1 * KB], w) : cmul(v[k + r1 * KB], w);
+                if (r2 < R) v[k + r2 * KB] = INV ? cmul_conj(v[k + r2 * KB], w_) : cmul(v[k + r2 * KB], w_);
             }
             asm volatile("" ::: "memory");
         }
@@ -202,7 +229,8 @@ __device__ __forceinline__ void fft_stage(float2 (&v)[FftPlan<N>::E], float2 *bu
 //   buf: the line group's shared buffer (C interleaved lines, padded)
 //   c:   this thread's line within the group; t: index within the line
 //   tw:  FftPlan<N>::TWN twiddles in global memory (stage 2 table, then
-//        stage 3 table), read through the L1 cache
+//        stage 3 table; each in pairs, see the host's twiddle tables), read
+//        through the L1 cache; 16-byte aligned
 // Every thread of the group must call it (it contains group barriers).
 template <int N, bool INV, int C, bool BLOCK>
 __device__ __forceinline__ void fft_line(float2 (&v)[FftPlan<N>::E], float2 *buf, int c, int t,

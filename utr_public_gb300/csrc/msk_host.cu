@@ -593,18 +593,23 @@ static bool grid_pre(GridPre &gp, int nx, int ny, float ax, float by, float v0, 
     return true;
 }
 
-// Stockham stage twiddles for line length n, matching FftPlan<n>.
+// Stockham stage twiddles for line length n, matching FftPlan<n>: per stage
+// of radix R entered by sub-transforms of size NS, w(r, j) = exp(2 pi i r j /
+// (NS R)) for r = 1..R-1, stored in pairs -- float2 index 2 (p NS + j) + q
+// holds w(2p + 1 + q, j), so one 16-byte load fetches the twiddles of r = 2p+1
+// and 2p+2 (the pair of r = R-1 is padded with 1).  Computed in double.
 template <int N>
 static void twiddles_n(std::vector<float2> &out)
 {
     using P = FftPlan<N>;
-    out.assign(std::max(P::TWN, 1), make_float2(1.0f, 0.0f));
+    out.assign(std::max(P::TWN, 2), make_float2(1.0f, 0.0f));
     const double twopi = 8.0 * atan(1.0);
     auto fill = [&](int off, int ns, int r_) {
-        for (int r = 0; r < r_; r++)
+        for (int r = 1; r < r_; r++)
             for (int j = 0; j < ns; j++) {
                 const double a = twopi * (double)r * (double)j / (double)(ns * r_);
-                out[off + r * ns + j] = make_float2((float)cos(a), (float)sin(a));
+                const int pr = (r - 1) / 2, q = (r - 1) % 2;
+                out[off + 2 * (pr * ns + j) + q] = make_float2((float)cos(a), (float)sin(a));
             }
     };
     if (P::S >= 2) fill(0, P::NS2, P::R2);

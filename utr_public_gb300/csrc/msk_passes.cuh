@@ -33,6 +33,7 @@
 
 #include "fft_line.cuh"
 #include "msk_types.h"
+#include "sincos_poly.cuh"
 #include "tma.cuh"
 
 namespace msk {
@@ -86,10 +87,12 @@ __device__ __forceinline__ void store_band_rows(const Geom &g, float2 *rows_smem
     }
 }
 
-// exp(i*ph), kept out of line: 32 inlined sincosf bodies per thread (with
-// their large-argument paths) overflow the instruction cache of the splat
+// exp(i*ph) by the polynomial form of sincos_poly.cuh (the library's sincosf
+// beyond its range), kept out of line: 32 inlined bodies per thread would
+// overflow the instruction cache of the splat
 static __device__ __noinline__ float2 expi(float ph)
 {
+    if (fabsf(ph) <= kExpiMax) return expi_poly(ph);
     float s, c;
     sincosf(ph, &s, &c);
     return make_float2(c, s);
@@ -100,7 +103,13 @@ static __device__ __noinline__ float2 expi(float ph)
 static __device__ __noinline__ float2 expm1i(float ph)
 {
     float s, c;
-    sincosf(0.5f * ph, &s, &c);
+    if (fabsf(0.5f * ph) <= kExpiMax) {
+        const float2 e = expi_poly(0.5f * ph);
+        c = e.x;
+        s = e.y;
+    } else {
+        sincosf(0.5f * ph, &s, &c);
+    }
     return make_float2(-2.0f * s * s, 2.0f * s * c);
 }
 
