@@ -175,13 +175,43 @@ __device__ __forceinline__ void group_sync()
     else __syncwarp();
 }
 
+// Stage twiddles are fetched in groups of kTwG 16-byte loads (two twiddles
+// each), one group ahead of the multiplies that use it: the first group of
+// stage 2 is requested before stage 1's register DFT, and every later group
+// while the previous one is being applied, so the L1 latency of a load hides
+// behind arithmetic instead of stalling the warp.
+constexpr int kTwG = 4;
+
+template <int N, int R, int NS>
+struct StageTw {
+    static constexpr int E = FftPlan<N>::E, T = FftPlan<N>::T, KB = E / R;
+    static constexpr int NP = R / 2;                    // twiddle pairs per sub-transform
+    static constexpr int GPK = (NP + kTwG - 1) / kTwG;  // load groups per sub-transform
+    static constexpr int NG = KB * GPK;                 // load groups in the stage
+};
+
+// Group gi (compile-time once unrolled) of a stage's twiddles into w.
+template <int N, int R, int NS>
+__device__ __forceinline__ void tw_fetch(float4 (&w)[kTwG], const float2 *tw, int t, int gi)
+{
+    using S = StageTw<N, R, NS>;
+    const int k = gi / S::GPK, p0 = (gi % S::GPK) * kTwG;
+    const int j = (t + k * S::T) % NS;
+    const float4 *tw4 = reinterpret_cast<const float4 *>(tw);
+#pragma unroll
+    for (int q = 0; q < kTwG; q++)
+        if (p0 + q < S::NP) w[q] = __ldg(&tw4[(p0 + q) * NS + j]);
+}
+
 // One middle/last Stockham stage.  Reads the line from shared memory into
 // registers (all reads before any write), twiddles, radix-R DFT; a middle
 // stage writes back, the last stage leaves the result in strided order.
+// `pre` holds the stage's first twiddle group, fetched by the caller.
 template <int N, int R, int NS, bool LAST, bool INV, int C, bool BLOCK>
 __device__ __forceinline__ void fft_stage(float2 (&v)[FftPlan<N>::E], float2 *buf, int c, int t,
-                                          const float2 *tw)
+                                          const float2 *tw, const float4 (&pre)[kTwG])
 {
+    using S = StageTw<N, R, NS>;
     constexpr int E = FftPlan<N>::E, T = FftPlan<N>::T, KB = E / R;
 #pragma unroll
     for (int k = 0; k < KB; k++) {
@@ -190,27 +220,29 @@ __device__ __forceinline__ void fft_stage(float2 (&v)[FftPlan<N>::E], float2 *bu
         for (int r = 0; r < R; r++) v[k + r * KB] = buf[pidx<N>(b + r * (N / R)) * C + c];
     }
     if constexpr (!LAST) group_sync<BLOCK>();
-    const float4 *tw4 = reinterpret_cast<const float4 *>(tw);
+    float4 cur[kTwG], nxt[kTwG];
 #pragma unroll
-    for (int k = 0; k < KB; k++) {
-        const int b = t + k * T;
-        const int j = b % NS;
-        // twiddles of r = 2p+1 and 2p+2 in one 16-byte load, in groups of four
-        // loads: the empty asm keeps the compiler from hoisting all of them
-        // (4 registers each) ahead of the multiplies
+    for (int q = 0; q < kTwG; q++) cur[q] = pre[q];
 #pragma unroll
-        for (int p0 = 0; p0 < R / 2; p0 += 4) {
+    for (int gi = 0; gi < S::NG; gi++) {
+        if (gi + 1 < S::NG) tw_fetch<N, R, NS>(nxt, tw, t, gi + 1);
+        const int k = gi / S::GPK, p0 = (gi % S::GPK) * kTwG;
 #pragma unroll
-            for (int p = p0; p < p0 + 4 && p < R / 2; p++) {
-                const float4 w2 = __ldg(&tw4[p * NS + j]);
+        for (int q = 0; q < kTwG; q++) {
+            const int p = p0 + q;
+            if (p < S::NP) {
                 const int r1 = 2 * p + 1, r2 = 2 * p + 2;
-                const float2 w = make_float2(w2.x, w2.y), w_ = make_float2(w2.z, w2.w);
+                const float2 w = make_float2(cur[q].x, cur[q].y), w_ = make_float2(cur[q].z, cur[q].w);
                 v[k + r1 * KB] = INV ? cmul_conj(v[k + r1 * KB], w) : cmul(v[k + r1 * KB], w);
-                if (r2 < R) v[k + r2 * KB] = INV ? cmul_conj(v[k + r2 * KB], w_) : cmul(v[k + r2 * KB], w_);
+                if (r2 < R)
+                    v[k + r2 * KB] = INV ? cmul_conj(v[k + r2 * KB], w_) : cmul(v[k + r2 * KB], w_);
             }
-            asm volatile("" ::: "memory");
         }
-        dft<R, INV, KB>(&v[k]);
+        if (gi % S::GPK == S::GPK - 1) dft<R, INV, KB>(&v[k]);
+        // keeps the compiler from hoisting later groups' loads (4 registers each)
+        asm volatile("" ::: "memory");
+#pragma unroll
+        for (int q = 0; q < kTwG; q++) cur[q] = nxt[q];
     }
     if constexpr (!LAST) {
 #pragma unroll
@@ -238,6 +270,8 @@ __device__ __forceinline__ void fft_line(float2 (&v)[FftPlan<N>::E], float2 *buf
 {
     using P = FftPlan<N>;
     constexpr int E = P::E;
+    float4 pre2[kTwG];
+    if constexpr (P::S >= 2) tw_fetch<N, P::R2, P::NS2>(pre2, tw, t, 0);
     dft<E, INV, 1>(v);
     if constexpr (P::S >= 2) {
         group_sync<BLOCK>();  // earlier readers of buf are done
@@ -245,10 +279,12 @@ __device__ __forceinline__ void fft_line(float2 (&v)[FftPlan<N>::E], float2 *buf
         for (int r = 0; r < E; r++) buf[pidx<N>(t * E + r) * C + c] = v[r];
         group_sync<BLOCK>();
         if constexpr (P::S == 2) {
-            fft_stage<N, P::R2, P::NS2, true, INV, C, BLOCK>(v, buf, c, t, tw);
+            fft_stage<N, P::R2, P::NS2, true, INV, C, BLOCK>(v, buf, c, t, tw, pre2);
         } else {
-            fft_stage<N, P::R2, P::NS2, false, INV, C, BLOCK>(v, buf, c, t, tw);
-            fft_stage<N, P::R3, P::NS3, true, INV, C, BLOCK>(v, buf, c, t, tw + P::TW2);
+            float4 pre3[kTwG];
+            tw_fetch<N, P::R3, P::NS3>(pre3, tw + P::TW2, t, 0);
+            fft_stage<N, P::R2, P::NS2, false, INV, C, BLOCK>(v, buf, c, t, tw, pre2);
+            fft_stage<N, P::R3, P::NS3, true, INV, C, BLOCK>(v, buf, c, t, tw + P::TW2, pre3);
         }
     }
 }

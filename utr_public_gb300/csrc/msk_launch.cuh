@@ -84,8 +84,8 @@ const SizeOps *size_ops(int n);
 template <int N> struct Smem {
     using P = FftPlan<N>;
     static constexpr int NTS = RowCfg<N>::L * P::T;
-    static constexpr size_t splat = (size_t)RowCfg<N>::L * P::PADN * 8 + NTS * 16 + 128 * 4 +
-                                    ((NTS + 31) / 32 + 1) * 4;
+    static constexpr size_t splat = (size_t)RowCfg<N>::L * SplatCfg<N>::SROW * 8 + NTS * 16 +
+                                    128 * 4 + ((NTS + 31) / 32 + 1) * 4;
     template <int V> static constexpr size_t col() { return (size_t)ColCfg<N, V>::C * P::PADN * 8 + 16; }
     static constexpr size_t transmit = (size_t)2 * RowCfg<N>::LT * P::PADN * 8 + 16;
     static constexpr size_t row = (size_t)RowCfg<N>::L * P::PADN * 8;

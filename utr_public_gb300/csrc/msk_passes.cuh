@@ -204,18 +204,98 @@ __device__ __forceinline__ float spline_vz(const Geom &g, const float *knots, co
 }
 
 // ---------------------------------------------------------------- P1
-// One CTA = L rows of one unit.  Atoms of the (unit, slice) whose window
-// touches these rows are staged into shared memory in slice order (ordered
-// block compaction), then every thread adds the potential of each staged
-// atom to the pixels it owns (iy = t mod T of its row) -- a gather with a
-// fixed pixel owner, so the sum order per pixel is the atom order and the
-// result is deterministic, with no atomics (autoslic.cpp:950-984 is a racy
-// scatter in the reference).  Then t = exp(i sigma v) and the row FFT.
+// One CTA = L rows of one unit.  Every thread adds the potential of each atom
+// of the (unit, slice) whose window touches its row to the pixels it owns
+// (iy = t mod T of its row) -- a gather with a fixed pixel owner, so the sum
+// order per pixel is the atom order and the result is deterministic, with no
+// atomics (autoslic.cpp:950-984 is a racy scatter in the reference).  Then
+// t = exp(i sigma v) and the row FFT.
+//   Lines of <= 32 threads (NY <= 1024): every warp owns RW = 32/T whole rows
+//   and works alone -- it scans the slice's atom list 32 at a time, a ballot
+//   picks the atoms whose window touches its rows, each is broadcast by
+//   shuffles -- and stores its own rows, so no row waits for another.
+//   Longer lines (a row spans several warps): the atoms touching the CTA's
+//   rows are staged into shared memory in slice order (ordered block
+//   compaction) and every row's threads loop over them.
 // MODE kSplatTrans: A = S(exp(i sigma v)), in-band row segments to tbuf
 //      kSplatPot:   v itself (float) to vout + u * vstride
 //      kSplatSpec:  S(v) (v as a complex field), whole rows to tbuf (the
 //                   Debye-Waller branch filters it before the phase)
 enum { kSplatTrans = 0, kSplatPot = 1, kSplatSpec = 2 };
+
+// Per-row shared-memory stride of the splat (float2 units): the padded line,
+// rounded to an even count so every row starts 16-byte aligned (bulk copies).
+template <int NY> struct SplatCfg {
+    static constexpr int SROW = (FftPlan<NY>::PADN + 1) & ~1;
+};
+
+// The potential of atom `sa` at this thread's pixels of row ix.
+__device__ __forceinline__ void splat_atom(const Geom &g, const SplatAtom &sa, int ix, int t,
+                                           int T, int NY, int W, float *vacc, const float *s_knots)
+{
+    const int nx = g.nx;
+    const int ixo = (int)(sa.meta & kMetaMask);
+    const int iyo = (int)((sa.meta >> kMetaBits) & kMetaMask);
+    const float4 *coef = g.coef + (sa.meta >> (2 * kMetaBits)) * kKnots;
+    const int ws = ixo - g.idx;
+    for (int ixp = ws + pmod(ix - ws, nx); ixp < ws + W; ixp += nx) {
+        const float dx = sa.fx - (float)(ixp - ixo) * g.scalex_f;
+        const float dx2 = dx * dx;
+        const int ys = iyo - g.idy;
+        for (int iyp = ys + pmod(t - ys, T); iyp <= iyo + g.idy; iyp += T) {
+            const float dy = sa.fy - (float)(iyp - iyo) * g.scaley_f;
+            float rsq = dx2 + dy * dy;
+            if (rsq <= 9.0f) {
+                rsq = fmaxf(rsq, g.rminsq);
+                vacc[pmod(iyp, NY)] += sa.occ * spline_vz(g, s_knots, coef, rsq);
+            }
+        }
+    }
+}
+
+// This warp's `rows` dense rows (row r at rows_smem + r * stride, 16-byte
+// aligned) as their in-band segments [0, seg_e1) and [seg_s2, NY), the (at
+// most two) out-of-band elements inside the segments zeroed first; lane 0
+// issues the bulk copies and waits until they have read shared memory.
+template <int NY>
+__device__ __forceinline__ void warp_store_band_rows(const Geom &g, float2 *rows_smem, int stride,
+                                                     int rows, float2 *dst)
+{
+    const int e1 = g.seg_e1, s2 = g.seg_s2, lane = threadIdx.x & 31;
+    __syncwarp();  // every element written before the fix-up
+    for (int q = lane; q < 2 * rows; q += 32) {
+        const int r = q >> 1;
+        const int iy = (q & 1) ? s2 : e1 - 1;
+        if (iy >= 0 && iy < NY && out_of_band(g, iy)) rows_smem[r * stride + iy] = make_float2(0.0f, 0.0f);
+    }
+    fence_proxy_async();
+    __syncwarp();
+    if (lane == 0 && rows > 0) {
+        for (int r = 0; r < rows; r++) {
+            bulk_store(dst + (size_t)r * NY, rows_smem + r * stride, (uint32_t)e1 * 8u);
+            if (s2 < NY)
+                bulk_store(dst + (size_t)r * NY + s2, rows_smem + r * stride + s2, (uint32_t)(NY - s2) * 8u);
+        }
+        bulk_commit();
+        bulk_wait_read();
+    }
+    __syncwarp();
+}
+
+// The same for whole rows.
+template <int NY>
+__device__ __forceinline__ void warp_store_rows(float2 *rows_smem, int stride, int rows, float2 *dst)
+{
+    fence_proxy_async();
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0 && rows > 0) {
+        for (int r = 0; r < rows; r++)
+            bulk_store(dst + (size_t)r * NY, rows_smem + r * stride, (uint32_t)NY * 8u);
+        bulk_commit();
+        bulk_wait_read();
+    }
+    __syncwarp();
+}
 
 template <int NY, int MODE>
 __global__ void __launch_bounds__(RowCfg<NY>::L * FftPlan<NY>::T)
@@ -225,10 +305,12 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
 {
     using P = FftPlan<NY>;
     constexpr int T = P::T, E = P::E, L = RowCfg<NY>::L, NT = L * T, NW = (NT + 31) / 32;
+    constexpr int SROW = SplatCfg<NY>::SROW;
     constexpr bool BLK = RowCfg<NY>::BLK;
+    constexpr int RW = BLK ? 1 : 32 / T;  // rows per warp (lines of <= 32 threads)
     extern __shared__ __align__(128) unsigned char smem[];
     float2 *s_lines = reinterpret_cast<float2 *>(smem);
-    SplatAtom *s_atoms = reinterpret_cast<SplatAtom *>(s_lines + L * P::PADN);
+    SplatAtom *s_atoms = reinterpret_cast<SplatAtom *>(s_lines + L * SROW);
     float *s_knots = reinterpret_cast<float *>(s_atoms + NT);
     int *s_cnt = reinterpret_cast<int *>(s_knots + 128);
 
@@ -239,68 +321,78 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
     const int ix0 = (blockIdx.x % bpu) * L;
     const int ix = ix0 + l;
     const bool row_ok = ix < nx;
+    const int lane = tid & 31, warp = tid >> 5;
 
     for (int i = tid; i < kKnots; i += NT) s_knots[i] = g.knots[i];
-    float *vacc = reinterpret_cast<float *>(s_lines + l * P::PADN);
+    float *vacc = reinterpret_cast<float *>(s_lines + l * SROW);
 #pragma unroll
     for (int m = 0; m < E; m++) vacc[t + m * T] = 0.0f;
     __syncthreads();
 
     const int a0 = slice_off[u * nsl1 + slice], a1 = slice_off[u * nsl1 + slice + 1];
     const int W = 2 * g.idx + 1;
-    const int lane = tid & 31, warp = tid >> 5;
-    for (int base = a0; base < a1; base += NT) {
-        const int a = base + tid;
-        bool hit = false;
-        SplatAtom at;
-        if (a < a1) {
-            at = atoms[a];
-            const int ixo = (int)(at.meta & kMetaMask);
-            const int rel = pmod(ixo - g.idx - ix0, nx);
-            hit = (W >= nx) || (rel < L) || (rel + W > nx);
+    if constexpr (!BLK) {
+        const int wx0 = ix0 + warp * RW;  // this warp's first row
+        for (int base = a0; base < a1; base += 32) {
+            const int a = base + lane;
+            bool hit = false;
+            SplatAtom at = {};
+            if (a < a1) {
+                at = atoms[a];
+                const int ixo = (int)(at.meta & kMetaMask);
+                const int rel = pmod(ixo - g.idx - wx0, nx);
+                hit = (W >= nx) || (rel < RW) || (rel + W > nx);
+            }
+            unsigned bal = __ballot_sync(0xffffffffu, hit);
+            while (bal) {  // in atom order: the per-pixel sums keep the slice order
+                const int k = __ffs(bal) - 1;
+                bal &= bal - 1;
+                SplatAtom sa;
+                sa.fx = __shfl_sync(0xffffffffu, at.fx, k);
+                sa.fy = __shfl_sync(0xffffffffu, at.fy, k);
+                sa.occ = __shfl_sync(0xffffffffu, at.occ, k);
+                sa.meta = __shfl_sync(0xffffffffu, at.meta, k);
+                if (row_ok) splat_atom(g, sa, ix, t, T, NY, W, vacc, s_knots);
+            }
         }
-        const unsigned bal = __ballot_sync(0xffffffffu, hit);
-        if (lane == 0) s_cnt[warp] = __popc(bal);
-        __syncthreads();
-        if (warp == 0) {
-            int c = lane < NW ? s_cnt[lane] : 0;
-            int incl = c;
+        __syncwarp();
+    } else {
+        for (int base = a0; base < a1; base += NT) {
+            const int a = base + tid;
+            bool hit = false;
+            SplatAtom at;
+            if (a < a1) {
+                at = atoms[a];
+                const int ixo = (int)(at.meta & kMetaMask);
+                const int rel = pmod(ixo - g.idx - ix0, nx);
+                hit = (W >= nx) || (rel < L) || (rel + W > nx);
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, hit);
+            if (lane == 0) s_cnt[warp] = __popc(bal);
+            __syncthreads();
+            if (warp == 0) {
+                int c = lane < NW ? s_cnt[lane] : 0;
+                int incl = c;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                int y = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += y;
-            }
-            if (lane < NW) s_cnt[lane] = incl - c;
-            if (lane == 31) s_cnt[NW] = incl;
-        }
-        __syncthreads();
-        if (hit) s_atoms[s_cnt[warp] + __popc(bal & ((1u << lane) - 1u))] = at;
-        const int nsel = s_cnt[NW];
-        __syncthreads();
-        if (row_ok) {
-            for (int k = 0; k < nsel; k++) {
-                const SplatAtom sa = s_atoms[k];
-                const int ixo = (int)(sa.meta & kMetaMask);
-                const int iyo = (int)((sa.meta >> kMetaBits) & kMetaMask);
-                const float4 *coef = g.coef + (sa.meta >> (2 * kMetaBits)) * kKnots;
-                const int ws = ixo - g.idx;
-                for (int ixp = ws + pmod(ix - ws, nx); ixp < ws + W; ixp += nx) {
-                    const float dx = sa.fx - (float)(ixp - ixo) * g.scalex_f;
-                    const float dx2 = dx * dx;
-                    const int ys = iyo - g.idy;
-                    for (int iyp = ys + pmod(t - ys, T); iyp <= iyo + g.idy; iyp += T) {
-                        const float dy = sa.fy - (float)(iyp - iyo) * g.scaley_f;
-                        float rsq = dx2 + dy * dy;
-                        if (rsq <= 9.0f) {
-                            rsq = fmaxf(rsq, g.rminsq);
-                            vacc[pmod(iyp, NY)] += sa.occ * spline_vz(g, s_knots, coef, rsq);
-                        }
-                    }
+                for (int o = 1; o < 32; o <<= 1) {
+                    int y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += y;
                 }
+                if (lane < NW) s_cnt[lane] = incl - c;
+                if (lane == 31) s_cnt[NW] = incl;
             }
+            __syncthreads();
+            if (hit) s_atoms[s_cnt[warp] + __popc(bal & ((1u << lane) - 1u))] = at;
+            const int nsel = s_cnt[NW];
+            __syncthreads();
+            if (row_ok)
+                for (int k = 0; k < nsel; k++) splat_atom(g, s_atoms[k], ix, t, T, NY, W, vacc, s_knots);
+            __syncthreads();
         }
-        __syncthreads();
     }
+    // rows of this warp (lines <= 32 threads) or of the CTA that exist
+    const int wrow0 = BLK ? 0 : warp * RW;
+    const int wrows = BLK ? min(L, nx - ix0) : min(RW, nx - ix0 - wrow0);
     if constexpr (MODE == kSplatPot) {
         // the projected potential itself: vout -> slice `slice` of unit 0
         if (row_ok) {
@@ -317,24 +409,31 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
             nz |= v[m].x != 0.0f;
         }
         if (!group_none<BLK>(nz))  // S(0) = 0: rows without atoms skip the transform
-            fft_line<NY, false, 1, BLK>(v, s_lines + l * P::PADN, 0, t, g.tw_row);
-        __syncthreads();
+            fft_line<NY, false, 1, BLK>(v, s_lines + l * SROW, 0, t, g.tw_row);
+        if constexpr (BLK) {
+            __syncthreads();
 #pragma unroll
-        for (int m = 0; m < E; m++) s_lines[l * NY + t + m * T] = v[m];
-        fence_proxy_async();
-        __syncthreads();
-        if (tid == 0) {
-            bulk_store(tbuf + ((size_t)u * nx + ix0) * NY, s_lines,
-                       (uint32_t)min(L, nx - ix0) * NY * 8u);
-            bulk_commit();
-            bulk_wait_read();
+            for (int m = 0; m < E; m++) s_lines[l * NY + t + m * T] = v[m];
+            fence_proxy_async();
+            __syncthreads();
+            if (tid == 0) {
+                bulk_store(tbuf + ((size_t)u * nx + ix0) * NY, s_lines, (uint32_t)wrows * NY * 8u);
+                bulk_commit();
+                bulk_wait_read();
+            }
+        } else {
+            __syncwarp();  // the row's reads of its region are done
+#pragma unroll
+            for (int m = 0; m < E; m++) s_lines[l * SROW + t + m * T] = v[m];
+            warp_store_rows<NY>(s_lines + wrow0 * SROW, SROW, wrows,
+                                tbuf + ((size_t)u * nx + ix0 + wrow0) * NY);
         }
     } else {
         float2 v[E];
         bool nz = false;
 #pragma unroll
         for (int m = 0; m < E; m++) {
-            // most of a slice is empty: exp(i*0) = 1 exactly, as sincosf(0) gives
+            // most of a slice is empty: exp(i*0) = 1 exactly
             const float ph = vacc[t + m * T] * g.sigma_f;
             v[m] = make_float2(1.0f, 0.0f);
             nz |= ph != 0.0f;
@@ -347,14 +446,22 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
             for (int m = 0; m < E; m++)
                 v[m] = make_float2(m == 0 && t == 0 ? (float)NY : 0.0f, 0.0f);
         } else {
-            fft_line<NY, false, 1, BLK>(v, s_lines + l * P::PADN, 0, t, g.tw_row);
+            fft_line<NY, false, 1, BLK>(v, s_lines + l * SROW, 0, t, g.tw_row);
         }
         // dense rows into shared memory, then their in-band segments to the
         // buffer (its out-of-band columns hold zeros: the band limit zeroes them)
-        __syncthreads();
+        if constexpr (BLK) {
+            __syncthreads();
 #pragma unroll
-        for (int m = 0; m < E; m++) s_lines[l * NY + t + m * T] = v[m];
-        store_band_rows<NY>(g, s_lines, min(L, nx - ix0), tbuf + ((size_t)u * nx + ix0) * NY);
+            for (int m = 0; m < E; m++) s_lines[l * NY + t + m * T] = v[m];
+            store_band_rows<NY>(g, s_lines, wrows, tbuf + ((size_t)u * nx + ix0) * NY);
+        } else {
+            __syncwarp();  // the row's reads of its region are done
+#pragma unroll
+            for (int m = 0; m < E; m++) s_lines[l * SROW + t + m * T] = v[m];
+            warp_store_band_rows<NY>(g, s_lines + wrow0 * SROW, SROW, wrows,
+                                     tbuf + ((size_t)u * nx + ix0 + wrow0) * NY);
+        }
     }
 }
 
