@@ -142,6 +142,77 @@ def oracle_slice_count():
     return int(orc.Oracle().slice_count(DZ, FOV))
 
 
+# The other configurations, one subprocess each (fresh device state, own clock
+# record): (workload, extra arguments, what the summary keeps of its error).
+OTHER_CONFIGS = (
+    ("C1_plain", ["--workload", "plain", "--steps", "20", "--warmup", "3"]),
+    ("C3_phonon", ["--workload", "phonon", "--steps", "1", "--warmup", "3"]),
+    ("C4_uneven", ["--workload", "uneven", "--steps", "1", "--warmup", "3", "--quick"]),
+    ("C5_adjoint", ["--workload", "adjoint", "--steps", "3", "--warmup", "3", "--quick",
+                    "--fd-voxels", "64"]),
+)
+
+
+def run_other_configs(timeout_s=600):
+    """One timed step (after three warm-ups) of every other configuration, each in
+    its own process, summarised for the tilt line: value, e2e, dominant kernel's
+    roofline fraction, clocks and the FP64 error of its own check."""
+    out = {}
+    for name, extra in OTHER_CONFIGS:
+        t0 = time.perf_counter()
+        try:
+            r = subprocess.run([sys.executable, os.path.abspath(__file__), "--no-cpu-baseline",
+                                "--no-per-angle"] + extra, capture_output=True, text=True,
+                               timeout=timeout_s, cwd=ROOT)
+            lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+            if r.returncode != 0 or not lines:
+                out[name] = {"error": "exit %d: %s" % (r.returncode, r.stderr.strip()[-300:])}
+                continue
+            d = json.loads(lines[-1])
+            roof = d.get("roofline") or {}
+            e2e = d.get("e2e") or {}
+            out[name] = {
+                "metric": d.get("metric"), "value": d.get("value"), "unit": d.get("unit"),
+                "ms_per_step": d.get("ms_per_step"), "steps": d.get("steps"),
+                "warmup": d.get("warmup"), "workload": (d.get("config") or {}).get("workload"),
+                "e2e": {"value": e2e.get("value"), "ms_per_step": e2e.get("ms_per_step")},
+                "roofline": {"kernel": roof.get("kernel"), "frac": roof.get("frac"),
+                             "achieved": roof.get("achieved"), "unit": roof.get("unit")},
+                "gpu_launches": d.get("gpu_launches"), "clocks": d.get("clocks"),
+                "err_vs_fp64": d.get("err_vs_fp64", d.get("err")),
+                "wall_s": round(time.perf_counter() - t0, 1)}
+        except Exception as ex:  # reported, not fatal
+            out[name] = {"error": repr(ex)}
+    return out
+
+
+def host_memory_facts(ptr):
+    """NUMA layout of the host and the node holding the page at `ptr` (a pinned
+    host buffer): where the e2e copies land on a Grace host."""
+    import ctypes
+    nodes = sorted(n for n in os.listdir("/sys/devices/system/node") if n.startswith("node")) \
+        if os.path.isdir("/sys/devices/system/node") else []
+    facts = {"numa_nodes": len(nodes), "cpus": os.cpu_count()}
+    try:
+        bus = subprocess.run(["nvidia-smi", "--query-gpu=pci.bus_id", "--format=csv,noheader"],
+                             capture_output=True, text=True, timeout=20).stdout.split()[0]
+        bus = bus.lower().replace("00000000:", "0000:")
+        with open("/sys/bus/pci/devices/%s/numa_node" % bus) as f:
+            facts["gpu_numa_node"] = int(f.read())
+    except Exception:
+        pass
+    try:  # get_mempolicy(MPOL_F_NODE | MPOL_F_ADDR) on the buffer's first page
+        libc = ctypes.CDLL("libc.so.6", use_errno=True)
+        nr = {"aarch64": 236, "x86_64": 239}.get(os.uname().machine)
+        mode = ctypes.c_int(-1)
+        if nr and libc.syscall(nr, ctypes.byref(mode), None, ctypes.c_ulong(0),
+                               ctypes.c_void_p(ptr), ctypes.c_ulong(3)) == 0:
+            facts["pinned_buffer_numa_node"] = mode.value
+    except Exception:
+        pass
+    return facts
+
+
 def tilt_config(nang, nslices, world):
     """The `config` of the tilt-series line, shared by both arms."""
     return {"workload": "tilt series 1024^2, 160 A box, 20000 atoms in a 120^3 A cube, "
@@ -313,10 +384,11 @@ def run_adjoint(args, rank, world, local_rank):
     steps_per = nang * S
     value = world * steps_per / (ms / 1000.0)
     loss_dev, _ = ctx.adjoint(st, v, rp, target, grad=grad)
-    pick = [0, nang // 4]  # the orientations the oracle checks (0 and 44 degrees)
+    # the orientations the oracle checks (0 and 44 degrees; --quick: 0 only)
+    pick = [0] if args.quick else [0, nang // 4]
     g_dev = {a: grad[a].cpu().numpy() for a in pick}
     keep_all = None
-    if args.adj_checkpoint != 0:  # the same call keeping every wave and transmission
+    if args.adj_checkpoint != 0 and not args.quick:  # keeping every wave and transmission
         st.checkpoint = 0
         for _ in range(2):
             step()
@@ -326,7 +398,7 @@ def run_adjoint(args, rank, world, local_rank):
                     "ms_per_step": ms_keep, "checkpoint": 0}
     # forward alone (images of the same stacks)
     fimg = torch.empty_like(target)
-    ms_fwd = timed(lambda: ctx.stack_images(st, v, rp, images=fimg), args.steps)
+    ms_fwd = timed(lambda: ctx.stack_images(st, v, rp, images=fimg), 1 if args.quick else args.steps)
     # per-kernel attribution of one adjoint call
     ctx.profile(True)
     ms_serial = timed(step, 1)
@@ -662,9 +734,9 @@ def run_uneven(args, rank, world, local_rank):
     clk = clocks.stop()
     total = sum(steps)
     value = world * total / (ms / 1000.0)
-    ms_streams = timed(lambda: run(False), 1)
+    ms_streams = None if args.quick else timed(lambda: run(False), 1)
     per_size = {}
-    for n in (256, 512, 1024, 2048):
+    for n in (() if args.quick else (256, 512, 1024, 2048)):
         sel = [i for i, c in enumerate(cases) if c[1] == n]
         if not sel:
             continue
@@ -717,6 +789,8 @@ def run_uneven(args, rank, world, local_rank):
                                                np.linalg.norm(ref[d])) for d in range(len(defoci))]}
 
             sizes = sorted({c[1] for c in cases})
+            if args.quick:
+                sizes = sizes[:1]
             with cf.ThreadPoolExecutor(len(sizes)) as ex:
                 err = {"per_grid": list(ex.map(check, sizes))}
             err["max_image_rel_l2"] = max(max(e["image_rel_l2"]) for e in err["per_grid"])
@@ -733,7 +807,8 @@ def run_uneven(args, rank, world, local_rank):
                    "slice_steps_per_step": total, "images_per_step": 2 * sum(len(c[2]) for c in cases),
                    "l2": "inputs larger than L2 (tens of GB of waves)"},
         "per_size": per_size,
-        "streams_without_graph": {"ms": ms_streams, "value": total / (ms_streams / 1000.0)},
+        "streams_without_graph": None if ms_streams is None else
+                                 {"ms": ms_streams, "value": total / (ms_streams / 1000.0)},
         "e2e": {"value": total / (ms_e2e / 1000.0), "unit": UNIT, "h2d_bytes_per_step":
                 int(prof.get("copy_h2d", (0, 0, 0))[2]),
                 "d2h_bytes_per_step": int(sum(h.numel() * 4 for h in host)), "ms_per_step": ms_e2e,
@@ -969,6 +1044,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-check", action="store_true")
     ap.add_argument("--no-per-angle", action="store_true")
+    ap.add_argument("--no-other-configs", action="store_true",
+                    help="tilt workload: skip the one-step runs of the other configurations")
+    ap.add_argument("--quick", action="store_true",
+                    help="uneven / adjoint: the timed step, its profile, e2e and one FP64 "
+                         "check only (the form the tilt line's other_configs runs)")
     ap.add_argument("--orientations", type=int, default=NANG,
                     help="orientations per step (180 for the headline workload)")
     ap.add_argument("--workload", default="tilt",
@@ -1126,8 +1206,13 @@ def main():
     h2d = prof_e2e.get("copy_h2d", (0, 0.0, 0.0))[2]
     d2h = prof_e2e.get("copy_d2h", (0, 0.0, 0.0))[2]
     e2e_value = world * steps_per / (ms_e2e / 1000.0)
+    # where the e2e time beyond the device-timed step goes: the image copy-out
+    # (event-timed inside the library) and the rest
+    cp = prof_e2e.get("copy_images_d2h", (0, 0.0, 0.0))
+    copy_ms, copy_bytes = cp[1], cp[2]
     if rank == 0:
         same = torch.equal(host_images, images.cpu())
+        host_facts = host_memory_facts(host_images.data_ptr())
 
     # the per-orientation comparison form (cuFFT, unfused kernels, one orientation
     # at a time) on a subset of the same orientations
@@ -1216,7 +1301,12 @@ def main():
         "config": tilt_config(nang, nslices, world),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": ms_e2e,
-                "matches_device_output": bool(same)},
+                "matches_device_output": bool(same),
+                "ms_over_device_step": ms_e2e - ms,
+                "image_copy_ms": copy_ms,
+                "image_copy_GBps": copy_bytes / (copy_ms / 1000.0) / 1e9 if copy_ms > 0 else None,
+                "ms_over_device_step_not_copy": ms_e2e - ms - copy_ms,
+                "host": host_facts},
         "gpu_launches": launches * world,
         "ms_per_step_serialized": ms_serial,
         "kernels": {k: {"launches": v[0], "ms": round(v[1], 3),
@@ -1231,6 +1321,9 @@ def main():
         "cpu_baseline": cpu,
         "err_vs_fp64": err,
     }
+    if world == 1 and not args.no_other_configs:
+        # the other configurations, after this line's own measurements
+        out["other_configs"] = run_other_configs()
     print(json.dumps(out))
 
 

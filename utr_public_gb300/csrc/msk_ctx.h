@@ -70,6 +70,8 @@ enum Kind {
     kExpv, kAdjTransmit, kGrad, kImGrad, kAccum, kDW, kDWExp, kRotShift,
     // UTR reconstruction
     kUtrImgRows, kUtrImgCols, kUtrGrid, kUtrFourier, kUtrVolCols, kUtrFinal, kUtrPoint,
+    // the tilt series' image copy to host memory (event-timed, not a kernel)
+    kCopyImages,
     kKinds
 };
 extern const char *const kKindName[kKinds];

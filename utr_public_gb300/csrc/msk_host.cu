@@ -858,7 +858,7 @@ const char *const kKindName[kKinds] = {
     "row_expv", "row_adj_transmit", "row_grad", "row_imgrad", "accumulate", "col_debye_waller",
     "row_dw_phase", "image_rotate_shift",
     "utr_image_rows", "utr_image_cols", "utr_grid", "utr_fourier_rows", "utr_volume_cols",
-    "utr_final_cols", "utr_pointwise"};
+    "utr_final_cols", "utr_pointwise", "copy_images_d2h"};
 }  // namespace msk
 
 namespace msk {
@@ -1943,8 +1943,8 @@ int tilt_series_impl(msk_context *ctx, const msk_series *s, int natom, const int
     }
     MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     prof_collect(ctx);
-    if (ndefocus > 0 && !img_dev)
-    {
+    if (ndefocus > 0 && !img_dev) {
+        Prof p(ctx, kCopyImages, (double)img_bytes);
         MSK_CUDA(ctx, cudaMemcpyAsync(images, d_images, img_bytes, cudaMemcpyDeviceToHost,
                                       ctx->stream));
         count_copy(ctx, 1, (double)img_bytes);
