@@ -1,0 +1,67 @@
+"""Small grids (64^2 to 256^2) run their whole slice loop in one launch: one
+thread-block cluster per unit (msk_small.cuh).  Every row and column is
+computed as the launch-per-pass loop computes it, so the two paths must give
+the same exit waves and images bit for bit (MSK_SMALL_GRID=0 selects the
+loop), and both must match the FP64 oracle.  The reference golden at 256^2
+(C1's grid) is checked through the cluster path by test_gpu_parity."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from utr_public_gb300 import specimen as sp
+
+pytestmark = pytest.mark.gpu
+
+
+def both_paths(fn):
+    os.environ["MSK_SMALL_GRID"] = "0"
+    try:
+        loop = fn()
+    finally:
+        os.environ.pop("MSK_SMALL_GRID", None)
+    return fn(), loop
+
+
+@pytest.mark.parametrize("n,fov,v0,dz", [(64, 32.0, 200.0, 2.0), (128, 48.0, 300.0, 1.0),
+                                          (256, 64.0, 200.0, 2.0)])
+def test_calculate_cluster_path_equals_pass_loop(ctx, msk, oracle, n, fov, v0, dz):
+    s = sp.random_specimen(400, fov, 0.1 * fov, 0.9 * fov, 900 + n)
+    atoms = (s.Znum, s.x, s.y, s.z, s.occ)
+    param = msk.make_param(fov, fov, n, n, v0, dz)
+    fast, loop = both_paths(lambda: ctx.calculate(param, *atoms, fov, fov))
+    assert np.array_equal(fast.view(np.uint32), loop.view(np.uint32))
+    ref64 = oracle.calculate(param, *atoms, fov, fov, fp64=True)
+    assert rel_l2(fast, ref64) < 1e-5
+
+
+def test_calculate_cluster_path_with_incident_wave_and_tilt(ctx, msk, oracle):
+    s = sp.random_specimen(300, 32.0, 4.0, 28.0, 917)
+    atoms = (s.Znum, s.x, s.y, s.z, s.occ)
+    param = msk.make_param(32.0, 32.0, 128, 128, 200.0, 1.0, ctiltx=0.003, ctilty=-0.002)
+    rng = np.random.default_rng(8)
+    ph = rng.uniform(0, 2 * np.pi, (128, 128))
+    w0 = np.stack([np.cos(ph), np.sin(ph)], -1).astype(np.float32)
+    fast, loop = both_paths(lambda: ctx.calculate(param, *atoms, 32.0, 32.0, wave0=w0))
+    assert np.array_equal(fast.view(np.uint32), loop.view(np.uint32))
+    ref64 = oracle.calculate(param, *atoms, 32.0, 32.0, wave0=w0.astype(np.float64), fp64=True)
+    assert rel_l2(fast, ref64) < 1e-5
+
+
+def test_tilt_series_cluster_path_equals_pass_loop(ctx, msk):
+    """Many units in one launch (one cluster each), slices without atoms at both
+    ends of the box, two defoci: images and exit waves equal bit for bit."""
+    spec = sp.random_specimen(700, 64.0, 14.0, 50.0, 931)
+    atoms = (spec.Znum, spec.x, spec.y, spec.z, spec.occ)
+    s = msk.Series()
+    s.nx = s.ny = 256
+    s.ctblength = s.ctblengthz = 64.0
+    s.v0, s.deltaz = 300.0, 1.0
+    angY = np.deg2rad(np.arange(0.0, 180.0, 15.0))
+    angZ = np.linspace(0.0, 0.5, len(angY))
+    run = lambda: ctx.tilt_series(s, *atoms, angZ, angY, [0.0, 400.0], want_exit=True)
+    (fi, fe, fk), (li, le, lk) = both_paths(run)
+    assert np.array_equal(fk, lk)
+    assert np.array_equal(fe.view(np.uint32), le.view(np.uint32))
+    assert np.array_equal(fi.view(np.uint32), li.view(np.uint32))

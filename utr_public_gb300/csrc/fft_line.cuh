@@ -167,12 +167,20 @@ struct FftPlan {
 template <int N>
 __device__ __forceinline__ int pidx(int idx) { return idx + (idx >> 5); }
 
-// Barrier among the threads that share a line group.
-template <bool BLOCK>
+// Barrier among the threads that share a line group: SYNC 0 the warp (lines of
+// <= 32 threads), 1 the CTA, 2 the half of the CTA the thread is in (named
+// barriers 1 and 2, for CTAs whose halves run different passes).
+template <int SYNC>
 __device__ __forceinline__ void group_sync()
 {
-    if constexpr (BLOCK) __syncthreads();
-    else __syncwarp();
+    if constexpr (SYNC == 1) {
+        __syncthreads();
+    } else if constexpr (SYNC == 2) {
+        const unsigned h = blockDim.x >> 1;
+        asm volatile("bar.sync %0, %1;" ::"r"(1u + (threadIdx.x >= h ? 1u : 0u)), "r"(h) : "memory");
+    } else {
+        __syncwarp();
+    }
 }
 
 // Stage twiddles are fetched in groups of kTwG 16-byte loads (two twiddles
@@ -207,7 +215,7 @@ __device__ __forceinline__ void tw_fetch(float4 (&w)[kTwG], const float2 *tw, in
 // registers (all reads before any write), twiddles, radix-R DFT; a middle
 // stage writes back, the last stage leaves the result in strided order.
 // `pre` holds the stage's first twiddle group, fetched by the caller.
-template <int N, int R, int NS, bool LAST, bool INV, int C, bool BLOCK>
+template <int N, int R, int NS, bool LAST, bool INV, int C, int BLOCK>
 __device__ __forceinline__ void fft_stage(float2 (&v)[FftPlan<N>::E], float2 *buf, int c, int t,
                                           const float2 *tw, const float4 (&pre)[kTwG])
 {
@@ -263,8 +271,9 @@ __device__ __forceinline__ void fft_stage(float2 (&v)[FftPlan<N>::E], float2 *bu
 //   tw:  FftPlan<N>::TWN twiddles in global memory (stage 2 table, then
 //        stage 3 table; each in pairs, see the host's twiddle tables), read
 //        through the L1 cache; 16-byte aligned
+//   BLOCK: the group barrier (group_sync's SYNC)
 // Every thread of the group must call it (it contains group barriers).
-template <int N, bool INV, int C, bool BLOCK>
+template <int N, bool INV, int C, int BLOCK>
 __device__ __forceinline__ void fft_line(float2 (&v)[FftPlan<N>::E], float2 *buf, int c, int t,
                                          const float2 *tw)
 {

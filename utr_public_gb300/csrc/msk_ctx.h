@@ -72,6 +72,8 @@ enum Kind {
     kUtrImgRows, kUtrImgCols, kUtrGrid, kUtrFourier, kUtrVolCols, kUtrFinal, kUtrPoint,
     // the tilt series' image copy to host memory (event-timed, not a kernel)
     kCopyImages,
+    // the whole slice loop of a small grid in one cluster launch
+    kSmall,
     kKinds
 };
 extern const char *const kKindName[kKinds];

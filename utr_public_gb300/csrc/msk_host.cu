@@ -858,7 +858,7 @@ const char *const kKindName[kKinds] = {
     "row_expv", "row_adj_transmit", "row_grad", "row_imgrad", "accumulate", "col_debye_waller",
     "row_dw_phase", "image_rotate_shift",
     "utr_image_rows", "utr_image_cols", "utr_grid", "utr_fourier_rows", "utr_volume_cols",
-    "utr_final_cols", "utr_pointwise", "copy_images_d2h"};
+    "utr_final_cols", "utr_pointwise", "copy_images_d2h", "small_slices"};
 }  // namespace msk
 
 namespace msk {
@@ -1247,10 +1247,35 @@ int upload_batch(msk_context *ctx, const std::vector<UnitAtoms> &ua, int u0, int
 // order P3 after its P2 and the reuse of a transmission buffer after the P3
 // that read it.  With per-kernel profiling on, everything runs in order on
 // one stream so that each launch is timed alone.
+// Whether the slice loop of this grid runs as one cluster launch (msk_small.cuh):
+// square grids of 64^2 to 256^2 in the coherent branch with two transmission
+// buffers, on a device that fits the clusters.  MSK_SMALL_GRID=0 in the
+// environment keeps the launch-per-pass loop (=1: the default).
+static bool small_path(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode)
+{
+    const char *forced = getenv("MSK_SMALL_GRID");
+    if (forced && forced[0] == '0') return false;
+    const SizeOps *op = size_ops(gp.nx);
+    return nmode == 0 && b.dw.empty() && gp.nx == gp.ny && op && op->small_slices &&
+           ctx->tbuf2.cap >= ctx->tbuf.cap && ctx->tbuf.cap > 0 && op->small_ok(ctx->device);
+}
+
 int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode, bool w_in_band)
 {
     const SizeOps *rop = size_ops(gp.ny), *cop = size_ops(gp.nx);
     const Geom &g = gp.g;
+    if (small_path(ctx, gp, b, nmode)) {
+        // every slice of every unit in one launch; algorithmic bytes as the
+        // passes count them (64 N per slice-step with atoms, 16 N without)
+        const double plane = (double)gp.nx * gp.ny;
+        const double ne = b.act_off[b.nslices], all = (double)b.nunits * b.nslices;
+        Prof p(ctx, kSmall, plane * (64.0 * ne + 16.0 * (all - ne)));
+        MSK_CUDA(ctx, cop->small_slices(g, b.nunits, b.nslices, b.nslices + 1,
+                                        ctx->slice_off.as<int>(), ctx->atoms.as<SplatAtom>(),
+                                        ctx->psi.as<float2>(), ctx->tbuf.as<float2>(),
+                                        ctx->tbuf2.as<float2>(), ctx->stream));
+        return MSK_OK;
+    }
     // Debye-Waller branch: the second transmission buffer holds the potential's
     // spectrum, so the two slice chains run in order on one stream
     const bool dw = !b.dw.empty();

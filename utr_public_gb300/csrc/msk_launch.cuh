@@ -6,6 +6,7 @@
 #include <mutex>
 
 #include "msk_passes.cuh"
+#include "msk_small.cuh"
 #include "msk_types.h"
 
 namespace msk {
@@ -76,6 +77,14 @@ struct SizeOps {
     // returns the number of loss partials written
     int (*row_imgrad)(const Geom &, int nunits, const float2 *E, const float *target,
                       size_t tstride, float2 *G, double *partial, cudaStream_t);
+    // square grids of N <= 256: every slice of every unit in one cluster launch
+    // (msk_small.cuh); W holds S(psi) on entry and exit, T0 / T1 scratch of the
+    // same size.  small_ok: whether this device can run the clusters.  Both
+    // null for other sizes.
+    cudaError_t (*small_slices)(const Geom &, int nunits, int nslices, int nsl1,
+                                const int *slice_off, const SplatAtom *atoms, float2 *W,
+                                float2 *T0, float2 *T1, cudaStream_t);
+    bool (*small_ok)(int device);
 };
 
 // Line lengths with kernels: 16 .. 4096, powers of two.
@@ -283,6 +292,72 @@ struct Launch {
         return nb;
     }
 
+    static cudaLaunchConfig_t small_cfg(int nunits, cudaStream_t s, cudaLaunchAttribute *at)
+    {
+        using C = SmallCfg<N>;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)(nunits * C::Q));
+        cfg.blockDim = dim3(C::NT);
+        cfg.dynamicSmemBytes = C::SMEM;
+        cfg.stream = s;
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = C::Q;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        return cfg;
+    }
+    static void small_attrs()
+    {
+        static std::once_flag f;
+        std::call_once(f, [] {
+            using C = SmallCfg<N>;
+            cudaFuncSetAttribute(k_small_slices<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)C::SMEM);
+            if (C::Q > 8)
+                cudaFuncSetAttribute(k_small_slices<N>,
+                                     cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        });
+    }
+    static cudaError_t small_slices(const Geom &g, int nunits, int nslices, int nsl1,
+                                    const int *slice_off, const SplatAtom *atoms, float2 *W,
+                                    float2 *T0, float2 *T1, cudaStream_t s)
+    {
+        if constexpr (N >= 64 && N <= 256) {
+            small_attrs();
+            cudaLaunchAttribute at[1];
+            cudaLaunchConfig_t cfg = small_cfg(nunits, s, at);
+            return cudaLaunchKernelEx(&cfg, k_small_slices<N>, g, nslices, nsl1, slice_off, atoms,
+                                      W, T0, T1);
+        } else {
+            return cudaErrorNotSupported;
+        }
+    }
+    // at least one cluster fits on the device (cluster size and shared memory)
+    static bool small_ok(int device)
+    {
+        if constexpr (N >= 64 && N <= 256) {
+            static std::mutex m;
+            static int known[64] = {};  // 0 unknown, 1 yes, 2 no
+            if (device < 0 || device >= 64) return false;
+            std::lock_guard<std::mutex> lk(m);
+            if (!known[device]) {
+                small_attrs();
+                cudaLaunchAttribute at[1];
+                cudaLaunchConfig_t cfg = small_cfg(1, nullptr, at);
+                int n = 0;
+                const cudaError_t e = cudaOccupancyMaxActiveClusters(&n, k_small_slices<N>, &cfg);
+                if (e != cudaSuccess) cudaGetLastError();
+                known[device] = (e == cudaSuccess && n > 0) ? 1 : 2;
+            }
+            return known[device] == 1;
+        } else {
+            (void)device;
+            return false;
+        }
+    }
+
     static const SizeOps *ops()
     {
         static const SizeOps o = {N,        {ColCfg<N, 0>::C, ColCfg<N, 1>::C}, ColCfg<N>::BR, splat,
@@ -290,7 +365,9 @@ struct Launch {
                                   col_mask, col_prop,     col_fresnel,      row_transmit_t<false>,
                                   row_transmit_t<true>,   row_init, row_exit, row_inverse,
                                   row_intensity_t<false>, row_intensity_t<true>, row_expv,
-                                  row_adj_transmit,       row_grad,         row_imgrad};
+                                  row_adj_transmit,       row_grad,         row_imgrad,
+                                  (N >= 64 && N <= 256) ? small_slices : nullptr,
+                                  (N >= 64 && N <= 256) ? small_ok : nullptr};
         return &o;
     }
 };

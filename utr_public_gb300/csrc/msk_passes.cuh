@@ -253,6 +253,70 @@ __device__ __forceinline__ void splat_atom(const Geom &g, const SplatAtom &sa, i
     }
 }
 
+// The atoms [a0, a1) of a (unit, slice) whose window touches this warp's RW
+// rows (from wx0), added to the pixels of the row each thread owns (lines of
+// <= 32 threads): the list is scanned 32 atoms at a time, a ballot picks the
+// atoms that touch the warp's rows, each is broadcast by shuffles; per pixel
+// the sums keep the atom order.  vacc = this thread's row (float), zeroed.
+template <int NY>
+__device__ __forceinline__ void splat_scan_warp(const Geom &g, const SplatAtom *__restrict__ atoms,
+                                                int a0, int a1, int wx0, int RW, int ix,
+                                                bool row_ok, int t, float *vacc,
+                                                const float *s_knots)
+{
+    constexpr int T = FftPlan<NY>::T;
+    const int nx = g.nx, lane = threadIdx.x & 31;
+    const int W = 2 * g.idx + 1;
+    for (int base = a0; base < a1; base += 32) {
+        const int a = base + lane;
+        bool hit = false;
+        SplatAtom at = {};
+        if (a < a1) {
+            at = atoms[a];
+            const int ixo = (int)(at.meta & kMetaMask);
+            const int rel = pmod(ixo - g.idx - wx0, nx);
+            hit = (W >= nx) || (rel < RW) || (rel + W > nx);
+        }
+        unsigned bal = __ballot_sync(0xffffffffu, hit);
+        while (bal) {  // in atom order: the per-pixel sums keep the slice order
+            const int k = __ffs(bal) - 1;
+            bal &= bal - 1;
+            SplatAtom sa;
+            sa.fx = __shfl_sync(0xffffffffu, at.fx, k);
+            sa.fy = __shfl_sync(0xffffffffu, at.fy, k);
+            sa.occ = __shfl_sync(0xffffffffu, at.occ, k);
+            sa.meta = __shfl_sync(0xffffffffu, at.meta, k);
+            if (row_ok) splat_atom(g, sa, ix, t, T, NY, W, vacc, s_knots);
+        }
+    }
+    __syncwarp();
+}
+
+// A = S(exp(i sigma v)) of this thread's row from its potential vacc (float;
+// the row's shared region, which the transform then uses as its exchange
+// buffer): exp(i 0) = 1 exactly where the potential is 0, and rows without
+// atoms take S(1) = NY at iy = 0 directly (what the transform of ones gives).
+template <int NY, int SYNC>
+__device__ __forceinline__ void trans_row(const Geom &g, int t, const float *vacc, float2 *xbuf,
+                                          float2 (&v)[FftPlan<NY>::E])
+{
+    constexpr int T = FftPlan<NY>::T, E = FftPlan<NY>::E;
+    bool nz = false;
+#pragma unroll
+    for (int m = 0; m < E; m++) {
+        const float ph = vacc[t + m * T] * g.sigma_f;
+        v[m] = make_float2(1.0f, 0.0f);
+        nz |= ph != 0.0f;
+        if (__any_sync(0xffffffffu, ph != 0.0f)) v[m] = expi(ph);
+    }
+    if (group_none<SYNC == 1>(nz)) {
+#pragma unroll
+        for (int m = 0; m < E; m++) v[m] = make_float2(m == 0 && t == 0 ? (float)NY : 0.0f, 0.0f);
+    } else {
+        fft_line<NY, false, 1, SYNC>(v, xbuf, 0, t, g.tw_row);
+    }
+}
+
 // This warp's `rows` dense rows (row r at rows_smem + r * stride, 16-byte
 // aligned) as their in-band segments [0, seg_e1) and [seg_s2, NY), the (at
 // most two) out-of-band elements inside the segments zeroed first; lane 0
@@ -332,30 +396,7 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
     const int a0 = slice_off[u * nsl1 + slice], a1 = slice_off[u * nsl1 + slice + 1];
     const int W = 2 * g.idx + 1;
     if constexpr (!BLK) {
-        const int wx0 = ix0 + warp * RW;  // this warp's first row
-        for (int base = a0; base < a1; base += 32) {
-            const int a = base + lane;
-            bool hit = false;
-            SplatAtom at = {};
-            if (a < a1) {
-                at = atoms[a];
-                const int ixo = (int)(at.meta & kMetaMask);
-                const int rel = pmod(ixo - g.idx - wx0, nx);
-                hit = (W >= nx) || (rel < RW) || (rel + W > nx);
-            }
-            unsigned bal = __ballot_sync(0xffffffffu, hit);
-            while (bal) {  // in atom order: the per-pixel sums keep the slice order
-                const int k = __ffs(bal) - 1;
-                bal &= bal - 1;
-                SplatAtom sa;
-                sa.fx = __shfl_sync(0xffffffffu, at.fx, k);
-                sa.fy = __shfl_sync(0xffffffffu, at.fy, k);
-                sa.occ = __shfl_sync(0xffffffffu, at.occ, k);
-                sa.meta = __shfl_sync(0xffffffffu, at.meta, k);
-                if (row_ok) splat_atom(g, sa, ix, t, T, NY, W, vacc, s_knots);
-            }
-        }
-        __syncwarp();
+        splat_scan_warp<NY>(g, atoms, a0, a1, ix0 + warp * RW, RW, ix, row_ok, t, vacc, s_knots);
     } else {
         for (int base = a0; base < a1; base += NT) {
             const int a = base + tid;
@@ -430,24 +471,7 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
         }
     } else {
         float2 v[E];
-        bool nz = false;
-#pragma unroll
-        for (int m = 0; m < E; m++) {
-            // most of a slice is empty: exp(i*0) = 1 exactly
-            const float ph = vacc[t + m * T] * g.sigma_f;
-            v[m] = make_float2(1.0f, 0.0f);
-            nz |= ph != 0.0f;
-            if (__any_sync(0xffffffffu, ph != 0.0f)) v[m] = expi(ph);
-        }
-        if (group_none<BLK>(nz)) {
-            // rows without atoms: t = 1 and S(t) = NY at iy = 0, 0 elsewhere
-            // (what the transform of ones gives, every step exact)
-#pragma unroll
-            for (int m = 0; m < E; m++)
-                v[m] = make_float2(m == 0 && t == 0 ? (float)NY : 0.0f, 0.0f);
-        } else {
-            fft_line<NY, false, 1, BLK>(v, s_lines + l * SROW, 0, t, g.tw_row);
-        }
+        trans_row<NY, BLK ? 1 : 0>(g, t, vacc, s_lines + l * SROW, v);
         // dense rows into shared memory, then their in-band segments to the
         // buffer (its out-of-band columns hold zeros: the band limit zeroes them)
         if constexpr (BLK) {
