@@ -148,8 +148,7 @@ OTHER_CONFIGS = (
     ("C1_plain", ["--workload", "plain", "--steps", "20", "--warmup", "3"]),
     ("C3_phonon", ["--workload", "phonon", "--steps", "1", "--warmup", "3"]),
     ("C4_uneven", ["--workload", "uneven", "--steps", "1", "--warmup", "3", "--quick"]),
-    ("C5_adjoint", ["--workload", "adjoint", "--steps", "3", "--warmup", "3", "--quick",
-                    "--fd-voxels", "64"]),
+    ("C5_adjoint", ["--workload", "adjoint", "--steps", "3", "--warmup", "3", "--quick"]),
 )
 
 

@@ -270,3 +270,23 @@ def test_full_size_tilt_series(ctx, msk, oracle):
         for d in range(2):
             assert rel_l2(imgs[a, d], ref_img[d]) < 1e-5, (a, d)
     assert kept[1] < 20000 and kept[3] < 20000 and kept[2] == 20000
+
+
+@pytest.mark.parametrize("nconf,max_batch", [(1, 0), (3, 2)])
+def test_tilt_series_pinned_host_output(ctx, msk, nconf, max_batch):
+    """Page-locked host images are written in place by the image pass (the GPU
+    addresses them directly): equal bit for bit to device images, also when a
+    configuration average spans batches and the pass adds onto partial sums
+    already in host memory."""
+    torch = pytest.importorskip("torch")
+    spec = sp.random_specimen(300, 64.0, 10.0, 54.0, 1015)
+    atoms = (spec.Znum, spec.x, spec.y, spec.z, spec.occ)
+    s = series(msk, 64, 64.0, 200.0, 2.0, max_batch=max_batch)
+    disp = sp.phonon_displacements(spec, nconf, 0.08, 1015) if nconf > 1 else None
+    angZ, angY, df = [0.0, 0.5, 0.1], [0.2, 1.0, 2.0], [0.0, 100.0]
+    dev = torch.zeros((3, 2, 64, 64), dtype=torch.float32, device="cuda")
+    ctx.tilt_series(s, *atoms, angZ, angY, df, nconfig=nconf, displacements=disp, images=dev)
+    pin = torch.full((3, 2, 64, 64), -1.0, dtype=torch.float32, pin_memory=True)
+    ctx.tilt_series(s, *atoms, angZ, angY, df, nconfig=nconf, displacements=disp, images=pin)
+    torch.cuda.synchronize()
+    assert torch.equal(pin, dev.cpu())

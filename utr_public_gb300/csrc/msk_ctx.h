@@ -138,6 +138,8 @@ bool pow2_supported(int n);
 bool twiddles(int n, std::vector<float2> &out);
 bool is_device_ptr(const void *p);
 bool is_pinned_host(const void *p);
+// The device address of mapped page-locked host memory, or null.
+void *mapped_host(void *p);
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point.
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();

@@ -1143,6 +1143,18 @@ bool is_device_ptr(const void *p)
 
 // Page-locked host memory (cudaHostAlloc / cudaHostRegister): a copy to it
 // may be captured into a graph and runs asynchronously.
+// The device address of page-locked host memory the GPU can address directly
+// (mapped: over NVLink-C2C on a Grace host, PCIe elsewhere), or null.
+void *mapped_host(void *p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 bool is_pinned_host(const void *p)
 {
     cudaPointerAttributes a;
@@ -1709,9 +1721,14 @@ int tilt_series_impl(msk_context *ctx, const msk_series *s, int natom, const int
     MSK_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
     // psi + t per unit; the image and exit-wave outputs are held separately
     const bool img_dev = ndefocus > 0 && is_device_ptr(images);
+    // page-locked host images the GPU can address: the image pass writes them
+    // in place (no staging buffer, no copy after the last batch)
+    float *img_mapped =
+        ndefocus > 0 && !img_dev ? static_cast<float *>(mapped_host(images)) : nullptr;
+    const bool img_direct = img_dev || img_mapped;
     const bool ew_dev = exitwaves && is_device_ptr(exitwaves);
     const size_t img_bytes = (size_t)ndefocus * plane * sizeof(float);
-    size_t budget = free_b - std::min(free_b, (size_t)(img_dev ? 0 : img_bytes));
+    size_t budget = free_b - std::min(free_b, (size_t)(img_direct ? 0 : img_bytes));
     budget = std::min<size_t>(budget / 2, (size_t)64 << 30);
     // psi and two transmission buffers per unit in flight
     int B = (int)std::max<size_t>(1, std::min<size_t>(nunits, budget / (3 * plane * sizeof(float2))));
@@ -1732,8 +1749,8 @@ int tilt_series_impl(msk_context *ctx, const msk_series *s, int natom, const int
         while (bounds.back() < nunits) bounds.push_back(std::min(nunits, bounds.back() + B));
     }
 
-    float *d_images = images;
-    if (ndefocus > 0 && !img_dev) {
+    float *d_images = img_mapped ? img_mapped : images;
+    if (ndefocus > 0 && !img_direct) {
         MSK_CUDA(ctx, ctx->images.reserve(img_bytes));
         d_images = ctx->images.as<float>();
     }
@@ -1968,7 +1985,8 @@ int tilt_series_impl(msk_context *ctx, const msk_series *s, int natom, const int
     }
     MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     prof_collect(ctx);
-    if (ndefocus > 0 && !img_dev) {
+    if (ndefocus > 0 && img_mapped) count_copy(ctx, 1, (double)img_bytes);  // written in place
+    if (ndefocus > 0 && !img_direct) {
         Prof p(ctx, kCopyImages, (double)img_bytes);
         MSK_CUDA(ctx, cudaMemcpyAsync(images, d_images, img_bytes, cudaMemcpyDeviceToHost,
                                       ctx->stream));
