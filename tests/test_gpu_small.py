@@ -1,9 +1,11 @@
 """Small grids (64^2 to 256^2) run their whole slice loop in one launch: one
-thread-block cluster per unit (msk_small.cuh).  Every row and column is
-computed as the launch-per-pass loop computes it, so the two paths must give
-the same exit waves and images bit for bit (MSK_SMALL_GRID=0 selects the
-loop), and both must match the FP64 oracle.  The reference golden at 256^2
-(C1's grid) is checked through the cluster path by test_gpu_parity."""
+thread-block cluster per unit (msk_small.cuh).  The potentials, multipliers
+and atom order are those of the launch-per-pass loop (MSK_SMALL_GRID=0
+selects it); the line transforms use another radix split (16 points a
+thread), so the two paths agree to FP32 rounding (relative L2 2e-6) and both
+must match the FP64 oracle within 1e-5.  The reference golden at 256^2 (C1's
+grid) is checked through the cluster path by test_gpu_parity, and repeated
+calls through it are bit-stable (test_gpu_parity.test_deterministic)."""
 import os
 
 import numpy as np
@@ -31,9 +33,9 @@ def test_calculate_cluster_path_equals_pass_loop(ctx, msk, oracle, n, fov, v0, d
     atoms = (s.Znum, s.x, s.y, s.z, s.occ)
     param = msk.make_param(fov, fov, n, n, v0, dz)
     fast, loop = both_paths(lambda: ctx.calculate(param, *atoms, fov, fov))
-    assert np.array_equal(fast.view(np.uint32), loop.view(np.uint32))
+    assert rel_l2(fast, loop) < 2e-6
     ref64 = oracle.calculate(param, *atoms, fov, fov, fp64=True)
-    assert rel_l2(fast, ref64) < 1e-5
+    assert rel_l2(fast, ref64) < 1e-5 and rel_l2(loop, ref64) < 1e-5
 
 
 def test_calculate_cluster_path_with_incident_wave_and_tilt(ctx, msk, oracle):
@@ -44,14 +46,15 @@ def test_calculate_cluster_path_with_incident_wave_and_tilt(ctx, msk, oracle):
     ph = rng.uniform(0, 2 * np.pi, (128, 128))
     w0 = np.stack([np.cos(ph), np.sin(ph)], -1).astype(np.float32)
     fast, loop = both_paths(lambda: ctx.calculate(param, *atoms, 32.0, 32.0, wave0=w0))
-    assert np.array_equal(fast.view(np.uint32), loop.view(np.uint32))
+    assert rel_l2(fast, loop) < 2e-6
     ref64 = oracle.calculate(param, *atoms, 32.0, 32.0, wave0=w0.astype(np.float64), fp64=True)
     assert rel_l2(fast, ref64) < 1e-5
 
 
 def test_tilt_series_cluster_path_equals_pass_loop(ctx, msk):
     """Many units in one launch (one cluster each), slices without atoms at both
-    ends of the box, two defoci: images and exit waves equal bit for bit."""
+    ends of the box, two defoci: images and exit waves as the loop's; every
+    unit of the launch equal to the same orientation computed alone."""
     spec = sp.random_specimen(700, 64.0, 14.0, 50.0, 931)
     atoms = (spec.Znum, spec.x, spec.y, spec.z, spec.occ)
     s = msk.Series()
@@ -63,5 +66,9 @@ def test_tilt_series_cluster_path_equals_pass_loop(ctx, msk):
     run = lambda: ctx.tilt_series(s, *atoms, angZ, angY, [0.0, 400.0], want_exit=True)
     (fi, fe, fk), (li, le, lk) = both_paths(run)
     assert np.array_equal(fk, lk)
-    assert np.array_equal(fe.view(np.uint32), le.view(np.uint32))
-    assert np.array_equal(fi.view(np.uint32), li.view(np.uint32))
+    for a in range(len(angY)):
+        assert rel_l2(fe[a], le[a]) < 2e-6, a
+        for d in range(2):
+            assert rel_l2(fi[a, d], li[a, d]) < 2e-6, (a, d)
+    one, ew1, _ = ctx.tilt_series(s, *atoms, angZ[5:6], angY[5:6], [0.0, 400.0], want_exit=True)
+    assert np.array_equal(one[0], fi[5]) and np.array_equal(ew1[0], fe[5])

@@ -144,28 +144,42 @@ __host__ __device__ __forceinline__ void dft(float2 *v)
     for (int i = 0; i < R; i++) v[i * S] = a[i];
 }
 
-// Radix plan per line length.
-template <int N>
+// Radix plan per line length.  EV = 0: E = 32 elements per thread (the
+// default plan of every pass); EV = 16: 16 elements per thread, twice the
+// threads per line (lines up to 1024 points), for passes that need more
+// threads per line and fewer registers per thread.
+template <int N, int EV = 0>
 struct FftPlan {
     static_assert(N >= 16 && N <= 4096 && (N & (N - 1)) == 0, "line length");
-    static constexpr int E = N >= 32 ? 32 : N;   // elements per thread
+    static_assert(EV == 0 || (EV == 16 && N >= 16 && N <= 1024), "plan variant");
+    static constexpr int E = EV ? (N >= EV ? EV : N) : (N >= 32 ? 32 : N);  // elements per thread
     static constexpr int T = N / E;              // threads per line
     static constexpr int REST = N / E;
-    // stages after the first: REST <= 32 -> one stage; else two
-    static constexpr int S = (REST == 1) ? 1 : (REST <= 32 ? 2 : 3);
-    static constexpr int R2 = (S >= 2) ? (REST <= 32 ? REST : (REST == 64 ? 8 : 16)) : 1;
+    // stages after the first: REST <= E -> one stage of radix REST; else two,
+    // the last of radix 8
+    static constexpr int S = (REST == 1) ? 1 : (REST <= E ? 2 : 3);
+    static constexpr int R2 = (S >= 2) ? (REST <= E ? REST : REST / 8) : 1;
     static constexpr int R3 = (S == 3) ? REST / R2 : 1;
+    static_assert(R2 <= E && R3 <= E, "stage radix within a thread's elements");
     static constexpr int NS2 = E;          // sub-transform size entering stage 2
     static constexpr int NS3 = E * R2;     // entering stage 3
     // per-stage twiddle tables tw[r*Ns + j], r < R, j < Ns
     static constexpr int TW2 = (S >= 2) ? NS2 * R2 : 0;
     static constexpr int TW3 = (S == 3) ? NS3 * R3 : 0;
     static constexpr int TWN = TW2 + TW3;
-    static constexpr int PADN = N + N / 32;  // padded line length in shared memory
+    // shared memory: one padding element every PER (conflict-free exchanges;
+    // 32 for the default plan, E for the others)
+    static constexpr int PER = EV ? E : 32;
+    static constexpr int PADN = N + N / PER;
 };
 
-template <int N>
-__device__ __forceinline__ int pidx(int idx) { return idx + (idx >> 5); }
+// Padded shared-memory index of line element idx.
+template <int N, int EV = 0>
+__device__ __forceinline__ int pidx(int idx)
+{
+    constexpr int PER = FftPlan<N, EV>::PER;
+    return idx + idx / PER;
+}
 
 // Barrier among the threads that share a line group: SYNC 0 the warp (lines of
 // <= 32 threads), 1 the CTA, 2 the half of the CTA the thread is in (named
@@ -190,19 +204,19 @@ __device__ __forceinline__ void group_sync()
 // behind arithmetic instead of stalling the warp.
 constexpr int kTwG = 4;
 
-template <int N, int R, int NS>
+template <int N, int R, int NS, int EV = 0>
 struct StageTw {
-    static constexpr int E = FftPlan<N>::E, T = FftPlan<N>::T, KB = E / R;
+    static constexpr int E = FftPlan<N, EV>::E, T = FftPlan<N, EV>::T, KB = E / R;
     static constexpr int NP = R / 2;                    // twiddle pairs per sub-transform
     static constexpr int GPK = (NP + kTwG - 1) / kTwG;  // load groups per sub-transform
     static constexpr int NG = KB * GPK;                 // load groups in the stage
 };
 
 // Group gi (compile-time once unrolled) of a stage's twiddles into w.
-template <int N, int R, int NS>
+template <int N, int R, int NS, int EV = 0>
 __device__ __forceinline__ void tw_fetch(float4 (&w)[kTwG], const float2 *tw, int t, int gi)
 {
-    using S = StageTw<N, R, NS>;
+    using S = StageTw<N, R, NS, EV>;
     const int k = gi / S::GPK, p0 = (gi % S::GPK) * kTwG;
     const int j = (t + k * S::T) % NS;
     const float4 *tw4 = reinterpret_cast<const float4 *>(tw);
@@ -215,17 +229,17 @@ __device__ __forceinline__ void tw_fetch(float4 (&w)[kTwG], const float2 *tw, in
 // registers (all reads before any write), twiddles, radix-R DFT; a middle
 // stage writes back, the last stage leaves the result in strided order.
 // `pre` holds the stage's first twiddle group, fetched by the caller.
-template <int N, int R, int NS, bool LAST, bool INV, int C, int BLOCK>
-__device__ __forceinline__ void fft_stage(float2 (&v)[FftPlan<N>::E], float2 *buf, int c, int t,
-                                          const float2 *tw, const float4 (&pre)[kTwG])
+template <int N, int R, int NS, bool LAST, bool INV, int C, int BLOCK, int EV = 0>
+__device__ __forceinline__ void fft_stage(float2 (&v)[FftPlan<N, EV>::E], float2 *buf, int c,
+                                          int t, const float2 *tw, const float4 (&pre)[kTwG])
 {
-    using S = StageTw<N, R, NS>;
-    constexpr int E = FftPlan<N>::E, T = FftPlan<N>::T, KB = E / R;
+    using S = StageTw<N, R, NS, EV>;
+    constexpr int E = FftPlan<N, EV>::E, T = FftPlan<N, EV>::T, KB = E / R;
 #pragma unroll
     for (int k = 0; k < KB; k++) {
         const int b = t + k * T;
 #pragma unroll
-        for (int r = 0; r < R; r++) v[k + r * KB] = buf[pidx<N>(b + r * (N / R)) * C + c];
+        for (int r = 0; r < R; r++) v[k + r * KB] = buf[pidx<N, EV>(b + r * (N / R)) * C + c];
     }
     if constexpr (!LAST) group_sync<BLOCK>();
     float4 cur[kTwG], nxt[kTwG];
@@ -233,7 +247,7 @@ __device__ __forceinline__ void fft_stage(float2 (&v)[FftPlan<N>::E], float2 *bu
     for (int q = 0; q < kTwG; q++) cur[q] = pre[q];
 #pragma unroll
     for (int gi = 0; gi < S::NG; gi++) {
-        if (gi + 1 < S::NG) tw_fetch<N, R, NS>(nxt, tw, t, gi + 1);
+        if (gi + 1 < S::NG) tw_fetch<N, R, NS, EV>(nxt, tw, t, gi + 1);
         const int k = gi / S::GPK, p0 = (gi % S::GPK) * kTwG;
 #pragma unroll
         for (int q = 0; q < kTwG; q++) {
@@ -259,7 +273,7 @@ __device__ __forceinline__ void fft_stage(float2 (&v)[FftPlan<N>::E], float2 *bu
             const int j = b % NS;
             const int o = (b / NS) * NS * R + j;
 #pragma unroll
-            for (int r = 0; r < R; r++) buf[pidx<N>(o + r * NS) * C + c] = v[k + r * KB];
+            for (int r = 0; r < R; r++) buf[pidx<N, EV>(o + r * NS) * C + c] = v[k + r * KB];
         }
         group_sync<BLOCK>();
     }
@@ -273,27 +287,27 @@ __device__ __forceinline__ void fft_stage(float2 (&v)[FftPlan<N>::E], float2 *bu
 //        through the L1 cache; 16-byte aligned
 //   BLOCK: the group barrier (group_sync's SYNC)
 // Every thread of the group must call it (it contains group barriers).
-template <int N, bool INV, int C, int BLOCK>
-__device__ __forceinline__ void fft_line(float2 (&v)[FftPlan<N>::E], float2 *buf, int c, int t,
+template <int N, bool INV, int C, int BLOCK, int EV = 0>
+__device__ __forceinline__ void fft_line(float2 (&v)[FftPlan<N, EV>::E], float2 *buf, int c, int t,
                                          const float2 *tw)
 {
-    using P = FftPlan<N>;
+    using P = FftPlan<N, EV>;
     constexpr int E = P::E;
     float4 pre2[kTwG];
-    if constexpr (P::S >= 2) tw_fetch<N, P::R2, P::NS2>(pre2, tw, t, 0);
+    if constexpr (P::S >= 2) tw_fetch<N, P::R2, P::NS2, EV>(pre2, tw, t, 0);
     dft<E, INV, 1>(v);
     if constexpr (P::S >= 2) {
         group_sync<BLOCK>();  // earlier readers of buf are done
 #pragma unroll
-        for (int r = 0; r < E; r++) buf[pidx<N>(t * E + r) * C + c] = v[r];
+        for (int r = 0; r < E; r++) buf[pidx<N, EV>(t * E + r) * C + c] = v[r];
         group_sync<BLOCK>();
         if constexpr (P::S == 2) {
-            fft_stage<N, P::R2, P::NS2, true, INV, C, BLOCK>(v, buf, c, t, tw, pre2);
+            fft_stage<N, P::R2, P::NS2, true, INV, C, BLOCK, EV>(v, buf, c, t, tw, pre2);
         } else {
             float4 pre3[kTwG];
-            tw_fetch<N, P::R3, P::NS3>(pre3, tw + P::TW2, t, 0);
-            fft_stage<N, P::R2, P::NS2, false, INV, C, BLOCK>(v, buf, c, t, tw, pre2);
-            fft_stage<N, P::R3, P::NS3, true, INV, C, BLOCK>(v, buf, c, t, tw + P::TW2, pre3);
+            tw_fetch<N, P::R3, P::NS3, EV>(pre3, tw + P::TW2, t, 0);
+            fft_stage<N, P::R2, P::NS2, false, INV, C, BLOCK, EV>(v, buf, c, t, tw, pre2);
+            fft_stage<N, P::R3, P::NS3, true, INV, C, BLOCK, EV>(v, buf, c, t, tw + P::TW2, pre3);
         }
     }
 }

@@ -135,7 +135,8 @@ int fail(msk_context *ctx, int code, const std::string &msg);
 
 bool pow2_supported(int n);
 // Stockham stage twiddles of the line FFT of length n (false: no kernels for n).
-bool twiddles(int n, std::vector<float2> &out);
+// ev = 16: the twiddles of the 16-points-a-thread plan FftPlan<n, 16>.
+bool twiddles(int n, std::vector<float2> &out, int ev = 0);
 bool is_device_ptr(const void *p);
 bool is_pinned_host(const void *p);
 // The device address of mapped page-locked host memory, or null.

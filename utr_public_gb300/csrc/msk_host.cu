@@ -593,15 +593,15 @@ static bool grid_pre(GridPre &gp, int nx, int ny, float ax, float by, float v0, 
     return true;
 }
 
-// Stockham stage twiddles for line length n, matching FftPlan<n>: per stage
-// of radix R entered by sub-transforms of size NS, w(r, j) = exp(2 pi i r j /
-// (NS R)) for r = 1..R-1, stored in pairs -- float2 index 2 (p NS + j) + q
-// holds w(2p + 1 + q, j), so one 16-byte load fetches the twiddles of r = 2p+1
-// and 2p+2 (the pair of r = R-1 is padded with 1).  Computed in double.
-template <int N>
+// Stockham stage twiddles for line length n, matching FftPlan<n, ev>: per
+// stage of radix R entered by sub-transforms of size NS, w(r, j) = exp(2 pi i
+// r j / (NS R)) for r = 1..R-1, stored in pairs -- float2 index 2 (p NS + j) +
+// q holds w(2p + 1 + q, j), so one 16-byte load fetches the twiddles of r =
+// 2p+1 and 2p+2 (the pair of r = R-1 is padded with 1).  Computed in double.
+template <int N, int EV>
 static void twiddles_n(std::vector<float2> &out)
 {
-    using P = FftPlan<N>;
+    using P = FftPlan<N, EV>;
     out.assign(std::max(P::TWN, 2), make_float2(1.0f, 0.0f));
     const double twopi = 8.0 * atan(1.0);
     auto fill = [&](int off, int ns, int r_) {
@@ -616,18 +616,30 @@ static void twiddles_n(std::vector<float2> &out)
     if (P::S == 3) fill(P::TW2, P::NS3, P::R3);
 }
 
-bool twiddles(int n, std::vector<float2> &out)
+bool twiddles(int n, std::vector<float2> &out, int ev)
 {
+    if (ev == 16) {
+        switch (n) {
+        case 16: twiddles_n<16, 16>(out); return true;
+        case 32: twiddles_n<32, 16>(out); return true;
+        case 64: twiddles_n<64, 16>(out); return true;
+        case 128: twiddles_n<128, 16>(out); return true;
+        case 256: twiddles_n<256, 16>(out); return true;
+        case 512: twiddles_n<512, 16>(out); return true;
+        case 1024: twiddles_n<1024, 16>(out); return true;
+        default: return false;
+        }
+    }
     switch (n) {
-    case 16: twiddles_n<16>(out); return true;
-    case 32: twiddles_n<32>(out); return true;
-    case 64: twiddles_n<64>(out); return true;
-    case 128: twiddles_n<128>(out); return true;
-    case 256: twiddles_n<256>(out); return true;
-    case 512: twiddles_n<512>(out); return true;
-    case 1024: twiddles_n<1024>(out); return true;
-    case 2048: twiddles_n<2048>(out); return true;
-    case 4096: twiddles_n<4096>(out); return true;
+    case 16: twiddles_n<16, 0>(out); return true;
+    case 32: twiddles_n<32, 0>(out); return true;
+    case 64: twiddles_n<64, 0>(out); return true;
+    case 128: twiddles_n<128, 0>(out); return true;
+    case 256: twiddles_n<256, 0>(out); return true;
+    case 512: twiddles_n<512, 0>(out); return true;
+    case 1024: twiddles_n<1024, 0>(out); return true;
+    case 2048: twiddles_n<2048, 0>(out); return true;
+    case 4096: twiddles_n<4096, 0>(out); return true;
     default: return false;
     }
 }
@@ -1038,15 +1050,55 @@ int col_variant(msk_context *ctx, const GridPre &gp, int mode)
 // Device tables of one grid (frequency grids, propagator, twiddles, potential
 // spline, band-limit ranges) laid out in one block of 256-byte aligned pieces.
 struct TableLayout {
-    size_t kx2, ky2, kx, ky, px, py, twr, twc, kn, cf, kb, bytes;
+    size_t kx2, ky2, kx, ky, px, py, twr, twc, twr16, twc16, kn, cf, kb, bytes;
+    size_t n_twr, n_twc, n_twr16, n_twc16;  // twiddle counts (float2)
 };
+
+// Offsets (256-byte aligned pieces) of the grid tables of an nx x ny grid with
+// nz compact atomic numbers; the 16-point-plan twiddles only for lines of
+// <= 1024 points.  The one formula behind the table upload and the fixed
+// scratch of msk_calculate_static.
+TableLayout layout_tables(int nx, int ny, int nz)
+{
+    TableLayout o{};
+    std::vector<float2> t;
+    twiddles(ny, t);
+    o.n_twr = t.size();
+    twiddles(nx, t);
+    o.n_twc = t.size();
+    o.n_twr16 = twiddles(ny, t, 16) ? t.size() : 0;
+    o.n_twc16 = twiddles(nx, t, 16) ? t.size() : 0;
+    size_t off = 0;
+    auto piece = [&](size_t bytes) {
+        size_t q = off;
+        off += (bytes + 255) & ~size_t(255);
+        return q;
+    };
+    o.kx2 = piece(4 * (size_t)nx);
+    o.ky2 = piece(4 * (size_t)ny);
+    o.kx = piece(4 * (size_t)nx);
+    o.ky = piece(4 * (size_t)ny);
+    o.px = piece(8 * (size_t)nx);
+    o.py = piece(8 * (size_t)ny);
+    o.twr = piece(8 * o.n_twr);
+    o.twc = piece(8 * o.n_twc);
+    o.twr16 = piece(8 * o.n_twr16);
+    o.twc16 = piece(8 * o.n_twc16);
+    o.kn = piece(4 * (size_t)phys::kN);
+    o.cf = piece(16 * (size_t)std::max(nz, 1) * phys::kN);
+    o.kb = piece(8 * (size_t)ny);
+    o.bytes = off;
+    return o;
+}
 
 static void build_tables(const GridPre &gp, const std::vector<int> &zlist,
                          std::vector<unsigned char> &host, TableLayout &o)
 {
-    std::vector<float2> twr, twc;
+    std::vector<float2> twr, twc, twr16, twc16;
     twiddles(gp.ny, twr);
     twiddles(gp.nx, twc);
+    twiddles(gp.ny, twr16, 16);
+    twiddles(gp.nx, twc16, 16);
     const int nz = (int)zlist.size();
     auto &L = phys::lut();
     for (int Z : zlist) L.build(Z);
@@ -1059,25 +1111,8 @@ static void build_tables(const GridPre &gp, const std::vector<int> &zlist,
             coef[(size_t)zi * phys::kN + i] = make_float4((float)L.y[Z][i], (float)L.b[Z][i],
                                                           (float)L.c[Z][i], (float)L.d[Z][i]);
     }
-    size_t off = 0;
-    auto piece = [&](size_t bytes) {
-        size_t q = off;
-        off += (bytes + 255) & ~size_t(255);
-        return q;
-    };
-    o.kx2 = piece(4 * gp.nx);
-    o.ky2 = piece(4 * gp.ny);
-    o.kx = piece(4 * gp.nx);
-    o.ky = piece(4 * gp.ny);
-    o.px = piece(8 * gp.nx);
-    o.py = piece(8 * gp.ny);
-    o.twr = piece(8 * twr.size());
-    o.twc = piece(8 * twc.size());
-    o.kn = piece(4 * knots.size());
-    o.cf = piece(16 * coef.size());
-    o.kb = piece(8 * gp.ny);
-    o.bytes = off;
-    host.assign(off, 0);
+    o = layout_tables(gp.nx, gp.ny, nz);
+    host.assign(o.bytes, 0);
     std::memcpy(&host[o.kx2], gp.kx2.data(), 4 * gp.nx);
     std::memcpy(&host[o.ky2], gp.ky2.data(), 4 * gp.ny);
     std::memcpy(&host[o.kx], gp.kx.data(), 4 * gp.nx);
@@ -1086,6 +1121,8 @@ static void build_tables(const GridPre &gp, const std::vector<int> &zlist,
     std::memcpy(&host[o.py], gp.propy.data(), 8 * gp.ny);
     std::memcpy(&host[o.twr], twr.data(), 8 * twr.size());
     std::memcpy(&host[o.twc], twc.data(), 8 * twc.size());
+    if (o.n_twr16) std::memcpy(&host[o.twr16], twr16.data(), 8 * twr16.size());
+    if (o.n_twc16) std::memcpy(&host[o.twc16], twc16.data(), 8 * twc16.size());
     std::memcpy(&host[o.kn], knots.data(), 4 * knots.size());
     std::memcpy(&host[o.cf], coef.data(), 16 * coef.size());
     std::memcpy(&host[o.kb], gp.kband.data(), 8 * gp.ny);
@@ -1102,6 +1139,8 @@ static void bind_tables(GridPre &gp, const unsigned char *b, const TableLayout &
     g.propy = reinterpret_cast<const float2 *>(b + o.py);
     g.tw_row = reinterpret_cast<const float2 *>(b + o.twr);
     g.tw_col = reinterpret_cast<const float2 *>(b + o.twc);
+    g.tw_row16 = o.n_twr16 ? reinterpret_cast<const float2 *>(b + o.twr16) : nullptr;
+    g.tw_col16 = o.n_twc16 ? reinterpret_cast<const float2 *>(b + o.twc16) : nullptr;
     g.knots = reinterpret_cast<const float *>(b + o.kn);
     g.coef = reinterpret_cast<const float4 *>(b + o.cf);
     g.kband = reinterpret_cast<const int2 *>(b + o.kb);
@@ -3295,19 +3334,8 @@ struct NoAllocScope {
     ~NoAllocScope() { t_no_alloc = prev; }
 };
 
-// Bytes upload_tables() needs for this grid (its 256-byte aligned pieces).
-size_t static_table_bytes(int nx, int ny, int nz)
-{
-    auto a = [](size_t b) { return (b + 255) & ~size_t(255); };
-    std::vector<float2> t;
-    twiddles(nx, t);
-    const size_t twc = t.size();
-    twiddles(ny, t);
-    const size_t twr = t.size();
-    return a(4 * (size_t)nx) * 2 + a(4 * (size_t)ny) * 2 + a(8 * (size_t)nx) + a(8 * (size_t)ny) +
-           a(8 * twr) + a(8 * twc) + a(4 * phys::kN) + a(16 * (size_t)std::max(nz, 1) * phys::kN) +
-           a(8 * (size_t)ny);
-}
+// Bytes upload_tables() needs for this grid.
+size_t static_table_bytes(int nx, int ny, int nz) { return layout_tables(nx, ny, nz).bytes; }
 
 }  // namespace
 

@@ -258,13 +258,13 @@ __device__ __forceinline__ void splat_atom(const Geom &g, const SplatAtom &sa, i
 // <= 32 threads): the list is scanned 32 atoms at a time, a ballot picks the
 // atoms that touch the warp's rows, each is broadcast by shuffles; per pixel
 // the sums keep the atom order.  vacc = this thread's row (float), zeroed.
-template <int NY>
+template <int NY, int EV = 0>
 __device__ __forceinline__ void splat_scan_warp(const Geom &g, const SplatAtom *__restrict__ atoms,
                                                 int a0, int a1, int wx0, int RW, int ix,
                                                 bool row_ok, int t, float *vacc,
                                                 const float *s_knots)
 {
-    constexpr int T = FftPlan<NY>::T;
+    constexpr int T = FftPlan<NY, EV>::T;
     const int nx = g.nx, lane = threadIdx.x & 31;
     const int W = 2 * g.idx + 1;
     for (int base = a0; base < a1; base += 32) {
@@ -296,11 +296,11 @@ __device__ __forceinline__ void splat_scan_warp(const Geom &g, const SplatAtom *
 // the row's shared region, which the transform then uses as its exchange
 // buffer): exp(i 0) = 1 exactly where the potential is 0, and rows without
 // atoms take S(1) = NY at iy = 0 directly (what the transform of ones gives).
-template <int NY, int SYNC>
+template <int NY, int SYNC, int EV = 0>
 __device__ __forceinline__ void trans_row(const Geom &g, int t, const float *vacc, float2 *xbuf,
-                                          float2 (&v)[FftPlan<NY>::E])
+                                          float2 (&v)[FftPlan<NY, EV>::E])
 {
-    constexpr int T = FftPlan<NY>::T, E = FftPlan<NY>::E;
+    constexpr int T = FftPlan<NY, EV>::T, E = FftPlan<NY, EV>::E;
     bool nz = false;
 #pragma unroll
     for (int m = 0; m < E; m++) {
@@ -313,7 +313,7 @@ __device__ __forceinline__ void trans_row(const Geom &g, int t, const float *vac
 #pragma unroll
         for (int m = 0; m < E; m++) v[m] = make_float2(m == 0 && t == 0 ? (float)NY : 0.0f, 0.0f);
     } else {
-        fft_line<NY, false, 1, SYNC>(v, xbuf, 0, t, g.tw_row);
+        fft_line<NY, false, 1, SYNC, EV>(v, xbuf, 0, t, EV ? g.tw_row16 : g.tw_row);
     }
 }
 

@@ -25,9 +25,13 @@
 // buffers.  Every row and column is computed with the same line transforms,
 // multipliers and atom order as the multi-launch passes (k_row_splat,
 // k_col_pass, k_row_transmit), whole rows and columns instead of the in-band
-// segments, so the results are the same bit for bit.  Loads of data another
-// CTA wrote go through L2 (ld.global.cg).
+// segments.  Loads of data another CTA wrote go through L2 (ld.global.cg).
 //
+// The line transforms use the 16-points-a-thread plan (FftPlan<N, 16>: twice
+// the threads per line of the multi-launch passes, half the registers and the
+// serial chain per thread), so a CTA of 2 x 16 lines has 512 threads at 256^2;
+// the results equal the multi-launch loop's to FP32 rounding (the same
+// potentials, multipliers and atom order; another radix split of the FFT).
 // The grid is `units x Q` CTAs in clusters of Q (Q = 16 for 256^2 needs the
 // non-portable cluster size); no CTA leaves the slice loop early, so every one
 // arrives at every cluster barrier.
@@ -39,7 +43,8 @@ namespace msk {
 
 template <int N>
 struct SmallCfg {
-    using P = FftPlan<N>;
+    static constexpr int EV = 16;  // the plan's elements per thread
+    using P = FftPlan<N, EV>;
     static constexpr int T = P::T, E = P::E;
     static constexpr int LPC = 16;        // rows (and columns) one CTA owns
     static constexpr int Q = N / LPC;     // CTAs per cluster: one unit
@@ -47,7 +52,7 @@ struct SmallCfg {
     static constexpr int NT = 2 * HALF;
     static constexpr int RW = 32 / T;     // rows per warp in the row phase
     static constexpr int PADN = P::PADN;
-    static constexpr int SROW = SplatCfg<N>::SROW;
+    static constexpr int SROW = (P::PADN + 1) & ~1;
     // shared memory in float2 units.  Row phase: half 0 a transform buffer and
     // a stash of iS(B) per row; half 1 the splat row (potential, then the
     // transform's exchange).  Column phase: one tile of LPC interleaved columns
@@ -59,6 +64,7 @@ struct SmallCfg {
     static constexpr size_t SMEM = (size_t)F2 * 8 + 128 * 4;
     static_assert(N >= 64 && N <= 256, "small-grid sizes");
     static_assert(T <= 32 && 32 % T == 0, "a warp holds whole lines");
+    static_assert(HALF % 32 == 0, "halves of whole warps");
 };
 
 __device__ __forceinline__ unsigned cluster_rank()
@@ -82,7 +88,7 @@ k_small_slices(const Geom g, int nslices, int nsl1, const int *__restrict__ slic
                const SplatAtom *__restrict__ atoms, float2 *W, float2 *Tb0, float2 *Tb1)
 {
     using C = SmallCfg<N>;
-    constexpr int T = C::T, E = C::E, LPC = C::LPC, HALF = C::HALF;
+    constexpr int T = C::T, E = C::E, LPC = C::LPC, HALF = C::HALF, EV = C::EV;
     extern __shared__ __align__(128) unsigned char smem[];
     float2 *sm = reinterpret_cast<float2 *>(smem);
     float *s_knots = reinterpret_cast<float *>(sm + C::F2);
@@ -122,15 +128,15 @@ k_small_slices(const Geom g, int nslices, int nsl1, const int *__restrict__ slic
                 float2 v[E];
 #pragma unroll
                 for (int m = 0; m < E; m++) v[m] = __ldcg(&brow[rt + m * T]);
-                fft_line<N, true, 1, 0>(v, xb, 0, rt, g.tw_row);
+                fft_line<N, true, 1, 0, EV>(v, xb, 0, rt, g.tw_row16);
 #pragma unroll
                 for (int m = 0; m < E; m++) stash[rt + m * T] = v[m];
 #pragma unroll
                 for (int m = 0; m < E; m++) v[m] = __ldcg(&wrow[rt + m * T]);
-                fft_line<N, true, 1, 0>(v, xb, 0, rt, g.tw_row);
+                fft_line<N, true, 1, 0, EV>(v, xb, 0, rt, g.tw_row16);
 #pragma unroll
                 for (int m = 0; m < E; m++) v[m] = cmul(v[m], stash[rt + m * T]);
-                fft_line<N, false, 1, 0>(v, xb, 0, rt, g.tw_row);
+                fft_line<N, false, 1, 0, EV>(v, xb, 0, rt, g.tw_row16);
 #pragma unroll
                 for (int m = 0; m < E; m++) wrow[rt + m * T] = v[m];
             }
@@ -141,10 +147,10 @@ k_small_slices(const Geom g, int nslices, int nsl1, const int *__restrict__ slic
             for (int m = 0; m < E; m++) vacc[rt + m * T] = 0.0f;
             __syncwarp();
             const int wx0 = rank * LPC + ((ht >> 5) * C::RW);  // this warp's first row
-            splat_scan_warp<N>(g, atoms, so[k + 1], so[k + 2], wx0, C::RW, row, true, rt, vacc,
-                               s_knots);
+            splat_scan_warp<N, EV>(g, atoms, so[k + 1], so[k + 2], wx0, C::RW, row, true, rt,
+                                   vacc, s_knots);
             float2 v[E];
-            trans_row<N, 0>(g, rt, vacc, xb, v);
+            trans_row<N, 0, EV>(g, rt, vacc, xb, v);
             float2 *arow = Tu[tb_next] + (size_t)row * N;
 #pragma unroll
             for (int m = 0; m < E; m++)
@@ -158,7 +164,7 @@ k_small_slices(const Geom g, int nslices, int nsl1, const int *__restrict__ slic
                 float2 v[E];
 #pragma unroll
                 for (int m = 0; m < E; m++) v[m] = __ldcg(&Wu[(size_t)(ct + m * T) * N + col]);
-                fft_line<N, false, LPC, 2>(v, buf, cc, ct, g.tw_col);
+                fft_line<N, false, LPC, 2, EV>(v, buf, cc, ct, g.tw_col16);
                 const int2 ab = __ldg(&g.kband[col]);
                 const float2 py = __ldg(&g.propy[col]);
 #pragma unroll
@@ -167,7 +173,7 @@ k_small_slices(const Geom g, int nslices, int nsl1, const int *__restrict__ slic
                     v[m] = (ix <= ab.x || ix >= ab.y) ? cmul(cmul(v[m], py), __ldg(&g.propx[ix]))
                                                       : make_float2(0.0f, 0.0f);
                 }
-                fft_line<N, true, LPC, 2>(v, buf, cc, ct, g.tw_col);
+                fft_line<N, true, LPC, 2, EV>(v, buf, cc, ct, g.tw_col16);
 #pragma unroll
                 for (int m = 0; m < E; m++) Wu[(size_t)(ct + m * T) * N + col] = v[m];
             }
@@ -177,14 +183,14 @@ k_small_slices(const Geom g, int nslices, int nsl1, const int *__restrict__ slic
             float2 v[E];
 #pragma unroll
             for (int m = 0; m < E; m++) v[m] = __ldcg(&tu[(size_t)(ct + m * T) * N + col]);
-            fft_line<N, false, LPC, 2>(v, buf, cc, ct, g.tw_col);
+            fft_line<N, false, LPC, 2, EV>(v, buf, cc, ct, g.tw_col16);
             const int2 ab = __ldg(&g.kband[col]);
 #pragma unroll
             for (int m = 0; m < E; m++) {
                 const int ix = ct + m * T;
                 v[m] = (ix <= ab.x || ix >= ab.y) ? cscale(v[m], mask_scale) : make_float2(0.0f, 0.0f);
             }
-            fft_line<N, true, LPC, 2>(v, buf, cc, ct, g.tw_col);
+            fft_line<N, true, LPC, 2, EV>(v, buf, cc, ct, g.tw_col16);
 #pragma unroll
             for (int m = 0; m < E; m++) tu[(size_t)(ct + m * T) * N + col] = v[m];
         }
