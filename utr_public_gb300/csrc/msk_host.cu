@@ -1302,13 +1302,19 @@ int upload_batch(msk_context *ctx, const std::vector<UnitAtoms> &ua, int u0, int
 // square grids of 64^2 to 256^2 in the coherent branch with two transmission
 // buffers, on a device that fits the clusters.  MSK_SMALL_GRID=0 in the
 // environment keeps the launch-per-pass loop (=1: the default).
-static bool small_path(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode)
+static bool small_grid_ok(msk_context *ctx, const GridPre &gp, bool dw, int nmode)
 {
     const char *forced = getenv("MSK_SMALL_GRID");
     if (forced && forced[0] == '0') return false;
     const SizeOps *op = size_ops(gp.nx);
-    return nmode == 0 && b.dw.empty() && gp.nx == gp.ny && op && op->small_slices &&
-           ctx->tbuf2.cap >= ctx->tbuf.cap && ctx->tbuf.cap > 0 && op->small_ok(ctx->device);
+    return nmode == 0 && !dw && gp.nx == gp.ny && op && op->small_slices &&
+           op->small_ok(ctx->device);
+}
+
+static bool small_path(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode)
+{
+    return ctx->tbuf2.cap >= ctx->tbuf.cap && ctx->tbuf.cap > 0 &&
+           small_grid_ok(ctx, gp, !b.dw.empty(), nmode);
 }
 
 int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode, bool w_in_band)
@@ -2758,6 +2764,8 @@ struct SpecPlan {
     size_t o_tab = 0, o_atoms = 0, o_soff = 0, o_act = 0, o_meta = 0, o_w0 = 0;  // upload region
     size_t o_fres = 0, o_psi = 0, o_tbuf = 0, o_img = 0, o_phi = 0, o_fill = 0;  // work region
     size_t o_dw = 0, o_spec = 0;  // Debye-Waller branch: -B/4 per (unit, slice); S(v) grids
+    bool small = false;      // the slice loop as one cluster launch (msk_small.cuh)
+    size_t o_tbuf2 = 0;      // its second transmission buffer
     bool img_dev = false;
     bool img_pinned = false;  // host images in page-locked memory: copied on the lane
     float *ew = nullptr;      // exit waves out (may be null)
@@ -2831,7 +2839,13 @@ int enqueue_specimen(msk_context *ctx, SpecPlan &P, unsigned char *arena, const 
                       st);
     }
     const int nsl1 = P.nslices + 1;
-    for (int sl = 0; sl < P.nslices; sl++) {
+    if (P.small) {  // every slice of every unit in one cluster launch, as run_slices
+        const double ne = P.b.act_off[P.nslices], all = (double)na * P.nslices;
+        Prof p(ctx, kSmall, pl * (64.0 * ne + 16.0 * (all - ne)), st);
+        MSK_CUDA(ctx, cop->small_slices(g, na, P.nslices, nsl1, soff, atoms, psi, tb,
+                                        reinterpret_cast<float2 *>(arena + P.o_tbuf2), st));
+    }
+    for (int sl = 0; sl < (P.small ? 0 : P.nslices); sl++) {
         const int nact = P.b.act_off[sl + 1] - P.b.act_off[sl];
         const int *units = act + P.b.act_off[sl];
         if (nact > 0) {
@@ -3101,6 +3115,9 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
         work += align256((size_t)q.nunits * plane * sizeof(float2));
         q.o_tbuf = work;
         work += align256((size_t)q.nunits * plane * sizeof(float2));
+        q.small = small_grid_ok(ctx, q.gp, !q.b.dw.empty(), s->nmode);
+        q.o_tbuf2 = work;
+        if (q.small) work += align256((size_t)q.nunits * plane * sizeof(float2));
         q.o_img = work;
         if (!q.img_dev) work += align256((size_t)q.nimages * plane * sizeof(float));
         // a rotated or shifted image plane: a real-space scratch grid per unit and
