@@ -290,3 +290,33 @@ def test_tilt_series_pinned_host_output(ctx, msk, nconf, max_batch):
     ctx.tilt_series(s, *atoms, angZ, angY, df, nconfig=nconf, displacements=disp, images=pin)
     torch.cuda.synchronize()
     assert torch.equal(pin, dev.cpu())
+
+
+def test_calculate_reuses_its_grid(ctx, msk, oracle):
+    """Calls on one grid reuse the grid tables of the previous call; a call with
+    other atomic numbers, another grid in between, or a tilt series (which
+    uploads tables of its own) must not leave stale tables behind: every call
+    equals the same call in a fresh context bit for bit."""
+    a = sp.random_specimen(200, 32.0, 4.0, 28.0, 71)
+    b = sp.random_specimen(200, 32.0, 4.0, 28.0, 72)
+    b.Znum[:] = 79  # gold only: another table of potentials
+    p = msk.make_param(32.0, 32.0, 128, 128, 200.0, 1.0)
+    q = msk.make_param(32.0, 32.0, 64, 64, 300.0, 2.0)
+    atoms = lambda s: (s.Znum, s.x, s.y, s.z, s.occ)
+    seq = [(p, a), (p, a), (p, b), (q, a), (p, a), (p, b)]
+    got = []
+    for param, s in seq:
+        got.append(ctx.calculate(param, *atoms(s), 32.0, 32.0))
+        if len(got) == 4:
+            ctx.tilt_series(series(msk, 64, 32.0, 300.0, 2.0), *atoms(a), [0.0], [0.3], [0.0])
+    fresh = msk.Context(0)
+    try:
+        for (param, s), g in zip(seq, got):
+            ref = fresh.calculate(param, *atoms(s), 32.0, 32.0)
+            assert np.array_equal(g.view(np.uint32), ref.view(np.uint32))
+            fresh.close()
+            fresh = msk.Context(0)
+    finally:
+        fresh.close()
+    ref64 = oracle.calculate(p, *atoms(b), 32.0, 32.0, fp64=True)
+    assert rel_l2(got[-1], ref64) < 1e-5

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -117,6 +118,10 @@ struct msk_context {
     std::vector<cudaStream_t> lanes;                  // concurrent specimens of a batch
     std::vector<cudaEvent_t> lane_ev;                 // lane joins (one per lane) + fork
     size_t units_alloc = 0;  // units the psi / tbuf buffers hold
+    // msk_calculate's grid and tables as last uploaded (its grid parameters
+    // and atomic numbers): repeated calls on one grid skip their preparation;
+    // any other upload of the tables clears it
+    std::shared_ptr<void> calc_cache;
     std::vector<int> zmap = std::vector<int>(104, -1);
 };
 

@@ -482,6 +482,14 @@ struct GridPre {
     int band_p = 0, band_q = 0;  // in-band columns: iy <= band_p or iy >= band_q
 };
 
+// msk_calculate's last grid and the atomic numbers of its tables.
+struct CalcCache {
+    std::vector<float> key;
+    std::vector<int> zlist;
+    GridPre gp;
+    const void *tables = nullptr;
+};
+
 static bool grid_pre(GridPre &gp, int nx, int ny, float ax, float by, float v0, float deltaz,
                      float ctiltx, float ctilty)
 {
@@ -1151,6 +1159,7 @@ static void bind_tables(GridPre &gp, const unsigned char *b, const TableLayout &
 // Tables of one grid into the context's table buffer.
 int upload_tables(msk_context *ctx, GridPre &gp, const std::vector<int> &zlist)
 {
+    ctx->calc_cache.reset();  // the tables msk_calculate cached are replaced
     std::vector<unsigned char> host;
     TableLayout o;
     build_tables(gp, zlist, host, o);
@@ -1641,10 +1650,19 @@ int msk_calculate(msk_context *ctx, float *pix, const float *wave0, const float 
     if (!pow2_supported(nx) || !pow2_supported(ny))
         return fail(ctx, MSK_EUNSUPPORTED, "grid must be a power of two from 16 to 4096");
     MSK_CUDA(ctx, cudaSetDevice(ctx->device));
+    // the grid of the previous call, when its parameters are the same (the
+    // reference's per-orientation loop calls calculate() on one grid)
+    const std::vector<float> key = {(float)nx, (float)ny, ax, by, param[MSK_pENERGY],
+                                    param[MSK_pDELTAZ], param[MSK_pXCTILT], param[MSK_pYCTILT]};
+    auto cache = std::static_pointer_cast<CalcCache>(ctx->calc_cache);
+    const bool same_grid = cache && cache->key == key && cache->tables == ctx->tables.p;
     GridPre gp;
-    if (!grid_pre(gp, nx, ny, ax, by, param[MSK_pENERGY], param[MSK_pDELTAZ], param[MSK_pXCTILT],
-                  param[MSK_pYCTILT]))
+    if (same_grid) {
+        gp = cache->gp;
+    } else if (!grid_pre(gp, nx, ny, ax, by, param[MSK_pENERGY], param[MSK_pDELTAZ],
+                         param[MSK_pXCTILT], param[MSK_pYCTILT])) {
         return fail(ctx, MSK_EUNSUPPORTED, "band limit is not two index ranges per column");
+    }
     const int nslices = slice_count(param[MSK_pDELTAZ], ctblengthz);
     std::vector<int> zlist;
     // the reference's range check comes before any atomic-number check
@@ -1676,8 +1694,17 @@ int msk_calculate(msk_context *ctx, float *pix, const float *wave0, const float 
     ps.iseed = iseed;
     prep_unit(gp, ps, ua[0]);
     if (ua[0].status) return fail(ctx, ua[0].status, msk_status_string(ua[0].status));
-    int st = upload_tables(ctx, gp, zlist);
-    if (st) return st;
+    int st = MSK_OK;
+    if (!(same_grid && cache->zlist == zlist)) {
+        st = upload_tables(ctx, gp, zlist);
+        if (st) return st;
+        auto c = std::make_shared<CalcCache>();
+        c->key = key;
+        c->zlist = zlist;
+        c->gp = gp;
+        c->tables = ctx->tables.p;
+        ctx->calc_cache = c;
+    }
     Batch b;
     st = upload_batch(ctx, ua, 0, 1, nslices, b);
     if (st) return st;
