@@ -253,6 +253,14 @@ int msk_calculate_static(void *stream, float *pix, const float *wave0, const flo
                          const float *z, const float *occ, float ctblength, float ctblengthz,
                          int nmode);
 
+/* The schedule the column-pass tuner chose for a grid on a device -- no
+ * counterpart in the reference (whose FFTW planning, cfpix.cpp:225-228, is
+ * internal to FFTW).  pass: 0 band limit, 1 propagator, 2 free-space step,
+ * 3 Debye-Waller damping.  info[0] = variant (MSK_COL_TILE's numbering),
+ * info[1] = points a thread holds in the FFT's first stage (32 or 16),
+ * info[2] = columns per CTA.  MSK_EINVAL until that pass has run on that grid. */
+int msk_column_plan(int device, int nx, int ny, int pass, int *info);
+
 /* Device allocations (cudaMalloc) this library has made in this process so far,
  * over every context -- no counterpart in the reference; lets a caller check
  * that a run of msk_calculate_static calls allocated nothing. */

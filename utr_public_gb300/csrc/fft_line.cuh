@@ -145,13 +145,14 @@ __host__ __device__ __forceinline__ void dft(float2 *v)
 }
 
 // Radix plan per line length.  EV = 0: E = 32 elements per thread (the
-// default plan of every pass); EV = 16: 16 elements per thread, twice the
-// threads per line (lines up to 1024 points), for passes that need more
-// threads per line and fewer registers per thread.
+// default plan of every pass: 1024 = 32 x 32, 2048 = 32 x 8 x 8, ...); EV = 16:
+// 16 elements per thread and twice the threads per line (lines up to 2048
+// points: 256 = 16 x 16, 1024 = 16 x 8 x 8, 2048 = 16 x 16 x 8), for passes
+// that need more threads per line and fewer registers per thread.
 template <int N, int EV = 0>
 struct FftPlan {
     static_assert(N >= 16 && N <= 4096 && (N & (N - 1)) == 0, "line length");
-    static_assert(EV == 0 || (EV == 16 && N >= 16 && N <= 1024), "plan variant");
+    static_assert(EV == 0 || (EV == 16 && N >= 16 && N <= 2048), "plan variant");
     static constexpr int E = EV ? (N >= EV ? EV : N) : (N >= 32 ? 32 : N);  // elements per thread
     static constexpr int T = N / E;              // threads per line
     static constexpr int REST = N / E;

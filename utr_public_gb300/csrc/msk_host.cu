@@ -590,7 +590,7 @@ static bool grid_pre(GridPre &gp, int nx, int ny, float ax, float by, float v0, 
     // column blocks of the column passes (C columns each) holding in-band columns
     g.band_p = gp.band_p;
     g.band_q = gp.band_q;
-    for (int v = 0; v < 2; v++) {
+    for (int v = 0; v < kColVariants; v++) {
         const int C = size_ops(nx)->col_c[v], nblk = ny / C;
         g.cb_lo[v] = std::min(nblk, (gp.band_p + 1 + C - 1) / C);
         g.cb_hi0[v] = std::max(g.cb_lo[v], gp.band_q / C);
@@ -984,11 +984,15 @@ void prof_collect(msk_context *ctx)
 
 namespace {
 
-// The column tile of each pass (ColCfg variant), per device, grid and pass:
-// the first time a pass runs on a grid, both widths run on a scratch grid
-// (three timed launches each, after one untimed) and the faster is kept for the
-// life of the process.  The widths compute every column identically, so the
-// choice changes speed only.  MSK_COL_TILE=0 or 1 in the environment fixes it.
+// The schedule of each column pass (ColCfg variant: FFT plan and tile width),
+// per device, grid and pass, in the manner of FFTW_MEASURE planning
+// (TemsimLibrary/cfpix.cpp:225-228): the first time a pass runs on a grid,
+// every variant with kernels for the line length -- 32 and (64 to 2048 points)
+// 16 points a thread, each at two tile widths -- runs on a scratch grid (three
+// timed launches each, after one untimed) and the fastest is kept for the life
+// of the process (the default unless another gains 3%).  Tile widths compute
+// every column identically; the plans differ by FP32 rounding.  MSK_COL_TILE=
+// 0..3 in the environment fixes the variant (0, 1: 32 points, 2, 3: 16).
 struct ColChoices {
     std::mutex m;
     std::map<std::array<int, 4>, int> v;  // (device, nx, ny, pass) -> variant
@@ -1002,18 +1006,19 @@ ColChoices &col_choices()
 int col_variant(msk_context *ctx, const GridPre &gp, int mode)
 {
     if (ctx->no_tune) return 0;
-    static const char *forced = getenv("MSK_COL_TILE");
-    if (forced && (forced[0] == '0' || forced[0] == '1') && forced[1] == 0) return forced[0] - '0';
+    const SizeOps *cop = size_ops(gp.nx);
+    const char *forced = getenv("MSK_COL_TILE");
+    if (forced && forced[0] >= '0' && forced[0] < '0' + cop->col_nv && forced[1] == 0)
+        return forced[0] - '0';
     const std::array<int, 4> key = {ctx->device, gp.nx, gp.ny, mode};
     ColChoices &cc = col_choices();
     std::lock_guard<std::mutex> lock(cc.m);
     auto it = cc.v.find(key);
     if (it != cc.v.end()) return it->second;
-    const SizeOps *cop = size_ops(gp.nx);
     const size_t plane = (size_t)gp.nx * gp.ny;
     const int U = (int)std::max<size_t>(2, std::min<size_t>(64, ((size_t)256 << 20) / (plane * 8)));
     int choice = 0;
-    float ms[2] = {0.0f, 0.0f};
+    float ms[kColVariants] = {};
     bool ok = ctx->tune.reserve((size_t)(U + 1) * plane * sizeof(float2)) == cudaSuccess &&
               cudaMemsetAsync(ctx->tune.p, 0, (size_t)(U + 1) * plane * sizeof(float2),
                               ctx->stream) == cudaSuccess;
@@ -1025,7 +1030,7 @@ int col_variant(msk_context *ctx, const GridPre &gp, int mode)
     fr.dw = reinterpret_cast<const float *>(grid + (size_t)U * plane);
     fr.dw_stride = 1;
     const Geom &g = gp.g;
-    for (int v = 0; v < 2 && ok; v++) {
+    for (int v = 0; v < cop->col_nv && ok; v++) {
         ColView view;
         if (column_map(ctx, &view, grid, gp.nx, gp.ny, U, cop, v) != MSK_OK) {
             ok = false;
@@ -1049,7 +1054,9 @@ int col_variant(msk_context *ctx, const GridPre &gp, int mode)
     }
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
-    if (ok && ms[1] < 0.97f * ms[0]) choice = 1;  // keep the default unless clearly slower
+    // the fastest variant, unless it gains less than 3% on the default
+    for (int v = 1; ok && v < cop->col_nv; v++)
+        if (ms[v] < 0.97f * ms[0] && ms[v] < ms[choice]) choice = v;
     if (!ok) cudaGetLastError();
     cc.v[key] = choice;
     return choice;
@@ -3177,6 +3184,7 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
             P[i].o_fres += align256(up);
             P[i].o_psi += align256(up);
             P[i].o_tbuf += align256(up);
+            P[i].o_tbuf2 += align256(up);
             P[i].o_img += align256(up);
             P[i].o_phi += align256(up);
             P[i].o_fill += align256(up);
@@ -3488,6 +3496,21 @@ extern "C" int msk_calculate_static(void *stream, float *pix, const float *wave0
                         ctx.stream) != cudaSuccess)
         return MSK_ECUDA;
     return flags_check(&ctx);
+}
+
+extern "C" int msk_column_plan(int device, int nx, int ny, int pass, int *info)
+{
+    if (!info || pass < 0 || pass > 3 || !size_ops(nx)) return MSK_EINVAL;
+    const int modes[4] = {kColMask, kColProp, kColFresnel, kColDW};
+    ColChoices &cc = col_choices();
+    std::lock_guard<std::mutex> lock(cc.m);
+    auto it = cc.v.find(std::array<int, 4>{device, nx, ny, modes[pass]});
+    if (it == cc.v.end()) return MSK_EINVAL;
+    const int v = it->second;
+    info[0] = v;
+    info[1] = v >= 2 ? 16 : std::min(nx, 32);
+    info[2] = size_ops(nx)->col_c[v];
+    return MSK_OK;
 }
 
 extern "C" long long msk_device_allocations(void)

@@ -20,7 +20,8 @@ struct ColView {
 
 struct SizeOps {
     int n;
-    int col_c[2], col_box_rows;  // column tile widths (per variant), TMA box height
+    int col_c[kColVariants], col_box_rows;  // column tile widths per variant, TMA box height
+    int col_nv;                             // variants with kernels (2, or 4 with the 16-point plan)
     void (*splat)(const Geom &, const int *units, int nunits, int slice, int nsl1,
                   const int *slice_off, const SplatAtom *atoms, float2 *tbuf, cudaStream_t);
     // the same splat writing the projected potential of the slice (float) to
@@ -95,7 +96,8 @@ template <int N> struct Smem {
     static constexpr int NTS = RowCfg<N>::L * P::T;
     static constexpr size_t splat = (size_t)RowCfg<N>::L * SplatCfg<N>::SROW * 8 + NTS * 16 +
                                     128 * 4 + ((NTS + 31) / 32 + 1) * 4;
-    template <int V> static constexpr size_t col() { return (size_t)ColCfg<N, V>::C * P::PADN * 8 + 16; }
+    template <int V, int EV = 0>
+    static constexpr size_t col() { return (size_t)ColCfg<N, V, EV>::C * FftPlan<N, EV>::PADN * 8 + 16; }
     static constexpr size_t transmit = (size_t)2 * RowCfg<N>::LT * P::PADN * 8 + 16;
     static constexpr size_t row = (size_t)RowCfg<N>::L * P::PADN * 8;
     static constexpr size_t adj = (size_t)RowCfg<N>::LT * (P::PADN + N) * 8;
@@ -157,28 +159,37 @@ struct Launch {
         k_row_dwexp<N><<<nunits * row_blocks(g, L), L * P::T, Smem<N>::row, s>>>(g, units, spec,
                                                                                 tbuf);
     }
-    template <int MODE, int V>
+    template <int MODE, int V, int EV>
     static void colv(const Geom &g, const CUtensorMap &in, const CUtensorMap &out,
                      const int *units, int nunits, const Fresnel &fr, float scale, int band,
                      cudaStream_t s)
     {
         static std::once_flag f;
-        set_smem(k_col_pass<N, MODE, V>, Smem<N>::template col<V>(), f);
-        const int C = ColCfg<N, V>::C;
-        const int bpu = band ? g.cb_n[V] : g.ny / C;
-        k_col_pass<N, MODE, V><<<nunits * bpu, ColCfg<N, V>::NT, Smem<N>::template col<V>(), s>>>(
-            g, in, out, units, fr, scale, band);
+        constexpr size_t sm = Smem<N>::template col<V, EV>();
+        set_smem(k_col_pass<N, MODE, V, EV>, sm, f);
+        using CC = ColCfg<N, V, EV>;
+        const int vi = V + (EV ? 2 : 0);
+        const int bpu = band ? g.cb_n[vi] : g.ny / CC::C;
+        k_col_pass<N, MODE, V, EV><<<nunits * bpu, CC::NT, sm, s>>>(g, in, out, units, fr, scale,
+                                                                     band);
     }
-    // in and out must be views of the same tile variant (the kernel's box)
+    // in and out must be views of the same variant (the kernel's box)
     template <int MODE>
     static void col(const Geom &g, const ColView &in, const ColView &out, const int *units,
                     int nunits, const Fresnel &fr, float scale, int band, cudaStream_t s)
     {
         if (in.v != out.v) return;
-        if (in.v == 1)
-            colv<MODE, 1>(g, in.map, out.map, units, nunits, fr, scale, band, s);
-        else
-            colv<MODE, 0>(g, in.map, out.map, units, nunits, fr, scale, band, s);
+        switch (in.v) {
+        case 1: colv<MODE, 1, 0>(g, in.map, out.map, units, nunits, fr, scale, band, s); return;
+        case 2:
+        case 3:
+            if constexpr (col_plan16_ok(N)) {
+                if (in.v == 2) colv<MODE, 0, 16>(g, in.map, out.map, units, nunits, fr, scale, band, s);
+                else colv<MODE, 1, 16>(g, in.map, out.map, units, nunits, fr, scale, band, s);
+            }
+            return;
+        default: colv<MODE, 0, 0>(g, in.map, out.map, units, nunits, fr, scale, band, s); return;
+        }
     }
     static void col_mask(const Geom &g, const ColView &in, const ColView &out,
                          const int *units, int nunits, int band, float post, cudaStream_t s)
@@ -360,7 +371,11 @@ struct Launch {
 
     static const SizeOps *ops()
     {
-        static const SizeOps o = {N,        {ColCfg<N, 0>::C, ColCfg<N, 1>::C}, ColCfg<N>::BR, splat,
+        static const SizeOps o = {N,
+                                  {ColCfg<N, 0>::C, ColCfg<N, 1>::C,
+                                   col_plan16_ok(N) ? ColCfg<N, 0, col_plan16_ok(N) ? 16 : 0>::C : ColCfg<N, 0>::C,
+                                   col_plan16_ok(N) ? ColCfg<N, 1, col_plan16_ok(N) ? 16 : 0>::C : ColCfg<N, 1>::C},
+                                  ColCfg<N>::BR, col_plan16_ok(N) ? kColVariants : 2, splat,
                                   splat_potential, splat_spec, col_dw, row_dwexp,
                                   col_mask, col_prop,     col_fresnel,      row_transmit_t<false>,
                                   row_transmit_t<true>,   row_init, row_exit, row_inverse,

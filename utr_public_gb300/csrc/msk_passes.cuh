@@ -145,11 +145,13 @@ template <int NY> struct RowCfg {
     static constexpr int MB = NY <= 1024 ? 3 : 2;
 };
 // Columns per CTA for the column passes, and the TMA boxes of a column tile.
-// Two widths per line length, chosen per pass at run time by timing both
-// (the column tuner of the host code): V = 0 the width that gives a 128-thread
-// CTA (clamped to 2..16), V = 1 half of it, or twice where half would be < 2.
-template <int NX, int V = 0> struct ColCfg {
-    static constexpr int T = FftPlan<NX>::T;
+// Per line length up to four variants, chosen per pass at run time by timing
+// them (the column tuner of the host code): the FFT plan EV (0: 32 points a
+// thread, 16: 16 points a thread), and the tile width V = 0 (the width that
+// gives a 128-thread CTA, clamped to 2..16) or V = 1 (half of it, or twice
+// where half would be < 2).
+template <int NX, int V = 0, int EV = 0> struct ColCfg {
+    static constexpr int T = FftPlan<NX, EV>::T;
     static constexpr int C0 = (128 / T) < 2 ? 2 : ((128 / T) > 16 ? 16 : 128 / T);
     static constexpr int C = V == 0 ? C0 : (C0 / 2 >= 2 ? C0 / 2 : 2 * C0);
     static constexpr int NT = C * T;
@@ -157,6 +159,9 @@ template <int NX, int V = 0> struct ColCfg {
     static constexpr int NBOX = NX / BR;
     static constexpr uint32_t TILE_BYTES = (uint32_t)NX * C * 8;
 };
+// Column-pass variant index: tile width + 2 x plan (16 points a thread).
+constexpr int kColVariants = 4;
+__host__ __device__ constexpr bool col_plan16_ok(int n) { return n >= 64 && n <= 2048; }
 
 // One thread arms the CTA's barrier; everyone waits for the phase with a
 // bound.  On a timeout the flag is raised and every thread returns false.
@@ -177,10 +182,12 @@ __device__ __forceinline__ void cta_drain(uint64_t *bar, uint32_t parity)
 }
 
 // Resident CTAs per SM the column pass is compiled for (its register budget):
-// the propagator pass fits 128 registers, the band-limit and free-space
-// passes need ~168 to stay free of spills at 1024 points.
-template <int NX, int MODE, int V> struct ColMinBlocks {
-    static constexpr int per = (MODE == 1 ? 512 : 384) / ColCfg<NX, V>::NT;
+// with 32 points a thread the propagator pass fits 128 registers, the
+// band-limit and free-space passes need ~168 to stay free of spills at 1024
+// points.
+// With 16 points a thread, five 128-thread CTAs (102 registers).
+template <int NX, int MODE, int V, int EV = 0> struct ColMinBlocks {
+    static constexpr int per = (EV ? 640 : (MODE == 1 ? 512 : 384)) / ColCfg<NX, V, EV>::NT;
     static constexpr int value = per > 0 ? per : 1;
 };
 
@@ -502,14 +509,16 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
 //           spectrum (autoslic.cpp:1098-1106), -B/4 per unit in fr.dw
 enum { kColMask = 0, kColProp = 1, kColFresnel = 2, kColDW = 3 };
 
-template <int NX, int MODE, int V>
-__global__ void __launch_bounds__(ColCfg<NX, V>::NT, ColMinBlocks<NX, MODE, V>::value)
+template <int NX, int MODE, int V, int EV = 0>
+__global__ void __launch_bounds__(ColCfg<NX, V, EV>::NT, ColMinBlocks<NX, MODE, V, EV>::value)
 k_col_pass(const Geom g, const __grid_constant__ CUtensorMap in_map,
            const __grid_constant__ CUtensorMap out_map, const int *__restrict__ units,
            const Fresnel fr, float fscale, int band)
 {
-    using P = FftPlan<NX>;
-    using CC = ColCfg<NX, V>;
+    using P = FftPlan<NX, EV>;
+    using CC = ColCfg<NX, V, EV>;
+    constexpr int VI = V + 2 * (EV ? 1 : 0);  // the variant's index in Geom::cb_*
+    const float2 *tw = EV ? g.tw_col16 : g.tw_col;
     constexpr int T = P::T, E = P::E, C = CC::C;
     extern __shared__ __align__(128) unsigned char smem[];
     float2 *buf = reinterpret_cast<float2 *>(smem);                       // PADN*C
@@ -519,10 +528,10 @@ k_col_pass(const Geom g, const __grid_constant__ CUtensorMap in_map,
     const int ny = g.ny;
     // band mode: only the column blocks that hold in-band columns (the others
     // are zero on input and output)
-    const int bpu = band ? g.cb_n[V] : ny / C;
+    const int bpu = band ? g.cb_n[VI] : ny / C;
     const int u = units ? units[blockIdx.x / bpu] : (int)(blockIdx.x / bpu);
     int cb = blockIdx.x % bpu;
-    if (band && cb >= g.cb_lo[V]) cb = g.cb_hi0[V] + (cb - g.cb_lo[V]);
+    if (band && cb >= g.cb_lo[VI]) cb = g.cb_hi0[VI] + (cb - g.cb_lo[VI]);
     const int iy = cb * C + c;
     // tile = rows u*NX .. u*NX+NX-1, float columns 2*cb*C .. 2*cb*C+2C-1
     if (tid == 0) {
@@ -543,7 +552,7 @@ k_col_pass(const Geom g, const __grid_constant__ CUtensorMap in_map,
     float2 v[E];
 #pragma unroll
     for (int m = 0; m < E; m++) v[m] = buf[(t + m * T) * C + c];
-    fft_line<NX, false, C, true>(v, buf, c, t, g.tw_col);
+    fft_line<NX, false, C, true, EV>(v, buf, c, t, tw);
 
     if constexpr (MODE == kColMask) {
         // the band limit ky2 + kx2 < k2max keeps ix <= A or ix >= B (host-exact)
@@ -577,7 +586,7 @@ k_col_pass(const Geom g, const __grid_constant__ CUtensorMap in_map,
 #pragma unroll
         for (int m = 0; m < E; m++) v[m] = cmul(v[m], __ldg(&tab[(size_t)(t + m * T) * ny]));
     }
-    fft_line<NX, true, C, true>(v, buf, c, t, g.tw_col);
+    fft_line<NX, true, C, true, EV>(v, buf, c, t, tw);
     __syncthreads();  // every thread is done with the exchange layout
 #pragma unroll
     for (int m = 0; m < E; m++) buf[(t + m * T) * C + c] = v[m];

@@ -29,9 +29,9 @@ struct Geom {
     // by the propagator: in band <=> iy <= band_p or iy >= band_q.  Column
     // passes in band mode run only the column blocks [0, cb_lo) and
     // [cb_hi0, ny/C) (C columns per block); cb_n blocks per unit; one set per
-    // column-tile variant.
+    // column-pass variant (tile width and FFT plan).
     int band_p, band_q;
-    int cb_lo[2], cb_hi0[2], cb_n[2];
+    int cb_lo[4], cb_hi0[4], cb_n[4];
     // Row segments [0, seg_e1) and [seg_s2, ny) with even bounds that cover
     // the in-band columns: what a band-mode row pass loads and stores.
     int seg_e1, seg_s2;
