@@ -914,6 +914,7 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 int column_map(msk_context *ctx, ColView *view, void *base, int nx, int ny, size_t units,
                const SizeOps *cop, int v)
 {
+    if (v < 0 || v >= cop->col_nv) return fail(ctx, MSK_EINVAL, "no column-pass variant " + std::to_string(v));
     auto enc = tensor_map_encoder();
     if (!enc) return fail(ctx, MSK_ECUDA, "cuTensorMapEncodeTiled is not available");
     const cuuint64_t dims[2] = {(cuuint64_t)2 * ny, (cuuint64_t)units * nx};
@@ -2316,8 +2317,11 @@ int stack_run(msk_context *ctx, const StackJob &J)
     // one view per grid buffer the column passes touch and tile variant
     const int vmask = col_variant(ctx, gp, kColMask), vprop = col_variant(ctx, gp, kColProp),
               vfres = col_variant(ctx, gp, kColFresnel);
-    std::vector<ColView> maps[2];
-    for (int v = 0; v < 2; v++) {
+    // (views of every variant the tuner chose for these passes; indexed by variant)
+    std::vector<ColView> maps[kColVariants];
+    for (int v : {vmask, vprop, vfres}) {
+        if (v < 0 || v >= cop->col_nv) return fail(ctx, MSK_ECUDA, "column variant out of range");
+        if (!maps[v].empty()) continue;
         maps[v].resize(planes);
         for (int i = 0; i < planes; i++) {
             st = column_map(ctx, &maps[v][i], grid_at(i), nx, ny, B, cop, v);
