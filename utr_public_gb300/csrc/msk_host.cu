@@ -635,6 +635,7 @@ bool twiddles(int n, std::vector<float2> &out, int ev)
         case 256: twiddles_n<256, 16>(out); return true;
         case 512: twiddles_n<512, 16>(out); return true;
         case 1024: twiddles_n<1024, 16>(out); return true;
+        case 2048: twiddles_n<2048, 16>(out); return true;
         default: return false;
         }
     }
@@ -1072,7 +1073,7 @@ struct TableLayout {
 
 // Offsets (256-byte aligned pieces) of the grid tables of an nx x ny grid with
 // nz compact atomic numbers; the 16-point-plan twiddles only for lines of
-// <= 1024 points.  The one formula behind the table upload and the fixed
+// <= 2048 points.  The one formula behind the table upload and the fixed
 // scratch of msk_calculate_static.
 TableLayout layout_tables(int nx, int ny, int nz)
 {

@@ -164,6 +164,7 @@ struct Launch {
                      const int *units, int nunits, const Fresnel &fr, float scale, int band,
                      cudaStream_t s)
     {
+        if (EV && !g.tw_col16) return;  // no table for the plan: nothing may run
         static std::once_flag f;
         constexpr size_t sm = Smem<N>::template col<V, EV>();
         set_smem(k_col_pass<N, MODE, V, EV>, sm, f);

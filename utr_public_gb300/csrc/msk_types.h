@@ -38,7 +38,7 @@ struct Geom {
     const float2 *zeros;  // >= 4096 zero complex values: the source of zero fills
     const float2 *tw_row;  // twiddles for line length ny
     const float2 *tw_col;  // twiddles for line length nx
-    const float2 *tw_row16;  // the same for the 16-points-a-thread plan (null above 1024)
+    const float2 *tw_row16;  // the same for the 16-points-a-thread plan (null above 2048)
     const float2 *tw_col16;
     const float *knots;    // [100] spline knots in r^2
     const float4 *coef;    // [nz][100] spline {y, b, c, d} per compact atomic number
