@@ -1009,12 +1009,12 @@ int col_variant(msk_context *ctx, const GridPre &gp, int mode)
 {
     if (ctx->no_tune) return 0;
     const SizeOps *cop = size_ops(gp.nx);
-    const char *forced = getenv("MSK_COL_TILE");
-    if (forced && forced[0] >= '0' && forced[0] < '0' + cop->col_nv && forced[1] == 0)
-        return forced[0] - '0';
     const std::array<int, 4> key = {ctx->device, gp.nx, gp.ny, mode};
     ColChoices &cc = col_choices();
     std::lock_guard<std::mutex> lock(cc.m);
+    const char *forced = getenv("MSK_COL_TILE");
+    if (forced && forced[0] >= '0' && forced[0] < '0' + cop->col_nv && forced[1] == 0)
+        return cc.v[key] = forced[0] - '0';  // recorded, so msk_column_plan reports it
     auto it = cc.v.find(key);
     if (it != cc.v.end()) return it->second;
     const size_t plane = (size_t)gp.nx * gp.ny;
