@@ -743,7 +743,9 @@ def run_uneven(args, rank, world, local_rank):
         t = timed(lambda: run(True, sel), 1)
         st_ = sum(steps[i] for i in sel)
         per_size[str(n)] = {"specimens": len(sel), "slice_steps": st_, "ms": t,
-                            "slice_steps_per_s": st_ / (t / 1000.0)}
+                            "slice_steps_per_s": st_ / (t / 1000.0),
+                            "column_plans": {p: msk.column_plan(local_rank, n, n, p)
+                                             for p in ("band_limit", "propagate", "free_space")}}
     ctx.profile(True)
     ms_serial = timed(lambda: run(False), 1)
     prof = ctx.profile_read()
@@ -1312,6 +1314,9 @@ def main():
                         "GBps": round(v[2] / (v[1] / 1000.0) / 1e9, 1) if v[1] > 0 else None}
                     for k, v in kernels.items()},
         "per_angle_gpu": per_angle,
+        # the column-pass schedules the tuner chose for this grid (FFT plan, tile)
+        "column_plans": {p: msk.column_plan(local_rank, NX, NX, p)
+                         for p in ("band_limit", "propagate", "free_space")},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "peak_source": peak_kind, "traffic": traffic,
