@@ -80,12 +80,12 @@ struct SizeOps {
                       size_t tstride, float2 *G, double *partial, cudaStream_t);
     // square grids of N <= 256: every slice of every unit in one cluster launch
     // (msk_small.cuh); W holds S(psi) on entry and exit, T0 / T1 scratch of the
-    // same size.  small_ok: whether this device can run the clusters.  Both
-    // null for other sizes.
+    // same size.  small_ok: how many of its clusters the device runs at once
+    // (0: none fit).  Both null for other sizes.
     cudaError_t (*small_slices)(const Geom &, int nunits, int nslices, int nsl1,
                                 const int *slice_off, const SplatAtom *atoms, float2 *W,
                                 float2 *T0, float2 *T1, cudaStream_t);
-    bool (*small_ok)(int device);
+    int (*small_ok)(int device);  // clusters of this size active at once (0: none fit)
 };
 
 // Line lengths with kernels: 16 .. 4096, powers of two.
@@ -346,27 +346,32 @@ struct Launch {
             return cudaErrorNotSupported;
         }
     }
-    // at least one cluster fits on the device (cluster size and shared memory)
-    static bool small_ok(int device)
+    // clusters the device runs at once (cluster size and shared memory), 0 if none fit
+    static int small_ok(int device)
     {
         if constexpr (N >= 64 && N <= 256) {
             static std::mutex m;
-            static int known[64] = {};  // 0 unknown, 1 yes, 2 no
-            if (device < 0 || device >= 64) return false;
+            static int known[64];  // -1 unknown
+            static bool init = false;
+            if (device < 0 || device >= 64) return 0;
             std::lock_guard<std::mutex> lk(m);
-            if (!known[device]) {
+            if (!init) {
+                for (int &k : known) k = -1;
+                init = true;
+            }
+            if (known[device] < 0) {
                 small_attrs();
                 cudaLaunchAttribute at[1];
                 cudaLaunchConfig_t cfg = small_cfg(1, nullptr, at);
                 int n = 0;
                 const cudaError_t e = cudaOccupancyMaxActiveClusters(&n, k_small_slices<N>, &cfg);
                 if (e != cudaSuccess) cudaGetLastError();
-                known[device] = (e == cudaSuccess && n > 0) ? 1 : 2;
+                known[device] = e == cudaSuccess ? n : 0;
             }
-            return known[device] == 1;
+            return known[device];
         } else {
             (void)device;
-            return false;
+            return 0;
         }
     }
 
