@@ -174,7 +174,8 @@ def run_other_configs(timeout_s=600):
                 "metric": d.get("metric"), "value": d.get("value"), "unit": d.get("unit"),
                 "ms_per_step": d.get("ms_per_step"), "steps": d.get("steps"),
                 "warmup": d.get("warmup"), "workload": (d.get("config") or {}).get("workload"),
-                "e2e": {"value": e2e.get("value"), "ms_per_step": e2e.get("ms_per_step")},
+                "e2e": {k: e2e.get(k) for k in ("value", "ms_per_step", "h2d_GBps", "d2h_GBps",
+                                                "copies_alone_ms") if k in e2e},
                 "roofline": {"kernel": roof.get("kernel"), "frac": roof.get("frac"),
                              "achieved": roof.get("achieved"), "unit": roof.get("unit")},
                 "gpu_launches": d.get("gpu_launches"), "clocks": d.get("clocks"),
@@ -419,6 +420,20 @@ def run_adjoint(args, rank, world, local_rank):
     h2d = prof_e2e.get("copy_h2d", (0, 0.0, 0.0))[2]
     d2h = prof_e2e.get("copy_d2h", (0, 0.0, 0.0))[2]
     same = bool(torch.equal(hg, grad.cpu())) if rank == 0 else None
+
+    # the host link alone on the same buffers (one step's copies, serialised): what
+    # bounds the e2e figure when the host side is slow (these page-locked
+    # buffers sit in the Grace host's memory, shared with the machine's other jobs)
+    def link_ms(dst, src):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        with torch.cuda.stream(stream):
+            dst.copy_(src, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+    ms_h2d, ms_d2h = link_ms(v, hv), link_ms(hg, grad)
     kernels = {k: x for k, x in prof.items() if not k.startswith("copy_")}
     launches = int(sum(x[0] for x in kernels.values())) * args.steps
     dom = max(kernels, key=lambda k: kernels[k][1])
@@ -475,7 +490,10 @@ def run_adjoint(args, rank, world, local_rank):
         "loss": loss_dev,
         "e2e": {"value": world * steps_per / (ms_e2e / 1000.0), "unit": UNIT,
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "ms_per_step": ms_e2e, "matches_device_output": same},
+                "ms_per_step": ms_e2e, "matches_device_output": same,
+                "h2d_GBps": round(hv.numel() * 4 / ms_h2d / 1e6, 1),
+                "d2h_GBps": round(hg.numel() * 4 / ms_d2h / 1e6, 1),
+                "copies_alone_ms": round(ms_h2d + ms_d2h, 2)},
         "gpu_launches": launches * world,
         "ms_per_step_serialized": ms_serial,
         "kernels": {k: {"launches": x[0], "ms": round(x[1], 3),
@@ -745,7 +763,8 @@ def run_uneven(args, rank, world, local_rank):
         per_size[str(n)] = {"specimens": len(sel), "slice_steps": st_, "ms": t,
                             "slice_steps_per_s": st_ / (t / 1000.0),
                             "column_plans": {p: msk.column_plan(local_rank, n, n, p)
-                                             for p in ("band_limit", "propagate", "free_space")}}
+                                             for p in ("band_limit", "propagate", "free_space")},
+                            "row_plans": {"transmit": msk.row_plan(local_rank, n, n)}}
     ctx.profile(True)
     ms_serial = timed(lambda: run(False), 1)
     prof = ctx.profile_read()
@@ -1317,6 +1336,8 @@ def main():
         # the column-pass schedules the tuner chose for this grid (FFT plan, tile)
         "column_plans": {p: msk.column_plan(local_rank, NX, NX, p)
                          for p in ("band_limit", "propagate", "free_space")},
+        # and the transmit's (its row FFT plan)
+        "row_plans": {"transmit": msk.row_plan(local_rank, NX, NX)},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "peak_source": peak_kind, "traffic": traffic,

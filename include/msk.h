@@ -261,6 +261,14 @@ int msk_calculate_static(void *stream, float *pix, const float *wave0, const flo
  * info[2] = columns per CTA.  MSK_EINVAL until that pass has run on that grid. */
 int msk_column_plan(int device, int nx, int ny, int pass, int *info);
 
+/* The schedule the row tuner chose for a grid on a device -- no counterpart in
+ * the reference (FFTW planning, as above).  pass: 0 the transmit (the wave's
+ * and the transmission's row transforms and their product; both the wave and
+ * the scattered form).  info[0] = variant (MSK_ROW_PLAN's numbering: 0 = 32
+ * points a thread, 1 = 16), info[1] = points a thread, info[2] = rows per CTA.
+ * MSK_EINVAL until the transmit has run on that grid. */
+int msk_row_plan(int device, int nx, int ny, int pass, int *info);
+
 /* Device allocations (cudaMalloc) this library has made in this process so far,
  * over every context -- no counterpart in the reference; lets a caller check
  * that a run of msk_calculate_static calls allocated nothing. */

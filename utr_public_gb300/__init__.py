@@ -32,7 +32,7 @@ EXPORTS = ("msk_create", "msk_destroy", "msk_last_error", "msk_status_string", "
            "msk_tilt_series_planes", "msk_utr_depth", "msk_utr_reconstruct",
            "msk_utr_reconstruct_planes", "msk_utr_grid",
            "msk_utr_ctf_correction3d", "msk_utr_inverse_mlaplacian3d",
-           "msk_device_allocations", "msk_column_plan")
+           "msk_device_allocations", "msk_column_plan", "msk_row_plan")
 MSK_BATCH_GRAPH = 1
 
 
@@ -171,6 +171,7 @@ def load():
     L.msk_calculate_static.argtypes = [vp, vp, vp, _fp, C.c_int, vp, vp, vp, vp, vp, C.c_float,
                                        C.c_float, C.c_int]
     L.msk_column_plan.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]
+    L.msk_row_plan.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]
     L.msk_device_allocations.argtypes = []
     L.msk_device_allocations.restype = C.c_longlong
     L.msk_stack_images.argtypes = [vp, C.POINTER(Stack), C.c_int, vp, C.c_int, vp, vp]
@@ -331,6 +332,20 @@ def column_plan(device, nx, ny, pass_):
     if load().msk_column_plan(device, nx, ny, p, info) != 0:
         return None
     return {"variant": info[0], "points_per_thread": info[1], "columns_per_cta": info[2]}
+
+
+ROW_PASSES = ("transmit",)
+
+
+def row_plan(device, nx, ny, pass_="transmit"):
+    """The transmit schedule the row tuner chose on `device` for an nx x ny grid:
+    {"variant", "points_per_thread", "rows_per_cta"}, or None before the
+    transmit has run on that grid (msk_row_plan)."""
+    info = (C.c_int * 3)()
+    p = ROW_PASSES.index(pass_) if isinstance(pass_, str) else int(pass_)
+    if load().msk_row_plan(device, nx, ny, p, info) != 0:
+        return None
+    return {"variant": info[0], "points_per_thread": info[1], "rows_per_cta": info[2]}
 
 
 def device_allocations():

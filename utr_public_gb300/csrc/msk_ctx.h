@@ -110,9 +110,9 @@ struct msk_context {
     msk::DevBuf arena;                                // specimen batches
     msk::DevBuf dwbuf;                                // Debye-Waller -B/4 per (unit, slice)
     msk::DevBuf imgfill;                              // image-plane fill values per unit
-    msk::DevBuf tune;                                 // scratch grid of the column tuner
+    msk::DevBuf tune;                                 // scratch grids of the schedule tuners
     msk::DevBuf utr_img, utr_k2, utr_acc, utr_vol, utr_out, utr_tab, utr_stage;  // UTR reconstruction
-    bool no_tune = false;                             // column tiles fixed at variant 0
+    bool no_tune = false;                             // schedules fixed at variant 0
     cudaEvent_t stk_ev[7] = {};                       // potential stacks: copy / kernel handoffs
     std::vector<cudaEvent_t> stk_sev;                 // the same per slice (2 per slice)
     std::vector<cudaStream_t> lanes;                  // concurrent specimens of a batch

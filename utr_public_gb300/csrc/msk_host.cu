@@ -1064,6 +1064,65 @@ int col_variant(msk_context *ctx, const GridPre &gp, int mode)
     return choice;
 }
 
+// The transmit's schedule (TrCfg: 32 or, for 64 to 2048 points, 16 points a
+// thread), chosen per device and grid the way the column passes' is: the
+// first time the transmit runs on a grid both schedules run on a scratch grid
+// (three timed launches each, after one untimed) and the faster is kept for
+// the process (the default unless the other gains 3%).  The two differ by
+// FP32 rounding (another radix split of the same transforms).  MSK_ROW_PLAN=
+// 0 or 1 in the environment fixes it.  The wave and scattered forms share it.
+struct RowChoices {
+    std::mutex m;
+    std::map<std::array<int, 3>, int> v;  // (device, nx, ny) -> variant
+};
+RowChoices &row_choices()
+{
+    static RowChoices c;
+    return c;
+}
+
+int row_variant(msk_context *ctx, const GridPre &gp)
+{
+    if (ctx->no_tune) return 0;
+    const SizeOps *rop = size_ops(gp.ny);
+    const std::array<int, 3> key = {ctx->device, gp.nx, gp.ny};
+    RowChoices &rc = row_choices();
+    std::lock_guard<std::mutex> lock(rc.m);
+    const char *forced = getenv("MSK_ROW_PLAN");
+    if (forced && forced[0] >= '0' && forced[0] < '0' + rop->row_nv && forced[1] == 0)
+        return rc.v[key] = forced[0] - '0';  // recorded, so msk_row_plan reports it
+    auto it = rc.v.find(key);
+    if (it != rc.v.end()) return it->second;
+    if (rop->row_nv < 2) return rc.v[key] = 0;
+    const size_t plane = (size_t)gp.nx * gp.ny;
+    const int U = (int)std::max<size_t>(2, std::min<size_t>(32, ((size_t)128 << 20) / (plane * 8)));
+    int choice = 0;
+    float ms[kRowVariants] = {};
+    bool ok = ctx->tune.reserve((size_t)2 * U * plane * sizeof(float2)) == cudaSuccess &&
+              cudaMemsetAsync(ctx->tune.p, 0, (size_t)2 * U * plane * sizeof(float2),
+                              ctx->stream) == cudaSuccess;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ok = ok && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess;
+    float2 *tb = ctx->tune.as<float2>(), *psi = tb + (size_t)U * plane;
+    for (int v = 0; v < rop->row_nv && ok; v++) {
+        auto launch = [&] { rop->row_transmit(gp.g, nullptr, U, tb, psi, psi, 1.0f, 1, v, ctx->stream); };
+        launch();
+        ok = cudaEventRecord(e0, ctx->stream) == cudaSuccess;
+        for (int r = 0; r < 3; r++) launch();
+        ok = ok && cudaEventRecord(e1, ctx->stream) == cudaSuccess &&
+             cudaEventSynchronize(e1) == cudaSuccess &&
+             cudaEventElapsedTime(&ms[v], e0, e1) == cudaSuccess &&
+             cudaGetLastError() == cudaSuccess;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    for (int v = 1; ok && v < rop->row_nv; v++)
+        if (ms[v] < 0.97f * ms[0] && ms[v] < ms[choice]) choice = v;
+    if (!ok) cudaGetLastError();
+    rc.v[key] = choice;
+    return choice;
+}
+
 // Device tables of one grid (frequency grids, propagator, twiddles, potential
 // spline, band-limit ranges) laid out in one block of 256-byte aligned pieces.
 struct TableLayout {
@@ -1368,6 +1427,7 @@ int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode, b
     const int nsl1 = b.nslices + 1;
     ColView tmaps[2], pmap;
     const int vm = col_variant(ctx, gp, kColMask), vp = col_variant(ctx, gp, kColProp);
+    const int rv = row_variant(ctx, gp);
     int st = column_map(ctx, &tmaps[0], tbs[0], gp.nx, gp.ny, ctx->units_alloc, cop, vm);
     if (st) return st;
     st = column_map(ctx, &tmaps[1], tbs[1], gp.nx, gp.ny, ctx->units_alloc, cop, vm);
@@ -1424,7 +1484,8 @@ int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode, b
             }
             {
                 Prof p(ctx, kTransmit, 24.0 * plane * na, sB);
-                rop->row_transmit(g, units, na, tb, psi, psi, 1.0f, nmode == 0 && w_in_band, sB);
+                rop->row_transmit(g, units, na, tb, psi, psi, 1.0f, nmode == 0 && w_in_band, rv,
+                                  sB);
             }
             if (overlap) {
                 MSK_CUDA(ctx, cudaEventRecord(ctx->ev_free[k], sB));
@@ -2321,7 +2382,7 @@ int stack_run(msk_context *ctx, const StackJob &J)
     const SizeOps *rop = size_ops(ny), *cop = size_ops(nx);
     // one view per grid buffer the column passes touch and tile variant
     const int vmask = col_variant(ctx, gp, kColMask), vprop = col_variant(ctx, gp, kColProp),
-              vfres = col_variant(ctx, gp, kColFresnel);
+              vfres = col_variant(ctx, gp, kColFresnel), rv = row_variant(ctx, gp);
     // (views of every variant the tuner chose for these passes; indexed by variant)
     std::vector<ColView> maps[kColVariants];
     for (int v : {vmask, vprop, vfres}) {
@@ -2405,7 +2466,7 @@ int stack_run(msk_context *ctx, const StackJob &J)
         auto step = [&](const float2 *tb, const float2 *in, float2 *out) {
             {
                 Prof p(ctx, kTransmit, 24.0 * P * nb);
-                rop->row_transmit_scat(g, nullptr, nb, tb, in, out, tscale, 1, ctx->stream);
+                rop->row_transmit_scat(g, nullptr, nb, tb, in, out, tscale, 1, rv, ctx->stream);
             }
             Prof p(ctx, kKColProp, 16.0 * P * nb);
             cop->col_prop(g, map_of(out, vprop), map_of(out, vprop), nullptr, nb, 1,
@@ -2853,7 +2914,7 @@ int enqueue_specimen(msk_context *ctx, SpecPlan &P, unsigned char *arena, const 
     const SplatAtom *atoms = reinterpret_cast<const SplatAtom *>(arena + P.o_atoms);
     // views for each pass's tile variant (chosen before any capture begins)
     const int vm = col_variant(ctx, gp, kColMask), vp = col_variant(ctx, gp, kColProp),
-              vf = col_variant(ctx, gp, kColFresnel);
+              vf = col_variant(ctx, gp, kColFresnel), rv = row_variant(ctx, gp);
     ColView pmap, tmap, pmapf, tmapf, smap;
     int rc = column_map(ctx, &pmap, psi, nx, ny, na, cop, vp);
     if (rc) return rc;
@@ -2913,7 +2974,8 @@ int enqueue_specimen(msk_context *ctx, SpecPlan &P, unsigned char *arena, const 
                 cop->col_mask(g, tmap, tmap, units, nact, 1, 1.0f / ((float)ny * (float)ny), st);
             }
             Prof p(ctx, kTransmit, 24.0 * pl * nact, st);
-            rop->row_transmit(g, units, nact, tb, psi, psi, 1.0f, s->nmode == 0 && w_in_band, st);
+            rop->row_transmit(g, units, nact, tb, psi, psi, 1.0f, s->nmode == 0 && w_in_band, rv,
+                              st);
         }
         if (s->nmode == 0) {
             Prof p(ctx, kKColProp, 16.0 * pl * na, st);
@@ -3249,10 +3311,12 @@ extern "C" int msk_tilt_series_batch(msk_context *ctx, const msk_series *s, int 
             load[l] += P[i].work;
             lane_of[l].push_back(i);
         }
-        // the column tuner runs launches of its own: settle every choice first
-        for (int i = first; i < last; i++)
+        // the tuners run launches of their own: settle every choice first
+        for (int i = first; i < last; i++) {
             for (int mode : {(int)kColMask, (int)kColProp, (int)kColFresnel, (int)kColDW})
                 (void)col_variant(ctx, P[i].gp, mode);
+            (void)row_variant(ctx, P[i].gp);
+        }
         cudaGraph_t gr = nullptr;
         if (graph)
             MSK_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed));
@@ -3441,7 +3505,7 @@ extern "C" int msk_calculate_static(void *stream, float *pix, const float *wave0
     msk_context ctx;
     ctx.device = dev;
     ctx.stream = (cudaStream_t)stream;
-    ctx.no_tune = true;  // the tuner would allocate: the default column tiles
+    ctx.no_tune = true;  // the tuners would allocate: the default schedules
     unsigned char *base = static_cast<unsigned char *>(scratch);
     auto view = [&](DevBuf &b, size_t off, size_t bytes) { b.borrow(base + off, bytes); };
     view(ctx.psi, kOffPsi, kSGrid);
@@ -3519,6 +3583,20 @@ extern "C" int msk_column_plan(int device, int nx, int ny, int pass, int *info)
     info[0] = v;
     info[1] = v >= 2 ? 16 : std::min(nx, 32);
     info[2] = size_ops(nx)->col_c[v];
+    return MSK_OK;
+}
+
+extern "C" int msk_row_plan(int device, int nx, int ny, int pass, int *info)
+{
+    if (!info || pass != 0 || !size_ops(ny)) return MSK_EINVAL;
+    RowChoices &rc = row_choices();
+    std::lock_guard<std::mutex> lock(rc.m);
+    auto it = rc.v.find(std::array<int, 3>{device, nx, ny});
+    if (it == rc.v.end()) return MSK_EINVAL;
+    const int v = it->second;
+    info[0] = v;
+    info[1] = v == 1 ? 16 : std::min(ny, 32);
+    info[2] = std::max(1, 128 / (ny / info[1]));
     return MSK_OK;
 }
 

@@ -144,6 +144,20 @@ template <int NY> struct RowCfg {
     // (80 registers a thread at 256 threads); fewer where that would spill
     static constexpr int MB = NY <= 1024 ? 3 : 2;
 };
+// The transmit's schedules, chosen per row length at run time by timing them
+// (the row tuner of the host code): EV = 0 (32 points a thread, three
+// resident 128-thread CTAs per SM) or, for 64 to 2048 points, EV = 16 (16
+// points a thread, four CTAs: 128 registers; a 2048-point row is one CTA of
+// 128 threads instead of two rows of 64).
+constexpr int kRowVariants = 2;
+__host__ __device__ constexpr bool row_plan16_ok(int n) { return n >= 64 && n <= 2048; }
+template <int NY, int EV = 0> struct TrCfg {
+    using P = FftPlan<NY, EV>;
+    static constexpr int T = P::T;
+    static constexpr int LT = (128 / T) > 0 ? 128 / T : 1;  // rows per CTA
+    static constexpr bool BLK = T > 32;
+    static constexpr int MB = EV ? 4 : 3;
+};
 // Columns per CTA for the column passes, and the TMA boxes of a column tile.
 // Per line length up to four variants, chosen per pass at run time by timing
 // them (the column tuner of the host code): the FFT plan EV (0: 32 points a
@@ -606,14 +620,16 @@ k_col_pass(const Geom g, const __grid_constant__ CUtensorMap in_map,
 // (cfpix.cpp:349-372) between the transmission's and the wave's row
 // transforms.  `out` may be `psi` (in place).  SCAT: the scattered form,
 // W = S(phi), B = S(tau_bl), out = S(phi + tau + phi tau) * out_scale * ny.
-template <int NY, bool SCAT = false>
-__global__ void __launch_bounds__(RowCfg<NY>::LT * FftPlan<NY>::T, 3)
+// EV: the line FFT plan (TrCfg).
+template <int NY, bool SCAT = false, int EV = 0>
+__global__ void __launch_bounds__(TrCfg<NY, EV>::LT * TrCfg<NY, EV>::T, TrCfg<NY, EV>::MB)
 k_row_transmit(const Geom g, const int *__restrict__ units, const float2 *__restrict__ tbuf,
                const float2 *psi, float2 *out, float out_scale, int band)
 {
-    using P = FftPlan<NY>;
-    constexpr int T = P::T, E = P::E, L = RowCfg<NY>::LT;
-    constexpr bool BLK = RowCfg<NY>::BLK;
+    using P = FftPlan<NY, EV>;
+    constexpr int T = P::T, E = P::E, L = TrCfg<NY, EV>::LT;
+    constexpr bool BLK = TrCfg<NY, EV>::BLK;
+    const float2 *tw = EV ? g.tw_row16 : g.tw_row;
     extern __shared__ __align__(128) unsigned char smem[];
     float2 *bufB = reinterpret_cast<float2 *>(smem);   // transmission rows, then t_bl
     float2 *bufW = bufB + L * P::PADN;                  // wave rows
@@ -665,19 +681,19 @@ k_row_transmit(const Geom g, const int *__restrict__ units, const float2 *__rest
 #pragma unroll
     for (int m = 0; m < E; m++) v[m] = bufB[l * NY + t + m * T];
     __syncthreads();  // dense rows read before any line's exchange overwrites them
-    fft_line<NY, true, 1, BLK>(v, bufB + l * P::PADN, 0, t, g.tw_row);
+    fft_line<NY, true, 1, BLK, EV>(v, bufB + l * P::PADN, 0, t, tw);
     __syncthreads();
 #pragma unroll
     for (int m = 0; m < E; m++) bufB[l * NY + t + m * T] = v[m];  // t_bl, own elements only
 #pragma unroll
     for (int m = 0; m < E; m++) v[m] = bufW[l * NY + t + m * T];
     __syncthreads();
-    fft_line<NY, true, 1, BLK>(v, bufW + l * P::PADN, 0, t, g.tw_row);
+    fft_line<NY, true, 1, BLK, EV>(v, bufW + l * P::PADN, 0, t, tw);
 #pragma unroll
     for (int m = 0; m < E; m++)
         v[m] = SCAT ? scat_transmit(v[m], bufB[l * NY + t + m * T], 1.0f / (float)NY)
                     : cmul(v[m], bufB[l * NY + t + m * T]);
-    fft_line<NY, false, 1, BLK>(v, bufW + l * P::PADN, 0, t, g.tw_row);
+    fft_line<NY, false, 1, BLK, EV>(v, bufW + l * P::PADN, 0, t, tw);
     __syncthreads();
     if (out_scale == 1.0f) {  // the scale already carried by B (no multiply)
 #pragma unroll
