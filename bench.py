@@ -174,8 +174,7 @@ def run_other_configs(timeout_s=600):
                 "metric": d.get("metric"), "value": d.get("value"), "unit": d.get("unit"),
                 "ms_per_step": d.get("ms_per_step"), "steps": d.get("steps"),
                 "warmup": d.get("warmup"), "workload": (d.get("config") or {}).get("workload"),
-                "e2e": {k: e2e.get(k) for k in ("value", "ms_per_step", "h2d_GBps", "d2h_GBps",
-                                                "copies_alone_ms") if k in e2e},
+                "e2e": {"value": e2e.get("value"), "ms_per_step": e2e.get("ms_per_step")},
                 "roofline": {"kernel": roof.get("kernel"), "frac": roof.get("frac"),
                              "achieved": roof.get("achieved"), "unit": roof.get("unit")},
                 "gpu_launches": d.get("gpu_launches"), "clocks": d.get("clocks"),
@@ -420,20 +419,6 @@ def run_adjoint(args, rank, world, local_rank):
     h2d = prof_e2e.get("copy_h2d", (0, 0.0, 0.0))[2]
     d2h = prof_e2e.get("copy_d2h", (0, 0.0, 0.0))[2]
     same = bool(torch.equal(hg, grad.cpu())) if rank == 0 else None
-
-    # the host link alone on the same buffers (one step's copies, serialised): what
-    # bounds the e2e figure when the host side is slow (these page-locked
-    # buffers sit in the Grace host's memory, shared with the machine's other jobs)
-    def link_ms(dst, src):
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        with torch.cuda.stream(stream):
-            dst.copy_(src, non_blocking=True)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        return e0.elapsed_time(e1)
-    ms_h2d, ms_d2h = link_ms(v, hv), link_ms(hg, grad)
     kernels = {k: x for k, x in prof.items() if not k.startswith("copy_")}
     launches = int(sum(x[0] for x in kernels.values())) * args.steps
     dom = max(kernels, key=lambda k: kernels[k][1])
@@ -490,10 +475,7 @@ def run_adjoint(args, rank, world, local_rank):
         "loss": loss_dev,
         "e2e": {"value": world * steps_per / (ms_e2e / 1000.0), "unit": UNIT,
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "ms_per_step": ms_e2e, "matches_device_output": same,
-                "h2d_GBps": round(hv.numel() * 4 / ms_h2d / 1e6, 1),
-                "d2h_GBps": round(hg.numel() * 4 / ms_d2h / 1e6, 1),
-                "copies_alone_ms": round(ms_h2d + ms_d2h, 2)},
+                "ms_per_step": ms_e2e, "matches_device_output": same},
         "gpu_launches": launches * world,
         "ms_per_step_serialized": ms_serial,
         "kernels": {k: {"launches": x[0], "ms": round(x[1], 3),

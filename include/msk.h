@@ -265,7 +265,8 @@ int msk_column_plan(int device, int nx, int ny, int pass, int *info);
  * the reference (FFTW planning, as above).  pass: 0 the transmit (the wave's
  * and the transmission's row transforms and their product; both the wave and
  * the scattered form).  info[0] = variant (MSK_ROW_PLAN's numbering: 0 = 32
- * points a thread, 1 = 16), info[1] = points a thread, info[2] = rows per CTA.
+ * points a thread in 64-thread CTAs, 1 = 32 points in 128-thread CTAs, 2 = 16
+ * points in 128-thread CTAs), info[1] = points a thread, info[2] = rows per CTA.
  * MSK_EINVAL until the transmit has run on that grid. */
 int msk_row_plan(int device, int nx, int ny, int pass, int *info);
 

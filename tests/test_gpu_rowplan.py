@@ -1,8 +1,10 @@
 """The transmit's schedules (chosen per grid by timing at run time: the row
-FFT plan, 32 or 16 points a thread).  A tilt series run with each schedule
-forced (MSK_ROW_PLAN) in its own process and with the tuner's choice: every
-one matches the FP64 oracle within 1e-5, the two plans agree with each other
-to FP32 rounding, and the tuner reports the schedule it ran (msk_row_plan).
+FFT plan, 32 or 16 points a thread, and the CTA width).  A tilt series run
+with each schedule forced (MSK_ROW_PLAN) in its own process and with the
+tuner's choice: every one matches the FP64 oracle within 1e-5, the two CTA
+widths of the 32-point plan compute every row identically (bit for bit), the
+two plans agree to FP32 rounding, and the tuner reports the schedule it ran
+(msk_row_plan).
 Grids of 512^2 and up run the launch-per-pass slice loop, so every slice
 takes the transmit."""
 import concurrent.futures as cf
@@ -58,14 +60,18 @@ def run(tmp_path, variant):
 def test_transmit_schedules(tmp_path, oracle):
     from oracle.oracle import SeriesParams
     from utr_public_gb300 import specimen as sp
-    res = {v: run(tmp_path, v) for v in (0, 1, None)}
+    res = {v: run(tmp_path, v) for v in (0, 1, 2, None)}
+    for k in res[0][0].files:
+        assert np.array_equal(res[0][0][k].view(np.uint32), res[1][0][k].view(np.uint32)), k
     for n, _ in CASES:
         assert res[0][1][str(n)] == {"variant": 0, "points_per_thread": 32,
+                                     "rows_per_cta": max(1, 64 // (n // 32))}, n
+        assert res[1][1][str(n)] == {"variant": 1, "points_per_thread": 32,
                                      "rows_per_cta": max(1, 128 // (n // 32))}, n
-        assert res[1][1][str(n)]["variant"] == 1 and res[1][1][str(n)]["points_per_thread"] == 16, n
-        assert res[None][1][str(n)]["variant"] in (0, 1), n
+        assert res[2][1][str(n)]["variant"] == 2 and res[2][1][str(n)]["points_per_thread"] == 16, n
+        assert res[None][1][str(n)]["variant"] in (0, 1, 2), n
         # another radix split of the same transforms: FP32 rounding apart
-        assert rel_l2(res[1][0]["ew%d" % n], res[0][0]["ew%d" % n]) < 5e-6, n
+        assert rel_l2(res[2][0]["ew%d" % n], res[0][0]["ew%d" % n]) < 5e-6, n
 
     def ref(job):
         n, fov, a = job
@@ -82,7 +88,7 @@ def test_transmit_schedules(tmp_path, oracle):
     with cf.ThreadPoolExecutor(8) as ex:
         refs = list(ex.map(ref, jobs))
     for (n, fov, a), img, ew in refs:
-        for v in (0, 1, None):
+        for v in (0, 2, None):
             got = res[v][0]
             assert rel_l2(got["ew%d" % n][a, 0], ew) < 1e-5, (n, a, v)
             for d in range(2):

@@ -1064,13 +1064,15 @@ int col_variant(msk_context *ctx, const GridPre &gp, int mode)
     return choice;
 }
 
-// The transmit's schedule (TrCfg: 32 or, for 64 to 2048 points, 16 points a
-// thread), chosen per device and grid the way the column passes' is: the
-// first time the transmit runs on a grid both schedules run on a scratch grid
-// (three timed launches each, after one untimed) and the faster is kept for
-// the process (the default unless the other gains 3%).  The two differ by
-// FP32 rounding (another radix split of the same transforms).  MSK_ROW_PLAN=
-// 0 or 1 in the environment fixes it.  The wave and scattered forms share it.
+// The transmit's schedule (TrCfg: the FFT plan, 32 or, for 64 to 2048 points,
+// 16 points a thread, and the CTA width), chosen per device and grid the way
+// the column passes' is: the first time the transmit runs on a grid every
+// schedule runs on a scratch grid (three timed launches each, after one
+// untimed) and the fastest is kept for the process (the default unless
+// another gains 3%).  The two widths of one plan compute every row
+// identically; the plans differ by FP32 rounding (another radix split of the
+// same transforms).  MSK_ROW_PLAN=0..2 in the environment fixes it.  The wave
+// and scattered forms share it.
 struct RowChoices {
     std::mutex m;
     std::map<std::array<int, 3>, int> v;  // (device, nx, ny) -> variant
@@ -3595,8 +3597,8 @@ extern "C" int msk_row_plan(int device, int nx, int ny, int pass, int *info)
     if (it == rc.v.end()) return MSK_EINVAL;
     const int v = it->second;
     info[0] = v;
-    info[1] = v == 1 ? 16 : std::min(ny, 32);
-    info[2] = std::max(1, 128 / (ny / info[1]));
+    info[1] = v == 2 ? 16 : std::min(ny, 32);
+    info[2] = std::max(1, (v == 0 ? 64 : 128) / (ny / info[1]));
     return MSK_OK;
 }
 

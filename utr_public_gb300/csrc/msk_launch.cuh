@@ -22,7 +22,7 @@ struct SizeOps {
     int n;
     int col_c[kColVariants], col_box_rows;  // column tile widths per variant, TMA box height
     int col_nv;                             // variants with kernels (2, or 4 with the 16-point plan)
-    int row_nv;                             // transmit schedules with kernels (1, or 2: TrCfg)
+    int row_nv;                             // transmit schedules with kernels (2, or 3: TrCfg)
     void (*splat)(const Geom &, const int *units, int nunits, int slice, int nsl1,
                   const int *slice_off, const SplatAtom *atoms, float2 *tbuf, cudaStream_t);
     // the same splat writing the projected potential of the slice (float) to
@@ -49,7 +49,7 @@ struct SizeOps {
                         const int *units, int nunits, const Fresnel &, float scale, cudaStream_t);
     // band != 0: only the in-band row segments are loaded and stored (B and
     // W must be zero out of band, and `out` too; a propagator pass follows).
-    // rv: the schedule (0 .. row_nv-1: TrCfg's EV = 0, 16)
+    // rv: the schedule (0 .. row_nv-1, as TrCfg numbers them)
     void (*row_transmit)(const Geom &, const int *units, int nunits, const float2 *tbuf,
                          const float2 *psi, float2 *out, float out_scale, int band, int rv,
                          cudaStream_t);
@@ -100,10 +100,10 @@ template <int N> struct Smem {
                                     128 * 4 + ((NTS + 31) / 32 + 1) * 4;
     template <int V, int EV = 0>
     static constexpr size_t col() { return (size_t)ColCfg<N, V, EV>::C * FftPlan<N, EV>::PADN * 8 + 16; }
-    template <int EV = 0>
+    template <int EV = 0, int W = 128>
     static constexpr size_t transmit()
     {
-        return (size_t)2 * TrCfg<N, EV>::LT * FftPlan<N, EV>::PADN * 8 + 16;
+        return (size_t)2 * TrCfg<N, EV, W>::LT * FftPlan<N, EV>::PADN * 8 + 16;
     }
     static constexpr size_t row = (size_t)RowCfg<N>::L * P::PADN * 8;
     static constexpr size_t adj = (size_t)RowCfg<N>::LT * (P::PADN + N) * 8;
@@ -224,17 +224,17 @@ struct Launch {
         if (!fr.table) return;  // the pass multiplies by fr.table; nothing to run without it
         col<kColFresnel>(g, in, out, units, nunits, fr, scale, 0, s);
     }
-    template <bool SCAT, int EV>
+    template <bool SCAT, int EV, int W>
     static void row_transmit_v(const Geom &g, const int *units, int nunits, const float2 *tbuf,
                                const float2 *psi, float2 *out, float out_scale, int band,
                                cudaStream_t s)
     {
         if (EV && !g.tw_row16) return;  // no 16-point twiddles bound: nothing to run
         static std::once_flag f;
-        constexpr size_t sm = Smem<N>::template transmit<EV>();
-        set_smem(k_row_transmit<N, SCAT, EV>, sm, f);
-        constexpr int L = TrCfg<N, EV>::LT;
-        k_row_transmit<N, SCAT, EV><<<nunits * row_blocks(g, L), L * TrCfg<N, EV>::T, sm, s>>>(
+        constexpr size_t sm = Smem<N>::template transmit<EV, W>();
+        set_smem(k_row_transmit<N, SCAT, EV, W>, sm, f);
+        constexpr int L = TrCfg<N, EV, W>::LT;
+        k_row_transmit<N, SCAT, EV, W><<<nunits * row_blocks(g, L), L * TrCfg<N, EV, W>::T, sm, s>>>(
             g, units, tbuf, psi, out, out_scale, band);
     }
     template <bool SCAT>
@@ -243,12 +243,15 @@ struct Launch {
                                cudaStream_t s)
     {
         if constexpr (row_plan16_ok(N)) {
-            if (rv == 1) {
-                row_transmit_v<SCAT, 16>(g, units, nunits, tbuf, psi, out, out_scale, band, s);
+            if (rv == 2) {
+                row_transmit_v<SCAT, 16, 128>(g, units, nunits, tbuf, psi, out, out_scale, band, s);
                 return;
             }
         }
-        row_transmit_v<SCAT, 0>(g, units, nunits, tbuf, psi, out, out_scale, band, s);
+        if (rv == 1)
+            row_transmit_v<SCAT, 0, 128>(g, units, nunits, tbuf, psi, out, out_scale, band, s);
+        else
+            row_transmit_v<SCAT, 0, 64>(g, units, nunits, tbuf, psi, out, out_scale, band, s);
     }
     static void row_init(const Geom &g, const int *units, int nunits, const float2 *wave0,
                          float2 *psi, float scale, cudaStream_t s)
@@ -403,7 +406,7 @@ struct Launch {
                                    col_plan16_ok(N) ? ColCfg<N, 0, col_plan16_ok(N) ? 16 : 0>::C : ColCfg<N, 0>::C,
                                    col_plan16_ok(N) ? ColCfg<N, 1, col_plan16_ok(N) ? 16 : 0>::C : ColCfg<N, 1>::C},
                                   ColCfg<N>::BR, col_plan16_ok(N) ? kColVariants : 2,
-                                  row_plan16_ok(N) ? kRowVariants : 1, splat,
+                                  row_plan16_ok(N) ? kRowVariants : 2, splat,
                                   splat_potential, splat_spec, col_dw, row_dwexp,
                                   col_mask, col_prop,     col_fresnel,      row_transmit_t<false>,
                                   row_transmit_t<true>,   row_init, row_exit, row_inverse,

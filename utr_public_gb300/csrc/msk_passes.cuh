@@ -145,18 +145,24 @@ template <int NY> struct RowCfg {
     static constexpr int MB = NY <= 1024 ? 3 : 2;
 };
 // The transmit's schedules, chosen per row length at run time by timing them
-// (the row tuner of the host code): EV = 0 (32 points a thread, three
-// resident 128-thread CTAs per SM) or, for 64 to 2048 points, EV = 16 (16
-// points a thread, four CTAs: 128 registers; a 2048-point row is one CTA of
-// 128 threads instead of two rows of 64).
-constexpr int kRowVariants = 2;
+// (the row tuner of the host code): the FFT plan EV and the CTA width W.
+//   variant 0: EV = 0 (32 points a thread), CTAs of 64 threads (rows of up to
+//              32 threads: two or more rows a CTA, so a CTA barrier waits for
+//              fewer warps; the registers of six CTAs per SM)
+//   variant 1: EV = 0, CTAs of 128 threads (three per SM)
+//   variant 2: (64 to 2048 points) EV = 16 (16 points a thread), CTAs of 128
+//              threads, four per SM at 128 registers; a 2048-point row is one
+//              CTA of 128 threads instead of a 64-thread row that spills
+// Shared memory (two rows of complex64 per row in flight) holds every variant
+// to ~12-16 resident warps per SM at 1024 points.
+constexpr int kRowVariants = 3;
 __host__ __device__ constexpr bool row_plan16_ok(int n) { return n >= 64 && n <= 2048; }
-template <int NY, int EV = 0> struct TrCfg {
+template <int NY, int EV = 0, int W = 128> struct TrCfg {
     using P = FftPlan<NY, EV>;
     static constexpr int T = P::T;
-    static constexpr int LT = (128 / T) > 0 ? 128 / T : 1;  // rows per CTA
+    static constexpr int LT = (W / T) > 0 ? W / T : 1;  // rows per CTA
     static constexpr bool BLK = T > 32;
-    static constexpr int MB = EV ? 4 : 3;
+    static constexpr int MB = EV ? 4 : 3 * (128 / (LT * T) > 0 ? 128 / (LT * T) : 1);
 };
 // Columns per CTA for the column passes, and the TMA boxes of a column tile.
 // Per line length up to four variants, chosen per pass at run time by timing
@@ -620,15 +626,15 @@ k_col_pass(const Geom g, const __grid_constant__ CUtensorMap in_map,
 // (cfpix.cpp:349-372) between the transmission's and the wave's row
 // transforms.  `out` may be `psi` (in place).  SCAT: the scattered form,
 // W = S(phi), B = S(tau_bl), out = S(phi + tau + phi tau) * out_scale * ny.
-// EV: the line FFT plan (TrCfg).
-template <int NY, bool SCAT = false, int EV = 0>
-__global__ void __launch_bounds__(TrCfg<NY, EV>::LT * TrCfg<NY, EV>::T, TrCfg<NY, EV>::MB)
+// EV, W: the line FFT plan and the CTA width (TrCfg).
+template <int NY, bool SCAT = false, int EV = 0, int W = 128>
+__global__ void __launch_bounds__(TrCfg<NY, EV, W>::LT * TrCfg<NY, EV, W>::T, TrCfg<NY, EV, W>::MB)
 k_row_transmit(const Geom g, const int *__restrict__ units, const float2 *__restrict__ tbuf,
                const float2 *psi, float2 *out, float out_scale, int band)
 {
     using P = FftPlan<NY, EV>;
-    constexpr int T = P::T, E = P::E, L = TrCfg<NY, EV>::LT;
-    constexpr bool BLK = TrCfg<NY, EV>::BLK;
+    constexpr int T = P::T, E = P::E, L = TrCfg<NY, EV, W>::LT;
+    constexpr bool BLK = TrCfg<NY, EV, W>::BLK;
     const float2 *tw = EV ? g.tw_row16 : g.tw_row;
     extern __shared__ __align__(128) unsigned char smem[];
     float2 *bufB = reinterpret_cast<float2 *>(smem);   // transmission rows, then t_bl
