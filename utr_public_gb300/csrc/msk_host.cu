@@ -986,13 +986,50 @@ void prof_collect(msk_context *ctx)
 
 namespace {
 
+// Times launch(v) for the variants v in [0, nv): two warm-up launches of every
+// variant, then kTuneRounds rounds in which every variant runs once between two
+// events, the order rotating from round to round; ms[v] = the variant's fastest
+// launch.  Interleaving the variants keeps a clock that is still rising (the
+// first launches of a process) from favouring whichever variant runs last.
+template <typename F>
+bool time_variants(cudaStream_t s, int nv, F launch, float *ms)
+{
+    constexpr int kTuneRounds = 5;
+    std::vector<cudaEvent_t> ev((size_t)2 * nv * kTuneRounds, nullptr);
+    bool ok = true;
+    for (auto &e : ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+    for (int w = 0; w < 2 && ok; w++)
+        for (int v = 0; v < nv; v++) launch(v);
+    for (int r = 0; r < kTuneRounds && ok; r++)
+        for (int i = 0; i < nv && ok; i++) {
+            const int v = (i + r) % nv;
+            cudaEvent_t *e = &ev[(size_t)2 * (r * nv + v)];
+            ok = cudaEventRecord(e[0], s) == cudaSuccess;
+            launch(v);
+            ok = ok && cudaEventRecord(e[1], s) == cudaSuccess;
+        }
+    ok = ok && cudaStreamSynchronize(s) == cudaSuccess && cudaGetLastError() == cudaSuccess;
+    for (int v = 0; v < nv; v++) {
+        ms[v] = 3.0e38f;
+        for (int r = 0; r < kTuneRounds && ok; r++) {
+            float t = 0.0f;
+            ok = cudaEventElapsedTime(&t, ev[(size_t)2 * (r * nv + v)],
+                                      ev[(size_t)2 * (r * nv + v) + 1]) == cudaSuccess;
+            ms[v] = std::min(ms[v], t);
+        }
+    }
+    for (auto &e : ev)
+        if (e) cudaEventDestroy(e);
+    return ok;
+}
+
 // The schedule of each column pass (ColCfg variant: FFT plan and tile width),
 // per device, grid and pass, in the manner of FFTW_MEASURE planning
 // (TemsimLibrary/cfpix.cpp:225-228): the first time a pass runs on a grid,
 // every variant with kernels for the line length -- 32 and (64 to 2048 points)
-// 16 points a thread, each at two tile widths -- runs on a scratch grid (three
-// timed launches each, after one untimed) and the fastest is kept for the life
-// of the process (the default unless another gains 3%).  Tile widths compute
+// 16 points a thread, each at two tile widths -- runs on a scratch grid
+// (time_variants) and the fastest is kept for the life of the process (the
+// default unless another gains 3%).  Tile widths compute
 // every column identically; the plans differ by FP32 rounding.  MSK_COL_TILE=
 // 0..3 in the environment fixes the variant (0, 1: 32 points, 2, 3: 16).
 struct ColChoices {
@@ -1024,38 +1061,25 @@ int col_variant(msk_context *ctx, const GridPre &gp, int mode)
     bool ok = ctx->tune.reserve((size_t)(U + 1) * plane * sizeof(float2)) == cudaSuccess &&
               cudaMemsetAsync(ctx->tune.p, 0, (size_t)(U + 1) * plane * sizeof(float2),
                               ctx->stream) == cudaSuccess;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    ok = ok && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess;
     float2 *grid = ctx->tune.as<float2>();
     Fresnel fr{};
     fr.table = grid + (size_t)U * plane;  // zeros
     fr.dw = reinterpret_cast<const float *>(grid + (size_t)U * plane);
     fr.dw_stride = 1;
     const Geom &g = gp.g;
-    for (int v = 0; v < cop->col_nv && ok; v++) {
-        ColView view;
-        if (column_map(ctx, &view, grid, gp.nx, gp.ny, U, cop, v) != MSK_OK) {
-            ok = false;
-            break;
+    ColView views[kColVariants];
+    for (int v = 0; v < cop->col_nv && ok; v++)
+        ok = column_map(ctx, &views[v], grid, gp.nx, gp.ny, U, cop, v) == MSK_OK;
+    auto launch = [&](int v) {
+        const ColView &view = views[v];
+        switch (mode) {
+        case kColMask: cop->col_mask(g, view, view, nullptr, U, 1, 1.0f, ctx->stream); break;
+        case kColProp: cop->col_prop(g, view, view, nullptr, U, 1, ctx->stream); break;
+        case kColFresnel: cop->col_fresnel(g, view, view, nullptr, U, fr, 1.0f, ctx->stream); break;
+        default: cop->col_dw(g, view, nullptr, U, fr.dw, 1, ctx->stream); break;
         }
-        auto launch = [&] {
-            switch (mode) {
-            case kColMask: cop->col_mask(g, view, view, nullptr, U, 1, 1.0f, ctx->stream); break;
-            case kColProp: cop->col_prop(g, view, view, nullptr, U, 1, ctx->stream); break;
-            case kColFresnel: cop->col_fresnel(g, view, view, nullptr, U, fr, 1.0f, ctx->stream); break;
-            default: cop->col_dw(g, view, nullptr, U, fr.dw, 1, ctx->stream); break;
-            }
-        };
-        launch();
-        ok = cudaEventRecord(e0, ctx->stream) == cudaSuccess;
-        for (int r = 0; r < 3; r++) launch();
-        ok = ok && cudaEventRecord(e1, ctx->stream) == cudaSuccess &&
-             cudaEventSynchronize(e1) == cudaSuccess &&
-             cudaEventElapsedTime(&ms[v], e0, e1) == cudaSuccess &&
-             cudaGetLastError() == cudaSuccess;
-    }
-    if (e0) cudaEventDestroy(e0);
-    if (e1) cudaEventDestroy(e1);
+    };
+    ok = ok && time_variants(ctx->stream, cop->col_nv, launch, ms);
     // the fastest variant, unless it gains less than 3% on the default
     for (int v = 1; ok && v < cop->col_nv; v++)
         if (ms[v] < 0.97f * ms[0] && ms[v] < ms[choice]) choice = v;
@@ -1067,9 +1091,8 @@ int col_variant(msk_context *ctx, const GridPre &gp, int mode)
 // The transmit's schedule (TrCfg: the FFT plan, 32 or, for 64 to 2048 points,
 // 16 points a thread, and the CTA width), chosen per device and grid the way
 // the column passes' is: the first time the transmit runs on a grid every
-// schedule runs on a scratch grid (three timed launches each, after one
-// untimed) and the fastest is kept for the process (the default unless
-// another gains 3%).  The two widths of one plan compute every row
+// schedule runs on a scratch grid (time_variants) and the fastest is kept for
+// the process (the default unless another gains 3%).  The two widths of one plan compute every row
 // identically; the plans differ by FP32 rounding (another radix split of the
 // same transforms).  MSK_ROW_PLAN=0..2 in the environment fixes it.  The wave
 // and scattered forms share it.
@@ -1103,21 +1126,11 @@ int row_variant(msk_context *ctx, const GridPre &gp)
     bool ok = ctx->tune.reserve((size_t)2 * U * plane * sizeof(float2)) == cudaSuccess &&
               cudaMemsetAsync(ctx->tune.p, 0, (size_t)2 * U * plane * sizeof(float2),
                               ctx->stream) == cudaSuccess;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    ok = ok && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess;
     float2 *tb = ctx->tune.as<float2>(), *psi = tb + (size_t)U * plane;
-    for (int v = 0; v < rop->row_nv && ok; v++) {
-        auto launch = [&] { rop->row_transmit(gp.g, nullptr, U, tb, psi, psi, 1.0f, 1, v, ctx->stream); };
-        launch();
-        ok = cudaEventRecord(e0, ctx->stream) == cudaSuccess;
-        for (int r = 0; r < 3; r++) launch();
-        ok = ok && cudaEventRecord(e1, ctx->stream) == cudaSuccess &&
-             cudaEventSynchronize(e1) == cudaSuccess &&
-             cudaEventElapsedTime(&ms[v], e0, e1) == cudaSuccess &&
-             cudaGetLastError() == cudaSuccess;
-    }
-    if (e0) cudaEventDestroy(e0);
-    if (e1) cudaEventDestroy(e1);
+    auto launch = [&](int v) {
+        rop->row_transmit(gp.g, nullptr, U, tb, psi, psi, 1.0f, 1, v, ctx->stream);
+    };
+    ok = ok && time_variants(ctx->stream, rop->row_nv, launch, ms);
     for (int v = 1; ok && v < rop->row_nv; v++)
         if (ms[v] < 0.97f * ms[0] && ms[v] < ms[choice]) choice = v;
     if (!ok) cudaGetLastError();
