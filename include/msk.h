@@ -144,9 +144,10 @@ typedef struct {
  *     rotation (the reference's calculate() adds its random displacement to
  *     the rotated coordinates, autoslic.cpp:701-713)
  *   images   out: float[nangles][ndefocus][nx][ny]; host or device pointer
- *            (page-locked host memory the GPU can address is written in
- *            place by the image pass; other host memory gets one copy at
- *            the end)
+ *            (page-locked host memory the GPU can address receives each
+ *            batch's images while the next batch runs, written by the GPU
+ *            through the mapped address; other host memory gets one copy
+ *            at the end)
  *   exitwaves out (may be NULL): complex [nangles][nconfig][nx][ny]; host or
  *     device pointer
  *   kept     out (may be NULL): int[nangles*nconfig], atoms inside the box */

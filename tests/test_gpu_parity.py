@@ -272,21 +272,25 @@ def test_full_size_tilt_series(ctx, msk, oracle):
     assert kept[1] < 20000 and kept[3] < 20000 and kept[2] == 20000
 
 
-@pytest.mark.parametrize("nconf,max_batch", [(1, 0), (3, 2)])
-def test_tilt_series_pinned_host_output(ctx, msk, nconf, max_batch):
-    """Page-locked host images are written in place by the image pass (the GPU
-    addresses them directly): equal bit for bit to device images, also when a
-    configuration average spans batches and the pass adds onto partial sums
-    already in host memory."""
+@pytest.mark.parametrize("nconf,max_batch,nang", [(1, 0, 3), (3, 2, 3), (1, 0, 40), (2, 0, 20)])
+def test_tilt_series_pinned_host_output(ctx, msk, nconf, max_batch, nang):
+    """Page-locked host images: each batch's images made in a device buffer and
+    copied out on the library's third stream beside the next batch (40 units:
+    batches of 8, 24 and 8 units, the copies waiting on one another), or, when a
+    configuration average spans batches, written in place by the image pass
+    (the GPU addresses them directly) adding onto partial sums already in host
+    memory: equal bit for bit to device images."""
     torch = pytest.importorskip("torch")
     spec = sp.random_specimen(300, 64.0, 10.0, 54.0, 1015)
     atoms = (spec.Znum, spec.x, spec.y, spec.z, spec.occ)
     s = series(msk, 64, 64.0, 200.0, 2.0, max_batch=max_batch)
     disp = sp.phonon_displacements(spec, nconf, 0.08, 1015) if nconf > 1 else None
-    angZ, angY, df = [0.0, 0.5, 0.1], [0.2, 1.0, 2.0], [0.0, 100.0]
-    dev = torch.zeros((3, 2, 64, 64), dtype=torch.float32, device="cuda")
+    angZ = np.linspace(0.0, 0.5, nang)
+    angY = np.linspace(0.2, 2.0, nang)
+    df = [0.0, 100.0]
+    dev = torch.zeros((nang, 2, 64, 64), dtype=torch.float32, device="cuda")
     ctx.tilt_series(s, *atoms, angZ, angY, df, nconfig=nconf, displacements=disp, images=dev)
-    pin = torch.full((3, 2, 64, 64), -1.0, dtype=torch.float32, pin_memory=True)
+    pin = torch.full((nang, 2, 64, 64), -1.0, dtype=torch.float32, pin_memory=True)
     ctx.tilt_series(s, *atoms, angZ, angY, df, nconfig=nconf, displacements=disp, images=pin)
     torch.cuda.synchronize()
     assert torch.equal(pin, dev.cpu())

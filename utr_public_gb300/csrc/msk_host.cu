@@ -66,6 +66,35 @@ __global__ void k_plane_init(float2 *psi, const int *__restrict__ units, int nun
     }
 }
 
+// n floats from device memory to page-locked host memory the GPU addresses
+// (mapped): the SMs' stores cross NVLink-C2C several times faster than a
+// copy-engine transfer into the same memory does on the Grace hosts.  Run on
+// its own stream beside the next batch's kernels, with a small grid (a CTA of
+// it takes registers a CTA of those kernels would use on its SM) and four
+// 16-byte stores in flight a thread.
+constexpr int kCopyOutCtas = 38;
+__global__ void __launch_bounds__(256) k_copy_out(const float *__restrict__ src, float *dst, size_t n)
+{
+    const size_t nt = (size_t)gridDim.x * blockDim.x, tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    size_t done = 0;
+    if (((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15) == 0) {
+        const float4 *s4 = reinterpret_cast<const float4 *>(src);
+        float4 *d4 = reinterpret_cast<float4 *>(dst);
+        const size_t n4 = n / 4;
+        size_t i = tid;
+        for (; i + 3 * nt < n4; i += 4 * nt) {
+            float4 v[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) v[k] = __ldcs(&s4[i + k * nt]);
+#pragma unroll
+            for (int k = 0; k < 4; k++) d4[i + k * nt] = v[k];
+        }
+        for (; i < n4; i += nt) d4[i] = __ldcs(&s4[i]);
+        done = n4 * 4;
+    }
+    for (size_t i = done + tid; i < n; i += nt) dst[i] = src[i];
+}
+
 __global__ void k_fresnel_table(const Geom g, const Fresnel fr, float scale, float2 *table)
 {
     const size_t n = (size_t)g.nx * g.ny;
@@ -1908,12 +1937,39 @@ int tilt_series_impl(msk_context *ctx, const msk_series *s, int natom, const int
         }
         bounds.push_back(std::min(first, nunits));
         while (bounds.back() < nunits) bounds.push_back(std::min(nunits, bounds.back() + B));
+        // images bound for page-locked host memory leave a batch at a time,
+        // beside the next batch's kernels: end with a small batch too, so that
+        // little of the copy is left after the last kernel
+        const int nb_last = bounds.back() - bounds[bounds.size() - 2];
+        if (img_mapped && s->max_batch <= 0 && nunits >= 32 && nb_last >= 3 * first)
+            bounds.insert(bounds.end() - 1, bounds.back() - first);
     }
-
+    // page-locked host images: each batch's images are made in a device buffer
+    // and written out (k_copy_out, through the mapped address) on the third
+    // stream while the next batch runs -- when no orientation's configurations
+    // span two batches (a configuration average is completed within its
+    // batch); else the image pass writes them in place
+    bool img_stage = img_mapped != nullptr;
+    size_t stage_planes = 0;
+    for (size_t bi = 0; img_stage && bi + 1 < bounds.size(); bi++) {
+        img_stage = bounds[bi] % nconfig == 0 && bounds[bi + 1] % nconfig == 0;
+        const int a0 = bounds[bi] / nconfig, a1 = (bounds[bi + 1] - 1) / nconfig;
+        stage_planes = std::max<size_t>(stage_planes, (size_t)(pl.off[a1 + 1] - pl.off[a0]));
+    }
     float *d_images = img_mapped ? img_mapped : images;
     if (ndefocus > 0 && !img_direct) {
         MSK_CUDA(ctx, ctx->images.reserve(img_bytes));
         d_images = ctx->images.as<float>();
+    }
+    cudaEvent_t ev_ready = nullptr, ev_copied = nullptr;
+    if (img_stage) {
+        MSK_CUDA(ctx, ctx->images.reserve(stage_planes * plane * sizeof(float)));
+        d_images = ctx->images.as<float>();
+        if (!ctx->stk_ev[0])
+            for (cudaEvent_t &e : ctx->stk_ev)
+                MSK_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ev_ready = ctx->stk_ev[0];
+        ev_copied = ctx->stk_ev[1];
     }
     MSK_CUDA(ctx, ctx->psi.reserve((size_t)B * plane * sizeof(float2)));
     MSK_CUDA(ctx, ctx->tbuf.reserve((size_t)B * plane * sizeof(float2)));
@@ -2039,6 +2095,10 @@ int tilt_series_impl(msk_context *ctx, const msk_series *s, int natom, const int
             }
             MSK_CUDA(ctx, ctx->fresnel.reserve(plane * sizeof(float2)));
             MSK_CUDA(ctx, ctx->imgfill.reserve((size_t)B * sizeof(float2)));
+            // staged: this batch's planes from the start of the device buffer,
+            // once the previous batch's copy out of it has finished
+            const int dst_base = img_stage ? pl.off[a_first] : 0;
+            if (img_stage && bi > 0) MSK_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ev_copied, 0));
             for (int k = 0; k < kmax; k++) {
                 // the k-th plane of every orientation, grouped by equal free-space
                 // and image-plane parameters: one table and one pass per group
@@ -2075,7 +2135,7 @@ int tilt_series_impl(msk_context *ctx, const msk_series *s, int natom, const int
                     gr.n_units = cnt;
                     for (int oa : gr.ori) meta.insert(meta.end(), aunits[oa].begin(), aunits[oa].end());
                     gr.o_dst = meta.size();
-                    for (int oa : gr.ori) meta.push_back(pl.off[a_first + oa] + k);
+                    for (int oa : gr.ori) meta.push_back(pl.off[a_first + oa] + k - dst_base);
                     gr.o_flags = meta.size();
                     for (int oa : gr.ori) meta.push_back(aflags[oa]);
                     (void)n;
@@ -2139,14 +2199,27 @@ int tilt_series_impl(msk_context *ctx, const msk_series *s, int natom, const int
                     }
                 }
             }
+            if (img_stage) {
+                const size_t bytes = (size_t)(pl.off[a_last + 1] - dst_base) * plane * sizeof(float);
+                MSK_CUDA(ctx, cudaEventRecord(ev_ready, ctx->stream));
+                MSK_CUDA(ctx, cudaStreamWaitEvent(ctx->aux2, ev_ready, 0));
+                {
+                    Prof p(ctx, kCopyImages, (double)bytes, ctx->aux2);
+                    k_copy_out<<<kCopyOutCtas, 256, 0, ctx->aux2>>>(d_images, img_mapped + (size_t)dst_base * plane,
+                                                               bytes / sizeof(float));
+                }
+                MSK_CUDA(ctx, cudaEventRecord(ev_copied, ctx->aux2));
+                count_copy(ctx, 1, (double)bytes);
+            }
         }
         MSK_CUDA(ctx, cudaGetLastError());
         // the next batch's atoms while this one runs (its upload waits for it)
         if (bi + 2 < bounds.size()) prep_batch(bounds[bi + 1], bounds[bi + 2] - bounds[bi + 1]);
     }
+    if (img_stage) MSK_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ev_copied, 0));
     MSK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     prof_collect(ctx);
-    if (ndefocus > 0 && img_mapped) count_copy(ctx, 1, (double)img_bytes);  // written in place
+    if (ndefocus > 0 && img_mapped && !img_stage) count_copy(ctx, 1, (double)img_bytes);  // in place
     if (ndefocus > 0 && !img_direct) {
         Prof p(ctx, kCopyImages, (double)img_bytes);
         MSK_CUDA(ctx, cudaMemcpyAsync(images, d_images, img_bytes, cudaMemcpyDeviceToHost,
