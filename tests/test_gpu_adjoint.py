@@ -163,6 +163,18 @@ def test_adjoint_batching_and_device_pointers(ctx, msk, oracle):
     di = torch.zeros((5, 1, nx, ny), dtype=torch.float32, device="cuda")
     ctx.stack_images(s, torch.from_numpy(vt).cuda(), rp, images=di)
     assert np.array_equal(di.cpu().numpy(), target)
+    # page-locked host stacks: their slices move through the mapped addresses
+    # (one batch, and two batches sharing two staging slots)
+    hv = torch.from_numpy(v).pin_memory()
+    ht = torch.from_numpy(target).pin_memory()
+    for st in (s, s1):
+        hg = torch.full(v.shape, -1.0, dtype=torch.float32).pin_memory()
+        loss_d, _ = ctx.adjoint(st, hv, rp, ht, grad=hg)
+        assert np.array_equal(hg.numpy(), ga)
+        assert abs(loss_d / loss_a - 1.0) < 1e-12
+    hi = torch.zeros((5, 1, nx, ny), dtype=torch.float32).pin_memory()
+    ctx.stack_images(s1, torch.from_numpy(vt).pin_memory(), rp, images=hi)
+    assert np.array_equal(hi.numpy(), target)
 
 
 def test_stack_zero_potential_is_plane_wave(ctx, msk):

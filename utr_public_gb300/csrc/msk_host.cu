@@ -66,33 +66,42 @@ __global__ void k_plane_init(float2 *psi, const int *__restrict__ units, int nun
     }
 }
 
-// n floats from device memory to page-locked host memory the GPU addresses
-// (mapped): the SMs' stores cross NVLink-C2C several times faster than a
-// copy-engine transfer into the same memory does on the Grace hosts.  Run on
-// its own stream beside the next batch's kernels, with a small grid (a CTA of
-// it takes registers a CTA of those kernels would use on its SM) and four
-// 16-byte stores in flight a thread.
-constexpr int kCopyOutCtas = 38;
-__global__ void __launch_bounds__(256) k_copy_out(const float *__restrict__ src, float *dst, size_t n)
+// rows x width floats between device memory and page-locked host memory the
+// GPU addresses (mapped; row r at src + r * spitch, dst + r * dpitch): the SMs'
+// loads and stores cross NVLink-C2C several times faster than a copy-engine
+// transfer between the same buffers does on the Grace hosts.  Run on a stream
+// of its own beside the slice kernels, with a small grid (a CTA of it takes
+// registers a CTA of those kernels would use on its SM) and four 16-byte
+// accesses in flight a thread.
+constexpr int kCopyCtas = 38;
+__global__ void __launch_bounds__(256) k_copy_rows(const float *__restrict__ src, size_t spitch,
+                                                   float *dst, size_t dpitch, size_t width, int rows)
 {
     const size_t nt = (size_t)gridDim.x * blockDim.x, tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    size_t done = 0;
-    if (((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15) == 0) {
-        const float4 *s4 = reinterpret_cast<const float4 *>(src);
-        float4 *d4 = reinterpret_cast<float4 *>(dst);
-        const size_t n4 = n / 4;
-        size_t i = tid;
-        for (; i + 3 * nt < n4; i += 4 * nt) {
-            float4 v[4];
+    const bool v4 = ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src) |
+                      spitch | dpitch | width) & 3) == 0 &&
+                    ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15) == 0;
+    for (int r = 0; r < rows; r++) {
+        const float *sr = src + (size_t)r * spitch;
+        float *dr = dst + (size_t)r * dpitch;
+        size_t done = 0;
+        if (v4) {
+            const float4 *s4 = reinterpret_cast<const float4 *>(sr);
+            float4 *d4 = reinterpret_cast<float4 *>(dr);
+            const size_t n4 = width / 4;
+            size_t i = tid;
+            for (; i + 3 * nt < n4; i += 4 * nt) {
+                float4 v[4];
 #pragma unroll
-            for (int k = 0; k < 4; k++) v[k] = __ldcs(&s4[i + k * nt]);
+                for (int k = 0; k < 4; k++) v[k] = __ldcs(&s4[i + k * nt]);
 #pragma unroll
-            for (int k = 0; k < 4; k++) d4[i + k * nt] = v[k];
+                for (int k = 0; k < 4; k++) d4[i + k * nt] = v[k];
+            }
+            for (; i < n4; i += nt) d4[i] = __ldcs(&s4[i]);
+            done = n4 * 4;
         }
-        for (; i < n4; i += nt) d4[i] = __ldcs(&s4[i]);
-        done = n4 * 4;
+        for (size_t i = done + tid; i < width; i += nt) dr[i] = sr[i];
     }
-    for (size_t i = done + tid; i < n; i += nt) dst[i] = src[i];
 }
 
 __global__ void k_fresnel_table(const Geom g, const Fresnel fr, float scale, float2 *table)
@@ -1945,7 +1954,7 @@ int tilt_series_impl(msk_context *ctx, const msk_series *s, int natom, const int
             bounds.insert(bounds.end() - 1, bounds.back() - first);
     }
     // page-locked host images: each batch's images are made in a device buffer
-    // and written out (k_copy_out, through the mapped address) on the third
+    // and written out (k_copy_rows, through the mapped address) on the third
     // stream while the next batch runs -- when no orientation's configurations
     // span two batches (a configuration average is completed within its
     // batch); else the image pass writes them in place
@@ -2205,8 +2214,8 @@ int tilt_series_impl(msk_context *ctx, const msk_series *s, int natom, const int
                 MSK_CUDA(ctx, cudaStreamWaitEvent(ctx->aux2, ev_ready, 0));
                 {
                     Prof p(ctx, kCopyImages, (double)bytes, ctx->aux2);
-                    k_copy_out<<<kCopyOutCtas, 256, 0, ctx->aux2>>>(d_images, img_mapped + (size_t)dst_base * plane,
-                                                               bytes / sizeof(float));
+                    k_copy_rows<<<kCopyCtas, 256, 0, ctx->aux2>>>(
+                        d_images, 0, img_mapped + (size_t)dst_base * plane, 0, bytes / sizeof(float), 1);
                 }
                 MSK_CUDA(ctx, cudaEventRecord(ev_copied, ctx->aux2));
                 count_copy(ctx, 1, (double)bytes);
@@ -2385,6 +2394,13 @@ int stack_run(msk_context *ctx, const StackJob &J)
     const size_t pb = plane * sizeof(float2);
     const bool v_dev = is_device_ptr(J.v);
     const bool g_dev = adjoint && is_device_ptr(J.grad);
+    // page-locked host stacks the GPU addresses: their slices move by
+    // k_copy_rows through the mapped addresses (else by 2D copies)
+    const float *v_map = v_dev ? nullptr : static_cast<const float *>(mapped_host(const_cast<float *>(J.v)));
+    float *g_map = adjoint && !g_dev ? static_cast<float *>(mapped_host(J.grad)) : nullptr;
+    const float *t_map = adjoint && !is_device_ptr(J.target)
+                             ? static_cast<const float *>(mapped_host(const_cast<float *>(J.target)))
+                             : nullptr;
     const bool t_dev = adjoint && is_device_ptr(J.target);
     const bool i_dev = !adjoint && ndef > 0 && is_device_ptr(J.images);
     const size_t vb = (size_t)S * plane * sizeof(float);      // one unit's stack
@@ -2508,7 +2524,11 @@ int stack_run(msk_context *ctx, const StackJob &J)
                 MSK_CUDA(ctx, cudaMemcpyAsync(dst, J.v + (size_t)u0 * S * plane, nb * vb,
                                               cudaMemcpyHostToDevice, cin));
             for (int k = 0; k < S; k++) {
-                if (by_slice)
+                if (by_slice && v_map)
+                    k_copy_rows<<<kCopyCtas, 256, 0, cin>>>(v_map + ((size_t)u0 * S + k) * plane,
+                                                            (size_t)S * plane, dst + (size_t)k * plane,
+                                                            (size_t)S * plane, plane, nb);
+                else if (by_slice)
                     MSK_CUDA(ctx, cudaMemcpy2DAsync(dst + (size_t)k * plane, vb,
                                                     J.v + ((size_t)u0 * S + k) * plane, vb,
                                                     plane * sizeof(float), nb,
@@ -2518,9 +2538,14 @@ int stack_run(msk_context *ctx, const StackJob &J)
             count_copy(ctx, 0, (double)nb * vb);
         }
         if (adjoint && !t_dev) {
-            MSK_CUDA(ctx, cudaMemcpyAsync(slot_of(ctx->stk_t, ib, b),
-                                          J.target + (size_t)u0 * ndef * plane, nb * ib,
-                                          cudaMemcpyHostToDevice, cin));
+            if (t_map)
+                k_copy_rows<<<kCopyCtas, 256, 0, cin>>>(t_map + (size_t)u0 * ndef * plane, 0,
+                                                        slot_of(ctx->stk_t, ib, b), 0,
+                                                        (size_t)nb * ib / sizeof(float), 1);
+            else
+                MSK_CUDA(ctx, cudaMemcpyAsync(slot_of(ctx->stk_t, ib, b),
+                                              J.target + (size_t)u0 * ndef * plane, nb * ib,
+                                              cudaMemcpyHostToDevice, cin));
             count_copy(ctx, 0, (double)nb * ib);
         }
         if (host_io) MSK_CUDA(ctx, cudaEventRecord(ev_in[b % nslot], cin));
@@ -2659,10 +2684,16 @@ int stack_run(msk_context *ctx, const StackJob &J)
                 if (g_dev || !by_slice) return MSK_OK;
                 MSK_CUDA(ctx, cudaEventRecord(ev_sout[k - 1], ctx->stream));
                 MSK_CUDA(ctx, cudaStreamWaitEvent(cout, ev_sout[k - 1], 0));
-                MSK_CUDA(ctx, cudaMemcpy2DAsync(J.grad + ((size_t)u0 * S + (k - 1)) * plane, vb,
-                                                gd + (size_t)(k - 1) * plane, vb,
-                                                plane * sizeof(float), nb, cudaMemcpyDeviceToHost,
-                                                cout));
+                if (g_map)
+                    k_copy_rows<<<kCopyCtas, 256, 0, cout>>>(gd + (size_t)(k - 1) * plane,
+                                                             (size_t)S * plane,
+                                                             g_map + ((size_t)u0 * S + (k - 1)) * plane,
+                                                             (size_t)S * plane, plane, nb);
+                else
+                    MSK_CUDA(ctx, cudaMemcpy2DAsync(J.grad + ((size_t)u0 * S + (k - 1)) * plane, vb,
+                                                    gd + (size_t)(k - 1) * plane, vb,
+                                                    plane * sizeof(float), nb, cudaMemcpyDeviceToHost,
+                                                    cout));
                 return MSK_OK;
             };
             // backward with every wave and transmission kept: slice by slice
