@@ -324,3 +324,40 @@ def test_calculate_reuses_its_grid(ctx, msk, oracle):
         fresh.close()
     ref64 = oracle.calculate(p, *atoms(b), 32.0, 32.0, fp64=True)
     assert rel_l2(got[-1], ref64) < 1e-5
+
+
+def test_tilt_series_reuses_its_grid(ctx, msk):
+    """Tilt series, calculate() and potential stacks share the grid tables of
+    the previous call when the grid parameters match (the same tables either
+    way); other atomic numbers or another grid in between must not leave stale
+    tables behind: every call equals the same call in a fresh context bit for
+    bit."""
+    a = sp.random_specimen(300, 32.0, 4.0, 28.0, 73)
+    b = sp.random_specimen(300, 32.0, 4.0, 28.0, 74)
+    b.Znum[:] = 79
+    atoms = lambda s: (s.Znum, s.x, s.y, s.z, s.occ)
+    sa = series(msk, 128, 32.0, 200.0, 1.0)
+    sb = series(msk, 64, 32.0, 300.0, 2.0)
+    p = msk.make_param(32.0, 32.0, 128, 128, 200.0, 1.0)  # sa's grid
+    st = msk.Stack()  # sa's grid too, no atoms (potential stacks)
+    st.nx = st.ny = 128
+    st.ax = st.by = 32.0
+    st.v0, st.deltaz, st.nslices = 200.0, 1.0, 6
+    v = np.random.default_rng(75).uniform(0.0, 2.0, (2, 6, 128, 128)).astype(np.float32)
+    seq = [("t", sa, a), ("t", sa, a), ("t", sa, b), ("c", p, a), ("t", sa, a), ("t", sb, a),
+           ("t", sa, b), ("s", st, None), ("t", sa, b), ("c", p, b), ("s", st, None)]
+
+    def run(c, kind, g, s):
+        if kind == "c":
+            return c.calculate(g, *atoms(s), 32.0, 32.0)
+        if kind == "s":
+            return c.stack_images(g, v, [0.0])
+        return c.tilt_series(g, *atoms(s), [0.0, 0.4], [0.3, 1.1], [0.0, 150.0])[0]
+    got = [run(ctx, *x) for x in seq]
+    for x, g in zip(seq, got):
+        fresh = msk.Context(0)
+        try:
+            ref = run(fresh, *x)
+        finally:
+            fresh.close()
+        assert np.array_equal(g.view(np.uint32), ref.view(np.uint32)), x[0]

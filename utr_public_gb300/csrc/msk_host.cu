@@ -1294,6 +1294,35 @@ int upload_tables(msk_context *ctx, GridPre &gp, const std::vector<int> &zlist)
     return MSK_OK;
 }
 
+// The grid of the previous call (msk_calculate, a tilt series or a potential
+// stack), when it was made for the same grid parameters `key` and its tables
+// are still the context's: gp from it, and the record (else null, gp untouched).
+std::shared_ptr<CalcCache> grid_cached(msk_context *ctx, const std::vector<float> &key, GridPre &gp)
+{
+    auto cache = std::static_pointer_cast<CalcCache>(ctx->calc_cache);
+    if (!cache || cache->key != key || cache->tables != ctx->tables.p) return nullptr;
+    gp = cache->gp;
+    return cache;
+}
+
+// The grid's tables on the device for the atomic numbers zlist: kept when `hit`
+// (grid_cached) holds them for the same numbers -- no host build, upload or
+// synchronisation -- else built, uploaded and recorded for the next call.
+int grid_tables(msk_context *ctx, GridPre &gp, const std::vector<float> &key,
+                const std::shared_ptr<CalcCache> &hit, const std::vector<int> &zlist)
+{
+    if (hit && hit->zlist == zlist) return MSK_OK;
+    const int st = upload_tables(ctx, gp, zlist);
+    if (st) return st;
+    auto c = std::make_shared<CalcCache>();
+    c->key = key;
+    c->zlist = zlist;
+    c->gp = gp;
+    c->tables = ctx->tables.p;
+    ctx->calc_cache = c;
+    return MSK_OK;
+}
+
 const float *tables_kx(msk_context *, const GridPre &gp) { return gp.d_kx; }
 const float *tables_ky(msk_context *, const GridPre &gp) { return gp.d_ky; }
 
@@ -1781,15 +1810,11 @@ int msk_calculate(msk_context *ctx, float *pix, const float *wave0, const float 
     // reference's per-orientation loop calls calculate() on one grid)
     const std::vector<float> key = {(float)nx, (float)ny, ax, by, param[MSK_pENERGY],
                                     param[MSK_pDELTAZ], param[MSK_pXCTILT], param[MSK_pYCTILT]};
-    auto cache = std::static_pointer_cast<CalcCache>(ctx->calc_cache);
-    const bool same_grid = cache && cache->key == key && cache->tables == ctx->tables.p;
     GridPre gp;
-    if (same_grid) {
-        gp = cache->gp;
-    } else if (!grid_pre(gp, nx, ny, ax, by, param[MSK_pENERGY], param[MSK_pDELTAZ],
-                         param[MSK_pXCTILT], param[MSK_pYCTILT])) {
+    const auto hit = grid_cached(ctx, key, gp);
+    if (!hit && !grid_pre(gp, nx, ny, ax, by, param[MSK_pENERGY], param[MSK_pDELTAZ],
+                          param[MSK_pXCTILT], param[MSK_pYCTILT]))
         return fail(ctx, MSK_EUNSUPPORTED, "band limit is not two index ranges per column");
-    }
     const int nslices = slice_count(param[MSK_pDELTAZ], ctblengthz);
     std::vector<int> zlist;
     // the reference's range check comes before any atomic-number check
@@ -1821,17 +1846,8 @@ int msk_calculate(msk_context *ctx, float *pix, const float *wave0, const float 
     ps.iseed = iseed;
     prep_unit(gp, ps, ua[0]);
     if (ua[0].status) return fail(ctx, ua[0].status, msk_status_string(ua[0].status));
-    int st = MSK_OK;
-    if (!(same_grid && cache->zlist == zlist)) {
-        st = upload_tables(ctx, gp, zlist);
-        if (st) return st;
-        auto c = std::make_shared<CalcCache>();
-        c->key = key;
-        c->zlist = zlist;
-        c->gp = gp;
-        c->tables = ctx->tables.p;
-        ctx->calc_cache = c;
-    }
+    int st = grid_tables(ctx, gp, key, hit, zlist);
+    if (st) return st;
     Batch b;
     st = upload_batch(ctx, ua, 0, 1, nslices, b);
     if (st) return st;
@@ -1904,15 +1920,18 @@ int tilt_series_impl(msk_context *ctx, const msk_series *s, int natom, const int
         return fail(ctx, MSK_EUNSUPPORTED, "grid must be a power of two from 16 to 4096");
     MSK_CUDA(ctx, cudaSetDevice(ctx->device));
     GridPre gp;
-    // MsctKirkland passes a zero crystal tilt (autosliccmd.cpp:435-437)
-    if (!grid_pre(gp, nx, ny, s->ctblength, s->ctblength, s->v0, s->deltaz, 0.0f, 0.0f))
+    // MsctKirkland passes a zero crystal tilt (autosliccmd.cpp:435-437); the
+    // grid tables of the previous call (this or msk_calculate) when they match
+    const std::vector<float> key = {(float)nx, (float)ny, s->ctblength, s->ctblength, s->v0,
+                                    s->deltaz, 0.0f, 0.0f};
+    const auto hit = grid_cached(ctx, key, gp);
+    if (!hit && !grid_pre(gp, nx, ny, s->ctblength, s->ctblength, s->v0, s->deltaz, 0.0f, 0.0f))
         return fail(ctx, MSK_EUNSUPPORTED, "band limit is not two index ranges per column");
     const int nslices = slice_count(s->deltaz, s->ctblengthz);
     std::vector<int> zlist;
     int st = build_zmap(ctx, natom, Znum, zlist);
     if (st) return st;
-    st = upload_tables(ctx, gp, zlist);
-    if (st) return st;
+    if ((st = grid_tables(ctx, gp, key, hit, zlist))) return st;
 
     const size_t plane = (size_t)nx * ny;
     const int nunits = nangles * nconfig;
@@ -2368,9 +2387,12 @@ int stack_run(msk_context *ctx, const StackJob &J)
         return fail(ctx, MSK_EUNSUPPORTED, "grid must be a power of two from 16 to 4096");
     MSK_CUDA(ctx, cudaSetDevice(ctx->device));
     GridPre gp;
-    if (!grid_pre(gp, nx, ny, s->ax, s->by, s->v0, s->deltaz, s->ctiltx, s->ctilty))
+    const std::vector<float> key = {(float)nx, (float)ny, s->ax, s->by, s->v0, s->deltaz,
+                                    s->ctiltx, s->ctilty};
+    const auto hit = grid_cached(ctx, key, gp);
+    if (!hit && !grid_pre(gp, nx, ny, s->ax, s->by, s->v0, s->deltaz, s->ctiltx, s->ctilty))
         return fail(ctx, MSK_EUNSUPPORTED, "band limit is not two index ranges per column");
-    int st = upload_tables(ctx, gp, std::vector<int>());
+    int st = grid_tables(ctx, gp, key, hit, std::vector<int>());
     if (st) return st;
     Geom &g = gp.g;
     st = flags_reset(ctx, g);
