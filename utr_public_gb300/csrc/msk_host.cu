@@ -621,10 +621,6 @@ static bool grid_pre(GridPre &gp, int nx, int ny, float ax, float by, float v0, 
     g.rminsq = (float)(rmin * rmin);
     g.idx = (int)(nx * 3.0 / ax) + 1;
     g.idy = (int)(ny * 3.0 / by) + 1;
-    // knots r_i^2 = (0.01 exp(i dlnr))^2: i = (log r^2 - 2 log 0.01) / (2 dlnr)
-    const double dlnr = log(5.0 / 0.01) / (phys::kN - 1);
-    g.lut_c0 = (float)(-2.0 * log(0.01));
-    g.lut_c1 = (float)(1.0 / (2.0 * dlnr));
     // column blocks of the column passes (C columns each) holding in-band columns
     g.band_p = gp.band_p;
     g.band_q = gp.band_q;
@@ -1213,7 +1209,7 @@ TableLayout layout_tables(int nx, int ny, int nz)
     o.twc = piece(8 * o.n_twc);
     o.twr16 = piece(8 * o.n_twr16);
     o.twc16 = piece(8 * o.n_twc16);
-    o.kn = piece(4 * (size_t)phys::kN);
+    o.kn = piece(4 * (size_t)kKnotWords);
     o.cf = piece(16 * (size_t)std::max(nz, 1) * phys::kN);
     o.kb = piece(8 * (size_t)ny);
     o.bytes = off;
@@ -1231,8 +1227,20 @@ static void build_tables(const GridPre &gp, const std::vector<int> &zlist,
     const int nz = (int)zlist.size();
     auto &L = phys::lut();
     for (int Z : zlist) L.build(Z);
-    std::vector<float> knots(phys::kN);
+    // the knot piece: the knots, then spline_vz's interval per bucket of r^2
+    std::vector<float> knots(kKnotWords, 0.0f);
     for (int i = 0; i < phys::kN; i++) knots[i] = (float)L.knots[i];
+    unsigned char *bucket = reinterpret_cast<unsigned char *>(knots.data() + 128);
+    for (int bi = 0; bi < kKnotBuckets; bi++) {
+        // the last knot at or below the bucket's start; the knots being 13%
+        // apart, the bucket holds at most the next one
+        float lo;
+        const uint32_t blo = (uint32_t)(kKnotBucketBase + bi) << kKnotBucketShift;
+        std::memcpy(&lo, &blo, 4);
+        int i0 = 0;
+        while (i0 < phys::kN - 2 && knots[i0 + 1] <= lo) i0++;
+        bucket[bi] = (unsigned char)i0;
+    }
     std::vector<float4> coef((size_t)std::max(nz, 1) * phys::kN);
     for (int zi = 0; zi < nz; zi++) {
         const int Z = zlist[zi];
@@ -3810,7 +3818,7 @@ __global__ void k_plain_splat(const Geom g, const SplatAtom *__restrict__ atoms,
             rsq = fmaxf(rsq, g.rminsq);
             const float4 *coef = g.coef + (at.meta >> (2 * kMetaBits)) * kKnots;
             const int ix = (ixo + dxw) & (g.nx - 1), iy = (iyo + dyw) & (g.ny - 1);
-            atomicAdd(&v[(size_t)ix * g.ny + iy], at.occ * spline_vz(g, g.knots, coef, rsq));
+            atomicAdd(&v[(size_t)ix * g.ny + iy], at.occ * spline_vz(g.knots, coef, rsq));
         }
     }
 }

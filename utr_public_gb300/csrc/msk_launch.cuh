@@ -97,7 +97,7 @@ template <int N> struct Smem {
     using P = FftPlan<N>;
     static constexpr int NTS = RowCfg<N>::L * P::T;
     static constexpr size_t splat = (size_t)RowCfg<N>::L * SplatCfg<N>::SROW * 8 + NTS * 16 +
-                                    128 * 4 + ((NTS + 31) / 32 + 1) * 4;
+                                    kKnotWords * 4 + ((NTS + 31) / 32 + 1) * 4;
     template <int V, int EV = 0>
     static constexpr size_t col() { return (size_t)ColCfg<N, V, EV>::C * FftPlan<N, EV>::PADN * 8 + 16; }
     template <int EV = 0, int W = 128>

@@ -212,21 +212,32 @@ template <int NX, int MODE, int V, int EV = 0> struct ColMinBlocks {
 };
 
 constexpr int kKnots = 100;
+// The knot piece of the grid tables (and its shared-memory copy): the 100
+// knots of r^2 (float), padding to 128 words, then the interval table of
+// spline_vz -- one byte per bucket of r^2, a bucket being 1/16 of an octave
+// (the float's exponent and top four mantissa bits), from 2^-20 to 2^5: the
+// knots are 13% apart, so a bucket holds at most one of them.
+constexpr int kKnotBucketShift = 23 - 4;
+constexpr int kKnotBucketBase = (127 - 20) << 4;  // the bucket of 2^-20
+constexpr int kKnotBuckets = 25 << 4;
+constexpr int kKnotWords = 128 + kKnotBuckets / 4;
 
 // Spline of the projected potential vs r^2 (TemsimLibrary/slicelib.cpp:2402-2425,
 // 2812-2875), evaluated in float.  The interval is the one seval's bisection
-// finds (knot[i] <= r^2 < knot[i+1], clamped to [0, 98]); the knots are
-// log-spaced, so a logarithm gives the index to within one and a compare
-// with each neighbour settles it.
-__device__ __forceinline__ float spline_vz(const Geom &g, const float *knots, const float4 *coef,
-                                          float rsq)
+// finds (knot[i] <= r^2 < knot[i+1], clamped to [0, 98]): the bucket of r^2
+// gives the last knot at or below the bucket's start, and one compare with
+// the next knot settles it.  `knots` is the knot piece (kKnotWords words).
+__device__ __forceinline__ float spline_vz(const float *knots, const float4 *coef, float rsq)
 {
-    int i = __float2int_rd((__logf(rsq) + g.lut_c0) * g.lut_c1);
-    i = min(max(i, 0), kKnots - 2);
-    if (i > 0 && rsq < knots[i]) i--;
-    else if (i < kKnots - 2 && rsq >= knots[i + 1]) i++;
+    const unsigned char *bucket = reinterpret_cast<const unsigned char *>(knots + 128);
+    const int b = min(max((int)(__float_as_uint(rsq) >> kKnotBucketShift) - kKnotBucketBase, 0),
+                      kKnotBuckets - 1);
+    int i = bucket[b];
+    const float k0 = knots[i], k1 = knots[i + 1];
+    const bool up = rsq >= k1 && i < kKnots - 2;
+    i += up ? 1 : 0;
     const float4 c = __ldg(&coef[i]);
-    const float z = rsq - knots[i];
+    const float z = rsq - (up ? k1 : k0);
     return c.x + (c.y + (c.z + c.w * z) * z) * z;
 }
 
@@ -274,7 +285,7 @@ __device__ __forceinline__ void splat_atom(const Geom &g, const SplatAtom &sa, i
             float rsq = dx2 + dy * dy;
             if (rsq <= 9.0f) {
                 rsq = fmaxf(rsq, g.rminsq);
-                vacc[pmod(iyp, NY)] += sa.occ * spline_vz(g, s_knots, coef, rsq);
+                vacc[pmod(iyp, NY)] += sa.occ * spline_vz(s_knots, coef, rsq);
             }
         }
     }
@@ -403,7 +414,7 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
     float2 *s_lines = reinterpret_cast<float2 *>(smem);
     SplatAtom *s_atoms = reinterpret_cast<SplatAtom *>(s_lines + L * SROW);
     float *s_knots = reinterpret_cast<float *>(s_atoms + NT);
-    int *s_cnt = reinterpret_cast<int *>(s_knots + 128);
+    int *s_cnt = reinterpret_cast<int *>(s_knots + kKnotWords);
 
     const int tid = threadIdx.x, l = tid / T, t = tid % T;
     const int nx = g.nx;
@@ -414,7 +425,7 @@ k_row_splat(const Geom g, const int *__restrict__ units, int slice, int nsl1,
     const bool row_ok = ix < nx;
     const int lane = tid & 31, warp = tid >> 5;
 
-    for (int i = tid; i < kKnots; i += NT) s_knots[i] = g.knots[i];
+    for (int i = tid; i < kKnotWords; i += NT) s_knots[i] = g.knots[i];
     float *vacc = reinterpret_cast<float *>(s_lines + l * SROW);
 #pragma unroll
     for (int m = 0; m < E; m++) vacc[t + m * T] = 0.0f;

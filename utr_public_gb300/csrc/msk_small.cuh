@@ -61,7 +61,7 @@ struct SmallCfg {
     static constexpr int ROW1 = LPC * SROW;
     static constexpr int COL = LPC * PADN;
     static constexpr int F2 = (ROW0 + ROW1) > 2 * COL ? (ROW0 + ROW1) : 2 * COL;
-    static constexpr size_t SMEM = (size_t)F2 * 8 + 128 * 4;
+    static constexpr size_t SMEM = (size_t)F2 * 8 + kKnotWords * 4;
     static_assert(N >= 64 && N <= 256, "small-grid sizes");
     static_assert(T <= 32 && 32 % T == 0, "a warp holds whole lines");
     static_assert(HALF % 32 == 0, "halves of whole warps");
@@ -100,7 +100,7 @@ k_small_slices(const Geom g, int nslices, int nsl1, const int *__restrict__ slic
     float2 *Wu = W + (size_t)u * plane;
     float2 *Tu[2] = {Tb0 + (size_t)u * plane, Tb1 + (size_t)u * plane};
     const int *so = slice_off + (size_t)u * nsl1;
-    for (int i = threadIdx.x; i < kKnots; i += C::NT) s_knots[i] = g.knots[i];
+    for (int i = threadIdx.x; i < kKnotWords; i += C::NT) s_knots[i] = g.knots[i];
     __syncthreads();
 
     // row phase: line l of the CTA's rows, thread t of the line

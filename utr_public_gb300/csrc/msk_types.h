@@ -19,7 +19,6 @@ struct Geom {
     float scaley_f;
     float rminsq;       // (rmin)^2, rmin = 1/4 sqrt((dx^2+dy^2)/2)
     int idx, idy;       // splat window half widths int(n*3/a)+1
-    float lut_c0, lut_c1;  // knot index of r^2 ~ (log(r^2) + lut_c0) * lut_c1
     const float *kx2;   // [nx] kx^2 (freqn, float)
     const float *ky2;   // [ny]
     const float2 *propx;  // [nx] (cos t, -sin t) / nx, t = pi dz (kx^2 lambda - kx 2 tan(tilt_x))
