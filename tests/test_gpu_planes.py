@@ -154,3 +154,26 @@ def test_run_from_reference_orientation_file(ctx, msk, oracle):
         for j in range(2):
             worst = max(worst, rel_l2(imgs[2 * a + j], r[j]))
     assert worst < 1e-5, worst
+
+
+def test_file_run_to_page_locked_images(ctx, msk):
+    """The shipped orientation file (108 orientations, two planes each, Z''
+    rotations and shifts) into page-locked host images: each batch's planes
+    staged on the device and written out beside the next batch (batches of 8,
+    92 and 8 orientations), equal bit for bit to device images."""
+    import os
+    from conftest import GOLDEN
+    torch = pytest.importorskip("torch")
+    path = os.path.join(GOLDEN, "DefocusRand108_2_NEW2.txt")
+    spec = sp.random_specimen(300, 48.0, 8.0, 40.0, 1109)
+    atoms = (spec.Znum, spec.x, spec.y, spec.z, spec.occ)
+    s = msk.Series()
+    s.nx = s.ny = 64
+    s.ctblength = s.ctblengthz = 48.0
+    s.v0, s.deltaz = 200.0, 1.25
+    dev = torch.zeros((216, 64, 64), dtype=torch.float32, device="cuda")
+    ctx.tilt_series_from_file(s, *atoms, path, images=dev)
+    pin = torch.full((216, 64, 64), -1.0, dtype=torch.float32).pin_memory()
+    ctx.tilt_series_from_file(s, *atoms, path, images=pin)
+    torch.cuda.synchronize()
+    assert torch.equal(pin, dev.cpu())

@@ -1377,6 +1377,10 @@ namespace {
 // A batch of units (waves) with their atoms uploaded: the slice loop.
 struct Batch {
     int nunits = 0, nslices = 0;
+    // units of the whole call (0: this batch's): whether the small-grid path
+    // runs is decided for the call, so a unit's result does not depend on
+    // where the batches of the call are cut
+    int call_units = 0;
     std::vector<int> slice_off;   // [nunits][nslices+1] absolute atom offsets
     std::vector<int> act_off;     // [nslices+1]
     std::vector<int> act;         // active units per slice
@@ -1485,7 +1489,7 @@ static bool small_grid_ok(msk_context *ctx, const GridPre &gp, bool dw, int nmod
 static bool small_path(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode)
 {
     return ctx->tbuf2.cap >= ctx->tbuf.cap && ctx->tbuf.cap > 0 &&
-           small_grid_ok(ctx, gp, !b.dw.empty(), nmode, b.nunits);
+           small_grid_ok(ctx, gp, !b.dw.empty(), nmode, std::max(b.nunits, b.call_units));
 }
 
 int run_slices(msk_context *ctx, const GridPre &gp, const Batch &b, int nmode, bool w_in_band)
@@ -2091,6 +2095,7 @@ int tilt_series_impl(msk_context *ctx, const msk_series *s, int natom, const int
         Batch b;
         st = upload_batch(ctx, ua, u0, nb, nslices, b);
         if (st) return st;
+        b.call_units = nunits;
         float2 *psi = ctx->psi.as<float2>(), *tb = ctx->tbuf.as<float2>();
         if (spherical) {
             Prof p(ctx, kInit, 8.0 * plane * (nb + 1));
