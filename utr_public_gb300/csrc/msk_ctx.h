@@ -113,6 +113,9 @@ struct msk_context {
     msk::DevBuf tune;                                 // scratch grids of the schedule tuners
     msk::DevBuf utr_img, utr_k2, utr_acc, utr_vol, utr_out, utr_tab, utr_stage;  // UTR reconstruction
     bool no_tune = false;                             // schedules fixed at variant 0
+    bool no_host_stage = false;                       // no page-locked staging (allocates none)
+    void *h_stage = nullptr;                          // page-locked staging of a batch's atoms
+    size_t h_stage_cap = 0;
     cudaEvent_t stk_ev[7] = {};                       // potential stacks: copy / kernel handoffs
     std::vector<cudaEvent_t> stk_sev;                 // the same per slice (2 per slice)
     std::vector<cudaStream_t> lanes;                  // concurrent specimens of a batch

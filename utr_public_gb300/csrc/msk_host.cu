@@ -1387,10 +1387,9 @@ struct Batch {
     std::vector<float> dw;        // Debye-Waller branch: [nunits][nslices] -B/4 (else empty)
 };
 
-// Per-slice atom offsets, active units per slice and the packed atoms of
-// units u0 .. u0+nunits-1.
-void pack_batch(const std::vector<UnitAtoms> &ua, int u0, int nunits, int nslices, Batch &b,
-                std::vector<SplatAtom> &atoms)
+// Per-slice atom offsets and active units per slice of units u0 ..
+// u0+nunits-1 (and their Debye-Waller factors); returns the atom count.
+size_t pack_batch_meta(const std::vector<UnitAtoms> &ua, int u0, int nunits, int nslices, Batch &b)
 {
     b.nunits = nunits;
     b.nslices = nslices;
@@ -1415,39 +1414,89 @@ void pack_batch(const std::vector<UnitAtoms> &ua, int u0, int nunits, int nslice
             if (ua[u0 + i].counts[s] > 0) b.act.push_back(i);
     }
     b.act_off[nslices] = (int)b.act.size();
-    atoms.assign(std::max<size_t>(total, 1), SplatAtom{});
-    size_t o = 0;
-    for (int i = 0; i < nunits; i++) {
-        const auto &a = ua[u0 + i].atoms;
-        std::copy(a.begin(), a.end(), atoms.begin() + o);
-        o += a.size();
-    }
     b.dw.clear();
     if (nunits > 0 && !ua[u0].dw.empty()) {
         b.dw.assign((size_t)nunits * nslices, 0.0f);
         for (int i = 0; i < nunits; i++)
             std::copy(ua[u0 + i].dw.begin(), ua[u0 + i].dw.end(), b.dw.begin() + (size_t)i * nslices);
     }
+    return total;
+}
+
+// The packed atoms of the batch b describes (pack_batch_meta) into dst
+// (max(total, 1) records), a unit at a time on `threads` host threads.
+void pack_atoms(const std::vector<UnitAtoms> &ua, int u0, const Batch &b, SplatAtom *dst,
+                int threads)
+{
+    const int nsl1 = b.nslices + 1;
+    dst[0] = SplatAtom{};
+    parallel_for(b.nunits, threads, [&](int i) {
+        const auto &a = ua[u0 + i].atoms;
+        std::copy(a.begin(), a.end(), dst + b.slice_off[(size_t)i * nsl1]);
+    });
+}
+
+void pack_batch(const std::vector<UnitAtoms> &ua, int u0, int nunits, int nslices, Batch &b,
+                std::vector<SplatAtom> &atoms)
+{
+    atoms.assign(std::max<size_t>(pack_batch_meta(ua, u0, nunits, nslices, b), 1), SplatAtom{});
+    pack_atoms(ua, u0, b, atoms.data(), 1);  // (callers run one batch per host thread)
+}
+
+// Page-locked staging of at least `bytes` (grown by cudaHostAlloc; the copies
+// out of the old one have finished when it is replaced: every upload ends
+// with a stream synchronisation).  Null where the context allocates nothing.
+void *host_stage(msk_context *ctx, size_t bytes)
+{
+    if (ctx->no_host_stage) return nullptr;
+    if (ctx->h_stage_cap < bytes) {
+        if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+        ctx->h_stage = nullptr;
+        ctx->h_stage_cap = 0;
+        const size_t cap = bytes + bytes / 4;
+        if (cudaHostAlloc(&ctx->h_stage, cap, cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->h_stage = nullptr;
+            return nullptr;
+        }
+        ctx->h_stage_cap = cap;
+    }
+    return ctx->h_stage;
 }
 
 int upload_batch(msk_context *ctx, const std::vector<UnitAtoms> &ua, int u0, int nunits,
                  int nslices, Batch &b)
 {
+    const size_t na = std::max<size_t>(pack_batch_meta(ua, u0, nunits, nslices, b), 1);
+    const size_t ab = na * sizeof(SplatAtom), ob = b.slice_off.size() * sizeof(int),
+                 cb = b.act.size() * sizeof(int);
+    MSK_CUDA(ctx, ctx->atoms.reserve(ab));
+    MSK_CUDA(ctx, ctx->slice_off.reserve(ob));
+    MSK_CUDA(ctx, ctx->act.reserve(std::max<size_t>(cb, sizeof(int))));
+    // from page-locked staging when the context has it (the copies then run at
+    // the link's rate right after the previous batch, instead of through the
+    // driver's pageable bounce buffers with the GPU idle), else from vectors
     std::vector<SplatAtom> atoms;
-    pack_batch(ua, u0, nunits, nslices, b, atoms);
-    MSK_CUDA(ctx, ctx->atoms.reserve(atoms.size() * sizeof(SplatAtom)));
-    MSK_CUDA(ctx, ctx->slice_off.reserve(b.slice_off.size() * sizeof(int)));
-    MSK_CUDA(ctx, ctx->act.reserve(std::max<size_t>(b.act.size(), 1) * sizeof(int)));
-    MSK_CUDA(ctx, cudaMemcpyAsync(ctx->atoms.p, atoms.data(), atoms.size() * sizeof(SplatAtom),
-                                  cudaMemcpyHostToDevice, ctx->stream));
-    count_copy(ctx, 0, (double)(atoms.size() * sizeof(SplatAtom) + b.slice_off.size() * sizeof(int) +
-                                b.act.size() * sizeof(int)));
-    MSK_CUDA(ctx, cudaMemcpyAsync(ctx->slice_off.p, b.slice_off.data(),
-                                  b.slice_off.size() * sizeof(int), cudaMemcpyHostToDevice,
-                                  ctx->stream));
-    if (!b.act.empty())
-        MSK_CUDA(ctx, cudaMemcpyAsync(ctx->act.p, b.act.data(), b.act.size() * sizeof(int),
-                                      cudaMemcpyHostToDevice, ctx->stream));
+    const SplatAtom *src_atoms;
+    const int *src_off = b.slice_off.data(), *src_act = b.act.data();
+    if (unsigned char *st = static_cast<unsigned char *>(host_stage(ctx, ab + ob + cb))) {
+        SplatAtom *dst = reinterpret_cast<SplatAtom *>(st);
+        pack_atoms(ua, u0, b, dst, host_threads());
+        std::memcpy(st + ab, b.slice_off.data(), ob);
+        if (cb) std::memcpy(st + ab + ob, b.act.data(), cb);
+        src_atoms = dst;
+        src_off = reinterpret_cast<const int *>(st + ab);
+        src_act = reinterpret_cast<const int *>(st + ab + ob);
+    } else {
+        atoms.assign(na, SplatAtom{});
+        pack_atoms(ua, u0, b, atoms.data(), host_threads());
+        src_atoms = atoms.data();
+    }
+    MSK_CUDA(ctx, cudaMemcpyAsync(ctx->atoms.p, src_atoms, ab, cudaMemcpyHostToDevice, ctx->stream));
+    count_copy(ctx, 0, (double)(ab + ob + cb));
+    MSK_CUDA(ctx, cudaMemcpyAsync(ctx->slice_off.p, src_off, ob, cudaMemcpyHostToDevice, ctx->stream));
+    if (cb)
+        MSK_CUDA(ctx, cudaMemcpyAsync(ctx->act.p, src_act, cb, cudaMemcpyHostToDevice, ctx->stream));
     if (!b.dw.empty()) {
         MSK_CUDA(ctx, ctx->dwbuf.reserve(b.dw.size() * sizeof(float)));
         MSK_CUDA(ctx, cudaMemcpyAsync(ctx->dwbuf.p, b.dw.data(), b.dw.size() * sizeof(float),
@@ -1658,6 +1707,7 @@ void msk_destroy(msk_context *ctx)
     if (ctx->aux) cudaStreamDestroy(ctx->aux);
     if (ctx->aux2) cudaStreamDestroy(ctx->aux2);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     delete ctx;
 }
 
@@ -3660,6 +3710,7 @@ extern "C" int msk_calculate_static(void *stream, float *pix, const float *wave0
     ctx.device = dev;
     ctx.stream = (cudaStream_t)stream;
     ctx.no_tune = true;  // the tuners would allocate: the default schedules
+    ctx.no_host_stage = true;
     unsigned char *base = static_cast<unsigned char *>(scratch);
     auto view = [&](DevBuf &b, size_t off, size_t bytes) { b.borrow(base + off, bytes); };
     view(ctx.psi, kOffPsi, kSGrid);
