@@ -361,3 +361,22 @@ def test_tilt_series_reuses_its_grid(ctx, msk):
         finally:
             fresh.close()
         assert np.array_equal(g.view(np.uint32), ref.view(np.uint32)), x[0]
+
+
+def test_calculate_into_out_buffer(ctx, msk):
+    """calculate(out=...) writes the exit wave into the caller's array (reused
+    across calls) and equals the returned array bit for bit; the default plane
+    wave the wrapper keeps per grid size is left as it was."""
+    a = sp.random_specimen(200, 32.0, 4.0, 28.0, 76)
+    atoms = (a.Znum, a.x, a.y, a.z, a.occ)
+    p = msk.make_param(32.0, 32.0, 128, 128, 200.0, 1.0)
+    ref = ctx.calculate(p, *atoms, 32.0, 32.0)
+    out = np.full((128, 128, 2), np.nan, np.float32)
+    for _ in range(2):
+        got = ctx.calculate(p, *atoms, 32.0, 32.0, out=out)
+        assert got is out
+        assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
+    w0 = ctx._plane_waves[(128, 128)]
+    assert np.all(w0[..., 0] == 1.0) and np.all(w0[..., 1] == 0.0)
+    with pytest.raises(ValueError):
+        ctx.calculate(p, *atoms, 32.0, 32.0, out=np.zeros((64, 64, 2), np.float32))

@@ -366,6 +366,7 @@ class Context:
             raise MskError(st, "msk_create failed: %s" % L.msk_status_string(st).decode())
         self.h = h
         self.L = L
+        self._plane_waves = {}  # calculate()'s default incident wave per grid size
 
     def close(self):
         if self.h:
@@ -400,22 +401,33 @@ class Context:
                                        float(buf[i].bytes)) for i in range(min(n, 16))}
 
     def calculate(self, param, Znum, x, y, z, occ, ctblength, ctblengthz, nmode=0, wave0=None,
-                  wobble=None, lwobble=0, iseed=None):
-        """autoslic::calculate coherent branch; returns the exit wave [nx, ny, 2] float32.
+                  wobble=None, lwobble=0, iseed=None, out=None):
+        """autoslic::calculate coherent branch; returns the exit wave [nx, ny, 2] float32
+        (into `out` when given: a C-contiguous float32 array of that shape).
         lwobble = 1 takes its thermal branches (param[pNWOBBLE], param[pTEMPER]); with
         iseed given (nwobble > 1) returns (exit wave, advanced seed)."""
         param = np.ascontiguousarray(param, np.float32)
         nx, ny = int(param[pNX] + 0.1), int(param[pNY] + 0.1)
-        if wave0 is None:
-            wave0 = np.zeros((nx, ny, 2), np.float32)
-            wave0[..., 0] = 1.0
+        if wave0 is None:  # the unit plane wave, made once per grid size
+            wave0 = self._plane_waves.get((nx, ny))
+            if wave0 is None:
+                wave0 = np.zeros((nx, ny, 2), np.float32)
+                wave0[..., 0] = 1.0
+                self._plane_waves[(nx, ny)] = wave0
         wave0 = np.ascontiguousarray(wave0, np.float32)
-        pix = np.zeros((nx, ny, 2), np.float32)
+        if out is None:
+            pix = np.empty((nx, ny, 2), np.float32)  # every element is written
+        else:
+            if (out.dtype != np.float32 or out.shape != (nx, ny, 2) or
+                    not out.flags["C_CONTIGUOUS"]):
+                raise ValueError("out must be a C-contiguous float32 array [nx, ny, 2]")
+            pix = out
         arrs = [np.ascontiguousarray(a, dt) for a, dt in
                 ((Znum, np.int32), (x, np.float32), (y, np.float32), (z, np.float32),
                  (occ, np.float32))]
-        wob = np.zeros(len(arrs[1]), np.float32) if wobble is None else \
-            np.ascontiguousarray(wobble, np.float32)
+        wob = None if wobble is None else np.ascontiguousarray(wobble, np.float32)
+        if wob is None and lwobble:
+            wob = np.zeros(len(arrs[1]), np.float32)
         seed = None if iseed is None else C.c_long(iseed)
         st = self.L.msk_calculate(self.h, _ptr(pix), _ptr(wave0), param, len(arrs[1]),
                                   *[_ptr(a) for a in arrs], _ptr(wob), ctblength, ctblengthz,
