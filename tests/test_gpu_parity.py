@@ -380,3 +380,33 @@ def test_calculate_into_out_buffer(ctx, msk):
     assert np.all(w0[..., 0] == 1.0) and np.all(w0[..., 1] == 0.0)
     with pytest.raises(ValueError):
         ctx.calculate(p, *atoms, 32.0, 32.0, out=np.zeros((64, 64, 2), np.float32))
+
+
+def test_calculate_keeps_an_unchanged_incident_wave(ctx, msk):
+    """calculate() uploads its incident wave only when it differs from the
+    previous call's (compared on the host); a new wave, the same wave again
+    after another, and a spherical-wave tilt series in between (which writes
+    the same device buffer) must each give the fresh-context result."""
+    a = sp.random_specimen(200, 32.0, 4.0, 28.0, 77)
+    atoms = (a.Znum, a.x, a.y, a.z, a.occ)
+    p = msk.make_param(32.0, 32.0, 128, 128, 200.0, 1.0)
+    rng = np.random.default_rng(78)
+    w1 = rng.normal(size=(128, 128, 2)).astype(np.float32)
+    w2 = rng.normal(size=(128, 128, 2)).astype(np.float32)
+    sph = series(msk, 128, 32.0, 200.0, 1.0)
+    sph.R1 = 500.0
+    seq = ["w1", "w1", "w2", "w1", "sph", "w1"]
+    got = []
+    for k in seq:
+        if k == "sph":
+            ctx.tilt_series(sph, *atoms, [0.0], [0.2], [0.0])
+            continue
+        w = w1 if k == "w1" else w2
+        got.append((w, ctx.calculate(p, *atoms, 32.0, 32.0, wave0=w)))
+    for w, g in got:
+        fresh = msk.Context(0)
+        try:
+            ref = fresh.calculate(p, *atoms, 32.0, 32.0, wave0=w)
+        finally:
+            fresh.close()
+        assert np.array_equal(g.view(np.uint32), ref.view(np.uint32))

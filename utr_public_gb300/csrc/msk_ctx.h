@@ -116,6 +116,9 @@ struct msk_context {
     bool no_host_stage = false;                       // no page-locked staging (allocates none)
     void *h_stage = nullptr;                          // page-locked staging of a batch's atoms
     size_t h_stage_cap = 0;
+    std::vector<float> w0_host;                       // msk_calculate's last incident wave,
+    const void *w0_dev = nullptr;                     // uploaded to this wave0 buffer
+    bool w0_valid = false;
     cudaEvent_t stk_ev[7] = {};                       // potential stacks: copy / kernel handoffs
     std::vector<cudaEvent_t> stk_sev;                 // the same per slice (2 per slice)
     std::vector<cudaStream_t> lanes;                  // concurrent specimens of a batch

@@ -1924,9 +1924,19 @@ int msk_calculate(msk_context *ctx, float *pix, const float *wave0, const float 
     MSK_CUDA(ctx, ctx->wave0.reserve(plane * sizeof(float2)));
     st = flags_reset(ctx, gp.g);
     if (st) return st;
-    MSK_CUDA(ctx, cudaMemcpyAsync(ctx->wave0.p, wave0, plane * sizeof(float2),
-                                  cudaMemcpyHostToDevice, ctx->stream));
-    count_copy(ctx, 0, (double)(plane * sizeof(float2)));
+    // the incident wave of the previous call when it is the same (the
+    // reference's per-orientation loop passes one plane wave to every call):
+    // compared on the host, not uploaded again
+    const size_t wbytes = plane * sizeof(float2);
+    if (!(ctx->w0_valid && ctx->w0_dev == ctx->wave0.p && ctx->w0_host.size() * sizeof(float) == wbytes &&
+          std::memcmp(ctx->w0_host.data(), wave0, wbytes) == 0)) {
+        ctx->w0_valid = false;
+        MSK_CUDA(ctx, cudaMemcpyAsync(ctx->wave0.p, wave0, wbytes, cudaMemcpyHostToDevice, ctx->stream));
+        count_copy(ctx, 0, (double)wbytes);
+        ctx->w0_host.assign(wave0, wave0 + 2 * plane);
+        ctx->w0_dev = ctx->wave0.p;
+        ctx->w0_valid = true;
+    }
     const SizeOps *rop = size_ops(ny);
     {
         Prof p(ctx, kInit, 16.0 * plane);
@@ -2093,6 +2103,7 @@ int tilt_series_impl(msk_context *ctx, const msk_series *s, int natom, const int
         std::vector<float2> w0;
         spherical_wave(nx, ny, s->ctblength, s->v0, s->R1, w0);
         MSK_CUDA(ctx, ctx->wave0.reserve(plane * sizeof(float2)));
+        ctx->w0_valid = false;  // msk_calculate's incident wave is overwritten
         MSK_CUDA(ctx, cudaMemcpyAsync(ctx->wave0.p, w0.data(), plane * sizeof(float2),
                                       cudaMemcpyHostToDevice, ctx->stream));
         count_copy(ctx, 0, (double)(plane * sizeof(float2)));
